@@ -1,0 +1,275 @@
+// Test-oracle harness around the reference's own physics sources.
+//
+// Builds a Cloth (src/Cloth.cpp:3-50), an Environment and a PhysicsCloth
+// exactly as the reference drivers do (e.g. src/Simulate.h:34-64), then runs
+// the body of SimStep (src/TrainHelper.cpp:15-54) for a number of steps:
+//   FillMV -> A = M - h^2 dF/dx - h dF/dv, b = h (F - (dF/dv)^T v) + M v
+//   -> solve -> Cloth::update -> ResetMV
+// and writes the per-step state (plus, at selected steps, the dense system
+// pieces) to a binary record file. The solve uses the Eigen-CG stand-in in
+// shim/eigen_cg.cpp (the reference's EigenSolver::apply path) or, on request,
+// a dense LU solve (src/Solvers.h:27-29, TorchSolver).
+//
+// It is test infrastructure only: it produces golden vectors for the oracle
+// restatement and for the GPU path.
+//
+// Usage: ref_harness <config-file>
+// Config: key=value lines (see tests/golden/make_golden.py for the keys).
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "PhysicsCloth.h"
+
+void ref_cg_set_options(double tol, long max_iter);
+long ref_cg_last_iterations();
+double ref_cg_last_error();
+
+namespace {
+
+std::map<std::string, std::string> read_config(const char* path) {
+  std::map<std::string, std::string> kv;
+  std::ifstream f(path);
+  std::string line;
+  while (std::getline(f, line)) {
+    if (line.empty() || line[0] == '#') continue;
+    auto eq = line.find('=');
+    if (eq == std::string::npos) continue;
+    kv[line.substr(0, eq)] = line.substr(eq + 1);
+  }
+  return kv;
+}
+
+std::vector<double> parse_list(const std::string& s) {
+  std::vector<double> out;
+  std::string tok;
+  for (char c : s) {
+    if (c == ',' || c == ';' || c == ' ') {
+      if (!tok.empty()) out.push_back(std::stod(tok));
+      tok.clear();
+    } else {
+      tok.push_back(c);
+    }
+  }
+  if (!tok.empty()) out.push_back(std::stod(tok));
+  return out;
+}
+
+double get_d(const std::map<std::string, std::string>& kv, const std::string& k, double dflt) {
+  auto it = kv.find(k);
+  return it == kv.end() ? dflt : std::stod(it->second);
+}
+std::string get_s(const std::map<std::string, std::string>& kv, const std::string& k, const std::string& dflt) {
+  auto it = kv.find(k);
+  return it == kv.end() ? dflt : it->second;
+}
+
+struct Writer {
+  FILE* f;
+  explicit Writer(const std::string& path) { f = std::fopen(path.c_str(), "wb"); }
+  ~Writer() { if (f) std::fclose(f); }
+  void put(const std::string& name, const std::vector<long>& dims, const double* data) {
+    int nl = static_cast<int>(name.size());
+    std::fwrite(&nl, sizeof(int), 1, f);
+    std::fwrite(name.data(), 1, nl, f);
+    int nd = static_cast<int>(dims.size());
+    std::fwrite(&nd, sizeof(int), 1, f);
+    long total = 1;
+    for (long d : dims) { std::fwrite(&d, sizeof(long), 1, f); total *= d; }
+    std::fwrite(data, sizeof(double), total, f);
+  }
+  void put_tensor(const std::string& name, const Tensor& t) {
+    Tensor c = t.detach().contiguous().to(torch::kFloat64);
+    std::vector<long> dims;
+    for (auto d : c.sizes()) dims.push_back(d);
+    put(name, dims, c.data_ptr<double>());
+  }
+};
+
+std::string key(int u, int v) { return std::to_string(u) + "," + std::to_string(v); }
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 2) {
+    std::fprintf(stderr, "usage: %s config\n", argv[0]);
+    return 2;
+  }
+  torch::set_num_threads(1);
+  auto kv = read_config(argv[1]);
+
+  const int W = static_cast<int>(get_d(kv, "width", 5));
+  const int Lh = static_cast<int>(get_d(kv, "length", 5));
+  const double height = get_d(kv, "height", 5.0);
+  const double L = get_d(kv, "L", 1e-3);
+  const double R = get_d(kv, "R", 1e-4);
+  const std::string pose = get_s(kv, "pose", "flat");
+  const std::string weave = get_s(kv, "weave", "plain");
+  const int steps = static_cast<int>(get_d(kv, "steps", 1));
+  const std::string solver = get_s(kv, "solver", "cg");
+  ref_cg_set_options(get_d(kv, "cg_tol", DBL_EPSILON), static_cast<long>(get_d(kv, "cg_maxiter", -1)));
+
+  std::vector<double> y0 = parse_list(get_s(kv, "yarn0", "1e-3,3.1830988618379e10,318.30988618379"));
+  std::vector<Yarn> yarns{Yarn{R, torch::tensor({y0[0]}, opts), torch::tensor({y0[1]}, opts), torch::tensor({y0[2]}, opts)}};
+  if (kv.count("yarn1")) {
+    std::vector<double> y1 = parse_list(kv["yarn1"]);
+    yarns.push_back(Yarn{R, torch::tensor({y1[0]}, opts), torch::tensor({y1[1]}, opts), torch::tensor({y1[2]}, opts)});
+  }
+  auto T1 = [&](const std::string& k, double d) { return torch::tensor({get_d(kv, k, d)}, opts); };
+  WovenPattern wp = weave == "twill" ? WovenPattern::Twill : (weave == "satin" ? WovenPattern::Satin : WovenPattern::Plain);
+  InitPose ip = pose == "upright" ? InitPose::Upright : InitPose::Flat;
+
+  Cloth cloth(W, Lh, height, L, R, yarns, T1("kc", 1.0), T1("kf", 1000.0), T1("df", 1000.0), T1("mu", 0.3),
+              T1("S", 1e3), T1("handle_stiffness", 1e4), wp, ip);
+
+  // Optional per-yarn-line material: warp line = node row v, weft line = node column u.
+  if (kv.count("warp_lines") || kv.count("weft_lines")) {
+    std::vector<double> wl = parse_list(get_s(kv, "warp_lines", ""));
+    std::vector<double> fl = parse_list(get_s(kv, "weft_lines", ""));
+    auto mk = [&](const std::vector<double>& a, int line) {
+      return Yarn{R, torch::tensor({a[3 * line]}, opts), torch::tensor({a[3 * line + 1]}, opts),
+                  torch::tensor({a[3 * line + 2]}, opts)};
+    };
+    for (auto& e : cloth.edges) {
+      if (e.edge_type == "warp" && !wl.empty()) e.yarn = mk(wl, e.n0->idx_v);
+      if (e.edge_type == "weft" && !fl.empty()) e.yarn = mk(fl, e.n0->idx_u);
+    }
+    for (auto* segs : {&cloth.bend_segs, &cloth.crimp_bend_segs})
+      for (auto& b : *segs) {
+        if (b.seg_type == "warp" && !wl.empty()) b.yarn = mk(wl, b.n0->idx_v);
+        if (b.seg_type == "weft" && !fl.empty()) b.yarn = mk(fl, b.n0->idx_u);
+      }
+  }
+
+  std::vector<double> G = parse_list(get_s(kv, "G", "0,0,9.8"));
+  std::vector<double> wv = parse_list(get_s(kv, "wind_vel", "0,0,0"));
+  Wind wind{torch::tensor({wv[0], wv[1], wv[2]}, opts).view({3, 1}), T1("wind_density", 0.0), T1("wind_drag", 0.0)};
+  Environment env{&cloth, torch::tensor({G[0], G[1], G[2]}, opts).view({3, 1}), wind};
+
+  std::vector<std::pair<int, int>> handles;
+  {
+    std::vector<double> hl = parse_list(get_s(kv, "handles", ""));
+    for (size_t i = 0; i + 1 < hl.size(); i += 2) handles.emplace_back(static_cast<int>(hl[i]), static_cast<int>(hl[i + 1]));
+  }
+  cloth.set_handles(handles);
+
+  const int N = W * Lh;
+  // Optional initial state (raw doubles, node order u + v*W):
+  // LPos[N*3] LPosFix[N*3] LVel[N*3] EPos[N*2] EPosBar[N*2] EVel[N*2]
+  if (kv.count("init_state")) {
+    std::ifstream f(kv["init_state"], std::ios::binary);
+    std::vector<double> buf(N * 15);
+    f.read(reinterpret_cast<char*>(buf.data()), buf.size() * sizeof(double));
+    const double* lp = buf.data();
+    const double* lf = lp + 3 * N;
+    const double* lv = lf + 3 * N;
+    const double* ep = lv + 3 * N;
+    const double* eb = ep + 2 * N;
+    const double* ev = eb + 2 * N;
+    for (int v = 0; v < Lh; ++v)
+      for (int u = 0; u < W; ++u) {
+        int id = u + v * W;
+        Node& n = cloth.nodes[key(u, v)];
+        n.LPos = torch::tensor({lp[3 * id], lp[3 * id + 1], lp[3 * id + 2]}, opts).view({3, 1});
+        n.LPosFix = torch::tensor({lf[3 * id], lf[3 * id + 1], lf[3 * id + 2]}, opts).view({3, 1});
+        n.LVel = torch::tensor({lv[3 * id], lv[3 * id + 1], lv[3 * id + 2]}, opts).view({3, 1});
+        n.EPos = torch::tensor({ep[2 * id], ep[2 * id + 1]}, opts).view({2, 1});
+        n.EPosBar = torch::tensor({eb[2 * id], eb[2 * id + 1]}, opts).view({2, 1});
+        n.EVel = torch::tensor({ev[2 * id], ev[2 * id + 1]}, opts).view({2, 1});
+        cloth.warp_nodes[key(u, v)].LPos = n.LPos;
+        cloth.weft_nodes[key(u, v)].LPos = n.LPos;
+      }
+    cloth.UpdateClothUnits();
+  }
+
+  std::vector<double> dump_steps = parse_list(get_s(kv, "dump_steps", ""));
+  auto is_dump = [&](int s) {
+    for (double d : dump_steps)
+      if (static_cast<int>(d) == s) return true;
+    return false;
+  };
+
+  Writer w(get_s(kv, "out", "ref_out.bin"));
+  PhysicsCloth phy{&env};
+  phy.InitMV();
+  const Tensor h = torch::tensor({get_d(kv, "h", 1e-3)}, opts);
+
+  std::vector<double> ext;
+  if (kv.count("ext_force")) ext = parse_list(kv["ext_force"]);
+
+  auto dump_state = [&](const std::string& tag) {
+    std::vector<double> lp(N * 3), lv(N * 3), lf(N * 3), ep(N * 2), ev(N * 2), eb(N * 2), nrm(N * 3, 0.0);
+    for (int v = 0; v < Lh; ++v)
+      for (int u = 0; u < W; ++u) {
+        int id = u + v * W;
+        const Node& n = cloth.nodes.at(key(u, v));
+        for (int k = 0; k < 3; ++k) {
+          lp[3 * id + k] = n.LPos[k][0].item<double>();
+          lv[3 * id + k] = n.LVel[k][0].item<double>();
+          lf[3 * id + k] = n.LPosFix[k][0].item<double>();
+          if (n.n.defined()) nrm[3 * id + k] = n.n[k][0].item<double>();
+        }
+        for (int k = 0; k < 2; ++k) {
+          ep[2 * id + k] = n.EPos[k][0].item<double>();
+          ev[2 * id + k] = n.EVel[k][0].item<double>();
+          eb[2 * id + k] = n.EPosBar[k][0].item<double>();
+        }
+      }
+    w.put(tag + ".LPos", {N, 3}, lp.data());
+    w.put(tag + ".LVel", {N, 3}, lv.data());
+    w.put(tag + ".LPosFix", {N, 3}, lf.data());
+    w.put(tag + ".EPos", {N, 2}, ep.data());
+    w.put(tag + ".EVel", {N, 2}, ev.data());
+    w.put(tag + ".EPosBar", {N, 2}, eb.data());
+    w.put(tag + ".normal", {N, 3}, nrm.data());
+  };
+
+  dump_state("s0");
+  int status = 0;
+  for (int s = 0; s < steps; ++s) {
+    phy.FillMV();
+    const Tensor M = phy.get_SpaM();
+    const Tensor Kx = phy.get_SpaFPos();
+    const Tensor Dv = phy.get_SpaFVel();
+    Tensor F = phy.get_SpaF();
+    const Tensor V = phy.get_SpaVel();
+    if (!ext.empty()) F = F + torch::tensor(ext, opts).view({-1, 1});
+    const Tensor A = M - Kx * torch::pow(h, 2) - Dv * h;
+    const Tensor b = h * (F - torch::mm(Dv.transpose(0, 1), V)) + torch::mm(M, V);
+    if (DetectNaN(A, false) || DetectNaN(b, false) || DetectInf(A, false) || DetectInf(b, false)) {
+      status = 1;
+      break;
+    }
+    Tensor new_vel = solver == "lu" ? TorchSolver(A, b) : EigenSolver::apply(A, b);
+    if (DetectNaN(new_vel, false) || DetectInf(new_vel, false)) {
+      status = 1;
+      break;
+    }
+    if (is_dump(s)) {
+      std::string t = "d" + std::to_string(s);
+      w.put_tensor(t + ".M", M);
+      w.put_tensor(t + ".FPos", Kx);
+      w.put_tensor(t + ".FVel", Dv);
+      w.put_tensor(t + ".F", F);
+      w.put_tensor(t + ".Vel", V);
+      w.put_tensor(t + ".A", A);
+      w.put_tensor(t + ".b", b);
+      w.put_tensor(t + ".new_vel", new_vel);
+      w.put_tensor(t + ".slide", phy.F_E_is_Slides[0]);
+      double it = static_cast<double>(ref_cg_last_iterations());
+      double er = ref_cg_last_error();
+      w.put(t + ".cg_iters", {1}, &it);
+      w.put(t + ".cg_error", {1}, &er);
+    }
+    cloth.update(new_vel, phy.F_E_is_Slides[0], h);
+    phy.ResetMV();
+    dump_state("s" + std::to_string(s + 1));
+  }
+  double st = status;
+  w.put("status", {1}, &st);
+  return 0;
+}

@@ -1,0 +1,41 @@
+"""Helpers to load the reference-generated fixtures in tests/golden/."""
+import glob
+import os
+
+import numpy as np
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLDEN_DIR, name + ".npz")))
+
+
+def spec_kwargs(g):
+    """Construction parameters of a fixture, as keyword arguments."""
+    return dict(width=int(g["width"]), length=int(g["length"]), warp=g["warp"], weft=g["weft"],
+                height=float(g["height"]), L=float(g["L"]), R=float(g["R"]), pose=int(g["pose"]),
+                weave=int(g["weave"]), kc=float(g["kc"]), kf=float(g["kf"]), df=float(g["df"]),
+                mu=float(g["mu"]), S=float(g["S"]), handle_stiffness=float(g["handle_stiffness"]),
+                G=tuple(float(x) for x in g["G"]), wind_vel=tuple(float(x) for x in g["wind_vel"]),
+                wind_density=float(g["wind_density"]), wind_drag=float(g["wind_drag"]),
+                handles=[tuple(int(a) for a in r) for r in g["handles"].reshape(-1, 2)])
+
+
+def init_state(g):
+    if "init_LPos" not in g:
+        return None
+    return {k: g["init_" + k] for k in ("LPos", "LPosFix", "LVel", "EPos", "EPosBar", "EVel")}
+
+
+def state(g, step):
+    return {k: g["s%d_%s" % (step, k)] for k in ("LPos", "LPosFix", "LVel", "EPos", "EPosBar", "EVel")}
+
+
+def rel(a, b):
+    a = np.asarray(a); b = np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
