@@ -1,0 +1,605 @@
+// ys_api.cu -- host runtime and C ABI (include/yarnsim.h) of the batched
+// yarn-level cloth step on one GPU.
+//
+// The handle builds the batch topology once: per-node cloth id / grid
+// coordinates / flags, per-yarn-line material, the colour classes of every
+// element pass, and the thread-block partition used by the per-cloth solver.
+// All device memory is allocated here and nowhere else.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/yarnsim.h"
+#include "ys_kernels.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+ys_status fail(ys_status s, const std::string& msg) {
+  g_err = msg;
+  return s;
+}
+
+#define YS_CUDA(call)                                                                              \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      return fail(YS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));               \
+  } while (0)
+
+struct Pass {
+  int kind;  // 0 warp/weft edge, 1 bend, 2 face, 3 shear
+  int k;
+  int off, n;  // range inside the anchor list
+};
+
+// node-major [n][c] <-> component-major [c][n]
+__global__ void k_to_soa(const double* __restrict__ in, double* __restrict__ out, int64_t n, int c) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int k = 0; k < c; ++k) out[k * n + i] = in[i * c + k];
+}
+__global__ void k_to_aos(const double* __restrict__ in, double* __restrict__ out, int64_t n, int c) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int k = 0; k < c; ++k) out[i * c + k] = in[k * n + i];
+}
+// iteration bookkeeping only; the status bits set by the assembly are kept
+__global__ void k_reset_pc(ys::PcgCloth* pc, const int* maxiter, int ncloth, int maxiter_override) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncloth) return;
+  pc[c].status &= 1;
+  pc[c].active = 0;
+  pc[c].iters = 0;
+  pc[c].maxiter = maxiter_override >= 0 ? maxiter_override : maxiter[c];
+}
+__global__ void k_reset_status(ys::PcgCloth* pc, int ncloth) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncloth) pc[c].status = 0;
+}
+
+}  // namespace
+
+struct ys_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int ncloth = 0;
+  int ntot = 0;
+  std::vector<ys::ClothParams> cp;
+  std::vector<int64_t> dims;
+  std::vector<int> anchors_host;
+  std::vector<Pass> passes;
+  int geom_off = 0, geom_n = 0;  // interior-node list (normals, friction)
+  // device memory
+  std::vector<void*> allocs;
+  int64_t bytes = 0;
+  ys::View v{};
+  ys::Blocks blk{};
+  ys::Solver so{};
+  int* anchors = nullptr;
+  int* maxiter_dev = nullptr;
+  double* stage = nullptr;  // [5][ntot] staging for layout changes
+  double* ext = nullptr;    // [5][ntot]
+  int* h_nactive = nullptr; // pinned
+  bool assembled = false;
+  int max_maxiter = 0;
+
+  template <class T>
+  ys_status alloc(T** p, size_t count) {
+    void* q = nullptr;
+    size_t nb = std::max<size_t>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&q, nb);
+    if (e != cudaSuccess) return fail(YS_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    allocs.push_back(q);
+    bytes += (int64_t)nb;
+    *p = static_cast<T*>(q);
+    return YS_OK;
+  }
+  ~ys_batch() {
+    for (void* p : allocs) cudaFree(p);
+    if (h_nactive) cudaFreeHost(h_nactive);
+  }
+};
+
+namespace {
+
+ys_status upload_soa(ys_batch* b, const double* src, double* dst, int c, int32_t flags) {
+  const int64_t n = b->ntot;
+  if (!src) return YS_OK;
+  const double* d_src = src;
+  if (!(flags & YS_ON_DEVICE)) {
+    YS_CUDA(cudaMemcpyAsync(b->stage, src, sizeof(double) * n * c, cudaMemcpyHostToDevice, b->stream));
+    d_src = b->stage;
+  }
+  k_to_soa<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(d_src, dst, n, c);
+  YS_CUDA(cudaGetLastError());
+  if (!(flags & YS_ON_DEVICE)) YS_CUDA(cudaStreamSynchronize(b->stream));  // stage is reused
+  return YS_OK;
+}
+
+ys_status download_aos(ys_batch* b, const double* src, double* dst, int c, int32_t flags) {
+  const int64_t n = b->ntot;
+  if (!dst) return YS_OK;
+  double* d_dst = (flags & YS_ON_DEVICE) ? dst : b->stage;
+  k_to_aos<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(src, d_dst, n, c);
+  YS_CUDA(cudaGetLastError());
+  if (!(flags & YS_ON_DEVICE)) {
+    YS_CUDA(cudaMemcpyAsync(dst, b->stage, sizeof(double) * n * c, cudaMemcpyDeviceToHost, b->stream));
+    YS_CUDA(cudaStreamSynchronize(b->stream));
+  }
+  return YS_OK;
+}
+
+int weave_flip(int weave, int i, int j) {
+  // src/Cloth.cpp:69-92 (interior nodes only)
+  if (weave == 0) return (i + j) % 2 != 0;
+  if (weave == 1) {
+    int rv = j % 4, ru = (i + rv) % 4;
+    return ru < 2;
+  }
+  int rv = (j - 1) % 4, q = rv / 2, r = rv % 2, idx = q * 3 + r * 2, ru = (i - 1 + idx) % 4;
+  return ru == 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ys_last_error(void) { return g_err.c_str(); }
+
+ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t device, void* cuda_stream,
+                          ys_batch** out) {
+  if (!out || n_cloths <= 0 || !descs) return fail(YS_ERR_ARG, "n_cloths must be > 0 and descs non-null");
+  *out = nullptr;
+  for (int c = 0; c < n_cloths; ++c) {
+    const ys_cloth_desc& d = descs[c];
+    if (d.width < 3 || d.length < 3) return fail(YS_ERR_ARG, "cloth sides must be >= 3 crossings");
+    if (!d.warp_rho || !d.warp_Y || !d.warp_B || !d.weft_rho || !d.weft_Y || !d.weft_B)
+      return fail(YS_ERR_ARG, "yarn line material arrays must be non-null");
+    if (d.pose < 0 || d.pose > 1 || d.weave < 0 || d.weave > 2) return fail(YS_ERR_ARG, "bad pose or weave");
+    if (!(d.L > 0) || !(d.R > 0) || d.R >= d.L) return fail(YS_ERR_ARG, "need 0 < R < L");
+    if (d.n_handles < 0 || (d.n_handles > 0 && !d.handles)) return fail(YS_ERR_ARG, "bad handle list");
+  }
+  YS_CUDA(cudaSetDevice(device));
+  ys_batch* b = new ys_batch();
+  b->device = device;
+  b->stream = static_cast<cudaStream_t>(cuda_stream);
+  b->ncloth = n_cloths;
+  // ------------------------------------------------------------ topology
+  std::vector<int> node_cloth, node_u, node_v;
+  std::vector<uint8_t> flags;
+  std::vector<double> X, XF, UV, rho, ks, kb;
+  std::vector<int> blk_cloth, blk_node0, blk_count, cloth_blk0, cloth_nblk, maxiter;
+  std::vector<std::vector<int>> lists(2 + 2 + 3 + 3 + 4 + 9);
+  int off = 0, line_off = 0;
+  for (int c = 0; c < n_cloths; ++c) {
+    const ys_cloth_desc& d = descs[c];
+    ys::ClothParams P{};
+    P.W = d.width; P.H = d.length; P.node_off = off;
+    P.warp_line_off = line_off;
+    P.weft_line_off = line_off + d.length;
+    P.L = d.L; P.R = d.R; P.kc = d.kc; P.kf = d.kf; P.df = d.df; P.mu = d.mu; P.S = d.S;
+    P.kh = d.handle_stiffness;
+    P.jam = 2.0 * std::asin(d.R / d.L);  // src/Cloth.cpp:29
+    for (int k = 0; k < 3; ++k) { P.G[k] = d.G[k]; P.wind[k] = d.wind_vel[k]; }
+    P.wind_rho = d.wind_density; P.wind_drag = d.wind_drag;
+    b->cp.push_back(P);
+    for (int i = 0; i < d.length; ++i) {
+      rho.push_back(d.warp_rho[i]);
+      ks.push_back(d.warp_Y[i] * ys::kPi * std::pow(d.R, 2));  // src/Yarn.h:14-15
+      kb.push_back(d.warp_B[i] * ys::kPi * std::pow(d.R, 2));
+    }
+    for (int i = 0; i < d.width; ++i) {
+      rho.push_back(d.weft_rho[i]);
+      ks.push_back(d.weft_Y[i] * ys::kPi * std::pow(d.R, 2));
+      kb.push_back(d.weft_B[i] * ys::kPi * std::pow(d.R, 2));
+    }
+    line_off += d.length + d.width;
+    const int W = d.width, H = d.length;
+    std::vector<uint8_t> fixed(W * H, 0);
+    for (int hnd = 0; hnd < d.n_handles; ++hnd) {
+      const int u = d.handles[2 * hnd], vv = d.handles[2 * hnd + 1];
+      if (u >= 0 && u < W && vv >= 0 && vv < H) fixed[u + vv * W] = 1;
+    }
+    for (int j = 0; j < H; ++j)
+      for (int i = 0; i < W; ++i) {
+        const int n = off + i + j * W;
+        node_cloth.push_back(c);
+        node_u.push_back(i);
+        node_v.push_back(j);
+        const bool interior = !(i == 0 || i == W - 1 || j == 0 || j == H - 1);
+        uint8_t f = interior ? ys::YS_INTERIOR : 0;
+        if (interior && weave_flip(d.weave, i, j)) f |= ys::YS_FLIP;
+        if (fixed[i + j * W]) f |= ys::YS_FIXED;
+        flags.push_back(f);
+        // Cloth::build (src/Cloth.cpp:52-99)
+        if (d.pose == 0) { X.push_back(i * d.L); X.push_back(0.0); X.push_back(d.height - j * d.L); }
+        else { X.push_back(i * d.L); X.push_back(j * d.L); X.push_back(d.height); }
+        UV.push_back(i * d.L);
+        UV.push_back(j * d.L);
+        // colour classes
+        if (i < W - 1) lists[0 + (i & 1)].push_back(n);
+        if (j < H - 1) lists[2 + (j & 1)].push_back(n);
+        if (i >= 1 && i <= W - 2) lists[4 + i % 3].push_back(n);
+        if (j >= 1 && j <= H - 2) lists[7 + j % 3].push_back(n);
+        if (i < W - 1 && j < H - 1) lists[10 + (i & 1) + 2 * (j & 1)].push_back(n);
+        if (interior) lists[14 + (i % 3) + 3 * (j % 3)].push_back(n);
+      }
+    const int nb = (W * H + ys::kBlock - 1) / ys::kBlock;
+    cloth_blk0.push_back((int)blk_cloth.size());
+    cloth_nblk.push_back(nb);
+    for (int q = 0; q < nb; ++q) {
+      blk_cloth.push_back(c);
+      blk_node0.push_back(off + q * ys::kBlock);
+      blk_count.push_back(std::min(ys::kBlock, W * H - q * ys::kBlock));
+    }
+    const int64_t dim = 3LL * W * H + 2LL * (W - 2) * (H - 2);
+    b->dims.push_back(dim);
+    maxiter.push_back((int)std::min<int64_t>(2 * dim, 1 << 30));
+    off += W * H;
+  }
+  b->ntot = off;
+  b->max_maxiter = *std::max_element(maxiter.begin(), maxiter.end());
+  // anchor lists and passes
+  std::vector<int> interior_nodes;
+  for (int n = 0; n < off; ++n)
+    if (flags[n] & ys::YS_INTERIOR) interior_nodes.push_back(n);
+  auto add_pass = [&](int kind, int k, const std::vector<int>& L) {
+    Pass p{kind, k, (int)b->anchors_host.size(), (int)L.size()};
+    b->anchors_host.insert(b->anchors_host.end(), L.begin(), L.end());
+    b->passes.push_back(p);
+  };
+  // element order: edges (warp then weft), bends (warp then weft), faces,
+  // [friction], shear -- as in FillMV (src/PhysicsCloth.cpp:56-131)
+  add_pass(0, 0, lists[0]); add_pass(0, 0, lists[1]);
+  add_pass(0, 1, lists[2]); add_pass(0, 1, lists[3]);
+  for (int c = 0; c < 3; ++c) add_pass(1, 0, lists[4 + c]);
+  for (int c = 0; c < 3; ++c) add_pass(1, 1, lists[7 + c]);
+  for (int c = 0; c < 4; ++c) add_pass(2, 0, lists[10 + c]);
+  for (int c = 0; c < 9; ++c) add_pass(3, 0, lists[14 + c]);
+  b->geom_off = (int)b->anchors_host.size();
+  b->geom_n = (int)interior_nodes.size();
+  b->anchors_host.insert(b->anchors_host.end(), interior_nodes.begin(), interior_nodes.end());
+
+  // ------------------------------------------------------------ device memory
+  const int64_t nt = off;
+  ys_status st = YS_OK;
+  auto A = [&](auto** p, size_t cnt) {
+    if (st == YS_OK) st = b->alloc(p, cnt);
+  };
+  int *d_nc, *d_nu, *d_nv, *d_bc, *d_bn, *d_bk, *d_cb, *d_cn;
+  uint8_t* d_fl;
+  ys::ClothParams* d_cp;
+  double *d_rho, *d_ks, *d_kb;
+  A(&d_nc, nt); A(&d_nu, nt); A(&d_nv, nt); A(&d_fl, nt); A(&d_cp, n_cloths);
+  A(&d_rho, rho.size()); A(&d_ks, ks.size()); A(&d_kb, kb.size());
+  A(&d_bc, blk_cloth.size()); A(&d_bn, blk_cloth.size()); A(&d_bk, blk_cloth.size());
+  A(&d_cb, n_cloths); A(&d_cn, n_cloths);
+  A(&b->anchors, b->anchors_host.size());
+  A(&b->maxiter_dev, n_cloths);
+  ys::View& v = b->v;
+  A(&v.X, 3 * nt); A(&v.V, 3 * nt); A(&v.XF, 3 * nt); A(&v.UV, 2 * nt); A(&v.UVD, 2 * nt); A(&v.UVB, 2 * nt);
+  A(&v.UV0, 2 * nt); A(&v.NRM, 3 * nt); A(&v.COMP, nt); A(&v.SLIDE, 2 * nt);
+  A(&v.A, (size_t)ys::YS_NUM_SLOTS * nt); A(&v.B, 5 * nt); A(&v.CL, 3 * nt); A(&v.CLE, 6 * nt);
+  A(&v.FE, 2 * nt); A(&v.KEE, 2 * nt); A(&v.DEE, 2 * nt);
+  A(&b->so.x, 5 * nt); A(&b->so.r, 5 * nt); A(&b->so.p, 5 * nt); A(&b->so.q, 5 * nt); A(&b->so.dinv, 5 * nt);
+  A(&b->so.part, 3 * blk_cloth.size()); A(&b->so.pc, n_cloths); A(&b->so.nactive, 1);
+  A(&b->stage, 5 * nt); A(&b->ext, 5 * nt);
+  if (st != YS_OK) { delete b; return st; }
+  if (cudaMallocHost(&b->h_nactive, sizeof(int)) != cudaSuccess) {
+    delete b;
+    return fail(YS_ERR_CUDA, "cudaMallocHost failed");
+  }
+  auto up = [&](void* dst, const void* src, size_t nbytes) -> ys_status {
+    YS_CUDA(cudaMemcpy(dst, src, nbytes, cudaMemcpyHostToDevice));
+    return YS_OK;
+  };
+  ys_status s2 = YS_OK;
+  auto U = [&](void* dst, const void* src, size_t nbytes) { if (s2 == YS_OK && nbytes) s2 = up(dst, src, nbytes); };
+  U(d_nc, node_cloth.data(), sizeof(int) * nt); U(d_nu, node_u.data(), sizeof(int) * nt);
+  U(d_nv, node_v.data(), sizeof(int) * nt); U(d_fl, flags.data(), nt);
+  U(d_cp, b->cp.data(), sizeof(ys::ClothParams) * n_cloths);
+  U(d_rho, rho.data(), sizeof(double) * rho.size()); U(d_ks, ks.data(), sizeof(double) * ks.size());
+  U(d_kb, kb.data(), sizeof(double) * kb.size());
+  U(d_bc, blk_cloth.data(), sizeof(int) * blk_cloth.size()); U(d_bn, blk_node0.data(), sizeof(int) * blk_cloth.size());
+  U(d_bk, blk_count.data(), sizeof(int) * blk_cloth.size());
+  U(d_cb, cloth_blk0.data(), sizeof(int) * n_cloths); U(d_cn, cloth_nblk.data(), sizeof(int) * n_cloths);
+  U(b->anchors, b->anchors_host.data(), sizeof(int) * b->anchors_host.size());
+  U(b->maxiter_dev, maxiter.data(), sizeof(int) * n_cloths);
+  // initial state: positions, EPos, EPosBar = EPos, LPosFix = LPos, zero velocities
+  {
+    std::vector<double> soa(5 * nt, 0.0);
+    for (int k = 0; k < 3; ++k)
+      for (int64_t i = 0; i < nt; ++i) soa[k * nt + i] = X[3 * i + k];
+    U(v.X, soa.data(), sizeof(double) * 3 * nt);
+    U(v.XF, soa.data(), sizeof(double) * 3 * nt);
+    for (int k = 0; k < 2; ++k)
+      for (int64_t i = 0; i < nt; ++i) soa[k * nt + i] = UV[2 * i + k];
+    U(v.UV, soa.data(), sizeof(double) * 2 * nt);
+    U(v.UVB, soa.data(), sizeof(double) * 2 * nt);
+    U(v.UV0, soa.data(), sizeof(double) * 2 * nt);
+  }
+  if (s2 != YS_OK) { delete b; return s2; }
+  if (cudaMemset(v.V, 0, sizeof(double) * 3 * nt) != cudaSuccess ||
+      cudaMemset(v.UVD, 0, sizeof(double) * 2 * nt) != cudaSuccess ||
+      cudaMemset(v.NRM, 0, sizeof(double) * 3 * nt) != cudaSuccess ||
+      cudaMemset(v.COMP, 0, sizeof(double) * nt) != cudaSuccess ||
+      cudaMemset(v.SLIDE, 0, sizeof(double) * 2 * nt) != cudaSuccess ||
+      cudaMemset(b->so.pc, 0, sizeof(ys::PcgCloth) * n_cloths) != cudaSuccess) {
+    delete b;
+    return fail(YS_ERR_CUDA, "cudaMemset failed");
+  }
+  v.ntot = (int)nt;
+  v.ncloth = n_cloths;
+  v.node_cloth = d_nc; v.node_u = d_nu; v.node_v = d_nv; v.flags = d_fl; v.cp = d_cp;
+  v.line_rho = d_rho; v.line_ks = d_ks; v.line_kb = d_kb;
+  v.ext = nullptr;
+  v.h = 1e-3;
+  b->blk.nblk = (int)blk_cloth.size();
+  b->blk.blk_cloth = d_bc; b->blk.blk_node0 = d_bn; b->blk.blk_count = d_bk;
+  b->blk.cloth_blk0 = d_cb; b->blk.cloth_nblk = d_cn;
+  b->so.tol = DBL_EPSILON;
+  *out = b;
+  return YS_OK;
+}
+
+void ys_batch_destroy(ys_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  delete b;
+}
+
+ys_status ys_batch_get_info(const ys_batch* b, ys_batch_info* info) {
+  if (!b || !info) return fail(YS_ERR_ARG, "null argument");
+  info->n_cloths = b->ncloth;
+  info->total_nodes = b->ntot;
+  info->device_bytes = b->bytes;
+  return YS_OK;
+}
+
+int64_t ys_cloth_node_offset(const ys_batch* b, int32_t c) {
+  if (!b || c < 0 || c >= b->ncloth) return -1;
+  return b->cp[c].node_off;
+}
+
+int64_t ys_cloth_dim(const ys_batch* b, int32_t c) {
+  if (!b || c < 0 || c >= b->ncloth) return -1;
+  return b->dims[c];
+}
+
+ys_status ys_set_state(ys_batch* b, const double* lpos, const double* lposfix, const double* lvel,
+                       const double* epos, const double* eposbar, const double* evel, int32_t flags) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  YS_CUDA(cudaSetDevice(b->device));
+  ys_status s;
+  if ((s = upload_soa(b, lpos, b->v.X, 3, flags)) != YS_OK) return s;
+  if ((s = upload_soa(b, lposfix, b->v.XF, 3, flags)) != YS_OK) return s;
+  if ((s = upload_soa(b, lvel, b->v.V, 3, flags)) != YS_OK) return s;
+  if ((s = upload_soa(b, epos, b->v.UV, 2, flags)) != YS_OK) return s;
+  if ((s = upload_soa(b, eposbar, b->v.UVB, 2, flags)) != YS_OK) return s;
+  if ((s = upload_soa(b, evel, b->v.UVD, 2, flags)) != YS_OK) return s;
+  b->assembled = false;
+  return YS_OK;
+}
+
+ys_status ys_get_state(ys_batch* b, double* lpos, double* lposfix, double* lvel, double* epos, double* eposbar,
+                       double* evel, int32_t flags) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  YS_CUDA(cudaSetDevice(b->device));
+  ys_status s;
+  if ((s = download_aos(b, b->v.X, lpos, 3, flags)) != YS_OK) return s;
+  if ((s = download_aos(b, b->v.XF, lposfix, 3, flags)) != YS_OK) return s;
+  if ((s = download_aos(b, b->v.V, lvel, 3, flags)) != YS_OK) return s;
+  if ((s = download_aos(b, b->v.UV, epos, 2, flags)) != YS_OK) return s;
+  if ((s = download_aos(b, b->v.UVB, eposbar, 2, flags)) != YS_OK) return s;
+  if ((s = download_aos(b, b->v.UVD, evel, 2, flags)) != YS_OK) return s;
+  return YS_OK;
+}
+
+ys_status ys_set_wind(ys_batch* b, int32_t cloth, const double wind_vel[3]) {
+  if (!b || !wind_vel || cloth < -1 || cloth >= b->ncloth) return fail(YS_ERR_ARG, "bad argument");
+  YS_CUDA(cudaSetDevice(b->device));
+  const int c0 = cloth < 0 ? 0 : cloth, c1 = cloth < 0 ? b->ncloth : cloth + 1;
+  for (int c = c0; c < c1; ++c) {
+    for (int k = 0; k < 3; ++k) b->cp[c].wind[k] = wind_vel[k];
+    ys::ClothParams* dst = const_cast<ys::ClothParams*>(b->v.cp) + c;
+    YS_CUDA(cudaMemcpyAsync(&dst->wind[0], b->cp[c].wind, sizeof(double) * 3, cudaMemcpyHostToDevice, b->stream));
+  }
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  return YS_OK;
+}
+
+ys_status ys_assemble(ys_batch* b, double h, const double* ext_force, int32_t flags) {
+  if (!b || !(h > 0)) return fail(YS_ERR_ARG, "bad argument");
+  YS_CUDA(cudaSetDevice(b->device));
+  b->v.h = h;
+  b->v.ext = nullptr;
+  if (ext_force) {
+    ys_status s = upload_soa(b, ext_force, b->ext, 5, flags);
+    if (s != YS_OK) return s;
+    b->v.ext = b->ext;
+  }
+  cudaStream_t s = b->stream;
+  const ys::View& v = b->v;
+  k_reset_status<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->ncloth);
+  // UpdateClothUnits normals for the current positions (src/Cloth.cpp:307-327)
+  ys::launch_geom(v, b->anchors + b->geom_off, b->geom_n, s);
+  ys::launch_clear(v, s);
+  bool friction_done = false;
+  for (const Pass& p : b->passes) {
+    const int* a = b->anchors + p.off;
+    if (p.kind == 3 && !friction_done) {
+      // ConSlideFriction needs every edge and bend term; shear needs its
+      // compression (src/PhysicsCloth.cpp:97-131)
+      ys::launch_friction(v, b->anchors + b->geom_off, b->geom_n, s);
+      friction_done = true;
+    }
+    switch (p.kind) {
+      case 0: ys::launch_edges(v, a, p.n, p.k, s); break;
+      case 1: ys::launch_bends(v, a, p.n, p.k, s); break;
+      case 2: ys::launch_faces(v, a, p.n, s); break;
+      case 3: ys::launch_shear(v, a, p.n, s); break;
+    }
+  }
+  ys::launch_finalize(v, b->blk, b->so, s);
+  YS_CUDA(cudaGetLastError());
+  b->assembled = true;
+  return YS_OK;
+}
+
+ys_status ys_solve(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* stats) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  if (!b->assembled) return fail(YS_ERR_ARG, "ys_solve before ys_assemble");
+  YS_CUDA(cudaSetDevice(b->device));
+  cudaStream_t s = b->stream;
+  b->so.tol = (opts && opts->tol > 0) ? opts->tol : DBL_EPSILON;
+  const int override_max = (opts && opts->maxiter >= 0) ? opts->maxiter : -1;
+  const int every = (opts && opts->check_every > 0) ? opts->check_every : 16;
+  const int cap = override_max >= 0 ? override_max : b->max_maxiter;
+  k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
+  YS_CUDA(cudaGetLastError());
+  ys::launch_pcg_setup(b->v, b->blk, b->so, s);
+  int it = 0;
+  while (it < cap) {
+    const int n = std::min(every, cap - it);
+    for (int q = 0; q < n; ++q, ++it) ys::launch_pcg_iter(b->v, b->blk, b->so, it, s);
+    ys::launch_count_active(b->v, b->so, s);
+    YS_CUDA(cudaMemcpyAsync(b->h_nactive, b->so.nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
+    YS_CUDA(cudaStreamSynchronize(s));
+    if (*b->h_nactive == 0) break;
+  }
+  YS_CUDA(cudaGetLastError());
+  std::vector<ys::PcgCloth> pc(b->ncloth);
+  YS_CUDA(cudaMemcpyAsync(pc.data(), b->so.pc, sizeof(ys::PcgCloth) * b->ncloth, cudaMemcpyDeviceToHost, s));
+  YS_CUDA(cudaStreamSynchronize(s));
+  ys_status ret = YS_OK;
+  for (int c = 0; c < b->ncloth; ++c) {
+    if (pc[c].status & 1) ret = YS_ERR_NONFINITE;
+    else if ((pc[c].status & 4) && ret == YS_OK) ret = YS_ERR_MAXITER;
+    if (stats) {
+      stats[c].ok = (pc[c].status & 3) == 0;
+      stats[c].cg_iterations = pc[c].iters;
+      stats[c].cg_error = pc[c].bb > 0 ? std::sqrt(pc[c].rr / pc[c].bb) : 0.0;
+      stats[c].hit_maxiter = (pc[c].status & 4) ? 1 : 0;
+    }
+  }
+  return ret;
+}
+
+ys_status ys_get_solution(ys_batch* b, double* x, int32_t flags) {
+  if (!b || !x) return fail(YS_ERR_ARG, "bad argument");
+  YS_CUDA(cudaSetDevice(b->device));
+  return download_aos(b, b->so.x, x, 5, flags);
+}
+
+ys_status ys_step(ys_batch* b, double h, const double* ext_force, int32_t flags, const ys_solve_opts* opts,
+                  ys_cloth_stats* stats) {
+  ys_status s = ys_assemble(b, h, ext_force, flags);
+  if (s != YS_OK) return s;
+  std::vector<ys_cloth_stats> local;
+  ys_cloth_stats* st = stats;
+  if (!st) {
+    local.resize(b->ncloth);
+    st = local.data();
+  }
+  ys_status sol = ys_solve(b, opts, st);
+  if (sol == YS_ERR_ARG || sol == YS_ERR_CUDA) return sol;
+  ys::launch_update(b->v, b->blk, b->so, b->stream);
+  YS_CUDA(cudaGetLastError());
+  // the solution check may have flagged more cloths
+  std::vector<ys::PcgCloth> pc(b->ncloth);
+  YS_CUDA(cudaMemcpyAsync(pc.data(), b->so.pc, sizeof(ys::PcgCloth) * b->ncloth, cudaMemcpyDeviceToHost, b->stream));
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  ys_status ret = sol;
+  for (int c = 0; c < b->ncloth; ++c) {
+    st[c].ok = (pc[c].status & 3) == 0;
+    if (!st[c].ok) ret = YS_ERR_NONFINITE;
+  }
+  b->assembled = false;
+  return ret;
+}
+
+ys_status ys_apply_system(ys_batch* b, const double* x, double* y, int32_t flags) {
+  if (!b || !x || !y) return fail(YS_ERR_ARG, "bad argument");
+  if (!b->assembled) return fail(YS_ERR_ARG, "no assembled system");
+  YS_CUDA(cudaSetDevice(b->device));
+  ys_status s = upload_soa(b, x, b->so.q, 5, flags);
+  if (s != YS_OK) return s;
+  ys::launch_spmv(b->v, b->so.q, b->so.r, b->stream);
+  YS_CUDA(cudaGetLastError());
+  return download_aos(b, b->so.r, y, 5, flags);
+}
+
+ys_status ys_export_system(ys_batch* b, int32_t cloth, double* Aout, double* rhs) {
+  if (!b || cloth < 0 || cloth >= b->ncloth) return fail(YS_ERR_ARG, "bad argument");
+  if (!b->assembled) return fail(YS_ERR_ARG, "no assembled system");
+  YS_CUDA(cudaSetDevice(b->device));
+  const ys::ClothParams& P = b->cp[cloth];
+  const int W = P.W, H = P.H, N = W * H, off = P.node_off;
+  const int64_t nt = b->ntot, dim = b->dims[cloth];
+  std::vector<double> slots((size_t)ys::YS_NUM_SLOTS * N), bv(5 * (size_t)N);
+  YS_CUDA(cudaMemcpy2DAsync(slots.data(), sizeof(double) * N, b->v.A + off, sizeof(double) * nt, sizeof(double) * N,
+                            ys::YS_NUM_SLOTS, cudaMemcpyDeviceToHost, b->stream));
+  YS_CUDA(cudaMemcpy2DAsync(bv.data(), sizeof(double) * N, b->v.B + off, sizeof(double) * nt, sizeof(double) * N, 5,
+                            cudaMemcpyDeviceToHost, b->stream));
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  auto interior = [&](int u, int v) { return !(u == 0 || u == W - 1 || v == 0 || v == H - 1); };
+  auto erow = [&](int u, int v) { return 3LL * N + 2LL * ((u - 1) + (v - 1) * (W - 2)); };
+  auto S = [&](int sl, int n) { return slots[(size_t)sl * N + n]; };
+  if (Aout) std::memset(Aout, 0, sizeof(double) * dim * dim);
+  for (int vv = 0; vv < H; ++vv)
+    for (int u = 0; u < W; ++u) {
+      const int n = u + vv * W;
+      const bool in = interior(u, vv);
+      if (rhs) {
+        for (int r = 0; r < 3; ++r) rhs[3 * n + r] = bv[(size_t)r * N + n];
+        if (in)
+          for (int k = 0; k < 2; ++k) rhs[erow(u, vv) + k] = bv[(size_t)(3 + k) * N + n];
+      }
+      if (!Aout) continue;
+      for (int s = 0; s < ys::kNumStencil; ++s) {
+        const int uu = u + ys::stencil_du(s), w2 = vv + ys::stencil_dv(s);
+        if (uu < 0 || uu >= W || w2 < 0 || w2 >= H) continue;
+        const int j = uu + w2 * W;
+        for (int r = 0; r < 3; ++r)
+          for (int c = 0; c < 3; ++c) Aout[(3LL * n + r) * dim + 3LL * j + c] = S(ys::YS_SLOT_LL + 9 * s + 3 * r + c, n);
+      }
+      if (!in) continue;
+      const int64_t er = erow(u, vv);
+      for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 2; ++k) Aout[(3LL * n + r) * dim + er + k] = S(ys::YS_SLOT_LE_SELF + 2 * r + k, n);
+      for (int k = 0; k < 2; ++k) {
+        for (int c = 0; c < 3; ++c) Aout[(er + k) * dim + 3LL * n + c] = S(ys::YS_SLOT_EL_SELF + 3 * k + c, n);
+        Aout[(er + k) * dim + er + k] = S(ys::YS_SLOT_EE_SELF + k, n);
+      }
+      for (int m = 0; m < 4; ++m) {
+        const int du = m == 0 ? -1 : m == 1 ? 1 : 0, dv = m == 2 ? -1 : m == 3 ? 1 : 0, k = m < 2 ? 0 : 1;
+        const int uu = u + du, w2 = vv + dv;
+        if (!interior(uu, w2)) continue;
+        const int j = uu + w2 * W;
+        const int64_t ej = erow(uu, w2);
+        for (int r = 0; r < 3; ++r) Aout[(3LL * n + r) * dim + ej + k] = S(ys::YS_SLOT_LE_NBR + 3 * m + r, n);
+        for (int c = 0; c < 3; ++c) Aout[(er + k) * dim + 3LL * j + c] = S(ys::YS_SLOT_EL_NBR + 3 * m + c, n);
+        Aout[(er + k) * dim + ej + k] = S(ys::YS_SLOT_EE_NBR + m, n);
+      }
+    }
+  return YS_OK;
+}
+
+ys_status ys_synchronize(ys_batch* b) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  YS_CUDA(cudaSetDevice(b->device));
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  return YS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,61 @@
+// ys_kernels.cuh -- launch wrappers of the per-step kernels (ys_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ys_common.cuh"
+
+namespace ys {
+
+// per-cloth Jacobi-PCG bookkeeping (one entry per cloth)
+struct PcgCloth {
+  double bb;        // |b|^2
+  double thr;       // stop when |r|^2 < thr
+  double rz[2];     // r.z of the current iterate, double-buffered by parity
+  double rr;        // |r|^2 after the last update
+  int active;       // 1 while iterating
+  int iters;        // completed iterations
+  int maxiter;
+  int status;       // bit 0: non-finite system, bit 1: non-finite solution, bit 2: iteration cap
+};
+
+// thread-block partition of the nodes: blocks never straddle two cloths, so
+// per-cloth reductions are a fixed-order sum over a contiguous block range
+struct Blocks {
+  int nblk;
+  const int* blk_cloth;   // [nblk]
+  const int* blk_node0;   // [nblk] first node
+  const int* blk_count;   // [nblk] nodes in the block
+  const int* cloth_blk0;  // [ncloth] first block
+  const int* cloth_nblk;  // [ncloth]
+};
+
+struct Solver {
+  double* x;      // [5][ntot]
+  double* r;      // [5][ntot]
+  double* p;      // [5][ntot]
+  double* q;      // [5][ntot]
+  double* dinv;   // [5][ntot]
+  double* part;   // [3][nblk] block partial sums
+  PcgCloth* pc;   // [ncloth]
+  int* nactive;   // device counter
+  double tol;
+};
+
+constexpr int kBlock = 128;
+
+void launch_clear(const View& v, cudaStream_t s);
+void launch_geom(const View& v, const int* nodes, int n, cudaStream_t s);
+void launch_edges(const View& v, const int* anchors, int n, int k, cudaStream_t s);
+void launch_bends(const View& v, const int* anchors, int n, int k, cudaStream_t s);
+void launch_faces(const View& v, const int* anchors, int n, cudaStream_t s);
+void launch_friction(const View& v, const int* nodes, int n, cudaStream_t s);
+void launch_shear(const View& v, const int* anchors, int n, cudaStream_t s);
+void launch_finalize(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
+void launch_pcg_setup(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
+void launch_pcg_iter(const View& v, const Blocks& b, const Solver& so, int it, cudaStream_t s);
+void launch_count_active(const View& v, const Solver& so, cudaStream_t s);
+void launch_update(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
+void launch_spmv(const View& v, const double* x, double* y, cudaStream_t s);
+
+}  // namespace ys

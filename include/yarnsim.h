@@ -1,0 +1,139 @@
+/*
+ * yarnsim.h -- C ABI of the GB300 yarn-level cloth step.
+ *
+ * One handle (ys_batch) holds any number of cloths of uneven sizes, each a
+ * W x L grid of yarn crossings with 5 DOFs per interior crossing (x, y, z and
+ * the Eulerian u, v) and 3 per boundary crossing, exactly as the reference's
+ * Cloth (src/Cloth.h:40-84). The handle owns every device buffer; callers pass
+ * host pointers (copied on the handle's stream) or device pointers (flagged by
+ * YS_ON_DEVICE) and never see CUDA or torch types.
+ *
+ * Reference interface each entry point replaces (paths relative to the
+ * reference project root):
+ *   ys_batch_create   Cloth::Cloth + Cloth::set_handles + Environment +
+ *                     PhysicsCloth::InitMV  (src/Cloth.cpp:3-50, 386-394;
+ *                     src/Environment.h:16-21; src/PhysicsCloth.cpp:3-44)
+ *   ys_set_state      Cloth::set_ClothState        (src/Cloth.cpp:421-438)
+ *   ys_get_state      Cloth::get_ClothState        (src/Cloth.cpp:350-371)
+ *   ys_set_wind       Environment::wind            (src/Wind.h:6-17)
+ *   ys_assemble       PhysicsCloth::FillMV + the A, b formation of SimStep
+ *                     (src/PhysicsCloth.cpp:46-156; src/TrainHelper.cpp:19-20)
+ *   ys_export_system  PhysicsCloth::get_SpaM/get_SpaFPos/get_SpaFVel/get_SpaF
+ *                     combined into A and b, dense reference layout
+ *                     (src/PhysicsCloth.h:72-77, src/MatrixMp.cpp:40-111)
+ *   ys_solve          EigenSolver::apply on the assembled system
+ *                     (src/Solvers.h:35-52, src/Solvers.cpp:3-31)
+ *   ys_step           SimStep (src/TrainHelper.cpp:15-54) and
+ *                     SimStep(..., ext_force) (src/TrainHelper.cpp:56-97)
+ *
+ * Error convention: every call returns a ys_status; a cloth whose system or
+ * solution is non-finite is reported per cloth (SimStep returning false,
+ * src/TrainHelper.cpp:22-48) and left unchanged. Nothing ever exits.
+ * Threading: one handle per host thread; calls are ordered on the handle's
+ * stream.
+ */
+#ifndef YARNSIM_H
+#define YARNSIM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  YS_OK = 0,
+  YS_ERR_ARG = 1,        /* invalid argument */
+  YS_ERR_CUDA = 2,       /* a CUDA call failed (message via ys_last_error) */
+  YS_ERR_NONFINITE = 3,  /* at least one cloth had a non-finite system or solution */
+  YS_ERR_MAXITER = 4     /* at least one cloth stopped at the PCG iteration cap */
+} ys_status;
+
+/* flags */
+#define YS_ON_DEVICE 1 /* pointers are device pointers (else host) */
+
+typedef struct ys_batch ys_batch;
+
+/* Construction parameters of one cloth, in the reference's own units
+ * (Cloth(W, L, height, L_, R, yarns, kc, kf, df, mu, S, handle_stiffness,
+ * WovenPattern, InitPose), src/Cloth.h:55-60, plus gravity and wind).
+ * Yarn material is given per yarn line: warp line j is node row v = j
+ * (`length` entries), weft line i is node column u = i (`width` entries);
+ * ks = Y*PI*R^2 and kb = B*PI*R^2 (src/Yarn.h:12-16). */
+typedef struct {
+  int32_t width, length;
+  double height, L, R;
+  int32_t pose;  /* 0 Upright, 1 Flat  (src/Cloth.cpp:57-59) */
+  int32_t weave; /* 0 Plain, 1 Twill, 2 Satin (src/Cloth.cpp:69-92) */
+  const double *warp_rho, *warp_Y, *warp_B;
+  const double *weft_rho, *weft_Y, *weft_B;
+  double kc, kf, df, mu, S, handle_stiffness;
+  double G[3];
+  double wind_vel[3];
+  double wind_density, wind_drag;
+  int32_t n_handles;
+  const int32_t *handles; /* n_handles (u, v) pairs */
+} ys_cloth_desc;
+
+typedef struct {
+  double tol;         /* relative residual |r| / |b|; <= 0: DBL_EPSILON (Eigen default) */
+  int32_t maxiter;    /* per cloth; < 0: 2 * system dimension (Eigen default) */
+  int32_t check_every;/* iterations between device->host convergence polls; <= 0: 16 */
+} ys_solve_opts;
+
+typedef struct {
+  int32_t ok;         /* 1 if the step succeeded (SimStep's return value) */
+  int32_t cg_iterations;
+  double cg_error;    /* sqrt(|r|^2 / |b|^2) at exit */
+  int32_t hit_maxiter;
+} ys_cloth_stats;
+
+typedef struct {
+  int32_t n_cloths;
+  int64_t total_nodes;      /* sum of width*length */
+  int64_t device_bytes;     /* device memory held by the handle */
+} ys_batch_info;
+
+const char *ys_last_error(void);
+
+ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc *descs, int32_t device, void *cuda_stream,
+                          ys_batch **out);
+void ys_batch_destroy(ys_batch *b);
+ys_status ys_batch_get_info(const ys_batch *b, ys_batch_info *info);
+/* node offset of cloth c inside the batch's node-ordered arrays */
+int64_t ys_cloth_node_offset(const ys_batch *b, int32_t c);
+/* system dimension of cloth c in the reference's layout: 3*W*L + 2*(W-2)*(L-2) */
+int64_t ys_cloth_dim(const ys_batch *b, int32_t c);
+
+/* Node-ordered state of the whole batch (node = offset(c) + u + v*W):
+ * lpos, lposfix, lvel: [total_nodes][3]; epos, eposbar, evel: [total_nodes][2].
+ * Any pointer may be NULL (that field is left untouched). */
+ys_status ys_set_state(ys_batch *b, const double *lpos, const double *lposfix, const double *lvel,
+                       const double *epos, const double *eposbar, const double *evel, int32_t flags);
+ys_status ys_get_state(ys_batch *b, double *lpos, double *lposfix, double *lvel, double *epos, double *eposbar,
+                       double *evel, int32_t flags);
+ys_status ys_set_wind(ys_batch *b, int32_t cloth, const double wind_vel[3]);
+
+/* FillMV + A, b for step size h; ext_force: NULL or [total_nodes][5] (node
+ * layout x, y, z, u, v; the u, v entries of boundary nodes are ignored). */
+ys_status ys_assemble(ys_batch *b, double h, const double *ext_force, int32_t flags);
+/* Dense copy of cloth c's assembled A (dim x dim, row-major) and b (dim), in
+ * the reference's DOF order; meant for checks on small cloths. */
+ys_status ys_export_system(ys_batch *b, int32_t cloth, double *A, double *rhs);
+/* Jacobi-PCG on the assembled systems; the solution stays on the device. */
+ys_status ys_solve(ys_batch *b, const ys_solve_opts *opts, ys_cloth_stats *stats);
+/* Solution of the last ys_solve in node layout [total_nodes][5]. */
+ys_status ys_get_solution(ys_batch *b, double *x, int32_t flags);
+/* One SimStep for every cloth: assemble, solve, update. stats: NULL or
+ * n_cloths entries (host). */
+ys_status ys_step(ys_batch *b, double h, const double *ext_force, int32_t flags, const ys_solve_opts *opts,
+                  ys_cloth_stats *stats);
+/* y = A x with the assembled matrices (node layout [total_nodes][5]). */
+ys_status ys_apply_system(ys_batch *b, const double *x, double *y, int32_t flags);
+/* Waits for the handle's stream. */
+ys_status ys_synchronize(ys_batch *b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

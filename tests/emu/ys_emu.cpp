@@ -1,0 +1,242 @@
+// ys_emu.cpp -- TEST-ONLY host emulation of the GPU step for one cloth.
+//
+// Runs the product's per-element / per-node device functions
+// (csrc/ys_items.cuh, compiled here as plain C++) in host loops that mirror
+// the launch order of csrc/ys_api.cu, so the element arithmetic can be
+// checked against the CPU oracle on a machine without a GPU. It is built and
+// loaded only by tests/test_emu_vs_oracle.py; the package never loads it.
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/yarnsim.h"
+#include "../../fine-grained-differentiable-physics-a-yarn-level-model-for-fabrics_gb300/csrc/ys_items.cuh"
+
+namespace {
+
+struct Emu {
+  ys::ClothParams P;
+  int N;
+  std::vector<int> node_cloth, node_u, node_v;
+  std::vector<uint8_t> flags;
+  std::vector<double> rho, ks, kb;
+  std::vector<double> X, V, XF, UV, UVD, UVB, UV0, NRM, COMP, SLIDE, A, B, CL, CLE, FE, KEE, DEE, EXT, DINV, SOL;
+  ys::View v{};
+  int bad = 0;
+
+  void bind() {
+    v.ntot = N;
+    v.ncloth = 1;
+    v.node_cloth = node_cloth.data(); v.node_u = node_u.data(); v.node_v = node_v.data();
+    v.flags = flags.data(); v.cp = &P;
+    v.line_rho = rho.data(); v.line_ks = ks.data(); v.line_kb = kb.data();
+    v.X = X.data(); v.V = V.data(); v.XF = XF.data(); v.UV = UV.data(); v.UVD = UVD.data(); v.UVB = UVB.data();
+    v.UV0 = UV0.data(); v.NRM = NRM.data(); v.COMP = COMP.data(); v.SLIDE = SLIDE.data();
+    v.A = A.data(); v.B = B.data(); v.CL = CL.data(); v.CLE = CLE.data(); v.FE = FE.data(); v.KEE = KEE.data();
+    v.DEE = DEE.data();
+  }
+};
+
+int flip_of(int weave, int i, int j) {
+  if (weave == 0) return (i + j) % 2 != 0;
+  if (weave == 1) { int rv = j % 4, ru = (i + rv) % 4; return ru < 2; }
+  int rv = (j - 1) % 4, q = rv / 2, r = rv % 2, idx = q * 3 + r * 2, ru = (i - 1 + idx) % 4;
+  return ru == 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* emu_create(const ys_cloth_desc* d) {
+  Emu* e = new Emu();
+  const int W = d->width, H = d->length, N = W * H;
+  e->N = N;
+  ys::ClothParams& P = e->P;
+  P = ys::ClothParams{};
+  P.W = W; P.H = H; P.node_off = 0; P.warp_line_off = 0; P.weft_line_off = H;
+  P.L = d->L; P.R = d->R; P.kc = d->kc; P.kf = d->kf; P.df = d->df; P.mu = d->mu; P.S = d->S;
+  P.kh = d->handle_stiffness; P.jam = 2.0 * std::asin(d->R / d->L);
+  for (int k = 0; k < 3; ++k) { P.G[k] = d->G[k]; P.wind[k] = d->wind_vel[k]; }
+  P.wind_rho = d->wind_density; P.wind_drag = d->wind_drag;
+  for (int i = 0; i < H; ++i) {
+    e->rho.push_back(d->warp_rho[i]);
+    e->ks.push_back(d->warp_Y[i] * ys::kPi * std::pow(d->R, 2));
+    e->kb.push_back(d->warp_B[i] * ys::kPi * std::pow(d->R, 2));
+  }
+  for (int i = 0; i < W; ++i) {
+    e->rho.push_back(d->weft_rho[i]);
+    e->ks.push_back(d->weft_Y[i] * ys::kPi * std::pow(d->R, 2));
+    e->kb.push_back(d->weft_B[i] * ys::kPi * std::pow(d->R, 2));
+  }
+  auto Z = [&](std::vector<double>& a, int c) { a.assign((size_t)c * N, 0.0); };
+  Z(e->X, 3); Z(e->V, 3); Z(e->XF, 3); Z(e->UV, 2); Z(e->UVD, 2); Z(e->UVB, 2); Z(e->UV0, 2); Z(e->NRM, 3);
+  Z(e->COMP, 1); Z(e->SLIDE, 2); Z(e->A, ys::YS_NUM_SLOTS); Z(e->B, 5); Z(e->CL, 3); Z(e->CLE, 6); Z(e->FE, 2);
+  Z(e->KEE, 2); Z(e->DEE, 2); Z(e->EXT, 5); Z(e->DINV, 5); Z(e->SOL, 5);
+  std::vector<uint8_t> fixed(N, 0);
+  for (int h = 0; h < d->n_handles; ++h) fixed[d->handles[2 * h] + d->handles[2 * h + 1] * W] = 1;
+  for (int j = 0; j < H; ++j)
+    for (int i = 0; i < W; ++i) {
+      const int n = i + j * W;
+      e->node_cloth.push_back(0); e->node_u.push_back(i); e->node_v.push_back(j);
+      const bool in = !(i == 0 || i == W - 1 || j == 0 || j == H - 1);
+      uint8_t f = in ? ys::YS_INTERIOR : 0;
+      if (in && flip_of(d->weave, i, j)) f |= ys::YS_FLIP;
+      if (fixed[n]) f |= ys::YS_FIXED;
+      e->flags.push_back(f);
+      double x[3];
+      if (d->pose == 0) { x[0] = i * d->L; x[1] = 0.0; x[2] = d->height - j * d->L; }
+      else { x[0] = i * d->L; x[1] = j * d->L; x[2] = d->height; }
+      for (int k = 0; k < 3; ++k) { e->X[k * N + n] = x[k]; e->XF[k * N + n] = x[k]; }
+      const double uv[2] = {i * d->L, j * d->L};
+      for (int k = 0; k < 2; ++k) { e->UV[k * N + n] = uv[k]; e->UVB[k * N + n] = uv[k]; e->UV0[k * N + n] = uv[k]; }
+    }
+  e->bind();
+  return e;
+}
+
+void emu_destroy(void* h) { delete static_cast<Emu*>(h); }
+
+void emu_set_state(void* h, const double* lpos, const double* lposfix, const double* lvel, const double* epos,
+                   const double* eposbar, const double* evel) {
+  Emu* e = static_cast<Emu*>(h);
+  const int N = e->N;
+  auto S = [&](const double* src, std::vector<double>& dst, int c) {
+    if (src) for (int i = 0; i < N; ++i) for (int k = 0; k < c; ++k) dst[k * N + i] = src[i * c + k];
+  };
+  S(lpos, e->X, 3); S(lposfix, e->XF, 3); S(lvel, e->V, 3); S(epos, e->UV, 2); S(eposbar, e->UVB, 2); S(evel, e->UVD, 2);
+}
+
+void emu_get_state(void* h, double* lpos, double* lposfix, double* lvel, double* epos, double* eposbar, double* evel) {
+  Emu* e = static_cast<Emu*>(h);
+  const int N = e->N;
+  auto G = [&](double* dst, const std::vector<double>& src, int c) {
+    if (dst) for (int i = 0; i < N; ++i) for (int k = 0; k < c; ++k) dst[i * c + k] = src[k * N + i];
+  };
+  G(lpos, e->X, 3); G(lposfix, e->XF, 3); G(lvel, e->V, 3); G(epos, e->UV, 2); G(eposbar, e->UVB, 2); G(evel, e->UVD, 2);
+}
+
+void emu_get_normals(void* h, double* nrm) {
+  Emu* e = static_cast<Emu*>(h);
+  for (int i = 0; i < e->N; ++i) for (int k = 0; k < 3; ++k) nrm[i * 3 + k] = e->NRM[k * e->N + i];
+}
+
+// same pass order as ys_assemble in csrc/ys_api.cu
+void emu_assemble(void* h, double dt, const double* ext /* [N][5] or null */) {
+  Emu* e = static_cast<Emu*>(h);
+  ys::View& v = e->v;
+  const int W = e->P.W, H = e->P.H, N = e->N;
+  v.h = dt;
+  v.ext = nullptr;
+  if (ext) {
+    for (int i = 0; i < N; ++i) for (int k = 0; k < 5; ++k) e->EXT[k * N + i] = ext[i * 5 + k];
+    v.ext = e->EXT.data();
+  }
+  for (int j = 1; j < H - 1; ++j) for (int i = 1; i < W - 1; ++i) ys::node_normal(v, i + j * W, W);
+  for (int n = 0; n < N; ++n) ys::clear_node(v, n);
+  for (int c = 0; c < 2; ++c)
+    for (int j = 0; j < H; ++j) for (int i = 0; i < W - 1; ++i) if ((i & 1) == c) {
+      ys::EdgeAcc a; const int n0 = i + j * W;
+      ys::edge_terms(v, n0, n0 + 1, 0, a); ys::edge_scatter(v, n0, n0 + 1, 0, a);
+    }
+  for (int c = 0; c < 2; ++c)
+    for (int j = 0; j < H - 1; ++j) for (int i = 0; i < W; ++i) if ((j & 1) == c) {
+      ys::EdgeAcc a; const int n0 = i + j * W;
+      ys::edge_terms(v, n0, n0 + W, 1, a); ys::edge_scatter(v, n0, n0 + W, 1, a);
+    }
+  for (int c = 0; c < 3; ++c)
+    for (int j = 0; j < H; ++j) for (int i = 1; i < W - 1; ++i) if (i % 3 == c) {
+      const int n0 = i + j * W; const double kb = e->kb[j];
+      ys::bend_element(v, n0 - 1, n0, n0 + 1, 0, kb); ys::crimp_element(v, n0 - 1, n0, n0 + 1, 0, kb);
+    }
+  for (int c = 0; c < 3; ++c)
+    for (int j = 1; j < H - 1; ++j) for (int i = 0; i < W; ++i) if (j % 3 == c) {
+      const int n0 = i + j * W; const double kb = e->kb[H + i];
+      ys::bend_element(v, n0 - W, n0, n0 + W, 1, kb); ys::crimp_element(v, n0 - W, n0, n0 + W, 1, kb);
+    }
+  for (int j = 0; j < H - 1; ++j) for (int i = 0; i < W - 1; ++i) {
+    const int tl = i + j * W, tr = tl + 1, bl = tl + W, br = tl + W + 1;
+    if (((i + j) & 1) == 0) { ys::wind_face(v, e->P, tl, tr, br); ys::wind_face(v, e->P, tl, br, bl); }
+    else { ys::wind_face(v, e->P, tl, tr, bl); ys::wind_face(v, e->P, tr, br, bl); }
+  }
+  for (int j = 1; j < H - 1; ++j) for (int i = 1; i < W - 1; ++i) ys::friction_node(v, i + j * W);
+  for (int j = 1; j < H - 1; ++j) for (int i = 1; i < W - 1; ++i) {
+    const int n = i + j * W;
+    ys::shear_element(v, e->P, n, n - 1, n + W, -1, 1);
+    ys::shear_element(v, e->P, n, n - 1, n - W, -1, -1);
+    ys::shear_element(v, e->P, n, n + 1, n + W, 1, 1);
+    ys::shear_element(v, e->P, n, n + 1, n - W, 1, -1);
+  }
+  e->bad = 0;
+  for (int n = 0; n < N; ++n) if (!ys::finalize_node(v, n, e->DINV.data())) e->bad = 1;
+}
+
+// raw slots [159][N] and rhs [5][N]
+void emu_raw(void* h, double* slots, double* rhs) {
+  Emu* e = static_cast<Emu*>(h);
+  if (slots) std::memcpy(slots, e->A.data(), sizeof(double) * e->A.size());
+  if (rhs) std::memcpy(rhs, e->B.data(), sizeof(double) * e->B.size());
+}
+
+// Jacobi-PCG on the structured system (Eigen ConjugateGradient algorithm);
+// returns iterations, writes the relative residual.
+long emu_solve(void* h, double tol, long maxiter, double* err) {
+  Emu* e = static_cast<Emu*>(h);
+  ys::View& v = e->v;
+  const int N = e->N;
+  std::vector<double> r(5 * N), p(5 * N), q(5 * N), z(5 * N);
+  double* x = e->SOL.data();
+  if (tol <= 0) tol = DBL_EPSILON;
+  const long dim = 3L * N + 2L * (e->P.W - 2) * (e->P.H - 2);
+  if (maxiter < 0) maxiter = 2 * dim;
+  double bb = 0, rr = 0, rz = 0;
+  for (int i = 0; i < 5 * N; ++i) {
+    x[i] = 0; r[i] = e->B[i]; z[i] = e->DINV[i] * r[i]; p[i] = z[i];
+    bb += r[i] * r[i]; rz += r[i] * z[i];
+  }
+  rr = bb;
+  long it = 0;
+  double thr = std::max(tol * tol * bb, DBL_MIN);
+  if (bb == 0 || rr < thr) { *err = bb > 0 ? std::sqrt(rr / bb) : 0; return 0; }
+  while (it < maxiter) {
+    double pq = 0;
+    for (int n = 0; n < N; ++n) {
+      double y[5];
+      ys::spmv_row(v, p.data(), n, y);
+      for (int k = 0; k < 5; ++k) { q[k * N + n] = y[k]; pq += p[k * N + n] * y[k]; }
+    }
+    const double alpha = rz / pq;
+    rr = 0;
+    double rzn = 0;
+    for (int i = 0; i < 5 * N; ++i) {
+      x[i] += alpha * p[i]; r[i] -= alpha * q[i]; rr += r[i] * r[i]; z[i] = e->DINV[i] * r[i]; rzn += r[i] * z[i];
+    }
+    if (rr < thr) break;
+    const double beta = rzn / rz;
+    rz = rzn;
+    for (int i = 0; i < 5 * N; ++i) p[i] = z[i] + beta * p[i];
+    ++it;
+  }
+  *err = std::sqrt(rr / bb);
+  return it;
+}
+
+void emu_apply(void* h, const double* xin /* [5][N] */, double* yout /* [5][N] */) {
+  Emu* e = static_cast<Emu*>(h);
+  for (int n = 0; n < e->N; ++n) {
+    double y[5];
+    ys::spmv_row(e->v, xin, n, y);
+    for (int k = 0; k < 5; ++k) yout[k * e->N + n] = y[k];
+  }
+}
+
+int emu_update(void* h) {
+  Emu* e = static_cast<Emu*>(h);
+  if (e->bad) return 1;
+  for (double s : e->SOL) if (!std::isfinite(s)) return 1;
+  for (int n = 0; n < e->N; ++n) ys::update_node(e->v, e->SOL.data(), n);
+  return 0;
+}
+
+}  // extern "C"
