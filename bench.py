@@ -1,0 +1,376 @@
+#!/usr/bin/env python
+"""Batched yarn-level cloth stepping on GB300: one JSON line.
+
+Workload (the batched-cloth benchmark): 256 plain-weave cloths with side
+lengths drawn uniformly from 5..50 crossings (seeded), hanging from their two
+top corners, per-yarn-line material drawn within +-20% of rho = 1e-3 kg/m,
+Y = 1e3, B = 1e-5 (the reference's Yarn(R, rho, Y, B) arguments, R = 0.1 mm,
+L = 1 mm), S = 1e-4 and mu = 0.3 within +-20% per cloth, gravity 9.8, seeded
+sinusoidal wind (pressure amplitude 0..2 N/m^2 -> speed sqrt(p / rho_air),
+period 0.2..1 s), h = 1e-3 s, FP64 Jacobi-PCG to relative residual 1e-10.
+A step advances every cloth of the batch by h. Inputs are synthetic.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host cores (the C
+restatement in oracle/, as the reference's own LibTorch build does not run on
+the GPU host) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+H = 1e-3
+TOL = 1e-10
+N_CLOTHS = 256
+WIND_RHO = 1.0
+WIND_DRAG = 0.5
+
+
+# ---------------------------------------------------------------- workload
+def workload(seed: int, n_cloths: int = N_CLOTHS):
+    """Seeded cloth descriptions (dicts of ClothSpec fields) and wind table."""
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(5, 51, size=n_cloths)
+    base = np.array([1e-3, 1e3, 1e-5])
+    specs, wind = [], []
+    for s in sides:
+        W = Hh = int(s)
+        j = lambda n: base * (1.0 + 0.2 * (2.0 * rng.random((n, 3)) - 1.0))
+        specs.append(dict(width=W, length=Hh, warp=j(Hh), weft=j(W), height=0.05, L=1e-3, R=1e-4, pose=0, weave=0,
+                          kc=1.0, kf=1000.0, df=1000.0, mu=0.3 * (1 + 0.2 * (2 * rng.random() - 1)),
+                          S=1e-4 * (1 + 0.2 * (2 * rng.random() - 1)), handle_stiffness=1e4, G=(0.0, 0.0, 9.8),
+                          wind_vel=(0.0, 0.0, 0.0), wind_density=WIND_RHO, wind_drag=WIND_DRAG,
+                          handles=[(0, 0), (W - 1, 0)]))
+        wind.append((2.0 * rng.random(), 0.2 + 0.8 * rng.random(), 2 * math.pi * rng.random()))
+    return specs, np.array(wind)
+
+
+def wind_at(wind, step):
+    """[n, 3] wind velocity at time step*h: along +y (normal to the hanging cloth)."""
+    t = step * H
+    amp = np.sqrt(wind[:, 0] / WIND_RHO)
+    v = np.zeros((len(wind), 3))
+    v[:, 1] = amp * np.sin(2 * math.pi * t / wind[:, 1] + wind[:, 2])
+    return v
+
+
+# ---------------------------------------------------------------- helpers
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 9 for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def measure_fp64_peak(torch):
+    """cuBLAS DGEMM throughput (TFLOP/s): the FP64 ceiling of this GPU."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 1e30
+    for _ in range(3):
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+# ---------------------------------------------------------------- CPU arm
+def _cpu_worker(args):
+    specs, idx, steps, seed = args
+    from oracle.oracle import ClothSpec, OracleCloth
+    _, wind = workload(seed)
+    cloths = [OracleCloth(ClothSpec(**specs[i])) for i in idx]
+    t0 = time.perf_counter()
+    for s in range(steps):
+        wv = wind_at(wind, s)
+        for c, i in zip(cloths, idx):
+            c.set_wind(wv[i])
+            c.step(H, cg_tol=TOL)
+    return time.perf_counter() - t0
+
+
+def cpu_sample(specs, seed, target_nodes, steps, cores):
+    """Times the oracle on a bounded sample of the workload's cloths; returns
+    (batch steps/s extrapolated to the full batch, description)."""
+    import multiprocessing as mp
+    from oracle.oracle import build as build_oracle
+    build_oracle()
+    order = np.random.default_rng(seed + 99).permutation(len(specs))
+    idx, nodes = [], 0
+    for i in order:
+        if nodes >= target_nodes:
+            break
+        idx.append(int(i))
+        nodes += specs[i]["width"] * specs[i]["length"]
+    total = sum(s["width"] * s["length"] for s in specs)
+    # balance the sample over the workers by node count
+    shards = [[] for _ in range(cores)]
+    load = [0] * cores
+    for i in sorted(idx, key=lambda i: -specs[i]["width"] * specs[i]["length"]):
+        k = int(np.argmin(load))
+        shards[k].append(i)
+        load[k] += specs[i]["width"] * specs[i]["length"]
+    shards = [s for s in shards if s]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(len(shards)) as pool:
+        times = pool.map(_cpu_worker, [(specs, s, steps, seed) for s in shards])
+    wall = max(times)  # each worker times its own stepping loop (process start-up excluded)
+    per_step = wall / steps
+    value = (nodes / total) / per_step
+    desc = "%d of %d cloths (%d of %d nodes), %d step(s), %d processes; slowest worker's loop time" % (
+        len(idx), len(specs), nodes, total, steps, len(shards))
+    return value, desc, wall
+
+
+# ---------------------------------------------------------------- main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cloths", type=int, default=N_CLOTHS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="print the per-kernel table to stderr")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    seed = args.seed + 1000 * rank  # each rank steps its own batch (weak scaling)
+    specs, wind = workload(seed, args.cloths)
+    total_nodes = sum(s["width"] * s["length"] for s in specs)
+    config = {"workload": "batched hanging plain-weave cloths, sides U{5..50}, seeded material and wind",
+              "cloths_per_gpu": args.cloths, "nodes_per_gpu": int(total_nodes), "h": H, "pcg_rtol": TOL,
+              "precision": "fp64", "seed": args.seed,
+              "l2": "working set (A alone %.0f MB) exceeds the 129 MB L2; no flush between steps" %
+                    (159 * 8 * total_nodes / 1e6)}
+    metric = "batch steps/s (%d cloths advanced by h per step)" % args.cloths
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        cores = os.cpu_count() or 1
+        steps = 1
+        value, desc, wall = cpu_sample(specs, seed, target_nodes=total_nodes, steps=1, cores=cores)
+        line = {"impl": "reference", "metric": metric, "value": value, "unit": "steps/s", "n_gpus": 0,
+                "steps": steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
+                                 "sample": desc},
+                "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    import importlib
+    ys = importlib.import_module("fine-grained-differentiable-physics-a-yarn-level-model-for-fabrics_gb300")
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    dev = local_rank
+    torch.cuda.set_device(dev)
+
+    batch = ys.ClothBatch([ys.ClothSpec(**s) for s in specs], device=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    step_no = 0
+    iters = []
+
+    def do_step():
+        nonlocal step_no
+        batch.set_winds(wind_at(wind, step_no))
+        st = batch.step(H, tol=TOL)
+        step_no += 1
+        return st
+
+    for _ in range(args.warmup):
+        st = do_step()
+    assert all(s["ok"] for s in st), "warm-up step failed"
+    torch.cuda.synchronize()
+    batch.profile_read(reset=True)
+
+    # ---- timed region: device-resident state
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            st = do_step()
+            iters.append(max(s["cg_iterations"] for s in st))
+        e1.record()
+        torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    launches = batch.profile_read(reset=True)["total_launches"]
+    ok = all(s["ok"] for s in st)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * args.steps / (ms / 1e3)
+
+    # ---- end to end through the public API with host buffers
+    host = {k: torch.zeros((total_nodes, 3 if k.startswith("L") else 2), dtype=torch.float64).pin_memory()
+            for k in ("LPos", "LPosFix", "LVel", "EPos", "EPosBar", "EVel")}
+    hn = {k: v.numpy() for k, v in host.items()}
+    batch.get_state(out=hn)
+    e2e_steps = max(3, args.steps // 2)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        batch.set_state(**hn)
+        do_step()
+        batch.get_state(out=hn)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    state_bytes = total_nodes * 15 * 8
+    e2e = {"value": world * e2e_steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": state_bytes + 24 * args.cloths,
+           "d2h_bytes_per_step": state_bytes}
+
+    # ---- per-kernel profile (a second pass of the same steps, events per launch)
+    batch.profile(True)
+    for _ in range(max(3, args.steps // 4)):
+        do_step()
+    batch.profile(False)
+    prof = batch.profile_read(reset=True)
+    tot_ms = sum(prof["ms"].values())
+    share = {k: v / tot_ms for k, v in prof["ms"].items() if v > 0}
+    dominant = max(prof["ms"], key=lambda k: prof["ms"][k])
+    # algorithmic bytes / flops per launch of the main kernels
+    n = total_nodes
+    alg = {
+        # 159 coefficients + own p read + q write per node
+        "spmv": dict(bytes=n * (159 * 8 + 5 * 8 + 5 * 8), flops=n * (2 * 159 + 10)),
+        # x, p, r, q, dinv read; x, r written
+        "axpy": dict(bytes=n * (5 * 5 * 8 + 2 * 5 * 8), flops=n * 5 * 8),
+        "dir": dict(bytes=n * (3 * 5 * 8 + 5 * 8), flops=n * 5 * 3),
+        "clear": dict(bytes=n * (159 + 5 + 3 + 6 + 6) * 8, flops=0),
+    }
+    hbm_peak, peak_kind = peaks()
+    fp64_peak = measure_fp64_peak(torch)
+
+    def roof(kname):
+        if prof["launches"].get(kname, 0) == 0 or kname not in alg:
+            return None
+        per = prof["ms"][kname] / prof["launches"][kname] * 1e-3
+        a = alg[kname]
+        return dict(gbs=a["bytes"] / per / 1e9, tflops=a["flops"] / per / 1e12, us=per * 1e6)
+
+    spmv = roof("spmv")
+    roofline = None
+    if spmv:
+        roofline = {"kernel": "k_pcg_spmv (stencil SpMV, 159 FP64 coefficients per node)", "bound": "hbm",
+                    "achieved": spmv["gbs"], "peak": hbm_peak, "unit": "GB/s", "frac": spmv["gbs"] / hbm_peak,
+                    "peak_source": peak_kind, "traffic": None,
+                    "fp64": {"achieved_tflops": spmv["tflops"], "dgemm_tflops": fp64_peak,
+                             "frac": spmv["tflops"] / fp64_peak},
+                    "us_per_launch": spmv["us"],
+                    "dominant_kernel_by_time": dominant, "time_share": share}
+
+    line = {"metric": metric, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+            "cloth_steps_per_s": value * args.cloths, "pcg_iterations_per_step": statistics.mean(iters),
+            "all_cloths_ok": ok, "gpu_launches": int(launches), "e2e": e2e, "roofline": roofline,
+            "clocks": clk.summary()}
+
+    if rank == 0 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        v, desc, wall = cpu_sample(specs, seed, target_nodes=total_nodes, steps=1, cores=cores)
+        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": desc}
+    if args.profile and rank == 0:
+        for k in prof["ms"]:
+            if prof["launches"][k]:
+                print("%-10s %8.3f ms  %6d launches  %5.1f%%" % (k, prof["ms"][k], prof["launches"][k],
+                                                               100 * prof["ms"][k] / tot_ms), file=sys.stderr)
+    batch.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

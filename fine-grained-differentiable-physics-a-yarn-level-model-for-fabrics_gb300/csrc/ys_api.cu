@@ -91,6 +91,45 @@ struct ys_batch {
   int* h_nactive = nullptr; // pinned
   bool assembled = false;
   int max_maxiter = 0;
+  // launch accounting and optional per-kernel-class event timing
+  int64_t launches = 0;
+  bool profiling = false;
+  struct Rec { int kind; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> pool;
+  double prof_ms[YS_PROF_KINDS] = {0};
+  int64_t prof_n[YS_PROF_KINDS] = {0};
+
+  cudaEvent_t ev() {
+    if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+  // runs one launcher; `kernels` = kernels it launches
+  template <class F>
+  void run(int kind, int kernels, F&& f) {
+    launches += kernels;
+    if (!profiling) { f(); return; }
+    Rec r{kind, ev(), ev()};
+    cudaEventRecord(r.a, stream);
+    f();
+    cudaEventRecord(r.b, stream);
+    recs.push_back(r);
+  }
+  void drain() {
+    if (recs.empty()) return;
+    cudaStreamSynchronize(stream);
+    for (Rec& r : recs) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, r.a, r.b);
+      prof_ms[r.kind] += ms;
+      prof_n[r.kind] += 1;
+      pool.push_back(r.a);
+      pool.push_back(r.b);
+    }
+    recs.clear();
+  }
 
   template <class T>
   ys_status alloc(T** p, size_t count) {
@@ -104,6 +143,8 @@ struct ys_batch {
     return YS_OK;
   }
   ~ys_batch() {
+    drain();
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
     if (h_nactive) cudaFreeHost(h_nactive);
   }
@@ -119,6 +160,7 @@ ys_status upload_soa(ys_batch* b, const double* src, double* dst, int c, int32_t
     YS_CUDA(cudaMemcpyAsync(b->stage, src, sizeof(double) * n * c, cudaMemcpyHostToDevice, b->stream));
     d_src = b->stage;
   }
+  b->launches += 1;
   k_to_soa<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(d_src, dst, n, c);
   YS_CUDA(cudaGetLastError());
   if (!(flags & YS_ON_DEVICE)) YS_CUDA(cudaStreamSynchronize(b->stream));  // stage is reused
@@ -129,6 +171,7 @@ ys_status download_aos(ys_batch* b, const double* src, double* dst, int c, int32
   const int64_t n = b->ntot;
   if (!dst) return YS_OK;
   double* d_dst = (flags & YS_ON_DEVICE) ? dst : b->stage;
+  b->launches += 1;
   k_to_aos<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(src, d_dst, n, c);
   YS_CUDA(cudaGetLastError());
   if (!(flags & YS_ON_DEVICE)) {
@@ -418,6 +461,32 @@ ys_status ys_set_wind(ys_batch* b, int32_t cloth, const double wind_vel[3]) {
   return YS_OK;
 }
 
+namespace {
+__global__ void k_set_winds(ys::ClothParams* cp, const double* __restrict__ w, int ncloth) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncloth)
+    for (int k = 0; k < 3; ++k) cp[c].wind[k] = w[3 * c + k];
+}
+}  // namespace
+
+ys_status ys_set_winds(ys_batch* b, const double* wind_vel, int32_t flags) {
+  if (!b || !wind_vel) return fail(YS_ERR_ARG, "bad argument");
+  YS_CUDA(cudaSetDevice(b->device));
+  const double* src = wind_vel;
+  if (!(flags & YS_ON_DEVICE)) {
+    YS_CUDA(cudaMemcpyAsync(b->stage, wind_vel, sizeof(double) * 3 * b->ncloth, cudaMemcpyHostToDevice, b->stream));
+    src = b->stage;
+  }
+  b->launches += 1;
+  k_set_winds<<<(b->ncloth + 127) / 128, 128, 0, b->stream>>>(const_cast<ys::ClothParams*>(b->v.cp), src,
+                                                                 b->ncloth);
+  YS_CUDA(cudaGetLastError());
+  if (!(flags & YS_ON_DEVICE)) YS_CUDA(cudaStreamSynchronize(b->stream));
+  for (int c = 0; c < b->ncloth; ++c)
+    for (int k = 0; k < 3; ++k) b->cp[c].wind[k] = wind_vel == src ? b->cp[c].wind[k] : wind_vel[3 * c + k];
+  return YS_OK;
+}
+
 ys_status ys_assemble(ys_batch* b, double h, const double* ext_force, int32_t flags) {
   if (!b || !(h > 0)) return fail(YS_ERR_ARG, "bad argument");
   YS_CUDA(cudaSetDevice(b->device));
@@ -430,27 +499,29 @@ ys_status ys_assemble(ys_batch* b, double h, const double* ext_force, int32_t fl
   }
   cudaStream_t s = b->stream;
   const ys::View& v = b->v;
-  k_reset_status<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->ncloth);
+  b->run(YS_PROF_MISC, 1, [&] { k_reset_status<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->ncloth); });
   // UpdateClothUnits normals for the current positions (src/Cloth.cpp:307-327)
-  ys::launch_geom(v, b->anchors + b->geom_off, b->geom_n, s);
-  ys::launch_clear(v, s);
+  if (b->geom_n) b->run(YS_PROF_GEOM, 1, [&] { ys::launch_geom(v, b->anchors + b->geom_off, b->geom_n, s); });
+  b->run(YS_PROF_CLEAR, 1, [&] { ys::launch_clear(v, s); });
   bool friction_done = false;
   for (const Pass& p : b->passes) {
     const int* a = b->anchors + p.off;
     if (p.kind == 3 && !friction_done) {
       // ConSlideFriction needs every edge and bend term; shear needs its
       // compression (src/PhysicsCloth.cpp:97-131)
-      ys::launch_friction(v, b->anchors + b->geom_off, b->geom_n, s);
+      if (b->geom_n)
+        b->run(YS_PROF_FRICTION, 1, [&] { ys::launch_friction(v, b->anchors + b->geom_off, b->geom_n, s); });
       friction_done = true;
     }
+    if (p.n == 0) continue;
     switch (p.kind) {
-      case 0: ys::launch_edges(v, a, p.n, p.k, s); break;
-      case 1: ys::launch_bends(v, a, p.n, p.k, s); break;
-      case 2: ys::launch_faces(v, a, p.n, s); break;
-      case 3: ys::launch_shear(v, a, p.n, s); break;
+      case 0: b->run(YS_PROF_EDGES, 1, [&] { ys::launch_edges(v, a, p.n, p.k, s); }); break;
+      case 1: b->run(YS_PROF_BENDS, 1, [&] { ys::launch_bends(v, a, p.n, p.k, s); }); break;
+      case 2: b->run(YS_PROF_FACES, 1, [&] { ys::launch_faces(v, a, p.n, s); }); break;
+      case 3: b->run(YS_PROF_SHEAR, 1, [&] { ys::launch_shear(v, a, p.n, s); }); break;
     }
   }
-  ys::launch_finalize(v, b->blk, b->so, s);
+  b->run(YS_PROF_FINALIZE, 1, [&] { ys::launch_finalize(v, b->blk, b->so, s); });
   YS_CUDA(cudaGetLastError());
   b->assembled = true;
   return YS_OK;
@@ -465,14 +536,20 @@ ys_status ys_solve(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* stats
   const int override_max = (opts && opts->maxiter >= 0) ? opts->maxiter : -1;
   const int every = (opts && opts->check_every > 0) ? opts->check_every : 16;
   const int cap = override_max >= 0 ? override_max : b->max_maxiter;
-  k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
+  b->run(YS_PROF_MISC, 1, [&] {
+    k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
+  });
   YS_CUDA(cudaGetLastError());
-  ys::launch_pcg_setup(b->v, b->blk, b->so, s);
+  b->run(YS_PROF_PCG_SETUP, 2, [&] { ys::launch_pcg_setup(b->v, b->blk, b->so, s); });
   int it = 0;
   while (it < cap) {
     const int n = std::min(every, cap - it);
-    for (int q = 0; q < n; ++q, ++it) ys::launch_pcg_iter(b->v, b->blk, b->so, it, s);
-    ys::launch_count_active(b->v, b->so, s);
+    for (int q = 0; q < n; ++q, ++it) {
+      b->run(YS_PROF_SPMV, 1, [&] { ys::launch_pcg_spmv(b->v, b->blk, b->so, s); });
+      b->run(YS_PROF_AXPY, 1, [&] { ys::launch_pcg_axpy(b->v, b->blk, b->so, it, s); });
+      b->run(YS_PROF_DIR, 1, [&] { ys::launch_pcg_dir(b->v, b->blk, b->so, it, s); });
+    }
+    b->run(YS_PROF_MISC, 1, [&] { ys::launch_count_active(b->v, b->so, s); });
     YS_CUDA(cudaMemcpyAsync(b->h_nactive, b->so.nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
     YS_CUDA(cudaStreamSynchronize(s));
     if (*b->h_nactive == 0) break;
@@ -513,7 +590,7 @@ ys_status ys_step(ys_batch* b, double h, const double* ext_force, int32_t flags,
   }
   ys_status sol = ys_solve(b, opts, st);
   if (sol == YS_ERR_ARG || sol == YS_ERR_CUDA) return sol;
-  ys::launch_update(b->v, b->blk, b->so, b->stream);
+  b->run(YS_PROF_UPDATE, 2, [&] { ys::launch_update(b->v, b->blk, b->so, b->stream); });
   YS_CUDA(cudaGetLastError());
   // the solution check may have flagged more cloths
   std::vector<ys::PcgCloth> pc(b->ncloth);
@@ -534,7 +611,7 @@ ys_status ys_apply_system(ys_batch* b, const double* x, double* y, int32_t flags
   YS_CUDA(cudaSetDevice(b->device));
   ys_status s = upload_soa(b, x, b->so.q, 5, flags);
   if (s != YS_OK) return s;
-  ys::launch_spmv(b->v, b->so.q, b->so.r, b->stream);
+  b->run(YS_PROF_SPMV, 1, [&] { ys::launch_spmv(b->v, b->so.q, b->so.r, b->stream); });
   YS_CUDA(cudaGetLastError());
   return download_aos(b, b->so.r, y, 5, flags);
 }
@@ -592,6 +669,31 @@ ys_status ys_export_system(ys_batch* b, int32_t cloth, double* Aout, double* rhs
         Aout[(er + k) * dim + ej + k] = S(ys::YS_SLOT_EE_NBR + m, n);
       }
     }
+  return YS_OK;
+}
+
+ys_status ys_profile(ys_batch* b, int32_t enable) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  YS_CUDA(cudaSetDevice(b->device));
+  b->drain();
+  b->profiling = enable != 0;
+  return YS_OK;
+}
+
+ys_status ys_profile_read(ys_batch* b, double* ms, int64_t* launches_per_kind, int64_t* total_launches,
+                          int32_t reset) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  YS_CUDA(cudaSetDevice(b->device));
+  b->drain();
+  for (int k = 0; k < YS_PROF_KINDS; ++k) {
+    if (ms) ms[k] = b->prof_ms[k];
+    if (launches_per_kind) launches_per_kind[k] = b->prof_n[k];
+  }
+  if (total_launches) *total_launches = b->launches;
+  if (reset) {
+    for (int k = 0; k < YS_PROF_KINDS; ++k) { b->prof_ms[k] = 0; b->prof_n[k] = 0; }
+    b->launches = 0;
+  }
   return YS_OK;
 }
 

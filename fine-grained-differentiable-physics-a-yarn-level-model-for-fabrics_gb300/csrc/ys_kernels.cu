@@ -314,11 +314,14 @@ void launch_pcg_setup(const View& v, const Blocks& b, const Solver& so, cudaStre
   k_pcg_setup<<<b.nblk, kBlock, 0, s>>>(v, b, so);
   k_pcg_start<<<(v.ncloth + 127) / 128, 128, 0, s>>>(b, so, v.ncloth);
 }
-void launch_pcg_iter(const View& v, const Blocks& b, const Solver& so, int it, cudaStream_t s) {
-  const int parity = it & 1;
+void launch_pcg_spmv(const View& v, const Blocks& b, const Solver& so, cudaStream_t s) {
   k_pcg_spmv<<<b.nblk, kBlock, 0, s>>>(v, b, so);
-  k_pcg_axpy<<<b.nblk, kBlock, 0, s>>>(v, b, so, parity);
-  k_pcg_dir<<<b.nblk, kBlock, 0, s>>>(v, b, so, parity, it);
+}
+void launch_pcg_axpy(const View& v, const Blocks& b, const Solver& so, int it, cudaStream_t s) {
+  k_pcg_axpy<<<b.nblk, kBlock, 0, s>>>(v, b, so, it & 1);
+}
+void launch_pcg_dir(const View& v, const Blocks& b, const Solver& so, int it, cudaStream_t s) {
+  k_pcg_dir<<<b.nblk, kBlock, 0, s>>>(v, b, so, it & 1, it);
 }
 void launch_count_active(const View& v, const Solver& so, cudaStream_t s) {
   k_count_active<<<1, 256, 0, s>>>(so, v.ncloth);

@@ -53,7 +53,9 @@ void launch_friction(const View& v, const int* nodes, int n, cudaStream_t s);
 void launch_shear(const View& v, const int* anchors, int n, cudaStream_t s);
 void launch_finalize(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
 void launch_pcg_setup(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
-void launch_pcg_iter(const View& v, const Blocks& b, const Solver& so, int it, cudaStream_t s);
+void launch_pcg_spmv(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
+void launch_pcg_axpy(const View& v, const Blocks& b, const Solver& so, int it, cudaStream_t s);
+void launch_pcg_dir(const View& v, const Blocks& b, const Solver& so, int it, cudaStream_t s);
 void launch_count_active(const View& v, const Solver& so, cudaStream_t s);
 void launch_update(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
 void launch_spmv(const View& v, const double* x, double* y, cudaStream_t s);

@@ -56,6 +56,7 @@ YS_HD double& st(double* p, int comp, int ntot, int node) { return p[(int64_t)co
 YS_HD void add_A(const View& v, int rn, int rc, int cn, int cc, int k, double val, int du, int dv) {
   if (rc < 3 && cc < 3) {
     int s = stencil_index(du, dv);
+    if (s < 0) return;  // not reachable for the element types above; keeps every store in bounds
     slot(v, YS_SLOT_LL + s * 9 + rc * 3 + cc, rn) += val;
   } else if (rc < 3) {
     int n = yarn_nbr(du, dv);
@@ -605,6 +606,7 @@ YS_HD void bend_terms(const BendGeom& g, double kb, BendTerms& t) {
 // To_Sparse_Mat) for a node-node coupling at grid offset (du, dv).
 YS_HD void add_K_LL(const View& v, int rn, int du, int dv, const double blk[3][3], double s) {
   const int sidx = stencil_index(du, dv);
+  if (sidx < 0) return;  // not reachable for bend and shear offsets; keeps every store in bounds
   const double mh2 = -(v.h * v.h);
   for (int r = 0; r < 3; ++r)
     for (int c = 0; c < 3; ++c) slot(v, YS_SLOT_LL + sidx * 9 + r * 3 + c, rn) += mh2 * (s * blk[c][r]);

@@ -15,7 +15,7 @@
  *                     src/Environment.h:16-21; src/PhysicsCloth.cpp:3-44)
  *   ys_set_state      Cloth::set_ClothState        (src/Cloth.cpp:421-438)
  *   ys_get_state      Cloth::get_ClothState        (src/Cloth.cpp:350-371)
- *   ys_set_wind       Environment::wind            (src/Wind.h:6-17)
+ *   ys_set_wind(s)    Environment::wind            (src/Wind.h:6-17)
  *   ys_assemble       PhysicsCloth::FillMV + the A, b formation of SimStep
  *                     (src/PhysicsCloth.cpp:46-156; src/TrainHelper.cpp:19-20)
  *   ys_export_system  PhysicsCloth::get_SpaM/get_SpaFPos/get_SpaFVel/get_SpaF
@@ -113,6 +113,8 @@ ys_status ys_set_state(ys_batch *b, const double *lpos, const double *lposfix, c
 ys_status ys_get_state(ys_batch *b, double *lpos, double *lposfix, double *lvel, double *epos, double *eposbar,
                        double *evel, int32_t flags);
 ys_status ys_set_wind(ys_batch *b, int32_t cloth, const double wind_vel[3]);
+/* Wind velocity of every cloth at once: [n_cloths][3] (one copy). */
+ys_status ys_set_winds(ys_batch *b, const double *wind_vel, int32_t flags);
 
 /* FillMV + A, b for step size h; ext_force: NULL or [total_nodes][5] (node
  * layout x, y, z, u, v; the u, v entries of boundary nodes are ignored). */
@@ -132,6 +134,33 @@ ys_status ys_step(ys_batch *b, double h, const double *ext_force, int32_t flags,
 ys_status ys_apply_system(ys_batch *b, const double *x, double *y, int32_t flags);
 /* Waits for the handle's stream. */
 ys_status ys_synchronize(ys_batch *b);
+
+/* Kernel accounting (no counterpart in the reference). Kernel classes: */
+enum {
+  YS_PROF_GEOM = 0,      /* node normals */
+  YS_PROF_CLEAR = 1,     /* zero the step's system */
+  YS_PROF_EDGES = 2,     /* edge terms (mass, gravity, stretch, inertia, dM/dt, contact) */
+  YS_PROF_BENDS = 3,     /* bending + crimp */
+  YS_PROF_FACES = 4,     /* wind */
+  YS_PROF_FRICTION = 5,  /* sliding friction */
+  YS_PROF_SHEAR = 6,     /* shear (with jamming) */
+  YS_PROF_FINALIZE = 7,  /* handles, external force, Jacobi diagonal, finite check */
+  YS_PROF_PCG_SETUP = 8,
+  YS_PROF_SPMV = 9,      /* stencil SpMV q = A p (+ p.q) */
+  YS_PROF_AXPY = 10,     /* x, r update (+ r.r, r.z) */
+  YS_PROF_DIR = 11,      /* stop test, p update */
+  YS_PROF_UPDATE = 12,   /* Cloth::update */
+  YS_PROF_MISC = 13,     /* bookkeeping */
+  YS_PROF_KINDS = 14
+};
+/* enable = 1 brackets every launch with CUDA events on the handle's stream
+ * (adds a little host overhead); the totals accumulate until read. */
+ys_status ys_profile(ys_batch *b, int32_t enable);
+/* ms[YS_PROF_KINDS] summed event time, launches_per_kind[YS_PROF_KINDS] timed
+ * launches, total_launches = every kernel launched by the handle (timed or
+ * not) since the last reset. Any pointer may be NULL. */
+ys_status ys_profile_read(ys_batch *b, double *ms, int64_t *launches_per_kind, int64_t *total_launches,
+                          int32_t reset);
 
 #ifdef __cplusplus
 }
