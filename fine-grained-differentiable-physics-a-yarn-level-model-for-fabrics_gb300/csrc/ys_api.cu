@@ -234,6 +234,8 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
     P.jam = 2.0 * std::asin(d.R / d.L);  // src/Cloth.cpp:29
     for (int k = 0; k < 3; ++k) { P.G[k] = d.G[k]; P.wind[k] = d.wind_vel[k]; }
     P.wind_rho = d.wind_density; P.wind_drag = d.wind_drag;
+    P.pb4 = std::pow(ys::kPi / 2, 4);
+    P.pb5 = std::pow(ys::kPi / 2, 5);
     b->cp.push_back(P);
     for (int i = 0; i < d.length; ++i) {
       rho.push_back(d.warp_rho[i]);

@@ -86,6 +86,7 @@ struct ClothParams {
   double G[3];
   double wind[3];
   double wind_rho, wind_drag;
+  double pb4, pb5;  // (PI/2)^4 and (PI/2)^5 as std::pow gives them (src/PhysicsCloth.cpp:2680-2681)
 };
 
 // Device view of a batch (trivially copyable; passed by value to kernels).

@@ -761,11 +761,14 @@ YS_HD void sym3_min_eigvec(const double S[3][3], double* out) {
   double a[3][3], V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) a[i][j] = S[i][j];
+  // off-diagonal entries below 1e-24 of the diagonal scale move the
+  // eigenvectors by less than 1e-24 and are treated as zero
+  const double tiny = 1e-24 * (fabs(S[0][0]) + fabs(S[1][1]) + fabs(S[2][2]));
   for (int sweep = 0; sweep < 50; ++sweep) {
-    if (fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]) == 0.0) break;
+    if (fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]) <= tiny) break;
     for (int p = 0; p < 2; ++p)
       for (int q = p + 1; q < 3; ++q) {
-        if (a[p][q] == 0.0) continue;
+        if (fabs(a[p][q]) <= tiny) continue;
         const double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
         const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
         const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
@@ -908,136 +911,103 @@ YS_HD void shear_element(const View& v, const ClothParams& P, int n0, int n1, in
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) J31[i][j] *= k31;
   } else {
-    // jamming: smooth shear lock (src/PhysicsCloth.cpp:2656-2713, 2753-3031)
+    // jamming: smooth shear lock (src/PhysicsCloth.cpp:2656-2713, 2753-3031).
+    // Every first derivative in those expressions is a multiple of
+    // phi_x = -P d / (l sin phi) -- phi_s_x = sigma phi_x, con_func_x_x =
+    // mu phi_x, gamma_x = kappa phi_x -- except kx_x, whose "1 - cf^2 cfx"
+    // broadcasts a scalar 1 and so equals beta0 (1,1,1) + beta1 phi_x. With
+    // the scalars below each Hessian entry is a short combination of rank-1
+    // products; the arithmetic is the reference's, regrouped.
     const double pb = kPi / 2, pl = P.jam, sig = 0.6;
     const double cc = 3.0;
     const double LR = Lc / R;
+    const double rl1s = 1.0 / (l1 * s), rl3s = 1.0 / (l3 * s);
     double px1[3], px3[3];
-    for (int i = 0; i < 3; ++i) { px1[i] = -a3[i] / (l1 * s); px3[i] = -a1[i] / (l3 * s); }
+    for (int i = 0; i < 3; ++i) { px1[i] = -a3[i] * rl1s; px3[i] = -a1[i] * rl3s; }
     const double gamma = (Lc * sqrt(2.0) - 2 * Lc * sin(0.5 * phi)) / R;
     const double sh = sin(0.5 * phi), ch = cos(0.5 * phi);
-    double gx1[3], gx3[3];
-    for (int i = 0; i < 3; ++i) { gx1[i] = -LR * ch * px1[i]; gx3[i] = -LR * ch * px3[i]; }
+    const double kap = -LR * ch;                       // gamma_x = kap * phi_x
     const double Aq = phi - pl, Bq = phi - pb;
     const double phs = phi * Aq * Bq;
-    double phs1[3], phs3[3];
-    for (int i = 0; i < 3; ++i) {
-      phs1[i] = px1[i] * Aq * Bq + phi * px1[i] * Bq + phi * Aq * px1[i];
-      phs3[i] = px3[i] * Aq * Bq + phi * px3[i] * Bq + phi * Aq * px3[i];
-    }
-    const double pb5 = pow(pb, 5), pb4 = pow(pb, 4);
+    const double sgm = Aq * Bq + phi * Bq + phi * Aq;  // phi_s_x = sgm * phi_x
+    const double omg = 2.0 * (Aq + Bq + phi);
+    const double pb5 = P.pb5, pb4 = P.pb4;
     const double num = pb5 * Aq, den = phs * phs + pb4 * sig * sig;
     const double cf = tanh(num / den);
-    const double den2 = den * den;
-    double num1[3], num3[3], den1[3], den3[3], cfx1n[3], cfx3n[3], cfx1[3], cfx3[3];
-    for (int i = 0; i < 3; ++i) {
-      num1[i] = pb5 * px1[i]; num3[i] = pb5 * px3[i];
-      den1[i] = 2 * phs * phs1[i]; den3[i] = 2 * phs * phs3[i];
-      cfx1n[i] = num1[i] * den - num * den1[i];
-      cfx3n[i] = num3[i] * den - num * den3[i];
-      cfx1[i] = cfx1n[i] / den2;
-      cfx3[i] = cfx3n[i] / den2;
-    }
+    const double den2 = den * den, rden2 = 1.0 / den2, rden22 = 1.0 / (den2 * den2);
+    const double tau = pb5 * den - num * (2 * phs * sgm);  // con_func_x_x numerator / phi_x
+    const double muc = tau * rden2;                         // con_func_x_x = muc * phi_x
     const double g3 = gamma * gamma * gamma, g2 = gamma * gamma;
     const double base = 0.5 * (comp + 1.0) * S * kPi * (R * R);
     const double kx = base * ((1 + g3) + (1 - g3) * cf);
-    double kx1[3], kx3[3];
-    for (int i = 0; i < 3; ++i) {
-      kx1[i] = base * (cc * g2 * gx1[i] - cc * g2 * gx1[i] * cf + (1 - g3) * (1 - cf * cf * cfx1[i]));
-      kx3[i] = base * (cc * g2 * gx3[i] - cc * g2 * gx3[i] * cf + (1 - g3) * (1 - cf * cf * cfx3[i]));
-    }
+    const double beta0 = base * (1 - g3);
+    const double beta1 = base * (cc * g2 * kap * (1 - cf) - (1 - g3) * cf * cf * muc);
     const double Bq2 = Bq * Bq;
-    const double cf1 = (kx * Lc * Bq) / (l1 * s), cf3 = (kx * Lc * Bq) / (l3 * s);
+    const double cf1 = (kx * Lc * Bq) * rl1s, cf3 = (kx * Lc * Bq) * rl3s;
     for (int i = 0; i < 3; ++i) {
-      Fx1[i] = -0.5 * kx1[i] * Lc * Bq2 + cf1 * a3[i];
-      Fx3[i] = -0.5 * kx3[i] * Lc * Bq2 + cf3 * a1[i];
+      Fx1[i] = -0.5 * (beta0 + beta1 * px1[i]) * Lc * Bq2 + cf1 * a3[i];
+      Fx3[i] = -0.5 * (beta0 + beta1 * px3[i]) * Lc * Bq2 + cf3 * a1[i];
     }
-    double a3a1[3][3], a1a3[3][3], P1P3[3][3], P3P1[3][3], P3d3o[3][3];
-    outer3(a3, a1, a3a1);
-    outer3(a1, a3, a1a3);
+    // pass-invariant coefficients
+    double P1P3[3][3], P3P1[3][3], e3[3];
     matmul3(P1, P3, P1P3);
     matmul3(P3, P1, P3P1);
-    matmul3(a1d3, P3, P3d3o);  // outer(P3 d1, d3) P3 as written (src/PhysicsCloth.cpp:2775-2777)
-    double px11[3][3], px33[3][3], px13[3][3], px31[3][3];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        px11[i][j] = (a3d1[i][j] + d1a3[i][j] - (cs2 * a3a3[i][j]) + co * P1[i][j]) / ((l1 * l1) * s);
-        px33[i][j] = (a1d3[i][j] + d3a1[i][j] - (cs2 * a1a1[i][j]) + co * P3[i][j]) / ((l3 * l3) * s);
-        px13[i][j] = -(cs2 * a3a1[i][j] + P1P3[i][j]) / (l1 * l3 * s);
-        px31[i][j] = -(cs2 * P3d3o[i][j] + P3P1[i][j]) / (l3 * l1 * s);
-      }
-    // J11 and J33 first, then J13 and J31, to bound the live 3x3 temporaries
+    matvec3(P3, d3, e3);  // P3 d3: src/PhysicsCloth.cpp:2775-2777 multiplies outer(P3 d1, d3) by P3
     const double cfq = -2 * cf * (1 - cf * cf);
     const double c1 = cc * (cc - 1) * gamma, c2 = cc * g2;
     const double base2 = 0.5 * (comp + 1.0) * S * (R * R);
+    const double kO = c1 * kap * kap * (1 - cf) - 2 * c2 * kap * (1 - cf * cf) * muc;
+    const double kG = c2 * (1 - cf);
+    const double cfqm2 = cfq * muc * muc;
+    const double X4 = 4 * tau * den * phs * sgm;
+    const double two_num_sgm2 = 2 * num * sgm * sgm, two_num_phs = 2 * num * phs, pb5den = pb5 * den;
+    const double cross = 2 * phs * pb5 * sgm;
+    const double hLB2 = 0.5 * Lc * Bq2, LB = Lc * Bq;
     const double kL = kx * Lc;
-    double cfd1[3], cfd3[3];
-    for (int i = 0; i < 3; ++i) { cfd1[i] = (1.0 - cf * cf) * cfx1[i]; cfd3[i] = (1.0 - cf * cf) * cfx3[i]; }
+    const double r11 = 1.0 / ((l1 * l1) * s), r33 = 1.0 / ((l3 * l3) * s), r13 = 1.0 / (l1 * l3 * s);
+    const double qR11 = 0.5 * LR * sh / ((l1 * s) * (l1 * s)), qR33 = 0.5 * LR * sh / ((l3 * s) * (l3 * s));
+    const double qR13 = 0.5 * LR * sh / (l1 * l3 * (s * s));
     for (int pass = 0; pass < 4; ++pass) {
-      // pass 0: (1,1) 1: (3,3) 2: (1,3) 3: (3,1)
-      const double *pA = (pass == 0 || pass == 2) ? px1 : px3, *pB = (pass == 0 || pass == 3) ? px1 : px3;
-      const double *gA = (pass == 0 || pass == 2) ? gx1 : gx3, *gB = (pass == 0 || pass == 3) ? gx1 : gx3;
-      const double *kA = (pass == 0 || pass == 2) ? kx1 : kx3, *kB = (pass == 0 || pass == 3) ? kx1 : kx3;
-      const double *sA = (pass == 0 || pass == 2) ? phs1 : phs3, *sB = (pass == 0 || pass == 3) ? phs1 : phs3;
-      const double *cA = (pass == 0 || pass == 2) ? cfx1 : cfx3, *cB = (pass == 0 || pass == 3) ? cfx1 : cfx3;
-      const double *cnA = (pass == 0 || pass == 2) ? cfx1n : cfx3n;
-      const double *dB = (pass == 0 || pass == 3) ? den1 : den3;
-      const double *nA = (pass == 0 || pass == 2) ? num1 : num3, *nB = (pass == 0 || pass == 3) ? num1 : num3;
-      const double *cdA = (pass == 0 || pass == 2) ? cfd1 : cfd3, *cdB = (pass == 0 || pass == 3) ? cfd1 : cfd3;
-      double (*pxx)[3] = pass == 0 ? px11 : pass == 1 ? px33 : pass == 2 ? px13 : px31;
+      // pass 0: (x1,x1) 1: (x3,x3) 2: (x1,x3) 3: (x3,x1)
+      const double* pA = (pass == 0 || pass == 2) ? px1 : px3;
+      const double* pB = (pass == 0 || pass == 3) ? px1 : px3;
       double (*J)[3] = pass == 0 ? J11 : pass == 1 ? J33 : pass == 2 ? J13 : J31;
       for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) {
-          // gamma second derivative
-          double gxx;
-          if (pass == 0) gxx = (0.5 * LR * sh * a3a3[i][j]) / ((l1 * s) * (l1 * s)) - LR * ch * pxx[i][j];
-          else if (pass == 1) gxx = (0.5 * LR * sh * a1a1[i][j]) / ((l3 * s) * (l3 * s)) - LR * ch * pxx[i][j];
-          else if (pass == 2) gxx = (0.5 * LR * sh * a3a1[i][j]) / (l1 * l3 * (s * s)) - LR * ch * pxx[i][j];
-          else gxx = (0.5 * LR * sh * a1a3[i][j]) / (l3 * l1 * (s * s)) - LR * ch * pxx[i][j];
-          // phi_s second derivative
-          const double OAB = pA[i] * pB[j], OBA = pB[i] * pA[j];
-          double psx;
-          if (pass < 2)
-            psx = pxx[i][j] * Aq * Bq + OAB * Bq + OAB * Aq + OAB * Bq + phi * pxx[i][j] * Bq + phi * OAB + OAB * Aq +
-                  phi * OAB + phi * Aq * pxx[i][j];
-          else if (pass == 2)
-            psx = pxx[i][j] * Aq * Bq + OAB * Bq + OAB * Aq + OBA * Bq + phi * pxx[i][j] * Bq + phi * OAB + OBA * Aq +
-                  phi * OBA + phi * Aq * pxx[i][j];
-          else
-            psx = pxx[i][j] * Aq * Bq + OAB * Bq + OAB * Aq + OAB * Bq + phi * pxx[i][j] * Bq + phi * OAB + OAB * Aq +
-                  phi * OAB + phi * Aq * pxx[i][j];
-          // d^2 con_func_x
-          double nx;
-          if (pass < 2)
-            nx = (pb5 * pxx[i][j]) * den - 2 * num * (sA[i] * sB[j]) - 2 * num * phs * psx;
-          else
-            nx = ((pb5 * pxx[i][j]) * den + 2 * phs * (nA[i] * sB[j]) - 2 * phs * (nB[i] * sA[j]) -
-                  2 * num * (sA[i] * sB[j]) - 2 * num * phs * psx);
-          const double cfxx = (nx * den2 - cnA[i] * (2 * den * dB[j])) / (den2 * den2);
-          // d^2 con_func
-          double cfdd;
-          if (pass < 2) cfdd = cfq * (cA[i] * cB[j]) + (1 - cf * cf * cfxx);
-          else cfdd = cfq * (cB[i] * cA[j]) + (1 - cf * cf) * cfxx;
-          // d^2 kx
-          const double t1 = c1 * (gA[i] * gB[j]) + c2 * gxx;
-          const double t2 = c1 * (gA[i] * gB[j]) * cf + c2 * gxx * cf + c2 * (gA[i] * cdB[j]);
-          const double t3 = (pass < 2 ? -c2 * (gA[i] * cdB[j]) : -c2 * (cdA[i] * gB[j])) + (1 - g3) * cfdd;
-          const double kxx = base2 * (t1 - t2 + t3);
-          // the projected-angle part
-          double fo;
+          const double O = pA[i] * pB[j], Ob = pB[i] * pA[j];
+          double pxx, Rg, fo;
           if (pass == 0) {
-            const double o11a = a3[i] * a3[j];
-            fo = (kL / ((l1 * l1) * s)) * (Bq * (-a3d1[i][j] + cs2 * o11a - co * P1[i][j] - d1a3[i][j]) - (1.0 / s) * o11a);
+            const double aa = a3[i] * a3[j];
+            pxx = (a3[i] * d1[j] + d1[i] * a3[j] - cs2 * aa + co * P1[i][j]) * r11;
+            Rg = qR11 * aa;
+            fo = (kL * r11) * (Bq * (-(a3[i] * d1[j]) + cs2 * aa - co * P1[i][j] - d1[i] * a3[j]) - is * aa);
           } else if (pass == 1) {
-            const double o33a = a1[i] * a1[j];
-            fo = (kL / ((l3 * l3) * s)) * (Bq * (-a1d3[i][j] + cs2 * o33a - co * P3[i][j] - d3a1[i][j]) - (1.0 / s) * o33a);
+            const double aa = a1[i] * a1[j];
+            pxx = (a1[i] * d3[j] + d3[i] * a1[j] - cs2 * aa + co * P3[i][j]) * r33;
+            Rg = qR33 * aa;
+            fo = (kL * r33) * (Bq * (-(a1[i] * d3[j]) + cs2 * aa - co * P3[i][j] - d3[i] * a1[j]) - is * aa);
           } else if (pass == 2) {
-            fo = (kL / (l1 * l3 * s)) * (Bq * (cs2 * a3a1[i][j] + P1P3[i][j]) - (1.0 / s) * a3a1[i][j]);
+            const double aa = a3[i] * a1[j];
+            pxx = -(cs2 * aa + P1P3[i][j]) * r13;
+            Rg = qR13 * aa;
+            fo = (kL * r13) * (Bq * (cs2 * aa + P1P3[i][j]) - is * aa);
           } else {
-            fo = (kL / (l3 * l1 * s)) * (Bq * (cs2 * a1a3[i][j] + P3P1[i][j]) - (1.0 / s) * a1a3[i][j]);
+            const double aa = a1[i] * a3[j];
+            pxx = -(cs2 * (a1[i] * e3[j]) + P3P1[i][j]) * r13;
+            Rg = qR13 * aa;
+            fo = (kL * r13) * (Bq * (cs2 * aa + P3P1[i][j]) - is * aa);
           }
-          if (pass < 2) J[i][j] = -0.5 * kxx * Lc * Bq2 - 2 * Lc * Bq * (kA[i] * pB[j]) + fo;
-          else J[i][j] = (-0.5 * kxx * Lc * Bq2 - Lc * Bq * (kA[i] * pB[j]) - Lc * Bq * (pA[i] * kB[j]) + fo);
+          const double gxx = Rg + kap * pxx;
+          const double psx = sgm * pxx + (pass == 2 ? 0.5 * omg * (O + Ob) : omg * O);
+          double nx = pb5den * pxx - two_num_sgm2 * O - two_num_phs * psx;
+          if (pass >= 2) nx += cross * (O - Ob);
+          const double cfxx = (nx * den2 - X4 * O) * rden22;
+          const double cfdd = pass < 2 ? cfqm2 * O + (1 - cf * cf * cfxx) : cfqm2 * Ob + (1 - cf * cf) * cfxx;
+          const double kxx = base2 * (kO * O + kG * gxx + (1 - g3) * cfdd);
+          double kk;
+          if (pass < 2) kk = 2 * LB * (beta0 * pB[j] + beta1 * O);
+          else kk = LB * (beta0 * pB[j] + beta1 * O) + LB * (beta0 * pA[i] + beta1 * O);
+          J[i][j] = -kxx * hLB2 - kk + fo;
         }
     }
   }

@@ -185,12 +185,14 @@ static void build_pattern(yo_cloth *c) {
 static void sym3_min_eigvec(double A[3][3], double out[3]) {
   double a[3][3], V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
   memcpy(a, A, sizeof(a));
+  /* off-diagonal entries below 1e-24 of the diagonal scale are treated as zero */
+  const double tiny = 1e-24 * (fabs(A[0][0]) + fabs(A[1][1]) + fabs(A[2][2]));
   for (int sweep = 0; sweep < 50; ++sweep) {
     double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
-    if (off == 0.0) break;
+    if (off <= tiny) break;
     for (int p = 0; p < 2; ++p)
       for (int q = p + 1; q < 3; ++q) {
-        if (a[p][q] == 0.0) continue;
+        if (fabs(a[p][q]) <= tiny) continue;
         double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
         double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
         double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;

@@ -60,6 +60,8 @@ void* emu_create(const ys_cloth_desc* d) {
   P.kh = d->handle_stiffness; P.jam = 2.0 * std::asin(d->R / d->L);
   for (int k = 0; k < 3; ++k) { P.G[k] = d->G[k]; P.wind[k] = d->wind_vel[k]; }
   P.wind_rho = d->wind_density; P.wind_drag = d->wind_drag;
+  P.pb4 = std::pow(ys::kPi / 2, 4);
+  P.pb5 = std::pow(ys::kPi / 2, 5);
   for (int i = 0; i < H; ++i) {
     e->rho.push_back(d->warp_rho[i]);
     e->ks.push_back(d->warp_Y[i] * ys::kPi * std::pow(d->R, 2));

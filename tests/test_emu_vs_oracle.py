@@ -52,3 +52,32 @@ def test_emulated_trajectory_matches_reference(name):
         st = em.get_state()
         for k in ("LPos", "LVel", "EPos", "EVel", "EPosBar"):
             assert goldens.rel(st[k], ref[k]) <= STATE_TOL, (s + 1, k, goldens.rel(st[k], ref[k]))
+
+
+@pytest.mark.parametrize("weave", [0, 1, 2])
+@pytest.mark.parametrize("S", [1e6, 1e8])
+def test_shear_dominated_system_matches_oracle(weave, S):
+    """Shear (with jamming) made the dominant stiffness, on a perturbed state,
+    so its Hessian is resolved far below the system tolerance."""
+    from oracle.oracle import ClothSpec, OracleCloth
+    rng = np.random.default_rng(weave * 7 + int(np.log10(S)))
+    W, H = 7, 6
+    base = np.array([1e-3, 1e3, 1e-5])
+    kw = dict(width=W, length=H, warp=np.tile(base, (H, 1)), weft=np.tile(base, (W, 1)), weave=weave, pose=1,
+              S=S, handles=[(0, 0), (W - 1, 0)])
+    oc = OracleCloth(ClothSpec(**kw))
+    em = EmuCloth(**kw)
+    st = oc.get_state()
+    N = W * H
+    st["LPos"] = st["LPos"] + 1.5e-4 * rng.standard_normal((N, 3))
+    st["LVel"] = 1e-2 * rng.standard_normal((N, 3))
+    oc.set_state(st)
+    em.set_state(st)
+    oc.fill()
+    A_ref, b_ref = oc.system(1e-3)
+    em.assemble(1e-3)
+    A, b = em.system()
+    shear_scale = np.abs(A_ref[:3 * N, :3 * N]).max()
+    assert shear_scale > 1e-2  # shear dominates the node-node blocks
+    assert goldens.rel(A, A_ref) <= 1e-12
+    assert goldens.rel(b, b_ref) <= 1e-12
