@@ -325,7 +325,6 @@ def main():
         # x, p, r, q, dinv read; x, r written
         "axpy": dict(bytes=n * (5 * 5 * 8 + 2 * 5 * 8), flops=n * 5 * 8),
         "dir": dict(bytes=n * (3 * 5 * 8 + 5 * 8), flops=n * 5 * 3),
-        "clear": dict(bytes=n * (159 + 5 + 3 + 6 + 6) * 8, flops=0),
     }
     hbm_peak, peak_kind = peaks()
     fp64_peak = measure_fp64_peak(torch)

@@ -22,8 +22,8 @@ EXPORTED = [
     "ys_solve", "ys_get_solution", "ys_step", "ys_apply_system", "ys_synchronize", "ys_profile",
     "ys_profile_read",
 ]
-PROF_KINDS = ["geom", "clear", "edges", "bends", "faces", "friction", "shear", "finalize", "pcg_setup", "spmv",
-              "axpy", "dir", "update", "misc"]
+PROF_KINDS = ["geom", "edges", "bends", "faces", "gather", "shear", "finalize", "pcg_setup", "spmv", "axpy", "dir",
+              "update", "misc"]
 
 
 class ClothDesc(ctypes.Structure):

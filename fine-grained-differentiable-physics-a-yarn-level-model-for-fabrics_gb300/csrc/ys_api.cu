@@ -35,12 +35,6 @@ ys_status fail(ys_status s, const std::string& msg) {
       return fail(YS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));               \
   } while (0)
 
-struct Pass {
-  int kind;  // 0 warp/weft edge, 1 bend, 2 face, 3 shear
-  int k;
-  int off, n;  // range inside the anchor list
-};
-
 // node-major [n][c] <-> component-major [c][n]
 __global__ void k_to_soa(const double* __restrict__ in, double* __restrict__ out, int64_t n, int c) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -76,12 +70,12 @@ struct ys_batch {
   std::vector<ys::ClothParams> cp;
   std::vector<int64_t> dims;
   std::vector<int> anchors_host;
-  std::vector<Pass> passes;
-  int geom_off = 0, geom_n = 0;  // interior-node list (normals, friction)
+  int geom_off = 0, geom_n = 0;  // interior-node list (normals)
   // device memory
   std::vector<void*> allocs;
   int64_t bytes = 0;
   ys::View v{};
+  ys::Records rec{};
   ys::Blocks blk{};
   ys::Solver so{};
   int* anchors = nullptr;
@@ -221,7 +215,6 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
   std::vector<uint8_t> flags;
   std::vector<double> X, XF, UV, rho, ks, kb;
   std::vector<int> blk_cloth, blk_node0, blk_count, cloth_blk0, cloth_nblk, maxiter;
-  std::vector<std::vector<int>> lists(2 + 2 + 3 + 3 + 4 + 9);
   int off = 0, line_off = 0;
   for (int c = 0; c < n_cloths; ++c) {
     const ys_cloth_desc& d = descs[c];
@@ -270,13 +263,6 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
         else { X.push_back(i * d.L); X.push_back(j * d.L); X.push_back(d.height); }
         UV.push_back(i * d.L);
         UV.push_back(j * d.L);
-        // colour classes
-        if (i < W - 1) lists[0 + (i & 1)].push_back(n);
-        if (j < H - 1) lists[2 + (j & 1)].push_back(n);
-        if (i >= 1 && i <= W - 2) lists[4 + i % 3].push_back(n);
-        if (j >= 1 && j <= H - 2) lists[7 + j % 3].push_back(n);
-        if (i < W - 1 && j < H - 1) lists[10 + (i & 1) + 2 * (j & 1)].push_back(n);
-        if (interior) lists[14 + (i % 3) + 3 * (j % 3)].push_back(n);
       }
     const int nb = (W * H + ys::kBlock - 1) / ys::kBlock;
     cloth_blk0.push_back((int)blk_cloth.size());
@@ -293,26 +279,13 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
   }
   b->ntot = off;
   b->max_maxiter = *std::max_element(maxiter.begin(), maxiter.end());
-  // anchor lists and passes
+  // interior nodes (normals)
   std::vector<int> interior_nodes;
   for (int n = 0; n < off; ++n)
     if (flags[n] & ys::YS_INTERIOR) interior_nodes.push_back(n);
-  auto add_pass = [&](int kind, int k, const std::vector<int>& L) {
-    Pass p{kind, k, (int)b->anchors_host.size(), (int)L.size()};
-    b->anchors_host.insert(b->anchors_host.end(), L.begin(), L.end());
-    b->passes.push_back(p);
-  };
-  // element order: edges (warp then weft), bends (warp then weft), faces,
-  // [friction], shear -- as in FillMV (src/PhysicsCloth.cpp:56-131)
-  add_pass(0, 0, lists[0]); add_pass(0, 0, lists[1]);
-  add_pass(0, 1, lists[2]); add_pass(0, 1, lists[3]);
-  for (int c = 0; c < 3; ++c) add_pass(1, 0, lists[4 + c]);
-  for (int c = 0; c < 3; ++c) add_pass(1, 1, lists[7 + c]);
-  for (int c = 0; c < 4; ++c) add_pass(2, 0, lists[10 + c]);
-  for (int c = 0; c < 9; ++c) add_pass(3, 0, lists[14 + c]);
-  b->geom_off = (int)b->anchors_host.size();
+  b->geom_off = 0;
   b->geom_n = (int)interior_nodes.size();
-  b->anchors_host.insert(b->anchors_host.end(), interior_nodes.begin(), interior_nodes.end());
+  b->anchors_host = interior_nodes;
 
   // ------------------------------------------------------------ device memory
   const int64_t nt = off;
@@ -333,8 +306,9 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
   ys::View& v = b->v;
   A(&v.X, 3 * nt); A(&v.V, 3 * nt); A(&v.XF, 3 * nt); A(&v.UV, 2 * nt); A(&v.UVD, 2 * nt); A(&v.UVB, 2 * nt);
   A(&v.UV0, 2 * nt); A(&v.NRM, 3 * nt); A(&v.COMP, nt); A(&v.SLIDE, 2 * nt);
-  A(&v.A, (size_t)ys::YS_NUM_SLOTS * nt); A(&v.B, 5 * nt); A(&v.CL, 3 * nt); A(&v.CLE, 6 * nt);
-  A(&v.FE, 2 * nt); A(&v.KEE, 2 * nt); A(&v.DEE, 2 * nt);
+  A(&v.A, (size_t)ys::YS_NUM_SLOTS * nt); A(&v.B, 5 * nt);
+  A(&b->rec.edge, (size_t)ys::kEdgeFields * 2 * nt); A(&b->rec.bend, (size_t)ys::kBendFields * 2 * nt);
+  A(&b->rec.face, 6 * nt); A(&b->rec.shear, (size_t)ys::kShearFields * 4 * nt);
   A(&b->so.x, 5 * nt); A(&b->so.r, 5 * nt); A(&b->so.p, 5 * nt); A(&b->so.q, 5 * nt); A(&b->so.dinv, 5 * nt);
   A(&b->so.part, 3 * blk_cloth.size()); A(&b->so.pc, n_cloths); A(&b->so.nactive, 1);
   A(&b->stage, 5 * nt); A(&b->ext, 5 * nt);
@@ -504,26 +478,16 @@ ys_status ys_assemble(ys_batch* b, double h, const double* ext_force, int32_t fl
   b->run(YS_PROF_MISC, 1, [&] { k_reset_status<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->ncloth); });
   // UpdateClothUnits normals for the current positions (src/Cloth.cpp:307-327)
   if (b->geom_n) b->run(YS_PROF_GEOM, 1, [&] { ys::launch_geom(v, b->anchors + b->geom_off, b->geom_n, s); });
-  b->run(YS_PROF_CLEAR, 1, [&] { ys::launch_clear(v, s); });
-  bool friction_done = false;
-  for (const Pass& p : b->passes) {
-    const int* a = b->anchors + p.off;
-    if (p.kind == 3 && !friction_done) {
-      // ConSlideFriction needs every edge and bend term; shear needs its
-      // compression (src/PhysicsCloth.cpp:97-131)
-      if (b->geom_n)
-        b->run(YS_PROF_FRICTION, 1, [&] { ys::launch_friction(v, b->anchors + b->geom_off, b->geom_n, s); });
-      friction_done = true;
-    }
-    if (p.n == 0) continue;
-    switch (p.kind) {
-      case 0: b->run(YS_PROF_EDGES, 1, [&] { ys::launch_edges(v, a, p.n, p.k, s); }); break;
-      case 1: b->run(YS_PROF_BENDS, 1, [&] { ys::launch_bends(v, a, p.n, p.k, s); }); break;
-      case 2: b->run(YS_PROF_FACES, 1, [&] { ys::launch_faces(v, a, p.n, s); }); break;
-      case 3: b->run(YS_PROF_SHEAR, 1, [&] { ys::launch_shear(v, a, p.n, s); }); break;
-    }
-  }
-  b->run(YS_PROF_FINALIZE, 1, [&] { ys::launch_finalize(v, b->blk, b->so, s); });
+  // element records (FillMV's element loops, src/PhysicsCloth.cpp:64-95)
+  const ys::Records& R = b->rec;
+  b->run(YS_PROF_EDGES, 1, [&] { ys::launch_edge_records(v, R, s); });
+  b->run(YS_PROF_BENDS, 1, [&] { ys::launch_bend_records(v, R, s); });
+  b->run(YS_PROF_FACES, 1, [&] { ys::launch_face_records(v, R, s); });
+  // row blocks + ConSlideFriction (needs every edge and bend term; shear
+  // needs its compression, src/PhysicsCloth.cpp:97-131)
+  b->run(YS_PROF_GATHER, 1, [&] { ys::launch_gather(v, R, s); });
+  b->run(YS_PROF_SHEAR, 1, [&] { ys::launch_shear_records(v, R, s); });
+  b->run(YS_PROF_FINALIZE, 1, [&] { ys::launch_finalize(v, R, b->blk, b->so, s); });
   YS_CUDA(cudaGetLastError());
   b->assembled = true;
   return YS_OK;

@@ -1,37 +1,326 @@
 // ys_items.cuh -- per-node bodies of the step kernels that are not element
-// terms: clearing, finalising a row block, the stencil SpMV row, and the
-// state update. Kept separate from the launch code so one node's work is a
-// plain function of (View, node).
+// terms: gathering the element records into a row block, the stencil SpMV row,
+// and the state update. Kept separate from the launch code so one node's work
+// is a plain function of (View, node).
 #pragma once
 
 #include "ys_physics.cuh"
 
 namespace ys {
 
-YS_HD void clear_node(const View& v, int n) {
-  const int nt = v.ntot;
-  for (int s = 0; s < YS_NUM_SLOTS; ++s) slot(v, s, n) = 0.0;
-  for (int c = 0; c < 5; ++c) st(v.B, c, nt, n) = 0.0;
-  for (int c = 0; c < 3; ++c) st(v.CL, c, nt, n) = 0.0;
-  for (int c = 0; c < 6; ++c) st(v.CLE, c, nt, n) = 0.0;
-  for (int c = 0; c < 2; ++c) {
-    st(v.FE, c, nt, n) = 0.0;
-    st(v.KEE, c, nt, n) = 0.0;
-    st(v.DEE, c, nt, n) = 0.0;
-  }
+// Per-element record buffers of one step (field-major, coalesced over the
+// anchor node). Edges and bend segments have one slot per node and yarn
+// direction (slot = k * ntot + anchor), faces one per cell (top-left node),
+// shear segments four per crossing (slot = type * ntot + crossing).
+struct Records {
+  double* edge;   // [kEdgeFields][2][ntot]
+  double* bend;   // [kBendFields][2][ntot]
+  double* face;   // [6][ntot]
+  double* shear;  // [kShearFields][4][ntot]
+};
+
+YS_HD double rec(const double* buf, int field, int nslot, int slot_, int ntot, int node) {
+  return buf[((int64_t)field * nslot + slot_) * ntot + node];
 }
 
-// Handle springs (Constraint_F / Constraint_D, src/PhysicsCloth.cpp:232-248),
+// Gathers, for row block n, every contribution of the edges, bend segments
+// and faces that touch it, runs ConSlideFriction on the gathered no-slide
+// quantities, and writes all 159 coefficient slots and b (the diagonal
+// blocks, which only shear segments fill, are set to 0 here). Node-node
+// blocks of X_LL are written transposed into the dense matrix
+// (src/MatrixMp.cpp:54-65), hence the blk[3 * c + r] reads.
+YS_HD void gather_elements(const View& v, const Records& R, int n) {
+  const int nt = v.ntot;
+  const ClothParams& P = v.cp[v.node_cloth[n]];
+  const int W = P.W, H = P.H, u = v.node_u[n], w = v.node_v[n];
+  const bool in = (v.flags[n] & YS_INTERIOR) != 0;
+  const double h = v.h, mh2 = -(v.h * v.h);
+  // ------------------------------------------------------------ self block
+  {
+    double LL[9], LE[6], EL[6], EE[2], B[5], FE[2], KEE[2], DEE[2], CL[3], CLE[6];
+    for (int i = 0; i < 9; ++i) LL[i] = 0.0;
+    for (int i = 0; i < 6; ++i) LE[i] = EL[i] = CLE[i] = 0.0;
+    for (int i = 0; i < 2; ++i) EE[i] = FE[i] = KEE[i] = DEE[i] = 0.0;
+    for (int i = 0; i < 5; ++i) B[i] = 0.0;
+    for (int i = 0; i < 3; ++i) CL[i] = 0.0;
+    for (int k = 0; k < 2; ++k) {
+      // edges along k: this node as n0 (anchor n) and as n1 (anchor n - step)
+      const int step = k == 0 ? 1 : W;
+      const bool has0 = k == 0 ? (u < W - 1) : (w < H - 1);
+      const bool has1 = k == 0 ? (u > 0) : (w > 0);
+      for (int a = 0; a < 2; ++a) {
+        if (!(a == 0 ? has0 : has1)) continue;
+        const int anc = a == 0 ? n : n - step;
+        auto E = [&](int f) { return rec(R.edge, f, 2, k, nt, anc); };
+        const int p = 3 * a;  // block (a, a)
+        const double cI = E(kE_llI + p), cP = E(kE_llP + p);
+        const double d[3] = {E(kE_d), E(kE_d + 1), E(kE_d + 2)};
+        for (int r = 0; r < 3; ++r)
+          for (int c = 0; c < 3; ++c) LL[3 * r + c] += (r == c ? cI : 0.0) + cP * ((r == c ? 1.0 : 0.0) - d[r] * d[c]);
+        for (int r = 0; r < 3; ++r) {
+          LE[2 * r + k] += E(kE_le + 3 * p + r);
+          EL[3 * k + r] += E(kE_el + 3 * p + r);
+          B[r] += E(kE_b + 4 * a + r);
+          CL[r] += E(kE_cl + 3 * a + r);
+          CLE[3 * k + r] += E(kE_cle + 3 * a + r);
+        }
+        EE[k] += E(kE_ee + p);
+        B[3 + k] += E(kE_b + 4 * a + 3);
+        FE[k] += E(kE_fkd + 3 * a);
+        KEE[k] += E(kE_fkd + 3 * a + 1);
+        DEE[k] += E(kE_fkd + 3 * a + 2);
+      }
+      // bend segments along k with middle m: this node is n2 (m = n + step),
+      // n0 (m = n) or n1 (m = n - step)
+      const int pos = k == 0 ? u : w, len = k == 0 ? W : H;
+      const double sgn = (k == 0) ? 1.0 : -1.0;
+      for (int role = 0; role < 3; ++role) {
+        const int mid = role == 0 ? pos + 1 : role == 1 ? pos : pos - 1;
+        if (mid < 1 || mid > len - 2) continue;
+        const int anc = role == 0 ? n + step : role == 1 ? n : n - step;
+        auto Bf = [&](int f) { return rec(R.bend, f, 2, k, nt, anc); };
+        double blk[9];
+        if (role == 0) {
+          for (int i = 0; i < 9; ++i) blk[i] = Bf(kB_L22 + i);
+        } else if (role == 2) {
+          for (int i = 0; i < 9; ++i) blk[i] = Bf(kB_L11 + i);
+        } else {  // L00 = -(L10 + L20) (src/PhysicsCloth.cpp:709)
+          for (int i = 0; i < 9; ++i) {
+            const double L10 = -(Bf(kB_L11 + i) + Bf(kB_L12 + i)), L20 = -(Bf(kB_L21 + i) + Bf(kB_L22 + i));
+            blk[i] = -(L10 + L20);
+          }
+        }
+        for (int r = 0; r < 3; ++r)
+          for (int c = 0; c < 3; ++c) LL[3 * r + c] += mh2 * blk[3 * c + r];
+        if (role == 0) {  // n2 (src/PhysicsCloth.cpp:737-753)
+          for (int r = 0; r < 3; ++r) {
+            B[r] += h * Bf(kB_Fx2 + r);
+            CL[r] += sgn * Bf(kB_cFx2 + r);
+          }
+          if (in) {
+            const double e11 = Bf(kB_E1E1), fu2 = Bf(kB_Fu2);
+            for (int r = 0; r < 3; ++r) {
+              const double l2e2 = -Bf(kB_L2E1 + r);
+              LE[2 * r + k] += mh2 * l2e2;
+              EL[3 * k + r] += mh2 * l2e2;  // E2L2 = -E1L2 carries the values of -L2E1
+              CLE[3 * k + r] += sgn * (-Bf(kB_cL2E1 + r));
+            }
+            EE[k] += mh2 * e11;
+            KEE[k] += e11;
+            B[3 + k] += h * fu2;
+            FE[k] += fu2;
+          }
+        } else if (role == 2) {  // n1 (src/PhysicsCloth.cpp:755-772)
+          for (int r = 0; r < 3; ++r) {
+            B[r] += h * Bf(kB_Fx1 + r);
+            CL[r] += sgn * Bf(kB_cFx1 + r);
+          }
+          if (in) {
+            const double e11 = Bf(kB_E1E1), fu1 = -1 * Bf(kB_Fu2);
+            for (int r = 0; r < 3; ++r) {
+              const double l1e1 = Bf(kB_L1E1 + r);
+              LE[2 * r + k] += mh2 * l1e1;
+              EL[3 * k + r] += mh2 * l1e1;
+              CLE[3 * k + r] += sgn * Bf(kB_cL1E1 + r);
+            }
+            EE[k] += mh2 * e11;
+            KEE[k] += e11;
+            B[3 + k] += h * fu1;
+            FE[k] += fu1;
+          }
+        } else {  // n0: F_x0 = -(F_x1 + F_x2), F_u0 = 0
+          for (int r = 0; r < 3; ++r) {
+            B[r] += h * (-(Bf(kB_Fx1 + r) + Bf(kB_Fx2 + r)));
+            CL[r] += sgn * (-(Bf(kB_cFx1 + r) + Bf(kB_cFx2 + r)));
+          }
+        }
+      }
+    }
+    // faces of the (up to) four cells around the node (src/Cloth.cpp:271-287)
+    for (int cj = w - 1; cj <= w; ++cj)
+      for (int ci = u - 1; ci <= u; ++ci) {
+        if (ci < 0 || ci >= W - 1 || cj < 0 || cj >= H - 1) continue;
+        const int tl = n + (ci - u) + (cj - w) * W;
+        const bool right = ci != u, below = cj != w;  // node is tr / bl / br of that cell
+        const bool even = ((ci + cj) & 1) == 0;
+        bool inA, inB;
+        if (!right && !below) { inA = true; inB = even; }       // tl
+        else if (right && !below) { inA = true; inB = !even; }  // tr
+        else if (!right && below) { inA = !even; inB = true; }  // bl
+        else { inA = even; inB = true; }                        // br
+        for (int r = 0; r < 3; ++r) {
+          if (inA) B[r] += h * R.face[(int64_t)r * nt + tl];
+          if (inB) B[r] += h * R.face[(int64_t)(3 + r) * nt + tl];
+        }
+      }
+    if (in) {
+      double aEE[2], bE[2];
+      friction_node(v, n, FE, KEE, DEE, CL, CLE, aEE, bE);
+      for (int k = 0; k < 2; ++k) {
+        EE[k] += aEE[k];
+        B[3 + k] += bE[k];
+      }
+    }
+    for (int i = 0; i < 9; ++i) slot(v, YS_SLOT_LL + i, n) = LL[i];
+    for (int i = 0; i < 6; ++i) {
+      slot(v, YS_SLOT_LE_SELF + i, n) = LE[i];
+      slot(v, YS_SLOT_EL_SELF + i, n) = EL[i];
+    }
+    for (int k = 0; k < 2; ++k) slot(v, YS_SLOT_EE_SELF + k, n) = EE[k];
+    for (int i = 0; i < 5; ++i) st(v.B, i, nt, n) = B[i];
+  }
+  // ------------------------------------------------ yarn neighbours (+-1)
+  for (int m = 0; m < 4; ++m) {
+    const int k = m < 2 ? 0 : 1;
+    const int dir = (m & 1) ? 1 : -1;  // -1: previous, +1: next along the yarn
+    const int step = k == 0 ? 1 : W;
+    const int pos = k == 0 ? u : w, len = k == 0 ? W : H;
+    const int s = stencil_index(k == 0 ? dir : 0, k == 1 ? dir : 0);
+    double LL[9], LE[3], EL[3], EE = 0.0;
+    for (int i = 0; i < 9; ++i) LL[i] = 0.0;
+    for (int i = 0; i < 3; ++i) LE[i] = EL[i] = 0.0;
+    if (pos + dir >= 0 && pos + dir < len) {
+      const int nb = n + dir * step;
+      const bool inb = (v.flags[nb] & YS_INTERIOR) != 0;
+      // the edge between n and nb: n is its n0 when dir = +1
+      const int a = dir > 0 ? 0 : 1, o = 1 - a;
+      const int anc = dir > 0 ? n : nb;
+      auto E = [&](int f) { return rec(R.edge, f, 2, k, nt, anc); };
+      const int p = 2 * a + o;
+      const double cI = E(kE_llI + p), cP = E(kE_llP + p);
+      const double d[3] = {E(kE_d), E(kE_d + 1), E(kE_d + 2)};
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) LL[3 * r + c] += (r == c ? cI : 0.0) + cP * ((r == c ? 1.0 : 0.0) - d[r] * d[c]);
+      for (int r = 0; r < 3; ++r) {
+        LE[r] += E(kE_le + 3 * p + r);
+        EL[r] += E(kE_el + 3 * p + r);
+      }
+      EE += E(kE_ee + p);
+      // bend segments containing both n and nb
+      for (int which = 0; which < 2; ++which) {
+        // which 0: middle = n (nb is n1 if dir = +1, n2 if dir = -1)
+        // which 1: middle = nb (n is n2 if dir = +1, n1 if dir = -1)
+        const int mid = which == 0 ? pos : pos + dir;
+        if (mid < 1 || mid > len - 2) continue;
+        const int ancb = which == 0 ? n : nb;
+        auto Bf = [&](int f) { return rec(R.bend, f, 2, k, nt, ancb); };
+        double blk[9];
+        for (int i = 0; i < 9; ++i) {
+          const double L11 = Bf(kB_L11 + i), L12 = Bf(kB_L12 + i), L21 = Bf(kB_L21 + i), L22 = Bf(kB_L22 + i);
+          if (which == 0) blk[i] = dir > 0 ? -(L11 + L21) : -(L12 + L22);  // L01 or L02
+          else blk[i] = dir > 0 ? -(L21 + L22) : -(L11 + L12);             // L20 or L10
+        }
+        for (int r = 0; r < 3; ++r)
+          for (int c = 0; c < 3; ++c) LL[3 * r + c] += mh2 * blk[3 * c + r];
+        // Eulerian couplings of Bending_D (src/PhysicsCloth.cpp:774-822):
+        // q = L1E1 + L2E1 = L0E2 = E2L0 = -L0E1 = -E1L0
+        double q[3];
+        for (int r = 0; r < 3; ++r) q[r] = Bf(kB_L1E1 + r) + Bf(kB_L2E1 + r);
+        if (which == 0 && in && inb) {
+          if (dir < 0)  // row n0 = n, column e / x of n2 = nb
+            for (int r = 0; r < 3; ++r) { LE[r] += mh2 * q[r]; EL[r] += mh2 * q[r]; }
+          else  // row n0 = n, column e of n1 = nb
+            for (int r = 0; r < 3; ++r) LE[r] += mh2 * (-q[r]);
+        }
+        if (which == 1 && dir < 0 && in && inb)  // row n1 = n, column x of n0 = nb
+          for (int r = 0; r < 3; ++r) EL[r] += mh2 * (-q[r]);
+      }
+    }
+    for (int i = 0; i < 9; ++i) slot(v, YS_SLOT_LL + 9 * s + i, n) = LL[i];
+    for (int r = 0; r < 3; ++r) {
+      slot(v, YS_SLOT_LE_NBR + 3 * m + r, n) = LE[r];
+      slot(v, YS_SLOT_EL_NBR + 3 * m + r, n) = EL[r];
+    }
+    slot(v, YS_SLOT_EE_NBR + m, n) = EE;
+  }
+  // ------------------------------------------- second neighbours (+-2)
+  for (int m = 0; m < 4; ++m) {
+    const int k = m < 2 ? 0 : 1;
+    const int dir = (m & 1) ? 1 : -1;
+    const int step = k == 0 ? 1 : W;
+    const int pos = k == 0 ? u : w, len = k == 0 ? W : H;
+    const int s = stencil_index(k == 0 ? 2 * dir : 0, k == 1 ? 2 * dir : 0);
+    const int mid = pos + dir;
+    const bool ok = mid >= 1 && mid <= len - 2;
+    const int anc = n + dir * step;
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c)  // n is n2 (dir +1): L21; n is n1 (dir -1): L12
+        slot(v, YS_SLOT_LL + 9 * s + 3 * r + c, n) =
+            ok ? mh2 * rec(R.bend, (dir > 0 ? kB_L21 : kB_L12) + 3 * c + r, 2, k, nt, anc) : 0.0;
+  }
+  // diagonal neighbours: shear only (gather_shear_finalize)
+  for (int s = 9; s < 13; ++s)
+    for (int i = 0; i < 9; ++i) slot(v, YS_SLOT_LL + 9 * s + i, n) = 0.0;
+}
+
+// Adds the shear segments touching row block n (as crossing n0, as warp
+// neighbour n1 or as weft neighbour n3; src/PhysicsCloth.cpp:2643-3089), then
+// the handle springs (Constraint_F / Constraint_D, src/PhysicsCloth.cpp:232-248),
 // the external force of SimStep(..., ext_force) (src/TrainHelper.cpp:63),
-// identity rows for the Eulerian DOFs that boundary nodes do not have, and the
+// identity rows for the Eulerian DOFs boundary nodes do not have, and the
 // Jacobi preconditioner (zero diagonal -> 1, as Eigen's
 // DiagonalPreconditioner). Returns false if the row block holds a non-finite
 // value (SimStep's DetectNaN / DetectInf, src/TrainHelper.cpp:22-37).
-YS_HD bool finalize_node(const View& v, int n, double* dinv) {
+YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double* dinv) {
   const int nt = v.ntot;
   const ClothParams& P = v.cp[v.node_cloth[n]];
+  const int W = P.W, H = P.H, u = v.node_u[n], w = v.node_v[n];
   const uint8_t fl = v.flags[n];
-  const double h = v.h;
+  const double h = v.h, mh2 = -(v.h * v.h);
+  auto interior = [&](int uu, int vv) { return uu >= 1 && uu <= W - 2 && vv >= 1 && vv <= H - 2; };
+  auto S = [&](int f, int seg, int anc) { return rec(R.shear, f, 4, seg, nt, anc); };
+  auto addLL = [&](int du, int dv, const double* blk) {  // A[x(n)][x(n + (du, dv))] += -h^2 blk^T
+    const int s = stencil_index(du, dv);
+    if (s < 0) return;
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) slot(v, YS_SLOT_LL + 9 * s + 3 * r + c, n) += mh2 * blk[3 * c + r];
+  };
+  double Bx[3] = {0.0, 0.0, 0.0};
+  double J[9];
+  // as the crossing n0 (src/PhysicsCloth.cpp:3033-3047)
+  if (fl & YS_INTERIOR) {
+    for (int seg = 0; seg < 4; ++seg) {
+      for (int i = 0; i < 9; ++i) {
+        const double J10 = -(S(kS_J11 + i, seg, n) + S(kS_J13 + i, seg, n));
+        const double J30 = -(S(kS_J31 + i, seg, n) + S(kS_J33 + i, seg, n));
+        J[i] = -(J10 + J30);
+      }
+      addLL(0, 0, J);
+      for (int i = 0; i < 9; ++i) J[i] = -(S(kS_J11 + i, seg, n) + S(kS_J31 + i, seg, n));  // J01
+      addLL(shear_du(seg), 0, J);
+      for (int i = 0; i < 9; ++i) J[i] = -(S(kS_J13 + i, seg, n) + S(kS_J33 + i, seg, n));  // J03
+      addLL(0, shear_dv(seg), J);
+      for (int r = 0; r < 3; ++r) Bx[r] += h * (-1 * (S(kS_F1 + r, seg, n) + S(kS_F3 + r, seg, n)));
+    }
+  }
+  // as the warp neighbour n1 = n0 + (du, 0)
+  for (int seg = 0; seg < 4; ++seg) {
+    const int du = shear_du(seg), dv = shear_dv(seg);
+    if (!interior(u - du, w)) continue;
+    const int anc = n - du;
+    for (int i = 0; i < 9; ++i) J[i] = S(kS_J11 + i, seg, anc);
+    addLL(0, 0, J);
+    for (int i = 0; i < 9; ++i) J[i] = -(S(kS_J11 + i, seg, anc) + S(kS_J13 + i, seg, anc));  // J10
+    addLL(-du, 0, J);
+    for (int i = 0; i < 9; ++i) J[i] = S(kS_J13 + i, seg, anc);  // towards n3 = n + (-du, dv)
+    addLL(-du, dv, J);
+    for (int r = 0; r < 3; ++r) Bx[r] += h * S(kS_F1 + r, seg, anc);
+  }
+  // as the weft neighbour n3 = n0 + (0, dv)
+  for (int seg = 0; seg < 4; ++seg) {
+    const int du = shear_du(seg), dv = shear_dv(seg);
+    if (!interior(u, w - dv)) continue;
+    const int anc = n - dv * W;
+    for (int i = 0; i < 9; ++i) J[i] = S(kS_J33 + i, seg, anc);
+    addLL(0, 0, J);
+    for (int i = 0; i < 9; ++i) J[i] = -(S(kS_J31 + i, seg, anc) + S(kS_J33 + i, seg, anc));  // J30
+    addLL(0, -dv, J);
+    for (int i = 0; i < 9; ++i) J[i] = S(kS_J31 + i, seg, anc);  // towards n1 = n + (du, -dv)
+    addLL(du, -dv, J);
+    for (int r = 0; r < 3; ++r) Bx[r] += h * S(kS_F3 + r, seg, anc);
+  }
+  for (int r = 0; r < 3; ++r) st(v.B, r, nt, n) += Bx[r];
+  // handles, external force, boundary identity rows
   if (fl & YS_FIXED) {
     for (int i = 0; i < 3; ++i) {
       st(v.B, i, nt, n) += h * (-(P.kh * (ld(v.X, i, nt, n) - ld(v.XF, i, nt, n))));

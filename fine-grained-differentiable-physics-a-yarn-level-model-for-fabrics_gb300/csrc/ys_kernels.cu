@@ -16,11 +16,6 @@ namespace ys {
 
 static inline int nblocks(int n) { return (n + kBlock - 1) / kBlock; }
 
-__global__ void k_clear(View v) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n < v.ntot) clear_node(v, n);
-}
-
 __global__ void k_geom(View v, const int* __restrict__ nodes, int count) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= count) return;
@@ -28,59 +23,56 @@ __global__ void k_geom(View v, const int* __restrict__ nodes, int count) {
   node_normal(v, n, v.cp[v.node_cloth[n]].W);
 }
 
-__global__ void __launch_bounds__(kBlock) k_edges(View v, const int* __restrict__ anchors, int count, int k) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= count) return;
-  const int n0 = anchors[t];
-  const int n1 = n0 + (k == 0 ? 1 : v.cp[v.node_cloth[n0]].W);
-  EdgeAcc a;
-  edge_terms(v, n0, n1, k, a);
-  edge_scatter(v, n0, n1, k, a);
+// one thread per (yarn direction, node): the edge starting at that node
+__global__ void __launch_bounds__(kBlock) k_edge_rec(View v, Records R) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2LL * v.ntot) return;
+  const int k = t >= v.ntot ? 1 : 0;
+  const int n0 = (int)(t - (int64_t)k * v.ntot);
+  const ClothParams& P = v.cp[v.node_cloth[n0]];
+  if (k == 0 ? v.node_u[n0] >= P.W - 1 : v.node_v[n0] >= P.H - 1) return;
+  EdgeOut o;
+  edge_element(v, n0, n0 + (k == 0 ? 1 : P.W), k, o);
+  edge_store(v, R.edge, n0, k, o);
 }
 
-__global__ void __launch_bounds__(kBlock) k_bends(View v, const int* __restrict__ anchors, int count, int k) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= count) return;
-  const int n0 = anchors[t];
+// one thread per (yarn direction, middle node) of a bend segment
+__global__ void __launch_bounds__(kBlock) k_bend_rec(View v, Records R) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2LL * v.ntot) return;
+  const int k = t >= v.ntot ? 1 : 0;
+  const int n0 = (int)(t - (int64_t)k * v.ntot);
   const ClothParams& P = v.cp[v.node_cloth[n0]];
+  const int pos = k == 0 ? v.node_u[n0] : v.node_v[n0], len = k == 0 ? P.W : P.H;
+  if (pos < 1 || pos > len - 2) return;
   const int step = k == 0 ? 1 : P.W;
   const int line = k == 0 ? P.warp_line_off + v.node_v[n0] : P.weft_line_off + v.node_u[n0];
-  const double kb = v.line_kb[line];
-  bend_element(v, n0 - step, n0, n0 + step, k, kb);
-  crimp_element(v, n0 - step, n0, n0 + step, k, kb);
+  bend_element(v, R.bend, n0 - step, n0, n0 + step, k, v.line_kb[line]);
 }
 
-__global__ void k_faces(View v, const int* __restrict__ anchors, int count) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= count) return;
-  const int tl = anchors[t];
-  const ClothParams& P = v.cp[v.node_cloth[tl]];
-  const int tr = tl + 1, bl = tl + P.W, br = tl + P.W + 1;
-  if (((v.node_u[tl] + v.node_v[tl]) & 1) == 0) {
-    wind_face(v, P, tl, tr, br);
-    wind_face(v, P, tl, br, bl);
-  } else {
-    wind_face(v, P, tl, tr, bl);
-    wind_face(v, P, tr, br, bl);
-  }
-}
-
-__global__ void k_friction(View v, const int* __restrict__ nodes, int count) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < count) friction_node(v, nodes[t]);
-}
-
-__global__ void __launch_bounds__(kBlock) k_shear(View v, const int* __restrict__ anchors, int count) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= count) return;
-  const int n = anchors[t];
+// one thread per grid cell (top-left node): its two faces
+__global__ void k_face_rec(View v, Records R) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.ntot) return;
   const ClothParams& P = v.cp[v.node_cloth[n]];
-  const int W = P.W;
-  // segment order of src/Cloth.cpp:178-181
-  shear_element(v, P, n, n - 1, n + W, -1, 1);
-  shear_element(v, P, n, n - 1, n - W, -1, -1);
-  shear_element(v, P, n, n + 1, n + W, 1, 1);
-  shear_element(v, P, n, n + 1, n - W, 1, -1);
+  if (v.node_u[n] >= P.W - 1 || v.node_v[n] >= P.H - 1) return;
+  cell_faces(v, R.face, n);
+}
+
+// row blocks from edge / bend / face records, plus sliding friction
+__global__ void __launch_bounds__(kBlock) k_gather(View v, Records R) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n < v.ntot) gather_elements(v, R, n);
+}
+
+// one thread per (segment type, crossing)
+__global__ void __launch_bounds__(kBlock) k_shear_rec(View v, Records R) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 4LL * v.ntot) return;
+  const int seg = (int)(t / v.ntot);
+  const int n0 = (int)(t - (int64_t)seg * v.ntot);
+  if (!(v.flags[n0] & YS_INTERIOR)) return;
+  shear_element(v, R.shear, n0, seg);
 }
 
 // ----------------------------------------------------------------- solve
@@ -104,16 +96,15 @@ __device__ __forceinline__ double cloth_sum(const Blocks& b, const double* part,
   return s;
 }
 
-__global__ void __launch_bounds__(kBlock) k_finalize(View v, Blocks b, Solver so) {
-  __shared__ int bad;
-  if (threadIdx.x == 0) bad = 0;
-  __syncthreads();
+// shear records into the row blocks, then handles, external force, boundary
+// identity rows, Jacobi diagonal and the finite check of the system
+__global__ void __launch_bounds__(kBlock) k_finalize(View v, Records R, Blocks b, Solver so) {
   const int blk = blockIdx.x;
   const int c = b.blk_cloth[blk];
   const int n = b.blk_node0[blk] + threadIdx.x;
-  if (threadIdx.x < b.blk_count[blk] && !finalize_node(v, n, so.dinv)) bad = 1;  // every writer stores 1
-  __syncthreads();
-  if (threadIdx.x == 0 && bad) atomicOr(&so.pc[c].status, 1);
+  bool bad = false;
+  if (threadIdx.x < b.blk_count[blk]) bad = !gather_shear_finalize(v, R, n, so.dinv);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&so.pc[c].status, 1);
 }
 
 // x = 0, r = b, p = z = Dinv r; partials |b|^2 (row 0), |r|^2 (row 1) and
@@ -288,27 +279,26 @@ __global__ void k_spmv_plain(View v, const double* x, double* y) {
 }
 
 // ----------------------------------------------------------------- launchers
-void launch_clear(const View& v, cudaStream_t s) { k_clear<<<nblocks(v.ntot), kBlock, 0, s>>>(v); }
 void launch_geom(const View& v, const int* nodes, int n, cudaStream_t s) {
   if (n) k_geom<<<nblocks(n), kBlock, 0, s>>>(v, nodes, n);
 }
-void launch_edges(const View& v, const int* anchors, int n, int k, cudaStream_t s) {
-  if (n) k_edges<<<nblocks(n), kBlock, 0, s>>>(v, anchors, n, k);
+void launch_edge_records(const View& v, const Records& R, cudaStream_t s) {
+  k_edge_rec<<<nblocks(2 * v.ntot), kBlock, 0, s>>>(v, R);
 }
-void launch_bends(const View& v, const int* anchors, int n, int k, cudaStream_t s) {
-  if (n) k_bends<<<nblocks(n), kBlock, 0, s>>>(v, anchors, n, k);
+void launch_bend_records(const View& v, const Records& R, cudaStream_t s) {
+  k_bend_rec<<<nblocks(2 * v.ntot), kBlock, 0, s>>>(v, R);
 }
-void launch_faces(const View& v, const int* anchors, int n, cudaStream_t s) {
-  if (n) k_faces<<<nblocks(n), kBlock, 0, s>>>(v, anchors, n);
+void launch_face_records(const View& v, const Records& R, cudaStream_t s) {
+  k_face_rec<<<nblocks(v.ntot), kBlock, 0, s>>>(v, R);
 }
-void launch_friction(const View& v, const int* nodes, int n, cudaStream_t s) {
-  if (n) k_friction<<<nblocks(n), kBlock, 0, s>>>(v, nodes, n);
+void launch_gather(const View& v, const Records& R, cudaStream_t s) {
+  k_gather<<<nblocks(v.ntot), kBlock, 0, s>>>(v, R);
 }
-void launch_shear(const View& v, const int* anchors, int n, cudaStream_t s) {
-  if (n) k_shear<<<nblocks(n), kBlock, 0, s>>>(v, anchors, n);
+void launch_shear_records(const View& v, const Records& R, cudaStream_t s) {
+  k_shear_rec<<<nblocks(4 * v.ntot), kBlock, 0, s>>>(v, R);
 }
-void launch_finalize(const View& v, const Blocks& b, const Solver& so, cudaStream_t s) {
-  k_finalize<<<b.nblk, kBlock, 0, s>>>(v, b, so);
+void launch_finalize(const View& v, const Records& R, const Blocks& b, const Solver& so, cudaStream_t s) {
+  k_finalize<<<b.nblk, kBlock, 0, s>>>(v, R, b, so);
 }
 void launch_pcg_setup(const View& v, const Blocks& b, const Solver& so, cudaStream_t s) {
   k_pcg_setup<<<b.nblk, kBlock, 0, s>>>(v, b, so);

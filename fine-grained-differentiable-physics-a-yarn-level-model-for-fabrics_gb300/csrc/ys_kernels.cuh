@@ -3,7 +3,7 @@
 
 #include <cuda_runtime.h>
 
-#include "ys_common.cuh"
+#include "ys_items.cuh"
 
 namespace ys {
 
@@ -44,14 +44,13 @@ struct Solver {
 
 constexpr int kBlock = 128;
 
-void launch_clear(const View& v, cudaStream_t s);
 void launch_geom(const View& v, const int* nodes, int n, cudaStream_t s);
-void launch_edges(const View& v, const int* anchors, int n, int k, cudaStream_t s);
-void launch_bends(const View& v, const int* anchors, int n, int k, cudaStream_t s);
-void launch_faces(const View& v, const int* anchors, int n, cudaStream_t s);
-void launch_friction(const View& v, const int* nodes, int n, cudaStream_t s);
-void launch_shear(const View& v, const int* anchors, int n, cudaStream_t s);
-void launch_finalize(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
+void launch_edge_records(const View& v, const Records& R, cudaStream_t s);
+void launch_bend_records(const View& v, const Records& R, cudaStream_t s);
+void launch_face_records(const View& v, const Records& R, cudaStream_t s);
+void launch_gather(const View& v, const Records& R, cudaStream_t s);
+void launch_shear_records(const View& v, const Records& R, cudaStream_t s);
+void launch_finalize(const View& v, const Records& R, const Blocks& b, const Solver& so, cudaStream_t s);
 void launch_pcg_setup(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
 void launch_pcg_spmv(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
 void launch_pcg_axpy(const View& v, const Blocks& b, const Solver& so, int it, cudaStream_t s);

@@ -76,125 +76,125 @@ YS_HD void add_A(const View& v, int rn, int rc, int cn, int cc, int k, double va
 // ------------------------------------------------------------ edge element
 // Local DOFs of an edge: x0 (0..2), e0 (3), x1 (4..6), e1 (7), where e is the
 // Eulerian coordinate along the edge's yarn (u for warp, v for weft).
-struct EdgeAcc {
-  double A[8][8];   // contribution to A in reference layout
-  double b[8];      // contribution to b
-  double Vloc[8];   // the step's velocity vector restricted to the edge
-  double fe[2], kee[2], dee[2];
-  double cl[2][3], cle[2][3];
+// Every node-node 3x3 block an edge produces is a I + b P with P = I - d d^T
+// (mass, inertia and dM/dt blocks are multiples of I, stretch adds P), so an
+// edge's contribution to A is held as 4 (a, b) pairs plus the Eulerian
+// couplings; block index p = 2*(row node) + (column node).
+struct EdgeOut {
+  double llI[4], llP[4];  // A[x(n_a)][x(n_b)] = llI I + llP P
+  double d[3];            // edge direction (defines P)
+  double le[4][3];        // A[x(n_a)][e(n_b)]
+  double el[4][3];        // A[e(n_a)][x(n_b)]
+  double ee[4];           // A[e(n_a)][e(n_b)]
+  double b[8];            // contribution to b
+  double fe[2], kee[2], dee[2];  // F_E, dF_E/dE (position, velocity) before friction
+  double cl[2][3], cle[2][3];    // crimp-compression accumulators
+  double V[8];            // the step's velocity vector restricted to the edge (not stored)
   double h, h2;
   bool in[2];
 };
+constexpr int kEdgeFields = 65;
 
 enum Mat { kM = 0, kK = 1, kD = 2 };
 
-// X_LL[find_index(f, d, "LL")] += s * blk; the dense matrix receives the
-// block transposed (src/PhysicsCloth.cpp:202, src/MatrixMp.cpp:54-65).
-template <class F>
-YS_HD void acc_LL(EdgeAcc& a, int X, int f, int d, double s, const F& blk) {
-  for (int r = 0; r < 3; ++r)
-    for (int c = 0; c < 3; ++c) {
-      double val = s * blk(c, r);
-      int row = 4 * f + r, col = 4 * d + c;
-      if (X == kM) { a.A[row][col] += val; a.b[row] += val * a.Vloc[col]; }
-      else if (X == kK) { a.A[row][col] += -a.h2 * val; }
-      else { a.A[row][col] += -a.h * val; a.b[col] -= a.h * val * a.Vloc[row]; }
-    }
+YS_HD double wt(const EdgeOut& o, int X) { return X == kM ? 1.0 : X == kK ? -o.h2 : -o.h; }
+
+// block (a, b) += val I of matrix X; b receives M V and -h D^T V
+// (src/TrainHelper.cpp:19-20). LL blocks of X_LL[find_index(f, d, "LL")] are
+// written transposed by To_Sparse_Mat (src/MatrixMp.cpp:54-65); a I + b P is
+// symmetric, so the transpose changes nothing here.
+YS_HD void acc_LLi(EdgeOut& o, int X, int a, int b, double val) {
+  o.llI[2 * a + b] += wt(o, X) * val;
+  if (X == kM)
+    for (int r = 0; r < 3; ++r) o.b[4 * a + r] += val * o.V[4 * b + r];
+  else if (X == kD)
+    for (int r = 0; r < 3; ++r) o.b[4 * b + r] -= o.h * val * o.V[4 * a + r];
 }
-// X_LE[find_index(l, e, "EL") + k] += s * vec  ->  A[x(l)][e(e)]
-template <class F>
-YS_HD void acc_LE(EdgeAcc& a, int X, int l, int e, double s, const F& vec) {
+YS_HD void acc_LLp(EdgeOut& o, int a, int b, double val) { o.llP[2 * a + b] += -o.h2 * val; }  // stiffness only
+// A[x(n_a)][e(n_b)] (X_LE[find_index(n_a, n_b, "EL") + k])
+YS_HD void acc_LE(EdgeOut& o, int X, int a, int b, const double* vec) {
+  const double w = wt(o, X);
+  double s = 0.0;
   for (int r = 0; r < 3; ++r) {
-    double val = s * vec(r);
-    int row = 4 * l + r, col = 4 * e + 3;
-    if (X == kM) { a.A[row][col] += val; a.b[row] += val * a.Vloc[col]; }
-    else if (X == kK) { a.A[row][col] += -a.h2 * val; }
-    else { a.A[row][col] += -a.h * val; a.b[col] -= a.h * val * a.Vloc[row]; }
+    o.le[2 * a + b][r] += w * vec[r];
+    if (X == kM) o.b[4 * a + r] += vec[r] * o.V[4 * b + 3];
+    s += vec[r] * o.V[4 * a + r];
   }
+  if (X == kD) o.b[4 * b + 3] -= o.h * s;
 }
-// X_EL[find_index(l, e, "EL") + k] += s * row  ->  A[e(e)][x(l)]
-template <class F>
-YS_HD void acc_EL(EdgeAcc& a, int X, int l, int e, double s, const F& rowv) {
+// A[e(n_a)][x(n_b)] (X_EL[find_index(n_b, n_a, "EL") + k])
+YS_HD void acc_EL(EdgeOut& o, int X, int a, int b, const double* vec) {
+  const double w = wt(o, X);
+  double s = 0.0;
   for (int c = 0; c < 3; ++c) {
-    double val = s * rowv(c);
-    int row = 4 * e + 3, col = 4 * l + c;
-    if (X == kM) { a.A[row][col] += val; a.b[row] += val * a.Vloc[col]; }
-    else if (X == kK) { a.A[row][col] += -a.h2 * val; }
-    else { a.A[row][col] += -a.h * val; a.b[col] -= a.h * val * a.Vloc[row]; }
+    o.el[2 * a + b][c] += w * vec[c];
+    s += vec[c] * o.V[4 * b + c];
+    if (X == kD) o.b[4 * b + c] -= o.h * vec[c] * o.V[4 * a + 3];
+  }
+  if (X == kM) o.b[4 * a + 3] += s;
+}
+YS_HD void acc_EE(EdgeOut& o, int X, int a, int b, double val) {
+  o.ee[2 * a + b] += wt(o, X) * val;
+  if (X == kM) o.b[4 * a + 3] += val * o.V[4 * b + 3];
+  else if (X == kD) o.b[4 * b + 3] -= o.h * val * o.V[4 * a + 3];
+  if (a == b) {
+    if (X == kK) o.kee[a] += val;
+    else if (X == kD) o.dee[a] += val;
   }
 }
-YS_HD void acc_EE(EdgeAcc& a, int X, int f, int d, double val) {
-  int row = 4 * f + 3, col = 4 * d + 3;
-  if (X == kM) { a.A[row][col] += val; a.b[row] += val * a.Vloc[col]; }
-  else if (X == kK) { a.A[row][col] += -a.h2 * val; if (f == d) a.kee[f] += val; }
-  else { a.A[row][col] += -a.h * val; a.b[col] -= a.h * val * a.Vloc[row]; if (f == d) a.dee[f] += val; }
-}
-YS_HD void acc_F(EdgeAcc& a, int dof, double f) {
-  a.b[dof] += a.h * f;
-  if ((dof & 3) == 3) a.fe[dof >> 2] += f;
-}
-
-// The write pattern shared by Inertia_D_Pos, Inertia_D_Vel, MDotVDot_D_Pos
-// and MDotVDot_D_Vel (src/PhysicsCloth.cpp:1544-1600, 1848-1900,
-// 2226-2308, 2505-2577): C(i, j) = d(force DOF i)/d(DOF j) in edge-local
-// order, added with sign s.
-template <class F>
-YS_HD void acc_edge_jac(EdgeAcc& a, int X, double s, const F& C) {
-  acc_LL(a, X, 0, 0, s, [&](int i, int j) { return C(i, j); });
-  acc_LL(a, X, 0, 1, s, [&](int i, int j) { return C(i, 4 + j); });
-  acc_LL(a, X, 1, 0, s, [&](int i, int j) { return C(4 + i, j); });
-  acc_LL(a, X, 1, 1, s, [&](int i, int j) { return C(4 + i, 4 + j); });
-  if (a.in[0]) {
-    acc_EL(a, X, 0, 0, s, [&](int c) { return C(3, c); });
-    acc_LE(a, X, 0, 0, s, [&](int r) { return C(r, 3); });
-    acc_EE(a, X, 0, 0, s * C(3, 3));
-  }
-  if (a.in[1]) {
-    acc_EL(a, X, 1, 1, s, [&](int c) { return C(7, 4 + c); });
-    acc_LE(a, X, 1, 1, s, [&](int r) { return C(4 + r, 7); });
-    acc_EE(a, X, 1, 1, s * C(7, 7));
-  }
-  if (a.in[0] && a.in[1]) {
-    acc_LE(a, X, 1, 0, s, [&](int r) { return C(4 + r, 3); });
-    acc_LE(a, X, 0, 1, s, [&](int r) { return C(r, 7); });
-    acc_EL(a, X, 1, 0, s, [&](int c) { return C(3, 4 + c); });
-    acc_EL(a, X, 0, 1, s, [&](int c) { return C(7, c); });
-    acc_EE(a, X, 0, 1, s * C(3, 7));
-    acc_EE(a, X, 1, 0, s * C(7, 3));
-  }
+YS_HD void acc_F(EdgeOut& o, int dof, double f) {
+  o.b[dof] += o.h * f;
+  if ((dof & 3) == 3) o.fe[dof >> 2] += f;
 }
 
-// B y for B = [[z I, p], [q^T, s]] and a 4-vector y = (ya, ye)
-struct Blk {
-  double z, p[3], q[3], s;
+// One edge Jacobian written with the pattern shared by Inertia_D_Pos,
+// Inertia_D_Vel, MDotVDot_D_Pos and MDotVDot_D_Vel
+// (src/PhysicsCloth.cpp:1544-1600, 1848-1900, 2226-2308, 2505-2577):
+// C(i, j) = d(force DOF i)/d(DOF j) in edge-local order; here given as the
+// isotropic node-node factors iso[p], the (x, e) columns lec[p][r] =
+// C(4a+r, 4b+3), the (e, x) rows elr[p][c] = C(4a+3, 4b+c) and eev[p] =
+// C(4a+3, 4b+3), added with sign s under the reference's interior tests.
+struct EdgeJac {
+  double iso[4], lec[4][3], elr[4][3], eev[4];
 };
-YS_HD void blk_apply(const Blk& B, const double* ya, double ye, double* oa, double* oe) {
-  for (int i = 0; i < 3; ++i) oa[i] = B.z * ya[i] + B.p[i] * ye;
-  *oe = B.q[0] * ya[0] + B.q[1] * ya[1] + B.q[2] * ya[2] + B.s * ye;
+YS_HD void acc_jac(EdgeOut& o, int X, double s, const EdgeJac& C) {
+  for (int p = 0; p < 4; ++p) acc_LLi(o, X, p >> 1, p & 1, s * C.iso[p]);
+  double t[3];
+  for (int p = 0; p < 4; ++p) {
+    const int a = p >> 1, b = p & 1;
+    const bool ok = (a == b) ? o.in[a] : (o.in[0] && o.in[1]);
+    if (!ok) continue;
+    for (int r = 0; r < 3; ++r) t[r] = s * C.lec[p][r];
+    acc_LE(o, X, a, b, t);
+    for (int c = 0; c < 3; ++c) t[c] = s * C.elr[p][c];
+    acc_EL(o, X, a, b, t);
+    acc_EE(o, X, a, b, s * C.eev[p]);
+  }
 }
 
 // All terms of one edge (src/PhysicsCloth.cpp:64-80): Mass, Gravity, Stretch,
 // Inertia, MDotVDot, ParaColli; forces and both Jacobians.
-YS_HD void edge_terms(const View& v, int n0, int n1, int k, EdgeAcc& a) {
+YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut& o) {
   const int nt = v.ntot;
   const ClothParams& P = v.cp[v.node_cloth[n0]];
   const uint8_t f0 = v.flags[n0], f1 = v.flags[n1];
-  a.in[0] = (f0 & YS_INTERIOR) != 0;
-  a.in[1] = (f1 & YS_INTERIOR) != 0;
+  o.in[0] = (f0 & YS_INTERIOR) != 0;
+  o.in[1] = (f1 & YS_INTERIOR) != 0;
   const int line = (k == 0) ? P.warp_line_off + v.node_v[n0] : P.weft_line_off + v.node_u[n0];
   const double rho = v.line_rho[line], ks = v.line_ks[line];
-  a.h = v.h;
-  a.h2 = v.h * v.h;
-  for (int i = 0; i < 8; ++i) {
-    a.b[i] = 0.0;
-    for (int j = 0; j < 8; ++j) a.A[i][j] = 0.0;
+  o.h = v.h;
+  o.h2 = v.h * v.h;
+  for (int p = 0; p < 4; ++p) {
+    o.llI[p] = o.llP[p] = o.ee[p] = 0.0;
+    for (int r = 0; r < 3; ++r) o.le[p][r] = o.el[p][r] = 0.0;
   }
+  for (int i = 0; i < 8; ++i) o.b[i] = 0.0;
   for (int t = 0; t < 2; ++t) {
-    a.fe[t] = a.kee[t] = a.dee[t] = 0.0;
-    for (int i = 0; i < 3; ++i) a.cl[t][i] = a.cle[t][i] = 0.0;
+    o.fe[t] = o.kee[t] = o.dee[t] = 0.0;
+    for (int i = 0; i < 3; ++i) o.cl[t][i] = o.cle[t][i] = 0.0;
   }
   // geometry (src/ClothUnit.h:134-154)
-  double x0[3], x1[3], a0[3], a1[3], dx[3], w[3], d[3], Pm[3][3];
+  double x0[3], x1[3], a0[3], a1[3], dx[3], w[3], d[3];
   for (int i = 0; i < 3; ++i) {
     x0[i] = ld(v.X, i, nt, n0); x1[i] = ld(v.X, i, nt, n1);
     a0[i] = ld(v.V, i, nt, n0); a1[i] = ld(v.V, i, nt, n1);
@@ -203,57 +203,55 @@ YS_HD void edge_terms(const View& v, int n0, int n1, int k, EdgeAcc& a) {
   const double e0 = ld(v.UVD, k, nt, n0), e1 = ld(v.UVD, k, nt, n1);
   for (int i = 0; i < 3; ++i) { dx[i] = x1[i] - x0[i]; w[i] = dx[i] / du; }
   const double l = norm3(dx);
-  for (int i = 0; i < 3; ++i) d[i] = dx[i] / l;
-  proj3(d, Pm);
-  for (int i = 0; i < 3; ++i) { a.Vloc[i] = a0[i]; a.Vloc[4 + i] = a1[i]; }
-  a.Vloc[3] = a.in[0] ? e0 : 0.0;
-  a.Vloc[7] = a.in[1] ? e1 : 0.0;
+  for (int i = 0; i < 3; ++i) { d[i] = dx[i] / l; o.d[i] = d[i]; }
+  for (int i = 0; i < 3; ++i) { o.V[i] = a0[i]; o.V[4 + i] = a1[i]; }
+  o.V[3] = o.in[0] ? e0 : 0.0;
+  o.V[7] = o.in[1] ? e1 : 0.0;
   const double wTw = dot3(w, w);
   const double nw = norm3(w);
+  double t3[3];
 
   // ---- Mass (src/PhysicsCloth.cpp:250-338)
   {
     const double coeff = (1.0 / 6.0) * rho * du;
-    auto I2 = [&](int i, int j) { return i == j ? 2.0 * coeff : 0.0; };
-    auto I1 = [&](int i, int j) { return i == j ? coeff : 0.0; };
-    acc_LL(a, kM, 0, 0, 1.0, I2);
-    acc_LL(a, kM, 1, 0, 1.0, I1);
-    acc_LL(a, kM, 0, 1, 1.0, I1);
-    acc_LL(a, kM, 1, 1, 1.0, I2);
-    auto LE2 = [&](int r) { return -2.0 * coeff * w[r]; };
-    auto LE1 = [&](int r) { return -1.0 * coeff * w[r]; };
+    acc_LLi(o, kM, 0, 0, 2.0 * coeff);
+    acc_LLi(o, kM, 1, 0, coeff);
+    acc_LLi(o, kM, 0, 1, coeff);
+    acc_LLi(o, kM, 1, 1, 2.0 * coeff);
+    double LE2[3], LE1[3];
+    for (int r = 0; r < 3; ++r) { LE2[r] = -2.0 * coeff * w[r]; LE1[r] = -1.0 * coeff * w[r]; }
     const double EE2 = 2.0 * coeff * wTw, EE1 = 0.5 * EE2;
-    if (a.in[0]) { acc_LE(a, kM, 0, 0, 1.0, LE2); acc_EL(a, kM, 0, 0, 1.0, LE2); acc_EE(a, kM, 0, 0, EE2); }
-    if (a.in[1]) { acc_LE(a, kM, 1, 1, 1.0, LE2); acc_EL(a, kM, 1, 1, 1.0, LE2); acc_EE(a, kM, 1, 1, EE2); }
-    if (a.in[0] && a.in[1]) {
-      acc_LE(a, kM, 1, 0, 1.0, LE1);
-      acc_LE(a, kM, 0, 1, 1.0, LE1);
-      acc_EL(a, kM, 1, 0, 1.0, LE1);
-      acc_EL(a, kM, 0, 1, 1.0, LE1);
-      acc_EE(a, kM, 0, 1, EE1);
-      acc_EE(a, kM, 1, 0, EE1);
+    if (o.in[0]) { acc_LE(o, kM, 0, 0, LE2); acc_EL(o, kM, 0, 0, LE2); acc_EE(o, kM, 0, 0, EE2); }
+    if (o.in[1]) { acc_LE(o, kM, 1, 1, LE2); acc_EL(o, kM, 1, 1, LE2); acc_EE(o, kM, 1, 1, EE2); }
+    if (o.in[0] && o.in[1]) {
+      acc_LE(o, kM, 1, 0, LE1);
+      acc_LE(o, kM, 0, 1, LE1);
+      acc_EL(o, kM, 0, 1, LE1);  // M_EL[find_index(n1, n0)] = E0L1
+      acc_EL(o, kM, 1, 0, LE1);  // M_EL[find_index(n0, n1)] = E1L0
+      acc_EE(o, kM, 0, 1, EE1);
+      acc_EE(o, kM, 1, 0, EE1);
     }
   }
   // ---- Gravity_F / Gravity_D (src/PhysicsCloth.cpp:340-425)
   {
     for (int i = 0; i < 3; ++i) {
       const double g = 0.5 * rho * P.G[i] * du;
-      acc_F(a, i, -g);
-      acc_F(a, 4 + i, -g);
+      acc_F(o, i, -g);
+      acc_F(o, 4 + i, -g);
     }
     double sx[3] = {x0[0] + x1[0], x0[1] + x1[1], x0[2] + x1[2]};
     const double gx = dot3(P.G, sx);
-    if (a.in[0]) acc_F(a, 3, -((-0.5) * rho * gx));
-    if (a.in[1]) acc_F(a, 7, -(0.5 * rho * gx));
-    auto g0 = [&](int r) { return 0.5 * rho * P.G[r]; };
-    auto g1 = [&](int r) { return -(0.5 * rho * P.G[r]); };
-    if (a.in[0]) { acc_EL(a, kK, 0, 0, 1.0, g0); acc_LE(a, kK, 0, 0, 1.0, g0); }
-    if (a.in[1]) { acc_EL(a, kK, 1, 1, 1.0, g1); acc_LE(a, kK, 1, 1, 1.0, g1); }
-    if (a.in[0] && a.in[1]) {
-      acc_LE(a, kK, 1, 0, 1.0, g0);
-      acc_LE(a, kK, 0, 1, 1.0, g1);
-      acc_EL(a, kK, 1, 0, 1.0, g0);
-      acc_EL(a, kK, 0, 1, 1.0, g1);
+    if (o.in[0]) acc_F(o, 3, -((-0.5) * rho * gx));
+    if (o.in[1]) acc_F(o, 7, -(0.5 * rho * gx));
+    double g0[3], g1[3];
+    for (int r = 0; r < 3; ++r) { g0[r] = 0.5 * rho * P.G[r]; g1[r] = -g0[r]; }
+    if (o.in[0]) { acc_EL(o, kK, 0, 0, g0); acc_LE(o, kK, 0, 0, g0); }
+    if (o.in[1]) { acc_EL(o, kK, 1, 1, g1); acc_LE(o, kK, 1, 1, g1); }
+    if (o.in[0] && o.in[1]) {
+      acc_LE(o, kK, 1, 0, g0);  // L1E0
+      acc_LE(o, kK, 0, 1, g1);  // L0E1
+      acc_EL(o, kK, 0, 1, g0);  // E0L1
+      acc_EL(o, kK, 1, 0, g1);  // E1L0
     }
   }
   // ---- Stretch_F / Stretch_D (src/PhysicsCloth.cpp:427-577)
@@ -261,41 +259,38 @@ YS_HD void edge_terms(const View& v, int n0, int n1, int k, EdgeAcc& a) {
     const double sgn = (k == 0) ? 1.0 : -1.0;
     for (int i = 0; i < 3; ++i) {
       const double f = ks * (nw - 1) * d[i];
-      acc_F(a, i, f);
-      acc_F(a, 4 + i, -f);
-      a.cl[0][i] += sgn * f;
-      a.cl[1][i] -= sgn * f;
+      acc_F(o, i, f);
+      acc_F(o, 4 + i, -f);
+      o.cl[0][i] += sgn * f;
+      o.cl[1][i] -= sgn * f;
     }
     const double fe = 0.5 * ks * (nw * nw - 1);
-    if (a.in[0]) acc_F(a, 3, -fe);
-    if (a.in[1]) acc_F(a, 7, fe);
-    auto LL = [&](int i, int j) { return (ks / l) * Pm[i][j] - (ks / du) * (i == j ? 1.0 : 0.0); };
+    if (o.in[0]) acc_F(o, 3, -fe);
+    if (o.in[1]) acc_F(o, 7, fe);
+    // LL = (ks / l) P - (ks / du) I, +LL on (0,0), (1,1) and -LL across
+    const double cP = ks / l, cI = -(ks / du);
+    acc_LLp(o, 0, 0, cP); acc_LLp(o, 1, 0, -cP); acc_LLp(o, 0, 1, -cP); acc_LLp(o, 1, 1, cP);
+    acc_LLi(o, kK, 0, 0, cI); acc_LLi(o, kK, 1, 0, -cI); acc_LLi(o, kK, 0, 1, -cI); acc_LLi(o, kK, 1, 1, cI);
     const double EE = -ks * ((nw * nw) / du);
-    auto LE = [&](int r) { return ks * (nw / du) * d[r]; };
-    auto EL = [&](int c) { return ks / du * w[c]; };
-    acc_LL(a, kK, 0, 0, 1.0, LL);
-    acc_LL(a, kK, 1, 0, -1.0, LL);
-    acc_LL(a, kK, 0, 1, -1.0, LL);
-    acc_LL(a, kK, 1, 1, 1.0, LL);
-    if (a.in[0]) {
-      acc_LE(a, kK, 0, 0, 1.0, LE);
-      acc_EL(a, kK, 0, 0, 1.0, EL);
-      acc_EE(a, kK, 0, 0, EE);
-      for (int i = 0; i < 3; ++i) a.cle[0][i] += sgn * LE(i);
+    double LE[3], EL[3], nLE[3], nEL[3];
+    for (int r = 0; r < 3; ++r) {
+      LE[r] = ks * (nw / du) * d[r];
+      EL[r] = ks / du * w[r];
+      nLE[r] = -LE[r];
+      nEL[r] = -EL[r];
     }
-    if (a.in[1]) {
-      acc_LE(a, kK, 1, 1, 1.0, LE);
-      acc_EL(a, kK, 1, 1, 1.0, EL);
-      acc_EE(a, kK, 1, 1, EE);
-      for (int i = 0; i < 3; ++i) a.cle[1][i] += sgn * LE(i);
+    if (o.in[0]) {
+      acc_LE(o, kK, 0, 0, LE); acc_EL(o, kK, 0, 0, EL); acc_EE(o, kK, 0, 0, EE);
+      for (int i = 0; i < 3; ++i) o.cle[0][i] += sgn * LE[i];
     }
-    if (a.in[0] && a.in[1]) {
-      acc_LE(a, kK, 1, 0, -1.0, LE);
-      acc_LE(a, kK, 0, 1, -1.0, LE);
-      acc_EL(a, kK, 1, 0, -1.0, EL);
-      acc_EL(a, kK, 0, 1, -1.0, EL);
-      acc_EE(a, kK, 0, 1, -EE);
-      acc_EE(a, kK, 1, 0, -EE);
+    if (o.in[1]) {
+      acc_LE(o, kK, 1, 1, LE); acc_EL(o, kK, 1, 1, EL); acc_EE(o, kK, 1, 1, EE);
+      for (int i = 0; i < 3; ++i) o.cle[1][i] += sgn * LE[i];
+    }
+    if (o.in[0] && o.in[1]) {
+      acc_LE(o, kK, 1, 0, nLE); acc_LE(o, kK, 0, 1, nLE);
+      acc_EL(o, kK, 0, 1, nEL); acc_EL(o, kK, 1, 0, nEL);
+      acc_EE(o, kK, 0, 1, -EE); acc_EE(o, kK, 1, 0, -EE);
     }
   }
   // ---- ParaColli_F / ParaColli_D (src/PhysicsCloth.cpp:989-1069)
@@ -304,12 +299,12 @@ YS_HD void edge_terms(const View& v, int n0, int n1, int k, EdgeAcc& a) {
     double rl = dd - du;
     if (rl < 0) rl = 0.0;
     const double fu0 = P.kc * P.L * rl;
-    if (a.in[0]) acc_F(a, 3, fu0);
-    if (a.in[1]) acc_F(a, 7, -fu0);
+    if (o.in[0]) acc_F(o, 3, fu0);
+    if (o.in[1]) acc_F(o, 7, -fu0);
     const double ee = -P.kc * P.L * rl;
-    if (a.in[0]) acc_EE(a, kK, 0, 0, ee);
-    if (a.in[1]) acc_EE(a, kK, 1, 1, ee);
-    if (a.in[0] && a.in[1]) { acc_EE(a, kK, 0, 1, ee); acc_EE(a, kK, 1, 0, ee); }
+    if (o.in[0]) acc_EE(o, kK, 0, 0, ee);
+    if (o.in[1]) acc_EE(o, kK, 1, 1, ee);
+    if (o.in[0] && o.in[1]) { acc_EE(o, kK, 0, 1, ee); acc_EE(o, kK, 1, 0, ee); }
   }
 
   // ---- kinetic-energy terms: shared sums
@@ -323,28 +318,28 @@ YS_HD void edge_terms(const View& v, int n0, int n1, int k, EdgeAcc& a) {
   const double r6 = (1.0 / 6.0) * rho;
   const double sc = 1.0 / 6.0 * rho * du;
   const double wSae = dot3(w, Sae), wSea = dot3(w, Sea);
+  const double pj = -(-1.0 / du);  // (-w_x0)_j for the active component j
+  EdgeJac C;
 
   // ---- Inertia_F (src/PhysicsCloth.cpp:1071-1186)
   {
     for (int j = 0; j < 3; ++j) {
-      const double pj = -(-1.0 / du);
       const double sj = (-2.0 / (du * du) * dx[j]);
       const double T0 = 0.5 * (sc * (pj * Sae[j] + pj * Sea[j] + sj * See));
-      acc_F(a, j, T0);
-      acc_F(a, 4 + j, -T0);
+      acc_F(o, j, T0);
+      acc_F(o, 4 + j, -T0);
     }
     const double QM = Saa - wSae - wSea + wTw * See;
     const double Quv = (-1.0 / du) * wSae + (-1.0 / du) * wSea + (2.0 / du) * wTw * See;
     const double Tuv0 = 0.5 * (-(1.0 / 6.0) * rho * QM + (1.0 / 6.0) * rho * du * Quv);
-    if (a.in[0]) acc_F(a, 3, Tuv0);
-    if (a.in[1]) acc_F(a, 7, -Tuv0);
+    if (o.in[0]) acc_F(o, 3, Tuv0);
+    if (o.in[1]) acc_F(o, 7, -Tuv0);
   }
   // ---- Inertia_D_Pos (src/PhysicsCloth.cpp:1188-1601)
   {
     const double T00 = 0.5 * (r6 * ((2 / (du * du)) * See));
     double Tx0uv0[3], Tuv0x0[3];
     for (int j = 0; j < 3; ++j) {
-      const double pj = -(-1.0 / du);
       const double Qx0 = pj * Sae[j] + pj * Sea[j] + (-2.0 / (du * du) * dx[j]) * See;
       const double c2 = 1.0 / (du * du);
       // the sign-asymmetric mixed block of src/PhysicsCloth.cpp:1357-1361
@@ -356,42 +351,37 @@ YS_HD void edge_terms(const View& v, int n0, int n1, int k, EdgeAcc& a) {
     const double c6 = 2 / (du * du);
     const double Quvuv = (-c6) * wSae + (-c6) * wSea + (6 / (du * du)) * wTw * See;
     const double Tuu = 0.5 * ((-1.0 / 6.0) * rho * Quv0 - (1.0 / 6.0) * rho * Quv0 + (1.0 / 6.0) * rho * du * Quvuv);
-    auto C = [&](int i, int j) -> double {
-      const int bi = i >> 2, bj = j >> 2, ii = i & 3, jj = j & 3;
-      const double sgn = (bi == bj) ? 1.0 : -1.0;
-      if (ii < 3 && jj < 3) return ii == jj ? sgn * T00 : 0.0;
-      if (ii < 3) return sgn * Tx0uv0[ii];
-      if (jj < 3) return sgn * Tuv0x0[jj];
-      return sgn * Tuu;
-    };
-    acc_edge_jac(a, kK, 1.0, C);
+    for (int p = 0; p < 4; ++p) {
+      const double sgn = ((p >> 1) == (p & 1)) ? 1.0 : -1.0;
+      C.iso[p] = sgn * T00;
+      for (int r = 0; r < 3; ++r) { C.lec[p][r] = sgn * Tx0uv0[r]; C.elr[p][r] = sgn * Tuv0x0[r]; }
+      C.eev[p] = sgn * Tuu;
+    }
+    acc_jac(o, kK, 1.0, C);
   }
-  // ---- Inertia_D_Vel (src/PhysicsCloth.cpp:1602-1901): C(j, :) = M_xj qdot
+  // ---- Inertia_D_Vel (src/PhysicsCloth.cpp:1602-1901): row x_j of C = M_xj qdot
   {
-    double rowx[3][8], rowu[8];
-    for (int j = 0; j < 3; ++j) {
-      const double pj = -(-1.0 / du), sj = (-2.0 / (du * du) * dx[j]);
-      for (int i = 0; i < 8; ++i) rowx[j][i] = 0.0;
-      rowx[j][j] = sc * (pj * m0e);
-      rowx[j][3] = sc * (pj * m0a[j] + sj * m0e);
-      rowx[j][4 + j] = sc * (pj * m1e);
-      rowx[j][7] = sc * (pj * m1a[j] + sj * m1e);
+    const double me_[2] = {m0e, m1e};
+    const double* ma_[2] = {m0a, m1a};
+    for (int b = 0; b < 2; ++b) {
+      const double iso = sc * (pj * me_[b]);
+      double lec[3], elr[3];
+      const double wm = dot3(w, ma_[b]);
+      for (int r = 0; r < 3; ++r) {
+        lec[r] = sc * (pj * ma_[b][r] + (-2.0 / (du * du) * dx[r]) * me_[b]);
+        elr[r] = -(1.0 / 6.0) * rho * (ma_[b][r] - w[r] * me_[b]) + (1.0 / 6.0) * rho * du * ((-1.0 / du) * w[r] * me_[b]);
+      }
+      const double eev = -(1.0 / 6.0) * rho * (-wm + wTw * me_[b]) +
+                         (1.0 / 6.0) * rho * du * ((-1.0 / du) * wm + (2.0 / du) * wTw * me_[b]);
+      for (int a = 0; a < 2; ++a) {
+        const double sgn = a == 0 ? 1.0 : -1.0;  // rows of x1 / uv1 are the negated rows of x0 / uv0
+        const int p = 2 * a + b;
+        C.iso[p] = sgn * iso;
+        for (int r = 0; r < 3; ++r) { C.lec[p][r] = sgn * lec[r]; C.elr[p][r] = sgn * elr[r]; }
+        C.eev[p] = sgn * eev;
+      }
     }
-    for (int t = 0; t < 2; ++t) {
-      const double* ma = t == 0 ? m0a : m1a;
-      const double me = t == 0 ? m0e : m1e;
-      const double wm = dot3(w, ma);
-      for (int i = 0; i < 3; ++i)
-        rowu[4 * t + i] = -(1.0 / 6.0) * rho * (ma[i] - w[i] * me) + (1.0 / 6.0) * rho * du * ((-1.0 / du) * w[i] * me);
-      rowu[4 * t + 3] = -(1.0 / 6.0) * rho * (-wm + wTw * me) +
-                        (1.0 / 6.0) * rho * du * ((-1.0 / du) * wm + (2.0 / du) * wTw * me);
-    }
-    auto C = [&](int i, int j) -> double {
-      const int bi = i >> 2, ii = i & 3;
-      const double sgn = bi == 0 ? 1.0 : -1.0;
-      return ii < 3 ? sgn * rowx[ii][j] : sgn * rowu[j];
-    };
-    acc_edge_jac(a, kD, 1.0, C);
+    acc_jac(o, kD, 1.0, C);
   }
   // ---- MDotVDot (src/PhysicsCloth.cpp:1903-2577)
   {
@@ -399,137 +389,102 @@ YS_HD void edge_terms(const View& v, int n0, int n1, int k, EdgeAcc& a) {
     double wd[3];
     for (int i = 0; i < 3; ++i) wd[i] = ((a1[i] - a0[i]) * du - dx[i] * dud) / (du * du);
     const double wTwd = dot3(w, wd) + dot3(wd, w);
-    // M_dot qdot = r6*dud*[[2BM,BM],[BM,2BM]] qdot + r6*du*[[2Bd,Bd],[Bd,2Bd]] qdot
-    Blk BM, Bd;
-    BM.z = 1.0; BM.s = wTw;
-    Bd.z = 0.0; Bd.s = wTwd;
-    for (int i = 0; i < 3; ++i) { BM.p[i] = BM.q[i] = -w[i]; Bd.p[i] = Bd.q[i] = -wd[i]; }
+    // B_M m and B_dot m for m = m0, m1 (4-vectors); M_dot qdot = r6 dud (B_M m) + r6 du (B_dot m)
     double BMm[2][4], Bdm[2][4], r[8];
-    blk_apply(BM, m0a, m0e, &BMm[0][0], &BMm[0][3]);
-    blk_apply(BM, m1a, m1e, &BMm[1][0], &BMm[1][3]);
-    blk_apply(Bd, m0a, m0e, &Bdm[0][0], &Bdm[0][3]);
-    blk_apply(Bd, m1a, m1e, &Bdm[1][0], &Bdm[1][3]);
-    for (int t = 0; t < 2; ++t)
-      for (int i = 0; i < 4; ++i) r[4 * t + i] = r6 * dud * BMm[t][i] + r6 * du * Bdm[t][i];
+    for (int b = 0; b < 2; ++b) {
+      const double* ma = b == 0 ? m0a : m1a;
+      const double me = b == 0 ? m0e : m1e;
+      for (int i = 0; i < 3; ++i) { BMm[b][i] = ma[i] + (-w[i]) * me; Bdm[b][i] = (-wd[i]) * me; }
+      BMm[b][3] = (-w[0]) * ma[0] + (-w[1]) * ma[1] + (-w[2]) * ma[2] + wTw * me;
+      Bdm[b][3] = (-wd[0]) * ma[0] + (-wd[1]) * ma[1] + (-wd[2]) * ma[2] + wTwd * me;
+      for (int i = 0; i < 4; ++i) r[4 * b + i] = r6 * dud * BMm[b][i] + r6 * du * Bdm[b][i];
+    }
     // MDotVDot_F: F -= M_dot qdot
-    for (int i = 0; i < 3; ++i) { acc_F(a, i, -r[i]); acc_F(a, 4 + i, -r[4 + i]); }
-    if (a.in[0]) acc_F(a, 3, -r[3]);
-    if (a.in[1]) acc_F(a, 7, -r[7]);
-    // column c of M_dot
-    auto Mdot = [&](int i, int c) -> double {
-      const int bi = i >> 2, bc = c >> 2, ii = i & 3, cc = c & 3;
-      const double f = (bi == bc) ? 2.0 : 1.0;
-      double m, dm;
-      if (ii < 3 && cc < 3) { m = ii == cc ? 1.0 : 0.0; dm = 0.0; }
-      else if (ii < 3) { m = -w[ii]; dm = -wd[ii]; }
-      else if (cc < 3) { m = -w[cc]; dm = -wd[cc]; }
-      else { m = wTw; dm = wTwd; }
-      return r6 * dud * (f * m) + r6 * du * (f * dm);
-    };
+    for (int i = 0; i < 3; ++i) { acc_F(o, i, -r[i]); acc_F(o, 4 + i, -r[4 + i]); }
+    if (o.in[0]) acc_F(o, 3, -r[3]);
+    if (o.in[1]) acc_F(o, 7, -r[7]);
     // MDotVDot_D_Pos, added (src/PhysicsCloth.cpp:2154-2234)
-    {
-      double Cp[8][8];
-      for (int t = 0; t < 2; ++t) {
-        const double sw = t == 0 ? -1.0 : 1.0;
-        for (int j = 0; j < 3; ++j) {
-          const double wxj = sw * (1.0 / du);
-          const double P1 = -wxj, S1 = (sw * 2.0 / (du * du) * dx[j]);
-          const double wdxj = t == 0 ? (dud / (du * du)) : -(dud / (du * du));
-          const double P2 = -wdxj, S2 = 2 * (wxj * wd[j]) + 2 * (w[j] * wdxj);
-          const int col = 4 * t + j;
-          for (int b2 = 0; b2 < 2; ++b2) {
-            const double* ma = b2 == 0 ? m0a : m1a;
-            const double me = b2 == 0 ? m0e : m1e;
-            for (int i = 0; i < 3; ++i)
-              Cp[4 * b2 + i][col] = (i == j) ? (r6 * dud * (P1 * me) + r6 * du * (P2 * me)) : 0.0;
-            Cp[4 * b2 + 3][col] = r6 * dud * (P1 * ma[j] + S1 * me) + r6 * du * (P2 * ma[j] + S2 * me);
-          }
-        }
-        double wuv[3], wduv[3];
-        for (int i = 0; i < 3; ++i) wuv[i] = (sw * w[i]) / du;
-        const double wTwuv = sw * (2 / du) * wTw;
-        for (int i = 0; i < 3; ++i)
-          wduv[i] = (a1[i] - a0[i]) / (du * du) - (4 * dx[i] * dud) / (du * du * du);
-        if (t == 1)
-          for (int i = 0; i < 3; ++i) wduv[i] = -wduv[i];
-        const double wTwduv = 2 * dot3(wuv, wd) + 2 * dot3(wduv, w);
-        const int col = 4 * t + 3;
-        for (int b2 = 0; b2 < 2; ++b2) {
-          const double* ma = b2 == 0 ? m0a : m1a;
-          const double me = b2 == 0 ? m0e : m1e;
-          for (int i = 0; i < 3; ++i)
-            Cp[4 * b2 + i][col] = r6 * dud * (wuv[i] * me) - r6 * r[4 * b2 + i] + r6 * du * (-wduv[i] * me);
-          Cp[4 * b2 + 3][col] = r6 * dud * (dot3(wuv, ma) + wTwuv * me) - r6 * r[4 * b2 + 3] +
-                                r6 * du * (-dot3(wduv, ma) + wTwduv * me);
-        }
+    for (int t = 0; t < 2; ++t) {
+      const double sw = t == 0 ? -1.0 : 1.0;
+      const double wxj = sw * (1.0 / du);
+      const double P1 = -wxj;
+      const double wdxj = t == 0 ? (dud / (du * du)) : -(dud / (du * du));
+      const double P2 = -wdxj;
+      double wuv[3], wduv[3];
+      for (int i = 0; i < 3; ++i) wuv[i] = (sw * w[i]) / du;
+      const double wTwuv = sw * (2 / du) * wTw;
+      for (int i = 0; i < 3; ++i) {
+        wduv[i] = (a1[i] - a0[i]) / (du * du) - (4 * dx[i] * dud) / (du * du * du);
+        if (t == 1) wduv[i] = -wduv[i];
       }
-      acc_edge_jac(a, kK, 1.0, [&](int i, int j) { return Cp[i][j]; });
+      const double wTwduv = 2 * dot3(wuv, wd) + 2 * dot3(wduv, w);
+      for (int b = 0; b < 2; ++b) {
+        const double* ma = b == 0 ? m0a : m1a;
+        const double me = b == 0 ? m0e : m1e;
+        const int p = 2 * b + t;
+        C.iso[p] = r6 * dud * (P1 * me) + r6 * du * (P2 * me);
+        for (int j = 0; j < 3; ++j) {
+          const double S1 = (sw * 2.0 / (du * du) * dx[j]);
+          const double S2 = 2 * (wxj * wd[j]) + 2 * (w[j] * wdxj);
+          C.elr[p][j] = r6 * dud * (P1 * ma[j] + S1 * me) + r6 * du * (P2 * ma[j] + S2 * me);
+          C.lec[p][j] = r6 * dud * (wuv[j] * me) - r6 * r[4 * b + j] + r6 * du * (-wduv[j] * me);
+        }
+        C.eev[p] = r6 * dud * (dot3(wuv, ma) + wTwuv * me) - r6 * r[4 * b + 3] +
+                   r6 * du * (-dot3(wduv, ma) + wTwduv * me);
+      }
     }
+    acc_jac(o, kK, 1.0, C);
     // MDotVDot_D_Vel, subtracted (src/PhysicsCloth.cpp:2342-2577)
-    {
-      double Cv[8][8];
-      for (int t = 0; t < 2; ++t) {
-        const double sw = t == 0 ? -1.0 : 1.0;
+    for (int t = 0; t < 2; ++t) {
+      const double sw = t == 0 ? -1.0 : 1.0;
+      const double wdj = sw * (1.0 / du);
+      const double P1 = -wdj;
+      double wdv[3];
+      for (int i = 0; i < 3; ++i) wdv[i] = (t == 0 ? (1.0 / du) : (-1.0 / du)) * w[i];
+      const double wtwd = 2 * dot3(w, wdv);
+      const double cm = (t == 0 ? -1.0 : 1.0) * (1.0 / 6.0) * rho;
+      for (int b = 0; b < 2; ++b) {
+        const double* ma = b == 0 ? m0a : m1a;
+        const double me = b == 0 ? m0e : m1e;
+        const double f = (b == t) ? 2.0 : 1.0;  // [[2B, B], [B, 2B]] block factor of M_dot
+        const int p = 2 * b + t;
+        C.iso[p] = (1.0 / 6.0) * rho * du * (P1 * me) + (r6 * dud * (f * 1.0) + r6 * du * (f * 0.0));
         for (int j = 0; j < 3; ++j) {
-          const double wdj = sw * (1.0 / du);
-          const double P1 = -wdj, S1 = 2 * (w[j] * wdj);
-          const int col = 4 * t + j;
-          for (int b2 = 0; b2 < 2; ++b2) {
-            const double* ma = b2 == 0 ? m0a : m1a;
-            const double me = b2 == 0 ? m0e : m1e;
-            for (int i = 0; i < 3; ++i)
-              Cv[4 * b2 + i][col] = (1.0 / 6.0) * rho * du * ((i == j) ? P1 * me : 0.0) + Mdot(4 * b2 + i, col);
-            Cv[4 * b2 + 3][col] = (1.0 / 6.0) * rho * du * (P1 * ma[j] + S1 * me) + Mdot(4 * b2 + 3, col);
-          }
+          const double S1 = 2 * (w[j] * wdj);
+          C.elr[p][j] = (1.0 / 6.0) * rho * du * (P1 * ma[j] + S1 * me) +
+                        (r6 * dud * (f * -w[j]) + r6 * du * (f * -wd[j]));
+          C.lec[p][j] = cm * BMm[b][j] + (1.0 / 6.0) * rho * du * (-wdv[j] * me) +
+                        (r6 * dud * (f * -w[j]) + r6 * du * (f * -wd[j]));
         }
-        double wdv[3];
-        for (int i = 0; i < 3; ++i) wdv[i] = (t == 0 ? (1.0 / du) : (-1.0 / du)) * w[i];
-        const double wtwd = 2 * dot3(w, wdv);
-        const double cm = (t == 0 ? -1.0 : 1.0) * (1.0 / 6.0) * rho;
-        const int col = 4 * t + 3;
-        for (int b2 = 0; b2 < 2; ++b2) {
-          const double* ma = b2 == 0 ? m0a : m1a;
-          const double me = b2 == 0 ? m0e : m1e;
-          for (int i = 0; i < 3; ++i)
-            Cv[4 * b2 + i][col] = cm * BMm[b2][i] + (1.0 / 6.0) * rho * du * (-wdv[i] * me) + Mdot(4 * b2 + i, col);
-          Cv[4 * b2 + 3][col] = cm * BMm[b2][3] + (1.0 / 6.0) * rho * du * (-dot3(wdv, ma) + wtwd * me) +
-                                Mdot(4 * b2 + 3, col);
-        }
+        C.eev[p] = cm * BMm[b][3] + (1.0 / 6.0) * rho * du * (-dot3(wdv, ma) + wtwd * me) +
+                   (r6 * dud * (f * wTw) + r6 * du * (f * wTwd));
       }
-      acc_edge_jac(a, kD, -1.0, [&](int i, int j) { return Cv[i][j]; });
     }
+    acc_jac(o, kD, -1.0, C);
   }
+  (void)t3;
 }
 
-// Adds an edge's accumulated contributions into the node rows of n0 and n1.
-YS_HD void edge_scatter(const View& v, int n0, int n1, int k, const EdgeAcc& a) {
-  const int nt = v.ntot;
-  const int nd[2] = {n0, n1};
-  const int du_[2] = {0, k == 0 ? 1 : 0}, dv_[2] = {0, k == 1 ? 1 : 0};
-  for (int fa = 0; fa < 2; ++fa) {
-    const int rn = nd[fa];
-    for (int fb = 0; fb < 2; ++fb) {
-      const int ddu = du_[fb] - du_[fa], ddv = dv_[fb] - dv_[fa];
-      for (int r = 0; r < 4; ++r) {
-        if (r == 3 && !a.in[fa]) continue;
-        for (int c = 0; c < 4; ++c) {
-          if (c == 3 && !a.in[fb]) continue;
-          const double val = a.A[4 * fa + r][4 * fb + c];
-          add_A(v, rn, r, nd[fb], c, k, val, ddu, ddv);
-        }
-      }
-    }
-    for (int r = 0; r < 3; ++r) st(v.B, r, nt, rn) += a.b[4 * fa + r];
-    for (int i = 0; i < 3; ++i) st(v.CL, i, nt, rn) += a.cl[fa][i];
-    if (a.in[fa]) {
-      st(v.B, 3 + k, nt, rn) += a.b[4 * fa + 3];
-      st(v.FE, k, nt, rn) += a.fe[fa];
-      st(v.KEE, k, nt, rn) += a.kee[fa];
-      st(v.DEE, k, nt, rn) += a.dee[fa];
-      for (int i = 0; i < 3; ++i) st(v.CLE, 3 * k + i, nt, rn) += a.cle[fa][i];
-    }
-  }
+// record layout of an edge in the per-element buffer (field-major over the
+// 2 * ntot edge slots: slot = k * ntot + n0)
+YS_HD void edge_store(const View& v, double* buf, int n0, int k, const EdgeOut& o) {
+  const int64_t stride = 2LL * v.ntot, base = (int64_t)k * v.ntot + n0;
+  int f = 0;
+  auto put = [&](double x) { buf[(int64_t)(f++) * stride + base] = x; };
+  for (int p = 0; p < 4; ++p) put(o.llI[p]);
+  for (int p = 0; p < 4; ++p) put(o.llP[p]);
+  for (int i = 0; i < 3; ++i) put(o.d[i]);
+  for (int p = 0; p < 4; ++p) for (int r = 0; r < 3; ++r) put(o.le[p][r]);
+  for (int p = 0; p < 4; ++p) for (int r = 0; r < 3; ++r) put(o.el[p][r]);
+  for (int p = 0; p < 4; ++p) put(o.ee[p]);
+  for (int i = 0; i < 8; ++i) put(o.b[i]);
+  for (int t = 0; t < 2; ++t) { put(o.fe[t]); put(o.kee[t]); put(o.dee[t]); }
+  for (int t = 0; t < 2; ++t) for (int i = 0; i < 3; ++i) put(o.cl[t][i]);
+  for (int t = 0; t < 2; ++t) for (int i = 0; i < 3; ++i) put(o.cle[t][i]);
 }
+// field offsets of the layout above
+constexpr int kE_llI = 0, kE_llP = 4, kE_d = 8, kE_le = 11, kE_el = 23, kE_ee = 35, kE_b = 39, kE_fkd = 47,
+              kE_cl = 53, kE_cle = 59;
 
 // ------------------------------------------------------------ bend element
 struct BendGeom {
@@ -602,133 +557,75 @@ YS_HD void bend_terms(const BendGeom& g, double kb, BendTerms& t) {
   for (int i = 0; i < 3; ++i) { t.L1E1[i] = e1 * a[i]; t.L2E1[i] = e2 * b[i]; }
 }
 
-// Adds A[x(rn)][x(cn)] += -h^2 * blk^T (a dF/dx block, transposed as in
-// To_Sparse_Mat) for a node-node coupling at grid offset (du, dv).
-YS_HD void add_K_LL(const View& v, int rn, int du, int dv, const double blk[3][3], double s) {
-  const int sidx = stencil_index(du, dv);
-  if (sidx < 0) return;  // not reachable for bend and shear offsets; keeps every store in bounds
-  const double mh2 = -(v.h * v.h);
-  for (int r = 0; r < 3; ++r)
-    for (int c = 0; c < 3; ++c) slot(v, YS_SLOT_LL + sidx * 9 + r * 3 + c, rn) += mh2 * (s * blk[c][r]);
-}
+// Bend segment record (one per middle node and yarn direction): the four
+// independent Hessian blocks of Bending_D and its Eulerian couplings, the
+// forces of Bending_F, and the crimp-bending forces / couplings that feed the
+// compression estimate (Crimp_Bending_F/D). The other blocks follow from
+// these as in src/PhysicsCloth.cpp:705-727 and are formed by the gather.
+constexpr int kBendFields = 62;
+constexpr int kB_L11 = 0, kB_L12 = 9, kB_L21 = 18, kB_L22 = 27, kB_L1E1 = 36, kB_L2E1 = 39, kB_E1E1 = 42,
+              kB_Fx1 = 43, kB_Fx2 = 46, kB_Fu2 = 49, kB_cFx1 = 50, kB_cFx2 = 53, kB_cL1E1 = 56, kB_cL2E1 = 59;
 
-// Bending_F / Bending_D on the real nodes (n2, n0, n1) along yarn direction k
-// (k = 0: warp, neighbours at u -+ 1; k = 1: weft, neighbours at v -+ 1).
-YS_HD void bend_element(const View& v, int n2, int n0, int n1, int k, double kb) {
+// Bending_F / Bending_D on the real nodes (src/PhysicsCloth.cpp:579-822) and
+// Crimp_Bending_F / Crimp_Bending_D on the crimp-offset centre lines
+// (src/PhysicsCloth.cpp:824-987) for the segment n2 - n0 - n1 along yarn
+// direction k; written to the bend buffer at slot k * ntot + n0.
+YS_HD void bend_element(const View& v, double* buf, int n2, int n0, int n1, int k, double kb) {
   const int nt = v.ntot;
-  double x2[3], x0[3], x1[3];
-  for (int i = 0; i < 3; ++i) { x2[i] = ld(v.X, i, nt, n2); x0[i] = ld(v.X, i, nt, n0); x1[i] = ld(v.X, i, nt, n1); }
-  BendGeom g;
-  bend_geom(x2, x0, x1, ld(v.UV, k, nt, n1) - ld(v.UV, k, nt, n2), g);
-  BendTerms t;
-  bend_terms(g, kb, t);
-  const bool in2 = (v.flags[n2] & YS_INTERIOR) != 0, in0 = (v.flags[n0] & YS_INTERIOR) != 0,
-             in1 = (v.flags[n1] & YS_INTERIOR) != 0;
-  const double h = v.h, h2 = v.h * v.h, th = g.theta, du = g.du;
-  // forces
-  const double Fu2 = (-kb * th) / (du * du), Fu1 = -1 * Fu2;
-  for (int i = 0; i < 3; ++i) {
-    st(v.B, i, nt, n2) += h * t.Fx2[i];
-    st(v.B, i, nt, n0) += h * (-(t.Fx1[i] + t.Fx2[i]));
-    st(v.B, i, nt, n1) += h * t.Fx1[i];
-  }
-  if (in2) { st(v.B, 3 + k, nt, n2) += h * Fu2; st(v.FE, k, nt, n2) += Fu2; }
-  if (in1) { st(v.B, 3 + k, nt, n1) += h * Fu1; st(v.FE, k, nt, n1) += Fu1; }
-  // Jacobian blocks
-  double L10[3][3], L20[3][3], L01[3][3], L02[3][3], L00[3][3];
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
-      L10[i][j] = -(t.L11[i][j] + t.L12[i][j]);
-      L20[i][j] = -(t.L21[i][j] + t.L22[i][j]);
-      L01[i][j] = -(t.L11[i][j] + t.L21[i][j]);
-      L02[i][j] = -(t.L12[i][j] + t.L22[i][j]);
-    }
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) L00[i][j] = -(L10[i][j] + L20[i][j]);
-  const int su = k == 0 ? 1 : 0, sv = k == 1 ? 1 : 0;  // offset n2 -> n0 -> n1
-  add_K_LL(v, n2, 0, 0, t.L22, 1.0);
-  add_K_LL(v, n2, su, sv, L20, 1.0);
-  add_K_LL(v, n2, 2 * su, 2 * sv, t.L21, 1.0);
-  add_K_LL(v, n0, -su, -sv, L02, 1.0);
-  add_K_LL(v, n0, 0, 0, L00, 1.0);
-  add_K_LL(v, n0, su, sv, L01, 1.0);
-  add_K_LL(v, n1, -2 * su, -2 * sv, t.L12, 1.0);
-  add_K_LL(v, n1, -su, -sv, L10, 1.0);
-  add_K_LL(v, n1, 0, 0, t.L11, 1.0);
-  const double E1E1 = (-2 * kb * (th * th)) / (du * du * du);
-  double L2E2[3], L0E1[3], L0E2[3], E2L2[3], E1L0[3], E2L0[3];
-  for (int i = 0; i < 3; ++i) {
-    L2E2[i] = -t.L2E1[i];
-    L0E1[i] = -(t.L1E1[i] + t.L2E1[i]);
-    L0E2[i] = -L0E1[i];
-    E2L2[i] = -t.L2E1[i];           // E1L2 has the values of L2E1
-    E1L0[i] = -(t.L1E1[i] + t.L2E1[i]);
-    E2L0[i] = -E1L0[i];
-  }
-  if (in2) {
-    for (int r = 0; r < 3; ++r) {
-      slot(v, YS_SLOT_LE_SELF + r * 2 + k, n2) += -h2 * L2E2[r];
-      slot(v, YS_SLOT_EL_SELF + k * 3 + r, n2) += -h2 * E2L2[r];
-    }
-    slot(v, YS_SLOT_EE_SELF + k, n2) += -h2 * E1E1;
-    st(v.KEE, k, nt, n2) += E1E1;
-  }
-  if (in1) {
-    for (int r = 0; r < 3; ++r) {
-      slot(v, YS_SLOT_LE_SELF + r * 2 + k, n1) += -h2 * t.L1E1[r];
-      slot(v, YS_SLOT_EL_SELF + k * 3 + r, n1) += -h2 * t.L1E1[r];
-    }
-    slot(v, YS_SLOT_EE_SELF + k, n1) += -h2 * E1E1;
-    st(v.KEE, k, nt, n1) += E1E1;
-  }
-  // neighbour index of n2 seen from n0 is (-su,-sv), of n1 seen from n0 (su,sv)
-  const int nb_prev = yarn_nbr(-su, -sv), nb_next = yarn_nbr(su, sv);
-  if (in2 && in0) {
-    // F_LE_Pos[find_index(n0, n2)]: A[x(n0)][e(n2)]
-    for (int r = 0; r < 3; ++r) slot(v, YS_SLOT_LE_NBR + nb_prev * 3 + r, n0) += -h2 * L0E2[r];
-    // F_EL_Pos[find_index(n2, n0)]: A[e(n0)][x(n2)] (src/PhysicsCloth.cpp:780-795)
-    for (int c = 0; c < 3; ++c) slot(v, YS_SLOT_EL_NBR + nb_prev * 3 + c, n0) += -h2 * E2L0[c];
-  }
-  if (in0 && in1) {
-    for (int r = 0; r < 3; ++r) slot(v, YS_SLOT_LE_NBR + nb_next * 3 + r, n0) += -h2 * L0E1[r];
-    // F_EL_Pos[find_index(n0, n1)]: A[e(n1)][x(n0)]
-    for (int c = 0; c < 3; ++c) slot(v, YS_SLOT_EL_NBR + nb_prev * 3 + c, n1) += -h2 * E1L0[c];
-  }
-}
-
-// Crimp_Bending_F / Crimp_Bending_D (src/PhysicsCloth.cpp:824-987) on the
-// crimp-offset centre lines; only the compression accumulators are touched.
-YS_HD void crimp_element(const View& v, int n2, int n0, int n1, int k, double kb) {
-  const int nt = v.ntot;
-  const double R = v.cp[v.node_cloth[n0]].R;
-  const double sg = k == 0 ? -1.0 : 1.0;  // warp: x - R n, weft: x + R n
-  double x[3][3];
-  const int nd[3] = {n2, n0, n1};
-  for (int m = 0; m < 3; ++m) {
-    const bool in = (v.flags[nd[m]] & YS_INTERIOR) != 0;
+  const int64_t stride = 2LL * nt, base = (int64_t)k * nt + n0;
+  auto put = [&](int f, double x) { buf[(int64_t)f * stride + base] = x; };
+  {
+    double x2[3], x0[3], x1[3];
+    for (int i = 0; i < 3; ++i) { x2[i] = ld(v.X, i, nt, n2); x0[i] = ld(v.X, i, nt, n0); x1[i] = ld(v.X, i, nt, n1); }
+    BendGeom g;
+    bend_geom(x2, x0, x1, ld(v.UV, k, nt, n1) - ld(v.UV, k, nt, n2), g);
+    BendTerms t;
+    bend_terms(g, kb, t);
     for (int i = 0; i < 3; ++i)
-      x[m][i] = in ? ld(v.X, i, nt, nd[m]) + sg * (R * ld(v.NRM, i, nt, nd[m])) : ld(v.X, i, nt, nd[m]);
+      for (int j = 0; j < 3; ++j) {
+        put(kB_L11 + 3 * i + j, t.L11[i][j]);
+        put(kB_L12 + 3 * i + j, t.L12[i][j]);
+        put(kB_L21 + 3 * i + j, t.L21[i][j]);
+        put(kB_L22 + 3 * i + j, t.L22[i][j]);
+      }
+    for (int i = 0; i < 3; ++i) {
+      put(kB_L1E1 + i, t.L1E1[i]);
+      put(kB_L2E1 + i, t.L2E1[i]);
+      put(kB_Fx1 + i, t.Fx1[i]);
+      put(kB_Fx2 + i, t.Fx2[i]);
+    }
+    const double th = g.theta, du = g.du;
+    put(kB_E1E1, (-2 * kb * (th * th)) / (du * du * du));
+    put(kB_Fu2, (-kb * th) / (du * du));
   }
-  // crimp segments keep the EPos of the build (src/Cloth.cpp:107)
-  BendGeom g;
-  bend_geom(x[0], x[1], x[2], ld(v.UV0, k, nt, n1) - ld(v.UV0, k, nt, n2), g);
-  BendTerms t;
-  bend_terms(g, kb, t);
-  const double sgn = (k == 0) ? 1.0 : -1.0;
-  for (int i = 0; i < 3; ++i) {
-    st(v.CL, i, nt, n2) += sgn * t.Fx2[i];
-    st(v.CL, i, nt, n0) += sgn * (-(t.Fx1[i] + t.Fx2[i]));
-    st(v.CL, i, nt, n1) += sgn * t.Fx1[i];
+  {
+    const double R = v.cp[v.node_cloth[n0]].R;
+    const double sg = k == 0 ? -1.0 : 1.0;  // warp: x - R n, weft: x + R n
+    double x[3][3];
+    const int nd[3] = {n2, n0, n1};
+    for (int m = 0; m < 3; ++m) {
+      const bool in = (v.flags[nd[m]] & YS_INTERIOR) != 0;
+      for (int i = 0; i < 3; ++i)
+        x[m][i] = in ? ld(v.X, i, nt, nd[m]) + sg * (R * ld(v.NRM, i, nt, nd[m])) : ld(v.X, i, nt, nd[m]);
+    }
+    // crimp segments keep the EPos of the build (src/Cloth.cpp:107)
+    BendGeom g;
+    bend_geom(x[0], x[1], x[2], ld(v.UV0, k, nt, n1) - ld(v.UV0, k, nt, n2), g);
+    BendTerms t;
+    bend_terms(g, kb, t);
+    for (int i = 0; i < 3; ++i) {
+      put(kB_cFx1 + i, t.Fx1[i]);
+      put(kB_cFx2 + i, t.Fx2[i]);
+      put(kB_cL1E1 + i, t.L1E1[i]);
+      put(kB_cL2E1 + i, t.L2E1[i]);
+    }
   }
-  if (v.flags[n2] & YS_INTERIOR)
-    for (int i = 0; i < 3; ++i) st(v.CLE, 3 * k + i, nt, n2) += sgn * (-t.L2E1[i]);
-  if (v.flags[n1] & YS_INTERIOR)
-    for (int i = 0; i < 3; ++i) st(v.CLE, 3 * k + i, nt, n1) += sgn * t.L1E1[i];
 }
 
 // ------------------------------------------------------------ wind (faces)
-// Wind_F (src/PhysicsCloth.cpp:3091-3107), face geometry src/ClothUnit.h:268-273.
-YS_HD void wind_face(const View& v, const ClothParams& P, int n1, int n2, int n3) {
+// Wind_F (src/PhysicsCloth.cpp:3091-3107), face geometry src/ClothUnit.h:268-273;
+// returns wind_force / 3, the share of each of the face's three nodes.
+YS_HD void wind_face(const View& v, const ClothParams& P, int n1, int n2, int n3, double* f3) {
   const int nt = v.ntot;
   double e1[3], e2[3], cr[3], n[3], fv[3], rel[3];
   for (int i = 0; i < 3; ++i) {
@@ -746,9 +643,26 @@ YS_HD void wind_face(const View& v, const ClothParams& P, int n1, int n2, int n3
   for (int i = 0; i < 3; ++i) {
     const double tang = rel[i] - vn * n[i];
     const double f = P.wind_rho * area * fabs(vn) * vn * n[i] + P.wind_drag * area * tang;
-    st(v.B, i, nt, n1) += v.h * (f / 3.0);
-    st(v.B, i, nt, n2) += v.h * (f / 3.0);
-    st(v.B, i, nt, n3) += v.h * (f / 3.0);
+    f3[i] = f / 3.0;
+  }
+}
+
+// cell with top-left node tl: faces (src/Cloth.cpp:271-287) written to the
+// face buffer [6][ntot] (face A then face B, each wind_force / 3)
+YS_HD void cell_faces(const View& v, double* buf, int tl) {
+  const ClothParams& P = v.cp[v.node_cloth[tl]];
+  const int tr = tl + 1, bl = tl + P.W, br = tl + P.W + 1;
+  double fa[3], fb[3];
+  if (((v.node_u[tl] + v.node_v[tl]) & 1) == 0) {
+    wind_face(v, P, tl, tr, br, fa);
+    wind_face(v, P, tl, br, bl, fb);
+  } else {
+    wind_face(v, P, tl, tr, bl, fa);
+    wind_face(v, P, tr, br, bl, fb);
+  }
+  for (int i = 0; i < 3; ++i) {
+    buf[(int64_t)i * v.ntot + tl] = fa[i];
+    buf[(int64_t)(3 + i) * v.ntot + tl] = fb[i];
   }
 }
 
@@ -821,27 +735,25 @@ YS_HD void node_normal(const View& v, int n, int W) {
   for (int i = 0; i < 3; ++i) st(v.NRM, i, nt, n) = nn[i];
 }
 
-// ConSlideFriction (src/PhysicsCloth.cpp:2579-2641) for interior node n, after
-// every edge and bend term has been accumulated.
-YS_HD void friction_node(const View& v, int n) {
+// ConSlideFriction (src/PhysicsCloth.cpp:2579-2641) for interior node n from
+// its gathered no-slide force fe, dF_E/dE diagonals kee / dee and the crimp
+// compression sums cl / cle; returns the A and b contributions of the E rows
+// and stores COMP and SLIDE.
+YS_HD void friction_node(const View& v, int n, const double* fe, const double* kee, const double* dee,
+                         const double* cl, const double* cle, double* aEE, double* bE) {
   const int nt = v.ntot;
   const ClothParams& P = v.cp[v.node_cloth[n]];
-  double nrm[3], cl[3], cleu[3], clev[3];
-  for (int i = 0; i < 3; ++i) {
-    nrm[i] = ld(v.NRM, i, nt, n);
-    cl[i] = ld(v.CL, i, nt, n);
-    cleu[i] = ld(v.CLE, i, nt, n);
-    clev[i] = ld(v.CLE, 3 + i, nt, n);
-  }
+  double nrm[3];
+  for (int i = 0; i < 3; ++i) nrm[i] = ld(v.NRM, i, nt, n);
   double comp = 0.5 * dot3(nrm, cl);
   if (comp < 0) comp = 0.0;
-  const double compEE[2] = {0.5 * dot3(nrm, cleu), 0.5 * dot3(nrm, clev)};
+  const double compEE[2] = {0.5 * dot3(nrm, cle), 0.5 * dot3(nrm, cle + 3)};
   st(v.COMP, 0, nt, n) = comp;
   const double mu = P.mu, kf = P.kf, df = P.df, h = v.h, h2 = v.h * v.h;
   const double lim = 1.0 * comp * mu;
   for (int k = 0; k < 2; ++k) {
     const double uvm = ld(v.UV, k, nt, n) - ld(v.UVB, k, nt, n);
-    const double FEns = ld(v.FE, k, nt, n), EEp = ld(v.KEE, k, nt, n), EEv = ld(v.DEE, k, nt, n);
+    const double FEns = fe[k], EEp = kee[k], EEv = dee[k];
     const double slide = 1.0 / (1.0 + exp(-(1e4 * (fabs(FEns) - lim))));
     const double t = tanh(10 * uvm), tl = tanh(10 * (lim - FEns));
     const double uvdot = ld(v.UVD, k, nt, n);
@@ -853,15 +765,28 @@ YS_HD void friction_node(const View& v, int n) {
     const double tq = tanh(10 * lim - FEns);
     const double vel = (-0.5 * (kf * uvm - t * mu * comp)) * (1.0 - tq * tq) * EEv - df;
     st(v.SLIDE, k, nt, n) = slide;
-    slot(v, YS_SLOT_EE_SELF + k, n) += -h2 * pos - h * vel;
-    st(v.B, 3 + k, nt, n) += h * (force - vel * uvdot);
+    aEE[k] = -h2 * pos - h * vel;
+    bE[k] = h * (force - vel * uvdot);
   }
 }
 
 // ------------------------------------------------------------ shear
+// Shear segment record (one per crossing and segment type): the forces on the
+// warp and weft neighbours and the four independent Hessian blocks; the
+// crossing's own force and blocks follow from them (src/PhysicsCloth.cpp:2710,
+// 3033-3037) and are formed by the gather.
+constexpr int kShearFields = 42;
+constexpr int kS_F1 = 0, kS_F3 = 3, kS_J11 = 6, kS_J13 = 15, kS_J31 = 24, kS_J33 = 33;
+// segment types in the order of src/Cloth.cpp:178-181: (warp, weft) offsets
+YS_HD int shear_du(int seg) { return seg < 2 ? -1 : 1; }
+YS_HD int shear_dv(int seg) { return (seg & 1) ? -1 : 1; }
+
 // Shear_F / Shear_D (src/PhysicsCloth.cpp:2643-3089) for crossing n0 with warp
-// neighbour n1 (grid offset (s1u, 0)) and weft neighbour n3 (offset (0, s3v)).
-YS_HD void shear_element(const View& v, const ClothParams& P, int n0, int n1, int n3, int s1u, int s3v) {
+// neighbour n1 = n0 + (shear_du, 0) and weft neighbour n3 = n0 + (0, shear_dv),
+// written to the shear buffer at slot seg * ntot + n0.
+YS_HD void shear_element(const View& v, double* buf, int n0, int seg) {
+  const ClothParams& P = v.cp[v.node_cloth[n0]];
+  const int n1 = n0 + shear_du(seg), n3 = n0 + shear_dv(seg) * P.W;
   const int nt = v.ntot;
   const double Lc = P.L, R = P.R, S = P.S;
   const double comp = ld(v.COMP, 0, nt, n0);
@@ -1011,32 +936,15 @@ YS_HD void shear_element(const View& v, const ClothParams& P, int n0, int n1, in
         }
     }
   }
-  const double h = v.h;
-  for (int i = 0; i < 3; ++i) {
-    const double Fx0 = -1 * (Fx1[i] + Fx3[i]);
-    st(v.B, i, nt, n0) += h * Fx0;
-    st(v.B, i, nt, n1) += h * Fx1[i];
-    st(v.B, i, nt, n3) += h * Fx3[i];
-  }
-  double J10[3][3], J30[3][3], J01[3][3], J03[3][3], J00[3][3];
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
-      J10[i][j] = -(J11[i][j] + J13[i][j]);
-      J30[i][j] = -(J31[i][j] + J33[i][j]);
-      J01[i][j] = -(J11[i][j] + J31[i][j]);
-      J03[i][j] = -(J13[i][j] + J33[i][j]);
-    }
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) J00[i][j] = -(J10[i][j] + J30[i][j]);
-  add_K_LL(v, n0, 0, 0, J00, 1.0);
-  add_K_LL(v, n0, s1u, 0, J01, 1.0);
-  add_K_LL(v, n0, 0, s3v, J03, 1.0);
-  add_K_LL(v, n1, -s1u, 0, J10, 1.0);
-  add_K_LL(v, n1, 0, 0, J11, 1.0);
-  add_K_LL(v, n1, -s1u, s3v, J13, 1.0);
-  add_K_LL(v, n3, 0, -s3v, J30, 1.0);
-  add_K_LL(v, n3, s1u, -s3v, J31, 1.0);
-  add_K_LL(v, n3, 0, 0, J33, 1.0);
+  const int64_t stride = 4LL * nt, base = (int64_t)seg * nt + n0;
+  int f = 0;
+  auto put = [&](double x) { buf[(int64_t)(f++) * stride + base] = x; };
+  for (int i = 0; i < 3; ++i) put(Fx1[i]);
+  for (int i = 0; i < 3; ++i) put(Fx3[i]);
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) put(J11[i][j]);
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) put(J13[i][j]);
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) put(J31[i][j]);
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) put(J33[i][j]);
 }
 
 }  // namespace ys

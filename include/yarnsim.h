@@ -138,20 +138,19 @@ ys_status ys_synchronize(ys_batch *b);
 /* Kernel accounting (no counterpart in the reference). Kernel classes: */
 enum {
   YS_PROF_GEOM = 0,      /* node normals */
-  YS_PROF_CLEAR = 1,     /* zero the step's system */
-  YS_PROF_EDGES = 2,     /* edge terms (mass, gravity, stretch, inertia, dM/dt, contact) */
-  YS_PROF_BENDS = 3,     /* bending + crimp */
-  YS_PROF_FACES = 4,     /* wind */
-  YS_PROF_FRICTION = 5,  /* sliding friction */
-  YS_PROF_SHEAR = 6,     /* shear (with jamming) */
-  YS_PROF_FINALIZE = 7,  /* handles, external force, Jacobi diagonal, finite check */
-  YS_PROF_PCG_SETUP = 8,
-  YS_PROF_SPMV = 9,      /* stencil SpMV q = A p (+ p.q) */
-  YS_PROF_AXPY = 10,     /* x, r update (+ r.r, r.z) */
-  YS_PROF_DIR = 11,      /* stop test, p update */
-  YS_PROF_UPDATE = 12,   /* Cloth::update */
-  YS_PROF_MISC = 13,     /* bookkeeping */
-  YS_PROF_KINDS = 14
+  YS_PROF_EDGES = 1,     /* edge records (mass, gravity, stretch, inertia, dM/dt, contact) */
+  YS_PROF_BENDS = 2,     /* bend + crimp records */
+  YS_PROF_FACES = 3,     /* wind records */
+  YS_PROF_GATHER = 4,    /* row blocks from edge/bend/face records + sliding friction */
+  YS_PROF_SHEAR = 5,     /* shear records (with jamming) */
+  YS_PROF_FINALIZE = 6,  /* shear into row blocks, handles, external force, Jacobi, finite check */
+  YS_PROF_PCG_SETUP = 7,
+  YS_PROF_SPMV = 8,      /* stencil SpMV q = A p (+ p.q) */
+  YS_PROF_AXPY = 9,      /* x, r update (+ r.r, r.z) */
+  YS_PROF_DIR = 10,      /* stop test, p update */
+  YS_PROF_UPDATE = 11,   /* Cloth::update */
+  YS_PROF_MISC = 12,     /* bookkeeping */
+  YS_PROF_KINDS = 13
 };
 /* enable = 1 brackets every launch with CUDA events on the handle's stream
  * (adds a little host overhead); the totals accumulate until read. */

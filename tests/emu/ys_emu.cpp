@@ -21,8 +21,10 @@ struct Emu {
   std::vector<int> node_cloth, node_u, node_v;
   std::vector<uint8_t> flags;
   std::vector<double> rho, ks, kb;
-  std::vector<double> X, V, XF, UV, UVD, UVB, UV0, NRM, COMP, SLIDE, A, B, CL, CLE, FE, KEE, DEE, EXT, DINV, SOL;
+  std::vector<double> X, V, XF, UV, UVD, UVB, UV0, NRM, COMP, SLIDE, A, B, EXT, DINV, SOL;
+  std::vector<double> RE, RB, RF, RS;  // element records
   ys::View v{};
+  ys::Records R{};
   int bad = 0;
 
   void bind() {
@@ -33,8 +35,8 @@ struct Emu {
     v.line_rho = rho.data(); v.line_ks = ks.data(); v.line_kb = kb.data();
     v.X = X.data(); v.V = V.data(); v.XF = XF.data(); v.UV = UV.data(); v.UVD = UVD.data(); v.UVB = UVB.data();
     v.UV0 = UV0.data(); v.NRM = NRM.data(); v.COMP = COMP.data(); v.SLIDE = SLIDE.data();
-    v.A = A.data(); v.B = B.data(); v.CL = CL.data(); v.CLE = CLE.data(); v.FE = FE.data(); v.KEE = KEE.data();
-    v.DEE = DEE.data();
+    v.A = A.data(); v.B = B.data();
+    R.edge = RE.data(); R.bend = RB.data(); R.face = RF.data(); R.shear = RS.data();
   }
 };
 
@@ -74,8 +76,8 @@ void* emu_create(const ys_cloth_desc* d) {
   }
   auto Z = [&](std::vector<double>& a, int c) { a.assign((size_t)c * N, 0.0); };
   Z(e->X, 3); Z(e->V, 3); Z(e->XF, 3); Z(e->UV, 2); Z(e->UVD, 2); Z(e->UVB, 2); Z(e->UV0, 2); Z(e->NRM, 3);
-  Z(e->COMP, 1); Z(e->SLIDE, 2); Z(e->A, ys::YS_NUM_SLOTS); Z(e->B, 5); Z(e->CL, 3); Z(e->CLE, 6); Z(e->FE, 2);
-  Z(e->KEE, 2); Z(e->DEE, 2); Z(e->EXT, 5); Z(e->DINV, 5); Z(e->SOL, 5);
+  Z(e->COMP, 1); Z(e->SLIDE, 2); Z(e->A, ys::YS_NUM_SLOTS); Z(e->B, 5); Z(e->EXT, 5); Z(e->DINV, 5); Z(e->SOL, 5);
+  Z(e->RE, ys::kEdgeFields * 2); Z(e->RB, ys::kBendFields * 2); Z(e->RF, 6); Z(e->RS, ys::kShearFields * 4);
   std::vector<uint8_t> fixed(N, 0);
   for (int h = 0; h < d->n_handles; ++h) fixed[d->handles[2 * h] + d->handles[2 * h + 1] * W] = 1;
   for (int j = 0; j < H; ++j)
@@ -136,42 +138,33 @@ void emu_assemble(void* h, double dt, const double* ext /* [N][5] or null */) {
     v.ext = e->EXT.data();
   }
   for (int j = 1; j < H - 1; ++j) for (int i = 1; i < W - 1; ++i) ys::node_normal(v, i + j * W, W);
-  for (int n = 0; n < N; ++n) ys::clear_node(v, n);
-  for (int c = 0; c < 2; ++c)
-    for (int j = 0; j < H; ++j) for (int i = 0; i < W - 1; ++i) if ((i & 1) == c) {
-      ys::EdgeAcc a; const int n0 = i + j * W;
-      ys::edge_terms(v, n0, n0 + 1, 0, a); ys::edge_scatter(v, n0, n0 + 1, 0, a);
+  // element records, then the two gathers (same order as ys_assemble)
+  for (int k = 0; k < 2; ++k)
+    for (int n = 0; n < N; ++n) {
+      const int i = n % W, j = n / W;
+      if (k == 0 ? i >= W - 1 : j >= H - 1) continue;
+      ys::EdgeOut o;
+      ys::edge_element(v, n, n + (k == 0 ? 1 : W), k, o);
+      ys::edge_store(v, e->R.edge, n, k, o);
     }
-  for (int c = 0; c < 2; ++c)
-    for (int j = 0; j < H - 1; ++j) for (int i = 0; i < W; ++i) if ((j & 1) == c) {
-      ys::EdgeAcc a; const int n0 = i + j * W;
-      ys::edge_terms(v, n0, n0 + W, 1, a); ys::edge_scatter(v, n0, n0 + W, 1, a);
+  for (int k = 0; k < 2; ++k)
+    for (int n = 0; n < N; ++n) {
+      const int i = n % W, j = n / W;
+      const int pos = k == 0 ? i : j, len = k == 0 ? W : H;
+      if (pos < 1 || pos > len - 2) continue;
+      const int step = k == 0 ? 1 : W;
+      const double kb = k == 0 ? e->kb[j] : e->kb[H + i];
+      ys::bend_element(v, e->R.bend, n - step, n, n + step, k, kb);
     }
-  for (int c = 0; c < 3; ++c)
-    for (int j = 0; j < H; ++j) for (int i = 1; i < W - 1; ++i) if (i % 3 == c) {
-      const int n0 = i + j * W; const double kb = e->kb[j];
-      ys::bend_element(v, n0 - 1, n0, n0 + 1, 0, kb); ys::crimp_element(v, n0 - 1, n0, n0 + 1, 0, kb);
-    }
-  for (int c = 0; c < 3; ++c)
-    for (int j = 1; j < H - 1; ++j) for (int i = 0; i < W; ++i) if (j % 3 == c) {
-      const int n0 = i + j * W; const double kb = e->kb[H + i];
-      ys::bend_element(v, n0 - W, n0, n0 + W, 1, kb); ys::crimp_element(v, n0 - W, n0, n0 + W, 1, kb);
-    }
-  for (int j = 0; j < H - 1; ++j) for (int i = 0; i < W - 1; ++i) {
-    const int tl = i + j * W, tr = tl + 1, bl = tl + W, br = tl + W + 1;
-    if (((i + j) & 1) == 0) { ys::wind_face(v, e->P, tl, tr, br); ys::wind_face(v, e->P, tl, br, bl); }
-    else { ys::wind_face(v, e->P, tl, tr, bl); ys::wind_face(v, e->P, tr, br, bl); }
-  }
-  for (int j = 1; j < H - 1; ++j) for (int i = 1; i < W - 1; ++i) ys::friction_node(v, i + j * W);
-  for (int j = 1; j < H - 1; ++j) for (int i = 1; i < W - 1; ++i) {
-    const int n = i + j * W;
-    ys::shear_element(v, e->P, n, n - 1, n + W, -1, 1);
-    ys::shear_element(v, e->P, n, n - 1, n - W, -1, -1);
-    ys::shear_element(v, e->P, n, n + 1, n + W, 1, 1);
-    ys::shear_element(v, e->P, n, n + 1, n - W, 1, -1);
-  }
+  for (int n = 0; n < N; ++n)
+    if (n % W < W - 1 && n / W < H - 1) ys::cell_faces(v, e->R.face, n);
+  for (int n = 0; n < N; ++n) ys::gather_elements(v, e->R, n);
+  for (int seg = 0; seg < 4; ++seg)
+    for (int n = 0; n < N; ++n)
+      if (e->flags[n] & ys::YS_INTERIOR) ys::shear_element(v, e->R.shear, n, seg);
   e->bad = 0;
-  for (int n = 0; n < N; ++n) if (!ys::finalize_node(v, n, e->DINV.data())) e->bad = 1;
+  for (int n = 0; n < N; ++n)
+    if (!ys::gather_shear_finalize(v, e->R, n, e->DINV.data())) e->bad = 1;
 }
 
 // raw slots [159][N] and rhs [5][N]
