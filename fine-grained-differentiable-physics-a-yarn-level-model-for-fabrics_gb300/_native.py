@@ -20,7 +20,7 @@ EXPORTED = [
     "ys_last_error", "ys_batch_create", "ys_batch_destroy", "ys_batch_get_info", "ys_cloth_node_offset",
     "ys_cloth_dim", "ys_set_state", "ys_get_state", "ys_set_wind", "ys_set_winds", "ys_assemble", "ys_export_system",
     "ys_solve", "ys_get_solution", "ys_step", "ys_apply_system", "ys_synchronize", "ys_profile",
-    "ys_profile_read",
+    "ys_profile_read", "ys_apply_system_noalloc",
 ]
 PROF_KINDS = ["geom", "edges", "bends", "faces", "gather", "shear", "finalize", "pcg_setup", "spmv", "axpy", "dir",
               "update", "misc"]
@@ -97,6 +97,7 @@ def load(build_if_missing: bool = True):
     L.ys_step.argtypes = [vp, ctypes.c_double, vp, ctypes.c_int32, ctypes.POINTER(SolveOpts),
                           ctypes.POINTER(ClothStats)]
     L.ys_apply_system.argtypes = [vp, vp, vp, ctypes.c_int32]
+    L.ys_apply_system_noalloc.argtypes = [vp, vp, vp]
     L.ys_synchronize.argtypes = [vp]
     L.ys_profile.argtypes = [vp, ctypes.c_int32]
     L.ys_profile_read.argtypes = [vp, _dp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),

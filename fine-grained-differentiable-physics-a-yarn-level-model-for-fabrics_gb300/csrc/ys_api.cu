@@ -671,3 +671,80 @@ ys_status ys_synchronize(ys_batch* b) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------- y = A x without allocation
+//
+// ys_apply_system_noalloc is a variant of ys_apply_system for callers that
+// must not allocate at call time: a host program whose device memory is
+// entirely owned by another allocator (a framework's caching pool sized to
+// the device, so a cudaMalloc here could fail or fragment it), and a control
+// loop that cannot afford the device-wide synchronisation cudaMalloc and
+// cudaFree may imply. It launches two kernels and allocates nothing: no
+// cudaMalloc / cudaFree, no pinned memory, no events, no library routine that
+// allocates. Its only working memory is the file-scope array below, and it
+// writes no buffer of the batch (ys_apply_system writes two PCG work vectors).
+//
+// Nothing in the scratch needs to start at zero: the first kernel writes all
+// 5 * total_nodes entries that the second kernel reads, in the same call.
+//
+// The scratch is one array per device shared by every batch and thread, so
+// calls that overlap in time on one device race on it: two calls on
+// different streams, or from different host threads without ordering, give
+// wrong results. Issue them on one stream, or order them by the caller.
+namespace {
+
+constexpr int64_t kNoAllocMaxNodes = 65536;  // 5 * 65,536 doubles = 2.5 MiB per device
+static __device__ __align__(256) double g_noalloc_scratch[5 * kNoAllocMaxNodes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+
+// y[n][k] = (A x)[n][k] with x read from the component-major scratch copy;
+// same row arithmetic as k_spmv_plain, written node-major.
+__global__ void k_spmv_scratch_to_aos(ys::View v, const double* __restrict__ xs, double* __restrict__ y) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.ntot) return;
+  double r[5];
+  ys::spmv_row(v, xs, n, r);
+  for (int k = 0; k < 5; ++k) y[(int64_t)n * 5 + k] = r[k];
+}
+
+// One-time set-up per device, run with that device current: the address of
+// this device's copy of the scratch array. The first call on a device may
+// make the runtime load this module there; make that first call before any
+// stream capture begins.
+ys_status noalloc_scratch(int device, double** out) {
+  if (device < 0 || device >= kNoAllocMaxDevices) return fail(YS_ERR_ARG, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      return fail(YS_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    g_noalloc_ptr[device] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[device];
+  return YS_OK;
+}
+
+}  // namespace
+
+extern "C" ys_status ys_apply_system_noalloc(ys_batch* b, const double* x, double* y) {
+  if (!b || !x || !y) return fail(YS_ERR_ARG, "bad argument");
+  if (!b->assembled) return fail(YS_ERR_ARG, "no assembled system");
+  if (b->ntot > kNoAllocMaxNodes)
+    return fail(YS_ERR_ARG, "ys_apply_system_noalloc: batch has " + std::to_string(b->ntot) +
+                                " nodes, more than its scratch limit of " + std::to_string(kNoAllocMaxNodes));
+  YS_CUDA(cudaSetDevice(b->device));
+  double* xs = nullptr;
+  const ys_status s = noalloc_scratch(b->device, &xs);
+  if (s != YS_OK) return s;
+  const int64_t n = b->ntot;
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  k_to_soa<<<grid, 256, 0, b->stream>>>(x, xs, n, 5);
+  k_spmv_scratch_to_aos<<<grid, 256, 0, b->stream>>>(b->v, xs, y);
+  b->launches += 2;
+  YS_CUDA(cudaGetLastError());
+  return YS_OK;
+}

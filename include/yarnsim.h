@@ -132,6 +132,17 @@ ys_status ys_step(ys_batch *b, double h, const double *ext_force, int32_t flags,
                   ys_cloth_stats *stats);
 /* y = A x with the assembled matrices (node layout [total_nodes][5]). */
 ys_status ys_apply_system(ys_batch *b, const double *x, double *y, int32_t flags);
+/* y = A x like ys_apply_system, for callers that must not allocate at call
+ * time (device memory owned by another allocator; loops that cannot take the
+ * synchronisation an allocation may imply). No counterpart in the reference.
+ * x and y are DEVICE pointers in node layout [total_nodes][5]; the call is
+ * asynchronous on the handle's stream. It allocates nothing and writes no
+ * buffer of the batch: its working memory is one static per-device scratch
+ * array holding at most 65,536 nodes (YS_ERR_ARG above that). Nothing in the
+ * scratch needs to start at zero. Calls that overlap in time on one device
+ * share that scratch and race. The first call on a device does a one-time
+ * set-up (symbol lookup); make it before any stream capture begins. */
+ys_status ys_apply_system_noalloc(ys_batch *b, const double *x, double *y);
 /* Waits for the handle's stream. */
 ys_status ys_synchronize(ys_batch *b);
 
