@@ -809,9 +809,6 @@ YS_HD void shear_element(const View& v, double* buf, int n0, int seg) {
   const bool jam = (((f0 & YS_FLIP) != 0) != ((f1 & YS_FLIP) != 0)) && (((f0 & YS_FLIP) != 0) != ((f3 & YS_FLIP) != 0));
   double Fx1[3], Fx3[3], J11[3][3], J13[3][3], J31[3][3], J33[3][3];
   const double cs2 = co / (s * s), is = 1 / s;
-  double a3d1[3][3], d1a3[3][3], a3a3[3][3], a1d3[3][3], d3a1[3][3], a1a1[3][3];
-  outer3(a3, d1, a3d1); outer3(d1, a3, d1a3); outer3(a3, a3, a3a3);
-  outer3(a1, d3, a1d3); outer3(d3, a1, d3a1); outer3(a1, a1, a1a1);
   if (!jam) {
     const double kx = (comp + 1.0) * S * R * R * kPi;
     const double ph = phi - kPi / 2;
@@ -819,22 +816,23 @@ YS_HD void shear_element(const View& v, double* buf, int n0, int seg) {
     for (int i = 0; i < 3; ++i) { Fx1[i] = cf1 * a3[i]; Fx3[i] = cf3 * a1[i]; }
     const double k11 = (kx * Lc) / ((l1 * l1) * s), k33 = (kx * Lc) / ((l3 * l3) * s);
     const double k13 = (kx * Lc) / (l3 * l1 * s), k31 = (kx * Lc) / (l1 * l3 * s);
-    double T[3][3];
-    for (int i = 0; i < 3; ++i)
+    // src/PhysicsCloth.cpp:2715-2751 per block:
+    //   J11 = k11 (ph (-a3 d1^T + cs2 a3 a3^T - co P1 - d1 a3^T) - a3 a3^T / s)
+    //   J13 = k13 ph (cs2 - 1/s) (a3 d1^T) P3 = k13 ph (cs2 - 1/s) a3 a1^T, as a1 = P3 d1
+    // (J33, J31 likewise with 1 <-> 3)
+    const double kA1 = k11 * (ph * cs2 - is), kS1 = -k11 * ph, kP1 = kS1 * co;
+    const double kA3 = k33 * (ph * cs2 - is), kS3 = -k33 * ph, kP3 = kS3 * co;
+    const double kx13 = k13 * ph * (cs2 - is), kx31 = k31 * ph * (cs2 - is);
+    for (int i = 0; i < 3; ++i) {
+      const double al1 = kA1 * a3[i] + kS1 * d1[i], be1 = kS1 * a3[i];
+      const double al3 = kA3 * a1[i] + kS3 * d3[i], be3 = kS3 * a1[i];
       for (int j = 0; j < 3; ++j) {
-        J11[i][j] = k11 * (ph * (-1 * a3d1[i][j] + cs2 * a3a3[i][j] - co * P1[i][j] - d1a3[i][j]) - is * a3a3[i][j]);
-        J33[i][j] = k33 * (ph * (-1 * a1d3[i][j] + cs2 * a1a1[i][j] - co * P3[i][j] - d3a1[i][j]) - is * a1a1[i][j]);
-        T[i][j] = ph * (cs2 * a3d1[i][j] - is * a3d1[i][j]);
+        J11[i][j] = al1 * a3[j] + be1 * d1[j] + kP1 * P1[i][j];
+        J33[i][j] = al3 * a1[j] + be3 * d3[j] + kP3 * P3[i][j];
+        J13[i][j] = kx13 * (a3[i] * a1[j]);
+        J31[i][j] = kx31 * (a1[i] * a3[j]);
       }
-    matmul3(T, P3, J13);
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        J13[i][j] *= k13;
-        T[i][j] = ph * (cs2 * a1d3[i][j] - is * a1d3[i][j]);
-      }
-    matmul3(T, P1, J31);
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) J31[i][j] *= k31;
+    }
   } else {
     // jamming: smooth shear lock (src/PhysicsCloth.cpp:2656-2713, 2753-3031).
     // Every first derivative in those expressions is a multiple of
@@ -873,11 +871,17 @@ YS_HD void shear_element(const View& v, double* buf, int n0, int seg) {
       Fx1[i] = -0.5 * (beta0 + beta1 * px1[i]) * Lc * Bq2 + cf1 * a3[i];
       Fx3[i] = -0.5 * (beta0 + beta1 * px3[i]) * Lc * Bq2 + cf3 * a1[i];
     }
-    // pass-invariant coefficients
-    double P1P3[3][3], P3P1[3][3], e3[3];
-    matmul3(P1, P3, P1P3);
-    matmul3(P3, P1, P3P1);
-    matvec3(P3, d3, e3);  // P3 d3: src/PhysicsCloth.cpp:2775-2777 multiplies outer(P3 d1, d3) by P3
+    // The Hessian entries of src/PhysicsCloth.cpp:2753-3031 are, for each
+    // block, one fixed linear map (scalars below) applied to a few per-entry
+    // quantities: pxx (phi_x_x), O = phi_xa phi_xb^T, Ob = its mirror, Rg
+    // (the gamma_x_x remainder), fo (the kx-constant term), plus the scalar 1
+    // broadcast by "1 - cf^2 cfx" (x1x1, x3x3 only) and kx_x's beta0 (1,1,1)
+    // rows/columns. Those quantities are in turn combinations of a handful of
+    // rank-1 matrices (a3 a3^T, a3 d1^T + d1 a3^T, P1, ...), so each block is
+    // J = sum_k c_k B_k with c_k computed once per block.
+    double P1P3[3][3], e3[3];
+    matmul3(P1, P3, P1P3);  // P3 P1 is its transpose (both projectors symmetric)
+    matvec3(P3, d3, e3);    // P3 d3: src/PhysicsCloth.cpp:2775-2777 multiplies outer(P3 d1, d3) by P3
     const double cfq = -2 * cf * (1 - cf * cf);
     const double c1 = cc * (cc - 1) * gamma, c2 = cc * g2;
     const double base2 = 0.5 * (comp + 1.0) * S * (R * R);
@@ -885,55 +889,77 @@ YS_HD void shear_element(const View& v, double* buf, int n0, int seg) {
     const double kG = c2 * (1 - cf);
     const double cfqm2 = cfq * muc * muc;
     const double X4 = 4 * tau * den * phs * sgm;
-    const double two_num_sgm2 = 2 * num * sgm * sgm, two_num_phs = 2 * num * phs, pb5den = pb5 * den;
+    const double tns2 = 2 * num * sgm * sgm, tnp = 2 * num * phs, pb5den = pb5 * den;
     const double cross = 2 * phs * pb5 * sgm;
     const double hLB2 = 0.5 * Lc * Bq2, LB = Lc * Bq;
     const double kL = kx * Lc;
     const double r11 = 1.0 / ((l1 * l1) * s), r33 = 1.0 / ((l3 * l3) * s), r13 = 1.0 / (l1 * l3 * s);
     const double qR11 = 0.5 * LR * sh / ((l1 * s) * (l1 * s)), qR33 = 0.5 * LR * sh / ((l3 * s) * (l3 * s));
     const double qR13 = 0.5 * LR * sh / (l1 * l3 * (s * s));
-    for (int pass = 0; pass < 4; ++pass) {
-      // pass 0: (x1,x1) 1: (x3,x3) 2: (x1,x3) 3: (x3,x1)
-      const double* pA = (pass == 0 || pass == 2) ? px1 : px3;
-      const double* pB = (pass == 0 || pass == 3) ? px1 : px3;
-      double (*J)[3] = pass == 0 ? J11 : pass == 1 ? J33 : pass == 2 ? J13 : J31;
+    const double rho1 = rl1s * rl1s, rho3 = rl3s * rl3s, rho13 = rl1s * rl3s;
+    // J = cP*pxx + cO*O + cOb*Ob + cR*Rg + fo (+ cOne*1 + row/column terms)
+    const double hb = hLB2 * base2, g3c = 1 - g3;
+    const double cR = -hb * kG;
+    const double cnx_p = pb5den - tnp * sgm;  // nx = cnx_p pxx + ...
+    // x1x1 and x3x3: psx = sgm pxx + omg O, cfdd = cfqm2 O + 1 - cf^2 cfx
+    const double eD = -cf * cf;
+    const double cPd = -hb * (kG * kap + g3c * eD * rden2 * cnx_p);
+    const double cOd = -hb * (kO + g3c * (eD * (rden2 * (-tns2 - tnp * omg) - rden22 * X4) + cfqm2)) - 2 * LB * beta1;
+    const double cOne = -hb * g3c;
+    // x1x3 (psx = sgm pxx + omg (O + Ob) / 2) and x3x1 (psx = sgm pxx + omg O);
+    // both: nx += cross (O - Ob), cfdd = cfqm2 Ob + (1 - cf^2) cfx
+    const double eX = 1 - cf * cf;
+    const double cPx = -hb * (kG * kap + g3c * eX * rden2 * cnx_p);
+    const double cO13 = -hb * (kO + g3c * eX * (rden2 * (-tns2 - tnp * 0.5 * omg + cross) - rden22 * X4)) -
+                        2 * LB * beta1;
+    const double cOb13 = -hb * g3c * (eX * rden2 * (-tnp * 0.5 * omg - cross) + cfqm2);
+    const double cO31 = -hb * (kO + g3c * eX * (rden2 * (-tns2 - tnp * omg + cross) - rden22 * X4)) - 2 * LB * beta1;
+    const double cOb31 = -hb * g3c * (eX * rden2 * (-cross) + cfqm2);
+    const double kq = Bq * cs2 - is;
+    // x1x1: pxx = r11 (S - cs2 A + co P1), O = Ob = rho1 A, Rg = qR11 A,
+    //       fo = kL r11 (-Bq S + kq A - Bq co P1); A = a3 a3^T, S = a3 d1^T + d1 a3^T
+    {
+      const double kA = cPd * (-cs2 * r11) + cOd * rho1 + cR * qR11 + kL * r11 * kq;
+      const double kS = (cPd - kL * Bq) * r11;
+      const double kP = (cPd - kL * Bq) * r11 * co;
+      for (int i = 0; i < 3; ++i) {
+        const double al = kA * a3[i] + kS * d1[i], be = kS * a3[i];
+        for (int j = 0; j < 3; ++j)
+          J11[i][j] = al * a3[j] + be * d1[j] + kP * P1[i][j] + (cOne - 2 * LB * beta0 * px1[j]);
+      }
+    }
+    // x3x3: the same with (a1, d3, P3, r33, qR33, rho3, px3)
+    {
+      const double kA = cPd * (-cs2 * r33) + cOd * rho3 + cR * qR33 + kL * r33 * kq;
+      const double kS = (cPd - kL * Bq) * r33;
+      const double kP = (cPd - kL * Bq) * r33 * co;
+      for (int i = 0; i < 3; ++i) {
+        const double al = kA * a1[i] + kS * d3[i], be = kS * a1[i];
+        for (int j = 0; j < 3; ++j)
+          J33[i][j] = al * a1[j] + be * d3[j] + kP * P3[i][j] + (cOne - 2 * LB * beta0 * px3[j]);
+      }
+    }
+    // x1x3: pxx = -r13 (cs2 A + M), O = rho13 A, Ob = rho13 B, Rg = qR13 A,
+    //       fo = kL r13 (kq A + Bq M); A = a3 a1^T, B = a1 a3^T, M = P1 P3
+    {
+      const double kA = -cPx * r13 * cs2 + cO13 * rho13 + cR * qR13 + kL * r13 * kq;
+      const double kB = cOb13 * rho13;
+      const double kM = (-cPx + kL * Bq) * r13;
       for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-          const double O = pA[i] * pB[j], Ob = pB[i] * pA[j];
-          double pxx, Rg, fo;
-          if (pass == 0) {
-            const double aa = a3[i] * a3[j];
-            pxx = (a3[i] * d1[j] + d1[i] * a3[j] - cs2 * aa + co * P1[i][j]) * r11;
-            Rg = qR11 * aa;
-            fo = (kL * r11) * (Bq * (-(a3[i] * d1[j]) + cs2 * aa - co * P1[i][j] - d1[i] * a3[j]) - is * aa);
-          } else if (pass == 1) {
-            const double aa = a1[i] * a1[j];
-            pxx = (a1[i] * d3[j] + d3[i] * a1[j] - cs2 * aa + co * P3[i][j]) * r33;
-            Rg = qR33 * aa;
-            fo = (kL * r33) * (Bq * (-(a1[i] * d3[j]) + cs2 * aa - co * P3[i][j] - d3[i] * a1[j]) - is * aa);
-          } else if (pass == 2) {
-            const double aa = a3[i] * a1[j];
-            pxx = -(cs2 * aa + P1P3[i][j]) * r13;
-            Rg = qR13 * aa;
-            fo = (kL * r13) * (Bq * (cs2 * aa + P1P3[i][j]) - is * aa);
-          } else {
-            const double aa = a1[i] * a3[j];
-            pxx = -(cs2 * (a1[i] * e3[j]) + P3P1[i][j]) * r13;
-            Rg = qR13 * aa;
-            fo = (kL * r13) * (Bq * (cs2 * aa + P3P1[i][j]) - is * aa);
-          }
-          const double gxx = Rg + kap * pxx;
-          const double psx = sgm * pxx + (pass == 2 ? 0.5 * omg * (O + Ob) : omg * O);
-          double nx = pb5den * pxx - two_num_sgm2 * O - two_num_phs * psx;
-          if (pass >= 2) nx += cross * (O - Ob);
-          const double cfxx = (nx * den2 - X4 * O) * rden22;
-          const double cfdd = pass < 2 ? cfqm2 * O + (1 - cf * cf * cfxx) : cfqm2 * Ob + (1 - cf * cf) * cfxx;
-          const double kxx = base2 * (kO * O + kG * gxx + (1 - g3) * cfdd);
-          double kk;
-          if (pass < 2) kk = 2 * LB * (beta0 * pB[j] + beta1 * O);
-          else kk = LB * (beta0 * pB[j] + beta1 * O) + LB * (beta0 * pA[i] + beta1 * O);
-          J[i][j] = -kxx * hLB2 - kk + fo;
-        }
+        for (int j = 0; j < 3; ++j)
+          J13[i][j] = kA * (a3[i] * a1[j]) + kB * (a1[i] * a3[j]) + kM * P1P3[i][j] - LB * beta0 * (px3[j] + px1[i]);
+    }
+    // x3x1: pxx = -r13 (cs2 E + M^T), O = rho13 A, Ob = rho13 B, Rg = qR13 A,
+    //       fo = kL r13 (kq A + Bq M^T); A = a1 a3^T, B = a3 a1^T, E = a1 e3^T
+    {
+      const double kA = cO31 * rho13 + cR * qR13 + kL * r13 * kq;
+      const double kB = cOb31 * rho13;
+      const double kE = -cPx * r13 * cs2;
+      const double kM = (-cPx + kL * Bq) * r13;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          J31[i][j] = kA * (a1[i] * a3[j]) + kB * (a3[i] * a1[j]) + kE * (a1[i] * e3[j]) + kM * P1P3[j][i] -
+                      LB * beta0 * (px1[j] + px3[i]);
     }
   }
   const int64_t stride = 4LL * nt, base = (int64_t)seg * nt + n0;
