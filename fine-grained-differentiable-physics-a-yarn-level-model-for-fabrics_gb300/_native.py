@@ -20,8 +20,10 @@ EXPORTED = [
     "ys_last_error", "ys_batch_create", "ys_batch_destroy", "ys_batch_get_info", "ys_cloth_node_offset",
     "ys_cloth_dim", "ys_set_state", "ys_get_state", "ys_set_wind", "ys_set_winds", "ys_assemble", "ys_export_system",
     "ys_solve", "ys_get_solution", "ys_step", "ys_apply_system", "ys_synchronize", "ys_profile",
-    "ys_profile_read", "ys_apply_system_noalloc",
+    "ys_profile_read", "ys_apply_system_noalloc", "ys_tangent_count", "ys_tangent_enable", "ys_tangent_seed",
+    "ys_tangent_set_state", "ys_tangent_get_state", "ys_step_tangent",
 ]
+YS_TANGENT_EXACT, YS_TANGENT_REFERENCE = 0, 1
 PROF_KINDS = ["geom", "edges", "bends", "faces", "gather", "shear", "finalize", "pcg_setup", "spmv", "axpy", "dir",
               "update", "misc"]
 
@@ -98,12 +100,20 @@ def load(build_if_missing: bool = True):
                           ctypes.POINTER(ClothStats)]
     L.ys_apply_system.argtypes = [vp, vp, vp, ctypes.c_int32]
     L.ys_apply_system_noalloc.argtypes = [vp, vp, vp]
+    L.ys_tangent_count.argtypes = []
+    L.ys_tangent_count.restype = ctypes.c_int32
+    L.ys_tangent_enable.argtypes = [vp, ctypes.c_int32]
+    L.ys_tangent_seed.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.ys_tangent_set_state.argtypes = [vp, vp, vp, vp, vp, vp, ctypes.c_int32]
+    L.ys_tangent_get_state.argtypes = [vp, vp, vp, vp, vp, vp, ctypes.c_int32]
+    L.ys_step_tangent.argtypes = [vp, ctypes.c_double, vp, ctypes.c_int32, vp, ctypes.c_int32, vp]
     L.ys_synchronize.argtypes = [vp]
     L.ys_profile.argtypes = [vp, ctypes.c_int32]
     L.ys_profile_read.argtypes = [vp, _dp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                   ctypes.c_int32]
     for name in EXPORTED:
-        if name not in ("ys_batch_destroy", "ys_last_error", "ys_cloth_node_offset", "ys_cloth_dim"):
+        if name not in ("ys_batch_destroy", "ys_last_error", "ys_cloth_node_offset", "ys_cloth_dim",
+                        "ys_tangent_count"):
             getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L

@@ -257,6 +257,57 @@ class ClothBatch:
             N.check(r, "ys_step")
         return self._stats(st)
 
+    # ---- forward-mode sensitivities
+    @property
+    def n_tangents(self):
+        return int(N.load().ys_tangent_count())
+
+    @property
+    def n_lines(self):
+        return sum(s.length + s.width for s in self.specs)
+
+    def tangent_enable(self, mode=0):
+        """Allocates and zeroes the tangents (mode 0: exact derivatives of the step)."""
+        N.check(N.load().ys_tangent_enable(self._h, int(mode)), "ys_tangent_enable")
+
+    def tangent_seed(self, drho=None, dY=None, dB=None, dS=None, dmu=None):
+        """Parameter directions: drho, dY, dB [K, lines] (cloth by cloth, warp
+        lines then weft lines); dS, dmu [K, n_cloths]."""
+        K, nl, nc = self.n_tangents, self.n_lines, self.n_cloths
+        arrs = []
+        for x, shape in ((drho, (K, nl)), (dY, (K, nl)), (dB, (K, nl)), (dS, (K, nc)), (dmu, (K, nc))):
+            arrs.append(None if x is None else np.ascontiguousarray(np.broadcast_to(np.asarray(x, float), shape)))
+        ptr = [ctypes.c_void_p(a.ctypes.data) if a is not None else None for a in arrs]
+        N.check(N.load().ys_tangent_seed(self._h, *ptr), "ys_tangent_seed")
+
+    def tangent_set_state(self, dlpos=None, dlvel=None, depos=None, deposbar=None, devel=None):
+        """State tangents [K, total_nodes, 3|2] (numpy or CUDA tensors; None = 0)."""
+        ps = [_ptr(a) for a in (dlpos, dlvel, depos, deposbar, devel)]
+        flags = max([f for _, f in ps] + [0])
+        N.check(N.load().ys_tangent_set_state(self._h, *[ctypes.c_void_p(p) if p else None for p, _ in ps], flags),
+                "ys_tangent_set_state")
+
+    def tangent_get_state(self):
+        """dict of state tangents [K, total_nodes, 3|2] (numpy)."""
+        K, T = self.n_tangents, self.total_nodes
+        out = dict(LPos=np.zeros((K, T, 3)), LVel=np.zeros((K, T, 3)), EPos=np.zeros((K, T, 2)),
+                   EPosBar=np.zeros((K, T, 2)), EVel=np.zeros((K, T, 2)))
+        N.check(N.load().ys_tangent_get_state(self._h, *[ctypes.c_void_p(out[k].ctypes.data) for k in
+                                                         ("LPos", "LVel", "EPos", "EPosBar", "EVel")], 0),
+                "ys_tangent_get_state")
+        return out
+
+    def step_tangent(self, h, ext_force=None, tol=0.0, maxiter=-1, check_every=16, kact=None):
+        """step() that also advances the first kact tangent directions."""
+        kact = self.n_tangents if kact is None else int(kact)
+        p, f = _ptr(ext_force)
+        st = (N.ClothStats * self.n_cloths)()
+        r = N.load().ys_step_tangent(self._h, h, ctypes.c_void_p(p) if p else None, f,
+                                     ctypes.byref(self._opts(tol, maxiter, check_every)), kact, st)
+        if r not in (N.YS_OK, N.YS_ERR_NONFINITE, N.YS_ERR_MAXITER):
+            N.check(r, "ys_step_tangent")
+        return self._stats(st)
+
     def export_system(self, c):
         """Dense (A, b) of cloth c in the reference's DOF layout."""
         dim = self.specs[c].dim

@@ -88,6 +88,19 @@ struct ys_batch {
   // launch accounting and optional per-kernel-class event timing
   int64_t launches = 0;
   bool profiling = false;
+  // forward-mode sensitivities (allocated by ys_tangent_enable)
+  struct Tan {
+    bool on = false;
+    int mode = 0;
+    double *dX = nullptr, *dV = nullptr, *dUV = nullptr, *dUVD = nullptr, *dUVB = nullptr;
+    double *dNRM = nullptr, *dCOMP = nullptr, *dSLIDE = nullptr;
+    double *drho = nullptr, *dks = nullptr, *dkb = nullptr, *dS = nullptr, *dmu = nullptr;
+    double *dA = nullptr, *dB = nullptr, *As = nullptr, *Bs = nullptr, *qsave = nullptr, *rt = nullptr, *dq = nullptr;
+    double *dedge = nullptr, *dbend = nullptr, *dface = nullptr, *dshear = nullptr;
+    double* io = nullptr;  // [kTangents][ntot][3] staging of host tangents
+  } tan;
+  int nlines = 0;
+  std::vector<double> line_R;  // yarn radius of each line's cloth
   struct Rec { int kind; cudaEvent_t a, b; };
   std::vector<Rec> recs;
   std::vector<cudaEvent_t> pool;
@@ -241,6 +254,7 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
       kb.push_back(d.weft_B[i] * ys::kPi * std::pow(d.R, 2));
     }
     line_off += d.length + d.width;
+    for (int i = 0; i < d.length + d.width; ++i) b->line_R.push_back(d.R);
     const int W = d.width, H = d.length;
     std::vector<uint8_t> fixed(W * H, 0);
     for (int hnd = 0; hnd < d.n_handles; ++hnd) {
@@ -360,6 +374,8 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
   v.ncloth = n_cloths;
   v.node_cloth = d_nc; v.node_u = d_nu; v.node_v = d_nv; v.flags = d_fl; v.cp = d_cp;
   v.line_rho = d_rho; v.line_ks = d_ks; v.line_kb = d_kb;
+  v.nlines = line_off;
+  b->nlines = line_off;
   v.ext = nullptr;
   v.h = 1e-3;
   b->blk.nblk = (int)blk_cloth.size();
@@ -493,10 +509,12 @@ ys_status ys_assemble(ys_batch* b, double h, const double* ext_force, int32_t fl
   return YS_OK;
 }
 
-ys_status ys_solve(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* stats) {
-  if (!b) return fail(YS_ERR_ARG, "null handle");
-  if (!b->assembled) return fail(YS_ERR_ARG, "ys_solve before ys_assemble");
-  YS_CUDA(cudaSetDevice(b->device));
+}  // extern "C"
+
+namespace {
+// Jacobi-PCG on the assembled A with the right-hand side v.B (the step's b,
+// or the right-hand side of a tangent solve); the solution lands in so.x.
+ys_status solve_impl(ys_batch* b, const ys::View& v, const ys_solve_opts* opts, ys_cloth_stats* stats) {
   cudaStream_t s = b->stream;
   b->so.tol = (opts && opts->tol > 0) ? opts->tol : DBL_EPSILON;
   const int override_max = (opts && opts->maxiter >= 0) ? opts->maxiter : -1;
@@ -506,16 +524,16 @@ ys_status ys_solve(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* stats
     k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
   });
   YS_CUDA(cudaGetLastError());
-  b->run(YS_PROF_PCG_SETUP, 2, [&] { ys::launch_pcg_setup(b->v, b->blk, b->so, s); });
+  b->run(YS_PROF_PCG_SETUP, 2, [&] { ys::launch_pcg_setup(v, b->blk, b->so, s); });
   int it = 0;
   while (it < cap) {
     const int n = std::min(every, cap - it);
     for (int q = 0; q < n; ++q, ++it) {
-      b->run(YS_PROF_SPMV, 1, [&] { ys::launch_pcg_spmv(b->v, b->blk, b->so, s); });
-      b->run(YS_PROF_AXPY, 1, [&] { ys::launch_pcg_axpy(b->v, b->blk, b->so, it, s); });
-      b->run(YS_PROF_DIR, 1, [&] { ys::launch_pcg_dir(b->v, b->blk, b->so, it, s); });
+      b->run(YS_PROF_SPMV, 1, [&] { ys::launch_pcg_spmv(v, b->blk, b->so, s); });
+      b->run(YS_PROF_AXPY, 1, [&] { ys::launch_pcg_axpy(v, b->blk, b->so, it, s); });
+      b->run(YS_PROF_DIR, 1, [&] { ys::launch_pcg_dir(v, b->blk, b->so, it, s); });
     }
-    b->run(YS_PROF_MISC, 1, [&] { ys::launch_count_active(b->v, b->so, s); });
+    b->run(YS_PROF_MISC, 1, [&] { ys::launch_count_active(v, b->so, s); });
     YS_CUDA(cudaMemcpyAsync(b->h_nactive, b->so.nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
     YS_CUDA(cudaStreamSynchronize(s));
     if (*b->h_nactive == 0) break;
@@ -536,6 +554,17 @@ ys_status ys_solve(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* stats
     }
   }
   return ret;
+}
+
+}  // namespace
+
+extern "C" {
+
+ys_status ys_solve(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* stats) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  if (!b->assembled) return fail(YS_ERR_ARG, "ys_solve before ys_assemble");
+  YS_CUDA(cudaSetDevice(b->device));
+  return solve_impl(b, b->v, opts, stats);
 }
 
 ys_status ys_get_solution(ys_batch* b, double* x, int32_t flags) {
@@ -748,3 +777,220 @@ extern "C" ys_status ys_apply_system_noalloc(ys_batch* b, const double* x, doubl
   YS_CUDA(cudaGetLastError());
   return YS_OK;
 }
+
+// ------------------------------------------------ forward-mode sensitivities
+namespace {
+
+constexpr int KT = ys::kTangents;
+
+// [K][ntot][c] (node layout) <-> [c][K][ntot] (device tangent layout)
+__global__ void k_tan_in(const double* __restrict__ src, double* __restrict__ dst, int64_t nt, int c) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt * KT) return;
+  const int64_t k = t / nt, i = t - k * nt;
+  for (int j = 0; j < c; ++j) dst[((int64_t)j * KT + k) * nt + i] = src ? src[(k * nt + i) * c + j] : 0.0;
+}
+__global__ void k_tan_out(const double* __restrict__ src, double* __restrict__ dst, int64_t nt, int c) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt * KT) return;
+  const int64_t k = t / nt, i = t - k * nt;
+  for (int j = 0; j < c; ++j) dst[(k * nt + i) * c + j] = src[((int64_t)j * KT + k) * nt + i];
+}
+
+ys_status tan_upload(ys_batch* b, const double* src, double* dst, int c, int32_t flags) {
+  const int64_t nt = b->ntot, cnt = nt * KT;
+  const double* d_src = nullptr;
+  if (src) {
+    d_src = src;
+    if (!(flags & YS_ON_DEVICE)) {
+      YS_CUDA(cudaMemcpyAsync(b->tan.io, src, sizeof(double) * cnt * c, cudaMemcpyHostToDevice, b->stream));
+      d_src = b->tan.io;
+    }
+  }
+  b->launches += 1;
+  k_tan_in<<<(unsigned)((cnt + 255) / 256), 256, 0, b->stream>>>(d_src, dst, nt, c);
+  YS_CUDA(cudaGetLastError());
+  if (src && !(flags & YS_ON_DEVICE)) YS_CUDA(cudaStreamSynchronize(b->stream));
+  return YS_OK;
+}
+ys_status tan_download(ys_batch* b, const double* src, double* dst, int c, int32_t flags) {
+  if (!dst) return YS_OK;
+  const int64_t nt = b->ntot, cnt = nt * KT;
+  double* d_dst = (flags & YS_ON_DEVICE) ? dst : b->tan.io;
+  b->launches += 1;
+  k_tan_out<<<(unsigned)((cnt + 255) / 256), 256, 0, b->stream>>>(src, d_dst, nt, c);
+  YS_CUDA(cudaGetLastError());
+  if (!(flags & YS_ON_DEVICE)) {
+    YS_CUDA(cudaMemcpyAsync(dst, b->tan.io, sizeof(double) * cnt * c, cudaMemcpyDeviceToHost, b->stream));
+    YS_CUDA(cudaStreamSynchronize(b->stream));
+  }
+  return YS_OK;
+}
+
+// the view of the dual assembly: values of A and b into shadows, tangents alongside
+ys::View dual_view(ys_batch* b) {
+  ys::View dv = b->v;
+  const ys_batch::Tan& t = b->tan;
+  dv.A = t.As;
+  dv.B = t.Bs;
+  dv.K = KT;
+  dv.trunc = t.mode == YS_TANGENT_REFERENCE ? 1 : 0;
+  dv.dX = t.dX; dv.dV = t.dV; dv.dUV = t.dUV; dv.dUVD = t.dUVD; dv.dUVB = t.dUVB;
+  dv.dNRM = t.dNRM; dv.dCOMP = t.dCOMP; dv.dSLIDE = t.dSLIDE;
+  dv.dline_rho = t.drho; dv.dline_ks = t.dks; dv.dline_kb = t.dkb; dv.dS = t.dS; dv.dmu = t.dmu;
+  dv.dA = t.dA; dv.dB = t.dB;
+  return dv;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t ys_tangent_count(void) { return KT; }
+
+ys_status ys_tangent_enable(ys_batch* b, int32_t mode) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  if (mode != YS_TANGENT_EXACT) return fail(YS_ERR_ARG, "tangent mode must be YS_TANGENT_EXACT");
+  YS_CUDA(cudaSetDevice(b->device));
+  ys_batch::Tan& t = b->tan;
+  const size_t nt = b->ntot, nl = b->nlines, nc = b->ncloth;
+  if (!t.on) {
+    ys_status st = YS_OK;
+    auto A = [&](double** p, size_t cnt) { if (st == YS_OK) st = b->alloc(p, cnt); };
+    A(&t.dX, 3 * KT * nt); A(&t.dV, 3 * KT * nt); A(&t.dUV, 2 * KT * nt); A(&t.dUVD, 2 * KT * nt);
+    A(&t.dUVB, 2 * KT * nt); A(&t.dNRM, 3 * KT * nt); A(&t.dCOMP, KT * nt); A(&t.dSLIDE, 2 * KT * nt);
+    A(&t.drho, KT * nl); A(&t.dks, KT * nl); A(&t.dkb, KT * nl); A(&t.dS, KT * nc); A(&t.dmu, KT * nc);
+    A(&t.dA, (size_t)ys::YS_NUM_SLOTS * KT * nt); A(&t.dB, 5 * KT * nt);
+    A(&t.As, (size_t)ys::YS_NUM_SLOTS * nt); A(&t.Bs, 5 * nt); A(&t.qsave, 5 * nt); A(&t.rt, 5 * KT * nt);
+    A(&t.dq, 5 * KT * nt);
+    A(&t.dedge, (size_t)ys::kEdgeFields * 2 * KT * nt); A(&t.dbend, (size_t)ys::kBendFields * 2 * KT * nt);
+    A(&t.dface, 6 * KT * nt); A(&t.dshear, (size_t)ys::kShearFields * 4 * KT * nt);
+    A(&t.io, 3 * KT * nt);
+    if (st != YS_OK) return st;
+    t.on = true;
+  }
+  t.mode = mode;
+  auto Z = [&](double* p, size_t cnt) { return cudaMemsetAsync(p, 0, sizeof(double) * cnt, b->stream); };
+  if (Z(t.dX, 3 * KT * nt) || Z(t.dV, 3 * KT * nt) || Z(t.dUV, 2 * KT * nt) || Z(t.dUVD, 2 * KT * nt) ||
+      Z(t.dUVB, 2 * KT * nt) || Z(t.drho, KT * nl) || Z(t.dks, KT * nl) || Z(t.dkb, KT * nl) || Z(t.dS, KT * nc) ||
+      Z(t.dmu, KT * nc) || Z(t.dq, 5 * KT * nt))
+    return fail(YS_ERR_CUDA, "cudaMemsetAsync failed");
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  return YS_OK;
+}
+
+ys_status ys_tangent_seed(ys_batch* b, const double* drho, const double* dY, const double* dB, const double* dS,
+                          const double* dmu) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  if (!b->tan.on) return fail(YS_ERR_ARG, "ys_tangent_seed before ys_tangent_enable");
+  YS_CUDA(cudaSetDevice(b->device));
+  const size_t nl = b->nlines, nc = b->ncloth;
+  std::vector<double> r(KT * nl, 0.0), ks(KT * nl, 0.0), kb(KT * nl, 0.0), S(KT * nc, 0.0), mu(KT * nc, 0.0);
+  for (int k = 0; k < KT; ++k)
+    for (size_t l = 0; l < nl; ++l) {
+      const size_t i = k * nl + l;
+      const double a = ys::kPi * std::pow(b->line_R[l], 2);  // ks, kb = (Y, B) pi R^2 (src/Yarn.h:14-15)
+      if (drho) r[i] = drho[i];
+      if (dY) ks[i] = dY[i] * a;
+      if (dB) kb[i] = dB[i] * a;
+    }
+  for (size_t i = 0; i < KT * nc; ++i) {
+    if (dS) S[i] = dS[i];
+    if (dmu) mu[i] = dmu[i];
+  }
+  const ys_batch::Tan& t = b->tan;
+  YS_CUDA(cudaMemcpyAsync(t.drho, r.data(), sizeof(double) * r.size(), cudaMemcpyHostToDevice, b->stream));
+  YS_CUDA(cudaMemcpyAsync(t.dks, ks.data(), sizeof(double) * ks.size(), cudaMemcpyHostToDevice, b->stream));
+  YS_CUDA(cudaMemcpyAsync(t.dkb, kb.data(), sizeof(double) * kb.size(), cudaMemcpyHostToDevice, b->stream));
+  YS_CUDA(cudaMemcpyAsync(t.dS, S.data(), sizeof(double) * S.size(), cudaMemcpyHostToDevice, b->stream));
+  YS_CUDA(cudaMemcpyAsync(t.dmu, mu.data(), sizeof(double) * mu.size(), cudaMemcpyHostToDevice, b->stream));
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  return YS_OK;
+}
+
+ys_status ys_tangent_set_state(ys_batch* b, const double* dlpos, const double* dlvel, const double* depos,
+                               const double* deposbar, const double* devel, int32_t flags) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  if (!b->tan.on) return fail(YS_ERR_ARG, "ys_tangent_set_state before ys_tangent_enable");
+  YS_CUDA(cudaSetDevice(b->device));
+  const ys_batch::Tan& t = b->tan;
+  ys_status s;
+  if ((s = tan_upload(b, dlpos, t.dX, 3, flags)) != YS_OK) return s;
+  if ((s = tan_upload(b, dlvel, t.dV, 3, flags)) != YS_OK) return s;
+  if ((s = tan_upload(b, depos, t.dUV, 2, flags)) != YS_OK) return s;
+  if ((s = tan_upload(b, deposbar, t.dUVB, 2, flags)) != YS_OK) return s;
+  if ((s = tan_upload(b, devel, t.dUVD, 2, flags)) != YS_OK) return s;
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  return YS_OK;
+}
+
+ys_status ys_tangent_get_state(ys_batch* b, double* dlpos, double* dlvel, double* depos, double* deposbar,
+                               double* devel, int32_t flags) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  if (!b->tan.on) return fail(YS_ERR_ARG, "ys_tangent_get_state before ys_tangent_enable");
+  YS_CUDA(cudaSetDevice(b->device));
+  const ys_batch::Tan& t = b->tan;
+  ys_status s;
+  if ((s = tan_download(b, t.dX, dlpos, 3, flags)) != YS_OK) return s;
+  if ((s = tan_download(b, t.dV, dlvel, 3, flags)) != YS_OK) return s;
+  if ((s = tan_download(b, t.dUV, depos, 2, flags)) != YS_OK) return s;
+  if ((s = tan_download(b, t.dUVB, deposbar, 2, flags)) != YS_OK) return s;
+  if ((s = tan_download(b, t.dUVD, devel, 2, flags)) != YS_OK) return s;
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  return YS_OK;
+}
+
+ys_status ys_step_tangent(ys_batch* b, double h, const double* ext_force, int32_t flags, const ys_solve_opts* opts,
+                          int32_t kact, ys_cloth_stats* stats) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  if (!b->tan.on) return fail(YS_ERR_ARG, "ys_step_tangent before ys_tangent_enable");
+  if (kact < 0 || kact > KT) return fail(YS_ERR_ARG, "kact must be in [0, ys_tangent_count()]");
+  ys_status s = ys_assemble(b, h, ext_force, flags);
+  if (s != YS_OK) return s;
+  std::vector<ys_cloth_stats> local;
+  ys_cloth_stats* st = stats;
+  if (!st) {
+    local.resize(b->ncloth);
+    st = local.data();
+  }
+  const ys_status sol = solve_impl(b, b->v, opts, st);
+  if (sol == YS_ERR_ARG || sol == YS_ERR_CUDA) return sol;
+  cudaStream_t cs = b->stream;
+  const int64_t nt = b->ntot;
+  ys_batch::Tan& t = b->tan;
+  YS_CUDA(cudaMemcpyAsync(t.qsave, b->so.x, sizeof(double) * 5 * nt, cudaMemcpyDeviceToDevice, cs));
+  // dual assembly: tangents of A and b
+  ys::View dv = dual_view(b);
+  ys::Records dr = b->rec;
+  dr.dedge = t.dedge; dr.dbend = t.dbend; dr.dface = t.dface; dr.dshear = t.dshear;
+  b->run(YS_PROF_MISC, 7, [&] { ys::launch_assembly_dual(dv, dr, b->anchors, b->geom_n, cs); });
+  YS_CUDA(cudaGetLastError());
+  b->run(YS_PROF_MISC, 1, [&] { ys::launch_tangent_rhs(dv, t.qsave, t.rt, kact, cs); });
+  YS_CUDA(cudaGetLastError());
+  // tangent solves A dq_k = db_k - dA_k q with the step's A and Jacobi diagonal
+  for (int k = 0; k < kact; ++k) {
+    ys::View vk = b->v;
+    vk.B = t.rt + (int64_t)k * 5 * nt;
+    const ys_status sk = solve_impl(b, vk, opts, nullptr);
+    if (sk == YS_ERR_ARG || sk == YS_ERR_CUDA) return sk;
+    YS_CUDA(cudaMemcpy2DAsync(t.dq + (int64_t)k * nt, sizeof(double) * KT * nt, b->so.x, sizeof(double) * nt,
+                              sizeof(double) * nt, 5, cudaMemcpyDeviceToDevice, cs));
+  }
+  YS_CUDA(cudaMemcpyAsync(b->so.x, t.qsave, sizeof(double) * 5 * nt, cudaMemcpyDeviceToDevice, cs));
+  ys::TangentState ts{t.dX, t.dV, t.dUV, t.dUVD, t.dUVB};
+  b->run(YS_PROF_UPDATE, 2, [&] { ys::launch_update_dual(dv, b->blk, b->so, t.dq, ts, cs); });
+  YS_CUDA(cudaGetLastError());
+  std::vector<ys::PcgCloth> pc(b->ncloth);
+  YS_CUDA(cudaMemcpyAsync(pc.data(), b->so.pc, sizeof(ys::PcgCloth) * b->ncloth, cudaMemcpyDeviceToHost, cs));
+  YS_CUDA(cudaStreamSynchronize(cs));
+  ys_status ret = sol;
+  for (int c = 0; c < b->ncloth; ++c) {
+    st[c].ok = (pc[c].status & 3) == 0;
+    if (!st[c].ok) ret = YS_ERR_NONFINITE;
+  }
+  b->assembled = false;
+  return ret;
+}
+
+}  // extern "C"
+

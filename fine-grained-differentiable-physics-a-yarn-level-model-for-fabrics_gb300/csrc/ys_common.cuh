@@ -122,6 +122,27 @@ struct View {
   double* DEE;   // [2][ntot]  same, velocity
   const double* ext;  // [5][ntot] external force or null
   double h;
+  // Forward-mode tangents (null in the plain step). Per-node arrays hold
+  // tangent k of comp c of node i at [(c * K + k) * ntot + i]; parameter
+  // tables hold tangent k of entry i at [k * n + i].
+  int K;
+  int trunc;  // 1: tangents of b through F and v only (M, D, A held constant)
+  int nlines;
+  const double* dX;
+  const double* dV;
+  const double* dUV;
+  const double* dUVD;
+  const double* dUVB;
+  double* dNRM;
+  double* dCOMP;
+  double* dSLIDE;
+  const double* dline_rho;  // [K][nlines]
+  const double* dline_ks;
+  const double* dline_kb;
+  const double* dS;   // [K][ncloth]
+  const double* dmu;
+  double* dA;  // [YS_NUM_SLOTS][K][ntot]
+  double* dB;  // [5][K][ntot]
 };
 
 YS_HD double& slot(const View& v, int s, int node) { return v.A[(int64_t)s * v.ntot + node]; }

@@ -17,11 +17,26 @@ struct Records {
   double* bend;   // [kBendFields][2][ntot]
   double* face;   // [6][ntot]
   double* shear;  // [kShearFields][4][ntot]
+  // tangents of the same records (forward-mode runs only; layout of ys_physics.cuh lds)
+  double* dedge;
+  double* dbend;
+  double* dface;
+  double* dshear;
 };
 
 YS_HD double rec(const double* buf, int field, int nslot, int slot_, int ntot, int node) {
   return buf[((int64_t)field * nslot + slot_) * ntot + node];
 }
+template <class T>
+YS_HD T recT(const double* buf, const double* dbuf, int field, int nslot, int slot_, int ntot, int node) {
+  return ldT<T>(buf, dbuf, field * nslot + slot_, ntot, node);
+}
+
+// one coefficient slot of row block n (value, and tangents when T is a Dual)
+template <class T>
+YS_HD void stA(const View& v, int s, int n, const T& x) { stT(v.A, v.dA, s, v.ntot, n, x); }
+template <class T>
+YS_HD T ldA(const View& v, int s, int n) { return ldT<T>(v.A, v.dA, s, v.ntot, n); }
 
 // Gathers, for row block n, every contribution of the edges, bend segments
 // and faces that touch it, runs ConSlideFriction on the gathered no-slide
@@ -29,6 +44,7 @@ YS_HD double rec(const double* buf, int field, int nslot, int slot_, int ntot, i
 // blocks, which only shear segments fill, are set to 0 here). Node-node
 // blocks of X_LL are written transposed into the dense matrix
 // (src/MatrixMp.cpp:54-65), hence the blk[3 * c + r] reads.
+template <class T>
 YS_HD void gather_elements(const View& v, const Records& R, int n) {
   const int nt = v.ntot;
   const ClothParams& P = v.cp[v.node_cloth[n]];
@@ -37,7 +53,7 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
   const double h = v.h, mh2 = -(v.h * v.h);
   // ------------------------------------------------------------ self block
   {
-    double LL[9], LE[6], EL[6], EE[2], B[5], FE[2], KEE[2], DEE[2], CL[3], CLE[6];
+    T LL[9], LE[6], EL[6], EE[2], B[5], FE[2], KEE[2], DEE[2], CL[3], CLE[6];
     for (int i = 0; i < 9; ++i) LL[i] = 0.0;
     for (int i = 0; i < 6; ++i) LE[i] = EL[i] = CLE[i] = 0.0;
     for (int i = 0; i < 2; ++i) EE[i] = FE[i] = KEE[i] = DEE[i] = 0.0;
@@ -51,10 +67,10 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
       for (int a = 0; a < 2; ++a) {
         if (!(a == 0 ? has0 : has1)) continue;
         const int anc = a == 0 ? n : n - step;
-        auto E = [&](int f) { return rec(R.edge, f, 2, k, nt, anc); };
+        auto E = [&](int f) { return recT<T>(R.edge, R.dedge, f, 2, k, nt, anc); };
         const int p = 3 * a;  // block (a, a)
-        const double cI = E(kE_llI + p), cP = E(kE_llP + p);
-        const double d[3] = {E(kE_d), E(kE_d + 1), E(kE_d + 2)};
+        const T cI = E(kE_llI + p), cP = E(kE_llP + p);
+        const T d[3] = {E(kE_d), E(kE_d + 1), E(kE_d + 2)};
         for (int r = 0; r < 3; ++r)
           for (int c = 0; c < 3; ++c) LL[3 * r + c] += (r == c ? cI : 0.0) + cP * ((r == c ? 1.0 : 0.0) - d[r] * d[c]);
         for (int r = 0; r < 3; ++r) {
@@ -78,15 +94,15 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
         const int mid = role == 0 ? pos + 1 : role == 1 ? pos : pos - 1;
         if (mid < 1 || mid > len - 2) continue;
         const int anc = role == 0 ? n + step : role == 1 ? n : n - step;
-        auto Bf = [&](int f) { return rec(R.bend, f, 2, k, nt, anc); };
-        double blk[9];
+        auto Bf = [&](int f) { return recT<T>(R.bend, R.dbend, f, 2, k, nt, anc); };
+        T blk[9];
         if (role == 0) {
           for (int i = 0; i < 9; ++i) blk[i] = Bf(kB_L22 + i);
         } else if (role == 2) {
           for (int i = 0; i < 9; ++i) blk[i] = Bf(kB_L11 + i);
         } else {  // L00 = -(L10 + L20) (src/PhysicsCloth.cpp:709)
           for (int i = 0; i < 9; ++i) {
-            const double L10 = -(Bf(kB_L11 + i) + Bf(kB_L12 + i)), L20 = -(Bf(kB_L21 + i) + Bf(kB_L22 + i));
+            const T L10 = -(Bf(kB_L11 + i) + Bf(kB_L12 + i)), L20 = -(Bf(kB_L21 + i) + Bf(kB_L22 + i));
             blk[i] = -(L10 + L20);
           }
         }
@@ -98,9 +114,9 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
             CL[r] += sgn * Bf(kB_cFx2 + r);
           }
           if (in) {
-            const double e11 = Bf(kB_E1E1), fu2 = Bf(kB_Fu2);
+            const T e11 = Bf(kB_E1E1), fu2 = Bf(kB_Fu2);
             for (int r = 0; r < 3; ++r) {
-              const double l2e2 = -Bf(kB_L2E1 + r);
+              const T l2e2 = -Bf(kB_L2E1 + r);
               LE[2 * r + k] += mh2 * l2e2;
               EL[3 * k + r] += mh2 * l2e2;  // E2L2 = -E1L2 carries the values of -L2E1
               CLE[3 * k + r] += sgn * (-Bf(kB_cL2E1 + r));
@@ -116,9 +132,9 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
             CL[r] += sgn * Bf(kB_cFx1 + r);
           }
           if (in) {
-            const double e11 = Bf(kB_E1E1), fu1 = -1 * Bf(kB_Fu2);
+            const T e11 = Bf(kB_E1E1), fu1 = -1 * Bf(kB_Fu2);
             for (int r = 0; r < 3; ++r) {
-              const double l1e1 = Bf(kB_L1E1 + r);
+              const T l1e1 = Bf(kB_L1E1 + r);
               LE[2 * r + k] += mh2 * l1e1;
               EL[3 * k + r] += mh2 * l1e1;
               CLE[3 * k + r] += sgn * Bf(kB_cL1E1 + r);
@@ -149,25 +165,25 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
         else if (!right && below) { inA = !even; inB = true; }  // bl
         else { inA = even; inB = true; }                        // br
         for (int r = 0; r < 3; ++r) {
-          if (inA) B[r] += h * R.face[(int64_t)r * nt + tl];
-          if (inB) B[r] += h * R.face[(int64_t)(3 + r) * nt + tl];
+          if (inA) B[r] += h * ldT<T>(R.face, R.dface, r, nt, tl);
+          if (inB) B[r] += h * ldT<T>(R.face, R.dface, 3 + r, nt, tl);
         }
       }
     if (in) {
-      double aEE[2], bE[2];
+      T aEE[2], bE[2];
       friction_node(v, n, FE, KEE, DEE, CL, CLE, aEE, bE);
       for (int k = 0; k < 2; ++k) {
         EE[k] += aEE[k];
         B[3 + k] += bE[k];
       }
     }
-    for (int i = 0; i < 9; ++i) slot(v, YS_SLOT_LL + i, n) = LL[i];
+    for (int i = 0; i < 9; ++i) stA(v, YS_SLOT_LL + i, n, LL[i]);
     for (int i = 0; i < 6; ++i) {
-      slot(v, YS_SLOT_LE_SELF + i, n) = LE[i];
-      slot(v, YS_SLOT_EL_SELF + i, n) = EL[i];
+      stA(v, YS_SLOT_LE_SELF + i, n, LE[i]);
+      stA(v, YS_SLOT_EL_SELF + i, n, EL[i]);
     }
-    for (int k = 0; k < 2; ++k) slot(v, YS_SLOT_EE_SELF + k, n) = EE[k];
-    for (int i = 0; i < 5; ++i) st(v.B, i, nt, n) = B[i];
+    for (int k = 0; k < 2; ++k) stA(v, YS_SLOT_EE_SELF + k, n, EE[k]);
+    for (int i = 0; i < 5; ++i) stT(v.B, v.dB, i, nt, n, B[i]);
   }
   // ------------------------------------------------ yarn neighbours (+-1)
   for (int m = 0; m < 4; ++m) {
@@ -176,7 +192,7 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
     const int step = k == 0 ? 1 : W;
     const int pos = k == 0 ? u : w, len = k == 0 ? W : H;
     const int s = stencil_index(k == 0 ? dir : 0, k == 1 ? dir : 0);
-    double LL[9], LE[3], EL[3], EE = 0.0;
+    T LL[9], LE[3], EL[3], EE = 0.0;
     for (int i = 0; i < 9; ++i) LL[i] = 0.0;
     for (int i = 0; i < 3; ++i) LE[i] = EL[i] = 0.0;
     if (pos + dir >= 0 && pos + dir < len) {
@@ -185,10 +201,10 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
       // the edge between n and nb: n is its n0 when dir = +1
       const int a = dir > 0 ? 0 : 1, o = 1 - a;
       const int anc = dir > 0 ? n : nb;
-      auto E = [&](int f) { return rec(R.edge, f, 2, k, nt, anc); };
+      auto E = [&](int f) { return recT<T>(R.edge, R.dedge, f, 2, k, nt, anc); };
       const int p = 2 * a + o;
-      const double cI = E(kE_llI + p), cP = E(kE_llP + p);
-      const double d[3] = {E(kE_d), E(kE_d + 1), E(kE_d + 2)};
+      const T cI = E(kE_llI + p), cP = E(kE_llP + p);
+      const T d[3] = {E(kE_d), E(kE_d + 1), E(kE_d + 2)};
       for (int r = 0; r < 3; ++r)
         for (int c = 0; c < 3; ++c) LL[3 * r + c] += (r == c ? cI : 0.0) + cP * ((r == c ? 1.0 : 0.0) - d[r] * d[c]);
       for (int r = 0; r < 3; ++r) {
@@ -203,10 +219,10 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
         const int mid = which == 0 ? pos : pos + dir;
         if (mid < 1 || mid > len - 2) continue;
         const int ancb = which == 0 ? n : nb;
-        auto Bf = [&](int f) { return rec(R.bend, f, 2, k, nt, ancb); };
-        double blk[9];
+        auto Bf = [&](int f) { return recT<T>(R.bend, R.dbend, f, 2, k, nt, ancb); };
+        T blk[9];
         for (int i = 0; i < 9; ++i) {
-          const double L11 = Bf(kB_L11 + i), L12 = Bf(kB_L12 + i), L21 = Bf(kB_L21 + i), L22 = Bf(kB_L22 + i);
+          const T L11 = Bf(kB_L11 + i), L12 = Bf(kB_L12 + i), L21 = Bf(kB_L21 + i), L22 = Bf(kB_L22 + i);
           if (which == 0) blk[i] = dir > 0 ? -(L11 + L21) : -(L12 + L22);  // L01 or L02
           else blk[i] = dir > 0 ? -(L21 + L22) : -(L11 + L12);             // L20 or L10
         }
@@ -214,7 +230,7 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
           for (int c = 0; c < 3; ++c) LL[3 * r + c] += mh2 * blk[3 * c + r];
         // Eulerian couplings of Bending_D (src/PhysicsCloth.cpp:774-822):
         // q = L1E1 + L2E1 = L0E2 = E2L0 = -L0E1 = -E1L0
-        double q[3];
+        T q[3];
         for (int r = 0; r < 3; ++r) q[r] = Bf(kB_L1E1 + r) + Bf(kB_L2E1 + r);
         if (which == 0 && in && inb) {
           if (dir < 0)  // row n0 = n, column e / x of n2 = nb
@@ -226,12 +242,12 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
           for (int r = 0; r < 3; ++r) EL[r] += mh2 * (-q[r]);
       }
     }
-    for (int i = 0; i < 9; ++i) slot(v, YS_SLOT_LL + 9 * s + i, n) = LL[i];
+    for (int i = 0; i < 9; ++i) stA(v, YS_SLOT_LL + 9 * s + i, n, LL[i]);
     for (int r = 0; r < 3; ++r) {
-      slot(v, YS_SLOT_LE_NBR + 3 * m + r, n) = LE[r];
-      slot(v, YS_SLOT_EL_NBR + 3 * m + r, n) = EL[r];
+      stA(v, YS_SLOT_LE_NBR + 3 * m + r, n, LE[r]);
+      stA(v, YS_SLOT_EL_NBR + 3 * m + r, n, EL[r]);
     }
-    slot(v, YS_SLOT_EE_NBR + m, n) = EE;
+    stA(v, YS_SLOT_EE_NBR + m, n, EE);
   }
   // ------------------------------------------- second neighbours (+-2)
   for (int m = 0; m < 4; ++m) {
@@ -245,12 +261,12 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
     const int anc = n + dir * step;
     for (int r = 0; r < 3; ++r)
       for (int c = 0; c < 3; ++c)  // n is n2 (dir +1): L21; n is n1 (dir -1): L12
-        slot(v, YS_SLOT_LL + 9 * s + 3 * r + c, n) =
-            ok ? mh2 * rec(R.bend, (dir > 0 ? kB_L21 : kB_L12) + 3 * c + r, 2, k, nt, anc) : 0.0;
+        stA(v, YS_SLOT_LL + 9 * s + 3 * r + c, n,
+            ok ? T(mh2 * recT<T>(R.bend, R.dbend, (dir > 0 ? kB_L21 : kB_L12) + 3 * c + r, 2, k, nt, anc)) : T(0.0));
   }
   // diagonal neighbours: shear only (gather_shear_finalize)
   for (int s = 9; s < 13; ++s)
-    for (int i = 0; i < 9; ++i) slot(v, YS_SLOT_LL + 9 * s + i, n) = 0.0;
+    for (int i = 0; i < 9; ++i) stA(v, YS_SLOT_LL + 9 * s + i, n, T(0.0));
 }
 
 // Adds the shear segments touching row block n (as crossing n0, as warp
@@ -261,6 +277,7 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
 // Jacobi preconditioner (zero diagonal -> 1, as Eigen's
 // DiagonalPreconditioner). Returns false if the row block holds a non-finite
 // value (SimStep's DetectNaN / DetectInf, src/TrainHelper.cpp:22-37).
+template <class T>
 YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double* dinv) {
   const int nt = v.ntot;
   const ClothParams& P = v.cp[v.node_cloth[n]];
@@ -268,21 +285,31 @@ YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double*
   const uint8_t fl = v.flags[n];
   const double h = v.h, mh2 = -(v.h * v.h);
   auto interior = [&](int uu, int vv) { return uu >= 1 && uu <= W - 2 && vv >= 1 && vv <= H - 2; };
-  auto S = [&](int f, int seg, int anc) { return rec(R.shear, f, 4, seg, nt, anc); };
-  auto addLL = [&](int du, int dv, const double* blk) {  // A[x(n)][x(n + (du, dv))] += -h^2 blk^T
+  auto S = [&](int f, int seg, int anc) { return recT<T>(R.shear, R.dshear, f, 4, seg, nt, anc); };
+  auto addLL = [&](int du, int dv, const T* blk) {  // A[x(n)][x(n + (du, dv))] += -h^2 blk^T
     const int s = stencil_index(du, dv);
     if (s < 0) return;
     for (int r = 0; r < 3; ++r)
-      for (int c = 0; c < 3; ++c) slot(v, YS_SLOT_LL + 9 * s + 3 * r + c, n) += mh2 * blk[3 * c + r];
+      for (int c = 0; c < 3; ++c) {
+        const int sl = YS_SLOT_LL + 9 * s + 3 * r + c;
+        T a = ldA<T>(v, sl, n);
+        a += mh2 * blk[3 * c + r];
+        stA(v, sl, n, a);
+      }
   };
-  double Bx[3] = {0.0, 0.0, 0.0};
-  double J[9];
+  auto addB = [&](int c, const T& x) {
+    T b = ldT<T>(v.B, v.dB, c, nt, n);
+    b += x;
+    stT(v.B, v.dB, c, nt, n, b);
+  };
+  T Bx[3] = {0.0, 0.0, 0.0};
+  T J[9];
   // as the crossing n0 (src/PhysicsCloth.cpp:3033-3047)
   if (fl & YS_INTERIOR) {
     for (int seg = 0; seg < 4; ++seg) {
       for (int i = 0; i < 9; ++i) {
-        const double J10 = -(S(kS_J11 + i, seg, n) + S(kS_J13 + i, seg, n));
-        const double J30 = -(S(kS_J31 + i, seg, n) + S(kS_J33 + i, seg, n));
+        const T J10 = -(S(kS_J11 + i, seg, n) + S(kS_J13 + i, seg, n));
+        const T J30 = -(S(kS_J31 + i, seg, n) + S(kS_J33 + i, seg, n));
         J[i] = -(J10 + J30);
       }
       addLL(0, 0, J);
@@ -319,35 +346,40 @@ YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double*
     addLL(du, -dv, J);
     for (int r = 0; r < 3; ++r) Bx[r] += h * S(kS_F3 + r, seg, anc);
   }
-  for (int r = 0; r < 3; ++r) st(v.B, r, nt, n) += Bx[r];
+  for (int r = 0; r < 3; ++r) addB(r, Bx[r]);
   // handles, external force, boundary identity rows
   if (fl & YS_FIXED) {
     for (int i = 0; i < 3; ++i) {
-      st(v.B, i, nt, n) += h * (-(P.kh * (ld(v.X, i, nt, n) - ld(v.XF, i, nt, n))));
-      slot(v, YS_SLOT_LL + i * 3 + i, n) += -(h * h) * (-P.kh);
+      addB(i, h * (-(P.kh * (ldT<T>(v.X, v.dX, i, nt, n) - ld(v.XF, i, nt, n)))));
+      const int sl = YS_SLOT_LL + i * 3 + i;
+      T a = ldA<T>(v, sl, n);
+      a += -(h * h) * (-P.kh);
+      stA(v, sl, n, a);
     }
   }
   if (v.ext) {
-    for (int i = 0; i < 3; ++i) st(v.B, i, nt, n) += h * ld(v.ext, i, nt, n);
+    for (int i = 0; i < 3; ++i) addB(i, T(h * ld(v.ext, i, nt, n)));
     if (fl & YS_INTERIOR)
-      for (int k = 0; k < 2; ++k) st(v.B, 3 + k, nt, n) += h * ld(v.ext, 3 + k, nt, n);
+      for (int k = 0; k < 2; ++k) addB(3 + k, T(h * ld(v.ext, 3 + k, nt, n)));
   }
   if (!(fl & YS_INTERIOR)) {
     for (int k = 0; k < 2; ++k) {
-      slot(v, YS_SLOT_EE_SELF + k, n) = 1.0;
-      st(v.B, 3 + k, nt, n) = 0.0;
+      stA(v, YS_SLOT_EE_SELF + k, n, T(1.0));
+      stT(v.B, v.dB, 3 + k, nt, n, T(0.0));
     }
   }
   bool ok = true;
   for (int s = 0; s < YS_NUM_SLOTS; ++s) ok = ok && isfinite(slot(v, s, n));
   for (int c = 0; c < 5; ++c) ok = ok && isfinite(ld(v.B, c, nt, n));
-  for (int i = 0; i < 3; ++i) {
-    const double dg = slot(v, YS_SLOT_LL + i * 3 + i, n);
-    st(dinv, i, nt, n) = dg != 0.0 ? 1.0 / dg : 1.0;
-  }
-  for (int k = 0; k < 2; ++k) {
-    const double dg = slot(v, YS_SLOT_EE_SELF + k, n);
-    st(dinv, 3 + k, nt, n) = dg != 0.0 ? 1.0 / dg : 1.0;
+  if (dinv) {
+    for (int i = 0; i < 3; ++i) {
+      const double dg = slot(v, YS_SLOT_LL + i * 3 + i, n);
+      st(dinv, i, nt, n) = dg != 0.0 ? 1.0 / dg : 1.0;
+    }
+    for (int k = 0; k < 2; ++k) {
+      const double dg = slot(v, YS_SLOT_EE_SELF + k, n);
+      st(dinv, 3 + k, nt, n) = dg != 0.0 ? 1.0 / dg : 1.0;
+    }
   }
   return ok;
 }
@@ -355,8 +387,10 @@ YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double*
 // y = A x for row block n (5 rows). Couplings to grid positions outside the
 // cloth have zero coefficients; their column index is clamped to n so the
 // load stays in bounds and adds 0 * x(n).
-YS_HD void spmv_row(const View& v, const double* YS_RESTRICT x, int n, double y[5]) {
+YS_HD void spmv_row_s(const View& v, const double* YS_RESTRICT Ab, int64_t ss, const double* YS_RESTRICT x, int n,
+                      double y[5]) {
   const int nt = v.ntot;
+  auto slot = [&](const View&, int s_, int n_) { return Ab[(int64_t)s_ * ss + n_]; };
   const ClothParams& P = v.cp[v.node_cloth[n]];
   const int u = v.node_u[n], w = v.node_v[n];
   double yl0 = 0.0, yl1 = 0.0, yl2 = 0.0;
@@ -399,6 +433,19 @@ YS_HD void spmv_row(const View& v, const double* YS_RESTRICT x, int n, double y[
   y[4] = ye[1];
 }
 
+YS_HD void spmv_row(const View& v, const double* YS_RESTRICT x, int n, double y[5]) {
+  spmv_row_s(v, v.A, v.ntot, x, n, y);
+}
+
+// Right-hand side of the tangent solve of row block n for tangent k:
+// A dq = db - dA q (q the step's solution; dA, db the tangents of A, b).
+YS_HD void tangent_rhs_row(const View& v, const double* YS_RESTRICT q, int n, int k, double r[5]) {
+  const int64_t nt = v.ntot;
+  double y[5];
+  spmv_row_s(v, v.dA + k * nt, (int64_t)v.K * nt, q, n, y);
+  for (int c = 0; c < 5; ++c) r[c] = v.dB[((int64_t)c * v.K + k) * nt + n] - (v.trunc ? 0.0 : y[c]);
+}
+
 // Cloth::update (src/Cloth.cpp:111-148) for node n with the solved velocity.
 YS_HD void update_node(const View& v, const double* YS_RESTRICT xs, int n) {
   const int nt = v.ntot;
@@ -417,6 +464,34 @@ YS_HD void update_node(const View& v, const double* YS_RESTRICT xs, int n) {
       st(v.UVD, k, nt, n) = e;
       st(v.UV, k, nt, n) = ld(v.UV, k, nt, n) + e * h;
       st(v.UVB, k, nt, n) = ld(v.UVB, k, nt, n) + ld(v.SLIDE, k, nt, n) * e * h;
+    }
+  }
+}
+
+// update_node with tangents: xs / dxs hold the solution and its tangents
+// ([5][K][ntot]); the state arrays and their tangent arrays are updated
+// together (the slide indicator's value is the step's, its tangents dSLIDE).
+template <int K>
+YS_HD void update_node_dual(const View& v, const double* YS_RESTRICT xs, const double* YS_RESTRICT dxs, double* dX,
+                            double* dV, double* dUV, double* dUVD, double* dUVB, int n) {
+  typedef Dual<K> D;
+  const int nt = v.ntot;
+  const uint8_t fl = v.flags[n];
+  const double h = v.h;
+  for (int i = 0; i < 3; ++i) {
+    const D vel = ldT<D>(xs, dxs, i, nt, n);
+    stT(v.V, dV, i, nt, n, vel);
+    const D x = ldT<D>(v.X, dX, i, nt, n) + vel * h;
+    stT(v.X, dX, i, nt, n, x);
+    if (!(fl & YS_FIXED)) st(v.XF, i, nt, n) = x.v;
+  }
+  if (fl & YS_INTERIOR) {
+    for (int k = 0; k < 2; ++k) {
+      const D e = ldT<D>(xs, dxs, 3 + k, nt, n);
+      stT(v.UVD, dUVD, k, nt, n, e);
+      stT(v.UV, dUV, k, nt, n, ldT<D>(v.UV, dUV, k, nt, n) + e * h);
+      stT(v.UVB, dUVB, k, nt, n,
+          ldT<D>(v.UVB, dUVB, k, nt, n) + ldT<D>(v.SLIDE, v.dSLIDE, k, nt, n) * e * h);
     }
   }
 }

@@ -1,14 +1,18 @@
 // ys_kernels.cu -- CUDA kernels of one implicit step of a batch of cloths.
 //
-// Assembly: one thread per element in graph-coloured passes (each pass is a
-// compact list of anchor nodes whose elements touch disjoint node rows), so
-// every row is accumulated in a fixed order without atomics.
+// Assembly: one thread per element writes that element's record (forces and
+// Jacobian blocks), then one thread per node gathers the records touching its
+// row block in a fixed order, so every row is accumulated deterministically
+// without atomics. The element and gather kernels are templates over the
+// scalar type: double for the step, Dual<kTangents> for its forward-mode
+// sensitivities.
 // Solve: per-cloth Jacobi-PCG (Eigen's ConjugateGradient algorithm, as used by
 // src/Solvers.cpp:3-31) on the structured stencil matrix; thread blocks never
 // straddle cloths, so each cloth's dot products are a fixed-order sum of its
 // blocks' partials, recomputed redundantly by every block that needs them.
 #include <cfloat>
 
+#include "ys_elem_kernels.cuh"
 #include "ys_items.cuh"
 #include "ys_kernels.cuh"
 
@@ -21,58 +25,6 @@ __global__ void k_geom(View v, const int* __restrict__ nodes, int count) {
   if (t >= count) return;
   const int n = nodes[t];
   node_normal(v, n, v.cp[v.node_cloth[n]].W);
-}
-
-// one thread per (yarn direction, node): the edge starting at that node
-__global__ void __launch_bounds__(kBlock) k_edge_rec(View v, Records R) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 2LL * v.ntot) return;
-  const int k = t >= v.ntot ? 1 : 0;
-  const int n0 = (int)(t - (int64_t)k * v.ntot);
-  const ClothParams& P = v.cp[v.node_cloth[n0]];
-  if (k == 0 ? v.node_u[n0] >= P.W - 1 : v.node_v[n0] >= P.H - 1) return;
-  EdgeOut o;
-  edge_element(v, n0, n0 + (k == 0 ? 1 : P.W), k, o);
-  edge_store(v, R.edge, n0, k, o);
-}
-
-// one thread per (yarn direction, middle node) of a bend segment
-__global__ void __launch_bounds__(kBlock) k_bend_rec(View v, Records R) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 2LL * v.ntot) return;
-  const int k = t >= v.ntot ? 1 : 0;
-  const int n0 = (int)(t - (int64_t)k * v.ntot);
-  const ClothParams& P = v.cp[v.node_cloth[n0]];
-  const int pos = k == 0 ? v.node_u[n0] : v.node_v[n0], len = k == 0 ? P.W : P.H;
-  if (pos < 1 || pos > len - 2) return;
-  const int step = k == 0 ? 1 : P.W;
-  const int line = k == 0 ? P.warp_line_off + v.node_v[n0] : P.weft_line_off + v.node_u[n0];
-  bend_element(v, R.bend, n0 - step, n0, n0 + step, k, v.line_kb[line]);
-}
-
-// one thread per grid cell (top-left node): its two faces
-__global__ void k_face_rec(View v, Records R) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= v.ntot) return;
-  const ClothParams& P = v.cp[v.node_cloth[n]];
-  if (v.node_u[n] >= P.W - 1 || v.node_v[n] >= P.H - 1) return;
-  cell_faces(v, R.face, n);
-}
-
-// row blocks from edge / bend / face records, plus sliding friction
-__global__ void __launch_bounds__(kBlock) k_gather(View v, Records R) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n < v.ntot) gather_elements(v, R, n);
-}
-
-// one thread per (segment type, crossing)
-__global__ void __launch_bounds__(kBlock) k_shear_rec(View v, Records R) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 4LL * v.ntot) return;
-  const int seg = (int)(t / v.ntot);
-  const int n0 = (int)(t - (int64_t)seg * v.ntot);
-  if (!(v.flags[n0] & YS_INTERIOR)) return;
-  shear_element(v, R.shear, n0, seg);
 }
 
 // ----------------------------------------------------------------- solve
@@ -103,7 +55,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize(View v, Records R, Blocks b
   const int c = b.blk_cloth[blk];
   const int n = b.blk_node0[blk] + threadIdx.x;
   bool bad = false;
-  if (threadIdx.x < b.blk_count[blk]) bad = !gather_shear_finalize(v, R, n, so.dinv);
+  if (threadIdx.x < b.blk_count[blk]) bad = !gather_shear_finalize<double>(v, R, n, so.dinv);
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&so.pc[c].status, 1);
 }
 
@@ -283,19 +235,19 @@ void launch_geom(const View& v, const int* nodes, int n, cudaStream_t s) {
   if (n) k_geom<<<nblocks(n), kBlock, 0, s>>>(v, nodes, n);
 }
 void launch_edge_records(const View& v, const Records& R, cudaStream_t s) {
-  k_edge_rec<<<nblocks(2 * v.ntot), kBlock, 0, s>>>(v, R);
+  k_edge_rec<double><<<nblocks(2 * v.ntot), kBlock, 0, s>>>(v, R);
 }
 void launch_bend_records(const View& v, const Records& R, cudaStream_t s) {
-  k_bend_rec<<<nblocks(2 * v.ntot), kBlock, 0, s>>>(v, R);
+  k_bend_rec<double><<<nblocks(2 * v.ntot), kBlock, 0, s>>>(v, R);
 }
 void launch_face_records(const View& v, const Records& R, cudaStream_t s) {
-  k_face_rec<<<nblocks(v.ntot), kBlock, 0, s>>>(v, R);
+  k_face_rec<double><<<nblocks(v.ntot), kBlock, 0, s>>>(v, R);
 }
 void launch_gather(const View& v, const Records& R, cudaStream_t s) {
-  k_gather<<<nblocks(v.ntot), kBlock, 0, s>>>(v, R);
+  k_gather<double><<<nblocks(v.ntot), kBlock, 0, s>>>(v, R);
 }
 void launch_shear_records(const View& v, const Records& R, cudaStream_t s) {
-  k_shear_rec<<<nblocks(4 * v.ntot), kBlock, 0, s>>>(v, R);
+  k_shear_rec<double><<<nblocks(4 * v.ntot), kBlock, 0, s>>>(v, R);
 }
 void launch_finalize(const View& v, const Records& R, const Blocks& b, const Solver& so, cudaStream_t s) {
   k_finalize<<<b.nblk, kBlock, 0, s>>>(v, R, b, so);
@@ -315,6 +267,9 @@ void launch_pcg_dir(const View& v, const Blocks& b, const Solver& so, int it, cu
 }
 void launch_count_active(const View& v, const Solver& so, cudaStream_t s) {
   k_count_active<<<1, 256, 0, s>>>(so, v.ncloth);
+}
+void launch_check_solution(const View& v, const Blocks& b, const Solver& so, cudaStream_t s) {
+  k_check_solution<<<b.nblk, kBlock, 0, s>>>(v, b, so);
 }
 void launch_update(const View& v, const Blocks& b, const Solver& so, cudaStream_t s) {
   k_check_solution<<<b.nblk, kBlock, 0, s>>>(v, b, so);

@@ -56,7 +56,25 @@ void launch_pcg_spmv(const View& v, const Blocks& b, const Solver& so, cudaStrea
 void launch_pcg_axpy(const View& v, const Blocks& b, const Solver& so, int it, cudaStream_t s);
 void launch_pcg_dir(const View& v, const Blocks& b, const Solver& so, int it, cudaStream_t s);
 void launch_count_active(const View& v, const Solver& so, cudaStream_t s);
+void launch_check_solution(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
 void launch_update(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
 void launch_spmv(const View& v, const double* x, double* y, cudaStream_t s);
+
+// state tangents updated by the tangent step (layout [c][kTangents][ntot])
+struct TangentState {
+  double* dX;
+  double* dV;
+  double* dUV;
+  double* dUVD;
+  double* dUVB;
+};
+// the element / gather / finalize kernels over Dual<kTangents>
+void launch_assembly_dual(const View& v, const Records& R, const int* geom_nodes, int geom_n, cudaStream_t s);
+// rt[k][c][ntot] = db_k - dA_k q (or db_k when v.trunc) for k < kact
+void launch_tangent_rhs(const View& v, const double* q, double* rt, int kact, cudaStream_t s);
+// solution check, then Cloth::update of the state (solution so.x) and its
+// tangents (dq, [5][kTangents][ntot])
+void launch_update_dual(const View& v, const Blocks& b, const Solver& so, const double* dq, const TangentState& ts,
+                        cudaStream_t s);
 
 }  // namespace ys

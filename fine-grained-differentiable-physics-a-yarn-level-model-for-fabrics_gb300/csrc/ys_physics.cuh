@@ -22,56 +22,95 @@
 #include <math.h>
 
 #include "ys_common.cuh"
+#include "ys_dual.cuh"
 
 namespace ys {
 
 // ---------------------------------------------------------------- helpers
-YS_HD double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
-YS_HD double norm3(const double* a) { return sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); }
-YS_HD void cross3(const double* a, const double* b, double* o) {
+template <class T>
+YS_HD T dot3(const T* a, const T* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+template <class T>
+YS_HD T norm3(const T* a) { return sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); }
+template <class T>
+YS_HD void cross3(const T* a, const T* b, T* o) {
   o[0] = a[1] * b[2] - a[2] * b[1];
   o[1] = a[2] * b[0] - a[0] * b[2];
   o[2] = a[0] * b[1] - a[1] * b[0];
 }
-YS_HD void proj3(const double* d, double P[3][3]) {
+template <class T>
+YS_HD void proj3(const T* d, T P[3][3]) {
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) P[i][j] = (i == j ? 1.0 : 0.0) - d[i] * d[j];
 }
-YS_HD void matvec3(const double P[3][3], const double* a, double* o) {
+template <class T>
+YS_HD void matvec3(const T P[3][3], const T* a, T* o) {
   for (int i = 0; i < 3; ++i) o[i] = P[i][0] * a[0] + P[i][1] * a[1] + P[i][2] * a[2];
 }
-YS_HD void outer3(const double* a, const double* b, double O[3][3]) {
+template <class T>
+YS_HD void outer3(const T* a, const T* b, T O[3][3]) {
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) O[i][j] = a[i] * b[j];
 }
-YS_HD void matmul3(const double A[3][3], const double B[3][3], double O[3][3]) {
+template <class T>
+YS_HD void matmul3(const T A[3][3], const T B[3][3], T O[3][3]) {
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) O[i][j] = A[i][0] * B[0][j] + A[i][1] * B[1][j] + A[i][2] * B[2][j];
 }
 YS_HD double ld(const double* p, int comp, int ntot, int node) { return p[(int64_t)comp * ntot + node]; }
 YS_HD double& st(double* p, int comp, int ntot, int node) { return p[(int64_t)comp * ntot + node]; }
 
-// Adds val into A at (row node, row comp) x (col node, col comp); comp 0..2 =
-// Lagrangian x,y,z, comp 3 = the Eulerian DOF k (0 = u, 1 = v).
-YS_HD void add_A(const View& v, int rn, int rc, int cn, int cc, int k, double val, int du, int dv) {
-  if (rc < 3 && cc < 3) {
-    int s = stencil_index(du, dv);
-    if (s < 0) return;  // not reachable for the element types above; keeps every store in bounds
-    slot(v, YS_SLOT_LL + s * 9 + rc * 3 + cc, rn) += val;
-  } else if (rc < 3) {
-    int n = yarn_nbr(du, dv);
-    if (n < 0) slot(v, YS_SLOT_LE_SELF + rc * 2 + k, rn) += val;
-    else slot(v, YS_SLOT_LE_NBR + n * 3 + rc, rn) += val;
-  } else if (cc < 3) {
-    int n = yarn_nbr(du, dv);
-    if (n < 0) slot(v, YS_SLOT_EL_SELF + k * 3 + cc, rn) += val;
-    else slot(v, YS_SLOT_EL_NBR + n * 3 + cc, rn) += val;
-  } else {
-    int n = yarn_nbr(du, dv);
-    if (n < 0) slot(v, YS_SLOT_EE_SELF + k, rn) += val;
-    else slot(v, YS_SLOT_EE_NBR + n, rn) += val;
-  }
+// Scalar-generic loads and stores. A per-node array p holds comp c of node i
+// at p[c * ntot + i]; its tangent array dp (forward-mode runs only) holds
+// tangent k at dp[(c * K + k) * ntot + i]. Record buffers use the same rule
+// with c = field * nslot + slot. With T = double the tangent arrays are
+// never touched.
+YS_HD void lds(const double* p, const double* dp, int c, int ntot, int i, double& x) {
+  (void)dp;
+  x = p[(int64_t)c * ntot + i];
 }
+template <int K>
+YS_HD void lds(const double* p, const double* dp, int c, int ntot, int i, Dual<K>& x) {
+  x.v = p[(int64_t)c * ntot + i];
+  for (int k = 0; k < K; ++k) x.d[k] = dp ? dp[((int64_t)c * K + k) * ntot + i] : 0.0;
+}
+template <class T>
+YS_HD T ldT(const double* p, const double* dp, int c, int ntot, int i) {
+  T x;
+  lds(p, dp, c, ntot, i, x);
+  return x;
+}
+YS_HD void stT(double* p, double* dp, int c, int ntot, int i, const double& x) {
+  (void)dp;
+  p[(int64_t)c * ntot + i] = x;
+}
+template <int K>
+YS_HD void stT(double* p, double* dp, int c, int ntot, int i, const Dual<K>& x) {
+  p[(int64_t)c * ntot + i] = x.v;
+  if (dp)
+    for (int k = 0; k < K; ++k) dp[((int64_t)c * K + k) * ntot + i] = x.d[k];
+}
+// a parameter of index i in a table of n entries (tangent k at dp[k * n + i])
+YS_HD void ldp(const double* p, const double* dp, int i, int n, double& x) {
+  (void)dp;
+  (void)n;
+  x = p[i];
+}
+template <int K>
+YS_HD void ldp(const double* p, const double* dp, int i, int n, Dual<K>& x) {
+  x.v = p[i];
+  for (int k = 0; k < K; ++k) x.d[k] = dp ? dp[(int64_t)k * n + i] : 0.0;
+}
+template <class T>
+YS_HD T ldpT(const double* p, const double* dp, int i, int n) {
+  T x;
+  ldp(p, dp, i, n, x);
+  return x;
+}
+// per-cloth parameters S and mu (values in ClothParams, tangents [K][ncloth])
+template <class T>
+YS_HD T cloth_S(const View& v, int c) { return ldpT<T>(&v.cp[c].S, v.dS ? v.dS + c : nullptr, 0, v.ncloth); }
+template <class T>
+YS_HD T cloth_mu(const View& v, int c) { return ldpT<T>(&v.cp[c].mu, v.dmu ? v.dmu + c : nullptr, 0, v.ncloth); }
 
 // ------------------------------------------------------------ edge element
 // Local DOFs of an edge: x0 (0..2), e0 (3), x1 (4..6), e1 (7), where e is the
@@ -80,69 +119,86 @@ YS_HD void add_A(const View& v, int rn, int rc, int cn, int cc, int k, double va
 // (mass, inertia and dM/dt blocks are multiples of I, stretch adds P), so an
 // edge's contribution to A is held as 4 (a, b) pairs plus the Eulerian
 // couplings; block index p = 2*(row node) + (column node).
+template <class T>
 struct EdgeOut {
-  double llI[4], llP[4];  // A[x(n_a)][x(n_b)] = llI I + llP P
-  double d[3];            // edge direction (defines P)
-  double le[4][3];        // A[x(n_a)][e(n_b)]
-  double el[4][3];        // A[e(n_a)][x(n_b)]
-  double ee[4];           // A[e(n_a)][e(n_b)]
-  double b[8];            // contribution to b
-  double fe[2], kee[2], dee[2];  // F_E, dF_E/dE (position, velocity) before friction
-  double cl[2][3], cle[2][3];    // crimp-compression accumulators
-  double V[8];            // the step's velocity vector restricted to the edge (not stored)
+  T llI[4], llP[4];  // A[x(n_a)][x(n_b)] = llI I + llP P
+  T d[3];            // edge direction (defines P)
+  T le[4][3];        // A[x(n_a)][e(n_b)]
+  T el[4][3];        // A[e(n_a)][x(n_b)]
+  T ee[4];           // A[e(n_a)][e(n_b)]
+  T b[8];            // contribution to b
+  T fe[2], kee[2], dee[2];  // F_E, dF_E/dE (position, velocity) before friction
+  T cl[2][3], cle[2][3];    // crimp-compression accumulators
+  T V[8];            // the step's velocity vector restricted to the edge (not stored)
   double h, h2;
   bool in[2];
+  bool trunc;        // tangents of b through F and v only (M and D held constant)
 };
 constexpr int kEdgeFields = 65;
 
 enum Mat { kM = 0, kK = 1, kD = 2 };
 
-YS_HD double wt(const EdgeOut& o, int X) { return X == kM ? 1.0 : X == kK ? -o.h2 : -o.h; }
+template <class T>
+YS_HD double wt(const EdgeOut<T>& o, int X) { return X == kM ? 1.0 : X == kK ? -o.h2 : -o.h; }
+// a matrix coefficient as it enters b = h F + (M - h D^T) v: detached when
+// the tangents follow the reference's autograd, where M and D are built
+// without a graph (src/MatrixMp.cpp:40-99)
+template <class T>
+YS_HD T mcoef(const EdgeOut<T>& o, const T& x) { return o.trunc ? detach(x) : x; }
 
 // block (a, b) += val I of matrix X; b receives M V and -h D^T V
 // (src/TrainHelper.cpp:19-20). LL blocks of X_LL[find_index(f, d, "LL")] are
 // written transposed by To_Sparse_Mat (src/MatrixMp.cpp:54-65); a I + b P is
 // symmetric, so the transpose changes nothing here.
-YS_HD void acc_LLi(EdgeOut& o, int X, int a, int b, double val) {
+template <class T>
+YS_HD void acc_LLi(EdgeOut<T>& o, int X, int a, int b, const T& val) {
   o.llI[2 * a + b] += wt(o, X) * val;
-  if (X == kM)
-    for (int r = 0; r < 3; ++r) o.b[4 * a + r] += val * o.V[4 * b + r];
-  else if (X == kD)
-    for (int r = 0; r < 3; ++r) o.b[4 * b + r] -= o.h * val * o.V[4 * a + r];
+  if (X == kM) {
+    const T m = mcoef(o, val);
+    for (int r = 0; r < 3; ++r) o.b[4 * a + r] += m * o.V[4 * b + r];
+  } else if (X == kD) {
+    const T m = mcoef(o, val);
+    for (int r = 0; r < 3; ++r) o.b[4 * b + r] -= o.h * m * o.V[4 * a + r];
+  }
 }
-YS_HD void acc_LLp(EdgeOut& o, int a, int b, double val) { o.llP[2 * a + b] += -o.h2 * val; }  // stiffness only
+template <class T>
+YS_HD void acc_LLp(EdgeOut<T>& o, int a, int b, const T& val) { o.llP[2 * a + b] += -o.h2 * val; }  // stiffness only
 // A[x(n_a)][e(n_b)] (X_LE[find_index(n_a, n_b, "EL") + k])
-YS_HD void acc_LE(EdgeOut& o, int X, int a, int b, const double* vec) {
+template <class T>
+YS_HD void acc_LE(EdgeOut<T>& o, int X, int a, int b, const T* vec) {
   const double w = wt(o, X);
-  double s = 0.0;
+  T s = 0.0;
   for (int r = 0; r < 3; ++r) {
     o.le[2 * a + b][r] += w * vec[r];
-    if (X == kM) o.b[4 * a + r] += vec[r] * o.V[4 * b + 3];
-    s += vec[r] * o.V[4 * a + r];
+    if (X == kM) o.b[4 * a + r] += mcoef(o, vec[r]) * o.V[4 * b + 3];
+    if (X == kD) s += mcoef(o, vec[r]) * o.V[4 * a + r];
   }
   if (X == kD) o.b[4 * b + 3] -= o.h * s;
 }
 // A[e(n_a)][x(n_b)] (X_EL[find_index(n_b, n_a, "EL") + k])
-YS_HD void acc_EL(EdgeOut& o, int X, int a, int b, const double* vec) {
+template <class T>
+YS_HD void acc_EL(EdgeOut<T>& o, int X, int a, int b, const T* vec) {
   const double w = wt(o, X);
-  double s = 0.0;
+  T s = 0.0;
   for (int c = 0; c < 3; ++c) {
     o.el[2 * a + b][c] += w * vec[c];
-    s += vec[c] * o.V[4 * b + c];
-    if (X == kD) o.b[4 * b + c] -= o.h * vec[c] * o.V[4 * a + 3];
+    if (X == kM) s += mcoef(o, vec[c]) * o.V[4 * b + c];
+    if (X == kD) o.b[4 * b + c] -= o.h * mcoef(o, vec[c]) * o.V[4 * a + 3];
   }
   if (X == kM) o.b[4 * a + 3] += s;
 }
-YS_HD void acc_EE(EdgeOut& o, int X, int a, int b, double val) {
+template <class T>
+YS_HD void acc_EE(EdgeOut<T>& o, int X, int a, int b, const T& val) {
   o.ee[2 * a + b] += wt(o, X) * val;
-  if (X == kM) o.b[4 * a + 3] += val * o.V[4 * b + 3];
-  else if (X == kD) o.b[4 * b + 3] -= o.h * val * o.V[4 * a + 3];
+  if (X == kM) o.b[4 * a + 3] += mcoef(o, val) * o.V[4 * b + 3];
+  else if (X == kD) o.b[4 * b + 3] -= o.h * mcoef(o, val) * o.V[4 * a + 3];
   if (a == b) {
     if (X == kK) o.kee[a] += val;
     else if (X == kD) o.dee[a] += val;
   }
 }
-YS_HD void acc_F(EdgeOut& o, int dof, double f) {
+template <class T>
+YS_HD void acc_F(EdgeOut<T>& o, int dof, const T& f) {
   o.b[dof] += o.h * f;
   if ((dof & 3) == 3) o.fe[dof >> 2] += f;
 }
@@ -154,12 +210,14 @@ YS_HD void acc_F(EdgeOut& o, int dof, double f) {
 // isotropic node-node factors iso[p], the (x, e) columns lec[p][r] =
 // C(4a+r, 4b+3), the (e, x) rows elr[p][c] = C(4a+3, 4b+c) and eev[p] =
 // C(4a+3, 4b+3), added with sign s under the reference's interior tests.
+template <class T>
 struct EdgeJac {
-  double iso[4], lec[4][3], elr[4][3], eev[4];
+  T iso[4], lec[4][3], elr[4][3], eev[4];
 };
-YS_HD void acc_jac(EdgeOut& o, int X, double s, const EdgeJac& C) {
+template <class T>
+YS_HD void acc_jac(EdgeOut<T>& o, int X, double s, const EdgeJac<T>& C) {
   for (int p = 0; p < 4; ++p) acc_LLi(o, X, p >> 1, p & 1, s * C.iso[p]);
-  double t[3];
+  T t[3];
   for (int p = 0; p < 4; ++p) {
     const int a = p >> 1, b = p & 1;
     const bool ok = (a == b) ? o.in[a] : (o.in[0] && o.in[1]);
@@ -174,16 +232,18 @@ YS_HD void acc_jac(EdgeOut& o, int X, double s, const EdgeJac& C) {
 
 // All terms of one edge (src/PhysicsCloth.cpp:64-80): Mass, Gravity, Stretch,
 // Inertia, MDotVDot, ParaColli; forces and both Jacobians.
-YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut& o) {
+template <class T>
+YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o) {
   const int nt = v.ntot;
   const ClothParams& P = v.cp[v.node_cloth[n0]];
   const uint8_t f0 = v.flags[n0], f1 = v.flags[n1];
   o.in[0] = (f0 & YS_INTERIOR) != 0;
   o.in[1] = (f1 & YS_INTERIOR) != 0;
   const int line = (k == 0) ? P.warp_line_off + v.node_v[n0] : P.weft_line_off + v.node_u[n0];
-  const double rho = v.line_rho[line], ks = v.line_ks[line];
+  const T rho = ldpT<T>(v.line_rho, v.dline_rho, line, v.nlines), ks = ldpT<T>(v.line_ks, v.dline_ks, line, v.nlines);
   o.h = v.h;
   o.h2 = v.h * v.h;
+  o.trunc = v.trunc != 0;
   for (int p = 0; p < 4; ++p) {
     o.llI[p] = o.llP[p] = o.ee[p] = 0.0;
     for (int r = 0; r < 3; ++r) o.le[p][r] = o.el[p][r] = 0.0;
@@ -194,33 +254,33 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut& o) {
     for (int i = 0; i < 3; ++i) o.cl[t][i] = o.cle[t][i] = 0.0;
   }
   // geometry (src/ClothUnit.h:134-154)
-  double x0[3], x1[3], a0[3], a1[3], dx[3], w[3], d[3];
+  T x0[3], x1[3], a0[3], a1[3], dx[3], w[3], d[3];
   for (int i = 0; i < 3; ++i) {
-    x0[i] = ld(v.X, i, nt, n0); x1[i] = ld(v.X, i, nt, n1);
-    a0[i] = ld(v.V, i, nt, n0); a1[i] = ld(v.V, i, nt, n1);
+    x0[i] = ldT<T>(v.X, v.dX, i, nt, n0); x1[i] = ldT<T>(v.X, v.dX, i, nt, n1);
+    a0[i] = ldT<T>(v.V, v.dV, i, nt, n0); a1[i] = ldT<T>(v.V, v.dV, i, nt, n1);
   }
-  const double du = ld(v.UV, k, nt, n1) - ld(v.UV, k, nt, n0);
-  const double e0 = ld(v.UVD, k, nt, n0), e1 = ld(v.UVD, k, nt, n1);
+  const T du = ldT<T>(v.UV, v.dUV, k, nt, n1) - ldT<T>(v.UV, v.dUV, k, nt, n0);
+  const T e0 = ldT<T>(v.UVD, v.dUVD, k, nt, n0), e1 = ldT<T>(v.UVD, v.dUVD, k, nt, n1);
   for (int i = 0; i < 3; ++i) { dx[i] = x1[i] - x0[i]; w[i] = dx[i] / du; }
-  const double l = norm3(dx);
+  const T l = norm3(dx);
   for (int i = 0; i < 3; ++i) { d[i] = dx[i] / l; o.d[i] = d[i]; }
   for (int i = 0; i < 3; ++i) { o.V[i] = a0[i]; o.V[4 + i] = a1[i]; }
   o.V[3] = o.in[0] ? e0 : 0.0;
   o.V[7] = o.in[1] ? e1 : 0.0;
-  const double wTw = dot3(w, w);
-  const double nw = norm3(w);
-  double t3[3];
+  const T wTw = dot3(w, w);
+  const T nw = norm3(w);
+  T t3[3];
 
   // ---- Mass (src/PhysicsCloth.cpp:250-338)
   {
-    const double coeff = (1.0 / 6.0) * rho * du;
+    const T coeff = (1.0 / 6.0) * rho * du;
     acc_LLi(o, kM, 0, 0, 2.0 * coeff);
     acc_LLi(o, kM, 1, 0, coeff);
     acc_LLi(o, kM, 0, 1, coeff);
     acc_LLi(o, kM, 1, 1, 2.0 * coeff);
-    double LE2[3], LE1[3];
+    T LE2[3], LE1[3];
     for (int r = 0; r < 3; ++r) { LE2[r] = -2.0 * coeff * w[r]; LE1[r] = -1.0 * coeff * w[r]; }
-    const double EE2 = 2.0 * coeff * wTw, EE1 = 0.5 * EE2;
+    const T EE2 = 2.0 * coeff * wTw, EE1 = 0.5 * EE2;
     if (o.in[0]) { acc_LE(o, kM, 0, 0, LE2); acc_EL(o, kM, 0, 0, LE2); acc_EE(o, kM, 0, 0, EE2); }
     if (o.in[1]) { acc_LE(o, kM, 1, 1, LE2); acc_EL(o, kM, 1, 1, LE2); acc_EE(o, kM, 1, 1, EE2); }
     if (o.in[0] && o.in[1]) {
@@ -235,15 +295,15 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut& o) {
   // ---- Gravity_F / Gravity_D (src/PhysicsCloth.cpp:340-425)
   {
     for (int i = 0; i < 3; ++i) {
-      const double g = 0.5 * rho * P.G[i] * du;
+      const T g = 0.5 * rho * P.G[i] * du;
       acc_F(o, i, -g);
       acc_F(o, 4 + i, -g);
     }
-    double sx[3] = {x0[0] + x1[0], x0[1] + x1[1], x0[2] + x1[2]};
-    const double gx = dot3(P.G, sx);
+    T sx[3] = {x0[0] + x1[0], x0[1] + x1[1], x0[2] + x1[2]};
+    const T gx = P.G[0] * sx[0] + P.G[1] * sx[1] + P.G[2] * sx[2];
     if (o.in[0]) acc_F(o, 3, -((-0.5) * rho * gx));
     if (o.in[1]) acc_F(o, 7, -(0.5 * rho * gx));
-    double g0[3], g1[3];
+    T g0[3], g1[3];
     for (int r = 0; r < 3; ++r) { g0[r] = 0.5 * rho * P.G[r]; g1[r] = -g0[r]; }
     if (o.in[0]) { acc_EL(o, kK, 0, 0, g0); acc_LE(o, kK, 0, 0, g0); }
     if (o.in[1]) { acc_EL(o, kK, 1, 1, g1); acc_LE(o, kK, 1, 1, g1); }
@@ -258,21 +318,21 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut& o) {
   {
     const double sgn = (k == 0) ? 1.0 : -1.0;
     for (int i = 0; i < 3; ++i) {
-      const double f = ks * (nw - 1) * d[i];
+      const T f = ks * (nw - 1) * d[i];
       acc_F(o, i, f);
       acc_F(o, 4 + i, -f);
       o.cl[0][i] += sgn * f;
       o.cl[1][i] -= sgn * f;
     }
-    const double fe = 0.5 * ks * (nw * nw - 1);
+    const T fe = 0.5 * ks * (nw * nw - 1);
     if (o.in[0]) acc_F(o, 3, -fe);
     if (o.in[1]) acc_F(o, 7, fe);
     // LL = (ks / l) P - (ks / du) I, +LL on (0,0), (1,1) and -LL across
-    const double cP = ks / l, cI = -(ks / du);
+    const T cP = ks / l, cI = -(ks / du);
     acc_LLp(o, 0, 0, cP); acc_LLp(o, 1, 0, -cP); acc_LLp(o, 0, 1, -cP); acc_LLp(o, 1, 1, cP);
     acc_LLi(o, kK, 0, 0, cI); acc_LLi(o, kK, 1, 0, -cI); acc_LLi(o, kK, 0, 1, -cI); acc_LLi(o, kK, 1, 1, cI);
-    const double EE = -ks * ((nw * nw) / du);
-    double LE[3], EL[3], nLE[3], nEL[3];
+    const T EE = -ks * ((nw * nw) / du);
+    T LE[3], EL[3], nLE[3], nEL[3];
     for (int r = 0; r < 3; ++r) {
       LE[r] = ks * (nw / du) * d[r];
       EL[r] = ks / du * w[r];
@@ -295,62 +355,62 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut& o) {
   }
   // ---- ParaColli_F / ParaColli_D (src/PhysicsCloth.cpp:989-1069)
   {
-    const double dd = (((f0 & YS_FLIP) != 0) != ((f1 & YS_FLIP) != 0)) ? 4.0 * P.R : 2.0 * P.R;
-    double rl = dd - du;
+    const T dd = (((f0 & YS_FLIP) != 0) != ((f1 & YS_FLIP) != 0)) ? 4.0 * P.R : 2.0 * P.R;
+    T rl = dd - du;
     if (rl < 0) rl = 0.0;
-    const double fu0 = P.kc * P.L * rl;
+    const T fu0 = P.kc * P.L * rl;
     if (o.in[0]) acc_F(o, 3, fu0);
     if (o.in[1]) acc_F(o, 7, -fu0);
-    const double ee = -P.kc * P.L * rl;
+    const T ee = -P.kc * P.L * rl;
     if (o.in[0]) acc_EE(o, kK, 0, 0, ee);
     if (o.in[1]) acc_EE(o, kK, 1, 1, ee);
     if (o.in[0] && o.in[1]) { acc_EE(o, kK, 0, 1, ee); acc_EE(o, kK, 1, 0, ee); }
   }
 
   // ---- kinetic-energy terms: shared sums
-  double m0a[3], m1a[3];
+  T m0a[3], m1a[3];
   for (int i = 0; i < 3; ++i) { m0a[i] = 2.0 * a0[i] + a1[i]; m1a[i] = a0[i] + 2.0 * a1[i]; }
-  const double m0e = 2.0 * e0 + e1, m1e = e0 + 2.0 * e1;
-  const double Saa = dot3(a0, m0a) + dot3(a1, m1a);
-  double Sae[3], Sea[3];
+  const T m0e = 2.0 * e0 + e1, m1e = e0 + 2.0 * e1;
+  const T Saa = dot3(a0, m0a) + dot3(a1, m1a);
+  T Sae[3], Sea[3];
   for (int i = 0; i < 3; ++i) { Sae[i] = a0[i] * m0e + a1[i] * m1e; Sea[i] = e0 * m0a[i] + e1 * m1a[i]; }
-  const double See = e0 * m0e + e1 * m1e;
-  const double r6 = (1.0 / 6.0) * rho;
-  const double sc = 1.0 / 6.0 * rho * du;
-  const double wSae = dot3(w, Sae), wSea = dot3(w, Sea);
-  const double pj = -(-1.0 / du);  // (-w_x0)_j for the active component j
-  EdgeJac C;
+  const T See = e0 * m0e + e1 * m1e;
+  const T r6 = (1.0 / 6.0) * rho;
+  const T sc = 1.0 / 6.0 * rho * du;
+  const T wSae = dot3(w, Sae), wSea = dot3(w, Sea);
+  const T pj = -(-1.0 / du);  // (-w_x0)_j for the active component j
+  EdgeJac<T> C;
 
   // ---- Inertia_F (src/PhysicsCloth.cpp:1071-1186)
   {
     for (int j = 0; j < 3; ++j) {
-      const double sj = (-2.0 / (du * du) * dx[j]);
-      const double T0 = 0.5 * (sc * (pj * Sae[j] + pj * Sea[j] + sj * See));
+      const T sj = (-2.0 / (du * du) * dx[j]);
+      const T T0 = 0.5 * (sc * (pj * Sae[j] + pj * Sea[j] + sj * See));
       acc_F(o, j, T0);
       acc_F(o, 4 + j, -T0);
     }
-    const double QM = Saa - wSae - wSea + wTw * See;
-    const double Quv = (-1.0 / du) * wSae + (-1.0 / du) * wSea + (2.0 / du) * wTw * See;
-    const double Tuv0 = 0.5 * (-(1.0 / 6.0) * rho * QM + (1.0 / 6.0) * rho * du * Quv);
+    const T QM = Saa - wSae - wSea + wTw * See;
+    const T Quv = (-1.0 / du) * wSae + (-1.0 / du) * wSea + (2.0 / du) * wTw * See;
+    const T Tuv0 = 0.5 * (-(1.0 / 6.0) * rho * QM + (1.0 / 6.0) * rho * du * Quv);
     if (o.in[0]) acc_F(o, 3, Tuv0);
     if (o.in[1]) acc_F(o, 7, -Tuv0);
   }
   // ---- Inertia_D_Pos (src/PhysicsCloth.cpp:1188-1601)
   {
-    const double T00 = 0.5 * (r6 * ((2 / (du * du)) * See));
-    double Tx0uv0[3], Tuv0x0[3];
+    const T T00 = 0.5 * (r6 * ((2 / (du * du)) * See));
+    T Tx0uv0[3], Tuv0x0[3];
     for (int j = 0; j < 3; ++j) {
-      const double Qx0 = pj * Sae[j] + pj * Sea[j] + (-2.0 / (du * du) * dx[j]) * See;
-      const double c2 = 1.0 / (du * du);
+      const T Qx0 = pj * Sae[j] + pj * Sea[j] + (-2.0 / (du * du) * dx[j]) * See;
+      const T c2 = 1.0 / (du * du);
       // the sign-asymmetric mixed block of src/PhysicsCloth.cpp:1357-1361
-      const double Qx0uv0 = (-c2) * Sae[j] + (-(-c2)) * Sea[j] + ((-4.0 / (du * du)) * w[j]) * See;
+      const T Qx0uv0 = (-c2) * Sae[j] + (-(-c2)) * Sea[j] + ((-4.0 / (du * du)) * w[j]) * See;
       Tx0uv0[j] = 0.5 * ((-1.0 / 6.0) * rho * Qx0 + (1.0 / 6.0) * rho * du * Qx0uv0);
       Tuv0x0[j] = 0.5 * ((-1.0 / 6.0) * rho * Qx0 + (1.0 / 6.0) * rho * du * (-Qx0uv0));
     }
-    const double Quv0 = (-1.0 / du) * wSae + (-1.0 / du) * wSea + (2.0 / du) * wTw * See;
-    const double c6 = 2 / (du * du);
-    const double Quvuv = (-c6) * wSae + (-c6) * wSea + (6 / (du * du)) * wTw * See;
-    const double Tuu = 0.5 * ((-1.0 / 6.0) * rho * Quv0 - (1.0 / 6.0) * rho * Quv0 + (1.0 / 6.0) * rho * du * Quvuv);
+    const T Quv0 = (-1.0 / du) * wSae + (-1.0 / du) * wSea + (2.0 / du) * wTw * See;
+    const T c6 = 2 / (du * du);
+    const T Quvuv = (-c6) * wSae + (-c6) * wSea + (6 / (du * du)) * wTw * See;
+    const T Tuu = 0.5 * ((-1.0 / 6.0) * rho * Quv0 - (1.0 / 6.0) * rho * Quv0 + (1.0 / 6.0) * rho * du * Quvuv);
     for (int p = 0; p < 4; ++p) {
       const double sgn = ((p >> 1) == (p & 1)) ? 1.0 : -1.0;
       C.iso[p] = sgn * T00;
@@ -361,17 +421,17 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut& o) {
   }
   // ---- Inertia_D_Vel (src/PhysicsCloth.cpp:1602-1901): row x_j of C = M_xj qdot
   {
-    const double me_[2] = {m0e, m1e};
-    const double* ma_[2] = {m0a, m1a};
+    const T me_[2] = {m0e, m1e};
+    const T* ma_[2] = {m0a, m1a};
     for (int b = 0; b < 2; ++b) {
-      const double iso = sc * (pj * me_[b]);
-      double lec[3], elr[3];
-      const double wm = dot3(w, ma_[b]);
+      const T iso = sc * (pj * me_[b]);
+      T lec[3], elr[3];
+      const T wm = dot3(w, ma_[b]);
       for (int r = 0; r < 3; ++r) {
         lec[r] = sc * (pj * ma_[b][r] + (-2.0 / (du * du) * dx[r]) * me_[b]);
         elr[r] = -(1.0 / 6.0) * rho * (ma_[b][r] - w[r] * me_[b]) + (1.0 / 6.0) * rho * du * ((-1.0 / du) * w[r] * me_[b]);
       }
-      const double eev = -(1.0 / 6.0) * rho * (-wm + wTw * me_[b]) +
+      const T eev = -(1.0 / 6.0) * rho * (-wm + wTw * me_[b]) +
                          (1.0 / 6.0) * rho * du * ((-1.0 / du) * wm + (2.0 / du) * wTw * me_[b]);
       for (int a = 0; a < 2; ++a) {
         const double sgn = a == 0 ? 1.0 : -1.0;  // rows of x1 / uv1 are the negated rows of x0 / uv0
@@ -385,15 +445,15 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut& o) {
   }
   // ---- MDotVDot (src/PhysicsCloth.cpp:1903-2577)
   {
-    const double dud = e1 - e0;
-    double wd[3];
+    const T dud = e1 - e0;
+    T wd[3];
     for (int i = 0; i < 3; ++i) wd[i] = ((a1[i] - a0[i]) * du - dx[i] * dud) / (du * du);
-    const double wTwd = dot3(w, wd) + dot3(wd, w);
+    const T wTwd = dot3(w, wd) + dot3(wd, w);
     // B_M m and B_dot m for m = m0, m1 (4-vectors); M_dot qdot = r6 dud (B_M m) + r6 du (B_dot m)
-    double BMm[2][4], Bdm[2][4], r[8];
+    T BMm[2][4], Bdm[2][4], r[8];
     for (int b = 0; b < 2; ++b) {
-      const double* ma = b == 0 ? m0a : m1a;
-      const double me = b == 0 ? m0e : m1e;
+      const T* ma = b == 0 ? m0a : m1a;
+      const T me = b == 0 ? m0e : m1e;
       for (int i = 0; i < 3; ++i) { BMm[b][i] = ma[i] + (-w[i]) * me; Bdm[b][i] = (-wd[i]) * me; }
       BMm[b][3] = (-w[0]) * ma[0] + (-w[1]) * ma[1] + (-w[2]) * ma[2] + wTw * me;
       Bdm[b][3] = (-wd[0]) * ma[0] + (-wd[1]) * ma[1] + (-wd[2]) * ma[2] + wTwd * me;
@@ -406,26 +466,26 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut& o) {
     // MDotVDot_D_Pos, added (src/PhysicsCloth.cpp:2154-2234)
     for (int t = 0; t < 2; ++t) {
       const double sw = t == 0 ? -1.0 : 1.0;
-      const double wxj = sw * (1.0 / du);
-      const double P1 = -wxj;
-      const double wdxj = t == 0 ? (dud / (du * du)) : -(dud / (du * du));
-      const double P2 = -wdxj;
-      double wuv[3], wduv[3];
+      const T wxj = sw * (1.0 / du);
+      const T P1 = -wxj;
+      const T wdxj = t == 0 ? (dud / (du * du)) : -(dud / (du * du));
+      const T P2 = -wdxj;
+      T wuv[3], wduv[3];
       for (int i = 0; i < 3; ++i) wuv[i] = (sw * w[i]) / du;
-      const double wTwuv = sw * (2 / du) * wTw;
+      const T wTwuv = sw * (2 / du) * wTw;
       for (int i = 0; i < 3; ++i) {
         wduv[i] = (a1[i] - a0[i]) / (du * du) - (4 * dx[i] * dud) / (du * du * du);
         if (t == 1) wduv[i] = -wduv[i];
       }
-      const double wTwduv = 2 * dot3(wuv, wd) + 2 * dot3(wduv, w);
+      const T wTwduv = 2 * dot3(wuv, wd) + 2 * dot3(wduv, w);
       for (int b = 0; b < 2; ++b) {
-        const double* ma = b == 0 ? m0a : m1a;
-        const double me = b == 0 ? m0e : m1e;
+        const T* ma = b == 0 ? m0a : m1a;
+        const T me = b == 0 ? m0e : m1e;
         const int p = 2 * b + t;
         C.iso[p] = r6 * dud * (P1 * me) + r6 * du * (P2 * me);
         for (int j = 0; j < 3; ++j) {
-          const double S1 = (sw * 2.0 / (du * du) * dx[j]);
-          const double S2 = 2 * (wxj * wd[j]) + 2 * (w[j] * wdxj);
+          const T S1 = (sw * 2.0 / (du * du) * dx[j]);
+          const T S2 = 2 * (wxj * wd[j]) + 2 * (w[j] * wdxj);
           C.elr[p][j] = r6 * dud * (P1 * ma[j] + S1 * me) + r6 * du * (P2 * ma[j] + S2 * me);
           C.lec[p][j] = r6 * dud * (wuv[j] * me) - r6 * r[4 * b + j] + r6 * du * (-wduv[j] * me);
         }
@@ -437,20 +497,20 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut& o) {
     // MDotVDot_D_Vel, subtracted (src/PhysicsCloth.cpp:2342-2577)
     for (int t = 0; t < 2; ++t) {
       const double sw = t == 0 ? -1.0 : 1.0;
-      const double wdj = sw * (1.0 / du);
-      const double P1 = -wdj;
-      double wdv[3];
+      const T wdj = sw * (1.0 / du);
+      const T P1 = -wdj;
+      T wdv[3];
       for (int i = 0; i < 3; ++i) wdv[i] = (t == 0 ? (1.0 / du) : (-1.0 / du)) * w[i];
-      const double wtwd = 2 * dot3(w, wdv);
-      const double cm = (t == 0 ? -1.0 : 1.0) * (1.0 / 6.0) * rho;
+      const T wtwd = 2 * dot3(w, wdv);
+      const T cm = (t == 0 ? -1.0 : 1.0) * (1.0 / 6.0) * rho;
       for (int b = 0; b < 2; ++b) {
-        const double* ma = b == 0 ? m0a : m1a;
-        const double me = b == 0 ? m0e : m1e;
+        const T* ma = b == 0 ? m0a : m1a;
+        const T me = b == 0 ? m0e : m1e;
         const double f = (b == t) ? 2.0 : 1.0;  // [[2B, B], [B, 2B]] block factor of M_dot
         const int p = 2 * b + t;
         C.iso[p] = (1.0 / 6.0) * rho * du * (P1 * me) + (r6 * dud * (f * 1.0) + r6 * du * (f * 0.0));
         for (int j = 0; j < 3; ++j) {
-          const double S1 = 2 * (w[j] * wdj);
+          const T S1 = 2 * (w[j] * wdj);
           C.elr[p][j] = (1.0 / 6.0) * rho * du * (P1 * ma[j] + S1 * me) +
                         (r6 * dud * (f * -w[j]) + r6 * du * (f * -wd[j]));
           C.lec[p][j] = cm * BMm[b][j] + (1.0 / 6.0) * rho * du * (-wdv[j] * me) +
@@ -466,11 +526,12 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut& o) {
 }
 
 // record layout of an edge in the per-element buffer (field-major over the
-// 2 * ntot edge slots: slot = k * ntot + n0)
-YS_HD void edge_store(const View& v, double* buf, int n0, int k, const EdgeOut& o) {
-  const int64_t stride = 2LL * v.ntot, base = (int64_t)k * v.ntot + n0;
+// 2 * ntot edge slots: slot = k * ntot + n0; tangents in dbuf)
+template <class T>
+YS_HD void edge_store(const View& v, double* buf, double* dbuf, int n0, int k, const EdgeOut<T>& o) {
+  const int nt = v.ntot;
   int f = 0;
-  auto put = [&](double x) { buf[(int64_t)(f++) * stride + base] = x; };
+  auto put = [&](const T& x) { stT(buf, dbuf, 2 * (f++) + k, nt, n0, x); };
   for (int p = 0; p < 4; ++p) put(o.llI[p]);
   for (int p = 0; p < 4; ++p) put(o.llP[p]);
   for (int i = 0; i < 3; ++i) put(o.d[i]);
@@ -487,13 +548,15 @@ constexpr int kE_llI = 0, kE_llP = 4, kE_d = 8, kE_le = 11, kE_el = 23, kE_ee = 
               kE_cl = 53, kE_cle = 59;
 
 // ------------------------------------------------------------ bend element
+template <class T>
 struct BendGeom {
-  double du, l1, l2, d1[3], d2[3], P1[3][3], P2[3][3], theta;
+  T du, l1, l2, d1[3], d2[3], P1[3][3], P2[3][3], theta;
 };
 // src/ClothUnit.h:197-210; the theta clamp uses EPS = DBL_MIN
 // (src/Constants.h:25) and so never changes a finite value.
-YS_HD void bend_geom(const double* x2, const double* x0, const double* x1, double du, BendGeom& g) {
-  double a1[3], a2[3];
+template <class T>
+YS_HD void bend_geom(const T* x2, const T* x0, const T* x1, T du, BendGeom<T>& g) {
+  T a1[3], a2[3];
   for (int i = 0; i < 3; ++i) { a1[i] = x1[i] - x0[i]; a2[i] = x2[i] - x0[i]; }
   g.du = du;
   g.l1 = norm3(a1);
@@ -501,7 +564,7 @@ YS_HD void bend_geom(const double* x2, const double* x0, const double* x1, doubl
   for (int i = 0; i < 3; ++i) { g.d1[i] = a1[i] / g.l1; g.d2[i] = a2[i] / g.l2; }
   proj3(g.d1, g.P1);
   proj3(g.d2, g.P2);
-  double c = -dot3(g.d1, g.d2);
+  T c = -dot3(g.d1, g.d2);
   const double lo = -1.0 + 2.2250738585072014e-308, hi = 1.0 - 2.2250738585072014e-308;
   if (c < lo) c = lo;
   if (c > hi) c = hi;
@@ -510,50 +573,52 @@ YS_HD void bend_geom(const double* x2, const double* x0, const double* x1, doubl
 
 // Bending force and Hessian blocks shared by Bending_* and Crimp_Bending_*
 // (src/PhysicsCloth.cpp:579-822, 824-987).
+template <class T>
 struct BendTerms {
-  double Fx1[3], Fx2[3];
-  double L11[3][3], L12[3][3], L21[3][3], L22[3][3];
-  double L1E1[3], L2E1[3];
+  T Fx1[3], Fx2[3];
+  T L11[3][3], L12[3][3], L21[3][3], L22[3][3];
+  T L1E1[3], L2E1[3];
   bool active;
 };
-YS_HD void bend_terms(const BendGeom& g, double kb, BendTerms& t) {
+template <class T>
+YS_HD void bend_terms(const BendGeom<T>& g, const T& kb, BendTerms<T>& t) {
   for (int i = 0; i < 3; ++i) {
     t.Fx1[i] = t.Fx2[i] = t.L1E1[i] = t.L2E1[i] = 0.0;
     for (int j = 0; j < 3; ++j) t.L11[i][j] = t.L12[i][j] = t.L21[i][j] = t.L22[i][j] = 0.0;
   }
-  const double th = g.theta, s = sin(th);
+  const T th = g.theta, s = sin(th);
   t.active = (s != 0.0);
   if (!t.active) return;
-  const double co = cos(th), du = g.du;
-  double a[3], b[3];
+  const T co = cos(th), du = g.du;
+  T a[3], b[3];
   matvec3(g.P1, g.d2, a);
   matvec3(g.P2, g.d1, b);
-  const double c1 = (-2 * kb * th) / (g.l1 * du * s), c2 = (-2 * kb * th) / (g.l2 * du * s);
+  const T c1 = (-2 * kb * th) / (g.l1 * du * s), c2 = (-2 * kb * th) / (g.l2 * du * s);
   for (int i = 0; i < 3; ++i) { t.Fx1[i] = c1 * a[i]; t.Fx2[i] = c2 * b[i]; }
-  const double k11 = (2 * kb) / ((g.l1 * g.l1) * du * s), k12 = (-2 * kb) / (g.l1 * g.l2 * du * s);
-  const double k22 = (2 * kb) / ((g.l2 * g.l2) * du * s);
-  const double cs2 = co / (s * s), is = 1 / s;
-  double T[3][3];
+  const T k11 = (2 * kb) / ((g.l1 * g.l1) * du * s), k12 = (-2 * kb) / (g.l1 * g.l2 * du * s);
+  const T k22 = (2 * kb) / ((g.l2 * g.l2) * du * s);
+  const T cs2 = co / (s * s), is = 1 / s;
+  T Tm[3][3];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
-      const double ad1 = a[i] * g.d1[j], aa = a[i] * a[j], d1a = g.d1[i] * a[j];
-      const double bd2 = b[i] * g.d2[j], bb = b[i] * b[j], d2b = g.d2[i] * b[j];
+      const T ad1 = a[i] * g.d1[j], aa = a[i] * a[j], d1a = g.d1[i] * a[j];
+      const T bd2 = b[i] * g.d2[j], bb = b[i] * b[j], d2b = g.d2[i] * b[j];
       t.L11[i][j] = k11 * (th * (ad1 + cs2 * aa + co * g.P1[i][j] + d1a) - is * aa);
       t.L22[i][j] = k22 * (th * (bd2 + cs2 * bb + co * g.P2[i][j] + d2b) - is * bb);
-      T[i][j] = th * (g.P1[i][j] - cs2 * ad1) + is * ad1;
+      Tm[i][j] = th * (g.P1[i][j] - cs2 * ad1) + is * ad1;
     }
-  matmul3(T, g.P2, t.L12);
+  matmul3(Tm, g.P2, t.L12);
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) t.L12[i][j] *= k12;
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
-      const double bd2 = b[i] * g.d2[j];
-      T[i][j] = th * (g.P2[i][j] - cs2 * bd2) + is * bd2;
+      const T bd2 = b[i] * g.d2[j];
+      Tm[i][j] = th * (g.P2[i][j] - cs2 * bd2) + is * bd2;
     }
-  matmul3(T, g.P1, t.L21);
+  matmul3(Tm, g.P1, t.L21);
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) t.L21[i][j] *= k12;
-  const double e1 = (2 * kb * th) / (g.l1 * (du * du) * s), e2 = (2 * kb * th) / (g.l2 * (du * du) * s);
+  const T e1 = (2 * kb * th) / (g.l1 * (du * du) * s), e2 = (2 * kb * th) / (g.l2 * (du * du) * s);
   for (int i = 0; i < 3; ++i) { t.L1E1[i] = e1 * a[i]; t.L2E1[i] = e2 * b[i]; }
 }
 
@@ -570,16 +635,24 @@ constexpr int kB_L11 = 0, kB_L12 = 9, kB_L21 = 18, kB_L22 = 27, kB_L1E1 = 36, kB
 // Crimp_Bending_F / Crimp_Bending_D on the crimp-offset centre lines
 // (src/PhysicsCloth.cpp:824-987) for the segment n2 - n0 - n1 along yarn
 // direction k; written to the bend buffer at slot k * ntot + n0.
-YS_HD void bend_element(const View& v, double* buf, int n2, int n0, int n1, int k, double kb) {
+template <class T>
+YS_HD void bend_element(const View& v, double* buf, double* dbuf, int n2, int n0, int n1, int k, int line) {
   const int nt = v.ntot;
   const int64_t stride = 2LL * nt, base = (int64_t)k * nt + n0;
-  auto put = [&](int f, double x) { buf[(int64_t)f * stride + base] = x; };
+  (void)stride;
+  (void)base;
+  const T kb = ldpT<T>(v.line_kb, v.dline_kb, line, v.nlines);
+  auto put = [&](int f, const T& x) { stT(buf, dbuf, 2 * f + k, nt, n0, x); };
   {
-    double x2[3], x0[3], x1[3];
-    for (int i = 0; i < 3; ++i) { x2[i] = ld(v.X, i, nt, n2); x0[i] = ld(v.X, i, nt, n0); x1[i] = ld(v.X, i, nt, n1); }
-    BendGeom g;
-    bend_geom(x2, x0, x1, ld(v.UV, k, nt, n1) - ld(v.UV, k, nt, n2), g);
-    BendTerms t;
+    T x2[3], x0[3], x1[3];
+    for (int i = 0; i < 3; ++i) {
+      x2[i] = ldT<T>(v.X, v.dX, i, nt, n2);
+      x0[i] = ldT<T>(v.X, v.dX, i, nt, n0);
+      x1[i] = ldT<T>(v.X, v.dX, i, nt, n1);
+    }
+    BendGeom<T> g;
+    bend_geom(x2, x0, x1, ldT<T>(v.UV, v.dUV, k, nt, n1) - ldT<T>(v.UV, v.dUV, k, nt, n2), g);
+    BendTerms<T> t;
     bend_terms(g, kb, t);
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) {
@@ -594,24 +667,25 @@ YS_HD void bend_element(const View& v, double* buf, int n2, int n0, int n1, int 
       put(kB_Fx1 + i, t.Fx1[i]);
       put(kB_Fx2 + i, t.Fx2[i]);
     }
-    const double th = g.theta, du = g.du;
+    const T th = g.theta, du = g.du;
     put(kB_E1E1, (-2 * kb * (th * th)) / (du * du * du));
     put(kB_Fu2, (-kb * th) / (du * du));
   }
   {
     const double R = v.cp[v.node_cloth[n0]].R;
     const double sg = k == 0 ? -1.0 : 1.0;  // warp: x - R n, weft: x + R n
-    double x[3][3];
+    T x[3][3];
     const int nd[3] = {n2, n0, n1};
     for (int m = 0; m < 3; ++m) {
       const bool in = (v.flags[nd[m]] & YS_INTERIOR) != 0;
       for (int i = 0; i < 3; ++i)
-        x[m][i] = in ? ld(v.X, i, nt, nd[m]) + sg * (R * ld(v.NRM, i, nt, nd[m])) : ld(v.X, i, nt, nd[m]);
+        x[m][i] = in ? ldT<T>(v.X, v.dX, i, nt, nd[m]) + sg * (R * ldT<T>(v.NRM, v.dNRM, i, nt, nd[m]))
+                     : ldT<T>(v.X, v.dX, i, nt, nd[m]);
     }
     // crimp segments keep the EPos of the build (src/Cloth.cpp:107)
-    BendGeom g;
-    bend_geom(x[0], x[1], x[2], ld(v.UV0, k, nt, n1) - ld(v.UV0, k, nt, n2), g);
-    BendTerms t;
+    BendGeom<T> g;
+    bend_geom(x[0], x[1], x[2], T(ld(v.UV0, k, nt, n1) - ld(v.UV0, k, nt, n2)), g);
+    BendTerms<T> t;
     bend_terms(g, kb, t);
     for (int i = 0; i < 3; ++i) {
       put(kB_cFx1 + i, t.Fx1[i]);
@@ -625,34 +699,37 @@ YS_HD void bend_element(const View& v, double* buf, int n2, int n0, int n1, int 
 // ------------------------------------------------------------ wind (faces)
 // Wind_F (src/PhysicsCloth.cpp:3091-3107), face geometry src/ClothUnit.h:268-273;
 // returns wind_force / 3, the share of each of the face's three nodes.
-YS_HD void wind_face(const View& v, const ClothParams& P, int n1, int n2, int n3, double* f3) {
+template <class T>
+YS_HD void wind_face(const View& v, const ClothParams& P, int n1, int n2, int n3, T* f3) {
   const int nt = v.ntot;
-  double e1[3], e2[3], cr[3], n[3], fv[3], rel[3];
+  T e1[3], e2[3], cr[3], n[3], fv[3], rel[3];
   for (int i = 0; i < 3; ++i) {
-    e1[i] = ld(v.X, i, nt, n2) - ld(v.X, i, nt, n1);
-    e2[i] = ld(v.X, i, nt, n3) - ld(v.X, i, nt, n1);
+    const T xa = ldT<T>(v.X, v.dX, i, nt, n1);
+    e1[i] = ldT<T>(v.X, v.dX, i, nt, n2) - xa;
+    e2[i] = ldT<T>(v.X, v.dX, i, nt, n3) - xa;
   }
   cross3(e1, e2, cr);
-  const double nc = norm3(cr), area = 0.5 * nc;
+  const T nc = norm3(cr), area = 0.5 * nc;
   for (int i = 0; i < 3; ++i) n[i] = (nc == 0.0) ? cr[i] : cr[i] / nc;
   for (int i = 0; i < 3; ++i) {
-    fv[i] = (ld(v.V, i, nt, n1) + ld(v.V, i, nt, n2) + ld(v.V, i, nt, n3)) / 3.0;
+    fv[i] = (ldT<T>(v.V, v.dV, i, nt, n1) + ldT<T>(v.V, v.dV, i, nt, n2) + ldT<T>(v.V, v.dV, i, nt, n3)) / 3.0;
     rel[i] = P.wind[i] - fv[i];
   }
-  const double vn = dot3(n, rel);
+  const T vn = dot3(n, rel);
   for (int i = 0; i < 3; ++i) {
-    const double tang = rel[i] - vn * n[i];
-    const double f = P.wind_rho * area * fabs(vn) * vn * n[i] + P.wind_drag * area * tang;
+    const T tang = rel[i] - vn * n[i];
+    const T f = P.wind_rho * area * fabs(vn) * vn * n[i] + P.wind_drag * area * tang;
     f3[i] = f / 3.0;
   }
 }
 
 // cell with top-left node tl: faces (src/Cloth.cpp:271-287) written to the
 // face buffer [6][ntot] (face A then face B, each wind_force / 3)
-YS_HD void cell_faces(const View& v, double* buf, int tl) {
+template <class T>
+YS_HD void cell_faces(const View& v, double* buf, double* dbuf, int tl) {
   const ClothParams& P = v.cp[v.node_cloth[tl]];
   const int tr = tl + 1, bl = tl + P.W, br = tl + P.W + 1;
-  double fa[3], fb[3];
+  T fa[3], fb[3];
   if (((v.node_u[tl] + v.node_v[tl]) & 1) == 0) {
     wind_face(v, P, tl, tr, br, fa);
     wind_face(v, P, tl, br, bl, fb);
@@ -661,8 +738,8 @@ YS_HD void cell_faces(const View& v, double* buf, int tl) {
     wind_face(v, P, tr, br, bl, fb);
   }
   for (int i = 0; i < 3; ++i) {
-    buf[(int64_t)i * v.ntot + tl] = fa[i];
-    buf[(int64_t)(3 + i) * v.ntot + tl] = fb[i];
+    stT(buf, dbuf, i, v.ntot, tl, fa[i]);
+    stT(buf, dbuf, 3 + i, v.ntot, tl, fb[i]);
   }
 }
 
@@ -671,8 +748,10 @@ YS_HD void cell_faces(const View& v, double* buf, int tl) {
 // centred 5-point stencil = eigenvector of the smallest eigenvalue of its 3x3
 // scatter matrix (cyclic Jacobi rotations), signed by warp x weft and the
 // weave's flip flag.
-YS_HD void sym3_min_eigvec(const double S[3][3], double* out) {
-  double a[3][3], V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+// a <- diagonalised S, V <- its eigenvectors (columns)
+YS_HD void sym3_jacobi(const double S[3][3], double a[3][3], double V[3][3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) V[i][j] = i == j ? 1.0 : 0.0;
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) a[i][j] = S[i][j];
   // off-diagonal entries below 1e-24 of the diagonal scale move the
@@ -703,9 +782,17 @@ YS_HD void sym3_min_eigvec(const double S[3][3], double* out) {
         }
       }
   }
+}
+YS_HD int sym3_argmin(const double a[3][3]) {
   int m = 0;
   if (a[1][1] < a[m][m]) m = 1;
   if (a[2][2] < a[m][m]) m = 2;
+  return m;
+}
+YS_HD void sym3_min_eigvec(const double S[3][3], double* out) {
+  double a[3][3], V[3][3];
+  sym3_jacobi(S, a, V);
+  const int m = sym3_argmin(a);
   for (int k = 0; k < 3; ++k) out[k] = V[k][m];
 }
 
@@ -735,38 +822,94 @@ YS_HD void node_normal(const View& v, int n, int W) {
   for (int i = 0; i < 3; ++i) st(v.NRM, i, nt, n) = nn[i];
 }
 
+// node_normal with tangents: the value as above; the tangent of the unit
+// eigenvector n of the smallest eigenvalue l_m of the scatter S along dS is
+// sum_{j != m} (v_j . dS n) / (l_m - l_j) v_j (first-order perturbation of a
+// symmetric eigenproblem with simple eigenvalues, the derivative autograd
+// takes through the SVD of src/Cloth.cpp:446). Values go to NRM, tangents
+// to dNRM.
+template <int K>
+YS_HD void node_normal_dual(const View& v, int n, int W) {
+  typedef Dual<K> D;
+  const int nt = v.ntot;
+  const int ids[5] = {n, n - 1, n + 1, n - W, n + W};
+  D p[5][3], mean[3], S[3][3];
+  for (int m = 0; m < 5; ++m)
+    for (int i = 0; i < 3; ++i) { p[m][i] = ldT<D>(v.X, v.dX, i, nt, ids[m]); mean[i] += p[m][i]; }
+  for (int i = 0; i < 3; ++i) mean[i] /= 5.0;
+  for (int m = 0; m < 5; ++m) {
+    D r[3] = {p[m][0] - mean[0], p[m][1] - mean[1], p[m][2] - mean[2]};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) S[i][j] += r[i] * r[j];
+  }
+  double Sv[3][3], a[3][3], V[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) Sv[i][j] = S[i][j].v;
+  sym3_jacobi(Sv, a, V);
+  const int mm = sym3_argmin(a);
+  D nn[3];
+  for (int i = 0; i < 3; ++i) nn[i] = D(V[i][mm]);
+  for (int jj = 0; jj < 3; ++jj) {
+    if (jj == mm) continue;
+    const double gap = a[mm][mm] - a[jj][jj];
+    for (int k = 0; k < K; ++k) {
+      double c = 0.0;  // v_j . dS_k n
+      for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) c += V[r][jj] * S[r][q].d[k] * V[q][mm];
+      for (int i = 0; i < 3; ++i) nn[i].d[k] += (c / gap) * V[i][jj];
+    }
+  }
+  const D len = norm3(nn);
+  for (int i = 0; i < 3; ++i) nn[i] /= len;
+  double vw[3], vf[3], cr[3], nv[3];
+  for (int i = 0; i < 3; ++i) {
+    vw[i] = p[2][i].v - p[1][i].v;
+    vf[i] = p[4][i].v - p[3][i].v;
+    nv[i] = nn[i].v;
+  }
+  cross3(vw, vf, cr);
+  if (dot3(cr, nv) / (norm3(cr) * norm3(nv)) < 0)
+    for (int i = 0; i < 3; ++i) nn[i] = -nn[i];
+  if (v.flags[n] & YS_FLIP)
+    for (int i = 0; i < 3; ++i) nn[i] = -nn[i];
+  for (int i = 0; i < 3; ++i) stT(v.NRM, v.dNRM, i, nt, n, nn[i]);
+}
+
 // ConSlideFriction (src/PhysicsCloth.cpp:2579-2641) for interior node n from
 // its gathered no-slide force fe, dF_E/dE diagonals kee / dee and the crimp
 // compression sums cl / cle; returns the A and b contributions of the E rows
 // and stores COMP and SLIDE.
-YS_HD void friction_node(const View& v, int n, const double* fe, const double* kee, const double* dee,
-                         const double* cl, const double* cle, double* aEE, double* bE) {
+template <class T>
+YS_HD void friction_node(const View& v, int n, const T* fe, const T* kee, const T* dee,
+                         const T* cl, const T* cle, T* aEE, T* bE) {
   const int nt = v.ntot;
   const ClothParams& P = v.cp[v.node_cloth[n]];
-  double nrm[3];
-  for (int i = 0; i < 3; ++i) nrm[i] = ld(v.NRM, i, nt, n);
-  double comp = 0.5 * dot3(nrm, cl);
+  T nrm[3];
+  for (int i = 0; i < 3; ++i) nrm[i] = ldT<T>(v.NRM, v.dNRM, i, nt, n);
+  T comp = 0.5 * dot3(nrm, cl);
   if (comp < 0) comp = 0.0;
-  const double compEE[2] = {0.5 * dot3(nrm, cle), 0.5 * dot3(nrm, cle + 3)};
-  st(v.COMP, 0, nt, n) = comp;
-  const double mu = P.mu, kf = P.kf, df = P.df, h = v.h, h2 = v.h * v.h;
-  const double lim = 1.0 * comp * mu;
+  const T compEE[2] = {0.5 * dot3(nrm, cle), 0.5 * dot3(nrm, cle + 3)};
+  stT(v.COMP, v.dCOMP, 0, nt, n, comp);
+  const T mu = cloth_mu<T>(v, v.node_cloth[n]);
+  const double kf = P.kf, df = P.df, h = v.h, h2 = v.h * v.h;
+  const T lim = 1.0 * comp * mu;
   for (int k = 0; k < 2; ++k) {
-    const double uvm = ld(v.UV, k, nt, n) - ld(v.UVB, k, nt, n);
-    const double FEns = fe[k], EEp = kee[k], EEv = dee[k];
-    const double slide = 1.0 / (1.0 + exp(-(1e4 * (fabs(FEns) - lim))));
-    const double t = tanh(10 * uvm), tl = tanh(10 * (lim - FEns));
-    const double uvdot = ld(v.UVD, k, nt, n);
-    const double force = (-0.5 * (kf * uvm - t * comp * mu) * tl + 0.5 * (kf * uvm + t * comp * mu)) - df * uvdot;
-    const double pos = (-0.5 * (kf - (1.0 - t * t) * mu * comp - t * mu * compEE[k])) * tl -
+    const T uvm = ldT<T>(v.UV, v.dUV, k, nt, n) - ldT<T>(v.UVB, v.dUVB, k, nt, n);
+    const T FEns = fe[k], EEp = kee[k], EEv = dee[k];
+    const T slide = 1.0 / (1.0 + exp(-(1e4 * (fabs(FEns) - lim))));
+    const T t = tanh(10 * uvm), tl = tanh(10 * (lim - FEns));
+    const T uvdot = ldT<T>(v.UVD, v.dUVD, k, nt, n);
+    const T force = (-0.5 * (kf * uvm - t * comp * mu) * tl + 0.5 * (kf * uvm + t * comp * mu)) - df * uvdot;
+    const T pos = (-0.5 * (kf - (1.0 - t * t) * mu * comp - t * mu * compEE[k])) * tl -
                        (0.5 * (kf * uvm - t * mu * comp)) * (1.0 - tl * tl) * (EEp - mu * compEE[k]) -
                        (0.5 * (kf + (1.0 - t * t) * mu * comp + t * mu * compEE[k]));
     // tanh(10 * fric_lim - F) as written at src/PhysicsCloth.cpp:2630-2631
-    const double tq = tanh(10 * lim - FEns);
-    const double vel = (-0.5 * (kf * uvm - t * mu * comp)) * (1.0 - tq * tq) * EEv - df;
-    st(v.SLIDE, k, nt, n) = slide;
+    const T tq = tanh(10 * lim - FEns);
+    const T vel = (-0.5 * (kf * uvm - t * mu * comp)) * (1.0 - tq * tq) * EEv - df;
+    stT(v.SLIDE, v.dSLIDE, k, nt, n, slide);
     aEE[k] = -h2 * pos - h * vel;
-    bE[k] = h * (force - vel * uvdot);
+    // D enters b without a graph in the reference (src/MatrixMp.cpp:40-99)
+    bE[k] = h * (force - (v.trunc ? detach(vel) : vel) * uvdot);
   }
 }
 
@@ -784,48 +927,50 @@ YS_HD int shear_dv(int seg) { return (seg & 1) ? -1 : 1; }
 // Shear_F / Shear_D (src/PhysicsCloth.cpp:2643-3089) for crossing n0 with warp
 // neighbour n1 = n0 + (shear_du, 0) and weft neighbour n3 = n0 + (0, shear_dv),
 // written to the shear buffer at slot seg * ntot + n0.
-YS_HD void shear_element(const View& v, double* buf, int n0, int seg) {
+template <class T>
+YS_HD void shear_element(const View& v, double* buf, double* dbuf, int n0, int seg) {
   const ClothParams& P = v.cp[v.node_cloth[n0]];
   const int n1 = n0 + shear_du(seg), n3 = n0 + shear_dv(seg) * P.W;
   const int nt = v.ntot;
-  const double Lc = P.L, R = P.R, S = P.S;
-  const double comp = ld(v.COMP, 0, nt, n0);
-  double a1v[3], a3v[3], d1[3], d3[3], P1[3][3], P3[3][3];
+  const double Lc = P.L, R = P.R;
+  const T S = cloth_S<T>(v, v.node_cloth[n0]);
+  const T comp = ldT<T>(v.COMP, v.dCOMP, 0, nt, n0);
+  T a1v[3], a3v[3], d1[3], d3[3], P1[3][3], P3[3][3];
   for (int i = 0; i < 3; ++i) {
-    const double x0 = ld(v.X, i, nt, n0);
-    a1v[i] = ld(v.X, i, nt, n1) - x0;
-    a3v[i] = ld(v.X, i, nt, n3) - x0;
+    const T x0 = ldT<T>(v.X, v.dX, i, nt, n0);
+    a1v[i] = ldT<T>(v.X, v.dX, i, nt, n1) - x0;
+    a3v[i] = ldT<T>(v.X, v.dX, i, nt, n3) - x0;
   }
-  const double l1 = norm3(a1v), l3 = norm3(a3v);
+  const T l1 = norm3(a1v), l3 = norm3(a3v);
   for (int i = 0; i < 3; ++i) { d1[i] = a1v[i] / l1; d3[i] = a3v[i] / l3; }
   proj3(d1, P1);
   proj3(d3, P3);
-  const double phi = acos(dot3(d1, d3));
-  const double s = sin(phi), co = cos(phi);
-  double a3[3], a1[3];  // a3 = P1 d3, a1 = P3 d1
+  const T phi = acos(dot3(d1, d3));
+  const T s = sin(phi), co = cos(phi);
+  T a3[3], a1[3];  // a3 = P1 d3, a1 = P3 d1
   matvec3(P1, d3, a3);
   matvec3(P3, d1, a1);
   const uint8_t f0 = v.flags[n0], f1 = v.flags[n1], f3 = v.flags[n3];
   const bool jam = (((f0 & YS_FLIP) != 0) != ((f1 & YS_FLIP) != 0)) && (((f0 & YS_FLIP) != 0) != ((f3 & YS_FLIP) != 0));
-  double Fx1[3], Fx3[3], J11[3][3], J13[3][3], J31[3][3], J33[3][3];
-  const double cs2 = co / (s * s), is = 1 / s;
+  T Fx1[3], Fx3[3], J11[3][3], J13[3][3], J31[3][3], J33[3][3];
+  const T cs2 = co / (s * s), is = 1 / s;
   if (!jam) {
-    const double kx = (comp + 1.0) * S * R * R * kPi;
-    const double ph = phi - kPi / 2;
-    const double cf1 = (kx * Lc * ph) / (l1 * s), cf3 = (kx * Lc * ph) / (l3 * s);
+    const T kx = (comp + 1.0) * S * R * R * kPi;
+    const T ph = phi - kPi / 2;
+    const T cf1 = (kx * Lc * ph) / (l1 * s), cf3 = (kx * Lc * ph) / (l3 * s);
     for (int i = 0; i < 3; ++i) { Fx1[i] = cf1 * a3[i]; Fx3[i] = cf3 * a1[i]; }
-    const double k11 = (kx * Lc) / ((l1 * l1) * s), k33 = (kx * Lc) / ((l3 * l3) * s);
-    const double k13 = (kx * Lc) / (l3 * l1 * s), k31 = (kx * Lc) / (l1 * l3 * s);
+    const T k11 = (kx * Lc) / ((l1 * l1) * s), k33 = (kx * Lc) / ((l3 * l3) * s);
+    const T k13 = (kx * Lc) / (l3 * l1 * s), k31 = (kx * Lc) / (l1 * l3 * s);
     // src/PhysicsCloth.cpp:2715-2751 per block:
     //   J11 = k11 (ph (-a3 d1^T + cs2 a3 a3^T - co P1 - d1 a3^T) - a3 a3^T / s)
     //   J13 = k13 ph (cs2 - 1/s) (a3 d1^T) P3 = k13 ph (cs2 - 1/s) a3 a1^T, as a1 = P3 d1
     // (J33, J31 likewise with 1 <-> 3)
-    const double kA1 = k11 * (ph * cs2 - is), kS1 = -k11 * ph, kP1 = kS1 * co;
-    const double kA3 = k33 * (ph * cs2 - is), kS3 = -k33 * ph, kP3 = kS3 * co;
-    const double kx13 = k13 * ph * (cs2 - is), kx31 = k31 * ph * (cs2 - is);
+    const T kA1 = k11 * (ph * cs2 - is), kS1 = -k11 * ph, kP1 = kS1 * co;
+    const T kA3 = k33 * (ph * cs2 - is), kS3 = -k33 * ph, kP3 = kS3 * co;
+    const T kx13 = k13 * ph * (cs2 - is), kx31 = k31 * ph * (cs2 - is);
     for (int i = 0; i < 3; ++i) {
-      const double al1 = kA1 * a3[i] + kS1 * d1[i], be1 = kS1 * a3[i];
-      const double al3 = kA3 * a1[i] + kS3 * d3[i], be3 = kS3 * a1[i];
+      const T al1 = kA1 * a3[i] + kS1 * d1[i], be1 = kS1 * a3[i];
+      const T al3 = kA3 * a1[i] + kS3 * d3[i], be3 = kS3 * a1[i];
       for (int j = 0; j < 3; ++j) {
         J11[i][j] = al1 * a3[j] + be1 * d1[j] + kP1 * P1[i][j];
         J33[i][j] = al3 * a1[j] + be3 * d3[j] + kP3 * P3[i][j];
@@ -844,29 +989,29 @@ YS_HD void shear_element(const View& v, double* buf, int n0, int seg) {
     const double pb = kPi / 2, pl = P.jam, sig = 0.6;
     const double cc = 3.0;
     const double LR = Lc / R;
-    const double rl1s = 1.0 / (l1 * s), rl3s = 1.0 / (l3 * s);
-    double px1[3], px3[3];
+    const T rl1s = 1.0 / (l1 * s), rl3s = 1.0 / (l3 * s);
+    T px1[3], px3[3];
     for (int i = 0; i < 3; ++i) { px1[i] = -a3[i] * rl1s; px3[i] = -a1[i] * rl3s; }
-    const double gamma = (Lc * sqrt(2.0) - 2 * Lc * sin(0.5 * phi)) / R;
-    const double sh = sin(0.5 * phi), ch = cos(0.5 * phi);
-    const double kap = -LR * ch;                       // gamma_x = kap * phi_x
-    const double Aq = phi - pl, Bq = phi - pb;
-    const double phs = phi * Aq * Bq;
-    const double sgm = Aq * Bq + phi * Bq + phi * Aq;  // phi_s_x = sgm * phi_x
-    const double omg = 2.0 * (Aq + Bq + phi);
+    const T gamma = (Lc * sqrt(2.0) - 2 * Lc * sin(0.5 * phi)) / R;
+    const T sh = sin(0.5 * phi), ch = cos(0.5 * phi);
+    const T kap = -LR * ch;                       // gamma_x = kap * phi_x
+    const T Aq = phi - pl, Bq = phi - pb;
+    const T phs = phi * Aq * Bq;
+    const T sgm = Aq * Bq + phi * Bq + phi * Aq;  // phi_s_x = sgm * phi_x
+    const T omg = 2.0 * (Aq + Bq + phi);
     const double pb5 = P.pb5, pb4 = P.pb4;
-    const double num = pb5 * Aq, den = phs * phs + pb4 * sig * sig;
-    const double cf = tanh(num / den);
-    const double den2 = den * den, rden2 = 1.0 / den2, rden22 = 1.0 / (den2 * den2);
-    const double tau = pb5 * den - num * (2 * phs * sgm);  // con_func_x_x numerator / phi_x
-    const double muc = tau * rden2;                         // con_func_x_x = muc * phi_x
-    const double g3 = gamma * gamma * gamma, g2 = gamma * gamma;
-    const double base = 0.5 * (comp + 1.0) * S * kPi * (R * R);
-    const double kx = base * ((1 + g3) + (1 - g3) * cf);
-    const double beta0 = base * (1 - g3);
-    const double beta1 = base * (cc * g2 * kap * (1 - cf) - (1 - g3) * cf * cf * muc);
-    const double Bq2 = Bq * Bq;
-    const double cf1 = (kx * Lc * Bq) * rl1s, cf3 = (kx * Lc * Bq) * rl3s;
+    const T num = pb5 * Aq, den = phs * phs + pb4 * sig * sig;
+    const T cf = tanh(num / den);
+    const T den2 = den * den, rden2 = 1.0 / den2, rden22 = 1.0 / (den2 * den2);
+    const T tau = pb5 * den - num * (2 * phs * sgm);  // con_func_x_x numerator / phi_x
+    const T muc = tau * rden2;                         // con_func_x_x = muc * phi_x
+    const T g3 = gamma * gamma * gamma, g2 = gamma * gamma;
+    const T base = 0.5 * (comp + 1.0) * S * kPi * (R * R);
+    const T kx = base * ((1 + g3) + (1 - g3) * cf);
+    const T beta0 = base * (1 - g3);
+    const T beta1 = base * (cc * g2 * kap * (1 - cf) - (1 - g3) * cf * cf * muc);
+    const T Bq2 = Bq * Bq;
+    const T cf1 = (kx * Lc * Bq) * rl1s, cf3 = (kx * Lc * Bq) * rl3s;
     for (int i = 0; i < 3; ++i) {
       Fx1[i] = -0.5 * (beta0 + beta1 * px1[i]) * Lc * Bq2 + cf1 * a3[i];
       Fx3[i] = -0.5 * (beta0 + beta1 * px3[i]) * Lc * Bq2 + cf3 * a1[i];
@@ -879,62 +1024,62 @@ YS_HD void shear_element(const View& v, double* buf, int n0, int seg) {
     // rows/columns. Those quantities are in turn combinations of a handful of
     // rank-1 matrices (a3 a3^T, a3 d1^T + d1 a3^T, P1, ...), so each block is
     // J = sum_k c_k B_k with c_k computed once per block.
-    double P1P3[3][3], e3[3];
+    T P1P3[3][3], e3[3];
     matmul3(P1, P3, P1P3);  // P3 P1 is its transpose (both projectors symmetric)
     matvec3(P3, d3, e3);    // P3 d3: src/PhysicsCloth.cpp:2775-2777 multiplies outer(P3 d1, d3) by P3
-    const double cfq = -2 * cf * (1 - cf * cf);
-    const double c1 = cc * (cc - 1) * gamma, c2 = cc * g2;
-    const double base2 = 0.5 * (comp + 1.0) * S * (R * R);
-    const double kO = c1 * kap * kap * (1 - cf) - 2 * c2 * kap * (1 - cf * cf) * muc;
-    const double kG = c2 * (1 - cf);
-    const double cfqm2 = cfq * muc * muc;
-    const double X4 = 4 * tau * den * phs * sgm;
-    const double tns2 = 2 * num * sgm * sgm, tnp = 2 * num * phs, pb5den = pb5 * den;
-    const double cross = 2 * phs * pb5 * sgm;
-    const double hLB2 = 0.5 * Lc * Bq2, LB = Lc * Bq;
-    const double kL = kx * Lc;
-    const double r11 = 1.0 / ((l1 * l1) * s), r33 = 1.0 / ((l3 * l3) * s), r13 = 1.0 / (l1 * l3 * s);
-    const double qR11 = 0.5 * LR * sh / ((l1 * s) * (l1 * s)), qR33 = 0.5 * LR * sh / ((l3 * s) * (l3 * s));
-    const double qR13 = 0.5 * LR * sh / (l1 * l3 * (s * s));
-    const double rho1 = rl1s * rl1s, rho3 = rl3s * rl3s, rho13 = rl1s * rl3s;
+    const T cfq = -2 * cf * (1 - cf * cf);
+    const T c1 = cc * (cc - 1) * gamma, c2 = cc * g2;
+    const T base2 = 0.5 * (comp + 1.0) * S * (R * R);
+    const T kO = c1 * kap * kap * (1 - cf) - 2 * c2 * kap * (1 - cf * cf) * muc;
+    const T kG = c2 * (1 - cf);
+    const T cfqm2 = cfq * muc * muc;
+    const T X4 = 4 * tau * den * phs * sgm;
+    const T tns2 = 2 * num * sgm * sgm, tnp = 2 * num * phs, pb5den = pb5 * den;
+    const T cross = 2 * phs * pb5 * sgm;
+    const T hLB2 = 0.5 * Lc * Bq2, LB = Lc * Bq;
+    const T kL = kx * Lc;
+    const T r11 = 1.0 / ((l1 * l1) * s), r33 = 1.0 / ((l3 * l3) * s), r13 = 1.0 / (l1 * l3 * s);
+    const T qR11 = 0.5 * LR * sh / ((l1 * s) * (l1 * s)), qR33 = 0.5 * LR * sh / ((l3 * s) * (l3 * s));
+    const T qR13 = 0.5 * LR * sh / (l1 * l3 * (s * s));
+    const T rho1 = rl1s * rl1s, rho3 = rl3s * rl3s, rho13 = rl1s * rl3s;
     // J = cP*pxx + cO*O + cOb*Ob + cR*Rg + fo (+ cOne*1 + row/column terms)
-    const double hb = hLB2 * base2, g3c = 1 - g3;
-    const double cR = -hb * kG;
-    const double cnx_p = pb5den - tnp * sgm;  // nx = cnx_p pxx + ...
+    const T hb = hLB2 * base2, g3c = 1 - g3;
+    const T cR = -hb * kG;
+    const T cnx_p = pb5den - tnp * sgm;  // nx = cnx_p pxx + ...
     // x1x1 and x3x3: psx = sgm pxx + omg O, cfdd = cfqm2 O + 1 - cf^2 cfx
-    const double eD = -cf * cf;
-    const double cPd = -hb * (kG * kap + g3c * eD * rden2 * cnx_p);
-    const double cOd = -hb * (kO + g3c * (eD * (rden2 * (-tns2 - tnp * omg) - rden22 * X4) + cfqm2)) - 2 * LB * beta1;
-    const double cOne = -hb * g3c;
+    const T eD = -cf * cf;
+    const T cPd = -hb * (kG * kap + g3c * eD * rden2 * cnx_p);
+    const T cOd = -hb * (kO + g3c * (eD * (rden2 * (-tns2 - tnp * omg) - rden22 * X4) + cfqm2)) - 2 * LB * beta1;
+    const T cOne = -hb * g3c;
     // x1x3 (psx = sgm pxx + omg (O + Ob) / 2) and x3x1 (psx = sgm pxx + omg O);
     // both: nx += cross (O - Ob), cfdd = cfqm2 Ob + (1 - cf^2) cfx
-    const double eX = 1 - cf * cf;
-    const double cPx = -hb * (kG * kap + g3c * eX * rden2 * cnx_p);
-    const double cO13 = -hb * (kO + g3c * eX * (rden2 * (-tns2 - tnp * 0.5 * omg + cross) - rden22 * X4)) -
+    const T eX = 1 - cf * cf;
+    const T cPx = -hb * (kG * kap + g3c * eX * rden2 * cnx_p);
+    const T cO13 = -hb * (kO + g3c * eX * (rden2 * (-tns2 - tnp * 0.5 * omg + cross) - rden22 * X4)) -
                         2 * LB * beta1;
-    const double cOb13 = -hb * g3c * (eX * rden2 * (-tnp * 0.5 * omg - cross) + cfqm2);
-    const double cO31 = -hb * (kO + g3c * eX * (rden2 * (-tns2 - tnp * omg + cross) - rden22 * X4)) - 2 * LB * beta1;
-    const double cOb31 = -hb * g3c * (eX * rden2 * (-cross) + cfqm2);
-    const double kq = Bq * cs2 - is;
+    const T cOb13 = -hb * g3c * (eX * rden2 * (-tnp * 0.5 * omg - cross) + cfqm2);
+    const T cO31 = -hb * (kO + g3c * eX * (rden2 * (-tns2 - tnp * omg + cross) - rden22 * X4)) - 2 * LB * beta1;
+    const T cOb31 = -hb * g3c * (eX * rden2 * (-cross) + cfqm2);
+    const T kq = Bq * cs2 - is;
     // x1x1: pxx = r11 (S - cs2 A + co P1), O = Ob = rho1 A, Rg = qR11 A,
     //       fo = kL r11 (-Bq S + kq A - Bq co P1); A = a3 a3^T, S = a3 d1^T + d1 a3^T
     {
-      const double kA = cPd * (-cs2 * r11) + cOd * rho1 + cR * qR11 + kL * r11 * kq;
-      const double kS = (cPd - kL * Bq) * r11;
-      const double kP = (cPd - kL * Bq) * r11 * co;
+      const T kA = cPd * (-cs2 * r11) + cOd * rho1 + cR * qR11 + kL * r11 * kq;
+      const T kS = (cPd - kL * Bq) * r11;
+      const T kP = (cPd - kL * Bq) * r11 * co;
       for (int i = 0; i < 3; ++i) {
-        const double al = kA * a3[i] + kS * d1[i], be = kS * a3[i];
+        const T al = kA * a3[i] + kS * d1[i], be = kS * a3[i];
         for (int j = 0; j < 3; ++j)
           J11[i][j] = al * a3[j] + be * d1[j] + kP * P1[i][j] + (cOne - 2 * LB * beta0 * px1[j]);
       }
     }
     // x3x3: the same with (a1, d3, P3, r33, qR33, rho3, px3)
     {
-      const double kA = cPd * (-cs2 * r33) + cOd * rho3 + cR * qR33 + kL * r33 * kq;
-      const double kS = (cPd - kL * Bq) * r33;
-      const double kP = (cPd - kL * Bq) * r33 * co;
+      const T kA = cPd * (-cs2 * r33) + cOd * rho3 + cR * qR33 + kL * r33 * kq;
+      const T kS = (cPd - kL * Bq) * r33;
+      const T kP = (cPd - kL * Bq) * r33 * co;
       for (int i = 0; i < 3; ++i) {
-        const double al = kA * a1[i] + kS * d3[i], be = kS * a1[i];
+        const T al = kA * a1[i] + kS * d3[i], be = kS * a1[i];
         for (int j = 0; j < 3; ++j)
           J33[i][j] = al * a1[j] + be * d3[j] + kP * P3[i][j] + (cOne - 2 * LB * beta0 * px3[j]);
       }
@@ -942,9 +1087,9 @@ YS_HD void shear_element(const View& v, double* buf, int n0, int seg) {
     // x1x3: pxx = -r13 (cs2 A + M), O = rho13 A, Ob = rho13 B, Rg = qR13 A,
     //       fo = kL r13 (kq A + Bq M); A = a3 a1^T, B = a1 a3^T, M = P1 P3
     {
-      const double kA = -cPx * r13 * cs2 + cO13 * rho13 + cR * qR13 + kL * r13 * kq;
-      const double kB = cOb13 * rho13;
-      const double kM = (-cPx + kL * Bq) * r13;
+      const T kA = -cPx * r13 * cs2 + cO13 * rho13 + cR * qR13 + kL * r13 * kq;
+      const T kB = cOb13 * rho13;
+      const T kM = (-cPx + kL * Bq) * r13;
       for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
           J13[i][j] = kA * (a3[i] * a1[j]) + kB * (a1[i] * a3[j]) + kM * P1P3[i][j] - LB * beta0 * (px3[j] + px1[i]);
@@ -952,19 +1097,18 @@ YS_HD void shear_element(const View& v, double* buf, int n0, int seg) {
     // x3x1: pxx = -r13 (cs2 E + M^T), O = rho13 A, Ob = rho13 B, Rg = qR13 A,
     //       fo = kL r13 (kq A + Bq M^T); A = a1 a3^T, B = a3 a1^T, E = a1 e3^T
     {
-      const double kA = cO31 * rho13 + cR * qR13 + kL * r13 * kq;
-      const double kB = cOb31 * rho13;
-      const double kE = -cPx * r13 * cs2;
-      const double kM = (-cPx + kL * Bq) * r13;
+      const T kA = cO31 * rho13 + cR * qR13 + kL * r13 * kq;
+      const T kB = cOb31 * rho13;
+      const T kE = -cPx * r13 * cs2;
+      const T kM = (-cPx + kL * Bq) * r13;
       for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
           J31[i][j] = kA * (a1[i] * a3[j]) + kB * (a3[i] * a1[j]) + kE * (a1[i] * e3[j]) + kM * P1P3[j][i] -
                       LB * beta0 * (px1[j] + px3[i]);
     }
   }
-  const int64_t stride = 4LL * nt, base = (int64_t)seg * nt + n0;
   int f = 0;
-  auto put = [&](double x) { buf[(int64_t)(f++) * stride + base] = x; };
+  auto put = [&](const T& x) { stT(buf, dbuf, 4 * (f++) + seg, nt, n0, x); };
   for (int i = 0; i < 3; ++i) put(Fx1[i]);
   for (int i = 0; i < 3; ++i) put(Fx3[i]);
   for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) put(J11[i][j]);

@@ -146,6 +146,41 @@ ys_status ys_apply_system_noalloc(ys_batch *b, const double *x, double *y);
 /* Waits for the handle's stream. */
 ys_status ys_synchronize(ys_batch *b);
 
+/* ---- Forward-mode sensitivities of the step (tangents).
+ * Replaces the gradient path of the reference's parameter learning
+ * (YarnSimNet* + loss.backward(), src/TrainHeter.h:194-231, through
+ * EigenSolver::backward, src/Solvers.h:35-52 / src/Solvers.cpp:33-58): the
+ * reference has 8 learned scalars (rho, Y, B of two yarn types, S, mu), so
+ * propagating ys_tangent_count() (4) directional derivatives per cloth alongside
+ * the state (more directions: a second pass, or copies of the cloth in one
+ * batch with their own seeds)
+ * gives d(state_t)/d(theta) for every step t of a rollout at the cost of a few
+ * extra solves per step, with no stored trajectory. Directions are seeded on
+ * the per-line materials (rho, Y, B), the per-cloth S and mu, and/or the
+ * initial state; the tangent of every later state is then exact for the
+ * discrete step (A dq = db - dA q). */
+enum { YS_TANGENT_EXACT = 0, YS_TANGENT_REFERENCE = 1 };
+/* Number of tangent directions a step carries (4). */
+int32_t ys_tangent_count(void);
+/* Allocates the tangent buffers (about 21 KB per node) and zeroes every
+ * tangent. mode: YS_TANGENT_EXACT. */
+ys_status ys_tangent_enable(ys_batch *b, int32_t mode);
+/* Parameter directions, host arrays, NULL = 0: drho, dY, dB
+ * [ys_tangent_count()][total lines] with lines ordered cloth by cloth, warp
+ * lines (length) then weft lines (width) as in ys_cloth_desc; dS, dmu
+ * [ys_tangent_count()][n_cloths]. */
+ys_status ys_tangent_seed(ys_batch *b, const double *drho, const double *dY, const double *dB, const double *dS,
+                          const double *dmu);
+/* State tangents [ys_tangent_count()][total_nodes][3|2] (NULL = 0 on set,
+ * skipped on get); flags as ys_set_state. */
+ys_status ys_tangent_set_state(ys_batch *b, const double *dlpos, const double *dlvel, const double *depos,
+                               const double *deposbar, const double *devel, int32_t flags);
+ys_status ys_tangent_get_state(ys_batch *b, double *dlpos, double *dlvel, double *depos, double *deposbar,
+                               double *devel, int32_t flags);
+/* ys_step, also advancing the first kact tangent directions (0..ys_tangent_count()). */
+ys_status ys_step_tangent(ys_batch *b, double h, const double *ext_force, int32_t flags, const ys_solve_opts *opts,
+                          int32_t kact, ys_cloth_stats *stats);
+
 /* Kernel accounting (no counterpart in the reference). Kernel classes: */
 enum {
   YS_PROF_GEOM = 0,      /* node normals */

@@ -7,6 +7,7 @@
 // loaded only by tests/test_emu_vs_oracle.py; the package never loads it.
 #include <cfloat>
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -26,6 +27,9 @@ struct Emu {
   ys::View v{};
   ys::Records R{};
   int bad = 0;
+  // forward-mode tangents (kTangents directions)
+  std::vector<double> dX, dV, dUV, dUVD, dUVB, dNRM, dCOMP, dSLIDE, drho, dks, dkb, dS, dmu, dA, dB, dRE, dRB, dRF,
+      dRS, As, Bs, RT, DQ, QS;
 
   void bind() {
     v.ntot = N;
@@ -33,6 +37,7 @@ struct Emu {
     v.node_cloth = node_cloth.data(); v.node_u = node_u.data(); v.node_v = node_v.data();
     v.flags = flags.data(); v.cp = &P;
     v.line_rho = rho.data(); v.line_ks = ks.data(); v.line_kb = kb.data();
+    v.nlines = (int)rho.size();
     v.X = X.data(); v.V = V.data(); v.XF = XF.data(); v.UV = UV.data(); v.UVD = UVD.data(); v.UVB = UVB.data();
     v.UV0 = UV0.data(); v.NRM = NRM.data(); v.COMP = COMP.data(); v.SLIDE = SLIDE.data();
     v.A = A.data(); v.B = B.data();
@@ -102,6 +107,181 @@ void* emu_create(const ys_cloth_desc* d) {
 
 void emu_destroy(void* h) { delete static_cast<Emu*>(h); }
 
+// ---------------------------------------------------------------- tangents
+constexpr int KT = ys::kTangents;
+void emu_assemble(void* h, double dt, const double* ext);
+
+int emu_tangent_count(void) { return KT; }
+
+void emu_tangent_init(void* h) {
+  Emu* e = static_cast<Emu*>(h);
+  const size_t N = e->N, nl = e->rho.size();
+  auto Z = [&](std::vector<double>& a, size_t c) { a.assign(c, 0.0); };
+  Z(e->dX, 3 * KT * N); Z(e->dV, 3 * KT * N); Z(e->dUV, 2 * KT * N); Z(e->dUVD, 2 * KT * N); Z(e->dUVB, 2 * KT * N);
+  Z(e->dNRM, 3 * KT * N); Z(e->dCOMP, KT * N); Z(e->dSLIDE, 2 * KT * N);
+  Z(e->drho, KT * nl); Z(e->dks, KT * nl); Z(e->dkb, KT * nl); Z(e->dS, KT); Z(e->dmu, KT);
+  Z(e->dA, (size_t)ys::YS_NUM_SLOTS * KT * N); Z(e->dB, 5 * KT * N);
+  Z(e->dRE, (size_t)ys::kEdgeFields * 2 * KT * N); Z(e->dRB, (size_t)ys::kBendFields * 2 * KT * N);
+  Z(e->dRF, 6 * KT * N); Z(e->dRS, (size_t)ys::kShearFields * 4 * KT * N);
+  Z(e->As, (size_t)ys::YS_NUM_SLOTS * N); Z(e->Bs, 5 * N); Z(e->RT, 5 * KT * N); Z(e->DQ, 5 * KT * N); Z(e->QS, 5 * N);
+  // buffers every step writes before reading start as NaN, as device memory
+  // may hold anything: a read of an unwritten entry shows up in the tests
+  const double nan = std::nan("");
+  for (auto* a : {&e->dNRM, &e->dCOMP, &e->dSLIDE, &e->dA, &e->dB, &e->dRE, &e->dRB, &e->dRF, &e->dRS, &e->As,
+                  &e->Bs, &e->RT})
+    std::fill(a->begin(), a->end(), nan);
+}
+
+// parameter tangents: [KT][nlines] for rho, Y, B (lines: warp rows then weft
+// columns), [KT] for S and mu; Y and B enter as ks, kb = (Y, B) pi R^2
+void emu_tangent_seed(void* h, const double* drho, const double* dY, const double* dBm, const double* dS,
+                      const double* dmu) {
+  Emu* e = static_cast<Emu*>(h);
+  const size_t nl = e->rho.size();
+  const double a = ys::kPi * std::pow(e->P.R, 2);
+  for (size_t i = 0; i < KT * nl; ++i) {
+    e->drho[i] = drho ? drho[i] : 0.0;
+    e->dks[i] = dY ? dY[i] * a : 0.0;
+    e->dkb[i] = dBm ? dBm[i] * a : 0.0;
+  }
+  for (int k = 0; k < KT; ++k) {
+    e->dS[k] = dS ? dS[k] : 0.0;
+    e->dmu[k] = dmu ? dmu[k] : 0.0;
+  }
+}
+
+// state tangents in node layout [KT][N][c]
+static void tan_io(Emu* e, double* ext, std::vector<double>& a, int c, bool in) {
+  const int N = e->N;
+  for (int k = 0; k < KT; ++k)
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < c; ++j) {
+        double& t = a[((size_t)j * KT + k) * N + i];
+        double& x = ext[((size_t)k * N + i) * c + j];
+        if (in) t = x; else x = t;
+      }
+}
+void emu_tangent_state(void* h, double* dlpos, double* dlvel, double* depos, double* deposbar, double* devel, int set) {
+  Emu* e = static_cast<Emu*>(h);
+  if (dlpos) tan_io(e, dlpos, e->dX, 3, set);
+  if (dlvel) tan_io(e, dlvel, e->dV, 3, set);
+  if (depos) tan_io(e, depos, e->dUV, 2, set);
+  if (deposbar) tan_io(e, deposbar, e->dUVB, 2, set);
+  if (devel) tan_io(e, devel, e->dUVD, 2, set);
+}
+
+// raw tangent buffers (for diagnosis): 0 dNRM 1 dCOMP 2 dSLIDE 3 dA 4 dB 5 dRE
+// 6 dRB 7 dRF 8 dRS 9 DQ; returns the element count, copies when out != 0
+long emu_tangent_raw(void* h, int which, double* out) {
+  Emu* e = static_cast<Emu*>(h);
+  std::vector<double>* t[18] = {&e->dNRM, &e->dCOMP, &e->dSLIDE, &e->dA, &e->dB, &e->dRE, &e->dRB, &e->dRF,
+                                &e->dRS, &e->DQ, &e->NRM, &e->COMP, &e->SLIDE, &e->As, &e->Bs, &e->RE, &e->RB, &e->RF};
+  if (which < 0 || which > 17) return -1;
+  if (out) std::memcpy(out, t[which]->data(), sizeof(double) * t[which]->size());
+  return (long)t[which]->size();
+}
+
+// Jacobi-PCG as emu_solve on an arbitrary right-hand side
+static long pcg(Emu* e, const double* b, double* x, double tol, long maxiter) {
+  ys::View& v = e->v;
+  const int N = e->N;
+  std::vector<double> r(5 * N), p(5 * N), q(5 * N), z(5 * N);
+  double bb = 0, rz = 0;
+  for (int i = 0; i < 5 * N; ++i) {
+    x[i] = 0; r[i] = b[i]; z[i] = e->DINV[i] * r[i]; p[i] = z[i];
+    bb += r[i] * r[i]; rz += r[i] * z[i];
+  }
+  double rr = bb;
+  const double thr = std::max(tol * tol * bb, DBL_MIN);
+  if (bb == 0 || rr < thr) return 0;
+  long it = 0;
+  while (it < maxiter) {
+    double pq = 0;
+    for (int n = 0; n < N; ++n) {
+      double y[5];
+      ys::spmv_row(v, p.data(), n, y);
+      for (int k = 0; k < 5; ++k) { q[k * N + n] = y[k]; pq += p[k * N + n] * y[k]; }
+    }
+    const double alpha = rz / pq;
+    rr = 0;
+    double rzn = 0;
+    for (int i = 0; i < 5 * N; ++i) {
+      x[i] += alpha * p[i]; r[i] -= alpha * q[i]; rr += r[i] * r[i]; z[i] = e->DINV[i] * r[i]; rzn += r[i] * z[i];
+    }
+    ++it;
+    if (rr < thr) break;
+    const double beta = rzn / rz;
+    rz = rzn;
+    for (int i = 0; i < 5 * N; ++i) p[i] = z[i] + beta * p[i];
+  }
+  return it;
+}
+
+// One step with tangents: the plain step's assemble and solve, the same
+// assembly over Dual<KT> (tangents of A, b), kact tangent solves
+// A dq = db - dA q, and the update of state and tangents. Returns non-zero if
+// the step was not finite.
+int emu_step_tangent(void* h, double dt, const double* ext, double tol, int kact) {
+  Emu* e = static_cast<Emu*>(h);
+  typedef ys::Dual<KT> D;
+  const int W = e->P.W, H = e->P.H, N = e->N;
+  emu_assemble(h, dt, ext);
+  if (e->bad) return 1;
+  const long dim = 3L * N + 2L * (W - 2) * (H - 2);
+  pcg(e, e->B.data(), e->SOL.data(), tol, 2 * dim);
+  for (double s : e->SOL) if (!std::isfinite(s)) return 1;
+  // dual pass: values of A, b into shadows, tangents alongside
+  ys::View dv = e->v;
+  dv.A = e->As.data(); dv.B = e->Bs.data();
+  dv.K = KT;
+  dv.dX = e->dX.data(); dv.dV = e->dV.data(); dv.dUV = e->dUV.data(); dv.dUVD = e->dUVD.data();
+  dv.dUVB = e->dUVB.data(); dv.dNRM = e->dNRM.data(); dv.dCOMP = e->dCOMP.data(); dv.dSLIDE = e->dSLIDE.data();
+  dv.dline_rho = e->drho.data(); dv.dline_ks = e->dks.data(); dv.dline_kb = e->dkb.data();
+  dv.dS = e->dS.data(); dv.dmu = e->dmu.data(); dv.dA = e->dA.data(); dv.dB = e->dB.data();
+  ys::Records R = e->R;
+  R.dedge = e->dRE.data(); R.dbend = e->dRB.data(); R.dface = e->dRF.data(); R.dshear = e->dRS.data();
+  for (int j = 1; j < H - 1; ++j) for (int i = 1; i < W - 1; ++i) ys::node_normal_dual<KT>(dv, i + j * W, W);
+  for (int k = 0; k < 2; ++k)
+    for (int n = 0; n < N; ++n) {
+      const int i = n % W, j = n / W;
+      if (k == 0 ? i >= W - 1 : j >= H - 1) continue;
+      ys::EdgeOut<D> o;
+      ys::edge_element(dv, n, n + (k == 0 ? 1 : W), k, o);
+      ys::edge_store(dv, R.edge, R.dedge, n, k, o);
+    }
+  for (int k = 0; k < 2; ++k)
+    for (int n = 0; n < N; ++n) {
+      const int i = n % W, j = n / W;
+      const int pos = k == 0 ? i : j, len = k == 0 ? W : H;
+      if (pos < 1 || pos > len - 2) continue;
+      const int step = k == 0 ? 1 : W;
+      ys::bend_element<D>(dv, R.bend, R.dbend, n - step, n, n + step, k, k == 0 ? j : H + i);
+    }
+  for (int n = 0; n < N; ++n)
+    if (n % W < W - 1 && n / W < H - 1) ys::cell_faces<D>(dv, R.face, R.dface, n);
+  for (int n = 0; n < N; ++n) ys::gather_elements<D>(dv, R, n);
+  for (int seg = 0; seg < 4; ++seg)
+    for (int n = 0; n < N; ++n)
+      if (e->flags[n] & ys::YS_INTERIOR) ys::shear_element<D>(dv, R.shear, R.dshear, n, seg);
+  for (int n = 0; n < N; ++n) ys::gather_shear_finalize<D>(dv, R, n, nullptr);
+  // tangent solves
+  std::vector<double> rk(5 * N), xk(5 * N);
+  for (int k = 0; k < kact && k < KT; ++k) {
+    for (int n = 0; n < N; ++n) {
+      double r[5];
+      ys::tangent_rhs_row(dv, e->SOL.data(), n, k, r);
+      for (int c = 0; c < 5; ++c) rk[c * N + n] = r[c];
+    }
+    pcg(e, rk.data(), xk.data(), tol, 2 * dim);
+    for (int c = 0; c < 5; ++c)
+      for (int n = 0; n < N; ++n) e->DQ[((size_t)c * KT + k) * N + n] = xk[c * N + n];
+  }
+  for (int n = 0; n < N; ++n)
+    ys::update_node_dual<KT>(dv, e->SOL.data(), e->DQ.data(), e->dX.data(), e->dV.data(), e->dUV.data(),
+                             e->dUVD.data(), e->dUVB.data(), n);
+  return 0;
+}
+
 void emu_set_state(void* h, const double* lpos, const double* lposfix, const double* lvel, const double* epos,
                    const double* eposbar, const double* evel) {
   Emu* e = static_cast<Emu*>(h);
@@ -143,9 +323,9 @@ void emu_assemble(void* h, double dt, const double* ext /* [N][5] or null */) {
     for (int n = 0; n < N; ++n) {
       const int i = n % W, j = n / W;
       if (k == 0 ? i >= W - 1 : j >= H - 1) continue;
-      ys::EdgeOut o;
+      ys::EdgeOut<double> o;
       ys::edge_element(v, n, n + (k == 0 ? 1 : W), k, o);
-      ys::edge_store(v, e->R.edge, n, k, o);
+      ys::edge_store(v, e->R.edge, e->R.dedge, n, k, o);
     }
   for (int k = 0; k < 2; ++k)
     for (int n = 0; n < N; ++n) {
@@ -153,18 +333,18 @@ void emu_assemble(void* h, double dt, const double* ext /* [N][5] or null */) {
       const int pos = k == 0 ? i : j, len = k == 0 ? W : H;
       if (pos < 1 || pos > len - 2) continue;
       const int step = k == 0 ? 1 : W;
-      const double kb = k == 0 ? e->kb[j] : e->kb[H + i];
-      ys::bend_element(v, e->R.bend, n - step, n, n + step, k, kb);
+      const int line = k == 0 ? j : H + i;
+      ys::bend_element<double>(v, e->R.bend, e->R.dbend, n - step, n, n + step, k, line);
     }
   for (int n = 0; n < N; ++n)
-    if (n % W < W - 1 && n / W < H - 1) ys::cell_faces(v, e->R.face, n);
-  for (int n = 0; n < N; ++n) ys::gather_elements(v, e->R, n);
+    if (n % W < W - 1 && n / W < H - 1) ys::cell_faces<double>(v, e->R.face, e->R.dface, n);
+  for (int n = 0; n < N; ++n) ys::gather_elements<double>(v, e->R, n);
   for (int seg = 0; seg < 4; ++seg)
     for (int n = 0; n < N; ++n)
-      if (e->flags[n] & ys::YS_INTERIOR) ys::shear_element(v, e->R.shear, n, seg);
+      if (e->flags[n] & ys::YS_INTERIOR) ys::shear_element<double>(v, e->R.shear, e->R.dshear, n, seg);
   e->bad = 0;
   for (int n = 0; n < N; ++n)
-    if (!ys::gather_shear_finalize(v, e->R, n, e->DINV.data())) e->bad = 1;
+    if (!ys::gather_shear_finalize<double>(v, e->R, n, e->DINV.data())) e->bad = 1;
 }
 
 // raw slots [159][N] and rhs [5][N]

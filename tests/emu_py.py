@@ -70,6 +70,12 @@ def lib():
         L.emu_apply.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.emu_update.argtypes = [ctypes.c_void_p]
         L.emu_update.restype = ctypes.c_int
+        L.emu_tangent_count.restype = ctypes.c_int
+        L.emu_tangent_init.argtypes = [ctypes.c_void_p]
+        L.emu_tangent_seed.argtypes = [ctypes.c_void_p] + [_dp] * 5
+        L.emu_tangent_state.argtypes = [ctypes.c_void_p] + [_dp] * 5 + [ctypes.c_int]
+        L.emu_step_tangent.argtypes = [ctypes.c_void_p, ctypes.c_double, _dp, ctypes.c_double, ctypes.c_int]
+        L.emu_step_tangent.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -124,6 +130,35 @@ class EmuCloth:
 
     def update(self):
         return lib().emu_update(self.h)
+
+    # ---- forward-mode tangents (K directions per step)
+    @property
+    def K(self):
+        return int(lib().emu_tangent_count())
+
+    def tangent_init(self):
+        lib().emu_tangent_init(self.h)
+
+    def tangent_seed(self, drho=None, dY=None, dB=None, dS=None, dmu=None):
+        """drho, dY, dB: [K][lines] (warp rows then weft columns); dS, dmu: [K]."""
+        a = [None if x is None else np.ascontiguousarray(x, float) for x in (drho, dY, dB, dS, dmu)]
+        lib().emu_tangent_seed(self.h, *[_p(x) for x in a])
+
+    def tangent_set_state(self, dlpos=None, dlvel=None, depos=None, deposbar=None, devel=None):
+        a = [None if x is None else np.ascontiguousarray(x, float) for x in (dlpos, dlvel, depos, deposbar, devel)]
+        lib().emu_tangent_state(self.h, *[_p(x) for x in a], 1)
+
+    def tangent_get_state(self):
+        K, N = self.K, self.N
+        out = dict(LPos=np.zeros((K, N, 3)), LVel=np.zeros((K, N, 3)), EPos=np.zeros((K, N, 2)),
+                   EPosBar=np.zeros((K, N, 2)), EVel=np.zeros((K, N, 2)))
+        lib().emu_tangent_state(self.h, *[_p(out[k]) for k in ("LPos", "LVel", "EPos", "EPosBar", "EVel")], 0)
+        return out
+
+    def step_tangent(self, h, ext5=None, tol=1e-14, kact=None):
+        kact = self.K if kact is None else kact
+        e = None if ext5 is None else np.ascontiguousarray(ext5, float)
+        return lib().emu_step_tangent(self.h, h, _p(e), tol, kact)
 
     def step(self, h, ext5=None, tol=0.0, maxiter=-1):
         self.assemble(h, ext5)
