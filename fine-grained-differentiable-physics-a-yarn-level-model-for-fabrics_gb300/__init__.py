@@ -1,17 +1,21 @@
 """GB300-native yarn-level cloth step (sm_103a CUDA behind a C ABI).
 
 The package exposes the reference's cloth interface (Cloth, Environment,
-PhysicsCloth, SimStep, EigenSolver) and the batched ClothBatch, all backed by
-libyarnsim.so. There is no CPU fallback: without the CUDA library every call
+PhysicsCloth, SimStep, EigenSolver), the batched ClothBatch and the
+parameter-learning interface (YarnSimNetHeter, differentiable rollouts), all
+backed by libyarnsim.so. There is no CPU fallback: without the CUDA library every call
 raises.
 """
 from .buildlib import build, LIB_PATH
 from .cloth import (PI, ClothBatch, ClothSpec, ClothState, Cloth, EigenSolver, Environment, InitPose,
                     PhysicsCloth, SimStep, Wind, WovenPattern, Yarn)
 from ._native import YarnSimError, load as load_library, library_path
+from .learn import (PARAM_NAMES, YarnSimNetHeter, constraint_para, invert_constraint_para, position_loss, rollout,
+                    rollout_with_jacobian, two_yarn_spec)
 
 __all__ = [
     "build", "LIB_PATH", "PI", "ClothBatch", "ClothSpec", "ClothState", "Cloth", "EigenSolver", "Environment",
     "InitPose", "PhysicsCloth", "SimStep", "Wind", "WovenPattern", "Yarn", "YarnSimError", "load_library",
-    "library_path",
+    "library_path", "PARAM_NAMES", "YarnSimNetHeter", "constraint_para", "invert_constraint_para", "position_loss",
+    "rollout", "rollout_with_jacobian", "two_yarn_spec",
 ]

@@ -850,7 +850,8 @@ int32_t ys_tangent_count(void) { return KT; }
 
 ys_status ys_tangent_enable(ys_batch* b, int32_t mode) {
   if (!b) return fail(YS_ERR_ARG, "null handle");
-  if (mode != YS_TANGENT_EXACT) return fail(YS_ERR_ARG, "tangent mode must be YS_TANGENT_EXACT");
+  if (mode != YS_TANGENT_EXACT && mode != YS_TANGENT_REFERENCE)
+    return fail(YS_ERR_ARG, "tangent mode must be YS_TANGENT_EXACT or YS_TANGENT_REFERENCE");
   YS_CUDA(cudaSetDevice(b->device));
   ys_batch::Tan& t = b->tan;
   const size_t nt = b->ntot, nl = b->nlines, nc = b->ncloth;
@@ -967,11 +968,15 @@ ys_status ys_step_tangent(ys_batch* b, double h, const double* ext_force, int32_
   YS_CUDA(cudaGetLastError());
   b->run(YS_PROF_MISC, 1, [&] { ys::launch_tangent_rhs(dv, t.qsave, t.rt, kact, cs); });
   YS_CUDA(cudaGetLastError());
-  // tangent solves A dq_k = db_k - dA_k q with the step's A and Jacobi diagonal
+  // tangent solves with the step's A and Jacobi diagonal: A dq_k = db_k - dA_k q
+  // (exact), or A^T dq_k = db_k with M, D held constant -- the transpose of
+  // the reference's backward b_bar = A^-1 q_bar (src/Solvers.cpp:33-58)
   for (int k = 0; k < kact; ++k) {
     ys::View vk = b->v;
     vk.B = t.rt + (int64_t)k * 5 * nt;
+    b->so.trans = t.mode == YS_TANGENT_REFERENCE ? 1 : 0;
     const ys_status sk = solve_impl(b, vk, opts, nullptr);
+    b->so.trans = 0;
     if (sk == YS_ERR_ARG || sk == YS_ERR_CUDA) return sk;
     YS_CUDA(cudaMemcpy2DAsync(t.dq + (int64_t)k * nt, sizeof(double) * KT * nt, b->so.x, sizeof(double) * nt,
                               sizeof(double) * nt, 5, cudaMemcpyDeviceToDevice, cs));

@@ -437,6 +437,50 @@ YS_HD void spmv_row(const View& v, const double* YS_RESTRICT x, int n, double y[
   spmv_row_s(v, v.A, v.ntot, x, n, y);
 }
 
+// y = A^T x for row block n: every coefficient that row block i stores for
+// column block n (i = n - offset of its slot) is read from row i, transposed.
+YS_HD void spmv_row_t(const View& v, const double* YS_RESTRICT x, int n, double y[5]) {
+  const int nt = v.ntot;
+  const ClothParams& P = v.cp[v.node_cloth[n]];
+  const int u = v.node_u[n], w = v.node_v[n];
+  double yl[3] = {0.0, 0.0, 0.0}, ye[2] = {0.0, 0.0};
+  for (int s = 0; s < kNumStencil; ++s) {
+    const int du = stencil_du(s), dv = stencil_dv(s);
+    const int uu = u - du, vv = w - dv;  // the row that refers to n through slot s
+    if (uu < 0 || uu >= P.W || vv < 0 || vv >= P.H) continue;
+    const int i = n - du - dv * P.W;
+    const double x0 = x[i], x1 = x[nt + i], x2 = x[2 * nt + i];
+    const int b = YS_SLOT_LL + 9 * s;
+    for (int c = 0; c < 3; ++c)
+      yl[c] += slot(v, b + c, i) * x0 + slot(v, b + 3 + c, i) * x1 + slot(v, b + 6 + c, i) * x2;
+  }
+  {  // the node's own Eulerian couplings
+    const double x0 = x[n], x1 = x[nt + n], x2 = x[2 * nt + n];
+    for (int k = 0; k < 2; ++k) {
+      const double xe = x[(3 + k) * nt + n];
+      ye[k] += slot(v, YS_SLOT_LE_SELF + 0 + k, n) * x0 + slot(v, YS_SLOT_LE_SELF + 2 + k, n) * x1 +
+               slot(v, YS_SLOT_LE_SELF + 4 + k, n) * x2 + slot(v, YS_SLOT_EE_SELF + k, n) * xe;
+      for (int c = 0; c < 3; ++c) yl[c] += slot(v, YS_SLOT_EL_SELF + 3 * k + c, n) * xe;
+    }
+  }
+  for (int m = 0; m < 4; ++m) {  // yarn neighbour i = n - offset(m) refers to n through m
+    const int du = m == 0 ? -1 : m == 1 ? 1 : 0, dv = m == 2 ? -1 : m == 3 ? 1 : 0;
+    const int k = m < 2 ? 0 : 1;
+    const int uu = u - du, vv = w - dv;
+    if (uu < 0 || uu >= P.W || vv < 0 || vv >= P.H) continue;
+    const int i = n - du - dv * P.W;
+    const double xe = x[(3 + k) * nt + i];
+    ye[k] += slot(v, YS_SLOT_LE_NBR + 3 * m + 0, i) * x[i] + slot(v, YS_SLOT_LE_NBR + 3 * m + 1, i) * x[nt + i] +
+             slot(v, YS_SLOT_LE_NBR + 3 * m + 2, i) * x[2 * nt + i] + slot(v, YS_SLOT_EE_NBR + m, i) * xe;
+    for (int c = 0; c < 3; ++c) yl[c] += slot(v, YS_SLOT_EL_NBR + 3 * m + c, i) * xe;
+  }
+  y[0] = yl[0];
+  y[1] = yl[1];
+  y[2] = yl[2];
+  y[3] = ye[0];
+  y[4] = ye[1];
+}
+
 // Right-hand side of the tangent solve of row block n for tangent k:
 // A dq = db - dA q (q the step's solution; dA, db the tangents of A, b).
 YS_HD void tangent_rhs_row(const View& v, const double* YS_RESTRICT q, int n, int k, double r[5]) {

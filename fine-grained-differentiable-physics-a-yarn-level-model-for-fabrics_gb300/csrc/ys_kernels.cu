@@ -105,6 +105,7 @@ __global__ void k_pcg_start(Blocks b, Solver so, int ncloth) {
 }
 
 // q = A p and partial p.q (row 0)
+template <bool TRANS>
 __global__ void __launch_bounds__(kBlock) k_pcg_spmv(View v, Blocks b, Solver so) {
   __shared__ double sh[kBlock / 32];
   const int blk = blockIdx.x;
@@ -115,7 +116,8 @@ __global__ void __launch_bounds__(kBlock) k_pcg_spmv(View v, Blocks b, Solver so
   double pq = 0.0;
   if (threadIdx.x < b.blk_count[blk]) {
     double y[5];
-    spmv_row(v, so.p, n, y);
+    if (TRANS) spmv_row_t(v, so.p, n, y);
+    else spmv_row(v, so.p, n, y);
     for (int k = 0; k < 5; ++k) {
       st(so.q, k, nt, n) = y[k];
       pq += ld(so.p, k, nt, n) * y[k];
@@ -257,7 +259,8 @@ void launch_pcg_setup(const View& v, const Blocks& b, const Solver& so, cudaStre
   k_pcg_start<<<(v.ncloth + 127) / 128, 128, 0, s>>>(b, so, v.ncloth);
 }
 void launch_pcg_spmv(const View& v, const Blocks& b, const Solver& so, cudaStream_t s) {
-  k_pcg_spmv<<<b.nblk, kBlock, 0, s>>>(v, b, so);
+  if (so.trans) k_pcg_spmv<true><<<b.nblk, kBlock, 0, s>>>(v, b, so);
+  else k_pcg_spmv<false><<<b.nblk, kBlock, 0, s>>>(v, b, so);
 }
 void launch_pcg_axpy(const View& v, const Blocks& b, const Solver& so, int it, cudaStream_t s) {
   k_pcg_axpy<<<b.nblk, kBlock, 0, s>>>(v, b, so, it & 1);

@@ -40,6 +40,7 @@ struct Solver {
   PcgCloth* pc;   // [ncloth]
   int* nactive;   // device counter
   double tol;
+  int trans;      // 1: solve A^T x = b (the reference-mode tangent solves)
 };
 
 constexpr int kBlock = 128;

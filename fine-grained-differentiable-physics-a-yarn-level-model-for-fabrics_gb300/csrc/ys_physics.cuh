@@ -957,7 +957,10 @@ YS_HD void shear_element(const View& v, double* buf, double* dbuf, int n0, int s
   if (!jam) {
     const T kx = (comp + 1.0) * S * R * R * kPi;
     const T ph = phi - kPi / 2;
-    const T cf1 = (kx * Lc * ph) / (l1 * s), cf3 = (kx * Lc * ph) / (l3 * s);
+    // Shear_F takes phi.item() in (phi - PI/2) (src/PhysicsCloth.cpp:2720-2721):
+    // that factor carries no derivative along the reference's gradient path
+    const T phf = v.trunc ? detach(phi) - kPi / 2 : ph;
+    const T cf1 = (kx * Lc * phf) / (l1 * s), cf3 = (kx * Lc * phf) / (l3 * s);
     for (int i = 0; i < 3; ++i) { Fx1[i] = cf1 * a3[i]; Fx3[i] = cf3 * a1[i]; }
     const T k11 = (kx * Lc) / ((l1 * l1) * s), k33 = (kx * Lc) / ((l3 * l3) * s);
     const T k13 = (kx * Lc) / (l3 * l1 * s), k31 = (kx * Lc) / (l1 * l3 * s);

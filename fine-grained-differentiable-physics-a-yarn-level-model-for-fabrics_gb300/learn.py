@@ -1,0 +1,214 @@
+"""Differentiable rollouts and the parameter-learning interface of the
+reference (YarnSimNetHeter + constraint_para + the training loss), on the GPU
+step's forward-mode sensitivities.
+
+The reference learns 8 scalars of a two-yarn cloth -- rho, Y, B of each yarn
+type, S and mu (src/YarnSimNetHeter.h:4-120) -- through LibTorch autograd over
+whole rollouts (src/TrainHeter.h:160-231). Here a rollout runs on the device
+with ys_step_tangent carrying d(state)/d(theta) for all 8 parameters (two
+copies of the cloth in one batch, each carrying ys_tangent_count() = 4
+directions), and `Rollout` exposes the trajectory as a torch.autograd.Function
+whose backward contracts the incoming gradient with that Jacobian. Nothing
+of the trajectory has to be kept for the backward pass beyond the Jacobian of
+the returned states.
+
+Two gradient definitions (`mode`):
+  "exact"     -- the derivative of the discrete step (A dq = db - dA q),
+                 checked against central finite differences;
+  "reference" -- what the reference's loss.backward() computes: A, M and
+                 dF/dv enter without a graph (src/MatrixMp.cpp:40-99), the
+                 solve's backward is A^-1 g (src/Solvers.cpp:33-58), and the
+                 (phi - PI/2) factor of Shear_F is taken by .item()
+                 (src/PhysicsCloth.cpp:2720-2721); checked against gradients
+                 of the reference itself.
+"""
+from __future__ import annotations
+
+import math
+from typing import Dict, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _native as N
+from .cloth import ClothBatch, ClothSpec, InitPose, WovenPattern
+
+PARAM_NAMES = ("rho0", "Y0", "B0", "rho1", "Y1", "B1", "S", "mu")
+MODES = {"exact": N.YS_TANGENT_EXACT, "reference": N.YS_TANGENT_REFERENCE}
+
+
+def constraint_para(para, upper: float = 1.0, lower: float = 0.0):
+    """(upper - lower) * sigmoid(para) + lower (src/TrainHelper.cpp:3-7); note
+    the reference's call sites pass (range.first = upper, range.second = lower)."""
+    import torch
+    return (upper - lower) * torch.sigmoid(para) + lower
+
+
+def invert_constraint_para(para: float, upper: float = 1.0, lower: float = 0.0) -> float:
+    """Inverse of constraint_para (src/TrainHelper.cpp:9-13)."""
+    return -math.log((upper - lower) / (para - lower) - 1.0)
+
+
+def two_yarn_spec(template: Dict, theta: Sequence[float]) -> ClothSpec:
+    """ClothSpec of a two-yarn cloth: warp line j and weft line i use yarn
+    (j % 2) and (i % 2) (src/Cloth.cpp:195-268); theta in PARAM_NAMES order."""
+    W, H = int(template["width"]), int(template["length"])
+    y = [np.array(theta[0:3], float), np.array(theta[3:6], float)]
+    kw = dict(template)
+    kw.update(warp=np.array([y[j % 2] for j in range(H)]), weft=np.array([y[i % 2] for i in range(W)]),
+              S=float(theta[6]), mu=float(theta[7]))
+    return ClothSpec(**kw)
+
+
+def position_loss(traj_x, traj_e, gt_x, gt_e):
+    """sum_s (mean_N |x_s - x^_s|^2 + mean_N |e_s - e^_s|^2) / max(steps - 1, 1)
+    (src/TrainHeter.h:194-222); traj_*: [steps, N, 3|2] torch tensors."""
+    steps = traj_x.shape[0]
+    dl = traj_x - gt_x
+    de = traj_e - gt_e
+    loss = (dl * dl).sum(-1).mean(-1).sum() + (de * de).sum(-1).mean(-1).sum()
+    return loss / max(steps - 1, 1)
+
+
+def rollout_with_jacobian(template: Dict, theta: Sequence[float], state0: Dict, steps: int, h: float = 1e-3,
+                          mode: str = "exact", tol: float = 0.0, maxiter: int = -1, device: int = 0):
+    """Runs `steps` steps of the two-yarn cloth from state0 and returns
+    (traj_x [steps, N, 3], traj_e [steps, N, 2], J_x [steps, N, 3, 8],
+    J_e [steps, N, 2, 8], stats), J = d state / d theta."""
+    spec = two_yarn_spec(template, theta)
+    K = int(N.load().ys_tangent_count())
+    P = len(PARAM_NAMES)
+    copies = (P + K - 1) // K
+    batch = ClothBatch([spec] * copies, device=device)
+    try:
+        Nn = spec.num_nodes
+        st = {k: np.concatenate([np.asarray(state0[k], float)] * copies) for k in
+              ("LPos", "LPosFix", "LVel", "EPos", "EPosBar", "EVel") if k in state0}
+        batch.set_state(**st)
+        batch.tangent_enable(MODES[mode])
+        nl = spec.length + spec.width
+        parity = np.array([j % 2 for j in range(spec.length)] + [i % 2 for i in range(spec.width)])
+        drho = np.zeros((K, copies * nl)); dY = np.zeros_like(drho); dB = np.zeros_like(drho)
+        dS = np.zeros((K, copies)); dmu = np.zeros((K, copies))
+        for c in range(copies):
+            for k in range(K):
+                p = c * K + k
+                if p >= P:
+                    continue
+                if p < 6:
+                    [drho, dY, dB][p % 3][k, c * nl:(c + 1) * nl] = (parity == p // 3)
+                elif p == 6:
+                    dS[k, c] = 1.0
+                else:
+                    dmu[k, c] = 1.0
+        batch.tangent_seed(drho, dY, dB, dS, dmu)
+        tx = np.zeros((steps, Nn, 3)); te = np.zeros((steps, Nn, 2))
+        Jx = np.zeros((steps, Nn, 3, P)); Je = np.zeros((steps, Nn, 2, P))
+        stats = []
+        for s in range(steps):
+            stats.append(batch.step_tangent(h, tol=tol, maxiter=maxiter, kact=K))
+            cur = batch.get_state()
+            tan = batch.tangent_get_state()
+            tx[s] = cur["LPos"][:Nn]
+            te[s] = cur["EPos"][:Nn]
+            for c in range(copies):
+                for k in range(K):
+                    p = c * K + k
+                    if p < P:
+                        Jx[s, :, :, p] = tan["LPos"][k, c * Nn:(c + 1) * Nn]
+                        Je[s, :, :, p] = tan["EPos"][k, c * Nn:(c + 1) * Nn]
+        return tx, te, Jx, Je, stats
+    finally:
+        batch.close()
+
+
+def _rollout_function():
+    import torch
+
+    class Rollout(torch.autograd.Function):
+        """traj_x, traj_e = Rollout.apply(theta, template, state0, steps, h, mode, tol):
+        the states of a rollout as a differentiable function of theta
+        (PARAM_NAMES order, a float64 tensor of 8)."""
+
+        @staticmethod
+        def forward(ctx, theta, template, state0, steps, h, mode, tol):
+            th = theta.detach().cpu().numpy().astype(np.float64)
+            tx, te, Jx, Je, stats = rollout_with_jacobian(template, th, state0, steps, h, mode, tol)
+            ctx.stats = stats
+            dev = theta.device
+            Jx_t = torch.as_tensor(Jx, device=dev)
+            Je_t = torch.as_tensor(Je, device=dev)
+            ctx.save_for_backward(Jx_t, Je_t)
+            return torch.as_tensor(tx, device=dev), torch.as_tensor(te, device=dev)
+
+        @staticmethod
+        def backward(ctx, gx, ge):
+            Jx, Je = ctx.saved_tensors
+            g = torch.einsum("snc,sncp->p", gx, Jx) + torch.einsum("snc,sncp->p", ge, Je)
+            return g, None, None, None, None, None, None
+
+    return Rollout
+
+
+_ROLLOUT = None
+
+
+def rollout(theta, template: Dict, state0: Dict, steps: int, h: float = 1e-3, mode: str = "exact",
+            tol: float = 0.0) -> Tuple:
+    """Differentiable rollout (see Rollout)."""
+    global _ROLLOUT
+    if _ROLLOUT is None:
+        _ROLLOUT = _rollout_function()
+    return _ROLLOUT.apply(theta, template, state0, steps, h, mode, tol)
+
+
+def _module_base():
+    import torch
+    return torch.nn.Module
+
+
+class YarnSimNetHeter(_module_base()):
+    """The reference's YarnSimNetHeter (src/YarnSimNetHeter.h:4-120): raw
+    parameters rho_1, rho_2, Y_1, Y_2, B_1, B_2, S, mu mapped into their ranges
+    by constraint_para (ranges given as (upper, lower) pairs, as the reference
+    passes them), a two-yarn cloth (upright, handles) and its step.
+
+    rollout(state0, steps) returns the trajectory, differentiable w.r.t. the
+    parameters; forward(state) is one step without a graph (the reference's
+    forward(ClothState, bool&))."""
+
+    def __init__(self, width: int, length: int, R: float, L: float, raw: Dict[str, float],
+                 ranges: Dict[str, Tuple[float, float]], handles: Sequence[Tuple[int, int]], h: float = 1e-3,
+                 kf: float = 1000.0, df: float = 1000.0, kc: float = 1.0, handle_stiffness: float = 1e4,
+                 gravity: float = 9.8, wind_vel=(0.0, 0.0, 0.0), wind_density: float = 0.0, wind_drag: float = 0.0,
+                 woven_pattern: int = WovenPattern.Plain, height: float = 5.0, mode: str = "reference"):
+        import torch
+        super().__init__()
+        names = ("rho_1", "rho_2", "Y_1", "Y_2", "B_1", "B_2", "S", "mu")
+        for n in names:
+            self.register_parameter(n, torch.nn.Parameter(torch.tensor([float(raw[n])], dtype=torch.float64)))
+        self.ranges = dict(ranges)
+        self.h = h
+        self.mode = mode
+        self.template = dict(width=width, length=length, height=height, L=L, R=R, pose=InitPose.Upright,
+                             weave=int(woven_pattern), kc=kc, kf=kf, df=df, handle_stiffness=handle_stiffness,
+                             G=(0.0, 0.0, gravity), wind_vel=tuple(wind_vel), wind_density=wind_density,
+                             wind_drag=wind_drag, handles=list(handles))
+
+    def theta(self):
+        """Constrained parameters in PARAM_NAMES order (a float64 tensor of 8)."""
+        import torch
+        p = {n: constraint_para(getattr(self, n), *self.ranges[n]) for n in self.ranges}
+        return torch.cat([p["rho_1"], p["Y_1"], p["B_1"], p["rho_2"], p["Y_2"], p["B_2"], p["S"], p["mu"]])
+
+    def rollout(self, state0: Dict, steps: int, tol: float = 0.0):
+        return rollout(self.theta(), self.template, state0, steps, self.h, self.mode, tol)
+
+    def forward(self, state: Dict, tol: float = 0.0) -> Tuple[Dict, bool]:
+        th = self.theta().detach().cpu().numpy()
+        b = ClothBatch([two_yarn_spec(self.template, th)])
+        try:
+            b.set_state(**state)
+            ok = b.step(self.h, tol=tol)[0]["ok"]
+            return b.get_state(), ok
+        finally:
+            b.close()

@@ -94,6 +94,237 @@ std::string key(int u, int v) { return std::to_string(u) + "," + std::to_string(
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// mode=grad: the gradient the reference's parameter learning computes
+// (src/TrainHeter.h:160-231 with YarnSimNetHeter, src/YarnSimNetHeter.h):
+// two yarn types (lines alternate by parity) whose rho, Y, B and the cloth's
+// S and mu are LibTorch leaves; a ground-truth rollout with a second
+// parameter set from the same initial state; the loss
+//   sum_s (mean_N |x_s - x^_s|^2 + mean_N |e_s - e^_s|^2) / max(steps - 1, 1)
+// and loss.backward() through SimStep (src/TrainHelper.cpp:15-54) and
+// EigenSolver's backward (shim/eigen_cg.cpp). Writes "loss" and "grad" =
+// d loss / d (rho0, Y0, B0, rho1, Y1, B1, S, mu).
+struct Sim {
+  Cloth cloth;
+  Environment env;
+  PhysicsCloth phy;
+};
+
+int run_grad(std::map<std::string, std::string>& kv) {
+  const int W = static_cast<int>(get_d(kv, "width", 5));
+  const int Lh = static_cast<int>(get_d(kv, "length", 5));
+  const double height = get_d(kv, "height", 5.0);
+  const double L = get_d(kv, "L", 1e-3);
+  const double R = get_d(kv, "R", 1e-4);
+  const int steps = static_cast<int>(get_d(kv, "steps", 2));
+  ref_cg_set_options(get_d(kv, "cg_tol", DBL_EPSILON), static_cast<long>(get_d(kv, "cg_maxiter", -1)));
+  const std::string weave = get_s(kv, "weave", "plain");
+  WovenPattern wp = weave == "twill" ? WovenPattern::Twill : (weave == "satin" ? WovenPattern::Satin : WovenPattern::Plain);
+  InitPose ip = get_s(kv, "pose", "flat") == "upright" ? InitPose::Upright : InitPose::Flat;
+  std::vector<double> G = parse_list(get_s(kv, "G", "0,0,9.8"));
+  std::vector<double> wv = parse_list(get_s(kv, "wind_vel", "0,0,0"));
+  std::vector<std::pair<int, int>> handles;
+  {
+    std::vector<double> hl = parse_list(get_s(kv, "handles", ""));
+    for (size_t i = 0; i + 1 < hl.size(); i += 2) handles.emplace_back(static_cast<int>(hl[i]), static_cast<int>(hl[i + 1]));
+  }
+  const int N = W * Lh;
+  std::vector<double> init(N * 15);
+  const bool has_init = kv.count("init_state") > 0;
+  if (has_init) {
+    std::ifstream f(kv["init_state"], std::ios::binary);
+    f.read(reinterpret_cast<char*>(init.data()), init.size() * sizeof(double));
+  }
+  auto T1 = [&](const std::string& k, double d) { return torch::tensor({get_d(kv, k, d)}, opts); };
+  // params: rho0 Y0 B0 rho1 Y1 B1 S mu
+  auto build = [&](const std::vector<Tensor>& p) {
+    std::vector<Yarn> yarns{Yarn{R, p[0], p[1], p[2]}, Yarn{R, p[3], p[4], p[5]}};
+    Sim* sim = new Sim{Cloth(W, Lh, height, L, R, yarns, T1("kc", 1.0), T1("kf", 1000.0), T1("df", 1000.0), p[7], p[6],
+                             T1("handle_stiffness", 1e4), wp, ip),
+                       Environment{}, PhysicsCloth{}};
+    sim->cloth.set_handles(handles);
+    Wind wind{torch::tensor({wv[0], wv[1], wv[2]}, opts).view({3, 1}), T1("wind_density", 0.0), T1("wind_drag", 0.0)};
+    sim->env = Environment{&sim->cloth, torch::tensor({G[0], G[1], G[2]}, opts).view({3, 1}), wind};
+    sim->phy = PhysicsCloth{&sim->env};
+    if (has_init) {
+      const double* lp = init.data();
+      const double* lf = lp + 3 * N;
+      const double* lv = lf + 3 * N;
+      const double* ep = lv + 3 * N;
+      const double* eb = ep + 2 * N;
+      const double* ev = eb + 2 * N;
+      for (int v = 0; v < Lh; ++v)
+        for (int u = 0; u < W; ++u) {
+          int id = u + v * W;
+          Node& n = sim->cloth.nodes[key(u, v)];
+          n.LPos = torch::tensor({lp[3 * id], lp[3 * id + 1], lp[3 * id + 2]}, opts).view({3, 1});
+          n.LPosFix = torch::tensor({lf[3 * id], lf[3 * id + 1], lf[3 * id + 2]}, opts).view({3, 1});
+          n.LVel = torch::tensor({lv[3 * id], lv[3 * id + 1], lv[3 * id + 2]}, opts).view({3, 1});
+          n.EPos = torch::tensor({ep[2 * id], ep[2 * id + 1]}, opts).view({2, 1});
+          n.EPosBar = torch::tensor({eb[2 * id], eb[2 * id + 1]}, opts).view({2, 1});
+          n.EVel = torch::tensor({ev[2 * id], ev[2 * id + 1]}, opts).view({2, 1});
+          sim->cloth.warp_nodes[key(u, v)].LPos = n.LPos;
+          sim->cloth.weft_nodes[key(u, v)].LPos = n.LPos;
+        }
+      sim->cloth.UpdateClothUnits();
+    }
+    sim->phy.InitMV();
+    return sim;
+  };
+  const Tensor h = torch::tensor({get_d(kv, "h", 1e-3)}, opts);
+  auto step = [&](Sim* sim) {
+    sim->phy.FillMV();
+    const Tensor M = sim->phy.get_SpaM();
+    const Tensor Kx = sim->phy.get_SpaFPos();
+    const Tensor Dv = sim->phy.get_SpaFVel();
+    const Tensor A = M - Kx * torch::pow(h, 2) - Dv * h;
+    const Tensor b = h * (sim->phy.get_SpaF() - torch::mm(Dv.transpose(0, 1), sim->phy.get_SpaVel())) +
+                     torch::mm(M, sim->phy.get_SpaVel());
+    Tensor new_vel = EigenSolver::apply(A, b);
+    sim->cloth.update(new_vel, sim->phy.F_E_is_Slides[0], h);
+    sim->phy.ResetMV();
+  };
+  auto positions = [&](Sim* sim, bool detach) {
+    std::vector<Tensor> xs, es;
+    for (int v = 0; v < Lh; ++v)
+      for (int u = 0; u < W; ++u) {
+        const Node& n = sim->cloth.nodes.at(key(u, v));
+        xs.push_back(detach ? n.LPos.detach() : n.LPos);
+        es.push_back(detach ? n.EPos.detach() : n.EPos);
+      }
+    return std::make_pair(torch::stack(xs), torch::stack(es));
+  };
+  // ground truth
+  std::vector<double> gt = parse_list(get_s(kv, "gt_params", ""));
+  std::vector<Tensor> gtp;
+  for (double x : gt) gtp.push_back(torch::tensor({x}, opts));
+  Sim* ref = build(gtp);
+  std::vector<std::pair<Tensor, Tensor>> target;
+  for (int s = 0; s < steps; ++s) {
+    step(ref);
+    target.push_back(positions(ref, true));
+  }
+  // learned parameters as leaves
+  std::vector<double> th = parse_list(get_s(kv, "params", ""));
+  std::vector<Tensor> leaves;
+  for (double x : th) leaves.push_back(torch::tensor({x}, opts).requires_grad_(true));
+  Sim* sim = build(leaves);
+  Tensor loss = torch::zeros(1, opts);
+  std::vector<std::pair<Tensor, Tensor>> traj;
+  for (int s = 0; s < steps; ++s) {
+    step(sim);
+    auto pe = positions(sim, false);
+    traj.push_back(std::make_pair(pe.first.detach(), pe.second.detach()));
+    Tensor dl = pe.first - target[s].first, de = pe.second - target[s].second;
+    Tensor pos_loss = torch::mean(torch::bmm(dl.transpose(2, 1), dl)) + torch::mean(torch::bmm(de.transpose(2, 1), de));
+    loss = loss + pos_loss;
+  }
+  loss = loss / (steps - 1 > 0 ? steps - 1 : 1);
+  loss.backward();
+  Writer w(get_s(kv, "out", "ref_out.bin"));
+  double lv = loss.item<double>();
+  w.put("loss", {1}, &lv);
+  std::vector<double> g;
+  for (auto& t : leaves) g.push_back(t.grad().defined() ? t.grad().item<double>() : 0.0);
+  w.put("grad", {static_cast<int>(g.size())}, g.data());
+  for (int s = 0; s < steps; ++s) {
+    const std::string t = std::to_string(s + 1);
+    w.put_tensor("target" + t + ".LPos", target[s].first.reshape({N, 3}));
+    w.put_tensor("target" + t + ".EPos", target[s].second.reshape({N, 2}));
+    w.put_tensor("traj" + t + ".LPos", traj[s].first.reshape({N, 3}));
+    w.put_tensor("traj" + t + ".EPos", traj[s].second.reshape({N, 2}));
+  }
+  double st = 0;
+  w.put("status", {1}, &st);
+  delete sim;
+  delete ref;
+  return 0;
+}
+
+// mode=vjp: c^T (db / d state) by autograd at one state, for a probe vector c
+// (key "probe", reference DOF layout), with b = h (F - D^T v) + M v as SimStep
+// forms it (M, D built without a graph). Writes "g.LPos", "g.LVel" [N][3],
+// "g.EPos", "g.EPosBar", "g.EVel" [N][2].
+int run_vjp(std::map<std::string, std::string>& kv) {
+  const int W = static_cast<int>(get_d(kv, "width", 5));
+  const int Lh = static_cast<int>(get_d(kv, "length", 5));
+  const double R = get_d(kv, "R", 1e-4);
+  std::vector<double> th = parse_list(get_s(kv, "params", ""));
+  std::vector<Tensor> p;
+  for (double x : th) p.push_back(torch::tensor({x}, opts));
+  std::vector<Yarn> yarns{Yarn{R, p[0], p[1], p[2]}, Yarn{R, p[3], p[4], p[5]}};
+  const std::string weave = get_s(kv, "weave", "plain");
+  WovenPattern wp = weave == "twill" ? WovenPattern::Twill : (weave == "satin" ? WovenPattern::Satin : WovenPattern::Plain);
+  InitPose ip = get_s(kv, "pose", "flat") == "upright" ? InitPose::Upright : InitPose::Flat;
+  auto T1 = [&](const std::string& k, double d) { return torch::tensor({get_d(kv, k, d)}, opts); };
+  Cloth cloth(W, Lh, get_d(kv, "height", 5.0), get_d(kv, "L", 1e-3), R, yarns, T1("kc", 1.0), T1("kf", 1000.0),
+              T1("df", 1000.0), p[7], p[6], T1("handle_stiffness", 1e4), wp, ip);
+  std::vector<std::pair<int, int>> handles;
+  {
+    std::vector<double> hl = parse_list(get_s(kv, "handles", ""));
+    for (size_t i = 0; i + 1 < hl.size(); i += 2) handles.emplace_back(static_cast<int>(hl[i]), static_cast<int>(hl[i + 1]));
+  }
+  cloth.set_handles(handles);
+  std::vector<double> G = parse_list(get_s(kv, "G", "0,0,9.8"));
+  std::vector<double> wv = parse_list(get_s(kv, "wind_vel", "0,0,0"));
+  Wind wind{torch::tensor({wv[0], wv[1], wv[2]}, opts).view({3, 1}), T1("wind_density", 0.0), T1("wind_drag", 0.0)};
+  Environment env{&cloth, torch::tensor({G[0], G[1], G[2]}, opts).view({3, 1}), wind};
+  const int N = W * Lh;
+  std::vector<double> init(N * 15);
+  {
+    std::ifstream f(kv["init_state"], std::ios::binary);
+    f.read(reinterpret_cast<char*>(init.data()), init.size() * sizeof(double));
+  }
+  const double* lp = init.data();
+  const double* lf = lp + 3 * N;
+  const double* lv = lf + 3 * N;
+  const double* ep = lv + 3 * N;
+  const double* eb = ep + 2 * N;
+  const double* ev = eb + 2 * N;
+  std::vector<Tensor> leaves;  // per node: LPos, LVel, EPos, EPosBar, EVel
+  for (int v = 0; v < Lh; ++v)
+    for (int u = 0; u < W; ++u) {
+      int id = u + v * W;
+      Node& n = cloth.nodes[key(u, v)];
+      n.LPos = torch::tensor({lp[3 * id], lp[3 * id + 1], lp[3 * id + 2]}, opts).view({3, 1}).requires_grad_(true);
+      n.LPosFix = torch::tensor({lf[3 * id], lf[3 * id + 1], lf[3 * id + 2]}, opts).view({3, 1});
+      n.LVel = torch::tensor({lv[3 * id], lv[3 * id + 1], lv[3 * id + 2]}, opts).view({3, 1}).requires_grad_(true);
+      n.EPos = torch::tensor({ep[2 * id], ep[2 * id + 1]}, opts).view({2, 1}).requires_grad_(true);
+      n.EPosBar = torch::tensor({eb[2 * id], eb[2 * id + 1]}, opts).view({2, 1}).requires_grad_(true);
+      n.EVel = torch::tensor({ev[2 * id], ev[2 * id + 1]}, opts).view({2, 1}).requires_grad_(true);
+      leaves.push_back(n.LPos); leaves.push_back(n.LVel); leaves.push_back(n.EPos);
+      leaves.push_back(n.EPosBar); leaves.push_back(n.EVel);
+      cloth.warp_nodes[key(u, v)].LPos = n.LPos;
+      cloth.weft_nodes[key(u, v)].LPos = n.LPos;
+    }
+  cloth.UpdateClothUnits();
+  PhysicsCloth phy{&env};
+  phy.InitMV();
+  const Tensor h = torch::tensor({get_d(kv, "h", 1e-3)}, opts);
+  phy.FillMV();
+  const Tensor M = phy.get_SpaM();
+  const Tensor Dv = phy.get_SpaFVel();
+  const Tensor b = h * (phy.get_SpaF() - torch::mm(Dv.transpose(0, 1), phy.get_SpaVel())) + torch::mm(M, phy.get_SpaVel());
+  std::vector<double> c = parse_list(get_s(kv, "probe", ""));
+  Tensor phi = torch::sum(b.view({-1}) * torch::tensor(c, opts));
+  phi.backward();
+  Writer w(get_s(kv, "out", "ref_out.bin"));
+  std::vector<double> gl(N * 3), gv(N * 3), ge(N * 2), gb(N * 2), gev(N * 2);
+  for (int id = 0; id < N; ++id) {
+    auto G3 = [&](const Tensor& t, std::vector<double>& o, int k) {
+      for (int r = 0; r < k; ++r) o[k * id + r] = t.grad().defined() ? t.grad()[r][0].item<double>() : 0.0;
+    };
+    G3(leaves[5 * id], gl, 3); G3(leaves[5 * id + 1], gv, 3); G3(leaves[5 * id + 2], ge, 2);
+    G3(leaves[5 * id + 3], gb, 2); G3(leaves[5 * id + 4], gev, 2);
+  }
+  w.put("g.LPos", {N, 3}, gl.data()); w.put("g.LVel", {N, 3}, gv.data()); w.put("g.EPos", {N, 2}, ge.data());
+  w.put("g.EPosBar", {N, 2}, gb.data()); w.put("g.EVel", {N, 2}, gev.data());
+  w.put_tensor("b", b);
+  double st = 0;
+  w.put("status", {1}, &st);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) {
     std::fprintf(stderr, "usage: %s config\n", argv[0]);
@@ -101,6 +332,8 @@ int main(int argc, char** argv) {
   }
   torch::set_num_threads(1);
   auto kv = read_config(argv[1]);
+  if (get_s(kv, "mode", "") == "grad") return run_grad(kv);
+  if (get_s(kv, "mode", "") == "vjp") return run_vjp(kv);
 
   const int W = static_cast<int>(get_d(kv, "width", 5));
   const int Lh = static_cast<int>(get_d(kv, "length", 5));

@@ -28,6 +28,7 @@ struct Emu {
   ys::Records R{};
   int bad = 0;
   // forward-mode tangents (kTangents directions)
+  int tmode = 0;  // 0 exact, 1 reference (M, D, A held constant; transposed solves)
   std::vector<double> dX, dV, dUV, dUVD, dUVB, dNRM, dCOMP, dSLIDE, drho, dks, dkb, dS, dmu, dA, dB, dRE, dRB, dRF,
       dRS, As, Bs, RT, DQ, QS;
 
@@ -112,6 +113,7 @@ constexpr int KT = ys::kTangents;
 void emu_assemble(void* h, double dt, const double* ext);
 
 int emu_tangent_count(void) { return KT; }
+void emu_tangent_mode(void* h, int mode) { static_cast<Emu*>(h)->tmode = mode; }
 
 void emu_tangent_init(void* h) {
   Emu* e = static_cast<Emu*>(h);
@@ -182,7 +184,7 @@ long emu_tangent_raw(void* h, int which, double* out) {
 }
 
 // Jacobi-PCG as emu_solve on an arbitrary right-hand side
-static long pcg(Emu* e, const double* b, double* x, double tol, long maxiter) {
+static long pcg(Emu* e, const double* b, double* x, double tol, long maxiter, bool trans = false) {
   ys::View& v = e->v;
   const int N = e->N;
   std::vector<double> r(5 * N), p(5 * N), q(5 * N), z(5 * N);
@@ -199,7 +201,8 @@ static long pcg(Emu* e, const double* b, double* x, double tol, long maxiter) {
     double pq = 0;
     for (int n = 0; n < N; ++n) {
       double y[5];
-      ys::spmv_row(v, p.data(), n, y);
+      if (trans) ys::spmv_row_t(v, p.data(), n, y);
+      else ys::spmv_row(v, p.data(), n, y);
       for (int k = 0; k < 5; ++k) { q[k * N + n] = y[k]; pq += p[k * N + n] * y[k]; }
     }
     const double alpha = rz / pq;
@@ -234,6 +237,7 @@ int emu_step_tangent(void* h, double dt, const double* ext, double tol, int kact
   ys::View dv = e->v;
   dv.A = e->As.data(); dv.B = e->Bs.data();
   dv.K = KT;
+  dv.trunc = e->tmode;
   dv.dX = e->dX.data(); dv.dV = e->dV.data(); dv.dUV = e->dUV.data(); dv.dUVD = e->dUVD.data();
   dv.dUVB = e->dUVB.data(); dv.dNRM = e->dNRM.data(); dv.dCOMP = e->dCOMP.data(); dv.dSLIDE = e->dSLIDE.data();
   dv.dline_rho = e->drho.data(); dv.dline_ks = e->dks.data(); dv.dline_kb = e->dkb.data();
@@ -272,7 +276,7 @@ int emu_step_tangent(void* h, double dt, const double* ext, double tol, int kact
       ys::tangent_rhs_row(dv, e->SOL.data(), n, k, r);
       for (int c = 0; c < 5; ++c) rk[c * N + n] = r[c];
     }
-    pcg(e, rk.data(), xk.data(), tol, 2 * dim);
+    pcg(e, rk.data(), xk.data(), tol, 2 * dim, e->tmode == 1);
     for (int c = 0; c < 5; ++c)
       for (int n = 0; n < N; ++n) e->DQ[((size_t)c * KT + k) * N + n] = xk[c * N + n];
   }

@@ -72,6 +72,7 @@ def lib():
         L.emu_update.restype = ctypes.c_int
         L.emu_tangent_count.restype = ctypes.c_int
         L.emu_tangent_init.argtypes = [ctypes.c_void_p]
+        L.emu_tangent_mode.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.emu_tangent_seed.argtypes = [ctypes.c_void_p] + [_dp] * 5
         L.emu_tangent_state.argtypes = [ctypes.c_void_p] + [_dp] * 5 + [ctypes.c_int]
         L.emu_step_tangent.argtypes = [ctypes.c_void_p, ctypes.c_double, _dp, ctypes.c_double, ctypes.c_int]
@@ -136,8 +137,11 @@ class EmuCloth:
     def K(self):
         return int(lib().emu_tangent_count())
 
-    def tangent_init(self):
+    def tangent_init(self, mode=0):
+        """mode 0: exact tangents; 1: the reference's gradient path (M, D, A
+        held constant, transposed solves)."""
         lib().emu_tangent_init(self.h)
+        lib().emu_tangent_mode(self.h, int(mode))
 
     def tangent_seed(self, drho=None, dY=None, dB=None, dS=None, dmu=None):
         """drho, dY, dB: [K][lines] (warp rows then weft columns); dS, dmu: [K]."""

@@ -126,3 +126,44 @@ def test_zero_seeds_give_zero_tangents():
         assert em.step_tangent(float(g["h"])) == 0
     for key, v in em.tangent_get_state().items():
         assert not np.any(v), key
+
+
+@pytest.mark.parametrize("name", ["grad_plain6_upright", "grad_twill6_upright"])
+def test_reference_mode_matches_libtorch_gradient(name):
+    """The reference-mode tangents (M, D, A held constant, transposed solves,
+    Shear_F's detached angle factor) reproduce the gradient the reference's
+    own loss.backward() computes (tests/golden/make_grad_golden.py)."""
+    g = np.load(goldens.os.path.join(goldens.GOLDEN_DIR, name + ".npz"))
+    W, H = int(g["width"]), int(g["length"])
+    N, steps, th = W * H, int(g["steps"]), g["params"]
+    warp = np.array([th[0:3] if j % 2 == 0 else th[3:6] for j in range(H)])
+    weft = np.array([th[0:3] if i % 2 == 0 else th[3:6] for i in range(W)])
+    kw = dict(width=W, length=H, warp=warp, weft=weft, weave=int(g["weave"]), pose=int(g["pose"]), R=float(g["R"]),
+              L=float(g["L"]), height=float(g["height"]), S=th[6], mu=th[7],
+              handles=[tuple(int(a) for a in x) for x in g["handles"]], wind_vel=tuple(float(x) for x in g["wind_vel"]),
+              wind_density=float(g["wind_density"]), wind_drag=float(g["wind_drag"]))
+    init = {k: g["init_" + k] for k in ("LPos", "LPosFix", "LVel", "EPos", "EPosBar", "EVel")}
+    parity = np.array([j % 2 for j in range(H)] + [i % 2 for i in range(W)])
+    K = EmuCloth(**kw).K
+    grad = np.zeros(8)
+    for g0 in range(0, 8, K):
+        em = EmuCloth(**kw)
+        em.set_state(init)
+        em.tangent_init(1)
+        seeds = [np.zeros((K, W + H)) for _ in range(3)] + [np.zeros(K), np.zeros(K)]
+        for kk in range(K):
+            p = g0 + kk
+            if p < 6:
+                seeds[p % 3][kk] = (parity == p // 3)
+            else:
+                seeds[3 if p == 6 else 4][kk] = 1.0
+        em.tangent_seed(*seeds)
+        for s in range(1, steps + 1):
+            assert em.step_tangent(1e-3, tol=1e-14) == 0
+            st, T = em.get_state(), em.tangent_get_state()
+            dx = st["LPos"] - g["target%d_LPos" % s]
+            de = st["EPos"] - g["target%d_EPos" % s]
+            for kk in range(K):
+                grad[g0 + kk] += 2.0 / N * (np.sum(dx * T["LPos"][kk]) + np.sum(de * T["EPos"][kk])) / max(steps - 1, 1)
+    err = np.abs(grad - g["grad"]) / np.abs(g["grad"])
+    assert err.max() <= 1e-9, err

@@ -170,3 +170,91 @@ def test_batched_tangents_equal_single():
             assert np.array_equal(T[key][:, off:off + N], single[key]), key
         off += N
     b.close()
+
+
+# ---------------------------------------------------------------- learning
+def _grad_setup(name):
+    import torch
+    g = goldens.load(name)
+    tmpl = dict(width=int(g["width"]), length=int(g["length"]), height=float(g["height"]), L=float(g["L"]),
+                R=float(g["R"]), pose=int(g["pose"]), weave=int(g["weave"]), kc=float(g["kc"]), kf=float(g["kf"]),
+                df=float(g["df"]), handle_stiffness=float(g["handle_stiffness"]),
+                G=tuple(float(x) for x in g["G"]), wind_vel=tuple(float(x) for x in g["wind_vel"]),
+                wind_density=float(g["wind_density"]), wind_drag=float(g["wind_drag"]),
+                handles=[tuple(int(a) for a in r) for r in g["handles"]])
+    state0 = {k: g["init_" + k] for k in ("LPos", "LPosFix", "LVel", "EPos", "EPosBar", "EVel")}
+    steps = int(g["steps"])
+    gt_x = torch.tensor(np.stack([g["target%d_LPos" % s] for s in range(1, steps + 1)]))
+    gt_e = torch.tensor(np.stack([g["target%d_EPos" % s] for s in range(1, steps + 1)]))
+    return g, tmpl, state0, steps, gt_x, gt_e
+
+
+@pytest.mark.parametrize("name", goldens.grad_names())
+def test_reference_gradient_matches_libtorch(name):
+    """ys.rollout(mode="reference") + the training loss: the gradient the
+    reference's own loss.backward() computes, 1e-7 relative per parameter."""
+    import torch
+    g, tmpl, state0, steps, gt_x, gt_e = _grad_setup(name)
+    theta = torch.tensor(g["params"], dtype=torch.float64, requires_grad=True)
+    tx, te = ys.rollout(theta, tmpl, state0, steps, 1e-3, "reference", tol=1e-14)
+    loss = ys.position_loss(tx, te, gt_x, gt_e)
+    loss.backward()
+    assert abs(loss.item() - float(g["loss"][0])) <= 1e-6 * abs(float(g["loss"][0]))
+    err = np.abs(theta.grad.numpy() - g["grad"]) / np.abs(g["grad"])
+    assert err.max() <= 1e-7, err
+
+
+def test_exact_gradient_matches_finite_differences():
+    """ys.rollout(mode="exact"): the loss gradient against Richardson central
+    differences of the GPU rollout, 1e-5 relative per parameter; 1e-3 for mu,
+    whose effect on this loss is about 1e-6 of the loss, the limit of what the
+    difference quotient resolves."""
+    import torch
+    g, tmpl, state0, steps, gt_x, gt_e = _grad_setup("grad_plain6_upright")
+    th0 = np.array(g["params"], float)
+    theta = torch.tensor(th0, requires_grad=True)
+    tx, te = ys.rollout(theta, tmpl, state0, steps, 1e-3, "exact", tol=1e-14)
+    loss = ys.position_loss(tx, te, gt_x, gt_e)
+    loss.backward()
+    grad = theta.grad.numpy()
+
+    def L(th):
+        with torch.no_grad():
+            a, b = ys.rollout(torch.tensor(th), tmpl, state0, steps, 1e-3, "exact", tol=1e-14)
+            return ys.position_loss(a, b, gt_x, gt_e).item()
+
+    for p in range(8):
+        eps = 1e-4 * th0[p]
+        d = np.zeros(8)
+        d[p] = eps
+        d1 = (L(th0 + d) - L(th0 - d)) / (2 * eps)
+        d2 = (L(th0 + d / 2) - L(th0 - d / 2)) / eps
+        fd = (4 * d2 - d1) / 3
+        if abs(fd) * th0[p] < 1e-8 * loss.item():
+            continue  # below the resolution of the loss
+        tol = 1e-3 if ys.PARAM_NAMES[p] == "mu" else 1e-5
+        assert abs(grad[p] - fd) <= tol * abs(fd), (ys.PARAM_NAMES[p], grad[p], fd)
+
+
+def test_yarnsimnet_heter_rollout_gradient():
+    """YarnSimNetHeter's raw parameters through constraint_para (the ranges of
+    src/TrainHeter.h:80-105): grad = dL/dtheta * dtheta/draw."""
+    import torch
+    g, tmpl, state0, steps, gt_x, gt_e = _grad_setup("grad_plain6_upright")
+    ranges = dict(rho_1=(0.003, 0.001), rho_2=(0.003, 0.001), Y_1=(800000.0, 0.0), Y_2=(300000.0, 0.0),
+                  B_1=(0.00018, 0.00005), B_2=(0.00018, 0.00005), S=(1200.0, 0.0), mu=(1.0, 0.0))
+    init = dict(zip(("rho_1", "Y_1", "B_1", "rho_2", "Y_2", "B_2", "S", "mu"), g["params"]))
+    raw = {k: ys.invert_constraint_para(v, *ranges[k]) for k, v in init.items()}
+    net = ys.YarnSimNetHeter(tmpl["width"], tmpl["length"], tmpl["R"], tmpl["L"], raw, ranges, tmpl["handles"],
+                             wind_vel=tmpl["wind_vel"], wind_density=tmpl["wind_density"],
+                             wind_drag=tmpl["wind_drag"], height=tmpl["height"], mode="reference")
+    assert np.allclose(net.theta().detach().numpy(), g["params"], rtol=1e-12)
+    tx, te = net.rollout(state0, steps, tol=1e-14)
+    ys.position_loss(tx, te, gt_x, gt_e).backward()
+    order = ("rho_1", "Y_1", "B_1", "rho_2", "Y_2", "B_2", "S", "mu")
+    for p, n in enumerate(order):
+        up, lo = ranges[n]
+        s = 1.0 / (1.0 + np.exp(-raw[n]))
+        expect = g["grad"][p] * (up - lo) * s * (1 - s)
+        got = getattr(net, n).grad.item()
+        assert abs(got - expect) <= 1e-7 * abs(expect), (n, got, expect)
