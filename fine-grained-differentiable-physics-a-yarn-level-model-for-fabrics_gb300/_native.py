@@ -21,7 +21,9 @@ EXPORTED = [
     "ys_cloth_dim", "ys_set_state", "ys_get_state", "ys_set_wind", "ys_set_winds", "ys_assemble", "ys_export_system",
     "ys_solve", "ys_get_solution", "ys_step", "ys_apply_system", "ys_synchronize", "ys_profile",
     "ys_profile_read", "ys_apply_system_noalloc", "ys_tangent_count", "ys_tangent_enable", "ys_tangent_seed",
-    "ys_tangent_set_state", "ys_tangent_get_state", "ys_step_tangent",
+    "ys_tangent_set_state", "ys_tangent_get_state", "ys_step_tangent", "ys_cloth_mesh_topology",
+    "ys_collider_create", "ys_collider_destroy", "ys_collider_set_positions", "ys_collider_find_pairs",
+    "ys_collider_get_pairs", "ys_collider_find_impacts", "ys_collider_get_impacts",
 ]
 YS_TANGENT_EXACT, YS_TANGENT_REFERENCE = 0, 1
 PROF_KINDS = ["geom", "edges", "bends", "faces", "gather", "shear", "finalize", "pcg_setup", "spmv", "axpy", "dir",
@@ -107,13 +109,23 @@ def load(build_if_missing: bool = True):
     L.ys_tangent_set_state.argtypes = [vp, vp, vp, vp, vp, vp, ctypes.c_int32]
     L.ys_tangent_get_state.argtypes = [vp, vp, vp, vp, vp, vp, ctypes.c_int32]
     L.ys_step_tangent.argtypes = [vp, ctypes.c_double, vp, ctypes.c_int32, vp, ctypes.c_int32, vp]
+    L.ys_cloth_mesh_topology.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp]
+    L.ys_collider_create.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int32, ctypes.c_int32, vp,
+                                     ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, ctypes.POINTER(vp)]
+    L.ys_collider_destroy.argtypes = [vp]
+    L.ys_collider_destroy.restype = None
+    L.ys_collider_set_positions.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int32]
+    L.ys_collider_find_pairs.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    L.ys_collider_get_pairs.argtypes = [vp, vp, ctypes.c_int64]
+    L.ys_collider_find_impacts.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    L.ys_collider_get_impacts.argtypes = [vp, vp, ctypes.c_int64]
     L.ys_synchronize.argtypes = [vp]
     L.ys_profile.argtypes = [vp, ctypes.c_int32]
     L.ys_profile_read.argtypes = [vp, _dp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                   ctypes.c_int32]
     for name in EXPORTED:
         if name not in ("ys_batch_destroy", "ys_last_error", "ys_cloth_node_offset", "ys_cloth_dim",
-                        "ys_tangent_count"):
+                        "ys_tangent_count", "ys_collider_destroy"):
             getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -121,6 +133,12 @@ def load(build_if_missing: bool = True):
 
 def last_error() -> str:
     return load().ys_last_error().decode()
+
+
+class Impact(ctypes.Structure):
+    """ys_impact (include/yarnsim.h)."""
+    _fields_ = [("type", ctypes.c_int32), ("nodes", ctypes.c_int32 * 4), ("t", ctypes.c_double),
+                ("w", ctypes.c_double * 4), ("n", ctypes.c_double * 3), ("pair", ctypes.c_int64)]
 
 
 class YarnSimError(RuntimeError):

@@ -15,8 +15,8 @@ ROOT = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
 LIB_DIR = os.path.join(PKG_DIR, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libyarnsim.so")
-SOURCES = ["ys_tangent.cu", "ys_kernels.cu", "ys_api.cu"]
-HEADERS = ["ys_common.cuh", "ys_dual.cuh", "ys_physics.cuh", "ys_items.cuh", "ys_elem_kernels.cuh", "ys_kernels.cuh"]
+SOURCES = ["ys_tangent.cu", "ys_kernels.cu", "ys_api.cu", "ys_collide.cu"]
+HEADERS = ["ys_common.cuh", "ys_dual.cuh", "ys_physics.cuh", "ys_items.cuh", "ys_elem_kernels.cuh", "ys_kernels.cuh", "ys_collide.cuh", "ys_bvh.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC"]
 

@@ -1,0 +1,86 @@
+"""Continuous collision detection of a cloth mesh against itself and an
+obstacle mesh on the GPU: the reference's Collision::find_impacts
+(src/Collision.cpp:184-208) -- its 18-DOP BVH broad phase and the
+vertex-face / edge-edge narrow phase -- behind the C ABI's ys_collider_*.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+
+from . import _native as N
+
+
+def cloth_mesh_topology(width: int, length: int):
+    """(faces [F, 3], face_edges [F, 3, 2]) of a width x length cloth's mesh in
+    the reference's order (src/Cloth.cpp:271-294)."""
+    F = 2 * (width - 1) * (length - 1)
+    faces = np.zeros((F, 3), np.int32)
+    edges = np.zeros((F, 3, 2), np.int32)
+    N.check(N.load().ys_cloth_mesh_topology(int(width), int(length), ctypes.c_void_p(faces.ctypes.data),
+                                            ctypes.c_void_p(edges.ctypes.data)), "ys_cloth_mesh_topology")
+    return faces, edges
+
+
+class Collider:
+    """Broad and narrow phase for one cloth of width x length nodes
+    (node u + v * width) and an optional obstacle (vertices [No, 3], faces
+    [Fo, 3]). thickness dilates the boxes (Collision::thickness); ccd = True
+    makes every box span the step's start and end positions."""
+
+    def __init__(self, width: int, length: int, obstacle_faces: Optional[np.ndarray] = None,
+                 n_obstacle_nodes: int = 0, thickness: float = 5e-4, ccd: bool = True, device: int = 0,
+                 stream: Optional[int] = None):
+        self.width, self.length = int(width), int(length)
+        self.n_nodes = self.width * self.length
+        self.faces, self.face_edges = cloth_mesh_topology(self.width, self.length)
+        of = np.zeros((0, 3), np.int32) if obstacle_faces is None else np.ascontiguousarray(obstacle_faces, np.int32)
+        self.obstacle_faces = of
+        self.n_obs_nodes = int(n_obstacle_nodes)
+        h = ctypes.c_void_p()
+        N.check(N.load().ys_collider_create(self.n_nodes, len(self.faces), ctypes.c_void_p(self.faces.ctypes.data),
+                                            ctypes.c_void_p(self.face_edges.ctypes.data), self.n_obs_nodes, len(of),
+                                            ctypes.c_void_p(of.ctypes.data) if len(of) else None, float(thickness),
+                                            int(bool(ccd)), int(device), ctypes.c_void_p(stream) if stream else None,
+                                            ctypes.byref(h)), "ys_collider_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.load().ys_collider_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_positions(self, x, x_prev, obs_x=None, obs_x_prev=None):
+        """Node positions at the end / start of the step, [n, 3] float64 (host)."""
+        arrs = [np.ascontiguousarray(a, np.float64) if a is not None else None for a in (x, x_prev, obs_x, obs_x_prev)]
+        ptr = [ctypes.c_void_p(a.ctypes.data) if a is not None else None for a in arrs]
+        N.check(N.load().ys_collider_set_positions(self._h, *ptr, 0), "ys_collider_set_positions")
+
+    def pairs(self) -> np.ndarray:
+        """Broad phase: [P, 3] int32 (first face, second face, 1 if obstacle)."""
+        n = ctypes.c_int64()
+        N.check(N.load().ys_collider_find_pairs(self._h, ctypes.byref(n)), "ys_collider_find_pairs")
+        out = np.zeros((n.value, 3), np.int32)
+        N.check(N.load().ys_collider_get_pairs(self._h, ctypes.c_void_p(out.ctypes.data), n.value),
+                "ys_collider_get_pairs")
+        return out
+
+    def impacts(self) -> dict:
+        """Narrow phase over the last pair list: dict of arrays type [I],
+        nodes [I, 4] (obstacle nodes as -1 - id), t [I], w [I, 4], n [I, 3],
+        pair [I]."""
+        n = ctypes.c_int64()
+        N.check(N.load().ys_collider_find_impacts(self._h, ctypes.byref(n)), "ys_collider_find_impacts")
+        buf = (N.Impact * max(n.value, 1))()
+        N.check(N.load().ys_collider_get_impacts(self._h, buf, n.value), "ys_collider_get_impacts")
+        a = np.ctypeslib.as_array(buf)[:n.value]
+        return dict(type=a["type"].copy(), nodes=a["nodes"].copy(), t=a["t"].copy(), w=a["w"].copy(),
+                    n=a["n"].copy(), pair=a["pair"].copy())

@@ -201,6 +201,11 @@ int weave_flip(int weave, int i, int j) {
 
 }  // namespace
 
+// error reporting for the other translation units of the library (not exported)
+extern "C" __attribute__((visibility("hidden"))) ys_status ys_internal_fail(ys_status s, const char* msg) {
+  return fail(s, msg);
+}
+
 extern "C" {
 
 const char* ys_last_error(void) { return g_err.c_str(); }

@@ -1,0 +1,522 @@
+// ys_collide.cu -- continuous collision detection of a cloth mesh against
+// itself and an obstacle mesh (the reference's Collision::find_impacts,
+// src/Collision.cpp:184-208): host tree construction (ys_bvh.h), device
+// refit, broad phase (one thread per cloth face traversing the cloth tree
+// and the obstacle tree) and narrow phase (one thread per face pair), with
+// deterministic output order (face-major, tree order within a face; impacts
+// in pair order, then the reference's test order).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/yarnsim.h"
+#include "ys_bvh.h"
+#include "ys_collide.cuh"
+
+extern "C" ys_status ys_internal_fail(ys_status s, const char* msg);
+
+namespace {
+
+using ys::CFace;
+using ys::CMesh;
+using ys::Impact;
+using ys::Kdop;
+
+constexpr int kStack = 64;  // traversal stack; deeper trees report an error
+
+#define YC_CUDA(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) return ys_internal_fail(YS_ERR_CUDA, cudaGetErrorString(e_)); \
+  } while (0)
+
+struct DevTree {
+  const int* left;
+  const int* right;
+  const int* face;
+  Kdop* box;
+  int nnodes;
+};
+
+// boxes of the tree nodes at one depth: leaves from their face's nodes,
+// inner nodes as the union of their children (BVHNode::refit, src/BVH.cpp:150-160)
+__global__ void k_refit(DevTree t, const int* __restrict__ level_nodes, int count, const CFace* __restrict__ faces,
+                        CMesh m, int ccd) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int n = level_nodes[i];
+  const int f = t.face[n];
+  Kdop b;
+  if (f >= 0) {
+    const CFace& fc = faces[f];
+    ys::kdop_node(b, ys::cc_pos(m, fc.v[0], false), ys::cc_pos(m, fc.v[0], true), ccd != 0);
+    for (int k = 1; k < 3; ++k) {
+      Kdop nb;
+      ys::kdop_node(nb, ys::cc_pos(m, fc.v[k], false), ys::cc_pos(m, fc.v[k], true), ccd != 0);
+      ys::kdop_add(b, nb);
+    }
+  } else {
+    b = t.box[t.left[n]];
+    ys::kdop_add(b, t.box[t.right[n]]);
+  }
+  t.box[n] = b;
+}
+
+struct BroadArgs {
+  DevTree cloth, obs;
+  const int* leaf_of_face;
+  const int* rank;
+  const int* upper;
+  int nfaces;
+  double thickness;
+  const int64_t* offset;  // write pass: first slot of each face
+  int* out;               // write pass: [P][3]
+  int64_t* count;         // count pass: pairs of each face
+  int* overflow;
+};
+
+// the pairs whose first face is f: cloth faces g the reference reports with
+// f first, then obstacle faces
+template <bool WRITE>
+__global__ void k_broad(BroadArgs a) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= a.nfaces) return;
+  const Kdop bf = a.cloth.box[a.leaf_of_face[f]];
+  const int uf = a.upper[f], rf = a.rank[f];
+  int64_t c = 0, o = WRITE ? a.offset[f] : 0;
+  int stack[kStack];
+  for (int pass = 0; pass < 2; ++pass) {
+    const DevTree& t = pass == 0 ? a.cloth : a.obs;
+    if (t.nnodes == 0) continue;
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+      const int n = stack[--sp];
+      const int g = t.face[n];
+      if (g >= 0) {
+        if (pass == 0) {
+          if (g == f || !ys::bvh_first(uf, rf, a.upper[g], a.rank[g])) continue;
+        }
+        if (!ys::kdop_overlap(bf, t.box[n], a.thickness)) continue;
+        if (WRITE) {
+          a.out[3 * (o + c)] = f;
+          a.out[3 * (o + c) + 1] = g;
+          a.out[3 * (o + c) + 2] = pass;
+        }
+        ++c;
+      } else {
+        if (!ys::kdop_overlap_loose(bf, t.box[n], a.thickness)) continue;
+        if (sp + 2 > kStack) {
+          atomicOr(a.overflow, 1);
+          continue;
+        }
+        stack[sp++] = t.right[n];
+        stack[sp++] = t.left[n];
+      }
+    }
+  }
+  if (!WRITE) a.count[f] = c;
+}
+
+__global__ void k_narrow(const int* __restrict__ pairs, int64_t npairs, const CFace* __restrict__ faces,
+                         const CFace* __restrict__ ofaces, CMesh m, double thickness, int ccd, Impact* slots,
+                         int64_t* count) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npairs) return;
+  const CFace& f0 = faces[pairs[3 * p]];
+  const CFace& f1 = pairs[3 * p + 2] ? ofaces[pairs[3 * p + 1]] : faces[pairs[3 * p + 1]];
+  count[p] = ys::cc_face_pair(m, f0, f1, thickness, ccd != 0, slots + 15 * p);
+}
+
+__global__ void k_compact(const Impact* __restrict__ slots, const int64_t* __restrict__ count,
+                          const int64_t* __restrict__ offset, int64_t npairs, ys_impact* out) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npairs) return;
+  for (int k = 0; k < count[p]; ++k) {
+    const Impact& s = slots[15 * p + k];
+    ys_impact& r = out[offset[p] + k];
+    r.type = s.type;
+    for (int q = 0; q < 4; ++q) r.nodes[q] = s.node[q];
+    r.t = s.t;
+    for (int q = 0; q < 4; ++q) r.w[q] = s.w[q];
+    for (int q = 0; q < 3; ++q) r.n[q] = s.n[q];
+    r.pair = p;
+  }
+}
+
+// exclusive scan of counts[n] into offset[n] (+ total), in fixed order
+constexpr int kScanChunk = 1024;
+__global__ void k_scan_chunks(const int64_t* __restrict__ c, int64_t n, int64_t* __restrict__ off,
+                              int64_t* __restrict__ sums) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t lo = b * kScanChunk;
+  if (lo >= n) return;
+  const int64_t hi = lo + kScanChunk < n ? lo + kScanChunk : n;
+  int64_t s = 0;
+  for (int64_t i = lo; i < hi; ++i) {
+    off[i] = s;
+    s += c[i];
+  }
+  sums[b] = s;
+}
+__global__ void k_scan_sums(int64_t* sums, int64_t nb, int64_t* total) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  int64_t s = 0;
+  for (int64_t i = 0; i < nb; ++i) {
+    const int64_t v = sums[i];
+    sums[i] = s;
+    s += v;
+  }
+  *total = s;
+}
+__global__ void k_scan_add(int64_t* off, int64_t n, const int64_t* __restrict__ sums) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) off[i] += sums[i / kScanChunk];
+}
+
+template <class T>
+struct DVec {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t reserve(size_t cnt) {
+    if (cnt <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(cnt, 1) * sizeof(T));
+    if (e == cudaSuccess) n = std::max<size_t>(cnt, 1);
+    return e;
+  }
+  ~DVec() {
+    if (p) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+struct ys_collider {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int n_nodes = 0, n_faces = 0, n_obs_nodes = 0, n_obs_faces = 0;
+  double thickness = 5e-4;
+  int ccd = 1;
+  std::vector<int> fv, ofv;  // face node ids (host, obstacle ids local)
+  DVec<CFace> faces, ofaces;
+  DVec<double> x, xp, ox, oxp;
+  std::vector<double> hx, hxp, hox, hoxp;  // host copies for the tree builds
+  // trees
+  ys::BvhTree ct, ot;
+  DVec<int> c_left, c_right, c_face, c_lof, c_rank, c_upper, c_levels, o_left, o_right, o_face, o_levels;
+  DVec<Kdop> c_box, o_box;
+  std::vector<int> c_level_off, o_level_off;  // level l nodes at [off[l], off[l+1])
+  // outputs
+  DVec<int64_t> counts, offsets, sums, total;
+  DVec<int> pairs;
+  int64_t npairs = 0;
+  DVec<Impact> slots;
+  DVec<int64_t> icount, ioffset;
+  DVec<ys_impact> impacts;
+  int64_t nimpacts = 0;
+  DVec<int> overflow;
+  bool have_pairs = false, have_impacts = false;
+};
+
+namespace {
+
+ys_status upload_tree(ys_collider* c, const ys::BvhTree& t, DVec<int>& l, DVec<int>& r, DVec<int>& f,
+                      DVec<int>& levels, DVec<Kdop>& box, std::vector<int>& level_off) {
+  const size_t nn = t.face.size();
+  YC_CUDA(l.reserve(nn));
+  YC_CUDA(r.reserve(nn));
+  YC_CUDA(f.reserve(nn));
+  YC_CUDA(box.reserve(nn));
+  YC_CUDA(levels.reserve(nn));
+  std::vector<int> lv;
+  level_off.assign(t.max_depth + 2, 0);
+  for (size_t n = 0; n < nn; ++n) level_off[t.depth[n] + 1]++;
+  for (int d = 0; d <= t.max_depth; ++d) level_off[d + 1] += level_off[d];
+  lv.resize(nn);
+  std::vector<int> fill(level_off.begin(), level_off.end() - 1);
+  for (size_t n = 0; n < nn; ++n) lv[fill[t.depth[n]]++] = (int)n;
+  if (nn) {
+    YC_CUDA(cudaMemcpyAsync(l.p, t.left.data(), nn * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    YC_CUDA(cudaMemcpyAsync(r.p, t.right.data(), nn * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    YC_CUDA(cudaMemcpyAsync(f.p, t.face.data(), nn * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    YC_CUDA(cudaMemcpyAsync(levels.p, lv.data(), nn * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    YC_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  return YS_OK;
+}
+
+ys_status refit(ys_collider* c, bool obstacle) {
+  const ys::BvhTree& t = obstacle ? c->ot : c->ct;
+  if (t.face.empty()) return YS_OK;
+  DevTree dt{obstacle ? c->o_left.p : c->c_left.p, obstacle ? c->o_right.p : c->c_right.p,
+             obstacle ? c->o_face.p : c->c_face.p, obstacle ? c->o_box.p : c->c_box.p, (int)t.face.size()};
+  const std::vector<int>& off = obstacle ? c->o_level_off : c->c_level_off;
+  const int* lv = obstacle ? c->o_levels.p : c->c_levels.p;
+  CMesh m{c->x.p, c->xp.p, c->ox.p, c->oxp.p};
+  for (int d = t.max_depth; d >= 0; --d) {
+    const int cnt = off[d + 1] - off[d];
+    if (cnt) k_refit<<<(cnt + 127) / 128, 128, 0, c->stream>>>(dt, lv + off[d], cnt, obstacle ? c->ofaces.p : c->faces.p,
+                                                               m, c->ccd);
+  }
+  YC_CUDA(cudaGetLastError());
+  return YS_OK;
+}
+
+ys_status scan(ys_collider* c, const int64_t* counts, int64_t n, int64_t* off, int64_t* total_host) {
+  const int64_t nb = (n + kScanChunk - 1) / kScanChunk;
+  YC_CUDA(c->sums.reserve(std::max<int64_t>(nb, 1)));
+  YC_CUDA(c->total.reserve(1));
+  if (n > 0) {
+    k_scan_chunks<<<(unsigned)((nb + 127) / 128), 128, 0, c->stream>>>(counts, n, off, c->sums.p);
+    k_scan_sums<<<1, 1, 0, c->stream>>>(c->sums.p, nb, c->total.p);
+    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(off, n, c->sums.p);
+    YC_CUDA(cudaGetLastError());
+    YC_CUDA(cudaMemcpyAsync(total_host, c->total.p, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    *total_host = 0;
+  }
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  return YS_OK;
+}
+
+void edges_of(const int* fv, int f, int e[3][2], bool obstacle, const std::vector<int>* ofv) {
+  (void)ofv;
+  for (int a = 0; a < 3; ++a) {
+    const int b = a != 2 ? a + 1 : 0;
+    e[a][0] = fv[3 * f + a];
+    e[a][1] = fv[3 * f + b];
+    if (obstacle && e[a][0] > e[a][1]) std::swap(e[a][0], e[a][1]);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+ys_status ys_cloth_mesh_topology(int32_t width, int32_t length, int32_t* faces, int32_t* face_edges) {
+  if (width < 2 || length < 2 || !faces) return ys_internal_fail(YS_ERR_ARG, "bad cloth mesh size");
+  // mesh faces of Cloth::build (src/Cloth.cpp:271-294): cell (i, j), i outer,
+  // faces (tl, tr, br) and (tl, br, bl); mesh edges along warp and weft point
+  // to the higher u / v, the cell diagonal from tl to br
+  int f = 0;
+  for (int i = 0; i < width - 1; ++i)
+    for (int j = 0; j < length - 1; ++j) {
+      const int tl = i + j * width, tr = tl + 1, bl = tl + width, br = bl + 1;
+      const int tri[2][3] = {{tl, tr, br}, {tl, br, bl}};
+      for (int q = 0; q < 2; ++q, ++f) {
+        for (int k = 0; k < 3; ++k) faces[3 * f + k] = tri[q][k];
+        if (!face_edges) continue;
+        for (int a = 0; a < 3; ++a) {
+          const int b = a != 2 ? a + 1 : 0;
+          int u0 = tri[q][a], u1 = tri[q][b];
+          if (u0 > u1) std::swap(u0, u1);  // every cloth mesh edge runs from its lower node
+          face_edges[6 * f + 2 * a] = u0;
+          face_edges[6 * f + 2 * a + 1] = u1;
+        }
+      }
+    }
+  return YS_OK;
+}
+
+ys_status ys_collider_create(int32_t n_nodes, int32_t n_faces, const int32_t* faces, const int32_t* face_edges,
+                             int32_t n_obs_nodes, int32_t n_obs_faces, const int32_t* obs_faces, double thickness,
+                             int32_t ccd, int32_t device, void* cuda_stream, ys_collider** out) {
+  if (!out || n_nodes <= 0 || n_faces <= 0 || !faces || !face_edges || n_obs_nodes < 0 || n_obs_faces < 0 ||
+      (n_obs_faces > 0 && !obs_faces))
+    return ys_internal_fail(YS_ERR_ARG, "bad collider arguments");
+  for (int i = 0; i < 3 * n_faces; ++i)
+    if (faces[i] < 0 || faces[i] >= n_nodes) return ys_internal_fail(YS_ERR_ARG, "cloth face node out of range");
+  for (int i = 0; i < 3 * n_obs_faces; ++i)
+    if (obs_faces[i] < 0 || obs_faces[i] >= n_obs_nodes)
+      return ys_internal_fail(YS_ERR_ARG, "obstacle face node out of range");
+  YC_CUDA(cudaSetDevice(device));
+  ys_collider* c = new ys_collider();
+  c->device = device;
+  c->stream = static_cast<cudaStream_t>(cuda_stream);
+  c->n_nodes = n_nodes;
+  c->n_faces = n_faces;
+  c->n_obs_nodes = n_obs_nodes;
+  c->n_obs_faces = n_obs_faces;
+  c->thickness = thickness;
+  c->ccd = ccd ? 1 : 0;
+  c->fv.assign(faces, faces + 3 * n_faces);
+  c->ofv.assign(obs_faces, obs_faces + 3 * (size_t)n_obs_faces);
+  std::vector<CFace> hf(n_faces), ho(n_obs_faces);
+  for (int f = 0; f < n_faces; ++f)
+    for (int k = 0; k < 3; ++k) {
+      hf[f].v[k] = faces[3 * f + k];
+      hf[f].e[k][0] = face_edges[6 * f + 2 * k];
+      hf[f].e[k][1] = face_edges[6 * f + 2 * k + 1];
+    }
+  // obstacle meshes as load_obj builds them (src/Loader.cpp:317-340): edges
+  // run from the lower node id; node ids are stored as -1 - id
+  for (int f = 0; f < n_obs_faces; ++f) {
+    int e[3][2];
+    edges_of(obs_faces, f, e, true, nullptr);
+    for (int k = 0; k < 3; ++k) {
+      ho[f].v[k] = -1 - obs_faces[3 * f + k];
+      ho[f].e[k][0] = -1 - e[k][0];
+      ho[f].e[k][1] = -1 - e[k][1];
+    }
+  }
+  auto cleanup = [&](ys_status s) {
+    delete c;
+    return s;
+  };
+  if (c->faces.reserve(n_faces) != cudaSuccess || c->ofaces.reserve(n_obs_faces) != cudaSuccess ||
+      c->x.reserve(3 * (size_t)n_nodes) != cudaSuccess || c->xp.reserve(3 * (size_t)n_nodes) != cudaSuccess ||
+      c->ox.reserve(3 * (size_t)n_obs_nodes) != cudaSuccess || c->oxp.reserve(3 * (size_t)n_obs_nodes) != cudaSuccess ||
+      c->overflow.reserve(1) != cudaSuccess || c->counts.reserve(n_faces) != cudaSuccess ||
+      c->offsets.reserve(n_faces) != cudaSuccess || c->c_lof.reserve(n_faces) != cudaSuccess ||
+      c->c_rank.reserve(n_faces) != cudaSuccess || c->c_upper.reserve(n_faces) != cudaSuccess)
+    return cleanup(ys_internal_fail(YS_ERR_CUDA, "cudaMalloc failed"));
+  if (cudaMemcpy(c->faces.p, hf.data(), sizeof(CFace) * n_faces, cudaMemcpyHostToDevice) != cudaSuccess ||
+      (n_obs_faces && cudaMemcpy(c->ofaces.p, ho.data(), sizeof(CFace) * n_obs_faces, cudaMemcpyHostToDevice) !=
+                          cudaSuccess))
+    return cleanup(ys_internal_fail(YS_ERR_CUDA, "cudaMemcpy failed"));
+  *out = c;
+  return YS_OK;
+}
+
+void ys_collider_destroy(ys_collider* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  delete c;
+}
+
+ys_status ys_collider_set_positions(ys_collider* c, const double* x, const double* x_prev, const double* obs_x,
+                                    const double* obs_x_prev, int32_t flags) {
+  if (!c || !x || !x_prev || (c->n_obs_nodes > 0 && (!obs_x || !obs_x_prev)))
+    return ys_internal_fail(YS_ERR_ARG, "bad collider positions");
+  YC_CUDA(cudaSetDevice(c->device));
+  const size_t n3 = 3 * (size_t)c->n_nodes, o3 = 3 * (size_t)c->n_obs_nodes;
+  c->hx.resize(n3);
+  c->hxp.resize(n3);
+  c->hox.resize(o3);
+  c->hoxp.resize(o3);
+  const cudaMemcpyKind kind = (flags & YS_ON_DEVICE) ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
+  YC_CUDA(cudaMemcpy(c->hx.data(), x, n3 * sizeof(double), kind));
+  YC_CUDA(cudaMemcpy(c->hxp.data(), x_prev, n3 * sizeof(double), kind));
+  if (o3) {
+    YC_CUDA(cudaMemcpy(c->hox.data(), obs_x, o3 * sizeof(double), kind));
+    YC_CUDA(cudaMemcpy(c->hoxp.data(), obs_x_prev, o3 * sizeof(double), kind));
+  }
+  YC_CUDA(cudaMemcpyAsync(c->x.p, c->hx.data(), n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  YC_CUDA(cudaMemcpyAsync(c->xp.p, c->hxp.data(), n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (o3) {
+    YC_CUDA(cudaMemcpyAsync(c->ox.p, c->hox.data(), o3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    YC_CUDA(cudaMemcpyAsync(c->oxp.p, c->hoxp.data(), o3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  }
+  // the trees of a fresh AccelStruct (src/CollisionUtil.cpp:3-9): rebuilt
+  // from these positions, as Collision::collision_response does every call
+  std::vector<int> verts(c->n_nodes);
+  for (int i = 0; i < c->n_nodes; ++i) verts[i] = i;
+  c->ct = ys::bvh_build(c->n_faces, c->fv.data(), c->n_nodes, verts.data(), c->hx.data(), c->hxp.data(), c->ccd != 0);
+  std::vector<int> overts(c->n_obs_nodes);
+  for (int i = 0; i < c->n_obs_nodes; ++i) overts[i] = i;
+  c->ot = ys::bvh_build(c->n_obs_faces, c->ofv.data(), c->n_obs_nodes, overts.data(), c->hox.data(), c->hoxp.data(),
+                        c->ccd != 0);
+  ys_status s;
+  if ((s = upload_tree(c, c->ct, c->c_left, c->c_right, c->c_face, c->c_levels, c->c_box, c->c_level_off)) != YS_OK)
+    return s;
+  if ((s = upload_tree(c, c->ot, c->o_left, c->o_right, c->o_face, c->o_levels, c->o_box, c->o_level_off)) != YS_OK)
+    return s;
+  YC_CUDA(cudaMemcpyAsync(c->c_lof.p, c->ct.leaf_of_face.data(), sizeof(int) * c->n_faces, cudaMemcpyHostToDevice,
+                          c->stream));
+  YC_CUDA(cudaMemcpyAsync(c->c_rank.p, c->ct.rank.data(), sizeof(int) * c->n_faces, cudaMemcpyHostToDevice, c->stream));
+  YC_CUDA(cudaMemcpyAsync(c->c_upper.p, c->ct.upper.data(), sizeof(int) * c->n_faces, cudaMemcpyHostToDevice,
+                          c->stream));
+  if ((s = refit(c, false)) != YS_OK) return s;
+  if ((s = refit(c, true)) != YS_OK) return s;
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  c->have_pairs = c->have_impacts = false;
+  return YS_OK;
+}
+
+ys_status ys_collider_find_pairs(ys_collider* c, int64_t* n_pairs) {
+  if (!c || c->ct.face.empty()) return ys_internal_fail(YS_ERR_ARG, "ys_collider_find_pairs before set_positions");
+  YC_CUDA(cudaSetDevice(c->device));
+  BroadArgs a{};
+  a.cloth = DevTree{c->c_left.p, c->c_right.p, c->c_face.p, c->c_box.p, (int)c->ct.face.size()};
+  a.obs = DevTree{c->o_left.p, c->o_right.p, c->o_face.p, c->o_box.p, (int)c->ot.face.size()};
+  a.leaf_of_face = c->c_lof.p;
+  a.rank = c->c_rank.p;
+  a.upper = c->c_upper.p;
+  a.nfaces = c->n_faces;
+  a.thickness = c->thickness;
+  a.count = c->counts.p;
+  a.overflow = c->overflow.p;
+  YC_CUDA(cudaMemsetAsync(c->overflow.p, 0, sizeof(int), c->stream));
+  const unsigned g = (unsigned)((c->n_faces + 127) / 128);
+  k_broad<false><<<g, 128, 0, c->stream>>>(a);
+  YC_CUDA(cudaGetLastError());
+  ys_status s = scan(c, c->counts.p, c->n_faces, c->offsets.p, &c->npairs);
+  if (s != YS_OK) return s;
+  int ovf = 0;
+  YC_CUDA(cudaMemcpy(&ovf, c->overflow.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (ovf) return ys_internal_fail(YS_ERR_ARG, "BVH deeper than the traversal stack");
+  YC_CUDA(c->pairs.reserve(3 * (size_t)std::max<int64_t>(c->npairs, 1)));
+  a.offset = c->offsets.p;
+  a.out = c->pairs.p;
+  k_broad<true><<<g, 128, 0, c->stream>>>(a);
+  YC_CUDA(cudaGetLastError());
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  c->have_pairs = true;
+  c->have_impacts = false;
+  if (n_pairs) *n_pairs = c->npairs;
+  return YS_OK;
+}
+
+ys_status ys_collider_get_pairs(ys_collider* c, int32_t* pairs, int64_t cap) {
+  if (!c || !c->have_pairs) return ys_internal_fail(YS_ERR_ARG, "no pairs found yet");
+  if (cap < c->npairs) return ys_internal_fail(YS_ERR_ARG, "pair buffer too small");
+  YC_CUDA(cudaSetDevice(c->device));
+  if (c->npairs)
+    YC_CUDA(cudaMemcpy(pairs, c->pairs.p, sizeof(int) * 3 * c->npairs, cudaMemcpyDeviceToHost));
+  return YS_OK;
+}
+
+ys_status ys_collider_find_impacts(ys_collider* c, int64_t* n_impacts) {
+  if (!c || !c->have_pairs) return ys_internal_fail(YS_ERR_ARG, "ys_collider_find_impacts before find_pairs");
+  YC_CUDA(cudaSetDevice(c->device));
+  const int64_t P = c->npairs;
+  YC_CUDA(c->slots.reserve(15 * (size_t)std::max<int64_t>(P, 1)));
+  YC_CUDA(c->icount.reserve(std::max<int64_t>(P, 1)));
+  YC_CUDA(c->ioffset.reserve(std::max<int64_t>(P, 1)));
+  CMesh m{c->x.p, c->xp.p, c->ox.p, c->oxp.p};
+  if (P) {
+    k_narrow<<<(unsigned)((P + 127) / 128), 128, 0, c->stream>>>(c->pairs.p, P, c->faces.p, c->ofaces.p, m,
+                                                                  c->thickness, c->ccd, c->slots.p, c->icount.p);
+    YC_CUDA(cudaGetLastError());
+  }
+  ys_status s = scan(c, c->icount.p, P, c->ioffset.p, &c->nimpacts);
+  if (s != YS_OK) return s;
+  YC_CUDA(c->impacts.reserve(std::max<int64_t>(c->nimpacts, 1)));
+  if (P) {
+    k_compact<<<(unsigned)((P + 127) / 128), 128, 0, c->stream>>>(c->slots.p, c->icount.p, c->ioffset.p, P,
+                                                                   c->impacts.p);
+    YC_CUDA(cudaGetLastError());
+  }
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  c->have_impacts = true;
+  if (n_impacts) *n_impacts = c->nimpacts;
+  return YS_OK;
+}
+
+ys_status ys_collider_get_impacts(ys_collider* c, ys_impact* impacts, int64_t cap) {
+  if (!c || !c->have_impacts) return ys_internal_fail(YS_ERR_ARG, "no impacts found yet");
+  if (cap < c->nimpacts) return ys_internal_fail(YS_ERR_ARG, "impact buffer too small");
+  YC_CUDA(cudaSetDevice(c->device));
+  if (c->nimpacts)
+    YC_CUDA(cudaMemcpy(impacts, c->impacts.p, sizeof(ys_impact) * c->nimpacts, cudaMemcpyDeviceToHost));
+  return YS_OK;
+}
+
+}  // extern "C"

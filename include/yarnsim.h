@@ -207,6 +207,47 @@ ys_status ys_profile(ys_batch *b, int32_t enable);
 ys_status ys_profile_read(ys_batch *b, double *ms, int64_t *launches_per_kind, int64_t *total_launches,
                           int32_t reset);
 
+/* ---- Continuous collision detection (broad + narrow phase).
+ * Replaces Collision::find_impacts (src/Collision.cpp:184-208) over the
+ * cloth mesh and one obstacle mesh: the reference's BVH over 18-DOP CCD
+ * boxes (src/BVH.cpp, src/CollisionUtil.cpp:3-9), its traversal
+ * (src/Collision.cpp:266-326) and comp_face_impacts' vertex-face and
+ * edge-edge tests (src/Collision.cpp:210-253, 327-419). The pair list equals
+ * the reference's as a set, each pair oriented as the reference reports it;
+ * the order is face-major (the reference's depends on its OpenMP threads). */
+typedef struct ys_collider ys_collider;
+typedef struct {
+  int32_t type;      /* 0 vertex-face, 1 edge-edge */
+  int32_t nodes[4];  /* cloth node id, or -1 - id for an obstacle node */
+  double t;          /* time of coplanarity in [0, 1] of the step */
+  double w[4];       /* barycentric weights (Impact::ws) */
+  double n[3];       /* contact normal */
+  int64_t pair;      /* index of the face pair in the pair list */
+} ys_impact;
+/* Faces [(W-1)(L-1)*2][3] of a W x L cloth's mesh in the reference's order
+ * (src/Cloth.cpp:271-294) and their edges [F][3][2] (edge k joins face nodes
+ * k and k+1, oriented as the reference's mesh edges; NULL to skip). */
+ys_status ys_cloth_mesh_topology(int32_t width, int32_t length, int32_t *faces, int32_t *face_edges);
+/* A collider for a cloth mesh (node ids 0..n_nodes-1) and an obstacle mesh
+ * (n_obs_faces may be 0); thickness dilates the boxes (src/BVH.cpp:268-286);
+ * ccd = 1: boxes span both positions of the step. */
+ys_status ys_collider_create(int32_t n_nodes, int32_t n_faces, const int32_t *faces, const int32_t *face_edges,
+                             int32_t n_obs_nodes, int32_t n_obs_faces, const int32_t *obs_faces, double thickness,
+                             int32_t ccd, int32_t device, void *cuda_stream, ys_collider **out);
+void ys_collider_destroy(ys_collider *c);
+/* Positions at the end (x) and start (x_prev) of the step, [n][3] each (host,
+ * or device with YS_ON_DEVICE); rebuilds both trees as the reference does for
+ * every collision_response call. */
+ys_status ys_collider_set_positions(ys_collider *c, const double *x, const double *x_prev, const double *obs_x,
+                                    const double *obs_x_prev, int32_t flags);
+/* Broad phase; n_pairs receives the count. */
+ys_status ys_collider_find_pairs(ys_collider *c, int64_t *n_pairs);
+/* pairs [n_pairs][3]: first face, second face, 1 if the second is an obstacle face. */
+ys_status ys_collider_get_pairs(ys_collider *c, int32_t *pairs, int64_t cap);
+/* Narrow phase over the pair list; n_impacts receives the count. */
+ys_status ys_collider_find_impacts(ys_collider *c, int64_t *n_impacts);
+ys_status ys_collider_get_impacts(ys_collider *c, ys_impact *impacts, int64_t cap);
+
 #ifdef __cplusplus
 }
 #endif

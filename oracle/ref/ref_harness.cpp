@@ -15,7 +15,10 @@
 //
 // Usage: ref_harness <config-file>
 // Config: key=value lines (see tests/golden/make_golden.py for the keys).
+#include <array>
+#include <cmath>
 #include <cstdio>
+#include <set>
 #include <cstdlib>
 #include <fstream>
 #include <map>
@@ -24,6 +27,7 @@
 #include <vector>
 
 #include "PhysicsCloth.h"
+#include "CollisionUtil.h"
 
 void ref_cg_set_options(double tol, long max_iter);
 long ref_cg_last_iterations();
@@ -325,6 +329,288 @@ int run_vjp(std::map<std::string, std::string>& kv) {
   return 0;
 }
 
+
+// ---------------------------------------------------------------------------
+// mode=collide: the broad and narrow phase of the reference's collision
+// detection on one cloth state, for golden pair lists and impacts.
+// The BVH is the reference's own (src/BVH.cpp, src/CollisionUtil.cpp:3-9:
+// AccelStruct = BVHTree(ccd, mesh) over the cloth mesh and the obstacle
+// mesh); the traversal restates Collision::for_overlapping_faces and
+// collect_upper_nodes (src/Collision.cpp:266-326) and the narrow phase
+// comp_face_impacts / vf / ee / collision_test (src/Collision.cpp:210-253,
+// 327-419) with the reference's Geometry.cpp, and the cubic solve restates
+// src/Solvers.cpp:60-178 (Solvers.cpp needs Eigen). The obstacle mesh is
+// built as load_obj builds it (src/Loader.cpp:269-345; Loader.cpp needs HDF5).
+// Inputs: cloth width/length (the reference's clothMesh topology) with node
+// positions x / x_prev from "cloth_state" ([N][3] x then [N][3] x_prev), an
+// optional obstacle from "obstacle" ([No] count, [No][3] x, [No][3] x_prev,
+// [Fo] count, [Fo][3] node ids, as doubles), thickness, ccd.
+// Writes "pairs" [P][3] (first face, second face, 1 if the second face is an
+// obstacle face) in emission order and "impacts" [I][15] (type 0 VF / 1 EE,
+// four node ids (obstacle nodes as -1 - id), t, ws[4], n[3], pair index).
+namespace collide {
+
+int quad(double a, double b, double c, double& x0, double& x1) {
+  const double d = b * b - 4.0 * a * c;
+  if (d < 0.0) {
+    x0 = -b / (2.0 * a);
+    return 0;
+  }
+  const double q = -(b + std::sqrt(d)) / 2.0, q1 = -(b - std::sqrt(d)) / 2.0;
+  if (std::fabs(a) > 1e-12) {
+    if (q / a < q1 / a) { x0 = q / a; x1 = q1 / a; }
+    else { x0 = q1 / a; x1 = q / a; }
+    return 2;
+  }
+  x0 = -c / b;
+  return 1;
+}
+double newton(double a, double b, double c, double d, double x0, int dir) {
+  if (dir != 0) {
+    const double y0 = d + x0 * (c + x0 * (b + x0 * a)), ddy0 = 2 * b + (x0 + dir * 1e-6) * (6 * a);
+    x0 = x0 + dir * std::sqrt(std::fabs(2 * y0 / ddy0));
+  }
+  for (int it = 0; it < 100; ++it) {
+    const double y = d + x0 * (c + x0 * (b + x0 * a)), dy = c + x0 * (2 * b + x0 * 3 * a);
+    if (dy == 0.0) return x0;
+    const double x1 = x0 - y / dy;
+    if (std::fabs(x0 - x1) < 1e-6) return x0;
+    x0 = x1;
+  }
+  return x0;
+}
+std::vector<double> cubic(double a, double b, double c, double d) {
+  double xc0 = -1.0, xc1 = -1.0, x0 = -1.0, x1 = -1.0, x2 = -1.0;
+  const int ncrit = quad(3.0 * a, 2.0 * b, c, xc0, xc1);
+  if (ncrit == 0) return {newton(a, b, c, d, xc0, 0)};
+  if (ncrit == 1) {
+    const int ns = quad(b, c, d, x0, x1);
+    if (ns == 1) return {x0};
+    if (ns == 2) return {x0, x1};
+    return {};
+  }
+  const double yc0 = d + xc0 * (c + xc0 * (b + xc0 * a)), yc1 = d + xc1 * (c + xc1 * (b + xc1 * a));
+  int ns = 0;
+  if (yc0 * a >= 0.0) { x0 = newton(a, b, c, d, xc0, -1); ns++; }
+  if (yc0 * yc1 <= 0.0) {
+    if (std::fabs(yc0) < std::fabs(yc1)) x1 = newton(a, b, c, d, xc0, 1);
+    else x1 = newton(a, b, c, d, xc1, -1);
+    ns++;
+  }
+  if (yc1 * a <= 0.0) { x2 = newton(a, b, c, d, xc1, 1); ns++; }
+  if (ns == 1) return {x0};
+  if (ns == 2) return {x0, x1};
+  if (ns == 3) return {x0, x1, x2};
+  return {};
+}
+
+struct Ctx {
+  Mesh* cloth;
+  Mesh* obs;
+  Tensor thickness;
+  bool ccd;
+  std::vector<std::array<double, 3>> pairs;
+  std::vector<std::array<double, 15>> impacts;
+};
+
+double node_id(Ctx& c, const MeshNode* n) {
+  if (n->index < (int)c.cloth->nodes.size() && n == &c.cloth->nodes.at(n->index)) return n->index;
+  return -1.0 - n->index;
+}
+
+bool test(Ctx& c, int type, const MeshNode* n0, const MeshNode* n1, const MeshNode* n2, const MeshNode* n3, int pair) {
+  Tensor x0 = n0->x_prev, v0 = n0->x - x0;
+  Tensor x1 = n1->x_prev - x0, x2 = n2->x_prev - x0, x3 = n3->x_prev - x0;
+  Tensor v1 = n1->x - n1->x_prev - v0, v2 = n2->x - n2->x_prev - v0, v3 = n3->x - n3->x_prev - v0;
+  auto dotc = [](const Tensor& a, const Tensor& b, const Tensor& cc) {
+    return torch::mm(a.transpose(0, 1), torch::cross(b, cc)).item<double>();
+  };
+  const double a0 = dotc(x1, x2, x3);
+  const double a1 = dotc(v1, x2, x3) + dotc(x1, v2, x3) + dotc(x1, x2, v3);
+  const double a2 = dotc(x1, v2, v3) + dotc(v1, x2, v3) + dotc(v1, v2, x3);
+  const double a3 = dotc(v1, v2, v3);
+  for (double t : cubic(a3, a2, a1, a0)) {
+    if (std::isnan(t) || std::isinf(t) || t < 0 || t > 1) continue;
+    Tensor tt = torch::tensor({t}, opts);
+    Tensor bx1 = x1 + tt * v1, bx2 = x2 + tt * v2, bx3 = x3 + tt * v3;
+    Tensor n;
+    std::array<Tensor, 4> ws;
+    bool over = false, inside = false;
+    if (type == 0) {
+      sub_signed_vf_distance(bx1, bx2, bx3, n, ws, 1e-12, over);
+      inside = std::min(-ws[1].item<double>(), std::min(-ws[2].item<double>(), -ws[3].item<double>())) >= -1e-12;
+    } else {
+      sub_signed_ee_distance(bx1, bx2, bx3, bx2 - bx1, bx3 - bx1, bx3 - bx2, n, ws, 1e-12, over);
+      inside = std::min(std::min(ws[0].item<double>(), ws[1].item<double>()),
+                        std::min(-ws[2].item<double>(), -ws[3].item<double>())) >= -1e-12;
+    }
+    if (over || !inside) continue;
+    if (torch::dot(n.squeeze(), (ws[1] * v1 + ws[2] * v2 + ws[3] * v3).squeeze()).item<double>() > 0.0) n = -1 * n;
+    std::array<double, 15> r;
+    r[0] = type;
+    r[1] = node_id(c, n0); r[2] = node_id(c, n1); r[3] = node_id(c, n2); r[4] = node_id(c, n3);
+    r[5] = t;
+    for (int k = 0; k < 4; ++k) r[6 + k] = ws[k].item<double>();
+    for (int k = 0; k < 3; ++k) r[10 + k] = n[k][0].item<double>();
+    r[13] = pair;
+    r[14] = 0;
+    c.impacts.push_back(r);
+    return true;
+  }
+  return false;
+}
+
+void face_impacts(Ctx& c, MeshFace* f0, MeshFace* f1, int pair) {
+  std::array<kDOP18, 6> nb, eb;
+  std::array<kDOP18, 2> fb;
+  for (int n = 0; n < 3; ++n) {
+    nb[n] = node_box(f0->v[n]->node, c.ccd);
+    nb[n + 3] = node_box(f1->v[n]->node, c.ccd);
+  }
+  for (int a = 0; a < 3; ++a) {
+    const int b = a != 2 ? a + 1 : 0;
+    eb[a] = nb[a] + nb[b];
+    eb[a + 3] = nb[a + 3] + nb[b + 3];
+  }
+  fb[0] = nb[0] + nb[1] + nb[2];
+  fb[1] = nb[3] + nb[4] + nb[5];
+  auto vf = [&](const MeshVert* v, const MeshFace* f) {
+    const MeshNode* nd = v->node;
+    if (nd == f->v[0]->node || nd == f->v[1]->node || nd == f->v[2]->node) return;
+    test(c, 0, nd, f->v[0]->node, f->v[1]->node, f->v[2]->node, pair);
+  };
+  for (int n = 0; n < 3; ++n)
+    if (overlap(nb[n], fb[1], c.thickness)) vf(f0->v[n], f1);
+  for (int n = 0; n < 3; ++n)
+    if (overlap(nb[n + 3], fb[0], c.thickness)) vf(f1->v[n], f0);
+  for (int e0 = 0; e0 < 3; ++e0)
+    for (int e1 = 0; e1 < 3; ++e1) {
+      if (!overlap(eb[e0], eb[e1 + 3], c.thickness)) continue;
+      const MeshEdge* a = f0->adj_edges[e0];
+      const MeshEdge* b = f1->adj_edges[e1];
+      if (a->n0 == b->n0 || a->n0 == b->n1 || a->n1 == b->n0 || a->n1 == b->n1) continue;
+      test(c, 1, a->n0, a->n1, b->n0, b->n1, pair);
+    }
+}
+
+void emit(Ctx& c, MeshFace* f0, MeshFace* f1, bool obs) {
+  c.pairs.push_back({(double)f0->index, (double)f1->index, obs ? 1.0 : 0.0});
+}
+void pair_nodes(Ctx& c, BVHNode* a, BVHNode* b, bool obs) {
+  if (!a->_actived && !b->_actived) return;
+  if (!overlap(a->_box, b->_box, c.thickness)) return;
+  if (a->isLeaf() && b->isLeaf()) emit(c, a->_face, b->_face, obs);
+  else if (a->isLeaf()) {
+    pair_nodes(c, a, b->_left, obs);
+    pair_nodes(c, a, b->_right, obs);
+  } else {
+    pair_nodes(c, a->_left, b, obs);
+    pair_nodes(c, a->_right, b, obs);
+  }
+}
+void self_nodes(Ctx& c, BVHNode* n) {
+  if (n->isLeaf() || !n->_actived) return;
+  self_nodes(c, n->_left);
+  self_nodes(c, n->_right);
+  pair_nodes(c, n->_left, n->_right, false);
+}
+
+}  // namespace collide
+
+int run_collide(std::map<std::string, std::string>& kv) {
+  const int W = static_cast<int>(get_d(kv, "width", 5));
+  const int Lh = static_cast<int>(get_d(kv, "length", 5));
+  const double R = get_d(kv, "R", 1e-4);
+  std::vector<Yarn> yarns{Yarn{R, torch::tensor({1e-3}, opts), torch::tensor({1e3}, opts), torch::tensor({1e-5}, opts)}};
+  auto T1 = [&](double d) { return torch::tensor({d}, opts); };
+  Cloth cloth(W, Lh, 0.05, get_d(kv, "L", 1e-3), R, yarns, T1(1.0), T1(1000.0), T1(1000.0), T1(0.3), T1(1e-4), T1(1e4),
+              WovenPattern::Plain, InitPose::Flat);
+  const int N = W * Lh;
+  std::vector<double> st(6 * N);
+  {
+    std::ifstream f(kv["cloth_state"], std::ios::binary);
+    f.read(reinterpret_cast<char*>(st.data()), st.size() * sizeof(double));
+  }
+  for (int n = 0; n < N; ++n) {
+    MeshNode& m = cloth.clothMesh.nodes.at(n);
+    m.x = torch::tensor({st[3 * n], st[3 * n + 1], st[3 * n + 2]}, opts).view({3, 1});
+    m.x_prev = torch::tensor({st[3 * N + 3 * n], st[3 * N + 3 * n + 1], st[3 * N + 3 * n + 2]}, opts).view({3, 1});
+  }
+  Mesh obs;
+  const bool has_obs = kv.count("obstacle") > 0;
+  if (has_obs) {
+    std::ifstream f(kv["obstacle"], std::ios::binary);
+    double cnt;
+    f.read(reinterpret_cast<char*>(&cnt), sizeof(double));
+    const int No = (int)cnt;
+    std::vector<double> xo(3 * No), xp(3 * No);
+    f.read(reinterpret_cast<char*>(xo.data()), xo.size() * sizeof(double));
+    f.read(reinterpret_cast<char*>(xp.data()), xp.size() * sizeof(double));
+    f.read(reinterpret_cast<char*>(&cnt), sizeof(double));
+    const int Fo = (int)cnt;
+    std::vector<double> fo(3 * Fo);
+    f.read(reinterpret_cast<char*>(fo.data()), fo.size() * sizeof(double));
+    obs.nodes.reserve(No);
+    obs.verts.reserve(No);
+    for (int i = 0; i < No; ++i) {
+      MeshNode nd(torch::tensor({xo[3 * i], xo[3 * i + 1], xo[3 * i + 2]}, opts).view({3, 1}));
+      obs.add(nd);
+      obs.nodes.back().x_prev = torch::tensor({xp[3 * i], xp[3 * i + 1], xp[3 * i + 2]}, opts).view({3, 1});
+      obs.add(MeshVert(torch::zeros({2, 1}, opts)));
+    }
+    for (int i = 0; i < No; ++i) connect(&obs.verts.at(i), &obs.nodes.at(i));
+    std::set<std::pair<int, int>> en;
+    for (int q = 0; q < Fo; ++q)
+      for (int a = 0; a < 3; ++a) {
+        const int b = a != 2 ? a + 1 : 0;
+        const int u = (int)fo[3 * q + a], w = (int)fo[3 * q + b];
+        en.insert(u < w ? std::make_pair(u, w) : std::make_pair(w, u));
+      }
+    obs.edges.reserve(en.size());
+    for (auto& e : en) obs.add(MeshEdge(&obs.nodes.at(e.first), &obs.nodes.at(e.second)));
+    obs.faces.reserve(Fo);
+    for (int q = 0; q < Fo; ++q)
+      obs.add(MeshFace(&obs.verts.at((int)fo[3 * q]), &obs.verts.at((int)fo[3 * q + 1]), &obs.verts.at((int)fo[3 * q + 2])));
+    obs.add_adjecent();
+  }
+  collide::Ctx c{&cloth.clothMesh, &obs, torch::tensor({get_d(kv, "thickness", 5e-4)}, opts),
+                 get_d(kv, "ccd", 1) != 0, {}, {}};
+  AccelStruct cacc(cloth.clothMesh, c.ccd);
+  AccelStruct* oacc = has_obs ? new AccelStruct(obs, c.ccd) : nullptr;
+  // collect_upper_nodes (src/Collision.cpp:306-326) with NThrd nodes
+  std::vector<BVHNode*> nodes{cacc.root};
+  while ((int)nodes.size() < NThrd) {
+    std::vector<BVHNode*> ch;
+    for (BVHNode* n : nodes) {
+      if (n->isLeaf()) ch.push_back(n);
+      else { ch.push_back(n->_left); ch.push_back(n->_right); }
+    }
+    if (ch.size() == nodes.size()) break;
+    nodes = ch;
+  }
+  for (int n = 0; n < (int)nodes.size(); ++n) {
+    collide::self_nodes(c, nodes[n]);
+    for (int m = 0; m < n; ++m) collide::pair_nodes(c, nodes[n], nodes[m], false);
+    if (oacc) collide::pair_nodes(c, nodes[n], oacc->root, true);
+  }
+  for (int p = 0; p < (int)c.pairs.size(); ++p) {
+    MeshFace* f0 = &cloth.clothMesh.faces.at((int)c.pairs[p][0]);
+    MeshFace* f1 = c.pairs[p][2] != 0 ? &obs.faces.at((int)c.pairs[p][1]) : &cloth.clothMesh.faces.at((int)c.pairs[p][1]);
+    collide::face_impacts(c, f0, f1, p);
+  }
+  Writer w(get_s(kv, "out", "ref_out.bin"));
+  std::vector<double> pf;
+  for (auto& q : c.pairs) pf.insert(pf.end(), q.begin(), q.end());
+  w.put("pairs", {(long)c.pairs.size(), 3}, pf.data());
+  std::vector<double> im;
+  for (auto& q : c.impacts) im.insert(im.end(), q.begin(), q.end());
+  w.put("impacts", {(long)c.impacts.size(), 15}, im.data());
+  double stv = 0;
+  w.put("status", {1}, &stv);
+  delete oacc;
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) {
     std::fprintf(stderr, "usage: %s config\n", argv[0]);
@@ -334,6 +620,7 @@ int main(int argc, char** argv) {
   auto kv = read_config(argv[1]);
   if (get_s(kv, "mode", "") == "grad") return run_grad(kv);
   if (get_s(kv, "mode", "") == "vjp") return run_vjp(kv);
+  if (get_s(kv, "mode", "") == "collide") return run_collide(kv);
 
   const int W = static_cast<int>(get_d(kv, "width", 5));
   const int Lh = static_cast<int>(get_d(kv, "length", 5));

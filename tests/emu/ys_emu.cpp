@@ -13,6 +13,7 @@
 
 #include "../../include/yarnsim.h"
 #include "../../fine-grained-differentiable-physics-a-yarn-level-model-for-fabrics_gb300/csrc/ys_items.cuh"
+#include "../../fine-grained-differentiable-physics-a-yarn-level-model-for-fabrics_gb300/csrc/ys_bvh.h"
 
 namespace {
 
@@ -415,6 +416,142 @@ int emu_update(void* h) {
   if (e->bad) return 1;
   for (double s : e->SOL) if (!std::isfinite(s)) return 1;
   for (int n = 0; n < e->N; ++n) ys::update_node(e->v, e->SOL.data(), n);
+  return 0;
+}
+
+
+// ---------------------------------------------------------------- collision
+// Host restatement of the reference's traversal (src/Collision.cpp:266-326)
+// over the product's tree (ys_bvh.h) and narrow phase (ys_collide.cuh), in
+// the reference's emission order. faces / face_edges: cloth mesh; obstacle
+// faces given by node ids. Writes pairs [P][3] and impacts [I][15] (type,
+// four node ids, t, w[4], n[3], pair index, 0); returns 0, or 1 if a buffer
+// was too small.
+namespace {
+struct HostColl {
+  const ys::BvhTree* t[2];
+  std::vector<ys::Kdop> box[2];
+  std::vector<ys::CFace> faces[2];
+  ys::CMesh m;
+  double thick;
+  bool ccd;
+  std::vector<int> pairs;
+};
+void hc_refit(HostColl& h, int which, int n) {
+  const ys::BvhTree& t = *h.t[which];
+  if (t.face[n] >= 0) {
+    const ys::CFace& f = h.faces[which][t.face[n]];
+    ys::Kdop b, nb;
+    ys::kdop_node(b, ys::cc_pos(h.m, f.v[0], false), ys::cc_pos(h.m, f.v[0], true), h.ccd);
+    for (int k = 1; k < 3; ++k) {
+      ys::kdop_node(nb, ys::cc_pos(h.m, f.v[k], false), ys::cc_pos(h.m, f.v[k], true), h.ccd);
+      ys::kdop_add(b, nb);
+    }
+    h.box[which][n] = b;
+  } else {
+    hc_refit(h, which, t.left[n]);
+    hc_refit(h, which, t.right[n]);
+    h.box[which][n] = h.box[which][t.left[n]];
+    ys::kdop_add(h.box[which][n], h.box[which][t.right[n]]);
+  }
+}
+void hc_pair(HostColl& h, int a, int wb, int b) {  // a: cloth node, b: node of tree wb
+  if (!ys::kdop_overlap(h.box[0][a], h.box[wb][b], h.thick)) return;
+  const ys::BvhTree& ta = *h.t[0];
+  const ys::BvhTree& tb = *h.t[wb];
+  if (ta.face[a] >= 0 && tb.face[b] >= 0) {
+    h.pairs.push_back(ta.face[a]);
+    h.pairs.push_back(tb.face[b]);
+    h.pairs.push_back(wb);
+  } else if (ta.face[a] >= 0) {
+    hc_pair(h, a, wb, tb.left[b]);
+    hc_pair(h, a, wb, tb.right[b]);
+  } else {
+    hc_pair(h, ta.left[a], wb, b);
+    hc_pair(h, ta.right[a], wb, b);
+  }
+}
+void hc_self(HostColl& h, int n) {
+  const ys::BvhTree& t = *h.t[0];
+  if (t.face[n] >= 0) return;
+  hc_self(h, t.left[n]);
+  hc_self(h, t.right[n]);
+  hc_pair(h, t.left[n], 0, t.right[n]);
+}
+}  // namespace
+
+int emu_collide(int nn, const double* x, const double* xp, int nf, const int* fv, const int* fe, int no,
+                const double* ox, const double* oxp, int nof, const int* ofv, double thick, int ccd, int* pairs,
+                long pcap, double* impacts, long icap, long* np, long* ni) {
+  HostColl h;
+  h.m = ys::CMesh{x, xp, ox, oxp};
+  h.thick = thick;
+  h.ccd = ccd != 0;
+  h.faces[0].resize(nf);
+  for (int f = 0; f < nf; ++f)
+    for (int k = 0; k < 3; ++k) {
+      h.faces[0][f].v[k] = fv[3 * f + k];
+      h.faces[0][f].e[k][0] = fe[6 * f + 2 * k];
+      h.faces[0][f].e[k][1] = fe[6 * f + 2 * k + 1];
+    }
+  h.faces[1].resize(nof);
+  for (int f = 0; f < nof; ++f)
+    for (int k = 0; k < 3; ++k) {
+      const int b = k != 2 ? k + 1 : 0;
+      int e0 = ofv[3 * f + k], e1 = ofv[3 * f + b];
+      if (e0 > e1) std::swap(e0, e1);
+      h.faces[1][f].v[k] = -1 - ofv[3 * f + k];
+      h.faces[1][f].e[k][0] = -1 - e0;
+      h.faces[1][f].e[k][1] = -1 - e1;
+    }
+  std::vector<int> cv(nn), ov(no);
+  for (int i = 0; i < nn; ++i) cv[i] = i;
+  for (int i = 0; i < no; ++i) ov[i] = i;
+  ys::BvhTree ct = ys::bvh_build(nf, fv, nn, cv.data(), x, xp, h.ccd);
+  ys::BvhTree ot = ys::bvh_build(nof, ofv, no, ov.data(), ox, oxp, h.ccd);
+  h.t[0] = &ct;
+  h.t[1] = &ot;
+  h.box[0].resize(ct.face.size());
+  h.box[1].resize(ot.face.size());
+  hc_refit(h, 0, 0);
+  if (nof) {
+    // obstacle boxes use obstacle ids: refit with the obstacle faces (ids < 0)
+    hc_refit(h, 1, 0);
+  }
+  std::vector<int> up{0};
+  while (up.size() < 8) {
+    std::vector<int> ch;
+    for (int n : up) {
+      if (ct.face[n] >= 0) ch.push_back(n);
+      else { ch.push_back(ct.left[n]); ch.push_back(ct.right[n]); }
+    }
+    if (ch.size() == up.size()) break;
+    up = ch;
+  }
+  for (size_t n = 0; n < up.size(); ++n) {
+    hc_self(h, up[n]);
+    for (size_t q = 0; q < n; ++q) hc_pair(h, up[n], 0, up[q]);
+    if (nof) hc_pair(h, up[n], 1, 0);
+  }
+  const long P = (long)h.pairs.size() / 3;
+  *np = P;
+  std::vector<double> imp;
+  for (long p = 0; p < P; ++p) {
+    const ys::CFace& f0 = h.faces[0][h.pairs[3 * p]];
+    const ys::CFace& f1 = h.faces[h.pairs[3 * p + 2]][h.pairs[3 * p + 1]];
+    ys::Impact out[15];
+    const int c = ys::cc_face_pair(h.m, f0, f1, thick, h.ccd, out);
+    for (int k = 0; k < c; ++k) {
+      const ys::Impact& s = out[k];
+      const double r[15] = {(double)s.type, (double)s.node[0], (double)s.node[1], (double)s.node[2], (double)s.node[3],
+                            s.t, s.w[0], s.w[1], s.w[2], s.w[3], s.n[0], s.n[1], s.n[2], (double)p, 0.0};
+      imp.insert(imp.end(), r, r + 15);
+    }
+  }
+  *ni = (long)imp.size() / 15;
+  if (P > pcap || *ni > icap) return 1;
+  std::memcpy(pairs, h.pairs.data(), sizeof(int) * h.pairs.size());
+  std::memcpy(impacts, imp.data(), sizeof(double) * imp.size());
   return 0;
 }
 
