@@ -199,6 +199,8 @@ def main():
     ap.add_argument("--cloths", type=int, default=N_CLOTHS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="print the per-kernel table to stderr")
+    ap.add_argument("--graphs", type=int, default=1, choices=[0, 1],
+                    help="1: each step is one CUDA graph launch (conditional PCG loop); 0: launch by launch")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -241,6 +243,8 @@ def main():
     torch.cuda.set_device(dev)
 
     batch = ys.ClothBatch([ys.ClothSpec(**s) for s in specs], device=dev)
+    batch.use_graphs(bool(args.graphs))
+    config["step_launch"] = "one CUDA graph per step" if args.graphs else "kernel by kernel"
 
     def barrier():
         if dist is not None:

@@ -23,7 +23,8 @@ EXPORTED = [
     "ys_profile_read", "ys_apply_system_noalloc", "ys_tangent_count", "ys_tangent_enable", "ys_tangent_seed",
     "ys_tangent_set_state", "ys_tangent_get_state", "ys_step_tangent", "ys_cloth_mesh_topology",
     "ys_collider_create", "ys_collider_destroy", "ys_collider_set_positions", "ys_collider_find_pairs",
-    "ys_collider_get_pairs", "ys_collider_find_impacts", "ys_collider_get_impacts",
+    "ys_collider_get_pairs", "ys_collider_find_impacts", "ys_collider_get_impacts", "ys_use_graphs",
+    "ys_step_graphed",
 ]
 YS_TANGENT_EXACT, YS_TANGENT_REFERENCE = 0, 1
 PROF_KINDS = ["geom", "edges", "bends", "faces", "gather", "shear", "finalize", "pcg_setup", "spmv", "axpy", "dir",
@@ -110,6 +111,8 @@ def load(build_if_missing: bool = True):
     L.ys_tangent_get_state.argtypes = [vp, vp, vp, vp, vp, vp, ctypes.c_int32]
     L.ys_step_tangent.argtypes = [vp, ctypes.c_double, vp, ctypes.c_int32, vp, ctypes.c_int32, vp]
     L.ys_cloth_mesh_topology.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp]
+    L.ys_use_graphs.argtypes = [vp, ctypes.c_int32]
+    L.ys_step_graphed.argtypes = [vp, ctypes.c_double, vp, ctypes.c_int32, vp, vp]
     L.ys_collider_create.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int32, ctypes.c_int32, vp,
                                      ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, ctypes.POINTER(vp)]
     L.ys_collider_destroy.argtypes = [vp]

@@ -257,6 +257,10 @@ class ClothBatch:
             N.check(r, "ys_step")
         return self._stats(st)
 
+    def use_graphs(self, enable: bool = True):
+        """Run step() as one CUDA graph launch per step (see ys_use_graphs)."""
+        N.check(N.load().ys_use_graphs(self._h, int(bool(enable))), "ys_use_graphs")
+
     # ---- forward-mode sensitivities
     @property
     def n_tangents(self):

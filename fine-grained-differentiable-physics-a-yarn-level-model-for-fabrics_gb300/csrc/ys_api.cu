@@ -101,6 +101,20 @@ struct ys_batch {
   } tan;
   int nlines = 0;
   std::vector<double> line_R;  // yarn radius of each line's cloth
+  // whole-step CUDA graph (ys_use_graphs): assembly, a conditional while node
+  // over the PCG iterations, update; rebuilt when its parameters change
+  struct Graph {
+    bool enabled = false;
+    bool built = false;
+    cudaStream_t capture = nullptr;  // capture needs a stream of its own
+    cudaGraph_t main = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    double h = 0.0, tol = 0.0;
+    bool has_ext = false;
+    int override_max = -1, m = 0, cap = 0;
+    int* it_base = nullptr;  // device
+    int h_it = 0;
+  } graph;
   struct Rec { int kind; cudaEvent_t a, b; };
   std::vector<Rec> recs;
   std::vector<cudaEvent_t> pool;
@@ -151,6 +165,9 @@ struct ys_batch {
   }
   ~ys_batch() {
     drain();
+    if (graph.exec) cudaGraphExecDestroy(graph.exec);
+    if (graph.main) cudaGraphDestroy(graph.main);
+    if (graph.capture) cudaStreamDestroy(graph.capture);
     for (cudaEvent_t e : pool) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
     if (h_nactive) cudaFreeHost(h_nactive);
@@ -580,6 +597,7 @@ ys_status ys_get_solution(ys_batch* b, double* x, int32_t flags) {
 
 ys_status ys_step(ys_batch* b, double h, const double* ext_force, int32_t flags, const ys_solve_opts* opts,
                   ys_cloth_stats* stats) {
+  if (b && b->graph.enabled && !b->profiling) return ys_step_graphed(b, h, ext_force, flags, opts, stats);
   ys_status s = ys_assemble(b, h, ext_force, flags);
   if (s != YS_OK) return s;
   std::vector<ys_cloth_stats> local;
@@ -1004,3 +1022,135 @@ ys_status ys_step_tangent(ys_batch* b, double h, const double* ext_force, int32_
 
 }  // extern "C"
 
+
+// ----------------------------------------------------------- graphed step
+namespace {
+
+ys_status graph_build(ys_batch* b, int m, int cap, int override_max) {
+  ys_batch::Graph& G = b->graph;
+  if (G.exec) { cudaGraphExecDestroy(G.exec); G.exec = nullptr; }
+  if (G.main) { cudaGraphDestroy(G.main); G.main = nullptr; }
+  if (!G.capture) YS_CUDA(cudaStreamCreateWithFlags(&G.capture, cudaStreamNonBlocking));
+  if (!G.it_base) {
+    const ys_status s = b->alloc(&G.it_base, 1);
+    if (s != YS_OK) return s;
+  }
+  ys::Solver so = b->so;
+  so.it_base = G.it_base;
+  const ys::View& v = b->v;
+  const ys::Records& R = b->rec;
+  cudaStream_t cs = G.capture;
+  // before the loop: ys_assemble's kernels, the PCG start, the loop counter
+  cudaGraph_t pre = nullptr, post = nullptr;
+  YS_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  k_reset_status<<<(b->ncloth + 127) / 128, 128, 0, cs>>>(b->so.pc, b->ncloth);
+  if (b->geom_n) ys::launch_geom(v, b->anchors + b->geom_off, b->geom_n, cs);
+  ys::launch_edge_records(v, R, cs);
+  ys::launch_bend_records(v, R, cs);
+  ys::launch_face_records(v, R, cs);
+  ys::launch_gather(v, R, cs);
+  ys::launch_shear_records(v, R, cs);
+  ys::launch_finalize(v, R, b->blk, b->so, cs);
+  k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, cs>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
+  ys::launch_pcg_setup(v, b->blk, so, cs);
+  ys::launch_graph_loop_begin(so, cs);
+  YS_CUDA(cudaStreamEndCapture(cs, &pre));
+  // after the loop: the solution check and Cloth::update
+  YS_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  ys::launch_update(v, b->blk, b->so, cs);
+  YS_CUDA(cudaStreamEndCapture(cs, &post));
+  YS_CUDA(cudaGraphCreate(&G.main, 0));
+  cudaGraphNode_t n_pre, n_loop, n_post;
+  YS_CUDA(cudaGraphAddChildGraphNode(&n_pre, G.main, nullptr, 0, pre));
+  cudaGraphConditionalHandle hcond;
+  YS_CUDA(cudaGraphConditionalHandleCreate(&hcond, G.main, 1, cudaGraphCondAssignDefault));
+  // cudaGraphNodeParams has no default constructor: zeroed storage instead
+  alignas(cudaGraphNodeParams) unsigned char cp_raw[sizeof(cudaGraphNodeParams)] = {};
+  cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cp_raw);
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = hcond;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  YS_CUDA(cudaGraphAddNode(&n_loop, G.main, &n_pre, nullptr, 1, &cp));
+  // the loop body: m PCG iterations (m even keeps the r.z parity of each
+  // iteration equal to its local index's), then the condition
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  YS_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  for (int j = 0; j < m; ++j) {
+    ys::launch_pcg_spmv(v, b->blk, so, cs);
+    ys::launch_pcg_axpy(v, b->blk, so, j, cs);
+    ys::launch_pcg_dir(v, b->blk, so, j, cs);
+  }
+  ys::launch_graph_loop_tail(so, b->ncloth, m, cap, hcond, cs);
+  YS_CUDA(cudaStreamEndCapture(cs, &body));
+  YS_CUDA(cudaGraphAddChildGraphNode(&n_post, G.main, &n_loop, 1, post));
+  cudaGraphDestroy(pre);
+  cudaGraphDestroy(post);
+  YS_CUDA(cudaGraphInstantiate(&G.exec, G.main, 0));
+  G.built = true;
+  return YS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ys_status ys_use_graphs(ys_batch* b, int32_t enable) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  b->graph.enabled = enable != 0;
+  return YS_OK;
+}
+
+ys_status ys_step_graphed(ys_batch* b, double h, const double* ext_force, int32_t flags, const ys_solve_opts* opts,
+                          ys_cloth_stats* stats) {
+  if (!b || !(h > 0)) return fail(YS_ERR_ARG, "bad argument");
+  YS_CUDA(cudaSetDevice(b->device));
+  ys_batch::Graph& G = b->graph;
+  b->v.h = h;
+  b->v.ext = nullptr;
+  if (ext_force) {
+    ys_status s = upload_soa(b, ext_force, b->ext, 5, flags);
+    if (s != YS_OK) return s;
+    b->v.ext = b->ext;
+  }
+  const double tol = (opts && opts->tol > 0) ? opts->tol : DBL_EPSILON;
+  const int override_max = (opts && opts->maxiter >= 0) ? opts->maxiter : -1;
+  int m = (opts && opts->check_every > 0) ? opts->check_every : 16;
+  m += m & 1;
+  const int cap = override_max >= 0 ? override_max : b->max_maxiter;
+  b->so.tol = tol;
+  if (!G.built || G.h != h || G.has_ext != (ext_force != nullptr) || G.tol != tol ||
+      G.override_max != override_max || G.m != m || G.cap != cap) {
+    ys_status s = graph_build(b, m, cap, override_max);
+    if (s != YS_OK) return s;
+    G.h = h;
+    G.has_ext = ext_force != nullptr;
+    G.tol = tol;
+    G.override_max = override_max;
+    G.m = m;
+    G.cap = cap;
+  }
+  YS_CUDA(cudaGraphLaunch(G.exec, b->stream));
+  std::vector<ys::PcgCloth> pc(b->ncloth);
+  YS_CUDA(cudaMemcpyAsync(pc.data(), b->so.pc, sizeof(ys::PcgCloth) * b->ncloth, cudaMemcpyDeviceToHost, b->stream));
+  YS_CUDA(cudaMemcpyAsync(&G.h_it, G.it_base, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  // kernels the graph ran: 11 (+ geometry) before the loop, 3 per iteration
+  // + 1 per trip through the body, 2 after
+  b->launches += 13 + (b->geom_n ? 1 : 0) + 3LL * G.h_it + G.h_it / m;
+  ys_status ret = YS_OK;
+  for (int c = 0; c < b->ncloth; ++c) {
+    if (pc[c].status & 3) ret = YS_ERR_NONFINITE;
+    else if ((pc[c].status & 4) && ret == YS_OK) ret = YS_ERR_MAXITER;
+    if (stats) {
+      stats[c].ok = (pc[c].status & 3) == 0;
+      stats[c].cg_iterations = pc[c].iters;
+      stats[c].cg_error = pc[c].bb > 0 ? std::sqrt(pc[c].rr / pc[c].bb) : 0.0;
+      stats[c].hit_maxiter = (pc[c].status & 4) ? 1 : 0;
+    }
+  }
+  b->assembled = false;
+  return ret;
+}
+
+}  // extern "C"

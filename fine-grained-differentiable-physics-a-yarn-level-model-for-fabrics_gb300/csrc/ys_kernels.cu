@@ -158,8 +158,9 @@ __global__ void __launch_bounds__(kBlock) k_pcg_axpy(View v, Blocks b, Solver so
 // stop test |r|^2 < thr, else beta = rz_new / rz and p = z + beta p. Every
 // block of a cloth reaches the same decision from the same fixed-order sums;
 // only the cloth's first block writes the cloth's bookkeeping.
-__global__ void __launch_bounds__(kBlock) k_pcg_dir(View v, Blocks b, Solver so, int parity, int it) {
+__global__ void __launch_bounds__(kBlock) k_pcg_dir(View v, Blocks b, Solver so, int parity, int it_local) {
   __shared__ int go_sh;
+  const int it = so.it_base ? *so.it_base + it_local : it_local;
   __shared__ double beta_sh;
   const int blk = blockIdx.x;
   const int c = b.blk_cloth[blk];
@@ -270,6 +271,30 @@ void launch_pcg_dir(const View& v, const Blocks& b, const Solver& so, int it, cu
 }
 void launch_count_active(const View& v, const Solver& so, cudaStream_t s) {
   k_count_active<<<1, 256, 0, s>>>(so, v.ncloth);
+}
+__global__ void k_graph_loop_begin(Solver so) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *so.it_base = 0;
+}
+__global__ void k_graph_loop_tail(Solver so, int ncloth, int m, int cap, cudaGraphConditionalHandle h) {
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  int mine = 0;
+  for (int c = threadIdx.x; c < ncloth; c += blockDim.x) mine += so.pc[c].active;
+  atomicAdd(&cnt, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *so.nactive = cnt;
+    const int done = *so.it_base + m;
+    *so.it_base = done;
+    // the loop ends when no cloth iterates or at the iteration cap, whichever first
+    cudaGraphSetConditional(h, (cnt > 0 && done < cap) ? 1u : 0u);
+  }
+}
+void launch_graph_loop_begin(const Solver& so, cudaStream_t s) { k_graph_loop_begin<<<1, 32, 0, s>>>(so); }
+void launch_graph_loop_tail(const Solver& so, int ncloth, int m, int cap, cudaGraphConditionalHandle h,
+                            cudaStream_t s) {
+  k_graph_loop_tail<<<1, 256, 0, s>>>(so, ncloth, m, cap, h);
 }
 void launch_check_solution(const View& v, const Blocks& b, const Solver& so, cudaStream_t s) {
   k_check_solution<<<b.nblk, kBlock, 0, s>>>(v, b, so);

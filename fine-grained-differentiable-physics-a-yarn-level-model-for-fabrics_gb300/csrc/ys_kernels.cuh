@@ -41,6 +41,7 @@ struct Solver {
   int* nactive;   // device counter
   double tol;
   int trans;      // 1: solve A^T x = b (the reference-mode tangent solves)
+  int* it_base;   // graph mode: iterations completed before this graph body (device), else null
 };
 
 constexpr int kBlock = 128;
@@ -58,6 +59,12 @@ void launch_pcg_axpy(const View& v, const Blocks& b, const Solver& so, int it, c
 void launch_pcg_dir(const View& v, const Blocks& b, const Solver& so, int it, cudaStream_t s);
 void launch_count_active(const View& v, const Solver& so, cudaStream_t s);
 void launch_check_solution(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
+// graph mode: *it_base = 0 before the loop; after each body of m iterations
+// count the active cloths, advance *it_base by m and set the while node's
+// condition to (some cloth active and *it_base < cap)
+void launch_graph_loop_begin(const Solver& so, cudaStream_t s);
+void launch_graph_loop_tail(const Solver& so, int ncloth, int m, int cap, cudaGraphConditionalHandle h,
+                            cudaStream_t s);
 void launch_update(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
 void launch_spmv(const View& v, const double* x, double* y, cudaStream_t s);
 

@@ -130,6 +130,17 @@ ys_status ys_get_solution(ys_batch *b, double *x, int32_t flags);
  * n_cloths entries (host). */
 ys_status ys_step(ys_batch *b, double h, const double *ext_force, int32_t flags, const ys_solve_opts *opts,
                   ys_cloth_stats *stats);
+/* Whole-step CUDA graphs (no counterpart in the reference): with enable = 1,
+ * ys_step runs as one graph launch -- the assembly kernels, a conditional
+ * while node over the PCG iterations (check_every of them per trip, ending
+ * when no cloth iterates or at the iteration cap), the check and the update --
+ * captured on first use and again when h, the presence of an external force
+ * or the solve options change. Results equal the launch-by-launch step bit
+ * for bit. Ignored while ys_profile is on. */
+ys_status ys_use_graphs(ys_batch *b, int32_t enable);
+/* ys_step through the graph regardless of ys_use_graphs. */
+ys_status ys_step_graphed(ys_batch *b, double h, const double *ext_force, int32_t flags, const ys_solve_opts *opts,
+                          ys_cloth_stats *stats);
 /* y = A x with the assembled matrices (node layout [total_nodes][5]). */
 ys_status ys_apply_system(ys_batch *b, const double *x, double *y, int32_t flags);
 /* y = A x like ys_apply_system, for callers that must not allocate at call

@@ -177,3 +177,36 @@ def test_reference_style_driver_loop():
         assert ys.SimStep(cloth, phy, 1e-3)
     st = cloth.get_ClothState()
     assert goldens.rel(st.LPos, g["s5_LPos"]) <= STATE_TOL
+
+
+def test_graphed_step_equals_launch_by_launch():
+    """ys_use_graphs: the whole step as one CUDA graph (conditional while node
+    over the PCG) gives the launch-by-launch step's states bit for bit, with
+    and without an external force and after h changes (graph rebuilt)."""
+    gs = [goldens.load("twill6_upright_wind_pert"), goldens.load("plain5_extforce")]
+    outs = []
+    for graphed in (False, True):
+        b = ys.ClothBatch([spec_from_golden(g) for g in gs])
+        full = b.get_state()
+        ext = np.zeros((b.total_nodes, 5))
+        for c, g in enumerate(gs):
+            st = goldens.init_state(g) or goldens.state(g, 0)
+            for k in full:
+                full[k][b.node_slice(c)] = st[k]
+            e = ext5(g)
+            if e is not None:
+                ext[b.node_slice(c)] = e
+        ext[b.node_slice(0), 2] = 1e-4
+        b.set_state(**full)
+        b.use_graphs(graphed)
+        st = []
+        for k, h in enumerate([1e-3] * 4 + [5e-4] * 3):
+            stats = b.step(h, ext if k % 2 else None, check_every=4)
+            assert all(s["ok"] for s in stats)
+            st.append((b.get_state(), [s["cg_iterations"] for s in stats]))
+        b.close()
+        outs.append(st)
+    for (a, ia), (c, ic) in zip(*outs):
+        assert ia == ic
+        for k in a:
+            assert np.array_equal(a[k], c[k]), k
