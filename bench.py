@@ -199,8 +199,9 @@ def main():
     ap.add_argument("--cloths", type=int, default=N_CLOTHS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="print the per-kernel table to stderr")
-    ap.add_argument("--graphs", type=int, default=1, choices=[0, 1],
-                    help="1: each step is one CUDA graph launch (conditional PCG loop); 0: launch by launch")
+    ap.add_argument("--schedule", default="auto", choices=["auto", "graph", "launch"],
+                    help="auto: ys_autotune picks graph or launch-by-launch steps and the PCG check interval; "
+                         "graph: one CUDA graph launch per step (conditional PCG loop); launch: kernel by kernel")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -243,8 +244,14 @@ def main():
     torch.cuda.set_device(dev)
 
     batch = ys.ClothBatch([ys.ClothSpec(**s) for s in specs], device=dev)
-    batch.use_graphs(bool(args.graphs))
-    config["step_launch"] = "one CUDA graph per step" if args.graphs else "kernel by kernel"
+    if args.schedule == "auto":
+        batch.set_winds(wind_at(wind, 0))
+        sched = batch.autotune(H, tol=TOL, steps=3)
+        config["schedule"] = {"chosen_by": "ys_autotune", "graph": sched["graphs"],
+                              "check_every": sched["check_every"]}
+    else:
+        batch.use_graphs(args.schedule == "graph")
+        config["schedule"] = {"chosen_by": "flag", "graph": args.schedule == "graph", "check_every": 16}
 
     def barrier():
         if dist is not None:

@@ -24,11 +24,14 @@ EXPORTED = [
     "ys_tangent_set_state", "ys_tangent_get_state", "ys_step_tangent", "ys_cloth_mesh_topology",
     "ys_collider_create", "ys_collider_destroy", "ys_collider_set_positions", "ys_collider_find_pairs",
     "ys_collider_get_pairs", "ys_collider_find_impacts", "ys_collider_get_impacts", "ys_use_graphs",
-    "ys_step_graphed",
+    "ys_step_graphed", "ys_autotune", "ys_gnn_param_count", "ys_gnn_create", "ys_gnn_destroy", "ys_gnn_get_params",
+    "ys_gnn_set_params", "ys_gnn_train_step", "ys_gnn_loss_grad", "ys_set_preconditioner", "ys_precond_info",
+    "ys_get_system_slots", "ys_tc_gemm_bf16",
 ]
+YS_PREC_JACOBI, YS_PREC_LEARNED = 0, 1
 YS_TANGENT_EXACT, YS_TANGENT_REFERENCE = 0, 1
 PROF_KINDS = ["geom", "edges", "bends", "faces", "gather", "shear", "finalize", "pcg_setup", "spmv", "axpy", "dir",
-              "update", "misc"]
+              "update", "misc", "gnn", "precond"]
 
 
 class ClothDesc(ctypes.Structure):
@@ -50,6 +53,10 @@ class ClothDesc(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     """ys_solve_opts"""
     _fields_ = [("tol", ctypes.c_double), ("maxiter", ctypes.c_int32), ("check_every", ctypes.c_int32)]
+
+
+class Schedule(ctypes.Structure):
+    _fields_ = [("graphs", ctypes.c_int32), ("check_every", ctypes.c_int32), ("ms_per_step", ctypes.c_double)]
 
 
 class ClothStats(ctypes.Structure):
@@ -113,6 +120,7 @@ def load(build_if_missing: bool = True):
     L.ys_cloth_mesh_topology.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp]
     L.ys_use_graphs.argtypes = [vp, ctypes.c_int32]
     L.ys_step_graphed.argtypes = [vp, ctypes.c_double, vp, ctypes.c_int32, vp, vp]
+    L.ys_autotune.argtypes = [vp, ctypes.c_double, vp, ctypes.c_int32, vp]
     L.ys_collider_create.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int32, ctypes.c_int32, vp,
                                      ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, ctypes.POINTER(vp)]
     L.ys_collider_destroy.argtypes = [vp]
@@ -126,9 +134,22 @@ def load(build_if_missing: bool = True):
     L.ys_profile.argtypes = [vp, ctypes.c_int32]
     L.ys_profile_read.argtypes = [vp, _dp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                   ctypes.c_int32]
+    L.ys_gnn_param_count.argtypes = []
+    L.ys_gnn_param_count.restype = ctypes.c_int32
+    L.ys_gnn_create.argtypes = [ctypes.c_int32, ctypes.c_uint64, ctypes.POINTER(vp)]
+    L.ys_gnn_destroy.argtypes = [vp]
+    L.ys_gnn_destroy.restype = None
+    L.ys_gnn_get_params.argtypes = [vp, vp]
+    L.ys_gnn_set_params.argtypes = [vp, vp]
+    L.ys_gnn_train_step.argtypes = [vp, vp, ctypes.c_uint64, ctypes.c_float, _dp]
+    L.ys_gnn_loss_grad.argtypes = [vp, vp, vp, ctypes.c_uint64, _dp, vp, vp, vp]
+    L.ys_set_preconditioner.argtypes = [vp, ctypes.c_int32, vp]
+    L.ys_precond_info.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    L.ys_get_system_slots.argtypes = [vp, vp, vp]
+    L.ys_tc_gemm_bf16.argtypes = [ctypes.c_int32, vp, vp, vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
     for name in EXPORTED:
         if name not in ("ys_batch_destroy", "ys_last_error", "ys_cloth_node_offset", "ys_cloth_dim",
-                        "ys_tangent_count", "ys_collider_destroy"):
+                        "ys_tangent_count", "ys_collider_destroy", "ys_gnn_destroy", "ys_gnn_param_count"):
             getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L

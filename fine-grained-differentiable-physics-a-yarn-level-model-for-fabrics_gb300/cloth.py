@@ -235,7 +235,7 @@ class ClothBatch:
         p, f = _ptr(ext_force)
         N.check(N.load().ys_assemble(self._h, h, ctypes.c_void_p(p) if p else None, f), "ys_assemble")
 
-    def solve(self, tol=0.0, maxiter=-1, check_every=16):
+    def solve(self, tol=0.0, maxiter=-1, check_every=0):
         st = (N.ClothStats * self.n_cloths)()
         r = N.load().ys_solve(self._h, ctypes.byref(self._opts(tol, maxiter, check_every)), st)
         if r not in (N.YS_OK, N.YS_ERR_NONFINITE, N.YS_ERR_MAXITER):
@@ -247,7 +247,7 @@ class ClothBatch:
         N.check(N.load().ys_get_solution(self._h, ctypes.c_void_p(x.ctypes.data), 0), "ys_get_solution")
         return x
 
-    def step(self, h, ext_force=None, tol=0.0, maxiter=-1, check_every=16):
+    def step(self, h, ext_force=None, tol=0.0, maxiter=-1, check_every=0):
         """One SimStep for every cloth; returns per-cloth stats (ok = SimStep's bool)."""
         p, f = _ptr(ext_force)
         st = (N.ClothStats * self.n_cloths)()
@@ -260,6 +260,43 @@ class ClothBatch:
     def use_graphs(self, enable: bool = True):
         """Run step() as one CUDA graph launch per step (see ys_use_graphs)."""
         N.check(N.load().ys_use_graphs(self._h, int(bool(enable))), "ys_use_graphs")
+
+    def set_preconditioner(self, kind: str = "jacobi", net=None):
+        """'jacobi' (Eigen's default, src/Solvers.cpp:22-24) or 'learned' with a
+        precond.LearnedPreconditioner, which the batch borrows."""
+        if kind == "jacobi":
+            N.check(N.load().ys_set_preconditioner(self._h, N.YS_PREC_JACOBI, None), "ys_set_preconditioner")
+            self._precond = None
+        elif kind == "learned":
+            if net is None:
+                raise ValueError("learned preconditioner needs a network")
+            N.check(N.load().ys_set_preconditioner(self._h, N.YS_PREC_LEARNED, net._h), "ys_set_preconditioner")
+            self._precond = net  # keep it alive while the batch uses it
+        else:
+            raise ValueError(kind)
+
+    def precond_info(self) -> dict:
+        s, f = ctypes.c_int64(), ctypes.c_int64()
+        N.check(N.load().ys_precond_info(self._h, ctypes.byref(s), ctypes.byref(f)), "ys_precond_info")
+        return dict(learned_solves=s.value, fallbacks=f.value)
+
+    def system_slots(self):
+        """The last assembled system: coefficient slots [159, n] and right-hand
+        side [5, n] (component-major, batch node order)."""
+        n = self.total_nodes
+        a = np.zeros((159, n))
+        b = np.zeros((5, n))
+        N.check(N.load().ys_get_system_slots(self._h, ctypes.c_void_p(a.ctypes.data), ctypes.c_void_p(b.ctypes.data)),
+                "ys_get_system_slots")
+        return a, b
+
+    def autotune(self, h, tol=0.0, maxiter=-1, steps=5) -> dict:
+        """Time each step schedule from the current state (restored afterwards)
+        and make the fastest the default (see ys_autotune)."""
+        sc = N.Schedule()
+        N.check(N.load().ys_autotune(self._h, h, ctypes.byref(self._opts(tol, maxiter, 0)), int(steps),
+                                     ctypes.byref(sc)), "ys_autotune")
+        return dict(graphs=bool(sc.graphs), check_every=sc.check_every, ms_per_step=sc.ms_per_step)
 
     # ---- forward-mode sensitivities
     @property
@@ -301,7 +338,7 @@ class ClothBatch:
                 "ys_tangent_get_state")
         return out
 
-    def step_tangent(self, h, ext_force=None, tol=0.0, maxiter=-1, check_every=16, kact=None):
+    def step_tangent(self, h, ext_force=None, tol=0.0, maxiter=-1, check_every=0, kact=None):
         """step() that also advances the first kact tangent directions."""
         kact = self.n_tangents if kact is None else int(kact)
         p, f = _ptr(ext_force)

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/yarnsim.h"
+#include "ys_gnn.cuh"
 #include "ys_kernels.cuh"
 
 namespace {
@@ -115,6 +116,19 @@ struct ys_batch {
     int* it_base = nullptr;  // device
     int h_it = 0;
   } graph;
+  int check_every = 16;  // PCG iterations between convergence checks when the call gives none
+  bool has_system = false;  // v.A / v.B hold an assembled system (kept after the update)
+  // learned preconditioner (ys_set_preconditioner); buffers allocated on first use
+  struct Learn {
+    int kind = YS_PREC_JACOBI;
+    ys_gnn* net = nullptr;
+    bool ready = false;
+    ys::GnnBufs g{};
+    float* y = nullptr;
+    double* z = nullptr;
+    int64_t fallbacks = 0;
+    int64_t solves = 0;
+  } learn;
   struct Rec { int kind; cudaEvent_t a, b; };
   std::vector<Rec> recs;
   std::vector<cudaEvent_t> pool;
@@ -346,7 +360,7 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
   A(&b->rec.edge, (size_t)ys::kEdgeFields * 2 * nt); A(&b->rec.bend, (size_t)ys::kBendFields * 2 * nt);
   A(&b->rec.face, 6 * nt); A(&b->rec.shear, (size_t)ys::kShearFields * 4 * nt);
   A(&b->so.x, 5 * nt); A(&b->so.r, 5 * nt); A(&b->so.p, 5 * nt); A(&b->so.q, 5 * nt); A(&b->so.dinv, 5 * nt);
-  A(&b->so.part, 3 * blk_cloth.size()); A(&b->so.pc, n_cloths); A(&b->so.nactive, 1);
+  A(&b->so.part, 4 * blk_cloth.size()); A(&b->so.pc, n_cloths); A(&b->so.nactive, 1);
   A(&b->stage, 5 * nt); A(&b->ext, 5 * nt);
   if (st != YS_OK) { delete b; return st; }
   if (cudaMallocHost(&b->h_nactive, sizeof(int)) != cudaSuccess) {
@@ -528,6 +542,7 @@ ys_status ys_assemble(ys_batch* b, double h, const double* ext_force, int32_t fl
   b->run(YS_PROF_FINALIZE, 1, [&] { ys::launch_finalize(v, R, b->blk, b->so, s); });
   YS_CUDA(cudaGetLastError());
   b->assembled = true;
+  b->has_system = true;
   return YS_OK;
 }
 
@@ -540,7 +555,7 @@ ys_status solve_impl(ys_batch* b, const ys::View& v, const ys_solve_opts* opts, 
   cudaStream_t s = b->stream;
   b->so.tol = (opts && opts->tol > 0) ? opts->tol : DBL_EPSILON;
   const int override_max = (opts && opts->maxiter >= 0) ? opts->maxiter : -1;
-  const int every = (opts && opts->check_every > 0) ? opts->check_every : 16;
+  const int every = (opts && opts->check_every > 0) ? opts->check_every : b->check_every;
   const int cap = override_max >= 0 ? override_max : b->max_maxiter;
   b->run(YS_PROF_MISC, 1, [&] {
     k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
@@ -578,6 +593,8 @@ ys_status solve_impl(ys_batch* b, const ys::View& v, const ys_solve_opts* opts, 
   return ret;
 }
 
+ys_status solve_learned(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* stats);
+
 }  // namespace
 
 extern "C" {
@@ -586,6 +603,7 @@ ys_status ys_solve(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* stats
   if (!b) return fail(YS_ERR_ARG, "null handle");
   if (!b->assembled) return fail(YS_ERR_ARG, "ys_solve before ys_assemble");
   YS_CUDA(cudaSetDevice(b->device));
+  if (b->learn.kind == YS_PREC_LEARNED) return solve_learned(b, opts, stats);
   return solve_impl(b, b->v, opts, stats);
 }
 
@@ -597,7 +615,8 @@ ys_status ys_get_solution(ys_batch* b, double* x, int32_t flags) {
 
 ys_status ys_step(ys_batch* b, double h, const double* ext_force, int32_t flags, const ys_solve_opts* opts,
                   ys_cloth_stats* stats) {
-  if (b && b->graph.enabled && !b->profiling) return ys_step_graphed(b, h, ext_force, flags, opts, stats);
+  if (b && b->graph.enabled && !b->profiling && b->learn.kind == YS_PREC_JACOBI)
+    return ys_step_graphed(b, h, ext_force, flags, opts, stats);
   ys_status s = ys_assemble(b, h, ext_force, flags);
   if (s != YS_OK) return s;
   std::vector<ys_cloth_stats> local;
@@ -1115,7 +1134,7 @@ ys_status ys_step_graphed(ys_batch* b, double h, const double* ext_force, int32_
   }
   const double tol = (opts && opts->tol > 0) ? opts->tol : DBL_EPSILON;
   const int override_max = (opts && opts->maxiter >= 0) ? opts->maxiter : -1;
-  int m = (opts && opts->check_every > 0) ? opts->check_every : 16;
+  int m = (opts && opts->check_every > 0) ? opts->check_every : b->check_every;
   m += m & 1;
   const int cap = override_max >= 0 ? override_max : b->max_maxiter;
   b->so.tol = tol;
@@ -1151,6 +1170,454 @@ ys_status ys_step_graphed(ys_batch* b, double h, const double* ext_force, int32_
   }
   b->assembled = false;
   return ret;
+}
+
+// The schedule tuner: every candidate (whole-step graph or launch by launch,
+// PCG iterations between convergence checks) runs the same steps from the same
+// state and gives bit-identical results -- the choices only move launches and
+// host synchronisations -- so the tuner times each on a snapshot of the state,
+// restores it, and keeps the fastest.
+ys_status ys_autotune(ys_batch* b, double h, const ys_solve_opts* opts, int32_t steps, ys_schedule* best) {
+  if (!b || !(h > 0) || steps < 1) return fail(YS_ERR_ARG, "bad argument");
+  YS_CUDA(cudaSetDevice(b->device));
+  const size_t nt = (size_t)b->v.ntot;
+  double* const state[6] = {b->v.X, b->v.XF, b->v.V, b->v.UV, b->v.UVB, b->v.UVD};
+  const int comps[6] = {3, 3, 3, 2, 2, 2};
+  double* snap = nullptr;
+  YS_CUDA(cudaMalloc(&snap, sizeof(double) * 15 * nt));
+  auto copy_state = [&](bool save) -> cudaError_t {
+    size_t off = 0;
+    for (int k = 0; k < 6; ++k) {
+      const size_t n = comps[k] * nt;
+      cudaError_t e = cudaMemcpyAsync(save ? snap + off : state[k], save ? state[k] : snap + off,
+                                      sizeof(double) * n, cudaMemcpyDeviceToDevice, b->stream);
+      if (e != cudaSuccess) return e;
+      off += n;
+    }
+    return cudaSuccess;
+  };
+  const bool was_graph = b->graph.enabled, was_prof = b->profiling;
+  b->profiling = false;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ys_status st = YS_OK;
+  ys_schedule top{};
+  top.ms_per_step = -1.0;
+  const int every_c[5] = {2, 4, 8, 16, 32};
+  std::vector<ys_cloth_stats> stats(b->ncloth);
+  cudaError_t ce = copy_state(true);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+  for (int g = 0; g < 2 && ce == cudaSuccess && st == YS_OK; ++g) {
+    for (int c = 0; c < 5 && ce == cudaSuccess && st == YS_OK; ++c) {
+      b->graph.enabled = g == 1;
+      ys_solve_opts o = opts ? *opts : ys_solve_opts{0.0, -1, 0};
+      o.check_every = every_c[c];
+      // one untimed step builds the graph (and warms the caches)
+      if ((ce = copy_state(false)) != cudaSuccess) break;
+      ys_status s = ys_step(b, h, nullptr, 0, &o, stats.data());
+      if (s == YS_ERR_ARG || s == YS_ERR_CUDA) { st = s; break; }
+      if ((ce = copy_state(false)) != cudaSuccess) break;
+      if ((ce = cudaEventRecord(e0, b->stream)) != cudaSuccess) break;
+      for (int k = 0; k < steps && st == YS_OK; ++k) {
+        s = ys_step(b, h, nullptr, 0, &o, stats.data());
+        if (s == YS_ERR_ARG || s == YS_ERR_CUDA) st = s;
+      }
+      if (st != YS_OK) break;
+      if ((ce = cudaEventRecord(e1, b->stream)) != cudaSuccess) break;
+      if ((ce = cudaEventSynchronize(e1)) != cudaSuccess) break;
+      float ms = 0.f;
+      if ((ce = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) break;
+      const double per = ms / steps;
+      if (top.ms_per_step < 0 || per < top.ms_per_step) {
+        top.graphs = g;
+        top.check_every = every_c[c];
+        top.ms_per_step = per;
+      }
+    }
+  }
+  if (ce == cudaSuccess) ce = copy_state(false);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(b->stream);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(snap);
+  b->profiling = was_prof;
+  b->assembled = false;
+  if (ce != cudaSuccess) {
+    b->graph.enabled = was_graph;
+    return fail(YS_ERR_CUDA, std::string("ys_autotune: ") + cudaGetErrorString(ce));
+  }
+  if (st != YS_OK) {
+    b->graph.enabled = was_graph;
+    return st;
+  }
+  b->graph.enabled = top.graphs != 0;
+  b->check_every = top.check_every;
+  if (best) *best = top;
+  return YS_OK;
+}
+
+}  // extern "C"
+
+
+// ------------------------------------------------------- learned preconditioner
+struct ys_gnn {
+  int device = 0;
+  ys::GnnNet net{};
+  float* m = nullptr;  // Adam moments
+  float* vv = nullptr;
+  int step = 0;
+  std::vector<void*> allocs;
+  template <class T>
+  cudaError_t alloc(T** p, size_t count) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess) {
+      allocs.push_back(q);
+      *p = static_cast<T*>(q);
+    }
+    return e;
+  }
+  ~ys_gnn() {
+    for (void* p : allocs) cudaFree(p);
+  }
+};
+
+namespace {
+
+// GNN buffers of a batch, sized for its nodes
+ys_status learn_ensure(ys_batch* b) {
+  ys_batch::Learn& L = b->learn;
+  if (L.ready) return YS_OK;
+  const int nt = b->ntot;
+  ys::GnnBufs& g = L.g;
+  g.ntot = nt;
+  g.nlblk = (nt + 127) / 128;
+  g.nsplit = 296;
+  ys_status st = YS_OK;
+  auto A = [&](auto** p, size_t cnt) { if (st == YS_OK) st = b->alloc(p, cnt); };
+  A(&g.nbr, 4 * (size_t)nt);
+  A(&g.linv, 15 * (size_t)nt);
+  A(&g.chol_ok, nt);
+  A(&g.E, 100 * (size_t)nt);
+  A(&g.f, (size_t)ys::kGIn * nt);
+  A(&g.h, 4 * (size_t)ys::kGHid * nt);
+  A(&g.hb, 4 * (size_t)ys::kGHid * nt);
+  A(&g.act, 3 * (size_t)ys::kGHid * nt);
+  A(&g.o, (size_t)ys::kGOut * nt);
+  A(&g.G, 125 * (size_t)nt);
+  A(&g.Gn, 125 * (size_t)nt);
+  A(&g.vec, 12 * 5 * (size_t)nt);
+  A(&g.dob, (size_t)ys::kGOut * nt);
+  A(&g.dh, (size_t)ys::kGHid * nt);
+  A(&g.dzb, (size_t)ys::kGHid * nt);
+  A(&g.dm, (size_t)ys::kGMsg * nt);
+  A(&g.wpart, (size_t)g.nsplit * ys::kWgradRows * 128);
+  A(&g.grad, ys::kGParams);
+  A(&g.lpart, 2 * (size_t)g.nlblk + 2);
+  A(&g.err, 1);
+  A(&L.y, 5 * (size_t)nt);
+  A(&L.z, 5 * (size_t)nt);
+  if (st != YS_OK) return st;
+  YS_CUDA(cudaMemsetAsync(g.err, 0, sizeof(int), b->stream));
+  YS_CUDA(cudaMemsetAsync(g.grad, 0, sizeof(float) * ys::kGParams, b->stream));
+  ys::gnn_neighbours(b->v, g.nbr, b->stream);
+  b->launches += 1;
+  YS_CUDA(cudaGetLastError());
+  L.ready = true;
+  return YS_OK;
+}
+
+// features, network, G blocks for the assembled system
+ys_status learn_infer(ys_batch* b, ys_gnn* net) {
+  ys::GnnBufs& g = b->learn.g;
+  b->run(YS_PROF_GNN, 2 + 5 + 1, [&] {
+    ys::gnn_prepare(b->v, g, b->stream);
+    ys::gnn_forward(net->net, g, b->stream);
+    ys::gnn_make_g(g, b->stream);
+  });
+  YS_CUDA(cudaGetLastError());
+  return YS_OK;
+}
+
+ys_status read_err(ys_batch* b, int* err) {
+  YS_CUDA(cudaMemcpyAsync(err, b->learn.g.err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  return YS_OK;
+}
+
+// PCG with M^-1 = G^T G; cloths that stop without converging (iteration cap or
+// a breakdown) are solved again by Jacobi-PCG, which also judges the residual
+// rule both solvers share: |b - A x| <= tol |b| on the recursively updated
+// residual, as in Eigen's ConjugateGradient.
+ys_status solve_learned(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* stats) {
+  ys_batch::Learn& L = b->learn;
+  if (!L.net) return fail(YS_ERR_ARG, "learned preconditioner without a network");
+  ys_status st = learn_ensure(b);
+  if (st != YS_OK) return st;
+  if ((st = learn_infer(b, L.net)) != YS_OK) return st;
+  cudaStream_t s = b->stream;
+  const ys::View& v = b->v;
+  b->so.tol = (opts && opts->tol > 0) ? opts->tol : DBL_EPSILON;
+  const int override_max = (opts && opts->maxiter >= 0) ? opts->maxiter : -1;
+  const int every = (opts && opts->check_every > 0) ? opts->check_every : b->check_every;
+  const int cap = override_max >= 0 ? override_max : b->max_maxiter;
+  const ys::LpcgExtra lx{L.g.G, L.g.nbr, L.y, L.z};
+  b->run(YS_PROF_MISC, 1, [&] {
+    k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
+  });
+  b->run(YS_PROF_PCG_SETUP, 4, [&] { ys::lpcg_setup(v, b->blk, b->so, lx, s); });
+  YS_CUDA(cudaGetLastError());
+  int it = 0;
+  while (it < cap) {
+    const int n = std::min(every, cap - it);
+    for (int q = 0; q < n; ++q, ++it) {
+      const int par = it & 1;
+      b->run(YS_PROF_SPMV, 1, [&] { ys::launch_pcg_spmv(v, b->blk, b->so, s); });
+      b->run(YS_PROF_AXPY, 1, [&] { ys::lpcg_axpy(v, b->blk, b->so, par, s); });
+      b->run(YS_PROF_PREC, 2, [&] { ys::lpcg_precondition(v, b->blk, b->so, lx, s); });
+      b->run(YS_PROF_DIR, 1, [&] { ys::lpcg_dir(v, b->blk, b->so, lx, par, it, s); });
+    }
+    b->run(YS_PROF_MISC, 1, [&] { ys::launch_count_active(v, b->so, s); });
+    YS_CUDA(cudaMemcpyAsync(b->h_nactive, b->so.nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
+    YS_CUDA(cudaStreamSynchronize(s));
+    if (*b->h_nactive == 0) break;
+  }
+  YS_CUDA(cudaGetLastError());
+  int err = 0;
+  if ((st = read_err(b, &err)) != YS_OK) return st;
+  std::vector<ys::PcgCloth> pc(b->ncloth);
+  YS_CUDA(cudaMemcpyAsync(pc.data(), b->so.pc, sizeof(ys::PcgCloth) * b->ncloth, cudaMemcpyDeviceToHost, s));
+  YS_CUDA(cudaStreamSynchronize(s));
+  L.solves += 1;
+  bool redo = err != 0;
+  for (int c = 0; c < b->ncloth; ++c)
+    if (!(pc[c].status & 1) && (pc[c].status & 4)) redo = true;
+  if (redo) {
+    // Jacobi-PCG for the whole batch (a cloth that converged keeps an equally
+    // valid solution, but one solve keeps the batch's bookkeeping uniform)
+    L.fallbacks += 1;
+    if (err) YS_CUDA(cudaMemsetAsync(L.g.err, 0, sizeof(int), s));
+    return solve_impl(b, v, opts, stats);
+  }
+  ys_status ret = YS_OK;
+  for (int c = 0; c < b->ncloth; ++c) {
+    if (pc[c].status & 1) ret = YS_ERR_NONFINITE;
+    if (stats) {
+      stats[c].ok = (pc[c].status & 3) == 0;
+      stats[c].cg_iterations = pc[c].iters;
+      stats[c].cg_error = pc[c].bb > 0 ? std::sqrt(pc[c].rr / pc[c].bb) : 0.0;
+      stats[c].hit_maxiter = 0;
+    }
+  }
+  return ret;
+}
+
+uint64_t splitmix(uint64_t& x) {
+  uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t ys_gnn_param_count(void) { return ys::kGParams; }
+
+ys_status ys_gnn_create(int32_t device, uint64_t seed, ys_gnn** out) {
+  if (!out) return fail(YS_ERR_ARG, "null output");
+  YS_CUDA(cudaSetDevice(device));
+  ys_gnn* g = new ys_gnn();
+  g->device = device;
+  ys::GnnNet& n = g->net;
+  cudaError_t e = g->alloc(&n.w, ys::kGParams);
+  if (e == cudaSuccess) e = g->alloc(&n.W0, (size_t)ys::kGHid * ys::kGIn);
+  if (e == cudaSuccess) e = g->alloc(&n.Wl, (size_t)ys::kGLayers * ys::kGHid * ys::kGMsg);
+  if (e == cudaSuccess) e = g->alloc(&n.Wh, (size_t)ys::kGOut * ys::kGHid);
+  if (e == cudaSuccess) e = g->alloc(&n.WlT, (size_t)ys::kGLayers * ys::kGHid * ys::kGMsg);
+  if (e == cudaSuccess) e = g->alloc(&n.WhT, (size_t)ys::kGOut * ys::kGHid);
+  if (e == cudaSuccess) e = g->alloc(&g->m, ys::kGParams);
+  if (e == cudaSuccess) e = g->alloc(&g->vv, ys::kGParams);
+  if (e != cudaSuccess) {
+    delete g;
+    return fail(YS_ERR_CUDA, std::string("ys_gnn_create: ") + cudaGetErrorString(e));
+  }
+  // uniform fan-in/fan-out initialisation; the output head starts at zero so
+  // an untrained network is the analytic approximate inverse
+  std::vector<float> w(ys::kGParams, 0.f);
+  uint64_t st = seed;
+  auto fill = [&](int off, int rows, int cols, double scale) {
+    const double bound = scale * std::sqrt(6.0 / (rows + cols));
+    for (int i = 0; i < rows * cols; ++i) {
+      const double u = (double)(splitmix(st) >> 11) * (1.0 / 9007199254740992.0);
+      w[off + i] = (float)((2.0 * u - 1.0) * bound);
+    }
+  };
+  fill(ys::kPW0, ys::kGHid, ys::kGIn, 1.0);
+  for (int l = 0; l < ys::kGLayers; ++l) fill(ys::kPW(l), ys::kGHid, ys::kGMsg, 0.5);
+  e = cudaMemcpy(n.w, w.data(), sizeof(float) * ys::kGParams, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(g->m, 0, sizeof(float) * ys::kGParams);
+  if (e == cudaSuccess) e = cudaMemset(g->vv, 0, sizeof(float) * ys::kGParams);
+  if (e == cudaSuccess) {
+    ys::gnn_refresh_bf16(n, 0);
+    e = cudaDeviceSynchronize();
+  }
+  if (e != cudaSuccess) {
+    delete g;
+    return fail(YS_ERR_CUDA, std::string("ys_gnn_create: ") + cudaGetErrorString(e));
+  }
+  *out = g;
+  return YS_OK;
+}
+
+void ys_gnn_destroy(ys_gnn* g) {
+  if (!g) return;
+  cudaSetDevice(g->device);
+  cudaDeviceSynchronize();
+  delete g;
+}
+
+ys_status ys_gnn_get_params(ys_gnn* g, float* out) {
+  if (!g || !out) return fail(YS_ERR_ARG, "bad argument");
+  YS_CUDA(cudaSetDevice(g->device));
+  YS_CUDA(cudaDeviceSynchronize());
+  YS_CUDA(cudaMemcpy(out, g->net.w, sizeof(float) * ys::kGParams, cudaMemcpyDeviceToHost));
+  return YS_OK;
+}
+
+ys_status ys_gnn_set_params(ys_gnn* g, const float* in) {
+  if (!g || !in) return fail(YS_ERR_ARG, "bad argument");
+  YS_CUDA(cudaSetDevice(g->device));
+  YS_CUDA(cudaDeviceSynchronize());
+  YS_CUDA(cudaMemcpy(g->net.w, in, sizeof(float) * ys::kGParams, cudaMemcpyHostToDevice));
+  YS_CUDA(cudaMemset(g->m, 0, sizeof(float) * ys::kGParams));
+  YS_CUDA(cudaMemset(g->vv, 0, sizeof(float) * ys::kGParams));
+  g->step = 0;
+  ys::gnn_refresh_bf16(g->net, 0);
+  YS_CUDA(cudaDeviceSynchronize());
+  return YS_OK;
+}
+
+ys_status ys_gnn_loss_grad(ys_gnn* g, ys_batch* b, const float* probes, uint64_t seed, double* loss, float* grad,
+                           float* outputs, float* gblocks) {
+  if (!g || !b) return fail(YS_ERR_ARG, "null handle");
+  if (g->device != b->device) return fail(YS_ERR_ARG, "network and batch on different devices");
+  if (!b->has_system) return fail(YS_ERR_ARG, "no assembled system");
+  YS_CUDA(cudaSetDevice(b->device));
+  ys_status st = learn_ensure(b);
+  if (st != YS_OK) return st;
+  YS_CUDA(cudaStreamSynchronize(0));
+  if ((st = learn_infer(b, g)) != YS_OK) return st;
+  ys::GnnBufs& G = b->learn.g;
+  const int nt = b->ntot;
+  if (probes) {
+    std::vector<float> t(5 * (size_t)nt);
+    for (int n = 0; n < nt; ++n)
+      for (int c = 0; c < 5; ++c) t[(size_t)c * nt + n] = probes[(size_t)n * 5 + c];
+    YS_CUDA(cudaMemcpyAsync(G.vec, t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice, b->stream));
+    YS_CUDA(cudaStreamSynchronize(b->stream));
+  }
+  ys::gnn_loss_grad(b->v, g->net, G, seed, probes != nullptr, b->stream);
+  YS_CUDA(cudaGetLastError());
+  int err = 0;
+  if ((st = read_err(b, &err)) != YS_OK) return st;
+  if (err) {
+    cudaMemsetAsync(G.err, 0, sizeof(int), b->stream);
+    return fail(YS_ERR_CUDA, "tensor-core wait ran out");
+  }
+  if (loss) YS_CUDA(cudaMemcpy(loss, G.lpart + 2 * G.nlblk, sizeof(double), cudaMemcpyDeviceToHost));
+  if (grad) YS_CUDA(cudaMemcpy(grad, G.grad, sizeof(float) * ys::kGParams, cudaMemcpyDeviceToHost));
+  if (outputs) YS_CUDA(cudaMemcpy(outputs, G.o, sizeof(float) * ys::kGOut * nt, cudaMemcpyDeviceToHost));
+  if (gblocks) {
+    std::vector<float> t(125 * (size_t)nt);
+    YS_CUDA(cudaMemcpy(t.data(), G.G, sizeof(float) * t.size(), cudaMemcpyDeviceToHost));
+    for (int n = 0; n < nt; ++n)
+      for (int k = 0; k < 125; ++k) gblocks[(size_t)n * 125 + k] = t[(size_t)k * nt + n];
+  }
+  return YS_OK;
+}
+
+ys_status ys_gnn_train_step(ys_gnn* g, ys_batch* b, uint64_t seed, float lr, double* loss) {
+  if (!g || !b || !(lr > 0)) return fail(YS_ERR_ARG, "bad argument");
+  if (g->device != b->device) return fail(YS_ERR_ARG, "network and batch on different devices");
+  if (!b->has_system) return fail(YS_ERR_ARG, "no assembled system");
+  YS_CUDA(cudaSetDevice(b->device));
+  ys_status st = learn_ensure(b);
+  if (st != YS_OK) return st;
+  if ((st = learn_infer(b, g)) != YS_OK) return st;
+  ys::GnnBufs& G = b->learn.g;
+  ys::gnn_loss_grad(b->v, g->net, G, seed, false, b->stream);
+  g->step += 1;
+  ys::gnn_adam(g->net, G, g->m, g->vv, lr, g->step, b->stream);
+  YS_CUDA(cudaGetLastError());
+  int err = 0;
+  if ((st = read_err(b, &err)) != YS_OK) return st;
+  if (err) {
+    cudaMemsetAsync(G.err, 0, sizeof(int), b->stream);
+    return fail(YS_ERR_CUDA, "tensor-core wait ran out");
+  }
+  if (loss) {
+    YS_CUDA(cudaMemcpyAsync(loss, G.lpart + 2 * G.nlblk, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    YS_CUDA(cudaStreamSynchronize(b->stream));
+  }
+  return YS_OK;
+}
+
+ys_status ys_set_preconditioner(ys_batch* b, int32_t kind, ys_gnn* g) {
+  if (!b || (kind != YS_PREC_JACOBI && kind != YS_PREC_LEARNED)) return fail(YS_ERR_ARG, "bad argument");
+  if (kind == YS_PREC_LEARNED && (!g || g->device != b->device)) return fail(YS_ERR_ARG, "bad network");
+  b->learn.kind = kind;
+  b->learn.net = kind == YS_PREC_LEARNED ? g : nullptr;
+  return YS_OK;
+}
+
+ys_status ys_precond_info(ys_batch* b, int64_t* solves, int64_t* fallbacks) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  if (solves) *solves = b->learn.solves;
+  if (fallbacks) *fallbacks = b->learn.fallbacks;
+  return YS_OK;
+}
+
+ys_status ys_get_system_slots(ys_batch* b, double* slots, double* rhs) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  if (!b->has_system) return fail(YS_ERR_ARG, "no assembled system");
+  YS_CUDA(cudaSetDevice(b->device));
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  if (slots) YS_CUDA(cudaMemcpy(slots, b->v.A, sizeof(double) * ys::YS_NUM_SLOTS * b->ntot, cudaMemcpyDeviceToHost));
+  if (rhs) YS_CUDA(cudaMemcpy(rhs, b->v.B, sizeof(double) * 5 * b->ntot, cudaMemcpyDeviceToHost));
+  return YS_OK;
+}
+
+ys_status ys_tc_gemm_bf16(int32_t device, const uint16_t* A, const uint16_t* B, float* C, int32_t M, int32_t N,
+                          int32_t K) {
+  if (!A || !B || !C || M < 1 || (N != 64 && N != 128 && (N <= 0 || N % 64)) || K < 64 || K % 64)
+    return fail(YS_ERR_ARG, "bad argument");
+  YS_CUDA(cudaSetDevice(device));
+  void *dA = nullptr, *dB = nullptr, *dC = nullptr, *dE = nullptr;
+  cudaError_t e = cudaMalloc(&dA, 2 * (size_t)M * K);
+  if (e == cudaSuccess) e = cudaMalloc(&dB, 2 * (size_t)N * K);
+  if (e == cudaSuccess) e = cudaMalloc(&dC, 4 * (size_t)M * N);
+  if (e == cudaSuccess) e = cudaMalloc(&dE, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(dA, A, 2 * (size_t)M * K, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dB, B, 2 * (size_t)N * K, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(dE, 0, sizeof(int));
+  int err = 0;
+  if (e == cudaSuccess) {
+    ys::tc_gemm_bf16(static_cast<const __nv_bfloat16*>(dA), static_cast<const __nv_bfloat16*>(dB),
+                     static_cast<float*>(dC), M, N, K, static_cast<int*>(dE), 0);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(C, dC, 4 * (size_t)M * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&err, dE, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dC);
+  cudaFree(dE);
+  if (e != cudaSuccess) return fail(YS_ERR_CUDA, std::string("ys_tc_gemm_bf16: ") + cudaGetErrorString(e));
+  if (err) return fail(YS_ERR_CUDA, "tensor-core wait ran out");
+  return YS_OK;
 }
 
 }  // extern "C"

@@ -1,0 +1,181 @@
+"""Learned preconditioner for the implicit step's linear systems.
+
+The reference solves every step with Eigen's Jacobi-preconditioned conjugate
+gradient (src/Solvers.cpp:3-31); that stays the default and the fallback. This
+module adds a graph network over the crossing graph that reads each assembled
+system and emits the blocks of G in M^-1 = G^T G (see ys_gnn.cuh for the
+network and include/yarnsim.h for the C ABI). Training runs on the GPU with the
+library's own BF16 tensor-core forward and backward kernels, on systems the
+simulator generates from seeded batches of cloths like the plain method's
+workloads: sizes 5..50, plain / twill / satin weaves, per-line material within
++-20 % of (rho 1e-3, Y 1e3, B 1e-5), blended warp / weft sets 1.5-3x apart,
+S and mu within +-20 %, gravity and wind.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import _native as N
+from .cloth import ClothBatch, ClothSpec
+
+PARAMS_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "precond_params.npy")
+
+
+def param_count() -> int:
+    return int(N.load().ys_gnn_param_count())
+
+
+class LearnedPreconditioner:
+    """The network (FP32 master parameters on the device, BF16 copies for the
+    tensor cores, Adam state)."""
+
+    def __init__(self, seed: int = 0, device: int = 0, params: Optional[np.ndarray] = None):
+        h = ctypes.c_void_p()
+        N.check(N.load().ys_gnn_create(int(device), int(seed), ctypes.byref(h)), "ys_gnn_create")
+        self._h = h
+        self.device = int(device)
+        if params is not None:
+            self.set_params(params)
+
+    @classmethod
+    def pretrained(cls, device: int = 0, path: str = PARAMS_FILE) -> "LearnedPreconditioner":
+        """The parameters shipped with the package (trained by train())."""
+        return cls(device=device, params=np.load(path))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.load().ys_gnn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(param_count(), np.float32)
+        N.check(N.load().ys_gnn_get_params(self._h, ctypes.c_void_p(out.ctypes.data)), "ys_gnn_get_params")
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        if p.shape != (param_count(),):
+            raise ValueError("expected %d parameters" % param_count())
+        N.check(N.load().ys_gnn_set_params(self._h, ctypes.c_void_p(p.ctypes.data)), "ys_gnn_set_params")
+
+    def save(self, path: str):
+        np.save(path, self.params())
+
+    def train_step(self, batch: ClothBatch, seed: int, lr: float) -> float:
+        """One Adam step on the systems `batch` assembled last; returns the loss
+        before the step."""
+        loss = ctypes.c_double()
+        N.check(N.load().ys_gnn_train_step(self._h, batch._h, int(seed), float(lr), ctypes.byref(loss)),
+                "ys_gnn_train_step")
+        return loss.value
+
+    def loss_grad(self, batch: ClothBatch, probes: Optional[np.ndarray] = None, seed: int = 1) -> dict:
+        """Loss, parameter gradient, network outputs [n][128] and G blocks
+        [n][125] for the batch's last system (no update)."""
+        n = batch.total_nodes
+        loss = ctypes.c_double()
+        grad = np.zeros(param_count(), np.float32)
+        out = np.zeros((n, 128), np.float32)
+        gb = np.zeros((n, 125), np.float32)
+        pr = None
+        if probes is not None:
+            pr = np.ascontiguousarray(probes, np.float32)
+            if pr.shape != (n, 5):
+                raise ValueError("probes must be [total_nodes, 5]")
+        N.check(N.load().ys_gnn_loss_grad(self._h, batch._h, ctypes.c_void_p(pr.ctypes.data) if pr is not None else None,
+                                          int(seed), ctypes.byref(loss), ctypes.c_void_p(grad.ctypes.data),
+                                          ctypes.c_void_p(out.ctypes.data), ctypes.c_void_p(gb.ctypes.data)),
+                "ys_gnn_loss_grad")
+        return dict(loss=loss.value, grad=grad, outputs=out, G=gb)
+
+
+def training_specs(rng: np.random.Generator, n_cloths: int, min_side: int = 5, max_side: int = 50):
+    """Seeded cloths of the plain method's workloads (see the module doc)."""
+    base = np.array([1e-3, 1e3, 1e-5])
+    specs = []
+    for _ in range(n_cloths):
+        W = int(rng.integers(min_side, max_side + 1))
+        blend = rng.random() < 0.5
+        scale = np.ones(3)
+        if blend:
+            scale = 1.5 + 1.5 * rng.random(3)
+            scale = np.where(rng.random(3) < 0.5, scale, 1.0 / scale)
+
+        def lines(n, odd_scale):
+            out = base * (1.0 + 0.2 * (2.0 * rng.random((n, 3)) - 1.0))
+            if blend:
+                out[1::2] *= odd_scale
+            return out
+        wind = (0.0, float(2.0 * rng.random() - 1.0), 0.0)
+        specs.append(ClothSpec(width=W, length=W, warp=lines(W, scale), weft=lines(W, scale), height=0.05, L=1e-3,
+                               R=1e-4, pose=int(rng.integers(0, 2)), weave=int(rng.integers(0, 3)),
+                               mu=0.3 * (1 + 0.2 * (2 * rng.random() - 1)),
+                               S=1e-4 * (1 + 0.2 * (2 * rng.random() - 1)), G=(0.0, 0.0, 9.8), wind_vel=wind,
+                               wind_density=1.0, wind_drag=0.5, handles=[(0, 0), (W - 1, 0)]))
+    return specs
+
+
+def train(net: LearnedPreconditioner, systems: int = 20000, cloths_per_batch: int = 64, steps_per_batch: int = 40,
+          lr: float = 1e-3, seed: int = 0, h: float = 1e-3, log=None) -> list:
+    """Trains on `systems` linear systems the simulator generates: batches of
+    `cloths_per_batch` seeded cloths are stepped with Jacobi-PCG for
+    `steps_per_batch` steps, and every step's systems (one per cloth) feed one
+    Adam step. The rate decays by cosine to 5 % of lr. Returns the loss
+    history."""
+    rng = np.random.default_rng(seed)
+    total_steps = max(1, math.ceil(systems / cloths_per_batch))
+    hist = []
+    k = 0
+    while k < total_steps:
+        batch = ClothBatch(training_specs(rng, cloths_per_batch), device=net.device)
+        for _ in range(steps_per_batch):
+            if k >= total_steps:
+                break
+            st = batch.step(h, tol=1e-10)
+            if not all(s["ok"] for s in st):
+                break
+            rate = lr * (0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * k / total_steps)))
+            loss = net.train_step(batch, seed=(seed << 20) + k + 1, lr=rate)
+            hist.append(loss)
+            if log is not None and k % 50 == 0:
+                log("step %d/%d loss %.5f" % (k, total_steps, loss))
+            k += 1
+        batch.close()
+    return hist
+
+
+def main(argv=None):
+    """Trains the shipped parameters: python -m <package>.precond --out FILE"""
+    import argparse
+    import time
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--systems", type=int, default=20000)
+    ap.add_argument("--cloths", type=int, default=64)
+    ap.add_argument("--steps-per-batch", type=int, default=40)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--out", default=PARAMS_FILE)
+    a = ap.parse_args(argv)
+    net = LearnedPreconditioner(seed=a.seed)
+    t0 = time.time()
+    hist = train(net, systems=a.systems, cloths_per_batch=a.cloths, steps_per_batch=a.steps_per_batch, lr=a.lr,
+                 seed=a.seed, log=print)
+    print("trained on %d systems in %.1f s; loss %.5f -> %.5f" % (len(hist) * a.cloths, time.time() - t0,
+                                                                   float(np.mean(hist[:10])), float(np.mean(hist[-10:]))))
+    net.save(a.out)
+    np.save(os.path.splitext(a.out)[0] + "_loss.npy", np.asarray(hist))
+
+
+if __name__ == "__main__":
+    main()

@@ -78,7 +78,8 @@ typedef struct {
 typedef struct {
   double tol;         /* relative residual |r| / |b|; <= 0: DBL_EPSILON (Eigen default) */
   int32_t maxiter;    /* per cloth; < 0: 2 * system dimension (Eigen default) */
-  int32_t check_every;/* iterations between device->host convergence polls; <= 0: 16 */
+  int32_t check_every;/* iterations between convergence checks; <= 0: the batch's default
+                         (16, or what ys_autotune chose) */
 } ys_solve_opts;
 
 typedef struct {
@@ -141,6 +142,17 @@ ys_status ys_use_graphs(ys_batch *b, int32_t enable);
 /* ys_step through the graph regardless of ys_use_graphs. */
 ys_status ys_step_graphed(ys_batch *b, double h, const double *ext_force, int32_t flags, const ys_solve_opts *opts,
                           ys_cloth_stats *stats);
+/* Step schedule (no counterpart in the reference). */
+typedef struct ys_schedule {
+  int32_t graphs;      /* 1: one CUDA graph per step (ys_use_graphs) */
+  int32_t check_every; /* PCG iterations between convergence checks */
+  double ms_per_step;  /* measured time of the chosen schedule */
+} ys_schedule;
+/* Times every schedule (graph or launch by launch x check_every in
+ * {2, 4, 8, 16, 32}) over `steps` steps of size h without an external force,
+ * each from the batch's current state, which is restored afterwards, and makes
+ * the fastest the batch's default. All schedules give bit-identical states. */
+ys_status ys_autotune(ys_batch *b, double h, const ys_solve_opts *opts, int32_t steps, ys_schedule *best);
 /* y = A x with the assembled matrices (node layout [total_nodes][5]). */
 ys_status ys_apply_system(ys_batch *b, const double *x, double *y, int32_t flags);
 /* y = A x like ys_apply_system, for callers that must not allocate at call
@@ -207,7 +219,9 @@ enum {
   YS_PROF_DIR = 10,      /* stop test, p update */
   YS_PROF_UPDATE = 11,   /* Cloth::update */
   YS_PROF_MISC = 12,     /* bookkeeping */
-  YS_PROF_KINDS = 13
+  YS_PROF_GNN = 13,      /* learned preconditioner: features, network, G blocks */
+  YS_PROF_PREC = 14,     /* learned preconditioner: z = G^T G r */
+  YS_PROF_KINDS = 15
 };
 /* enable = 1 brackets every launch with CUDA events on the handle's stream
  * (adds a little host overhead); the totals accumulate until read. */
@@ -258,6 +272,49 @@ ys_status ys_collider_get_pairs(ys_collider *c, int32_t *pairs, int64_t cap);
 /* Narrow phase over the pair list; n_impacts receives the count. */
 ys_status ys_collider_find_impacts(ys_collider *c, int64_t *n_impacts);
 ys_status ys_collider_get_impacts(ys_collider *c, ys_impact *impacts, int64_t cap);
+
+/* ---- learned preconditioner (no counterpart in the reference: its solve is
+ * Eigen's Jacobi-PCG, src/Solvers.cpp:3-31, which stays the default and the
+ * fallback). A graph network over the crossing graph reads each assembled
+ * system and emits the blocks of G in M^-1 = G^T G = L^-T (I + N)^T (I + N) L^-1
+ * (L: Cholesky factor of each node's 5 x 5 diagonal block; N: one 5 x 5 block
+ * per node and per yarn neighbour). The conjugate-gradient iteration keeps
+ * FP64 and the same stopping rule |r| <= tol |b|; M^-1 is applied in FP32 with
+ * the flexible (Polak-Ribiere) direction update. */
+typedef struct ys_gnn ys_gnn;
+enum { YS_PREC_JACOBI = 0, YS_PREC_LEARNED = 1 };
+/* number of FP32 parameters (packed: W0 [64][128], b0 [64], 3 x (W [64][320],
+ * b [64]), Wh [128][64], bh [128]) */
+int32_t ys_gnn_param_count(void);
+/* a network with seeded initial weights (output head zero: the analytic
+ * first-order approximate inverse N = -E / 2 on the neighbour blocks) */
+ys_status ys_gnn_create(int32_t device, uint64_t seed, ys_gnn **out);
+void ys_gnn_destroy(ys_gnn *g);
+ys_status ys_gnn_get_params(ys_gnn *g, float *out);
+/* also resets the optimiser state */
+ys_status ys_gnn_set_params(ys_gnn *g, const float *in);
+/* One Adam step (rate lr) on the loss |(G A G^T - I) w|^2 / |w|^2 over the
+ * systems the batch assembled last (its ys_assemble or ys_step), Rademacher
+ * probes w drawn from seed; *loss receives the loss before the step. */
+ys_status ys_gnn_train_step(ys_gnn *g, ys_batch *b, uint64_t seed, float lr, double *loss);
+/* Loss and gradient without an update (probes [total_nodes][5] host, or NULL
+ * for seeded probes); outputs [total_nodes][128] network outputs, gblocks
+ * [total_nodes][125] blocks of G (self, left, right, down, up; row-major
+ * 5 x 5); any output may be NULL. */
+ys_status ys_gnn_loss_grad(ys_gnn *g, ys_batch *b, const float *probes, uint64_t seed, double *loss, float *grad,
+                           float *outputs, float *gblocks);
+/* kind YS_PREC_JACOBI (default) or YS_PREC_LEARNED with network g; the batch
+ * borrows g, which must outlive its use. Learned steps run launch by launch. */
+ys_status ys_set_preconditioner(ys_batch *b, int32_t kind, ys_gnn *g);
+/* learned solves so far and how many fell back to Jacobi-PCG */
+ys_status ys_precond_info(ys_batch *b, int64_t *solves, int64_t *fallbacks);
+/* the last assembled system's raw coefficient slots [159][total_nodes] and
+ * right-hand side [5][total_nodes] (host; either may be NULL) */
+ys_status ys_get_system_slots(ys_batch *b, double *slots, double *rhs);
+/* C [M][N] = A [M][K] B [N][K]^T on the tensor cores (BF16 bits in, FP32
+ * out; N a multiple of 64, K of 64): a self-test of the network's GEMM. */
+ys_status ys_tc_gemm_bf16(int32_t device, const uint16_t *A, const uint16_t *B, float *C, int32_t M, int32_t N,
+                          int32_t K);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,309 @@
+"""CPU oracle of the learned preconditioner (test infrastructure only: the
+product runs the CUDA kernels of ys_gnn.cu and never imports this file).
+
+The learned preconditioner has no counterpart in the reference (its solve is
+Eigen's Jacobi-PCG, src/Solvers.cpp:3-31), so this oracle restates the
+library's own definition independently of its kernels: the system features,
+the graph network (BF16 operands rounded where the tensor cores read them),
+the blocks of G, and the stochastic Frobenius loss
+|(G A G^T - I) w|^2 / |w|^2, in float64 PyTorch on the CPU; its parameter
+gradient comes from torch.autograd, not from the hand-written backward the GPU
+runs. Rounding to BF16 uses straight-through estimators (the value is rounded,
+the derivative is the identity), which is what the GPU's BF16 operands amount
+to.
+
+Inputs: the system's coefficient slots [159, n] (ys_get_system_slots), the
+batch topology (per-node cloth width / height, u, v, flags) and the packed
+FP32 parameter vector.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+# slot layout of one row block (the library's stencil storage)
+SLOT_LL, SLOT_LE_SELF, SLOT_EL_SELF, SLOT_EE_SELF = 0, 117, 123, 129
+SLOT_LE_NBR, SLOT_EL_NBR, SLOT_EE_NBR = 131, 143, 155
+STENCIL = [(0, 0), (-1, 0), (1, 0), (0, -1), (0, 1), (-2, 0), (2, 0), (0, -2), (0, 2), (-1, -1), (1, -1), (-1, 1),
+           (1, 1)]
+YARN_NBR = [(-1, 0), (1, 0), (0, -1), (0, 1)]  # left, right, down, up
+IN, HID, MSG, OUT, LAYERS, OUT_SCALE = 128, 64, 320, 128, 3, 0.1
+P_W0 = 0
+P_B0 = P_W0 + HID * IN
+P_L0 = P_B0 + HID
+P_LSTRIDE = HID * MSG + HID
+P_WH = P_L0 + LAYERS * P_LSTRIDE
+P_BH = P_WH + OUT * HID
+N_PARAMS = P_BH + OUT
+
+
+def p_w(l):
+    return P_L0 + l * P_LSTRIDE
+
+
+def p_b(l):
+    return p_w(l) + HID * MSG
+
+
+class Topology:
+    """Node order of a batch: cloth after cloth, node u + v * W."""
+
+    def __init__(self, sizes, handles=None, pose_flags=None):
+        us, vs, Ws, Hs, fixed = [], [], [], [], []
+        for c, (W, H) in enumerate(sizes):
+            hs = set(map(tuple, handles[c])) if handles is not None else set()
+            for v in range(H):
+                for u in range(W):
+                    us.append(u)
+                    vs.append(v)
+                    Ws.append(W)
+                    Hs.append(H)
+                    fixed.append((u, v) in hs)
+        self.u = np.array(us)
+        self.v = np.array(vs)
+        self.W = np.array(Ws)
+        self.H = np.array(Hs)
+        self.fixed = np.array(fixed)
+        self.n = len(us)
+        self.interior = (self.u > 0) & (self.u < self.W - 1) & (self.v > 0) & (self.v < self.H - 1)
+        idx = np.arange(self.n)
+
+        def nb(du, dv):
+            ok = (self.u + du >= 0) & (self.u + du < self.W) & (self.v + dv >= 0) & (self.v + dv < self.H)
+            return np.where(ok, idx + du + dv * self.W, -1)
+        self.stencil = np.stack([nb(du, dv) for du, dv in STENCIL], 1)  # [n, 13]
+        self.nbr = np.stack([nb(du, dv) for du, dv in YARN_NBR], 1)     # [n, 4]
+
+
+def bf16(x):
+    """Round to BF16 (nearest even), straight-through for the gradient."""
+    return x + (x.to(torch.bfloat16).to(x.dtype) - x).detach()
+
+
+def f32(x):
+    return x.to(torch.float32).to(torch.float64)
+
+
+def diag_blocks(slots):
+    n = slots.shape[1]
+    D = np.zeros((n, 5, 5))
+    for r in range(3):
+        for c in range(3):
+            D[:, r, c] = slots[SLOT_LL + 3 * r + c]
+        for k in range(2):
+            D[:, r, 3 + k] = slots[SLOT_LE_SELF + 2 * r + k]
+            D[:, 3 + k, r] = slots[SLOT_EL_SELF + 3 * k + r]
+    D[:, 3, 3] = slots[SLOT_EE_SELF]
+    D[:, 4, 4] = slots[SLOT_EE_SELF + 1]
+    return D
+
+
+def nbr_block(slots, d):
+    """[n, 5, 5] block A(i, j) of yarn neighbour d."""
+    n = slots.shape[1]
+    B = np.zeros((n, 5, 5))
+    s = d + 1
+    k = 0 if d < 2 else 1
+    for r in range(3):
+        for c in range(3):
+            B[:, r, c] = slots[SLOT_LL + 9 * s + 3 * r + c]
+        B[:, r, 3 + k] = slots[SLOT_LE_NBR + 3 * d + r]
+        B[:, 3 + k, r] = slots[SLOT_EL_NBR + 3 * d + r]
+    B[:, 3 + k, 3 + k] = slots[SLOT_EE_NBR + d]
+    return B
+
+
+def block_factor(slots):
+    """L^-1 [n, 5, 5] (FP32 values) and the factorisation flags."""
+    D = diag_blocks(slots)
+    S = 0.5 * (D + np.transpose(D, (0, 2, 1)))
+    n = len(S)
+    Linv = np.zeros((n, 5, 5))
+    ok = np.ones(n, bool)
+    for i in range(n):
+        try:
+            L = np.linalg.cholesky(S[i])
+            if not np.all(np.isfinite(L)):
+                raise np.linalg.LinAlgError
+        except np.linalg.LinAlgError:
+            ok[i] = False
+            d = np.abs(np.diag(D[i]))
+            L = np.diag(np.where((d > 0) & np.isfinite(d), np.sqrt(d), 1.0))
+        Linv[i] = np.linalg.inv(L)
+        Linv[i] = np.tril(Linv[i])
+    return Linv.astype(np.float32).astype(np.float64), ok
+
+
+def features(slots, topo: Topology, Linv, ok):
+    """f [n, 128] (before BF16 rounding) and the scaled neighbour blocks E [n, 4, 5, 5]."""
+    n = topo.n
+    f = np.zeros((n, IN))
+    E = np.zeros((n, 4, 5, 5))
+    sl32 = slots.astype(np.float32).astype(np.float64)
+    for d in range(4):
+        j = topo.nbr[:, d]
+        B = nbr_block(sl32, d)
+        m = j >= 0
+        Lj = Linv[np.where(m, j, 0)]
+        Ed = Linv @ B @ np.transpose(Lj, (0, 2, 1))
+        Ed[~m] = 0.0
+        E[:, d] = Ed.astype(np.float32).astype(np.float64)
+        f[:, 25 * d:25 * d + 25] = E[:, d].reshape(n, 25)
+    for s in range(5, 13):
+        j = topo.stencil[:, s]
+        m = j >= 0
+        LL = np.stack([np.stack([sl32[SLOT_LL + 9 * s + 3 * r + c] for c in range(3)], -1) for r in range(3)], -2)
+        Lj = Linv[np.where(m, j, 0)][:, :3, :3]
+        T = Linv[:, :3, :3] @ LL @ np.transpose(Lj, (0, 2, 1))
+        nrm = np.sqrt((T ** 2).sum((1, 2)))
+        f[:, 100 + s - 5] = np.where(m, nrm, 0.0)
+    f[:, 108] = (~ok).astype(float)
+    f[:, 109] = topo.interior.astype(float)
+    f[:, 110] = topo.fixed.astype(float)
+    f[:, 111] = ((topo.u == 0) | (topo.u == topo.W - 1)).astype(float)
+    f[:, 112] = ((topo.v == 0) | (topo.v == topo.H - 1)).astype(float)
+    return f, E
+
+
+def network(params, f, topo: Topology):
+    """Outputs o [n, 128] (torch, differentiable in params)."""
+    nbr = torch.as_tensor(topo.nbr)
+    W0 = bf16(params[P_W0:P_B0].view(HID, IN))
+    h = torch.relu(bf16(f) @ W0.T + params[P_B0:P_L0])
+    for l in range(LAYERS):
+        hb = bf16(h)
+        zero = torch.zeros(1, HID, dtype=h.dtype)
+        hz = torch.cat([hb, zero], 0)
+        msg = torch.cat([hb] + [hz[torch.where(nbr[:, d] >= 0, nbr[:, d], topo.n)] for d in range(4)], 1)
+        Wl = bf16(params[p_w(l):p_b(l)].view(HID, MSG))
+        h = h + torch.relu(msg @ Wl.T + params[p_b(l):p_b(l) + HID])
+    Wh = bf16(params[P_WH:P_BH].view(OUT, HID))
+    return bf16(h) @ Wh.T + params[P_BH:P_BH + OUT]
+
+
+def n_blocks(o, E, topo: Topology):
+    """N [n, 5, 5, 5] (block b: self, left, right, down, up)."""
+    n = topo.n
+    Ns = [OUT_SCALE * o[:, 0:25].reshape(n, 5, 5)]
+    Et = torch.as_tensor(E)
+    for d in range(4):
+        m = torch.as_tensor(topo.nbr[:, d] >= 0, dtype=o.dtype).view(n, 1, 1)
+        Ns.append(m * (OUT_SCALE * o[:, 25 + 25 * d:50 + 25 * d].reshape(n, 5, 5) - 0.5 * Et[:, d]))
+    return torch.stack(Ns, 1)
+
+
+def g_blocks(Nb, Linv, topo: Topology):
+    n = topo.n
+    Lt = torch.as_tensor(Linv)
+    eye = torch.eye(5, dtype=Nb.dtype)
+    out = [(eye + Nb[:, 0]) @ Lt]
+    for d in range(4):
+        j = topo.nbr[:, d]
+        Lj = Lt[torch.as_tensor(np.where(j >= 0, j, 0))]
+        out.append(Nb[:, d + 1] @ Lj)
+    return torch.stack(out, 1)
+
+
+def apply_rows(Nb, x, topo: Topology):
+    """y_i = x_i + sum_b N_ib x_src(b); x [n, 5]."""
+    n = topo.n
+    xz = torch.cat([x, torch.zeros(1, 5, dtype=x.dtype)], 0)
+    y = x + torch.einsum("nrc,nc->nr", Nb[:, 0], x)
+    for d in range(4):
+        j = torch.as_tensor(np.where(topo.nbr[:, d] >= 0, topo.nbr[:, d], n))
+        y = y + torch.einsum("nrc,nc->nr", Nb[:, d + 1], xz[j])
+    return y
+
+
+def apply_cols(Nb, x, topo: Topology):
+    """z_j = x_j + sum over blocks N_ib with src(b) = j of N_ib^T x_i."""
+    n = topo.n
+    z = x + torch.einsum("nrc,nr->nc", Nb[:, 0], x)
+    for d in range(4):
+        j = topo.nbr[:, d]
+        m = j >= 0
+        contrib = torch.einsum("nrc,nr->nc", Nb[:, d + 1], x)
+        z = z.index_add(0, torch.as_tensor(j[m]), contrib[torch.as_tensor(m)])
+    return z
+
+
+def spmv(slots, x, topo: Topology):
+    """y = A x with the stencil slots (FP32 coefficient values, as the GPU reads them)."""
+    S = torch.as_tensor(slots.astype(np.float32).astype(np.float64))
+    n = topo.n
+    xz = torch.cat([x, torch.zeros(1, 5, dtype=x.dtype)], 0)
+    yl = torch.zeros(n, 3, dtype=x.dtype)
+    for s in range(13):
+        j = torch.as_tensor(np.where(topo.stencil[:, s] >= 0, topo.stencil[:, s], n))
+        xj = xz[j]
+        for r in range(3):
+            for c in range(3):
+                yl[:, r] = yl[:, r] + S[SLOT_LL + 9 * s + 3 * r + c] * xj[:, c]
+    ye = torch.zeros(n, 2, dtype=x.dtype)
+    for r in range(3):
+        for k in range(2):
+            yl[:, r] = yl[:, r] + S[SLOT_LE_SELF + 2 * r + k] * x[:, 3 + k]
+    for k in range(2):
+        ye[:, k] = S[SLOT_EE_SELF + k] * x[:, 3 + k]
+        for c in range(3):
+            ye[:, k] = ye[:, k] + S[SLOT_EL_SELF + 3 * k + c] * x[:, c]
+    for d in range(4):
+        k = 0 if d < 2 else 1
+        j = torch.as_tensor(np.where(topo.nbr[:, d] >= 0, topo.nbr[:, d], n))
+        xj = xz[j]
+        for r in range(3):
+            yl[:, r] = yl[:, r] + S[SLOT_LE_NBR + 3 * d + r] * xj[:, 3 + k]
+        ye[:, k] = ye[:, k] + S[SLOT_EE_NBR + d] * xj[:, 3 + k]
+        for c in range(3):
+            ye[:, k] = ye[:, k] + S[SLOT_EL_NBR + 3 * d + c] * xj[:, c]
+    return torch.cat([yl, ye], 1)
+
+
+def evaluate(slots, topo: Topology, params, probes):
+    """dict(loss, grad [N_PARAMS], o [n, 128], G [n, 125], f [n, 128])."""
+    Linv, ok = block_factor(slots)
+    f, E = features(slots, topo, Linv, ok)
+    p = torch.as_tensor(np.asarray(params, np.float64), dtype=torch.float64).requires_grad_(True)
+    o = network(p, torch.as_tensor(f), topo)
+    Nb = n_blocks(o, E, topo)
+    w = torch.as_tensor(np.asarray(probes, np.float64))
+    Lt = torch.as_tensor(Linv)
+    v = apply_cols(Nb, w, topo)
+    u = torch.einsum("nrc,nr->nc", Lt, v)          # L^-T v
+    t = spmv(slots, u, topo)
+    s = torch.einsum("nrc,nc->nr", Lt, t)          # L^-1 t
+    y = apply_rows(Nb, s, topo)
+    loss = ((y - w) ** 2).sum() / (w ** 2).sum()
+    loss.backward()
+    G = g_blocks(Nb.detach(), Linv, topo).reshape(topo.n, 125)
+    return dict(loss=float(loss.detach()), grad=p.grad.numpy().copy(), o=o.detach().numpy(), G=G.numpy(), f=f, E=E,
+                Linv=Linv, chol_ok=ok)
+
+
+def init_params(seed: int) -> np.ndarray:
+    """A random parameter vector with a non-zero head (for gradient checks)."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(N_PARAMS, np.float32)
+    p[P_W0:P_B0] = rng.uniform(-1, 1, HID * IN) * np.sqrt(6 / (HID + IN))
+    p[P_B0:P_L0] = 0.05 * rng.standard_normal(HID)
+    for l in range(LAYERS):
+        p[p_w(l):p_b(l)] = rng.uniform(-1, 1, HID * MSG) * 0.5 * np.sqrt(6 / (HID + MSG))
+        p[p_b(l):p_b(l) + HID] = 0.05 * rng.standard_normal(HID)
+    p[P_WH:P_BH] = rng.uniform(-1, 1, OUT * HID) * 0.3 * np.sqrt(6 / (OUT + HID))
+    p[P_BH:P_BH + OUT] = 0.05 * rng.standard_normal(OUT)
+    return p
+
+
+def rademacher(seed: int, n: int) -> np.ndarray:
+    """The GPU's probe generator: splitmix64 finaliser of seed + golden * (idx + 1),
+    idx = c * n + node, sign from the low bit -> [n, 5]."""
+    M = (1 << 64) - 1
+    out = np.zeros((5, n))
+    for c in range(5):
+        for i in range(n):
+            z = (seed + 0x9E3779B97F4A7C15 * (c * n + i + 1)) & M
+            z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+            z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+            z ^= z >> 31
+            out[c, i] = 1.0 if z & 1 else -1.0
+    return out.T.copy()

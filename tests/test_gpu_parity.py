@@ -210,3 +210,28 @@ def test_graphed_step_equals_launch_by_launch():
         assert ia == ic
         for k in a:
             assert np.array_equal(a[k], c[k]), k
+
+
+def test_autotune_restores_state_and_keeps_results():
+    """ys_autotune leaves the state as it found it, and the schedule it picks
+    gives the same states as the default schedule, bit for bit."""
+    gs = [goldens.load(n) for n in ("twill6_upright_wind_pert", "plain6_stiff_upright_wind")]
+    runs = []
+    for tune in (False, True):
+        b = ys.ClothBatch([spec_from_golden(g) for g in gs])
+        s0 = b.get_state()
+        if tune:
+            sc = b.autotune(1e-3, steps=2)
+            assert sc["check_every"] in (2, 4, 8, 16, 32) and sc["ms_per_step"] > 0
+            s1 = b.get_state()
+            for k in s0:
+                assert np.array_equal(s0[k], s1[k]), k
+        out = []
+        for _ in range(4):
+            assert all(s["ok"] for s in b.step(1e-3))
+            out.append(b.get_state())
+        b.close()
+        runs.append(out)
+    for a, c in zip(*runs):
+        for k in a:
+            assert np.array_equal(a[k], c[k]), k

@@ -1,0 +1,170 @@
+"""Learned preconditioner on the GPU: the tcgen05 GEMM against torch, the
+network's outputs, G blocks, loss and hand-written gradient against the CPU
+oracle (torch float64 autograd), training, and the learned solve against
+Jacobi-PCG at the same FP64 residual."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from pkg import gpu_available, ys
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), ".."))
+from oracle import gnn_oracle as go  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+
+
+def to_bf16_bits(x):
+    import torch
+    return torch.as_tensor(x, dtype=torch.float32).to(torch.bfloat16).view(torch.int16).numpy().view(np.uint16)
+
+
+@pytest.mark.parametrize("N", [64, 128, 192])
+def test_tc_gemm_matches_torch(N):
+    import ctypes
+    import torch
+    rng = np.random.default_rng(N)
+    M, K = 300, 192
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((N, K)).astype(np.float32)
+    Ab, Bb = to_bf16_bits(A), to_bf16_bits(B)
+    C = np.zeros((M, N), np.float32)
+    N_ = ys._native
+    N_.check(N_.load().ys_tc_gemm_bf16(0, ctypes.c_void_p(Ab.ctypes.data), ctypes.c_void_p(Bb.ctypes.data),
+                                       ctypes.c_void_p(C.ctypes.data), M, N, K), "ys_tc_gemm_bf16")
+    At = torch.as_tensor(Ab.view(np.int16)).view(torch.bfloat16).double()
+    Bt = torch.as_tensor(Bb.view(np.int16)).view(torch.bfloat16).double()
+    ref = (At @ Bt.T).numpy()
+    assert np.abs(C - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+def stepped_batch(seed, n_cloths, lo, hi, steps=4):
+    rng = np.random.default_rng(seed)
+    specs = ys.training_specs(rng, n_cloths, lo, hi)
+    b = ys.ClothBatch(specs)
+    for _ in range(steps):
+        assert all(s["ok"] for s in b.step(1e-3, tol=1e-10))
+    return b, specs
+
+
+def topo_of(specs):
+    return go.Topology([(s.width, s.length) for s in specs], handles=[s.handles for s in specs])
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_network_and_gradient_match_oracle():
+    """Outputs, G blocks and loss within BF16 tolerance (2e-2, 2e-2, 1e-2
+    relative); the hand-written gradient within 5e-2 relative of the oracle's
+    autograd gradient, cosine >= 0.998."""
+    b, specs = stepped_batch(11, 3, 5, 9)
+    params = go.init_params(3)
+    net = ys.LearnedPreconditioner(params=params)
+    n = b.total_nodes
+    w = go.rademacher(9, n)
+    gpu = net.loss_grad(b, probes=w)
+    seeded = net.loss_grad(b, seed=9)
+    assert abs(seeded["loss"] - gpu["loss"]) <= 1e-6 * gpu["loss"]
+    slots, _ = b.system_slots()
+    ora = go.evaluate(slots, topo_of(specs), params, w)
+    assert rel(gpu["outputs"], ora["o"]) < 2e-2
+    assert rel(gpu["G"], ora["G"]) < 2e-2
+    assert abs(gpu["loss"] - ora["loss"]) <= 1e-2 * ora["loss"]
+    g, o = gpu["grad"].astype(np.float64), ora["grad"]
+    assert rel(g, o) < 5e-2
+    assert g @ o / (np.linalg.norm(g) * np.linalg.norm(o)) >= 0.998
+    # every parameter group receives its share of the gradient
+    for lo, hi in [(go.P_W0, go.P_B0), (go.p_w(0), go.p_b(0)), (go.p_w(2), go.p_b(2)), (go.P_WH, go.P_BH)]:
+        assert rel(g[lo:hi], o[lo:hi]) < 8e-2
+    net.close()
+    b.close()
+
+
+def test_training_lowers_the_loss():
+    net = ys.LearnedPreconditioner(seed=1)
+    b, _ = stepped_batch(12, 16, 5, 20, steps=1)
+    losses = []
+    for k in range(80):
+        b.step(1e-3, tol=1e-10)
+        losses.append(net.train_step(b, seed=k + 1, lr=2e-3))
+    assert np.isfinite(losses).all()
+    assert np.mean(losses[-8:]) < 0.85 * np.mean(losses[:8])
+    b.close()
+    net.close()
+
+
+def trained_net():
+    if os.path.exists(ys.precond.PARAMS_FILE):
+        return ys.LearnedPreconditioner.pretrained()
+    net = ys.LearnedPreconditioner(seed=0)
+    ys.train_preconditioner(net, systems=64 * 120, cloths_per_batch=64, steps_per_batch=40, lr=2e-3, seed=0)
+    return net
+
+
+def test_learned_solve_same_residual_fewer_iterations():
+    """Held-out cloths: the learned solve meets the same |b - A x| <= 1e-10 |b|
+    rule as Jacobi-PCG (checked on the true residual), the states agree to the
+    solve's accuracy, and it needs fewer iterations."""
+    net = trained_net()
+    rng = np.random.default_rng(777)
+    specs = ys.training_specs(rng, 12, 10, 40)
+    runs = {}
+    for kind in ("jacobi", "learned"):
+        b = ys.ClothBatch(specs)
+        if kind == "learned":
+            b.set_preconditioner("learned", net)
+        its, states = [], []
+        for _ in range(6):
+            st = b.step(1e-3, tol=1e-10)
+            assert all(s["ok"] and s["cg_error"] <= 1e-10 for s in st)
+            its.append([s["cg_iterations"] for s in st])
+            states.append(b.get_state())
+        if kind == "learned":
+            assert b.precond_info()["fallbacks"] == 0
+            # the judge: true residual of a fresh learned solve
+            b.assemble(1e-3)
+            stats = b.solve(tol=1e-10)
+            x = b.solution()
+            ax = b.apply(x)
+            slots, rhs = b.system_slots()
+            for c in range(b.n_cloths):
+                sl = b.node_slice(c)
+                r = rhs.T[sl] - ax[sl]
+                assert np.linalg.norm(r) <= 1e-9 * np.linalg.norm(rhs.T[sl]), c
+        runs[kind] = (np.array(its), states)
+        b.close()
+    ij, il = runs["jacobi"][0], runs["learned"][0]
+    assert il.mean() < ij.mean()
+    for sj, sl in zip(runs["jacobi"][1], runs["learned"][1]):
+        for k in ("LPos", "LVel"):
+            assert np.linalg.norm(sl[k] - sj[k]) <= 1e-7 * np.linalg.norm(sj[k]) + 1e-15, k
+    net.close()
+
+
+def test_broken_network_falls_back_to_jacobi():
+    net = ys.LearnedPreconditioner(params=np.full(ys.precond.param_count(), np.nan, np.float32))
+    rng = np.random.default_rng(5)
+    specs = ys.training_specs(rng, 3, 6, 12)
+    ref = ys.ClothBatch(specs)
+    b = ys.ClothBatch(specs)
+    b.set_preconditioner("learned", net)
+    for _ in range(3):
+        assert all(s["ok"] for s in ref.step(1e-3, tol=1e-10))
+        assert all(s["ok"] for s in b.step(1e-3, tol=1e-10))
+    assert b.precond_info()["fallbacks"] == 3
+    a, c = ref.get_state(), b.get_state()
+    for k in a:
+        assert np.array_equal(a[k], c[k]), k
+    b.close()
+    ref.close()
+    net.close()

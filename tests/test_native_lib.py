@@ -10,7 +10,7 @@ from pkg import ROOT, ys
 
 def declared_symbols():
     txt = open(os.path.join(ROOT, "include", "yarnsim.h")).read()
-    return sorted(set(re.findall(r"\b(ys_[a-z_]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(ys_[a-z0-9_]+)\s*\(", txt)))
 
 
 def test_header_declares_the_entry_points():

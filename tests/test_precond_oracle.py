@@ -1,0 +1,96 @@
+"""The learned preconditioner's CPU oracle (oracle/gnn_oracle.py), checked on
+its own: its autograd gradient against central finite differences (BF16
+rounding switched off, so the loss is smooth), M^-1 = G^T G symmetric positive
+semi-definite, and the probe generator's Rademacher signs."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), ".."))
+from oracle import gnn_oracle as go  # noqa: E402
+
+
+def synthetic_system(topo, seed):
+    """Slots of a diagonally dominant system on the batch's stencil."""
+    rng = np.random.default_rng(seed)
+    n = topo.n
+    s = np.zeros((159, n))
+    for st in range(13):
+        m = topo.stencil[:, st] >= 0
+        for k in range(9):
+            s[go.SLOT_LL + 9 * st + k] = np.where(m, 0.05 * rng.standard_normal(n), 0.0)
+    for r in range(3):
+        s[go.SLOT_LL + 3 * r + r] = 2.0 + rng.random(n)
+    s[go.SLOT_LE_SELF:go.SLOT_EE_SELF] = 0.05 * rng.standard_normal((12, n))
+    s[go.SLOT_EE_SELF:go.SLOT_EE_SELF + 2] = 1.5 + rng.random((2, n))
+    for d in range(4):
+        m = topo.nbr[:, d] >= 0
+        s[go.SLOT_LE_NBR + 3 * d:go.SLOT_LE_NBR + 3 * d + 3] = np.where(m, 0.05 * rng.standard_normal((3, n)), 0)
+        s[go.SLOT_EL_NBR + 3 * d:go.SLOT_EL_NBR + 3 * d + 3] = np.where(m, 0.05 * rng.standard_normal((3, n)), 0)
+        s[go.SLOT_EE_NBR + d] = np.where(m, -0.3 * rng.random(n), 0)
+    return s
+
+
+@pytest.fixture()
+def smooth(monkeypatch):
+    monkeypatch.setattr(go, "bf16", lambda x: x)
+
+
+def test_oracle_gradient_matches_finite_differences(smooth):
+    topo = go.Topology([(4, 4), (5, 3)], handles=[[(0, 0)], [(0, 0), (4, 0)]])
+    slots = synthetic_system(topo, 1)
+    p0 = go.init_params(3).astype(np.float64)
+    w = go.rademacher(7, topo.n)
+    r = go.evaluate(slots, topo, p0, w)
+    rng = np.random.default_rng(5)
+    for _ in range(4):
+        d = rng.standard_normal(go.N_PARAMS)
+        eps = 1e-6
+        lp = go.evaluate(slots, topo, p0 + eps * d, w)["loss"]
+        lm = go.evaluate(slots, topo, p0 - eps * d, w)["loss"]
+        fd = (lp - lm) / (2 * eps)
+        an = float(r["grad"] @ d)
+        assert abs(fd - an) <= 1e-6 * max(1.0, abs(an)), (fd, an)
+
+
+def test_preconditioner_is_symmetric_psd():
+    topo = go.Topology([(5, 5)], handles=[[(0, 0), (4, 0)]])
+    slots = synthetic_system(topo, 2)
+    r = go.evaluate(slots, topo, go.init_params(4), go.rademacher(3, topo.n))
+    n = topo.n
+    G = np.zeros((5 * n, 5 * n))
+    Gb = r["G"].reshape(n, 5, 5, 5)
+    for i in range(n):
+        for b in range(5):
+            j = i if b == 0 else topo.nbr[i, b - 1]
+            if j >= 0:
+                G[5 * i:5 * i + 5, 5 * j:5 * j + 5] = Gb[i, b]
+    M = G.T @ G
+    assert np.allclose(M, M.T)
+    assert np.linalg.eigvalsh(M).min() > -1e-12
+
+
+def test_untrained_head_gives_the_analytic_inverse():
+    """Head weights and bias zero: N is -E / 2 on the neighbour blocks, zero on
+    the node itself, whatever the hidden layers compute."""
+    topo = go.Topology([(4, 5)], handles=[[(0, 0)]])
+    slots = synthetic_system(topo, 3)
+    p = go.init_params(5)
+    p[go.P_WH:] = 0.0
+    r = go.evaluate(slots, topo, p, go.rademacher(1, topo.n))
+    assert np.abs(r["o"]).max() == 0.0
+    Gb = r["G"].reshape(topo.n, 5, 5, 5)
+    for i in range(topo.n):
+        assert np.allclose(Gb[i, 0], r["Linv"][i])
+        for d in range(4):
+            j = topo.nbr[i, d]
+            if j >= 0:
+                assert np.allclose(Gb[i, d + 1], -0.5 * r["E"][i, d] @ r["Linv"][j])
+
+
+def test_rademacher_signs_are_balanced():
+    w = go.rademacher(11, 400)
+    assert set(np.unique(w)) == {-1.0, 1.0}
+    assert abs(w.mean()) < 0.1
