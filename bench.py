@@ -188,6 +188,64 @@ def cpu_sample(specs, seed, target_nodes, steps, cores):
     return value, desc, wall
 
 
+def precond_compare(ys, dev, repeats=6):
+    """Solve time and iterations of the learned preconditioner against
+    Jacobi-PCG on the same assembled systems, both to the same 1e-10 relative
+    residual: one 100 x 100 cloth and 64 cloths of 40 x 40 (plain weave,
+    material within +-20 %, hanging from two corners), after a few steps."""
+    import time
+    net = ys.LearnedPreconditioner.pretrained(device=dev)
+    out = {}
+    for name, sizes in [("cloth_100x100", [100]), ("batch_64x40x40", [40] * 64)]:
+        rng = np.random.default_rng(3)
+        base = np.array([1e-3, 1e3, 1e-5])
+        j = lambda m: base * (1.0 + 0.2 * (2.0 * rng.random((m, 3)) - 1.0))
+        b = ys.ClothBatch([ys.ClothSpec(width=W, length=W, warp=j(W), weft=j(W), height=0.05, L=1e-3, R=1e-4,
+                                        pose=0, weave=0, mu=0.3, S=1e-4, G=(0, 0, 9.8),
+                                        handles=[(0, 0), (W - 1, 0)]) for W in sizes], device=dev)
+        for _ in range(4):
+            b.step(H, tol=TOL)
+        res = {"jacobi": [], "learned": []}
+        for _ in range(repeats):
+            b.assemble(H)
+            for kind in ("jacobi", "learned"):
+                b.set_preconditioner(kind, net if kind == "learned" else None)
+                b.synchronize()
+                t0 = time.perf_counter()
+                st = b.solve(tol=TOL)
+                b.synchronize()
+                ms = (time.perf_counter() - t0) * 1e3
+                assert all(x["ok"] and x["cg_error"] <= TOL for x in st)
+                res[kind].append((max(x["cg_iterations"] for x in st), ms))
+            b.set_preconditioner("jacobi")
+            b.step(H, tol=TOL)
+        steps = {}
+        for kind, every in (("jacobi", 1), ("learned_refresh4", 4)):
+            b.set_preconditioner("learned" if kind != "jacobi" else "jacobi", net if kind != "jacobi" else None)
+            b.precond_refresh(every)
+            ts = []
+            for _ in range(8):
+                b.synchronize()
+                t0 = time.perf_counter()
+                b.step(H, tol=TOL)
+                b.synchronize()
+                ts.append((time.perf_counter() - t0) * 1e3)
+            steps[kind] = float(np.median(ts))
+        fb = b.precond_info()["fallbacks"]
+        b.close()
+        out[name] = {
+            "nodes": int(sum(W * W for W in sizes)),
+            "jacobi": {"max_iterations": float(np.mean([r[0] for r in res["jacobi"]])),
+                       "solve_ms": float(np.median([r[1] for r in res["jacobi"]]))},
+            "learned": {"max_iterations": float(np.mean([r[0] for r in res["learned"]])),
+                        "solve_ms_with_inference": float(np.median([r[1] for r in res["learned"]])),
+                        "fallbacks": fb},
+            "step_ms": steps,
+            "residual": "both |r| <= 1e-10 |b| (FP64)"}
+    net.close()
+    return out
+
+
 # ---------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -198,6 +256,7 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cloths", type=int, default=N_CLOTHS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-precond", action="store_true", help="skip the learned-vs-Jacobi solve comparison")
     ap.add_argument("--profile", action="store_true", help="print the per-kernel table to stderr")
     ap.add_argument("--schedule", default="auto", choices=["auto", "graph", "launch"],
                     help="auto: ys_autotune picks graph or launch-by-launch steps and the PCG check interval; "
@@ -320,9 +379,12 @@ def main():
            "d2h_bytes_per_step": state_bytes}
 
     # ---- per-kernel profile (a second pass of the same steps, events per launch)
+    sizes = np.array([s["width"] * s["length"] for s in specs])
+    node_iters = 0  # rows the SpMV launches processed: a cloth runs iters + 1 of them
     batch.profile(True)
     for _ in range(max(3, args.steps // 4)):
-        do_step()
+        st = do_step()
+        node_iters += int(sum(n * (x["cg_iterations"] + (0 if x["hit_maxiter"] else 1)) for n, x in zip(sizes, st)))
     batch.profile(False)
     prof = batch.profile_read(reset=True)
     tot_ms = sum(prof["ms"].values())
@@ -337,25 +399,36 @@ def main():
         "axpy": dict(bytes=n * (5 * 5 * 8 + 2 * 5 * 8), flops=n * 5 * 8),
         "dir": dict(bytes=n * (3 * 5 * 8 + 5 * 8), flops=n * 5 * 3),
     }
+    precond = None
+    if rank == 0 and not args.no_precond:
+        precond = precond_compare(ys, dev)
     hbm_peak, peak_kind = peaks()
     fp64_peak = measure_fp64_peak(torch)
 
     def roof(kname):
+        # cloths leave the PCG as they converge, so a launch processes only the
+        # rows of the cloths still iterating: rates use the rows counted
         if prof["launches"].get(kname, 0) == 0 or kname not in alg:
             return None
-        per = prof["ms"][kname] / prof["launches"][kname] * 1e-3
+        secs = prof["ms"][kname] * 1e-3
         a = alg[kname]
-        return dict(gbs=a["bytes"] / per / 1e9, tflops=a["flops"] / per / 1e12, us=per * 1e6)
+        frac_rows = node_iters / float(n)  # full-batch SpMV equivalents
+        return dict(gbs=a["bytes"] * frac_rows / secs / 1e9, tflops=a["flops"] * frac_rows / secs / 1e12,
+                    us=secs / frac_rows * 1e6, launches=prof["launches"][kname], row_passes=frac_rows)
 
     spmv = roof("spmv")
     roofline = None
     if spmv:
         roofline = {"kernel": "k_pcg_spmv (stencil SpMV, 159 FP64 coefficients per node)", "bound": "hbm",
                     "achieved": spmv["gbs"], "peak": hbm_peak, "unit": "GB/s", "frac": spmv["gbs"] / hbm_peak,
-                    "peak_source": peak_kind, "traffic": None,
+                    "peak_source": peak_kind,
+                    # DRAM bytes of one full-batch SpMV pass: ncu's dram__bytes_read + write of a
+                    # launch over every node of a 128-cloth batch (1355 B per node), times the nodes
+                    "traffic": 1355.0 * n, "traffic_source": "ncu capture at 122,512 nodes, scaled per node",
                     "fp64": {"achieved_tflops": spmv["tflops"], "dgemm_tflops": fp64_peak,
                              "frac": spmv["tflops"] / fp64_peak},
-                    "us_per_launch": spmv["us"],
+                    "us_per_full_batch_pass": spmv["us"], "full_batch_passes": spmv["row_passes"],
+                    "launches": spmv["launches"],
                     "dominant_kernel_by_time": dominant, "time_share": share}
 
     line = {"metric": metric, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
@@ -364,6 +437,8 @@ def main():
             "cloth_steps_per_s": value * args.cloths, "pcg_iterations_per_step": statistics.mean(iters),
             "all_cloths_ok": ok, "gpu_launches": int(launches), "e2e": e2e, "roofline": roofline,
             "clocks": clk.summary()}
+    if precond is not None:
+        line["precond"] = precond
 
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1

@@ -275,6 +275,10 @@ class ClothBatch:
         else:
             raise ValueError(kind)
 
+    def precond_refresh(self, every: int):
+        """Evaluate the learned preconditioner's network once per `every` solves."""
+        N.check(N.load().ys_precond_refresh(self._h, int(every)), "ys_precond_refresh")
+
     def precond_info(self) -> dict:
         s, f = ctypes.c_int64(), ctypes.c_int64()
         N.check(N.load().ys_precond_info(self._h, ctypes.byref(s), ctypes.byref(f)), "ys_precond_info")

@@ -128,6 +128,9 @@ struct ys_batch {
     double* z = nullptr;
     int64_t fallbacks = 0;
     int64_t solves = 0;
+    int refresh_every = 1;  // solves per network evaluation (G reused in between)
+    int since = 0;
+    bool have_g = false;
   } learn;
   struct Rec { int kind; cudaEvent_t a, b; };
   std::vector<Rec> recs;
@@ -1296,31 +1299,34 @@ ys_status learn_ensure(ys_batch* b) {
   ys_status st = YS_OK;
   auto A = [&](auto** p, size_t cnt) { if (st == YS_OK) st = b->alloc(p, cnt); };
   A(&g.nbr, 4 * (size_t)nt);
+  A(&g.pat, 8 * (size_t)nt);
+  A(&g.upat, 8 * (size_t)nt);
   A(&g.linv, 15 * (size_t)nt);
   A(&g.chol_ok, nt);
-  A(&g.E, 100 * (size_t)nt);
+  A(&g.E, 150 * (size_t)nt);
   A(&g.f, (size_t)ys::kGIn * nt);
   A(&g.h, 4 * (size_t)ys::kGHid * nt);
   A(&g.hb, 4 * (size_t)ys::kGHid * nt);
   A(&g.act, 3 * (size_t)ys::kGHid * nt);
   A(&g.o, (size_t)ys::kGOut * nt);
-  A(&g.G, 125 * (size_t)nt);
-  A(&g.Gn, 125 * (size_t)nt);
-  A(&g.vec, 12 * 5 * (size_t)nt);
+  A(&g.G, (size_t)ys::kGUsed * nt);
+  A(&g.Gh, (size_t)ys::kGUsed * nt);
+  A(&g.Gn, (size_t)ys::kGUsed * nt);
+  A(&g.vec, 4 * 5 * (size_t)nt);
   A(&g.dob, (size_t)ys::kGOut * nt);
   A(&g.dh, (size_t)ys::kGHid * nt);
   A(&g.dzb, (size_t)ys::kGHid * nt);
   A(&g.dm, (size_t)ys::kGMsg * nt);
-  A(&g.wpart, (size_t)g.nsplit * ys::kWgradRows * 128);
+  A(&g.wpart, (size_t)g.nsplit * ys::kWgradRows * ys::kGOut);
   A(&g.grad, ys::kGParams);
-  A(&g.lpart, 2 * (size_t)g.nlblk + 2);
+  A(&g.lpart, 2 * (size_t)g.nlblk + 3);
   A(&g.err, 1);
   A(&L.y, 5 * (size_t)nt);
   A(&L.z, 5 * (size_t)nt);
   if (st != YS_OK) return st;
   YS_CUDA(cudaMemsetAsync(g.err, 0, sizeof(int), b->stream));
   YS_CUDA(cudaMemsetAsync(g.grad, 0, sizeof(float) * ys::kGParams, b->stream));
-  ys::gnn_neighbours(b->v, g.nbr, b->stream);
+  ys::gnn_neighbours(b->v, g, b->stream);
   b->launches += 1;
   YS_CUDA(cudaGetLastError());
   L.ready = true;
@@ -1328,12 +1334,12 @@ ys_status learn_ensure(ys_batch* b) {
 }
 
 // features, network, G blocks for the assembled system
-ys_status learn_infer(ys_batch* b, ys_gnn* net) {
+ys_status learn_infer(ys_batch* b, ys_gnn* net, bool training = false) {
   ys::GnnBufs& g = b->learn.g;
   b->run(YS_PROF_GNN, 2 + 5 + 1, [&] {
     ys::gnn_prepare(b->v, g, b->stream);
     ys::gnn_forward(net->net, g, b->stream);
-    ys::gnn_make_g(g, b->stream);
+    ys::gnn_make_g(g, training, b->stream);
   });
   YS_CUDA(cudaGetLastError());
   return YS_OK;
@@ -1354,14 +1360,19 @@ ys_status solve_learned(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* 
   if (!L.net) return fail(YS_ERR_ARG, "learned preconditioner without a network");
   ys_status st = learn_ensure(b);
   if (st != YS_OK) return st;
-  if ((st = learn_infer(b, L.net)) != YS_OK) return st;
+  if (!L.have_g || ++L.since >= L.refresh_every) {
+    if ((st = learn_infer(b, L.net)) != YS_OK) return st;
+    L.have_g = true;
+    L.since = 0;
+  }
   cudaStream_t s = b->stream;
   const ys::View& v = b->v;
   b->so.tol = (opts && opts->tol > 0) ? opts->tol : DBL_EPSILON;
   const int override_max = (opts && opts->maxiter >= 0) ? opts->maxiter : -1;
-  const int every = (opts && opts->check_every > 0) ? opts->check_every : b->check_every;
+  // the learned solve converges in a few iterations: poll every 4 unless told
+  const int every = (opts && opts->check_every > 0) ? opts->check_every : 4;
   const int cap = override_max >= 0 ? override_max : b->max_maxiter;
-  const ys::LpcgExtra lx{L.g.G, L.g.nbr, L.y, L.z};
+  const ys::LpcgExtra lx{L.g.Gh, L.g.pat, L.g.upat, L.y, L.z};
   b->run(YS_PROF_MISC, 1, [&] {
     k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
   });
@@ -1508,7 +1519,8 @@ ys_status ys_gnn_loss_grad(ys_gnn* g, ys_batch* b, const float* probes, uint64_t
   ys_status st = learn_ensure(b);
   if (st != YS_OK) return st;
   YS_CUDA(cudaStreamSynchronize(0));
-  if ((st = learn_infer(b, g)) != YS_OK) return st;
+  if ((st = learn_infer(b, g, true)) != YS_OK) return st;
+  b->learn.have_g = false;
   ys::GnnBufs& G = b->learn.g;
   const int nt = b->ntot;
   if (probes) {
@@ -1528,12 +1540,17 @@ ys_status ys_gnn_loss_grad(ys_gnn* g, ys_batch* b, const float* probes, uint64_t
   }
   if (loss) YS_CUDA(cudaMemcpy(loss, G.lpart + 2 * G.nlblk, sizeof(double), cudaMemcpyDeviceToHost));
   if (grad) YS_CUDA(cudaMemcpy(grad, G.grad, sizeof(float) * ys::kGParams, cudaMemcpyDeviceToHost));
-  if (outputs) YS_CUDA(cudaMemcpy(outputs, G.o, sizeof(float) * ys::kGOut * nt, cudaMemcpyDeviceToHost));
+  if (outputs) {  // stored component-major on the device
+    std::vector<float> t((size_t)ys::kGOut * nt);
+    YS_CUDA(cudaMemcpy(t.data(), G.o, sizeof(float) * t.size(), cudaMemcpyDeviceToHost));
+    for (int n = 0; n < nt; ++n)
+      for (int k = 0; k < ys::kGOut; ++k) outputs[(size_t)n * ys::kGOut + k] = t[(size_t)k * nt + n];
+  }
   if (gblocks) {
-    std::vector<float> t(125 * (size_t)nt);
+    std::vector<float> t((size_t)ys::kGUsed * nt);
     YS_CUDA(cudaMemcpy(t.data(), G.G, sizeof(float) * t.size(), cudaMemcpyDeviceToHost));
     for (int n = 0; n < nt; ++n)
-      for (int k = 0; k < 125; ++k) gblocks[(size_t)n * 125 + k] = t[(size_t)k * nt + n];
+      for (int k = 0; k < ys::kGUsed; ++k) gblocks[(size_t)n * ys::kGUsed + k] = t[(size_t)k * nt + n];
   }
   return YS_OK;
 }
@@ -1545,7 +1562,8 @@ ys_status ys_gnn_train_step(ys_gnn* g, ys_batch* b, uint64_t seed, float lr, dou
   YS_CUDA(cudaSetDevice(b->device));
   ys_status st = learn_ensure(b);
   if (st != YS_OK) return st;
-  if ((st = learn_infer(b, g)) != YS_OK) return st;
+  if ((st = learn_infer(b, g, true)) != YS_OK) return st;
+  b->learn.have_g = false;
   ys::GnnBufs& G = b->learn.g;
   ys::gnn_loss_grad(b->v, g->net, G, seed, false, b->stream);
   g->step += 1;
@@ -1569,6 +1587,14 @@ ys_status ys_set_preconditioner(ys_batch* b, int32_t kind, ys_gnn* g) {
   if (kind == YS_PREC_LEARNED && (!g || g->device != b->device)) return fail(YS_ERR_ARG, "bad network");
   b->learn.kind = kind;
   b->learn.net = kind == YS_PREC_LEARNED ? g : nullptr;
+  b->learn.have_g = false;
+  return YS_OK;
+}
+
+ys_status ys_precond_refresh(ys_batch* b, int32_t every) {
+  if (!b || every < 1) return fail(YS_ERR_ARG, "bad argument");
+  b->learn.refresh_every = every;
+  b->learn.have_g = false;
   return YS_OK;
 }
 

@@ -4,6 +4,7 @@
 // gradient, Adam, and the preconditioned conjugate-gradient iteration that
 // applies M^-1 = G^T G.
 #include <cfloat>
+#include <cmath>
 
 #include "ys_gnn.cuh"
 #include "ys_items.cuh"
@@ -21,49 +22,89 @@ __device__ __forceinline__ int opp(int d) { return d ^ 1; }  // left<->right, do
 __device__ __forceinline__ int lt(int r, int c) { return r * (r + 1) / 2 + c; }
 
 // ------------------------------------------------------------ neighbours
-__global__ void k_gnn_nbr(View v, int* nbr) {
+// yarn neighbours (message passing) and the lower pattern of G with its transpose
+__global__ void k_gnn_nbr(View v, GnnBufs g) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= v.ntot) return;
   const ClothParams& P = v.cp[v.node_cloth[n]];
   const int u = v.node_u[n], w = v.node_v[n];
-  nbr[4 * n + 0] = u > 0 ? n - 1 : -1;
-  nbr[4 * n + 1] = u < P.W - 1 ? n + 1 : -1;
-  nbr[4 * n + 2] = w > 0 ? n - P.W : -1;
-  nbr[4 * n + 3] = w < P.H - 1 ? n + P.W : -1;
+  g.nbr[4 * n + 0] = u > 0 ? n - 1 : -1;
+  g.nbr[4 * n + 1] = u < P.W - 1 ? n + 1 : -1;
+  g.nbr[4 * n + 2] = w > 0 ? n - P.W : -1;
+  g.nbr[4 * n + 3] = w < P.H - 1 ? n + P.W : -1;
+  for (int b = 0; b < 8; ++b) {
+    int src = -1, row = -1;
+    if (b < kGBlocks) {
+      const int du = gpat_du(b), dv = gpat_dv(b);
+      if (u + du >= 0 && u + du < P.W && w + dv >= 0 && w + dv < P.H) src = n + du + dv * P.W;
+      if (u - du >= 0 && u - du < P.W && w - dv >= 0 && w - dv < P.H) row = n - du - dv * P.W;
+    }
+    g.pat[8 * n + b] = src;
+    g.upat[8 * n + b] = row;
+  }
 }
 
 // ------------------------------------------------- block factor and features
-// 5 x 5 diagonal block of row block n (DOF order x, y, z, u, v)
-__device__ void diag_block(const View& v, int n, double D[5][5]) {
-  for (int r = 0; r < 5; ++r)
-    for (int c = 0; c < 5; ++c) D[r][c] = 0.0;
-  for (int r = 0; r < 3; ++r)
-    for (int c = 0; c < 3; ++c) D[r][c] = slot(v, YS_SLOT_LL + 3 * r + c, n);
-  for (int r = 0; r < 3; ++r)
-    for (int k = 0; k < 2; ++k) {
-      D[r][3 + k] = slot(v, YS_SLOT_LE_SELF + 2 * r + k, n);
-      D[3 + k][r] = slot(v, YS_SLOT_EL_SELF + 3 * k + r, n);
-    }
-  D[3][3] = slot(v, YS_SLOT_EE_SELF + 0, n);
-  D[4][4] = slot(v, YS_SLOT_EE_SELF + 1, n);
-}
-
-// 5 x 5 block A(n, j) of yarn neighbour d (j = n + offset(d))
-__device__ void nbr_block(const View& v, int n, int d, float B[5][5]) {
-  for (int r = 0; r < 5; ++r)
-    for (int c = 0; c < 5; ++c) B[r][c] = 0.f;
-  const int s = d + 1;  // stencil slots 1..4 are (-1,0), (1,0), (0,-1), (0,1)
-  for (int r = 0; r < 3; ++r)
-    for (int c = 0; c < 3; ++c) B[r][c] = (float)slot(v, YS_SLOT_LL + 9 * s + 3 * r + c, n);
-  const int k = d < 2 ? 0 : 1;
+// 5 x 5 diagonal block of row block n (DOF order x, y, z, u, v), in FP32
+__device__ __forceinline__ void diag_block(const View& v, int n, float D[5][5]) {
+  const int64_t nt = v.ntot;
+  const double* a = v.A + n;
+#pragma unroll
   for (int r = 0; r < 3; ++r) {
-    B[r][3 + k] = (float)slot(v, YS_SLOT_LE_NBR + 3 * d + r, n);
-    B[3 + k][r] = (float)slot(v, YS_SLOT_EL_NBR + 3 * d + r, n);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) D[r][c] = (float)a[(YS_SLOT_LL + 3 * r + c) * nt];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      D[r][3 + k] = (float)a[(YS_SLOT_LE_SELF + 2 * r + k) * nt];
+      D[3 + k][r] = (float)a[(YS_SLOT_EL_SELF + 3 * k + r) * nt];
+    }
   }
-  B[3 + k][3 + k] = (float)slot(v, YS_SLOT_EE_NBR + d, n);
+  D[3][3] = (float)a[YS_SLOT_EE_SELF * nt];
+  D[4][4] = (float)a[(YS_SLOT_EE_SELF + 1) * nt];
+  D[3][4] = D[4][3] = 0.f;
 }
 
-__device__ void load_linv(const float* linv, int nt, int n, float L[5][5]) {
+// 5 x 5 block A(n, j) of yarn neighbour d (j = n + offset(d)); warp
+// neighbours (d < 2) couple u, weft neighbours v (selects, no runtime indexing)
+__device__ __forceinline__ void nbr_block(const View& v, int n, int d, float B[5][5]) {
+  const int s = d + 1;  // stencil slots 1..4 are (-1,0), (1,0), (0,-1), (0,1)
+  const bool ku = d < 2;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) B[r][c] = (float)slot(v, YS_SLOT_LL + 9 * s + 3 * r + c, n);
+    const float le = (float)slot(v, YS_SLOT_LE_NBR + 3 * d + r, n);
+    const float el = (float)slot(v, YS_SLOT_EL_NBR + 3 * d + r, n);
+    B[r][3] = ku ? le : 0.f;
+    B[r][4] = ku ? 0.f : le;
+    B[3][r] = ku ? el : 0.f;
+    B[4][r] = ku ? 0.f : el;
+  }
+  const float ee = (float)slot(v, YS_SLOT_EE_NBR + d, n);
+  B[3][3] = ku ? ee : 0.f;
+  B[4][4] = ku ? 0.f : ee;
+  B[3][4] = B[4][3] = 0.f;
+}
+
+// 5 x 5 block A(n, src) of lower-pattern block b > 0 (couplings through the
+// stencil slot of its offset; Eulerian entries for the yarn neighbours)
+__device__ __forceinline__ void pat_block(const View& v, int n, int b, float B[5][5]) {
+  if (b == 1 || b == 2) {
+    nbr_block(v, n, b == 1 ? 0 : 2, B);
+    return;
+  }
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+#pragma unroll
+    for (int c = 0; c < 5; ++c) B[r][c] = 0.f;
+  const int s = stencil_index(gpat_du(b), gpat_dv(b));
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) B[r][c] = (float)slot(v, YS_SLOT_LL + 9 * s + 3 * r + c, n);
+}
+
+__device__ __forceinline__ void load_linv(const float* linv, int nt, int n, float L[5][5]) {
   for (int r = 0; r < 5; ++r)
     for (int c = 0; c < 5; ++c) L[r][c] = c <= r ? linv[(int64_t)lt(r, c) * nt + n] : 0.f;
 }
@@ -73,43 +114,53 @@ __device__ void load_linv(const float* linv, int nt, int n, float L[5][5]) {
 __global__ void k_gnn_linv(View v, float* linv, int* chol_ok) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= v.ntot) return;
-  double D[5][5], L[5][5] = {};
+  // single precision: the factor only shapes the preconditioner
+  float D[5][5], L[5][5] = {};
   diag_block(v, n, D);
   bool ok = true;
-  for (int j = 0; j < 5 && ok; ++j) {
-    double s = 0.5 * (D[j][j] + D[j][j]);
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    float s = D[j][j];
+#pragma unroll
     for (int k = 0; k < j; ++k) s -= L[j][k] * L[j][k];
-    if (!(s > 0.0) || !isfinite(s)) {
-      ok = false;
-      break;
-    }
-    L[j][j] = sqrt(s);
+    ok = ok && s > 0.f && isfinite(s);
+    L[j][j] = sqrtf(fmaxf(s, FLT_MIN));
+#pragma unroll
     for (int i = j + 1; i < 5; ++i) {
-      double t = 0.5 * (D[i][j] + D[j][i]);
+      float t = 0.5f * (D[i][j] + D[j][i]);
+#pragma unroll
       for (int k = 0; k < j; ++k) t -= L[i][k] * L[j][k];
       L[i][j] = t / L[j][j];
     }
   }
   if (!ok) {
+#pragma unroll
     for (int r = 0; r < 5; ++r)
-      for (int c = 0; c < 5; ++c) L[r][c] = 0.0;
+#pragma unroll
+      for (int c = 0; c < 5; ++c) L[r][c] = 0.f;
+#pragma unroll
     for (int j = 0; j < 5; ++j) {
-      const double d = fabs(D[j][j]);
-      L[j][j] = (d > 0.0 && isfinite(d)) ? sqrt(d) : 1.0;
+      const float d = fabsf(D[j][j]);
+      L[j][j] = (d > 0.f && isfinite(d)) ? sqrtf(d) : 1.f;
     }
   }
-  double X[5][5] = {};
+  float X[5][5] = {};
+#pragma unroll
   for (int c = 0; c < 5; ++c) {
-    X[c][c] = 1.0 / L[c][c];
+    X[c][c] = 1.f / L[c][c];
+#pragma unroll
     for (int r = c + 1; r < 5; ++r) {
-      double t = 0.0;
+      float t = 0.f;
+#pragma unroll
       for (int k = c; k < r; ++k) t += L[r][k] * X[k][c];
       X[r][c] = -t / L[r][r];
     }
   }
   const int nt = v.ntot;
+#pragma unroll
   for (int r = 0; r < 5; ++r)
-    for (int c = 0; c <= r; ++c) linv[(int64_t)lt(r, c) * nt + n] = (float)X[r][c];
+#pragma unroll
+    for (int c = 0; c <= r; ++c) linv[(int64_t)lt(r, c) * nt + n] = X[r][c];
   chol_ok[n] = ok ? 1 : 0;
 }
 
@@ -131,73 +182,120 @@ __device__ __forceinline__ void mul_ab(const float A[5][5], const float B[5][5],
     }
 }
 
+__device__ __forceinline__ float frob(const float M[5][5]) {
+  float s = 0.f;
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+#pragma unroll
+    for (int c = 0; c < 5; ++c) s += M[r][c] * M[r][c];
+  return sqrtf(s);
+}
+
+// one thread per (coupling q, node): q < 6 the lower block b = q + 1 (its E
+// kept for the prior; features: E of left and down (50), x part of E of the
+// four other lower blocks (36)); q >= 6 the norm of the scaled coupling to
+// the upper neighbour right, up, right-up, left-up, right-2, up-2 (6); q = 0
+// also writes the flags (5) and the zero padding
 __global__ void k_gnn_feat(View v, GnnBufs g) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= v.ntot) return;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = v.ntot;
+  if (t >= 12LL * nt) return;
+  const int q = (int)(t / nt), n = (int)(t - (int64_t)q * nt);
   float Li[5][5], Lj[5][5], Bk[5][5], T[5][5], E[5][5];
-  load_linv(g.linv, nt, n, Li);
   bf16* f = g.f + (int64_t)n * kGIn;
-  float* Eo = g.E + (int64_t)n * 100;
-  for (int d = 0; d < 4; ++d) {
-    const int j = g.nbr[4 * n + d];
+  const ClothParams& P = v.cp[v.node_cloth[n]];
+  const int u = v.node_u[n], w = v.node_v[n];
+  if (q < 6) {
+    const int b = q + 1;
+    const int j = g.pat[8 * n + b];
     if (j >= 0) {
-      nbr_block(v, n, d, Bk);
+      load_linv(g.linv, nt, n, Li);
+      pat_block(v, n, b, Bk);
       load_linv(g.linv, nt, j, Lj);
       mul_ab(Li, Bk, T);
       mul_abt(T, Lj, E);
     } else {
+#pragma unroll
       for (int r = 0; r < 5; ++r)
+#pragma unroll
         for (int c = 0; c < 5; ++c) E[r][c] = 0.f;
     }
+#pragma unroll
     for (int r = 0; r < 5; ++r)
-      for (int c = 0; c < 5; ++c) {
-        Eo[25 * d + 5 * r + c] = E[r][c];
-        f[25 * d + 5 * r + c] = __float2bfloat16(E[r][c]);
-      }
-  }
-  // norms of the 8 other node-node couplings, scaled the same way (x part)
-  const ClothParams& P = v.cp[v.node_cloth[n]];
-  const int u = v.node_u[n], w = v.node_v[n];
-  for (int s = 5; s < kNumStencil; ++s) {
-    const int uu = u + stencil_du(s), vv = w + stencil_dv(s);
-    float nrm = 0.f;
-    if (uu >= 0 && uu < P.W && vv >= 0 && vv < P.H) {
-      const int j = n + stencil_du(s) + stencil_dv(s) * P.W;
-      load_linv(g.linv, nt, j, Lj);
+#pragma unroll
+      for (int c = 0; c < 5; ++c) g.E[(int64_t)(25 * q + 5 * r + c) * nt + n] = E[r][c];
+    if (b <= 2) {
+#pragma unroll
+      for (int r = 0; r < 5; ++r)
+#pragma unroll
+        for (int c = 0; c < 5; ++c) f[25 * q + 5 * r + c] = __float2bfloat16(E[r][c]);
+    } else {
+#pragma unroll
       for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) {
-          float t = 0.f;
-          for (int a = 0; a <= r; ++a)
-            for (int b = 0; b <= c; ++b) t += Li[r][a] * (float)slot(v, YS_SLOT_LL + 9 * s + 3 * a + b, n) * Lj[c][b];
-          nrm += t * t;
-        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) f[50 + 9 * (b - 3) + 3 * r + c] = __float2bfloat16(E[r][c]);
     }
-    f[100 + s - 5] = __float2bfloat16(sqrtf(nrm));
+    if (q == 0) {
+      const uint8_t fl = v.flags[n];
+      f[92] = __float2bfloat16(g.chol_ok[n] ? 0.f : 1.f);
+      f[93] = __float2bfloat16((fl & YS_INTERIOR) ? 1.f : 0.f);
+      f[94] = __float2bfloat16((fl & YS_FIXED) ? 1.f : 0.f);
+      f[95] = __float2bfloat16((u == 0 || u == P.W - 1) ? 1.f : 0.f);
+      f[96] = __float2bfloat16((w == 0 || w == P.H - 1) ? 1.f : 0.f);
+      for (int k = 97; k < kGIn; ++k) f[k] = __float2bfloat16(0.f);
+    }
+    return;
   }
-  const uint8_t fl = v.flags[n];
-  f[108] = __float2bfloat16(g.chol_ok[n] ? 0.f : 1.f);
-  f[109] = __float2bfloat16((fl & YS_INTERIOR) ? 1.f : 0.f);
-  f[110] = __float2bfloat16((fl & YS_FIXED) ? 1.f : 0.f);
-  f[111] = __float2bfloat16((u == 0 || u == P.W - 1) ? 1.f : 0.f);
-  f[112] = __float2bfloat16((w == 0 || w == P.H - 1) ? 1.f : 0.f);
-  for (int k = 113; k < kGIn; ++k) f[k] = __float2bfloat16(0.f);
+  const int k = q - 6;
+  const int du = k == 0 ? 1 : k == 1 ? 0 : k == 2 ? 1 : k == 3 ? -1 : k == 4 ? 2 : 0;
+  const int dv = k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 1 : k == 3 ? 1 : k == 4 ? 0 : 2;
+  float nrm = 0.f;
+  if (u + du >= 0 && u + du < P.W && w + dv >= 0 && w + dv < P.H) {
+    const int j = n + du + dv * P.W;
+    load_linv(g.linv, nt, n, Li);
+    load_linv(g.linv, nt, j, Lj);
+    if (k < 2) {
+      nbr_block(v, n, k == 0 ? 1 : 3, Bk);
+    } else {
+      const int s = stencil_index(du, dv);
+#pragma unroll
+      for (int r = 0; r < 5; ++r)
+#pragma unroll
+        for (int c = 0; c < 5; ++c)
+          Bk[r][c] = (r < 3 && c < 3) ? (float)slot(v, YS_SLOT_LL + 9 * s + 3 * r + c, n) : 0.f;
+    }
+    mul_ab(Li, Bk, T);
+    mul_abt(T, Lj, E);
+    nrm = frob(E);
+  }
+  f[86 + k] = __float2bfloat16(nrm);
 }
 
 // ------------------------------------------------------------ tensor-core GEMM
 // C[m][n] = sum_k A(m, k) B(n, k) over 128-row tiles (blockIdx.x), NT-column
 // tiles (blockIdx.y) and K splits (blockIdx.z); the Op stages A and B chunks
 // of 64 K into shared memory and consumes the FP32 accumulator rows.
+// asynchronous 16-byte global -> shared copies (zero-filled when !valid)
+__device__ __forceinline__ void cp_async16(uint8_t* dst, const void* src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc::smem_u32(dst)), "l"(src),
+               "r"(valid ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 constexpr int kGemmThreads = 128;
 constexpr int kGemmSmem = 56 * 1024;  // keeps at most 4 CTAs (4 x 128 TMEM columns) per SM
 constexpr uint32_t kWaitLimit = 1u << 22;
 
-template <class Op>
+// KCH chunks are staged before one batch of MMAs (all of K when it fits),
+// so a CTA pays one global-load round trip per KCH chunks
+template <class Op, int KCH>
 __global__ void __launch_bounds__(kGemmThreads) k_tc_gemm(Op op, int nchunk_total, int chunks_per_split, int* err) {
   extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr int kABytes = 16384, kBBytes = Op::NT * 128;
   uint8_t* sA = smem;
-  uint8_t* sB = smem + 16384;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 16384 + Op::NT * 128);
+  uint8_t* sB = smem + KCH * kABytes;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + KCH * (kABytes + kBBytes));
   uint32_t* slot_ = reinterpret_cast<uint32_t*>(bar + 1);
   constexpr uint32_t kCols = Op::NT < 32 ? 32 : Op::NT;
   const int warp = threadIdx.x >> 5;
@@ -213,18 +311,24 @@ __global__ void __launch_bounds__(kGemmThreads) k_tc_gemm(Op op, int nchunk_tota
   constexpr uint32_t idesc = tc::idesc_bf16(tc::kTileM, Op::NT);
   uint32_t phase = 0;
   bool ok = true;
-  for (int kc = kc0; kc < kc1; ++kc) {
-    op.stage_a(sA, m0, kc);
-    op.stage_b(sB, n0, kc);
+  for (int kc = kc0; kc < kc1; kc += KCH) {
+    const int nk = min(KCH, kc1 - kc);
+    for (int q = 0; q < nk; ++q) {
+      op.stage_a(sA + q * kABytes, m0, kc + q);
+      op.stage_b(sB + q * kBBytes, n0, kc + q);
+    }
+    cp_async_wait_all();
     tc::fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
       tc::fence_after_sync();
-      const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB);
+      for (int q = 0; q < nk; ++q) {
+        const uint32_t a0 = tc::smem_u32(sA + q * kABytes), b0 = tc::smem_u32(sB + q * kBBytes);
 #pragma unroll
-      for (int k = 0; k < tc::kChunkK / 16; ++k)
-        tc::mma_bf16(tmem, tc::smem_desc(a0 + k * 256), tc::smem_desc(b0 + k * 256), idesc,
-                     (kc > kc0 || k > 0) ? 1u : 0u);
+        for (int k = 0; k < tc::kChunkK / 16; ++k)
+          tc::mma_bf16(tmem, tc::smem_desc(a0 + k * 256), tc::smem_desc(b0 + k * 256), idesc,
+                       (kc > kc0 || q > 0 || k > 0) ? 1u : 0u);
+      }
       tc::mma_commit(bar);
     }
     bool done = tc::mbar_wait(bar, phase, kWaitLimit);
@@ -234,12 +338,31 @@ __global__ void __launch_bounds__(kGemmThreads) k_tc_gemm(Op op, int nchunk_tota
     tc::fence_after_sync();
   }
   if (ok && kc1 > kc0) {
+    // 32-column slabs of the accumulator go through shared memory (row
+    // stride 33 floats: conflict-free both ways) so that the stores of a warp
+    // cover 32 consecutive columns of one row
+    float* stage = reinterpret_cast<float*>(smem);
     const int row = warp * 32 + (threadIdx.x & 31);
 #pragma unroll 1
-    for (int c = 0; c < Op::NT; c += 16) {
+    for (int c = 0; c < Op::NT; c += 32) {
       float acc[16];
       tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, acc);
-      op.epilogue(m0 + row, n0 + c, acc);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) stage[row * 33 + i] = acc[i];
+      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c + 16), acc);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) stage[row * 33 + 16 + i] = acc[i];
+      __syncthreads();
+      // row-major outputs: a warp stores 32 columns of a row; column-major
+      // ones (Op::kColMajor): 32 rows of a column. Unrolled so that the loads
+      // an epilogue makes (bias, residual) are in flight together.
+#pragma unroll 8
+      for (int k = 0; k < tc::kTileM * 32 / kGemmThreads; ++k) {
+        const int i = threadIdx.x + k * kGemmThreads;
+        const int r = Op::kColMajor ? (i & 127) : (i >> 5), cc = Op::kColMajor ? (i >> 7) : (i & 31);
+        op.store(m0 + r, n0 + c + cc, stage[r * 33 + cc]);
+      }
+      __syncthreads();
     }
   } else if (!ok) {
     if (threadIdx.x == 0) atomicExch(err, 1);
@@ -253,31 +376,29 @@ __global__ void __launch_bounds__(kGemmThreads) k_tc_gemm(Op op, int nchunk_tota
   }
 }
 
-__device__ __forceinline__ void store16(uint8_t* tile, int r, int k8, uint4 val) {
-  *reinterpret_cast<uint4*>(tile + tc::core_off(r, k8)) = val;
-}
 __device__ __forceinline__ void store1(uint8_t* tile, int r, int k, bf16 val) {
   *reinterpret_cast<bf16*>(tile + tc::core_off(r, k)) = val;
 }
 
 // rows of X (ld elements, 64-wide chunk kc, or the neighbour given by the chunk
-// when gathering), one thread per row
+// when gathering), one thread per row, as asynchronous 16-byte copies
+// (missing rows are zero-filled); cp_async_wait_all completes them
 __device__ __forceinline__ void stage_rows(uint8_t* sA, const bf16* X, int ld, int M, const int* nbr, bool gather,
                                            int m0, int kc) {
   const int r = threadIdx.x;
   const int node = m0 + r;
   int src = -1;
   if (node < M) src = gather ? (kc == 0 ? node : nbr[4 * node + kc - 1]) : node;
-  const uint4* p = src >= 0 ? reinterpret_cast<const uint4*>(X + (int64_t)src * ld + (gather ? 0 : kc * 64)) : nullptr;
+  const bf16* p = X + (int64_t)(src >= 0 ? src : 0) * ld + (gather ? 0 : kc * 64);
 #pragma unroll
-  for (int q = 0; q < 8; ++q) store16(sA, r, q * 8, p ? p[q] : make_uint4(0, 0, 0, 0));
+  for (int q = 0; q < 8; ++q) cp_async16(sA + tc::core_off(r, q * 8), p + q * 8, src >= 0);
 }
 // NT rows of a row-major [rows][K] weight matrix
 template <int NT>
 __device__ __forceinline__ void stage_weights(uint8_t* sB, const bf16* W, int K, int n0, int kc) {
   for (int i = threadIdx.x; i < NT * 8; i += kGemmThreads) {
     const int n = i >> 3, q = i & 7;
-    store16(sB, n, q * 8, *reinterpret_cast<const uint4*>(W + (int64_t)(n0 + n) * K + kc * 64 + q * 8));
+    cp_async16(sB + tc::core_off(n, q * 8), W + (int64_t)(n0 + n) * K + kc * 64 + q * 8, true);
   }
 }
 
@@ -286,6 +407,7 @@ enum { kEpiEnc = 0, kEpiLayer = 1, kEpiHead = 2 };
 template <int NT_, int EPI>
 struct FwdOp {
   static constexpr int NT = NT_;
+  static constexpr bool kColMajor = EPI == kEpiHead;  // o is stored [192][ntot]
   const bf16* X;
   int ld, M;
   const int* nbr;
@@ -300,24 +422,21 @@ struct FwdOp {
   float* o_out;
   __device__ void stage_a(uint8_t* s, int m0, int kc) const { stage_rows(s, X, ld, M, nbr, gather != 0, m0, kc); }
   __device__ void stage_b(uint8_t* s, int n0, int kc) const { stage_weights<NT>(s, W, K, n0, kc); }
-  __device__ void epilogue(int node, int c0, const float* acc) const {
+  __device__ void store(int node, int j, float acc) const {
     if (node >= M) return;
-    for (int i = 0; i < 16; ++i) {
-      const int j = c0 + i;
-      const float z = acc[i] + bias[j];
-      if (EPI == kEpiHead) {
-        o_out[(int64_t)node * kGOut + j] = z;
-      } else {
-        const float a = fmaxf(z, 0.f);
-        const int64_t at = (int64_t)node * kGHid + j;
-        float hn = a;
-        if (EPI == kEpiLayer) {
-          act_out[at] = __float2bfloat16(a);
-          hn = h_in[at] + a;
-        }
-        h_out[at] = hn;
-        hb_out[at] = __float2bfloat16(hn);
+    const float z = acc + bias[j];
+    if (EPI == kEpiHead) {
+      o_out[(int64_t)j * M + node] = z;
+    } else {
+      const float a = fmaxf(z, 0.f);
+      const int64_t at = (int64_t)node * kGHid + j;
+      float hn = a;
+      if (EPI == kEpiLayer) {
+        act_out[at] = __float2bfloat16(a);
+        hn = h_in[at] + a;
       }
+      h_out[at] = hn;
+      hb_out[at] = __float2bfloat16(hn);
     }
   }
 };
@@ -325,6 +444,7 @@ struct FwdOp {
 // data gradient: dX = dZ W, with B = W^T stored [K_in][Nout]
 struct BwdDataOp {
   static constexpr int NT = 64;
+  static constexpr bool kColMajor = false;
   const bf16* dZ;
   int nout, M;
   const bf16* WT;
@@ -332,9 +452,8 @@ struct BwdDataOp {
   int kin;
   __device__ void stage_a(uint8_t* s, int m0, int kc) const { stage_rows(s, dZ, nout, M, nullptr, false, m0, kc); }
   __device__ void stage_b(uint8_t* s, int n0, int kc) const { stage_weights<NT>(s, WT, nout, n0, kc); }
-  __device__ void epilogue(int node, int c0, const float* acc) const {
-    if (node >= M) return;
-    for (int i = 0; i < 16; ++i) out[(int64_t)node * kin + c0 + i] = acc[i];
+  __device__ void store(int node, int col, float acc) const {
+    if (node < M) out[(int64_t)node * kin + col] = acc;
   }
 };
 
@@ -344,12 +463,14 @@ struct BwdDataOp {
 template <int NT_>
 struct WgradOp {
   static constexpr int NT = NT_;
+  static constexpr bool kColMajor = false;
   const bf16* X;
   int ld, kin, nodes;
   const int* nbr;
   int gather;
   const bf16* dZ;
-  float* part;  // [split][kWgradRows][NT]
+  int ldz;      // columns of dZ and of the partial sums; this CTA's are n0 .. n0 + NT
+  float* part;  // [split][kWgradRows][ldz]
   __device__ void stage_a(uint8_t* s, int m0, int kc) const {
     const int r = threadIdx.x;
     const int feat = m0 + r;
@@ -372,17 +493,15 @@ struct WgradOp {
       store1(s, r, kk, __float2bfloat16(val));
     }
   }
-  __device__ void stage_b(uint8_t* s, int, int kc) const {
+  __device__ void stage_b(uint8_t* s, int n0, int kc) const {
     for (int i = threadIdx.x; i < NT * 64; i += kGemmThreads) {
       const int n = i % NT, kk = i / NT;
       const int node = kc * 64 + kk;
-      store1(s, n, kk, node < nodes ? dZ[(int64_t)node * NT + n] : __float2bfloat16(0.f));
+      store1(s, n, kk, node < nodes ? dZ[(int64_t)node * ldz + n0 + n] : __float2bfloat16(0.f));
     }
   }
-  __device__ void epilogue(int row, int c0, const float* acc) const {
-    if (row > kin) return;
-    float* p = part + ((int64_t)blockIdx.z * kWgradRows + row) * NT + c0;
-    for (int i = 0; i < 16; ++i) p[i] = acc[i];
+  __device__ void store(int row, int col, float acc) const {
+    if (row <= kin) part[((int64_t)blockIdx.z * kWgradRows + row) * ldz + col] = acc;
   }
 };
 
@@ -390,118 +509,144 @@ struct WgradOp {
 template <int NT_>
 struct PlainOp {
   static constexpr int NT = NT_;
+  static constexpr bool kColMajor = false;
   const bf16* A;
   const bf16* B;
   float* C;
   int M, N, K;
-  __device__ void stage_a(uint8_t* s, int m0, int kc) const {
-    const int r = threadIdx.x, m = m0 + r;
-#pragma unroll
-    for (int q = 0; q < 8; ++q)
-      store16(s, r, q * 8,
-              m < M ? *reinterpret_cast<const uint4*>(A + (int64_t)m * K + kc * 64 + q * 8) : make_uint4(0, 0, 0, 0));
-  }
+  __device__ void stage_a(uint8_t* s, int m0, int kc) const { stage_rows(s, A, K, M, nullptr, false, m0, kc); }
   __device__ void stage_b(uint8_t* s, int n0, int kc) const { stage_weights<NT>(s, B, K, n0, kc); }
-  __device__ void epilogue(int m, int c0, const float* acc) const {
-    if (m >= M) return;
-    for (int i = 0; i < 16; ++i) C[(int64_t)m * N + c0 + i] = acc[i];
+  __device__ void store(int m, int col, float acc) const {
+    if (m < M) C[(int64_t)m * N + col] = acc;
   }
 };
 
-template <class Op>
+template <class Op, int KCH = 1>
 void launch_gemm(const Op& op, int M, int ncol_tiles, int nchunk, int nsplit, int* err, cudaStream_t s) {
+  // at least 56 KB keeps at most 4 CTAs (4 x 128 TMEM columns) on an SM
+  constexpr int smem_need = KCH * (16384 + Op::NT * 128) + 64;
+  constexpr int smem = smem_need > kGemmSmem ? smem_need : kGemmSmem;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_tc_gemm<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    cudaFuncSetAttribute(k_tc_gemm<Op, KCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
   const int per = (nchunk + nsplit - 1) / nsplit;
   const int splits = (nchunk + per - 1) / per;
   dim3 grid((M + tc::kTileM - 1) / tc::kTileM, ncol_tiles, splits);
-  k_tc_gemm<Op><<<grid, kGemmThreads, kGemmSmem, s>>>(op, nchunk, per, err);
+  k_tc_gemm<Op, KCH><<<grid, kGemmThreads, smem, s>>>(op, nchunk, per, err);
 }
 
-// sums the splits in a fixed order into the gradient: weights [nout][kin]
+// sums the splits in a fixed order into the gradient: weights [ncol][kin]
 // and the bias row
-template <int NT>
-__global__ void k_wgrad_reduce(const float* part, int splits, int kin, float* gW, float* gb) {
+__global__ void k_wgrad_reduce(const float* part, int splits, int kin, int ncol, float* gW, float* gb) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;  // (row, j)
-  if (i >= (kin + 1) * NT) return;
-  const int row = i / NT, j = i % NT;
+  if (i >= (kin + 1) * ncol) return;
+  const int row = i / ncol, j = i % ncol;
   float s = 0.f;
-  for (int z = 0; z < splits; ++z) s += part[((int64_t)z * kWgradRows + row) * NT + j];
+  for (int z = 0; z < splits; ++z) s += part[((int64_t)z * kWgradRows + row) * ncol + j];
   if (row < kin) gW[(int64_t)j * kin + row] = s;
   else gb[j] = s;
 }
 
 // ------------------------------------------------------------------ G blocks
-__global__ void k_gnn_g(GnnBufs g) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+// one thread per (block b, node); the blocks of N are kept only for training
+__global__ void __launch_bounds__(kNB, 8) k_gnn_g(GnnBufs g, int keep_n) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = g.ntot;
-  if (n >= nt) return;
-  const float* o = g.o + (int64_t)n * kGOut;
-  const float* E = g.E + (int64_t)n * 100;
-  float L[5][5], N[5][5], Gb[5][5];
-  for (int b = 0; b < 5; ++b) {
-    const int j = b == 0 ? n : g.nbr[4 * n + b - 1];
-    if (j < 0) {
-      for (int k = 0; k < 25; ++k) {
-        g.G[(int64_t)(25 * b + k) * nt + n] = 0.f;
-        g.Gn[(int64_t)(25 * b + k) * nt + n] = 0.f;
-      }
-      continue;
+  if (t >= (int64_t)kGBlocks * nt) return;
+  const int b = (int)(t / nt), n = (int)(t - (int64_t)b * nt);
+  const int j = g.pat[8 * n + b];
+  if (j < 0) {
+    for (int k = 0; k < 25; ++k) {
+      g.Gh[(int64_t)(25 * b + k) * nt + n] = __float2bfloat16(0.f);
+      if (keep_n) g.G[(int64_t)(25 * b + k) * nt + n] = 0.f;
+      if (keep_n) g.Gn[(int64_t)(25 * b + k) * nt + n] = 0.f;
     }
-    for (int r = 0; r < 5; ++r)
-      for (int c = 0; c < 5; ++c) {
-        const int k = 5 * r + c;
-        float val = kGOutScale * o[25 * b + k];
-        if (b > 0) val -= 0.5f * E[25 * (b - 1) + k];
-        N[r][c] = val;
-        g.Gn[(int64_t)(25 * b + k) * nt + n] = val;
-      }
-    if (b == 0)
-      for (int r = 0; r < 5; ++r) N[r][r] += 1.f;
-    load_linv(g.linv, nt, j, L);
-    mul_ab(N, L, Gb);
-    for (int r = 0; r < 5; ++r)
-      for (int c = 0; c < 5; ++c) g.G[(int64_t)(25 * b + 5 * r + c) * nt + n] = Gb[r][c];
+    return;
   }
+  const float* o = g.o + (int64_t)(25 * b) * nt + n;  // component-major
+  const float* E = b > 0 ? g.E + (int64_t)(25 * (b - 1)) * nt + n : nullptr;
+  float L[5][5], N[5][5], Gb[5][5];
+  load_linv(g.linv, nt, j, L);
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      const int k = 5 * r + c;
+      float val = kGOutScale * o[(int64_t)k * nt];
+      if (b > 0) val -= E[(int64_t)k * nt];
+      N[r][c] = val;
+      if (keep_n) g.Gn[(int64_t)(25 * b + k) * nt + n] = val;
+    }
+  if (b == 0)
+#pragma unroll
+    for (int r = 0; r < 5; ++r) N[r][r] += 1.f;
+  mul_ab(N, L, Gb);
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      const int64_t at = (int64_t)(25 * b + 5 * r + c) * nt + n;
+      g.Gh[at] = __float2bfloat16(Gb[r][c]);
+      if (keep_n) g.G[at] = Gb[r][c];
+    }
 }
 
 // ------------------------------------------------- blocked applications
-// y_i = sum_b B_ib x_src(b)  (B = blocks [125][nt] of G or of N (+ I on the
-// self block when add_identity)); x in [5][nt]
-template <class TX>
-__device__ __forceinline__ void apply_rows(const float* Bk, const int* nbr, int nt, const TX* x, int n,
-                                           bool add_identity, float y[5]) {
-  for (int r = 0; r < 5; ++r) y[r] = add_identity ? (float)x[(int64_t)r * nt + n] : 0.f;
-  for (int b = 0; b < 5; ++b) {
-    const int j = b == 0 ? n : nbr[4 * n + b - 1];
-    if (j < 0) continue;
-    float xj[5];
-    for (int c = 0; c < 5; ++c) xj[c] = (float)x[(int64_t)c * nt + j];
-    for (int r = 0; r < 5; ++r) {
-      float s = 0.f;
-      for (int c = 0; c < 5; ++c) s += Bk[(int64_t)(25 * b + 5 * r + c) * nt + n] * xj[c];
-      y[r] += s;
-    }
+// y_n = sum_b G_n,b x_pat(n,b);   x in [5][nt]. Every load is issued before
+// the arithmetic (absent sources read node n with a zero weight), so one
+// memory round trip serves all seven blocks.
+__device__ __forceinline__ float coef(const float* g, int64_t i) { return g[i]; }
+__device__ __forceinline__ float coef(const bf16* g, int64_t i) { return __bfloat162float(g[i]); }
+
+template <class TG, class TX>
+__device__ __forceinline__ void apply_rows(const TG* Gk, const int* pat, int nt, const TX* x, int n, float y[5]) {
+  int src[kGBlocks];
+#pragma unroll
+  for (int b = 0; b < kGBlocks; ++b) src[b] = pat[8 * n + b];
+  float xs[kGBlocks][5];
+#pragma unroll
+  for (int b = 0; b < kGBlocks; ++b) {
+    const int j = src[b] >= 0 ? src[b] : n;
+    const float m = src[b] >= 0 ? 1.f : 0.f;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) xs[b][c] = m * (float)x[(int64_t)c * nt + j];
+  }
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    float s = 0.f;
+#pragma unroll
+    for (int b = 0; b < kGBlocks; ++b)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) s += coef(Gk, (int64_t)(25 * b + 5 * r + c) * nt + n) * xs[b][c];
+    y[r] = s;
   }
 }
-// z_j = sum over the blocks B_ib with src(b) = j of B_ib^T x_i
-template <class TX>
-__device__ __forceinline__ void apply_cols(const float* Bk, const int* nbr, int nt, const TX* x, int n,
-                                           bool add_identity, float z[5]) {
-  for (int c = 0; c < 5; ++c) z[c] = add_identity ? (float)x[(int64_t)c * nt + n] : 0.f;
-  for (int b = 0; b < 5; ++b) {
-    const int i = b == 0 ? n : nbr[4 * n + opp(b - 1)];  // row i refers to n through block b
-    if (i < 0) continue;
-    float xi[5];
-    for (int r = 0; r < 5; ++r) xi[r] = (float)x[(int64_t)r * nt + i];
-    for (int c = 0; c < 5; ++c) {
-      float s = 0.f;
-      for (int r = 0; r < 5; ++r) s += Bk[(int64_t)(25 * b + 5 * r + c) * nt + i] * xi[r];
-      z[c] += s;
+// z_n = sum over the rows i = upat(n, b) of G_i,b^T x_i
+template <class TG, class TX>
+__device__ __forceinline__ void apply_cols(const TG* Gk, const int* upat, int nt, const TX* x, int n, float z[5]) {
+  int row[kGBlocks];
+#pragma unroll
+  for (int b = 0; b < kGBlocks; ++b) row[b] = upat[8 * n + b];
+  float xs[kGBlocks][5];
+#pragma unroll
+  for (int b = 0; b < kGBlocks; ++b) {
+    const int i = row[b] >= 0 ? row[b] : n;
+    const float m = row[b] >= 0 ? 1.f : 0.f;
+#pragma unroll
+    for (int r = 0; r < 5; ++r) xs[b][r] = m * (float)x[(int64_t)r * nt + i];
+  }
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    float s = 0.f;
+#pragma unroll
+    for (int b = 0; b < kGBlocks; ++b) {
+      const int i = row[b] >= 0 ? row[b] : n;
+#pragma unroll
+      for (int r = 0; r < 5; ++r) s += coef(Gk, (int64_t)(25 * b + 5 * r + c) * nt + i) * xs[b][r];
     }
+    z[c] = s;
   }
 }
 
@@ -553,7 +698,7 @@ __global__ void __launch_bounds__(kBlock) k_lp_g(View v, Blocks b, Solver so, Lp
   if (threadIdx.x >= b.blk_count[blk]) return;
   const int n = b.blk_node0[blk] + threadIdx.x;
   float y[5];
-  apply_rows(lx.G, lx.nbr, v.ntot, so.r, n, false, y);
+  apply_rows(lx.G, lx.pat, v.ntot, so.r, n, y);
   for (int k = 0; k < 5; ++k) lx.y[(int64_t)k * v.ntot + n] = y[k];
 }
 
@@ -568,7 +713,7 @@ __global__ void __launch_bounds__(kBlock) k_lp_gt(View v, Blocks b, Solver so, L
   double rz = 0.0, zq = 0.0;
   if (threadIdx.x < b.blk_count[blk]) {
     float z[5];
-    apply_cols(lx.G, lx.nbr, nt, lx.y, n, false, z);
+    apply_cols(lx.G, lx.upat, nt, lx.y, n, z);
     for (int k = 0; k < 5; ++k) {
       const double zk = (double)z[k];
       lx.z[(int64_t)k * nt + n] = zk;
@@ -669,7 +814,7 @@ __global__ void __launch_bounds__(kBlock) k_lp_dir(View v, Blocks b, Solver so, 
 // ------------------------------------------------------------- training
 // FP32 y = A x and y = A^T x of row block n (the FP64 step's spmv_row and
 // spmv_row_t in single precision)
-__device__ void spmv_f(const View& v, const float* x, int n, float y[5]) {
+__device__ __forceinline__ void spmv_f(const View& v, const float* x, int n, float y[5]) {
   const int nt = v.ntot;
   const ClothParams& P = v.cp[v.node_cloth[n]];
   const int u = v.node_u[n], w = v.node_v[n];
@@ -705,7 +850,7 @@ __device__ void spmv_f(const View& v, const float* x, int n, float y[5]) {
   y[3] = ye[0];
   y[4] = ye[1];
 }
-__device__ void spmv_tf(const View& v, const float* x, int n, float y[5]) {
+__device__ __forceinline__ void spmv_tf(const View& v, const float* x, int n, float y[5]) {
   const int nt = v.ntot;
   const ClothParams& P = v.cp[v.node_cloth[n]];
   const int u = v.node_u[n], w = v.node_v[n];
@@ -743,7 +888,7 @@ __device__ void spmv_tf(const View& v, const float* x, int n, float y[5]) {
   y[4] = ye[1];
 }
 
-enum { kVw = 0, kVv, kVu, kVt, kVs, kVe, kVgs, kVgt, kVgu, kVgv, kVcount };
+enum { kVw = 0, kVu, kVs, kVcount };
 __device__ __forceinline__ float* vslot(const GnnBufs& g, int k) { return g.vec + (int64_t)k * 5 * g.ntot; }
 
 // Rademacher probe from a counter hash (splitmix64 finaliser)
@@ -762,134 +907,145 @@ __global__ void k_tr_probe(GnnBufs g, uint64_t seed) {
   for (int c = 0; c < 5; ++c) w[(int64_t)c * g.ntot + n] = rademacher(seed, (uint64_t)c * g.ntot + n);
 }
 
-// v = (I + N)^T w, u = L^-T v; per-block partial of |w|^2 (lpart row 1)
-__global__ void __launch_bounds__(kNB) k_tr_vu(GnnBufs g) {
-  __shared__ double sh[kNB / 32];
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = g.ntot;
-  double ww = 0.0;
-  if (n < nt) {
-    float vv[5], L[5][5];
-    apply_cols(g.Gn, g.nbr, nt, vslot(g, kVw), n, true, vv);
-    load_linv(g.linv, nt, n, L);
-    float* u = vslot(g, kVu);
-    for (int c = 0; c < 5; ++c) {
-      float s = 0.f;
-      for (int r = c; r < 5; ++r) s += L[r][c] * vv[r];
-      u[(int64_t)c * nt + n] = s;
-      const float w = vslot(g, kVw)[(int64_t)c * nt + n];
-      ww += (double)w * w;
-    }
+// inverse and log |det| of a 5 x 5 matrix (Gauss-Jordan with partial pivoting)
+__device__ __forceinline__ float inv5(const float M[5][5], float X[5][5]) {
+  float a[5][10];
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+#pragma unroll
+    for (int c = 0; c < 10; ++c) a[r][c] = c < 5 ? M[r][c] : (c - 5 == r ? 1.f : 0.f);
+  float logdet = 0.f;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    int p = k;
+    float best = fabsf(a[k][k]);
+#pragma unroll
+    for (int r = k + 1; r < 5; ++r)
+      if (fabsf(a[r][k]) > best) {
+        best = fabsf(a[r][k]);
+        p = r;
+      }
+#pragma unroll
+    for (int r = k + 1; r < 5; ++r)
+      if (r == p)
+#pragma unroll
+        for (int c = 0; c < 10; ++c) {
+          const float t = a[k][c];
+          a[k][c] = a[r][c];
+          a[r][c] = t;
+        }
+    const float piv = a[k][k];
+    logdet += logf(fabsf(piv));
+    const float ip = 1.f / piv;
+#pragma unroll
+    for (int c = 0; c < 10; ++c) a[k][c] *= ip;
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+      if (r != k) {
+        const float f = a[r][k];
+#pragma unroll
+        for (int c = 0; c < 10; ++c) a[r][c] -= f * a[k][c];
+      }
   }
-  const double s = blk_sum(ww, sh);
-  if (threadIdx.x == 0) g.lpart[g.nlblk + blockIdx.x] = s;
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+#pragma unroll
+    for (int c = 0; c < 5; ++c) X[r][c] = a[r][5 + c];
+  return logdet;
 }
 
-// s = L^-1 (A u)
-__global__ void k_tr_ts(View v, GnnBufs g) {
+// u = G^T w
+__global__ void k_tr_u(GnnBufs g) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = g.ntot;
   if (n >= nt) return;
-  float t[5], L[5][5];
-  spmv_f(v, vslot(g, kVu), n, t);
-  load_linv(g.linv, nt, n, L);
-  float* s = vslot(g, kVs);
-  for (int r = 0; r < 5; ++r) {
-    float a = 0.f;
-    for (int c = 0; c <= r; ++c) a += L[r][c] * t[c];
-    s[(int64_t)r * nt + n] = a;
-  }
+  float u[5];
+  apply_cols(g.G, g.upat, nt, vslot(g, kVw), n, u);
+  for (int c = 0; c < 5; ++c) vslot(g, kVu)[(int64_t)c * nt + n] = u[c];
 }
 
-// e = (I + N) s - w; per-block partial of |e|^2 (lpart row 0)
-__global__ void __launch_bounds__(kNB) k_tr_e(GnnBufs g) {
+// t = (A + A^T) u / 2, s = L^-1 t; per-block partials of u.t (= w^T G A G^T w,
+// lpart row 0) and of log |det G_n,0| = log |det(I + N_n,0)| + log det L_n^-1 (row 1)
+__global__ void __launch_bounds__(kNB) k_tr_t(View v, GnnBufs g) {
   __shared__ double sh[kNB / 32];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = g.ntot;
-  double ee = 0.0;
+  double ut = 0.0, ld = 0.0;
   if (n < nt) {
-    float y[5];
-    apply_rows(g.Gn, g.nbr, nt, vslot(g, kVs), n, true, y);
+    float t1[5], t2[5], L[5][5];
+    const float* u = vslot(g, kVu);
+    spmv_f(v, u, n, t1);
+    spmv_tf(v, u, n, t2);
+    load_linv(g.linv, nt, n, L);
+#pragma unroll
     for (int r = 0; r < 5; ++r) {
-      const float e = y[r] - vslot(g, kVw)[(int64_t)r * nt + n];
-      vslot(g, kVe)[(int64_t)r * nt + n] = e;
-      ee += (double)e * e;
+      const float t = 0.5f * (t1[r] + t2[r]);
+      ut += (double)u[(int64_t)r * nt + n] * t;
+      t1[r] = t;
     }
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      float a = 0.f;
+#pragma unroll
+      for (int c = 0; c <= r; ++c) a += L[r][c] * t1[c];
+      vslot(g, kVs)[(int64_t)r * nt + n] = a;
+      ld += log((double)L[r][r]);
+    }
+    float N0[5][5], X[5][5];
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) N0[r][c] = g.Gn[(int64_t)(5 * r + c) * nt + n] + (r == c ? 1.f : 0.f);
+    ld += (double)inv5(N0, X);
   }
-  const double s = blk_sum(ee, sh);
-  if (threadIdx.x == 0) g.lpart[blockIdx.x] = s;
+  const double s1 = blk_sum(ut, sh);
+  if (threadIdx.x == 0) g.lpart[blockIdx.x] = s1;
+  const double s2 = blk_sum(ld, sh);
+  if (threadIdx.x == 0) g.lpart[g.nlblk + blockIdx.x] = s2;
 }
 
-// loss = |e|^2 / |w|^2 (fixed-order sums) into lpart[2 nlblk], its scale
-// 2 / |w|^2 into lpart[2 nlblk + 1]
+// loss = log(tr / n) - 2 logdet / n (n = DOFs; fixed-order sums) into
+// lpart[2 nlblk], its scales 2 / tr and 2 / n into the next two entries
 __global__ void k_tr_loss(GnnBufs g) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double ee = 0.0, ww = 0.0;
+  double tr = 0.0, ld = 0.0;
   for (int i = 0; i < g.nlblk; ++i) {
-    ee += g.lpart[i];
-    ww += g.lpart[g.nlblk + i];
+    tr += g.lpart[i];
+    ld += g.lpart[g.nlblk + i];
   }
-  g.lpart[2 * g.nlblk] = ww > 0.0 ? ee / ww : 0.0;
-  g.lpart[2 * g.nlblk + 1] = ww > 0.0 ? 2.0 / ww : 0.0;
+  const double nd = 5.0 * g.ntot;
+  g.lpart[2 * g.nlblk] = tr > 0.0 ? log(tr / nd) - 2.0 * ld / nd : 0.0;
+  g.lpart[2 * g.nlblk + 1] = tr > 0.0 ? 2.0 / tr : 0.0;
+  g.lpart[2 * g.nlblk + 2] = 2.0 / nd;
 }
 
-// ge = (2 / |w|^2) e (in place); gs = (I + N)^T ge; gt = L^-T gs
-__global__ void k_tr_ge(GnnBufs g) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = g.ntot;
-  if (n >= nt) return;
-  const float sc = (float)g.lpart[2 * g.nlblk + 1];
-  for (int r = 0; r < 5; ++r) vslot(g, kVgs)[(int64_t)r * nt + n] = sc * vslot(g, kVe)[(int64_t)r * nt + n];
-}
-__global__ void k_tr_gt(GnnBufs g) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = g.ntot;
-  if (n >= nt) return;
-  float gs[5], L[5][5];
-  apply_cols(g.Gn, g.nbr, nt, vslot(g, kVgs), n, true, gs);
-  load_linv(g.linv, nt, n, L);
-  for (int c = 0; c < 5; ++c) {
-    float s = 0.f;
-    for (int r = c; r < 5; ++r) s += L[r][c] * gs[r];
-    vslot(g, kVgt)[(int64_t)c * nt + n] = s;
-  }
-}
-// gv = L^-1 (A^T gt)
-__global__ void k_tr_gv(View v, GnnBufs g) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = g.ntot;
-  if (n >= nt) return;
-  float gu[5], L[5][5];
-  spmv_tf(v, vslot(g, kVgt), n, gu);
-  load_linv(g.linv, nt, n, L);
-  for (int r = 0; r < 5; ++r) {
-    float a = 0.f;
-    for (int c = 0; c <= r; ++c) a += L[r][c] * gu[c];
-    vslot(g, kVgv)[(int64_t)r * nt + n] = a;
-  }
-}
-// dN_ib = ge_i s_src(b)^T + w_i gv_src(b)^T  ->  d o = 0.1 dN (BF16, GEMM operand)
+// d loss / d N_n,b = (2 / tr) w_n s_src^T - [b = 0] (2 / n) (I + N_n,0)^-T;
+// d o = 0.1 d N (BF16: the head's GEMM operand)
 __global__ void k_tr_do(GnnBufs g) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = g.ntot;
   if (n >= nt) return;
-  float ge[5], w[5];
-  for (int r = 0; r < 5; ++r) {
-    ge[r] = vslot(g, kVgs)[(int64_t)r * nt + n];
-    w[r] = vslot(g, kVw)[(int64_t)r * nt + n];
-  }
+  const float c1 = (float)g.lpart[2 * g.nlblk + 1], c2 = (float)g.lpart[2 * g.nlblk + 2];
+  float w[5];
+  for (int r = 0; r < 5; ++r) w[r] = vslot(g, kVw)[(int64_t)r * nt + n];
+  float N0[5][5], X[5][5];
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+#pragma unroll
+    for (int c = 0; c < 5; ++c) N0[r][c] = g.Gn[(int64_t)(5 * r + c) * nt + n] + (r == c ? 1.f : 0.f);
+  inv5(N0, X);
   bf16* d = g.dob + (int64_t)n * kGOut;
-  for (int b = 0; b < 5; ++b) {
-    const int j = b == 0 ? n : g.nbr[4 * n + b - 1];
-    float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, gv[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int b = 0; b < kGBlocks; ++b) {
+    const int j = g.pat[8 * n + b];
+    float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     if (j >= 0)
-      for (int c = 0; c < 5; ++c) {
-        s[c] = vslot(g, kVs)[(int64_t)c * nt + j];
-        gv[c] = vslot(g, kVgv)[(int64_t)c * nt + j];
-      }
+      for (int c = 0; c < 5; ++c) s[c] = vslot(g, kVs)[(int64_t)c * nt + j];
     for (int r = 0; r < 5; ++r)
-      for (int c = 0; c < 5; ++c)
-        d[25 * b + 5 * r + c] = __float2bfloat16(j >= 0 ? kGOutScale * (ge[r] * s[c] + w[r] * gv[c]) : 0.f);
+      for (int c = 0; c < 5; ++c) {
+        float dn = j >= 0 ? c1 * w[r] * s[c] : 0.f;
+        if (b == 0) dn -= c2 * X[c][r];
+        d[25 * b + 5 * r + c] = __float2bfloat16(kGOutScale * dn);
+      }
   }
   for (int k = kGUsed; k < kGOut; ++k) d[k] = __float2bfloat16(0.f);
 }
@@ -955,11 +1111,11 @@ __global__ void k_refresh(GnnNet net) {
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
-void gnn_neighbours(const View& v, int* nbr, cudaStream_t s) { k_gnn_nbr<<<nblk(v.ntot), kNB, 0, s>>>(v, nbr); }
+void gnn_neighbours(const View& v, const GnnBufs& g, cudaStream_t s) { k_gnn_nbr<<<nblk(v.ntot), kNB, 0, s>>>(v, g); }
 
 void gnn_prepare(const View& v, const GnnBufs& g, cudaStream_t s) {
   k_gnn_linv<<<nblk(v.ntot), kNB, 0, s>>>(v, g.linv, g.chol_ok);
-  k_gnn_feat<<<nblk(v.ntot), kNB, 0, s>>>(v, g);
+  k_gnn_feat<<<(int)((12LL * v.ntot + kNB - 1) / kNB), kNB, 0, s>>>(v, g);
 }
 
 void gnn_forward(const GnnNet& net, const GnnBufs& g, cudaStream_t s) {
@@ -967,22 +1123,24 @@ void gnn_forward(const GnnNet& net, const GnnBufs& g, cudaStream_t s) {
   const int64_t hs = (int64_t)M * kGHid;
   {
     FwdOp<64, kEpiEnc> op{g.f, kGIn, M, nullptr, 0, net.W0, kGIn, net.w + kPb0, nullptr, g.h, g.hb, nullptr, nullptr};
-    launch_gemm(op, M, 1, kGIn / 64, 1, g.err, s);
+    launch_gemm<decltype(op), kGIn / 64>(op, M, 1, kGIn / 64, 1, g.err, s);
   }
   for (int l = 0; l < kGLayers; ++l) {
     FwdOp<64, kEpiLayer> op{g.hb + l * hs, kGHid, M, g.nbr, 1, net.Wl + (int64_t)l * kGHid * kGMsg, kGMsg,
                             net.w + kPb(l), g.h + l * hs, g.h + (l + 1) * hs, g.hb + (l + 1) * hs,
                             g.act + l * hs, nullptr};
-    launch_gemm(op, M, 1, kGMsg / 64, 1, g.err, s);
+    launch_gemm<decltype(op), 2>(op, M, 1, kGMsg / 64, 1, g.err, s);
   }
   {
-    FwdOp<128, kEpiHead> op{g.hb + 3 * hs, kGHid, M, nullptr, 0, net.Wh, kGHid, net.w + kPbh, nullptr, nullptr,
-                            nullptr, nullptr, g.o};
-    launch_gemm(op, M, 1, 1, 1, g.err, s);
+    FwdOp<64, kEpiHead> op{g.hb + 3 * hs, kGHid, M, nullptr, 0, net.Wh, kGHid, net.w + kPbh, nullptr, nullptr,
+                           nullptr, nullptr, g.o};
+    launch_gemm(op, M, kGOut / 64, 1, 1, g.err, s);
   }
 }
 
-void gnn_make_g(const GnnBufs& g, cudaStream_t s) { k_gnn_g<<<nblk(g.ntot), kNB, 0, s>>>(g); }
+void gnn_make_g(const GnnBufs& g, bool keep_n, cudaStream_t s) {
+  k_gnn_g<<<(int)(((int64_t)kGBlocks * g.ntot + kNB - 1) / kNB), kNB, 0, s>>>(g, keep_n ? 1 : 0);
+}
 
 void gnn_refresh_bf16(const GnnNet& net, cudaStream_t s) {
   k_refresh<<<(kGLayers * kGHid * kGMsg + 255) / 256, 256, 0, s>>>(net);
@@ -993,41 +1151,37 @@ void gnn_loss_grad(const View& v, const GnnNet& net, const GnnBufs& g, uint64_t 
   const int M = g.ntot;
   const int64_t hs = (int64_t)M * kGHid;
   if (!probes_given) k_tr_probe<<<nblk(M), kNB, 0, s>>>(g, seed);
-  k_tr_vu<<<g.nlblk, kNB, 0, s>>>(g);
-  k_tr_ts<<<nblk(M), kNB, 0, s>>>(v, g);
-  k_tr_e<<<g.nlblk, kNB, 0, s>>>(g);
+  k_tr_u<<<nblk(M), kNB, 0, s>>>(g);
+  k_tr_t<<<g.nlblk, kNB, 0, s>>>(v, g);
   k_tr_loss<<<1, 32, 0, s>>>(g);
-  k_tr_ge<<<nblk(M), kNB, 0, s>>>(g);
-  k_tr_gt<<<nblk(M), kNB, 0, s>>>(g);
-  k_tr_gv<<<nblk(M), kNB, 0, s>>>(v, g);
   k_tr_do<<<nblk(M), kNB, 0, s>>>(g);
   const int nchunk = (M + 63) / 64;
   const int per = (nchunk + g.nsplit - 1) / g.nsplit;
   const int splits = (nchunk + per - 1) / per;
   // head
   {
-    WgradOp<128> op{g.hb + 3 * hs, kGHid, kGHid, M, nullptr, 0, g.dob, g.wpart};
-    launch_gemm(op, kGHid + 1, 1, nchunk, g.nsplit, g.err, s);
-    k_wgrad_reduce<128><<<((kGHid + 1) * 128 + 255) / 256, 256, 0, s>>>(g.wpart, splits, kGHid, g.grad + kPWh,
-                                                                         g.grad + kPbh);
+    WgradOp<64> op{g.hb + 3 * hs, kGHid, kGHid, M, nullptr, 0, g.dob, kGOut, g.wpart};
+    launch_gemm(op, kGHid + 1, kGOut / 64, nchunk, g.nsplit, g.err, s);
+    k_wgrad_reduce<<<((kGHid + 1) * kGOut + 255) / 256, 256, 0, s>>>(g.wpart, splits, kGHid, kGOut, g.grad + kPWh,
+                                                                      g.grad + kPbh);
     BwdDataOp dop{g.dob, kGOut, M, net.WhT, g.dh, kGHid};
     launch_gemm(dop, M, kGHid / 64, kGOut / 64, 1, g.err, s);
   }
   for (int l = kGLayers - 1; l >= 0; --l) {
     k_relu_bwd<<<(int)((hs + 255) / 256), 256, 0, s>>>(g.dh, g.act + l * hs, nullptr, g.dzb, (int)hs);
-    WgradOp<64> op{g.hb + l * hs, kGHid, kGMsg, M, g.nbr, 1, g.dzb, g.wpart};
+    WgradOp<64> op{g.hb + l * hs, kGHid, kGMsg, M, g.nbr, 1, g.dzb, kGHid, g.wpart};
     launch_gemm(op, kGMsg + 1, 1, nchunk, g.nsplit, g.err, s);
-    k_wgrad_reduce<64><<<((kGMsg + 1) * 64 + 255) / 256, 256, 0, s>>>(g.wpart, splits, kGMsg, g.grad + kPW(l),
-                                                                       g.grad + kPb(l));
+    k_wgrad_reduce<<<((kGMsg + 1) * kGHid + 255) / 256, 256, 0, s>>>(g.wpart, splits, kGMsg, kGHid, g.grad + kPW(l),
+                                                                      g.grad + kPb(l));
     BwdDataOp dop{g.dzb, kGHid, M, net.WlT + (int64_t)l * kGMsg * kGHid, g.dm, kGMsg};
     launch_gemm(dop, M, kGMsg / 64, 1, 1, g.err, s);
     k_msg_bwd<<<(int)((hs + 255) / 256), 256, 0, s>>>(g.dm, g.nbr, g.dh, M, 1);
   }
   k_relu_bwd<<<(int)((hs + 255) / 256), 256, 0, s>>>(g.dh, nullptr, g.h, g.dzb, (int)hs);
-  WgradOp<64> op{g.f, kGIn, kGIn, M, nullptr, 0, g.dzb, g.wpart};
+  WgradOp<64> op{g.f, kGIn, kGIn, M, nullptr, 0, g.dzb, kGHid, g.wpart};
   launch_gemm(op, kGIn + 1, 1, nchunk, g.nsplit, g.err, s);
-  k_wgrad_reduce<64><<<((kGIn + 1) * 64 + 255) / 256, 256, 0, s>>>(g.wpart, splits, kGIn, g.grad + kPW0,
-                                                                    g.grad + kPb0);
+  k_wgrad_reduce<<<((kGIn + 1) * kGHid + 255) / 256, 256, 0, s>>>(g.wpart, splits, kGIn, kGHid, g.grad + kPW0,
+                                                                   g.grad + kPb0);
 }
 
 void gnn_adam(const GnnNet& net, const GnnBufs& g, float* m, float* vv, float lr, int step, cudaStream_t s) {

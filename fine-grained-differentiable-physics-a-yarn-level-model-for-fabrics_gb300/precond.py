@@ -3,7 +3,8 @@
 The reference solves every step with Eigen's Jacobi-preconditioned conjugate
 gradient (src/Solvers.cpp:3-31); that stays the default and the fallback. This
 module adds a graph network over the crossing graph that reads each assembled
-system and emits the blocks of G in M^-1 = G^T G (see ys_gnn.cuh for the
+system and emits the blocks of a block lower-triangular G in M^-1 = G^T G,
+trained on the Kaporin condition number of G A G^T (see ys_gnn.cuh for the
 network and include/yarnsim.h for the C ABI). Training runs on the GPU with the
 library's own BF16 tensor-core forward and backward kernels, on systems the
 simulator generates from seeded batches of cloths like the plain method's
@@ -73,21 +74,21 @@ class LearnedPreconditioner:
         np.save(path, self.params())
 
     def train_step(self, batch: ClothBatch, seed: int, lr: float) -> float:
-        """One Adam step on the systems `batch` assembled last; returns the loss
-        before the step."""
+        """One Adam step on the Kaporin condition number of the systems `batch`
+        assembled last; returns the loss before the step."""
         loss = ctypes.c_double()
         N.check(N.load().ys_gnn_train_step(self._h, batch._h, int(seed), float(lr), ctypes.byref(loss)),
                 "ys_gnn_train_step")
         return loss.value
 
     def loss_grad(self, batch: ClothBatch, probes: Optional[np.ndarray] = None, seed: int = 1) -> dict:
-        """Loss, parameter gradient, network outputs [n][128] and G blocks
-        [n][125] for the batch's last system (no update)."""
+        """Loss, parameter gradient, network outputs [n][192] and G blocks
+        [n][175] for the batch's last system (no update)."""
         n = batch.total_nodes
         loss = ctypes.c_double()
         grad = np.zeros(param_count(), np.float32)
-        out = np.zeros((n, 128), np.float32)
-        gb = np.zeros((n, 125), np.float32)
+        out = np.zeros((n, 192), np.float32)
+        gb = np.zeros((n, 175), np.float32)
         pr = None
         if probes is not None:
             pr = np.ascontiguousarray(probes, np.float32)
@@ -131,8 +132,8 @@ def train(net: LearnedPreconditioner, systems: int = 20000, cloths_per_batch: in
     """Trains on `systems` linear systems the simulator generates: batches of
     `cloths_per_batch` seeded cloths are stepped with Jacobi-PCG for
     `steps_per_batch` steps, and every step's systems (one per cloth) feed one
-    Adam step. The rate decays by cosine to 5 % of lr. Returns the loss
-    history."""
+    Adam step on the Kaporin condition number of G A G^T. The rate decays by
+    cosine to 5 % of lr. Returns the loss history."""
     rng = np.random.default_rng(seed)
     total_steps = max(1, math.ceil(systems / cloths_per_batch))
     hist = []

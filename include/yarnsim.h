@@ -276,36 +276,44 @@ ys_status ys_collider_get_impacts(ys_collider *c, ys_impact *impacts, int64_t ca
 /* ---- learned preconditioner (no counterpart in the reference: its solve is
  * Eigen's Jacobi-PCG, src/Solvers.cpp:3-31, which stays the default and the
  * fallback). A graph network over the crossing graph reads each assembled
- * system and emits the blocks of G in M^-1 = G^T G = L^-T (I + N)^T (I + N) L^-1
- * (L: Cholesky factor of each node's 5 x 5 diagonal block; N: one 5 x 5 block
- * per node and per yarn neighbour). The conjugate-gradient iteration keeps
- * FP64 and the same stopping rule |r| <= tol |b|; M^-1 is applied in FP32 with
- * the flexible (Polak-Ribiere) direction update. */
+ * system and emits a factorised sparse approximate inverse M^-1 = G^T G, G
+ * block lower triangular over the 7-block pattern self, left, down,
+ * left-down, right-down, left-2, down-2 (5 x 5 blocks; G_i,0 = (I + N_i,0)
+ * L_i^-1, G_i,b = N_i,b L_src^-1, L_i the Cholesky factor of node i's
+ * diagonal block). The conjugate-gradient iteration keeps FP64 and the same
+ * stopping rule |r| <= tol |b|; M^-1 is applied in FP32 with the flexible
+ * (Polak-Ribiere) direction update. */
 typedef struct ys_gnn ys_gnn;
 enum { YS_PREC_JACOBI = 0, YS_PREC_LEARNED = 1 };
 /* number of FP32 parameters (packed: W0 [64][128], b0 [64], 3 x (W [64][320],
- * b [64]), Wh [128][64], bh [128]) */
+ * b [64]), Wh [192][64], bh [192]) */
 int32_t ys_gnn_param_count(void);
 /* a network with seeded initial weights (output head zero: the analytic
- * first-order approximate inverse N = -E / 2 on the neighbour blocks) */
+ * first-order approximate inverse G = (I - E_lower) L^-1) */
 ys_status ys_gnn_create(int32_t device, uint64_t seed, ys_gnn **out);
 void ys_gnn_destroy(ys_gnn *g);
 ys_status ys_gnn_get_params(ys_gnn *g, float *out);
 /* also resets the optimiser state */
 ys_status ys_gnn_set_params(ys_gnn *g, const float *in);
-/* One Adam step (rate lr) on the loss |(G A G^T - I) w|^2 / |w|^2 over the
- * systems the batch assembled last (its ys_assemble or ys_step), Rademacher
- * probes w drawn from seed; *loss receives the loss before the step. */
+/* One Adam step (rate lr) on the Kaporin condition number of G A G^T,
+ * loss = log(tr(G A G^T) / n) - (2 / n) log |det G| (n DOFs; the trace from
+ * Rademacher probes drawn from seed, the determinant exact), over the systems
+ * the batch assembled last (its ys_assemble or ys_step); *loss receives the
+ * loss before the step. */
 ys_status ys_gnn_train_step(ys_gnn *g, ys_batch *b, uint64_t seed, float lr, double *loss);
 /* Loss and gradient without an update (probes [total_nodes][5] host, or NULL
- * for seeded probes); outputs [total_nodes][128] network outputs, gblocks
- * [total_nodes][125] blocks of G (self, left, right, down, up; row-major
- * 5 x 5); any output may be NULL. */
+ * for seeded probes); outputs [total_nodes][192] network outputs, gblocks
+ * [total_nodes][175] blocks of G (self, left, down, left-down, right-down,
+ * left-2, down-2; row-major 5 x 5); any output may be NULL. */
 ys_status ys_gnn_loss_grad(ys_gnn *g, ys_batch *b, const float *probes, uint64_t seed, double *loss, float *grad,
                            float *outputs, float *gblocks);
 /* kind YS_PREC_JACOBI (default) or YS_PREC_LEARNED with network g; the batch
  * borrows g, which must outlive its use. Learned steps run launch by launch. */
 ys_status ys_set_preconditioner(ys_batch *b, int32_t kind, ys_gnn *g);
+/* evaluate the network once per `every` learned solves (default 1) and reuse
+ * G in between: a G from an earlier step is still a symmetric positive
+ * definite preconditioner, only a less fitted one */
+ys_status ys_precond_refresh(ys_batch *b, int32_t every);
 /* learned solves so far and how many fell back to Jacobi-PCG */
 ys_status ys_precond_info(ys_batch *b, int64_t *solves, int64_t *fallbacks);
 /* the last assembled system's raw coefficient slots [159][total_nodes] and

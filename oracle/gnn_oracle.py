@@ -5,10 +5,10 @@ The learned preconditioner has no counterpart in the reference (its solve is
 Eigen's Jacobi-PCG, src/Solvers.cpp:3-31), so this oracle restates the
 library's own definition independently of its kernels: the system features,
 the graph network (BF16 operands rounded where the tensor cores read them),
-the blocks of G, and the stochastic Frobenius loss
-|(G A G^T - I) w|^2 / |w|^2, in float64 PyTorch on the CPU; its parameter
-gradient comes from torch.autograd, not from the hand-written backward the GPU
-runs. Rounding to BF16 uses straight-through estimators (the value is rounded,
+the blocks of the block lower-triangular G, and the Kaporin loss
+log(w^T G A G^T w / n) - (2 / n) log |det G|, in float64 PyTorch on the CPU;
+its parameter gradient comes from torch.autograd, not from the hand-written
+backward the GPU runs. Rounding to BF16 uses straight-through estimators (the value is rounded,
 the derivative is the identity), which is what the GPU's BF16 operands amount
 to.
 
@@ -27,7 +27,10 @@ SLOT_LE_NBR, SLOT_EL_NBR, SLOT_EE_NBR = 131, 143, 155
 STENCIL = [(0, 0), (-1, 0), (1, 0), (0, -1), (0, 1), (-2, 0), (2, 0), (0, -2), (0, 2), (-1, -1), (1, -1), (-1, 1),
            (1, 1)]
 YARN_NBR = [(-1, 0), (1, 0), (0, -1), (0, 1)]  # left, right, down, up
-IN, HID, MSG, OUT, LAYERS, OUT_SCALE = 128, 64, 320, 128, 3, 0.1
+IN, HID, MSG, OUT, LAYERS, OUT_SCALE, BLOCKS = 128, 64, 320, 192, 3, 0.1, 7
+# lower pattern of G: self, left, down, left-down, right-down, left-2, down-2
+PATTERN = [(0, 0), (-1, 0), (0, -1), (-1, -1), (1, -1), (-2, 0), (0, -2)]
+UPPER = [(1, 0), (0, 1), (1, 1), (-1, 1), (2, 0), (0, 2)]
 P_W0 = 0
 P_B0 = P_W0 + HID * IN
 P_L0 = P_B0 + HID
@@ -73,6 +76,8 @@ class Topology:
             return np.where(ok, idx + du + dv * self.W, -1)
         self.stencil = np.stack([nb(du, dv) for du, dv in STENCIL], 1)  # [n, 13]
         self.nbr = np.stack([nb(du, dv) for du, dv in YARN_NBR], 1)     # [n, 4]
+        self.pat = np.stack([nb(du, dv) for du, dv in PATTERN], 1)      # [n, 7]
+        self.upper = np.stack([nb(du, dv) for du, dv in UPPER], 1)      # [n, 6]
 
 
 def bf16(x):
@@ -113,6 +118,19 @@ def nbr_block(slots, d):
     return B
 
 
+def offset_block(slots, du, dv):
+    """[n, 5, 5] block A(i, i + (du, dv)): full for yarn neighbours, else the x part."""
+    if (du, dv) in YARN_NBR:
+        return nbr_block(slots, YARN_NBR.index((du, dv)))
+    n = slots.shape[1]
+    B = np.zeros((n, 5, 5))
+    s = STENCIL.index((du, dv))
+    for r in range(3):
+        for c in range(3):
+            B[:, r, c] = slots[SLOT_LL + 9 * s + 3 * r + c]
+    return B
+
+
 def block_factor(slots):
     """L^-1 [n, 5, 5] (FP32 values) and the factorisation flags."""
     D = diag_blocks(slots)
@@ -134,34 +152,36 @@ def block_factor(slots):
     return Linv.astype(np.float32).astype(np.float64), ok
 
 
+def scaled(slots, topo, Linv, du, dv, idx):
+    """E = L_i^-1 A(i, j) L_j^-T for j = idx (-1: zero), in FP32 values."""
+    m = idx >= 0
+    Lj = Linv[np.where(m, idx, 0)]
+    E = Linv @ offset_block(slots, du, dv) @ np.transpose(Lj, (0, 2, 1))
+    E[~m] = 0.0
+    return E.astype(np.float32).astype(np.float64)
+
+
 def features(slots, topo: Topology, Linv, ok):
-    """f [n, 128] (before BF16 rounding) and the scaled neighbour blocks E [n, 4, 5, 5]."""
+    """f [n, 128] (before BF16 rounding) and the scaled couplings E [n, 6, 5, 5]
+    of the lower-pattern blocks 1..6."""
     n = topo.n
     f = np.zeros((n, IN))
-    E = np.zeros((n, 4, 5, 5))
+    E = np.zeros((n, 6, 5, 5))
     sl32 = slots.astype(np.float32).astype(np.float64)
-    for d in range(4):
-        j = topo.nbr[:, d]
-        B = nbr_block(sl32, d)
-        m = j >= 0
-        Lj = Linv[np.where(m, j, 0)]
-        Ed = Linv @ B @ np.transpose(Lj, (0, 2, 1))
-        Ed[~m] = 0.0
-        E[:, d] = Ed.astype(np.float32).astype(np.float64)
-        f[:, 25 * d:25 * d + 25] = E[:, d].reshape(n, 25)
-    for s in range(5, 13):
-        j = topo.stencil[:, s]
-        m = j >= 0
-        LL = np.stack([np.stack([sl32[SLOT_LL + 9 * s + 3 * r + c] for c in range(3)], -1) for r in range(3)], -2)
-        Lj = Linv[np.where(m, j, 0)][:, :3, :3]
-        T = Linv[:, :3, :3] @ LL @ np.transpose(Lj, (0, 2, 1))
-        nrm = np.sqrt((T ** 2).sum((1, 2)))
-        f[:, 100 + s - 5] = np.where(m, nrm, 0.0)
-    f[:, 108] = (~ok).astype(float)
-    f[:, 109] = topo.interior.astype(float)
-    f[:, 110] = topo.fixed.astype(float)
-    f[:, 111] = ((topo.u == 0) | (topo.u == topo.W - 1)).astype(float)
-    f[:, 112] = ((topo.v == 0) | (topo.v == topo.H - 1)).astype(float)
+    for b in range(1, BLOCKS):
+        E[:, b - 1] = scaled(sl32, topo, Linv, *PATTERN[b], topo.pat[:, b])
+        if b <= 2:
+            f[:, 25 * (b - 1):25 * b] = E[:, b - 1].reshape(n, 25)
+        else:
+            f[:, 50 + 9 * (b - 3):59 + 9 * (b - 3)] = E[:, b - 1, :3, :3].reshape(n, 9)
+    for q, (du, dv) in enumerate(UPPER):
+        Eu = scaled(sl32, topo, Linv, du, dv, topo.upper[:, q])
+        f[:, 86 + q] = np.sqrt((Eu ** 2).sum((1, 2)))
+    f[:, 92] = (~ok).astype(float)
+    f[:, 93] = topo.interior.astype(float)
+    f[:, 94] = topo.fixed.astype(float)
+    f[:, 95] = ((topo.u == 0) | (topo.u == topo.W - 1)).astype(float)
+    f[:, 96] = ((topo.v == 0) | (topo.v == topo.H - 1)).astype(float)
     return f, E
 
 
@@ -182,49 +202,36 @@ def network(params, f, topo: Topology):
 
 
 def n_blocks(o, E, topo: Topology):
-    """N [n, 5, 5, 5] (block b: self, left, right, down, up)."""
+    """N [n, 7, 5, 5] over the lower pattern (zero where the source is outside)."""
     n = topo.n
     Ns = [OUT_SCALE * o[:, 0:25].reshape(n, 5, 5)]
     Et = torch.as_tensor(E)
-    for d in range(4):
-        m = torch.as_tensor(topo.nbr[:, d] >= 0, dtype=o.dtype).view(n, 1, 1)
-        Ns.append(m * (OUT_SCALE * o[:, 25 + 25 * d:50 + 25 * d].reshape(n, 5, 5) - 0.5 * Et[:, d]))
+    for b in range(1, BLOCKS):
+        m = torch.as_tensor(topo.pat[:, b] >= 0, dtype=o.dtype).view(n, 1, 1)
+        Ns.append(m * (OUT_SCALE * o[:, 25 * b:25 * b + 25].reshape(n, 5, 5) - Et[:, b - 1]))
     return torch.stack(Ns, 1)
 
 
 def g_blocks(Nb, Linv, topo: Topology):
-    n = topo.n
+    """G [n, 7, 5, 5]: (I + N_0) L_i^-1 and N_b L_src^-1."""
     Lt = torch.as_tensor(Linv)
     eye = torch.eye(5, dtype=Nb.dtype)
     out = [(eye + Nb[:, 0]) @ Lt]
-    for d in range(4):
-        j = topo.nbr[:, d]
-        Lj = Lt[torch.as_tensor(np.where(j >= 0, j, 0))]
-        out.append(Nb[:, d + 1] @ Lj)
+    for b in range(1, BLOCKS):
+        j = topo.pat[:, b]
+        out.append(Nb[:, b] @ Lt[torch.as_tensor(np.where(j >= 0, j, 0))])
     return torch.stack(out, 1)
 
 
-def apply_rows(Nb, x, topo: Topology):
-    """y_i = x_i + sum_b N_ib x_src(b); x [n, 5]."""
-    n = topo.n
-    xz = torch.cat([x, torch.zeros(1, 5, dtype=x.dtype)], 0)
-    y = x + torch.einsum("nrc,nc->nr", Nb[:, 0], x)
-    for d in range(4):
-        j = torch.as_tensor(np.where(topo.nbr[:, d] >= 0, topo.nbr[:, d], n))
-        y = y + torch.einsum("nrc,nc->nr", Nb[:, d + 1], xz[j])
-    return y
-
-
-def apply_cols(Nb, x, topo: Topology):
-    """z_j = x_j + sum over blocks N_ib with src(b) = j of N_ib^T x_i."""
-    n = topo.n
-    z = x + torch.einsum("nrc,nr->nc", Nb[:, 0], x)
-    for d in range(4):
-        j = topo.nbr[:, d]
+def apply_gt(Gb, w, topo: Topology):
+    """u = G^T w (each row's blocks scattered onto their sources)."""
+    u = torch.einsum("nrc,nr->nc", Gb[:, 0], w)
+    for b in range(1, BLOCKS):
+        j = topo.pat[:, b]
         m = j >= 0
-        contrib = torch.einsum("nrc,nr->nc", Nb[:, d + 1], x)
-        z = z.index_add(0, torch.as_tensor(j[m]), contrib[torch.as_tensor(m)])
-    return z
+        contrib = torch.einsum("nrc,nr->nc", Gb[:, b], w)
+        u = u.index_add(0, torch.as_tensor(j[m]), contrib[torch.as_tensor(m)])
+    return u
 
 
 def spmv(slots, x, topo: Topology):
@@ -260,24 +267,23 @@ def spmv(slots, x, topo: Topology):
 
 
 def evaluate(slots, topo: Topology, params, probes):
-    """dict(loss, grad [N_PARAMS], o [n, 128], G [n, 125], f [n, 128])."""
+    """dict(loss, grad [N_PARAMS], o [n, 192], G [n, 175], f, E, Linv, chol_ok)."""
     Linv, ok = block_factor(slots)
     f, E = features(slots, topo, Linv, ok)
     p = torch.as_tensor(np.asarray(params, np.float64), dtype=torch.float64).requires_grad_(True)
     o = network(p, torch.as_tensor(f), topo)
     Nb = n_blocks(o, E, topo)
+    Gb = g_blocks(Nb, Linv, topo)
     w = torch.as_tensor(np.asarray(probes, np.float64))
-    Lt = torch.as_tensor(Linv)
-    v = apply_cols(Nb, w, topo)
-    u = torch.einsum("nrc,nr->nc", Lt, v)          # L^-T v
-    t = spmv(slots, u, topo)
-    s = torch.einsum("nrc,nc->nr", Lt, t)          # L^-1 t
-    y = apply_rows(Nb, s, topo)
-    loss = ((y - w) ** 2).sum() / (w ** 2).sum()
+    u = apply_gt(Gb, w, topo)
+    tr = (u * spmv(slots, u, topo)).sum()
+    nd = 5.0 * topo.n
+    eye = torch.eye(5, dtype=torch.float64)
+    logdet = torch.linalg.slogdet(eye + Nb[:, 0])[1].sum() + float(np.log(np.diagonal(Linv, 0, 1, 2)).sum())
+    loss = torch.log(tr / nd) - 2.0 * logdet / nd
     loss.backward()
-    G = g_blocks(Nb.detach(), Linv, topo).reshape(topo.n, 125)
-    return dict(loss=float(loss.detach()), grad=p.grad.numpy().copy(), o=o.detach().numpy(), G=G.numpy(), f=f, E=E,
-                Linv=Linv, chol_ok=ok)
+    return dict(loss=float(loss.detach()), grad=p.grad.numpy().copy(), o=o.detach().numpy(),
+                G=Gb.detach().reshape(topo.n, 175).numpy(), f=f, E=E, Linv=Linv, chol_ok=ok)
 
 
 def init_params(seed: int) -> np.ndarray:

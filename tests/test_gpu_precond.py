@@ -1,7 +1,7 @@
 """Learned preconditioner on the GPU: the tcgen05 GEMM against torch, the
-network's outputs, G blocks, loss and hand-written gradient against the CPU
-oracle (torch float64 autograd), training, and the learned solve against
-Jacobi-PCG at the same FP64 residual."""
+network's outputs, G blocks, Kaporin loss and hand-written gradient against
+the CPU oracle (torch float64 autograd), training, and the learned solve
+against Jacobi-PCG at the same FP64 residual."""
 import os
 import sys
 
@@ -64,9 +64,9 @@ def rel(a, b):
 
 
 def test_network_and_gradient_match_oracle():
-    """Outputs, G blocks and loss within BF16 tolerance (2e-2, 2e-2, 1e-2
-    relative); the hand-written gradient within 5e-2 relative of the oracle's
-    autograd gradient, cosine >= 0.998."""
+    """Outputs and G blocks within BF16 tolerance (2e-2 relative), the loss
+    within 2e-3 absolute (a logarithm near 0); the hand-written gradient within
+    5e-2 relative of the oracle's autograd gradient, cosine >= 0.998."""
     b, specs = stepped_batch(11, 3, 5, 9)
     params = go.init_params(3)
     net = ys.LearnedPreconditioner(params=params)
@@ -74,12 +74,12 @@ def test_network_and_gradient_match_oracle():
     w = go.rademacher(9, n)
     gpu = net.loss_grad(b, probes=w)
     seeded = net.loss_grad(b, seed=9)
-    assert abs(seeded["loss"] - gpu["loss"]) <= 1e-6 * gpu["loss"]
+    assert abs(seeded["loss"] - gpu["loss"]) <= 1e-9
     slots, _ = b.system_slots()
     ora = go.evaluate(slots, topo_of(specs), params, w)
     assert rel(gpu["outputs"], ora["o"]) < 2e-2
     assert rel(gpu["G"], ora["G"]) < 2e-2
-    assert abs(gpu["loss"] - ora["loss"]) <= 1e-2 * ora["loss"]
+    assert abs(gpu["loss"] - ora["loss"]) <= 2e-3
     g, o = gpu["grad"].astype(np.float64), ora["grad"]
     assert rel(g, o) < 5e-2
     assert g @ o / (np.linalg.norm(g) * np.linalg.norm(o)) >= 0.998
@@ -94,11 +94,17 @@ def test_training_lowers_the_loss():
     net = ys.LearnedPreconditioner(seed=1)
     b, _ = stepped_batch(12, 16, 5, 20, steps=1)
     losses = []
-    for k in range(80):
+    for k in range(40):
         b.step(1e-3, tol=1e-10)
         losses.append(net.train_step(b, seed=k + 1, lr=2e-3))
     assert np.isfinite(losses).all()
-    assert np.mean(losses[-8:]) < 0.85 * np.mean(losses[:8])
+    # the Kaporin loss is log kappa / n plus a per-system constant: compare
+    # the same system before and after
+    before = net.loss_grad(b, seed=99)["loss"]
+    for k in range(40):
+        net.train_step(b, seed=200 + k, lr=2e-3)
+    after = net.loss_grad(b, seed=99)["loss"]
+    assert after < before
     b.close()
     net.close()
 
@@ -168,3 +174,19 @@ def test_broken_network_falls_back_to_jacobi():
     b.close()
     ref.close()
     net.close()
+
+
+def test_trained_network_lowers_the_kaporin_number_on_held_out_systems():
+    """What training adds to the untrained network (the analytic first-order
+    inverse): a lower Kaporin condition number of G A G^T on systems it never
+    saw (same systems, same probes; the loss differs from log kappa / n only
+    by the systems' own log det A / n)."""
+    b, _ = stepped_batch(4242, 24, 10, 45, steps=6)
+    trained = trained_net()
+    untrained = ys.LearnedPreconditioner(seed=0)
+    lt = trained.loss_grad(b, seed=5)["loss"]
+    lu = untrained.loss_grad(b, seed=5)["loss"]
+    assert lt < lu
+    b.close()
+    trained.close()
+    untrained.close()

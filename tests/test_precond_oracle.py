@@ -1,7 +1,9 @@
 """The learned preconditioner's CPU oracle (oracle/gnn_oracle.py), checked on
 its own: its autograd gradient against central finite differences (BF16
-rounding switched off, so the loss is smooth), M^-1 = G^T G symmetric positive
-semi-definite, and the probe generator's Rademacher signs."""
+rounding switched off, so the loss is smooth), G block lower triangular with
+M^-1 = G^T G symmetric positive definite and log |det G| the sum over its
+diagonal blocks, the untrained network's analytic inverse, and the probe
+generator's Rademacher signs."""
 import os
 import sys
 
@@ -55,39 +57,49 @@ def test_oracle_gradient_matches_finite_differences(smooth):
         assert abs(fd - an) <= 1e-6 * max(1.0, abs(an)), (fd, an)
 
 
-def test_preconditioner_is_symmetric_psd():
+def dense_g(r, topo):
+    n = topo.n
+    G = np.zeros((5 * n, 5 * n))
+    Gb = r["G"].reshape(n, 7, 5, 5)
+    for i in range(n):
+        for b in range(7):
+            j = topo.pat[i, b]
+            if j >= 0:
+                G[5 * i:5 * i + 5, 5 * j:5 * j + 5] = Gb[i, b]
+    return G
+
+
+def test_preconditioner_is_block_lower_triangular_and_spd():
     topo = go.Topology([(5, 5)], handles=[[(0, 0), (4, 0)]])
     slots = synthetic_system(topo, 2)
     r = go.evaluate(slots, topo, go.init_params(4), go.rademacher(3, topo.n))
+    G = dense_g(r, topo)
     n = topo.n
-    G = np.zeros((5 * n, 5 * n))
-    Gb = r["G"].reshape(n, 5, 5, 5)
     for i in range(n):
-        for b in range(5):
-            j = i if b == 0 else topo.nbr[i, b - 1]
-            if j >= 0:
-                G[5 * i:5 * i + 5, 5 * j:5 * j + 5] = Gb[i, b]
+        assert not G[5 * i:5 * i + 5, 5 * i + 5:].any()  # nothing right of the diagonal block
     M = G.T @ G
     assert np.allclose(M, M.T)
-    assert np.linalg.eigvalsh(M).min() > -1e-12
+    assert np.linalg.eigvalsh(M).min() > 0.0
+    ld = np.linalg.slogdet(G)[1]
+    blocks = sum(np.linalg.slogdet(G[5 * i:5 * i + 5, 5 * i:5 * i + 5])[1] for i in range(n))
+    assert abs(ld - blocks) < 1e-8 * max(1.0, abs(ld))
 
 
 def test_untrained_head_gives_the_analytic_inverse():
-    """Head weights and bias zero: N is -E / 2 on the neighbour blocks, zero on
-    the node itself, whatever the hidden layers compute."""
+    """Head weights and bias zero: G = (I - E_lower) L^-1 blockwise."""
     topo = go.Topology([(4, 5)], handles=[[(0, 0)]])
     slots = synthetic_system(topo, 3)
     p = go.init_params(5)
     p[go.P_WH:] = 0.0
     r = go.evaluate(slots, topo, p, go.rademacher(1, topo.n))
     assert np.abs(r["o"]).max() == 0.0
-    Gb = r["G"].reshape(topo.n, 5, 5, 5)
+    Gb = r["G"].reshape(topo.n, 7, 5, 5)
     for i in range(topo.n):
         assert np.allclose(Gb[i, 0], r["Linv"][i])
-        for d in range(4):
-            j = topo.nbr[i, d]
+        for b in range(1, 7):
+            j = topo.pat[i, b]
             if j >= 0:
-                assert np.allclose(Gb[i, d + 1], -0.5 * r["E"][i, d] @ r["Linv"][j])
+                assert np.allclose(Gb[i, b], -r["E"][i, b - 1] @ r["Linv"][j])
 
 
 def test_rademacher_signs_are_balanced():
