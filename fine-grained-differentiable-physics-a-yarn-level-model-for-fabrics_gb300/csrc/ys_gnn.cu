@@ -354,13 +354,22 @@ __global__ void __launch_bounds__(kGemmThreads) k_tc_gemm(Op op, int nchunk_tota
       for (int i = 0; i < 16; ++i) stage[row * 33 + 16 + i] = acc[i];
       __syncthreads();
       // row-major outputs: a warp stores 32 columns of a row; column-major
-      // ones (Op::kColMajor): 32 rows of a column. Unrolled so that the loads
-      // an epilogue makes (bias, residual) are in flight together.
-#pragma unroll 8
-      for (int k = 0; k < tc::kTileM * 32 / kGemmThreads; ++k) {
+      // ones (Op::kColMajor): 32 rows of a column. The operands an epilogue
+      // reads (bias, residual) are all loaded before the first store, so
+      // they are in flight together.
+      constexpr int kPer = tc::kTileM * 32 / kGemmThreads;
+      float2 pre[kPer];
+#pragma unroll
+      for (int k = 0; k < kPer; ++k) {
         const int i = threadIdx.x + k * kGemmThreads;
         const int r = Op::kColMajor ? (i & 127) : (i >> 5), cc = Op::kColMajor ? (i >> 7) : (i & 31);
-        op.store(m0 + r, n0 + c + cc, stage[r * 33 + cc]);
+        pre[k] = op.prefetch(m0 + r, n0 + c + cc);
+      }
+#pragma unroll
+      for (int k = 0; k < kPer; ++k) {
+        const int i = threadIdx.x + k * kGemmThreads;
+        const int r = Op::kColMajor ? (i & 127) : (i >> 5), cc = Op::kColMajor ? (i >> 7) : (i & 31);
+        op.store(m0 + r, n0 + c + cc, stage[r * 33 + cc], pre[k]);
       }
       __syncthreads();
     }
@@ -422,9 +431,14 @@ struct FwdOp {
   float* o_out;
   __device__ void stage_a(uint8_t* s, int m0, int kc) const { stage_rows(s, X, ld, M, nbr, gather != 0, m0, kc); }
   __device__ void stage_b(uint8_t* s, int n0, int kc) const { stage_weights<NT>(s, W, K, n0, kc); }
-  __device__ void store(int node, int j, float acc) const {
+  // (bias, residual) of output (node, j)
+  __device__ float2 prefetch(int node, int j) const {
+    if (node >= M) return make_float2(0.f, 0.f);
+    return make_float2(bias[j], EPI == kEpiLayer ? h_in[(int64_t)node * kGHid + j] : 0.f);
+  }
+  __device__ void store(int node, int j, float acc, float2 pre) const {
     if (node >= M) return;
-    const float z = acc + bias[j];
+    const float z = acc + pre.x;
     if (EPI == kEpiHead) {
       o_out[(int64_t)j * M + node] = z;
     } else {
@@ -433,7 +447,7 @@ struct FwdOp {
       float hn = a;
       if (EPI == kEpiLayer) {
         act_out[at] = __float2bfloat16(a);
-        hn = h_in[at] + a;
+        hn = pre.y + a;
       }
       h_out[at] = hn;
       hb_out[at] = __float2bfloat16(hn);
@@ -452,7 +466,8 @@ struct BwdDataOp {
   int kin;
   __device__ void stage_a(uint8_t* s, int m0, int kc) const { stage_rows(s, dZ, nout, M, nullptr, false, m0, kc); }
   __device__ void stage_b(uint8_t* s, int n0, int kc) const { stage_weights<NT>(s, WT, nout, n0, kc); }
-  __device__ void store(int node, int col, float acc) const {
+  __device__ float2 prefetch(int, int) const { return make_float2(0.f, 0.f); }
+  __device__ void store(int node, int col, float acc, float2) const {
     if (node < M) out[(int64_t)node * kin + col] = acc;
   }
 };
@@ -500,7 +515,8 @@ struct WgradOp {
       store1(s, n, kk, node < nodes ? dZ[(int64_t)node * ldz + n0 + n] : __float2bfloat16(0.f));
     }
   }
-  __device__ void store(int row, int col, float acc) const {
+  __device__ float2 prefetch(int, int) const { return make_float2(0.f, 0.f); }
+  __device__ void store(int row, int col, float acc, float2) const {
     if (row <= kin) part[((int64_t)blockIdx.z * kWgradRows + row) * ldz + col] = acc;
   }
 };
@@ -516,7 +532,8 @@ struct PlainOp {
   int M, N, K;
   __device__ void stage_a(uint8_t* s, int m0, int kc) const { stage_rows(s, A, K, M, nullptr, false, m0, kc); }
   __device__ void stage_b(uint8_t* s, int n0, int kc) const { stage_weights<NT>(s, B, K, n0, kc); }
-  __device__ void store(int m, int col, float acc) const {
+  __device__ float2 prefetch(int, int) const { return make_float2(0.f, 0.f); }
+  __device__ void store(int m, int col, float acc, float2) const {
     if (m < M) C[(int64_t)m * N + col] = acc;
   }
 };
