@@ -261,9 +261,13 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o) {
   }
   const T du = ldT<T>(v.UV, v.dUV, k, nt, n1) - ldT<T>(v.UV, v.dUV, k, nt, n0);
   const T e0 = ldT<T>(v.UVD, v.dUVD, k, nt, n0), e1 = ldT<T>(v.UVD, v.dUVD, k, nt, n1);
-  for (int i = 0; i < 3; ++i) { dx[i] = x1[i] - x0[i]; w[i] = dx[i] / du; }
+  // reciprocals of the Eulerian length and of the length: one division each,
+  // the terms below multiply by them
+  const T idu = 1.0 / du, idu2 = idu * idu, idu3 = idu2 * idu;
+  for (int i = 0; i < 3; ++i) { dx[i] = x1[i] - x0[i]; w[i] = dx[i] * idu; }
   const T l = norm3(dx);
-  for (int i = 0; i < 3; ++i) { d[i] = dx[i] / l; o.d[i] = d[i]; }
+  const T il = 1.0 / l;
+  for (int i = 0; i < 3; ++i) { d[i] = dx[i] * il; o.d[i] = d[i]; }
   for (int i = 0; i < 3; ++i) { o.V[i] = a0[i]; o.V[4 + i] = a1[i]; }
   o.V[3] = o.in[0] ? e0 : 0.0;
   o.V[7] = o.in[1] ? e1 : 0.0;
@@ -328,14 +332,14 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o) {
     if (o.in[0]) acc_F(o, 3, -fe);
     if (o.in[1]) acc_F(o, 7, fe);
     // LL = (ks / l) P - (ks / du) I, +LL on (0,0), (1,1) and -LL across
-    const T cP = ks / l, cI = -(ks / du);
+    const T cP = ks * il, cI = -(ks * idu);
     acc_LLp(o, 0, 0, cP); acc_LLp(o, 1, 0, -cP); acc_LLp(o, 0, 1, -cP); acc_LLp(o, 1, 1, cP);
     acc_LLi(o, kK, 0, 0, cI); acc_LLi(o, kK, 1, 0, -cI); acc_LLi(o, kK, 0, 1, -cI); acc_LLi(o, kK, 1, 1, cI);
-    const T EE = -ks * ((nw * nw) / du);
+    const T EE = -ks * ((nw * nw) * idu);
     T LE[3], EL[3], nLE[3], nEL[3];
     for (int r = 0; r < 3; ++r) {
-      LE[r] = ks * (nw / du) * d[r];
-      EL[r] = ks / du * w[r];
+      LE[r] = ks * (nw * idu) * d[r];
+      EL[r] = ks * idu * w[r];
       nLE[r] = -LE[r];
       nEL[r] = -EL[r];
     }
@@ -378,38 +382,38 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o) {
   const T r6 = (1.0 / 6.0) * rho;
   const T sc = 1.0 / 6.0 * rho * du;
   const T wSae = dot3(w, Sae), wSea = dot3(w, Sea);
-  const T pj = -(-1.0 / du);  // (-w_x0)_j for the active component j
+  const T pj = -(-idu);  // (-w_x0)_j for the active component j
   EdgeJac<T> C;
 
   // ---- Inertia_F (src/PhysicsCloth.cpp:1071-1186)
   {
     for (int j = 0; j < 3; ++j) {
-      const T sj = (-2.0 / (du * du) * dx[j]);
+      const T sj = (-2.0 * idu2 * dx[j]);
       const T T0 = 0.5 * (sc * (pj * Sae[j] + pj * Sea[j] + sj * See));
       acc_F(o, j, T0);
       acc_F(o, 4 + j, -T0);
     }
     const T QM = Saa - wSae - wSea + wTw * See;
-    const T Quv = (-1.0 / du) * wSae + (-1.0 / du) * wSea + (2.0 / du) * wTw * See;
+    const T Quv = (-idu) * wSae + (-idu) * wSea + (2.0 * idu) * wTw * See;
     const T Tuv0 = 0.5 * (-(1.0 / 6.0) * rho * QM + (1.0 / 6.0) * rho * du * Quv);
     if (o.in[0]) acc_F(o, 3, Tuv0);
     if (o.in[1]) acc_F(o, 7, -Tuv0);
   }
   // ---- Inertia_D_Pos (src/PhysicsCloth.cpp:1188-1601)
   {
-    const T T00 = 0.5 * (r6 * ((2 / (du * du)) * See));
+    const T T00 = 0.5 * (r6 * ((2.0 * idu2) * See));
     T Tx0uv0[3], Tuv0x0[3];
     for (int j = 0; j < 3; ++j) {
-      const T Qx0 = pj * Sae[j] + pj * Sea[j] + (-2.0 / (du * du) * dx[j]) * See;
-      const T c2 = 1.0 / (du * du);
+      const T Qx0 = pj * Sae[j] + pj * Sea[j] + (-2.0 * idu2 * dx[j]) * See;
+      const T c2 = idu2;
       // the sign-asymmetric mixed block of src/PhysicsCloth.cpp:1357-1361
-      const T Qx0uv0 = (-c2) * Sae[j] + (-(-c2)) * Sea[j] + ((-4.0 / (du * du)) * w[j]) * See;
+      const T Qx0uv0 = (-c2) * Sae[j] + (-(-c2)) * Sea[j] + ((-4.0 * idu2) * w[j]) * See;
       Tx0uv0[j] = 0.5 * ((-1.0 / 6.0) * rho * Qx0 + (1.0 / 6.0) * rho * du * Qx0uv0);
       Tuv0x0[j] = 0.5 * ((-1.0 / 6.0) * rho * Qx0 + (1.0 / 6.0) * rho * du * (-Qx0uv0));
     }
-    const T Quv0 = (-1.0 / du) * wSae + (-1.0 / du) * wSea + (2.0 / du) * wTw * See;
-    const T c6 = 2 / (du * du);
-    const T Quvuv = (-c6) * wSae + (-c6) * wSea + (6 / (du * du)) * wTw * See;
+    const T Quv0 = (-idu) * wSae + (-idu) * wSea + (2.0 * idu) * wTw * See;
+    const T c6 = 2.0 * idu2;
+    const T Quvuv = (-c6) * wSae + (-c6) * wSea + (6.0 * idu2) * wTw * See;
     const T Tuu = 0.5 * ((-1.0 / 6.0) * rho * Quv0 - (1.0 / 6.0) * rho * Quv0 + (1.0 / 6.0) * rho * du * Quvuv);
     for (int p = 0; p < 4; ++p) {
       const double sgn = ((p >> 1) == (p & 1)) ? 1.0 : -1.0;
@@ -428,11 +432,11 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o) {
       T lec[3], elr[3];
       const T wm = dot3(w, ma_[b]);
       for (int r = 0; r < 3; ++r) {
-        lec[r] = sc * (pj * ma_[b][r] + (-2.0 / (du * du) * dx[r]) * me_[b]);
-        elr[r] = -(1.0 / 6.0) * rho * (ma_[b][r] - w[r] * me_[b]) + (1.0 / 6.0) * rho * du * ((-1.0 / du) * w[r] * me_[b]);
+        lec[r] = sc * (pj * ma_[b][r] + (-2.0 * idu2 * dx[r]) * me_[b]);
+        elr[r] = -(1.0 / 6.0) * rho * (ma_[b][r] - w[r] * me_[b]) + (1.0 / 6.0) * rho * du * ((-idu) * w[r] * me_[b]);
       }
       const T eev = -(1.0 / 6.0) * rho * (-wm + wTw * me_[b]) +
-                         (1.0 / 6.0) * rho * du * ((-1.0 / du) * wm + (2.0 / du) * wTw * me_[b]);
+                         (1.0 / 6.0) * rho * du * ((-idu) * wm + (2.0 * idu) * wTw * me_[b]);
       for (int a = 0; a < 2; ++a) {
         const double sgn = a == 0 ? 1.0 : -1.0;  // rows of x1 / uv1 are the negated rows of x0 / uv0
         const int p = 2 * a + b;
@@ -447,7 +451,7 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o) {
   {
     const T dud = e1 - e0;
     T wd[3];
-    for (int i = 0; i < 3; ++i) wd[i] = ((a1[i] - a0[i]) * du - dx[i] * dud) / (du * du);
+    for (int i = 0; i < 3; ++i) wd[i] = ((a1[i] - a0[i]) * du - dx[i] * dud) * idu2;
     const T wTwd = dot3(w, wd) + dot3(wd, w);
     // B_M m and B_dot m for m = m0, m1 (4-vectors); M_dot qdot = r6 dud (B_M m) + r6 du (B_dot m)
     T BMm[2][4], Bdm[2][4], r[8];
@@ -466,15 +470,15 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o) {
     // MDotVDot_D_Pos, added (src/PhysicsCloth.cpp:2154-2234)
     for (int t = 0; t < 2; ++t) {
       const double sw = t == 0 ? -1.0 : 1.0;
-      const T wxj = sw * (1.0 / du);
+      const T wxj = sw * idu;
       const T P1 = -wxj;
-      const T wdxj = t == 0 ? (dud / (du * du)) : -(dud / (du * du));
+      const T wdxj = t == 0 ? (dud * idu2) : -(dud * idu2);
       const T P2 = -wdxj;
       T wuv[3], wduv[3];
-      for (int i = 0; i < 3; ++i) wuv[i] = (sw * w[i]) / du;
-      const T wTwuv = sw * (2 / du) * wTw;
+      for (int i = 0; i < 3; ++i) wuv[i] = (sw * w[i]) * idu;
+      const T wTwuv = sw * (2.0 * idu) * wTw;
       for (int i = 0; i < 3; ++i) {
-        wduv[i] = (a1[i] - a0[i]) / (du * du) - (4 * dx[i] * dud) / (du * du * du);
+        wduv[i] = (a1[i] - a0[i]) * idu2 - (4 * dx[i] * dud) * idu3;
         if (t == 1) wduv[i] = -wduv[i];
       }
       const T wTwduv = 2 * dot3(wuv, wd) + 2 * dot3(wduv, w);
@@ -484,7 +488,7 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o) {
         const int p = 2 * b + t;
         C.iso[p] = r6 * dud * (P1 * me) + r6 * du * (P2 * me);
         for (int j = 0; j < 3; ++j) {
-          const T S1 = (sw * 2.0 / (du * du) * dx[j]);
+          const T S1 = (sw * 2.0 * idu2 * dx[j]);
           const T S2 = 2 * (wxj * wd[j]) + 2 * (w[j] * wdxj);
           C.elr[p][j] = r6 * dud * (P1 * ma[j] + S1 * me) + r6 * du * (P2 * ma[j] + S2 * me);
           C.lec[p][j] = r6 * dud * (wuv[j] * me) - r6 * r[4 * b + j] + r6 * du * (-wduv[j] * me);
@@ -497,10 +501,10 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o) {
     // MDotVDot_D_Vel, subtracted (src/PhysicsCloth.cpp:2342-2577)
     for (int t = 0; t < 2; ++t) {
       const double sw = t == 0 ? -1.0 : 1.0;
-      const T wdj = sw * (1.0 / du);
+      const T wdj = sw * idu;
       const T P1 = -wdj;
       T wdv[3];
-      for (int i = 0; i < 3; ++i) wdv[i] = (t == 0 ? (1.0 / du) : (-1.0 / du)) * w[i];
+      for (int i = 0; i < 3; ++i) wdv[i] = (t == 0 ? idu : -idu) * w[i];
       const T wtwd = 2 * dot3(w, wdv);
       const T cm = (t == 0 ? -1.0 : 1.0) * (1.0 / 6.0) * rho;
       for (int b = 0; b < 2; ++b) {
@@ -593,11 +597,12 @@ YS_HD void bend_terms(const BendGeom<T>& g, const T& kb, BendTerms<T>& t) {
   T a[3], b[3];
   matvec3(g.P1, g.d2, a);
   matvec3(g.P2, g.d1, b);
-  const T c1 = (-2 * kb * th) / (g.l1 * du * s), c2 = (-2 * kb * th) / (g.l2 * du * s);
+  const T il1 = 1.0 / g.l1, il2 = 1.0 / g.l2, idu = 1.0 / du, is = 1.0 / s;  // one division each
+  const T c1 = (-2 * kb * th) * (il1 * idu * is), c2 = (-2 * kb * th) * (il2 * idu * is);
   for (int i = 0; i < 3; ++i) { t.Fx1[i] = c1 * a[i]; t.Fx2[i] = c2 * b[i]; }
-  const T k11 = (2 * kb) / ((g.l1 * g.l1) * du * s), k12 = (-2 * kb) / (g.l1 * g.l2 * du * s);
-  const T k22 = (2 * kb) / ((g.l2 * g.l2) * du * s);
-  const T cs2 = co / (s * s), is = 1 / s;
+  const T k11 = (2 * kb) * ((il1 * il1) * idu * is), k12 = (-2 * kb) * (il1 * il2 * idu * is);
+  const T k22 = (2 * kb) * ((il2 * il2) * idu * is);
+  const T cs2 = co * (is * is);
   T Tm[3][3];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
@@ -618,7 +623,7 @@ YS_HD void bend_terms(const BendGeom<T>& g, const T& kb, BendTerms<T>& t) {
   matmul3(Tm, g.P1, t.L21);
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) t.L21[i][j] *= k12;
-  const T e1 = (2 * kb * th) / (g.l1 * (du * du) * s), e2 = (2 * kb * th) / (g.l2 * (du * du) * s);
+  const T e1 = (2 * kb * th) * (il1 * (idu * idu) * is), e2 = (2 * kb * th) * (il2 * (idu * idu) * is);
   for (int i = 0; i < 3; ++i) { t.L1E1[i] = e1 * a[i]; t.L2E1[i] = e2 * b[i]; }
 }
 
@@ -667,9 +672,9 @@ YS_HD void bend_element(const View& v, double* buf, double* dbuf, int n2, int n0
       put(kB_Fx1 + i, t.Fx1[i]);
       put(kB_Fx2 + i, t.Fx2[i]);
     }
-    const T th = g.theta, du = g.du;
-    put(kB_E1E1, (-2 * kb * (th * th)) / (du * du * du));
-    put(kB_Fu2, (-kb * th) / (du * du));
+    const T th = g.theta, idu = 1.0 / g.du;
+    put(kB_E1E1, (-2 * kb * (th * th)) * (idu * idu * idu));
+    put(kB_Fu2, (-kb * th) * (idu * idu));
   }
   {
     const double R = v.cp[v.node_cloth[n0]].R;
@@ -942,7 +947,8 @@ YS_HD void shear_element(const View& v, double* buf, double* dbuf, int n0, int s
     a3v[i] = ldT<T>(v.X, v.dX, i, nt, n3) - x0;
   }
   const T l1 = norm3(a1v), l3 = norm3(a3v);
-  for (int i = 0; i < 3; ++i) { d1[i] = a1v[i] / l1; d3[i] = a3v[i] / l3; }
+  const T il1 = 1.0 / l1, il3 = 1.0 / l3;  // reciprocals, one division each
+  for (int i = 0; i < 3; ++i) { d1[i] = a1v[i] * il1; d3[i] = a3v[i] * il3; }
   proj3(d1, P1);
   proj3(d3, P3);
   const T phi = acos(dot3(d1, d3));
@@ -953,17 +959,17 @@ YS_HD void shear_element(const View& v, double* buf, double* dbuf, int n0, int s
   const uint8_t f0 = v.flags[n0], f1 = v.flags[n1], f3 = v.flags[n3];
   const bool jam = (((f0 & YS_FLIP) != 0) != ((f1 & YS_FLIP) != 0)) && (((f0 & YS_FLIP) != 0) != ((f3 & YS_FLIP) != 0));
   T Fx1[3], Fx3[3], J11[3][3], J13[3][3], J31[3][3], J33[3][3];
-  const T cs2 = co / (s * s), is = 1 / s;
+  const T is = 1.0 / s, cs2 = co * (is * is);
   if (!jam) {
     const T kx = (comp + 1.0) * S * R * R * kPi;
     const T ph = phi - kPi / 2;
     // Shear_F takes phi.item() in (phi - PI/2) (src/PhysicsCloth.cpp:2720-2721):
     // that factor carries no derivative along the reference's gradient path
     const T phf = v.trunc ? detach(phi) - kPi / 2 : ph;
-    const T cf1 = (kx * Lc * phf) / (l1 * s), cf3 = (kx * Lc * phf) / (l3 * s);
+    const T cf1 = (kx * Lc * phf) * (il1 * is), cf3 = (kx * Lc * phf) * (il3 * is);
     for (int i = 0; i < 3; ++i) { Fx1[i] = cf1 * a3[i]; Fx3[i] = cf3 * a1[i]; }
-    const T k11 = (kx * Lc) / ((l1 * l1) * s), k33 = (kx * Lc) / ((l3 * l3) * s);
-    const T k13 = (kx * Lc) / (l3 * l1 * s), k31 = (kx * Lc) / (l1 * l3 * s);
+    const T k11 = (kx * Lc) * ((il1 * il1) * is), k33 = (kx * Lc) * ((il3 * il3) * is);
+    const T k13 = (kx * Lc) * (il3 * il1 * is), k31 = (kx * Lc) * (il1 * il3 * is);
     // src/PhysicsCloth.cpp:2715-2751 per block:
     //   J11 = k11 (ph (-a3 d1^T + cs2 a3 a3^T - co P1 - d1 a3^T) - a3 a3^T / s)
     //   J13 = k13 ph (cs2 - 1/s) (a3 d1^T) P3 = k13 ph (cs2 - 1/s) a3 a1^T, as a1 = P3 d1
@@ -992,7 +998,7 @@ YS_HD void shear_element(const View& v, double* buf, double* dbuf, int n0, int s
     const double pb = kPi / 2, pl = P.jam, sig = 0.6;
     const double cc = 3.0;
     const double LR = Lc / R;
-    const T rl1s = 1.0 / (l1 * s), rl3s = 1.0 / (l3 * s);
+    const T rl1s = il1 * is, rl3s = il3 * is;
     T px1[3], px3[3];
     for (int i = 0; i < 3; ++i) { px1[i] = -a3[i] * rl1s; px3[i] = -a1[i] * rl3s; }
     const T gamma = (Lc * sqrt(2.0) - 2 * Lc * sin(0.5 * phi)) / R;
@@ -1005,7 +1011,7 @@ YS_HD void shear_element(const View& v, double* buf, double* dbuf, int n0, int s
     const double pb5 = P.pb5, pb4 = P.pb4;
     const T num = pb5 * Aq, den = phs * phs + pb4 * sig * sig;
     const T cf = tanh(num / den);
-    const T den2 = den * den, rden2 = 1.0 / den2, rden22 = 1.0 / (den2 * den2);
+    const T den2 = den * den, rden2 = 1.0 / den2, rden22 = rden2 * rden2;
     const T tau = pb5 * den - num * (2 * phs * sgm);  // con_func_x_x numerator / phi_x
     const T muc = tau * rden2;                         // con_func_x_x = muc * phi_x
     const T g3 = gamma * gamma * gamma, g2 = gamma * gamma;
@@ -1041,9 +1047,9 @@ YS_HD void shear_element(const View& v, double* buf, double* dbuf, int n0, int s
     const T cross = 2 * phs * pb5 * sgm;
     const T hLB2 = 0.5 * Lc * Bq2, LB = Lc * Bq;
     const T kL = kx * Lc;
-    const T r11 = 1.0 / ((l1 * l1) * s), r33 = 1.0 / ((l3 * l3) * s), r13 = 1.0 / (l1 * l3 * s);
-    const T qR11 = 0.5 * LR * sh / ((l1 * s) * (l1 * s)), qR33 = 0.5 * LR * sh / ((l3 * s) * (l3 * s));
-    const T qR13 = 0.5 * LR * sh / (l1 * l3 * (s * s));
+    const T r11 = (il1 * il1) * is, r33 = (il3 * il3) * is, r13 = il1 * il3 * is;
+    const T qR11 = 0.5 * LR * sh * (rl1s * rl1s), qR33 = 0.5 * LR * sh * (rl3s * rl3s);
+    const T qR13 = 0.5 * LR * sh * (il1 * il3 * (is * is));
     const T rho1 = rl1s * rl1s, rho3 = rl3s * rl3s, rho13 = rl1s * rl3s;
     // J = cP*pxx + cO*O + cOb*Ob + cR*Rg + fo (+ cOne*1 + row/column terms)
     const T hb = hLB2 * base2, g3c = 1 - g3;
