@@ -362,6 +362,7 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
   A(&v.A, (size_t)ys::YS_NUM_SLOTS * nt); A(&v.B, 5 * nt);
   A(&b->rec.edge, (size_t)ys::kEdgeFields * 2 * nt); A(&b->rec.bend, (size_t)ys::kBendFields * 2 * nt);
   A(&b->rec.face, 6 * nt); A(&b->rec.shear, (size_t)ys::kShearFields * 4 * nt);
+  A(&b->rec.nonfinite, nt);
   A(&b->so.x, 5 * nt); A(&b->so.r, 5 * nt); A(&b->so.p, 5 * nt); A(&b->so.q, 5 * nt); A(&b->so.dinv, 5 * nt);
   A(&b->so.part, 4 * blk_cloth.size()); A(&b->so.pc, n_cloths); A(&b->so.nactive, 1);
   A(&b->stage, 5 * nt); A(&b->ext, 5 * nt);

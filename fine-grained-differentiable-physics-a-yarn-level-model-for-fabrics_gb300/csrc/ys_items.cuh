@@ -4,6 +4,8 @@
 // is a plain function of (View, node).
 #pragma once
 
+#include <type_traits>
+
 #include "ys_physics.cuh"
 
 namespace ys {
@@ -22,6 +24,9 @@ struct Records {
   double* dbend;
   double* dface;
   double* dshear;
+  // per node: 1 if a coefficient or right-hand side the gather wrote is not
+  // finite (null: the finalize checks every slot itself)
+  uint8_t* nonfinite;
 };
 
 YS_HD double rec(const double* buf, int field, int nslot, int slot_, int ntot, int node) {
@@ -46,6 +51,11 @@ YS_HD T ldA(const View& v, int s, int n) { return ldT<T>(v.A, v.dA, s, v.ntot, n
 // (src/MatrixMp.cpp:54-65), hence the blk[3 * c + r] reads.
 template <class T>
 YS_HD void gather_elements(const View& v, const Records& R, int n) {
+  bool fin = true;  // every value written below is finite
+  auto putA = [&](int s_, int n_, const T& x) {
+    fin = fin && isfinite(val(x));
+    stA(v, s_, n_, x);
+  };
   const int nt = v.ntot;
   const ClothParams& P = v.cp[v.node_cloth[n]];
   const int W = P.W, H = P.H, u = v.node_u[n], w = v.node_v[n];
@@ -177,13 +187,16 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
         B[3 + k] += bE[k];
       }
     }
-    for (int i = 0; i < 9; ++i) stA(v, YS_SLOT_LL + i, n, LL[i]);
+    for (int i = 0; i < 9; ++i) putA(YS_SLOT_LL + i, n, LL[i]);
     for (int i = 0; i < 6; ++i) {
-      stA(v, YS_SLOT_LE_SELF + i, n, LE[i]);
-      stA(v, YS_SLOT_EL_SELF + i, n, EL[i]);
+      putA(YS_SLOT_LE_SELF + i, n, LE[i]);
+      putA(YS_SLOT_EL_SELF + i, n, EL[i]);
     }
-    for (int k = 0; k < 2; ++k) stA(v, YS_SLOT_EE_SELF + k, n, EE[k]);
-    for (int i = 0; i < 5; ++i) stT(v.B, v.dB, i, nt, n, B[i]);
+    for (int k = 0; k < 2; ++k) putA(YS_SLOT_EE_SELF + k, n, EE[k]);
+    for (int i = 0; i < 5; ++i) {
+      fin = fin && isfinite(val(B[i]));
+      stT(v.B, v.dB, i, nt, n, B[i]);
+    }
   }
   // ------------------------------------------------ yarn neighbours (+-1)
   for (int m = 0; m < 4; ++m) {
@@ -242,12 +255,12 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
           for (int r = 0; r < 3; ++r) EL[r] += mh2 * (-q[r]);
       }
     }
-    for (int i = 0; i < 9; ++i) stA(v, YS_SLOT_LL + 9 * s + i, n, LL[i]);
+    for (int i = 0; i < 9; ++i) putA(YS_SLOT_LL + 9 * s + i, n, LL[i]);
     for (int r = 0; r < 3; ++r) {
-      stA(v, YS_SLOT_LE_NBR + 3 * m + r, n, LE[r]);
-      stA(v, YS_SLOT_EL_NBR + 3 * m + r, n, EL[r]);
+      putA(YS_SLOT_LE_NBR + 3 * m + r, n, LE[r]);
+      putA(YS_SLOT_EL_NBR + 3 * m + r, n, EL[r]);
     }
-    stA(v, YS_SLOT_EE_NBR + m, n, EE);
+    putA(YS_SLOT_EE_NBR + m, n, EE);
   }
   // ------------------------------------------- second neighbours (+-2)
   for (int m = 0; m < 4; ++m) {
@@ -261,12 +274,13 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
     const int anc = n + dir * step;
     for (int r = 0; r < 3; ++r)
       for (int c = 0; c < 3; ++c)  // n is n2 (dir +1): L21; n is n1 (dir -1): L12
-        stA(v, YS_SLOT_LL + 9 * s + 3 * r + c, n,
+        putA(YS_SLOT_LL + 9 * s + 3 * r + c, n,
             ok ? T(mh2 * recT<T>(R.bend, R.dbend, (dir > 0 ? kB_L21 : kB_L12) + 3 * c + r, 2, k, nt, anc)) : T(0.0));
   }
   // diagonal neighbours: shear only (gather_shear_finalize)
   for (int s = 9; s < 13; ++s)
-    for (int i = 0; i < 9; ++i) stA(v, YS_SLOT_LL + 9 * s + i, n, T(0.0));
+    for (int i = 0; i < 9; ++i) putA(YS_SLOT_LL + 9 * s + i, n, T(0.0));
+  if (R.nonfinite) R.nonfinite[n] = fin ? 0 : 1;
 }
 
 // Adds the shear segments touching row block n (as crossing n0, as warp
@@ -286,6 +300,7 @@ YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double*
   const double h = v.h, mh2 = -(v.h * v.h);
   auto interior = [&](int uu, int vv) { return uu >= 1 && uu <= W - 2 && vv >= 1 && vv <= H - 2; };
   auto S = [&](int f, int seg, int anc) { return recT<T>(R.shear, R.dshear, f, 4, seg, nt, anc); };
+  bool finf = true;  // every slot value this routine writes is finite
   auto addLL = [&](int du, int dv, const T* blk) {  // A[x(n)][x(n + (du, dv))] += -h^2 blk^T
     const int s = stencil_index(du, dv);
     if (s < 0) return;
@@ -294,6 +309,7 @@ YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double*
         const int sl = YS_SLOT_LL + 9 * s + 3 * r + c;
         T a = ldA<T>(v, sl, n);
         a += mh2 * blk[3 * c + r];
+        finf = finf && isfinite(val(a));
         stA(v, sl, n, a);
       }
   };
@@ -303,48 +319,125 @@ YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double*
     stT(v.B, v.dB, c, nt, n, b);
   };
   T Bx[3] = {0.0, 0.0, 0.0};
-  T J[9];
-  // as the crossing n0 (src/PhysicsCloth.cpp:3033-3047)
-  if (fl & YS_INTERIOR) {
-    for (int seg = 0; seg < 4; ++seg) {
-      for (int i = 0; i < 9; ++i) {
-        const T J10 = -(S(kS_J11 + i, seg, n) + S(kS_J13 + i, seg, n));
-        const T J30 = -(S(kS_J31 + i, seg, n) + S(kS_J33 + i, seg, n));
-        J[i] = -(J10 + J30);
+  if constexpr (std::is_same<T, double>::value) {
+    // The contributions below are summed per target block in registers and
+    // each slot of A is then updated once (a global read-modify-write per
+    // contribution would serialise on its own stores). Same terms as the
+    // tangent path in the else branch, summed in another order.
+    const bool in0 = (fl & YS_INTERIOR) != 0;
+    {  // the node's own block and its four yarn neighbours
+      double self[9], xa[2][9], ya[2][9];  // xa: (-1, 0), (1, 0); ya: (0, -1), (0, 1)
+#pragma unroll
+      for (int i = 0; i < 9; ++i) self[i] = xa[0][i] = xa[1][i] = ya[0][i] = ya[1][i] = 0.0;
+#pragma unroll
+      for (int seg = 0; seg < 4; ++seg) {
+        const int du = shear_du(seg), dv = shear_dv(seg);
+        const int ix = du < 0 ? 0 : 1, iy = dv < 0 ? 0 : 1;
+        if (in0) {  // as the crossing n0 (src/PhysicsCloth.cpp:3033-3047)
+#pragma unroll
+          for (int i = 0; i < 9; ++i) {
+            const double a11 = S(kS_J11 + i, seg, n), a13 = S(kS_J13 + i, seg, n);
+            const double a31 = S(kS_J31 + i, seg, n), a33 = S(kS_J33 + i, seg, n);
+            self[i] += -(-(a11 + a13) + -(a31 + a33));  // -(J10 + J30)
+            xa[ix][i] += -(a11 + a31);                   // J01, towards n1 = n + (du, 0)
+            ya[iy][i] += -(a13 + a33);                   // J03, towards n3 = n + (0, dv)
+          }
+          for (int r = 0; r < 3; ++r) Bx[r] += h * (-1 * (S(kS_F1 + r, seg, n) + S(kS_F3 + r, seg, n)));
+        }
+        if (interior(u - du, w)) {  // as the warp neighbour n1 of the crossing n - (du, 0)
+          const int anc = n - du;
+#pragma unroll
+          for (int i = 0; i < 9; ++i) {
+            const double b11 = S(kS_J11 + i, seg, anc), b13 = S(kS_J13 + i, seg, anc);
+            self[i] += b11;
+            xa[1 - ix][i] += -(b11 + b13);  // J10, towards n0 = n + (-du, 0)
+          }
+          for (int r = 0; r < 3; ++r) Bx[r] += h * S(kS_F1 + r, seg, anc);
+        }
+        if (interior(u, w - dv)) {  // as the weft neighbour n3 of the crossing n - (0, dv)
+          const int anc = n - dv * W;
+#pragma unroll
+          for (int i = 0; i < 9; ++i) {
+            const double c31 = S(kS_J31 + i, seg, anc), c33 = S(kS_J33 + i, seg, anc);
+            self[i] += c33;
+            ya[1 - iy][i] += -(c31 + c33);  // J30, towards n0 = n + (0, -dv)
+          }
+          for (int r = 0; r < 3; ++r) Bx[r] += h * S(kS_F3 + r, seg, anc);
+        }
       }
-      addLL(0, 0, J);
-      for (int i = 0; i < 9; ++i) J[i] = -(S(kS_J11 + i, seg, n) + S(kS_J31 + i, seg, n));  // J01
-      addLL(shear_du(seg), 0, J);
-      for (int i = 0; i < 9; ++i) J[i] = -(S(kS_J13 + i, seg, n) + S(kS_J33 + i, seg, n));  // J03
-      addLL(0, shear_dv(seg), J);
-      for (int r = 0; r < 3; ++r) Bx[r] += h * (-1 * (S(kS_F1 + r, seg, n) + S(kS_F3 + r, seg, n)));
+      addLL(0, 0, self);
+      addLL(-1, 0, xa[0]);
+      addLL(1, 0, xa[1]);
+      addLL(0, -1, ya[0]);
+      addLL(0, 1, ya[1]);
     }
-  }
-  // as the warp neighbour n1 = n0 + (du, 0)
-  for (int seg = 0; seg < 4; ++seg) {
-    const int du = shear_du(seg), dv = shear_dv(seg);
-    if (!interior(u - du, w)) continue;
-    const int anc = n - du;
-    for (int i = 0; i < 9; ++i) J[i] = S(kS_J11 + i, seg, anc);
-    addLL(0, 0, J);
-    for (int i = 0; i < 9; ++i) J[i] = -(S(kS_J11 + i, seg, anc) + S(kS_J13 + i, seg, anc));  // J10
-    addLL(-du, 0, J);
-    for (int i = 0; i < 9; ++i) J[i] = S(kS_J13 + i, seg, anc);  // towards n3 = n + (-du, dv)
-    addLL(-du, dv, J);
-    for (int r = 0; r < 3; ++r) Bx[r] += h * S(kS_F1 + r, seg, anc);
-  }
-  // as the weft neighbour n3 = n0 + (0, dv)
-  for (int seg = 0; seg < 4; ++seg) {
-    const int du = shear_du(seg), dv = shear_dv(seg);
-    if (!interior(u, w - dv)) continue;
-    const int anc = n - dv * W;
-    for (int i = 0; i < 9; ++i) J[i] = S(kS_J33 + i, seg, anc);
-    addLL(0, 0, J);
-    for (int i = 0; i < 9; ++i) J[i] = -(S(kS_J31 + i, seg, anc) + S(kS_J33 + i, seg, anc));  // J30
-    addLL(0, -dv, J);
-    for (int i = 0; i < 9; ++i) J[i] = S(kS_J31 + i, seg, anc);  // towards n1 = n + (du, -dv)
-    addLL(du, -dv, J);
-    for (int r = 0; r < 3; ++r) Bx[r] += h * S(kS_F3 + r, seg, anc);
+    {  // the diagonal neighbours: J13 of a warp-neighbour role, J31 of a weft-neighbour role
+      double dg[4][9];  // (-1, -1), (1, -1), (-1, 1), (1, 1)
+#pragma unroll
+      for (int i = 0; i < 9; ++i) dg[0][i] = dg[1][i] = dg[2][i] = dg[3][i] = 0.0;
+#pragma unroll
+      for (int seg = 0; seg < 4; ++seg) {
+        const int du = shear_du(seg), dv = shear_dv(seg);
+        if (interior(u - du, w)) {  // towards n3 = n + (-du, dv)
+          const int t = (-du < 0 ? 0 : 1) + (dv < 0 ? 0 : 2);
+#pragma unroll
+          for (int i = 0; i < 9; ++i) dg[t][i] += S(kS_J13 + i, seg, n - du);
+        }
+        if (interior(u, w - dv)) {  // towards n1 = n + (du, -dv)
+          const int t = (du < 0 ? 0 : 1) + (-dv < 0 ? 0 : 2);
+#pragma unroll
+          for (int i = 0; i < 9; ++i) dg[t][i] += S(kS_J31 + i, seg, n - dv * W);
+        }
+      }
+      addLL(-1, -1, dg[0]);
+      addLL(1, -1, dg[1]);
+      addLL(-1, 1, dg[2]);
+      addLL(1, 1, dg[3]);
+    }
+  } else {
+    T J[9];
+    // as the crossing n0 (src/PhysicsCloth.cpp:3033-3047)
+    if (fl & YS_INTERIOR) {
+      for (int seg = 0; seg < 4; ++seg) {
+        for (int i = 0; i < 9; ++i) {
+          const T J10 = -(S(kS_J11 + i, seg, n) + S(kS_J13 + i, seg, n));
+          const T J30 = -(S(kS_J31 + i, seg, n) + S(kS_J33 + i, seg, n));
+          J[i] = -(J10 + J30);
+        }
+        addLL(0, 0, J);
+        for (int i = 0; i < 9; ++i) J[i] = -(S(kS_J11 + i, seg, n) + S(kS_J31 + i, seg, n));  // J01
+        addLL(shear_du(seg), 0, J);
+        for (int i = 0; i < 9; ++i) J[i] = -(S(kS_J13 + i, seg, n) + S(kS_J33 + i, seg, n));  // J03
+        addLL(0, shear_dv(seg), J);
+        for (int r = 0; r < 3; ++r) Bx[r] += h * (-1 * (S(kS_F1 + r, seg, n) + S(kS_F3 + r, seg, n)));
+      }
+    }
+    // as the warp neighbour n1 = n0 + (du, 0)
+    for (int seg = 0; seg < 4; ++seg) {
+      const int du = shear_du(seg), dv = shear_dv(seg);
+      if (!interior(u - du, w)) continue;
+      const int anc = n - du;
+      for (int i = 0; i < 9; ++i) J[i] = S(kS_J11 + i, seg, anc);
+      addLL(0, 0, J);
+      for (int i = 0; i < 9; ++i) J[i] = -(S(kS_J11 + i, seg, anc) + S(kS_J13 + i, seg, anc));  // J10
+      addLL(-du, 0, J);
+      for (int i = 0; i < 9; ++i) J[i] = S(kS_J13 + i, seg, anc);  // towards n3 = n + (-du, dv)
+      addLL(-du, dv, J);
+      for (int r = 0; r < 3; ++r) Bx[r] += h * S(kS_F1 + r, seg, anc);
+    }
+    // as the weft neighbour n3 = n0 + (0, dv)
+    for (int seg = 0; seg < 4; ++seg) {
+      const int du = shear_du(seg), dv = shear_dv(seg);
+      if (!interior(u, w - dv)) continue;
+      const int anc = n - dv * W;
+      for (int i = 0; i < 9; ++i) J[i] = S(kS_J33 + i, seg, anc);
+      addLL(0, 0, J);
+      for (int i = 0; i < 9; ++i) J[i] = -(S(kS_J31 + i, seg, anc) + S(kS_J33 + i, seg, anc));  // J30
+      addLL(0, -dv, J);
+      for (int i = 0; i < 9; ++i) J[i] = S(kS_J31 + i, seg, anc);  // towards n1 = n + (du, -dv)
+      addLL(du, -dv, J);
+      for (int r = 0; r < 3; ++r) Bx[r] += h * S(kS_F3 + r, seg, anc);
+    }
   }
   for (int r = 0; r < 3; ++r) addB(r, Bx[r]);
   // handles, external force, boundary identity rows
@@ -354,6 +447,7 @@ YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double*
       const int sl = YS_SLOT_LL + i * 3 + i;
       T a = ldA<T>(v, sl, n);
       a += -(h * h) * (-P.kh);
+      finf = finf && isfinite(val(a));
       stA(v, sl, n, a);
     }
   }
@@ -369,7 +463,13 @@ YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double*
     }
   }
   bool ok = true;
-  for (int s = 0; s < YS_NUM_SLOTS; ++s) ok = ok && isfinite(slot(v, s, n));
+  if (R.nonfinite) {
+    // the gather checked what it wrote; the slots changed here were checked
+    // as they were written
+    ok = finf && !R.nonfinite[n];
+  } else {
+    for (int s = 0; s < YS_NUM_SLOTS; ++s) ok = ok && isfinite(slot(v, s, n));
+  }
   for (int c = 0; c < 5; ++c) ok = ok && isfinite(ld(v.B, c, nt, n));
   if (dinv) {
     for (int i = 0; i < 3; ++i) {
