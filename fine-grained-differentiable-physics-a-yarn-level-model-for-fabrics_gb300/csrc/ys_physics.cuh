@@ -801,6 +801,53 @@ YS_HD void sym3_min_eigvec(const double S[3][3], double* out) {
   for (int k = 0; k < 3; ++k) out[k] = V[k][m];
 }
 
+// Eigenvector of the smallest eigenvalue of a symmetric 3x3 S by Rayleigh-
+// quotient iteration from a guess close to it: x <- adj(S - mu I) x / |.|,
+// mu = x^T S x (the adjugate solves the shifted system up to scale without a
+// division and stays exact when mu hits the eigenvalue). Converges cubically;
+// returns false (out untouched) unless the result is an eigenvector of the
+// smallest eigenvalue to 1e-12 relative, for the caller to fall back on the
+// Jacobi solver.
+YS_HD bool sym3_min_eigvec_rqi(const double S[3][3], const double* guess, double* out) {
+  double x[3] = {guess[0], guess[1], guess[2]};
+  double nx = norm3(x);
+  if (!(nx > 0.0)) return false;
+  for (int i = 0; i < 3; ++i) x[i] /= nx;
+  double mu = 0.0;
+  for (int it = 0; it < 4; ++it) {
+    double Sx[3];
+    for (int i = 0; i < 3; ++i) Sx[i] = S[i][0] * x[0] + S[i][1] * x[1] + S[i][2] * x[2];
+    mu = dot3(x, Sx);
+    const double m00 = S[0][0] - mu, m11 = S[1][1] - mu, m22 = S[2][2] - mu;
+    const double m01 = S[0][1], m02 = S[0][2], m12 = S[1][2];
+    // adjugate of the symmetric M = S - mu I
+    const double c00 = m11 * m22 - m12 * m12, c01 = m02 * m12 - m01 * m22, c02 = m01 * m12 - m02 * m11;
+    const double c11 = m00 * m22 - m02 * m02, c12 = m01 * m02 - m00 * m12, c22 = m00 * m11 - m01 * m01;
+    double y[3] = {c00 * x[0] + c01 * x[1] + c02 * x[2], c01 * x[0] + c11 * x[1] + c12 * x[2],
+                   c02 * x[0] + c12 * x[1] + c22 * x[2]};
+    const double ny = norm3(y);
+    if (!(ny > 0.0) || !isfinite(ny)) break;  // x is already exact
+    const double iy = 1.0 / ny;
+    for (int i = 0; i < 3; ++i) x[i] = y[i] * iy;
+  }
+  double Sx[3];
+  for (int i = 0; i < 3; ++i) Sx[i] = S[i][0] * x[0] + S[i][1] * x[1] + S[i][2] * x[2];
+  mu = dot3(x, Sx);
+  const double sc = fabs(S[0][0]) + fabs(S[1][1]) + fabs(S[2][2]) + 1e-300;
+  double r2 = 0.0;
+  for (int i = 0; i < 3; ++i) r2 += (Sx[i] - mu * x[i]) * (Sx[i] - mu * x[i]);
+  if (!(r2 <= 1e-24 * sc * sc)) return false;
+  // mu is the smallest eigenvalue iff the other two, l2 + l3 = tr - mu and
+  // l2 l3 = e2 - mu (tr - mu), are both >= mu
+  const double tr = S[0][0] + S[1][1] + S[2][2];
+  const double e2 = S[0][0] * S[1][1] + S[0][0] * S[2][2] + S[1][1] * S[2][2] - S[0][1] * S[0][1] -
+                    S[0][2] * S[0][2] - S[1][2] * S[1][2];
+  const double sum = tr - mu, prod = e2 - mu * sum;
+  if (!(sum >= 2.0 * mu && prod - mu * sum + mu * mu >= -1e-12 * sc * sc)) return false;
+  for (int i = 0; i < 3; ++i) out[i] = x[i];
+  return true;
+}
+
 YS_HD void node_normal(const View& v, int n, int W) {
   const int nt = v.ntot;
   const int ids[5] = {n, n - 1, n + 1, n - W, n + W};
@@ -813,13 +860,16 @@ YS_HD void node_normal(const View& v, int n, int W) {
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) S[i][j] += r[i] * r[j];
   }
-  double nn[3];
-  sym3_min_eigvec(S, nn);
-  const double len = norm3(nn);
-  for (int i = 0; i < 3; ++i) nn[i] /= len;
   double vw[3], vf[3], cr[3];
   for (int i = 0; i < 3; ++i) { vw[i] = p[2][i] - p[1][i]; vf[i] = p[4][i] - p[3][i]; }
   cross3(vw, vf, cr);
+  // the smallest right singular vector of the centred positions (the
+  // reference's torch::svd, src/Cloth.cpp:440-463) is the smallest
+  // eigenvector of their scatter S; warp x weft is a close starting guess
+  double nn[3];
+  if (!sym3_min_eigvec_rqi(S, cr, nn)) sym3_min_eigvec(S, nn);
+  const double len = norm3(nn);
+  for (int i = 0; i < 3; ++i) nn[i] /= len;
   if (dot3(cr, nn) / (norm3(cr) * norm3(nn)) < 0)
     for (int i = 0; i < 3; ++i) nn[i] = -nn[i];
   if (v.flags[n] & YS_FLIP)
