@@ -59,6 +59,23 @@ def workload(seed: int, n_cloths: int = N_CLOTHS):
     return specs, np.array(wind)
 
 
+def rank_seed(seed: int, rank: int) -> int:
+    """Each rank steps its own independent batch: the data path shards by
+    cloth with no exchange (weak scaling)."""
+    return seed + 1000 * rank
+
+
+def max_over_ranks(value: float, dist, device: str) -> float:
+    """The job's time is its slowest rank's (the only collective besides the
+    barriers)."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def wind_at(wind, step):
     """[n, 3] wind velocity at time step*h: along +y (normal to the hanging cloth)."""
     t = step * H
@@ -266,7 +283,7 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    seed = args.seed + 1000 * rank  # each rank steps its own batch (weak scaling)
+    seed = rank_seed(args.seed, rank)  # each rank steps its own batch (weak scaling)
     specs, wind = workload(seed, args.cloths)
     total_nodes = sum(s["width"] * s["length"] for s in specs)
     config = {"workload": "batched hanging plain-weave cloths, sides U{5..50}, seeded material and wind",
@@ -348,9 +365,7 @@ def main():
     launches = batch.profile_read(reset=True)["total_launches"]
     ok = all(s["ok"] for s in st)
     if dist is not None:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dist, "cuda")
     ms_per_step = ms / args.steps
     value = world * args.steps / (ms / 1e3)
 
@@ -371,9 +386,7 @@ def main():
     barrier()
     e2e_s = time.perf_counter() - t0
     if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, dist, "cuda")
     state_bytes = total_nodes * 15 * 8
     e2e = {"value": world * e2e_steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": state_bytes + 24 * args.cloths,
            "d2h_bytes_per_step": state_bytes}
