@@ -14,11 +14,13 @@ from .collide import Collider, cloth_mesh_topology
 from .learn import (PARAM_NAMES, YarnSimNetHeter, constraint_para, invert_constraint_para, position_loss, rollout,
                     rollout_with_jacobian, two_yarn_spec)
 from .precond import LearnedPreconditioner, train as train_preconditioner, training_specs
+from .render import RenderCloth, RenderType, obj_text, render_batch_cloth
 
 __all__ = [
     "build", "LIB_PATH", "PI", "ClothBatch", "ClothSpec", "ClothState", "Cloth", "EigenSolver", "Environment",
     "InitPose", "PhysicsCloth", "SimStep", "Wind", "WovenPattern", "Yarn", "YarnSimError", "load_library",
     "library_path", "PARAM_NAMES", "YarnSimNetHeter", "constraint_para", "invert_constraint_para", "position_loss",
     "rollout", "rollout_with_jacobian", "two_yarn_spec", "Collider", "cloth_mesh_topology",
-    "LearnedPreconditioner", "train_preconditioner", "training_specs",
+    "LearnedPreconditioner", "train_preconditioner", "training_specs", "RenderCloth", "RenderType", "obj_text",
+    "render_batch_cloth",
 ]

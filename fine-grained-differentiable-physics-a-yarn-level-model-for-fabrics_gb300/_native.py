@@ -26,7 +26,7 @@ EXPORTED = [
     "ys_collider_get_pairs", "ys_collider_find_impacts", "ys_collider_get_impacts", "ys_use_graphs",
     "ys_step_graphed", "ys_autotune", "ys_gnn_param_count", "ys_gnn_create", "ys_gnn_destroy", "ys_gnn_get_params",
     "ys_gnn_set_params", "ys_gnn_train_step", "ys_gnn_loss_grad", "ys_set_preconditioner", "ys_precond_info",
-    "ys_get_system_slots", "ys_tc_gemm_bf16", "ys_precond_refresh",
+    "ys_get_system_slots", "ys_tc_gemm_bf16", "ys_precond_refresh", "ys_get_normals",
 ]
 YS_PREC_JACOBI, YS_PREC_LEARNED = 0, 1
 YS_TANGENT_EXACT, YS_TANGENT_REFERENCE = 0, 1
@@ -145,6 +145,7 @@ def load(build_if_missing: bool = True):
     L.ys_gnn_loss_grad.argtypes = [vp, vp, vp, ctypes.c_uint64, _dp, vp, vp, vp]
     L.ys_set_preconditioner.argtypes = [vp, ctypes.c_int32, vp]
     L.ys_precond_refresh.argtypes = [vp, ctypes.c_int32]
+    L.ys_get_normals.argtypes = [vp, vp, ctypes.c_int32]
     L.ys_precond_info.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     L.ys_get_system_slots.argtypes = [vp, vp, vp]
     L.ys_tc_gemm_bf16.argtypes = [ctypes.c_int32, vp, vp, vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]

@@ -261,6 +261,12 @@ class ClothBatch:
         """Run step() as one CUDA graph launch per step (see ys_use_graphs)."""
         N.check(N.load().ys_use_graphs(self._h, int(bool(enable))), "ys_use_graphs")
 
+    def normals(self) -> np.ndarray:
+        """Node normals [total_nodes, 3] of the current positions (zero on boundary nodes)."""
+        out = np.zeros((self.total_nodes, 3))
+        N.check(N.load().ys_get_normals(self._h, ctypes.c_void_p(out.ctypes.data), 0), "ys_get_normals")
+        return out
+
     def set_preconditioner(self, kind: str = "jacobi", net=None):
         """'jacobi' (Eigen's default, src/Solvers.cpp:22-24) or 'learned' with a
         precond.LearnedPreconditioner, which the batch borrows."""

@@ -480,6 +480,20 @@ ys_status ys_get_state(ys_batch* b, double* lpos, double* lposfix, double* lvel,
   return YS_OK;
 }
 
+ys_status ys_get_normals(ys_batch* b, double* normals, int32_t flags) {
+  if (!b || !normals) return fail(YS_ERR_ARG, "bad argument");
+  YS_CUDA(cudaSetDevice(b->device));
+  // NodeNorm of the current positions (src/Cloth.cpp:440-463), as
+  // Cloth::UpdateClothUnits leaves them after every update; the step itself
+  // recomputes them when it assembles
+  if (b->geom_n) {
+    b->launches += 1;
+    ys::launch_geom(b->v, b->anchors + b->geom_off, b->geom_n, b->stream);
+    YS_CUDA(cudaGetLastError());
+  }
+  return download_aos(b, b->v.NRM, normals, 3, flags);
+}
+
 ys_status ys_set_wind(ys_batch* b, int32_t cloth, const double wind_vel[3]) {
   if (!b || !wind_vel || cloth < -1 || cloth >= b->ncloth) return fail(YS_ERR_ARG, "bad argument");
   YS_CUDA(cudaSetDevice(b->device));

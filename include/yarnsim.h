@@ -113,6 +113,10 @@ ys_status ys_set_state(ys_batch *b, const double *lpos, const double *lposfix, c
                        const double *epos, const double *eposbar, const double *evel, int32_t flags);
 ys_status ys_get_state(ys_batch *b, double *lpos, double *lposfix, double *lvel, double *epos, double *eposbar,
                        double *evel, int32_t flags);
+/* Node normals [total_nodes][3] of the current positions: NodeNorm
+ * (src/Cloth.cpp:440-463) of every interior node, as Cloth::UpdateClothUnits
+ * leaves them (src/Cloth.cpp:307-348); zero for boundary nodes. */
+ys_status ys_get_normals(ys_batch *b, double *normals, int32_t flags);
 ys_status ys_set_wind(ys_batch *b, int32_t cloth, const double wind_vel[3]);
 /* Wind velocity of every cloth at once: [n_cloths][3] (one copy). */
 ys_status ys_set_winds(ys_batch *b, const double *wind_vel, int32_t flags);

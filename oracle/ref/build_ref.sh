@@ -23,7 +23,8 @@ FLAGS=(-std=c++17 -O2 -fPIC -w -D_GLIBCXX_USE_CXX11_ABI=1
        -I "$HERE/shim" -I "$REF_SRC"
        -isystem "$TORCH_DIR/include" -isystem "$TORCH_DIR/include/torch/csrc/api/include")
 SRCS=("$REF_SRC/Cloth.cpp" "$REF_SRC/PhysicsCloth.cpp" "$REF_SRC/MatrixMp.cpp" "$REF_SRC/Mesh.cpp"
-      "$REF_SRC/Geometry.cpp" "$REF_SRC/BVH.cpp" "$REF_SRC/CollisionUtil.cpp" "$HERE/shim/eigen_cg.cpp"
+      "$REF_SRC/Geometry.cpp" "$REF_SRC/BVH.cpp" "$REF_SRC/CollisionUtil.cpp" "$REF_SRC/Render.cpp"
+      "$HERE/shim/eigen_cg.cpp"
       "$HERE/ref_harness.cpp")
 pids=()
 for s in "${SRCS[@]}"; do

@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "PhysicsCloth.h"
+#include "Render.h"
 #include "CollisionUtil.h"
 
 void ref_cg_set_options(double tol, long max_iter);
@@ -791,5 +792,13 @@ int main(int argc, char** argv) {
   }
   double st = status;
   w.put("status", {1}, &st);
+  // render=PREFIX: the reference's own OBJ writer (src/Render.cpp) on the
+  // final state, in its three forms
+  if (kv.count("render")) {
+    const std::string pre = kv["render"];
+    RenderCloth(cloth, pre + "_tri.obj", RenderType::MeshTriangle);
+    RenderCloth(cloth, pre + "_rect.obj", RenderType::MeshRectangle);
+    RenderCloth(cloth, pre + "_yarn.obj", RenderType::YarnSpline);
+  }
   return 0;
 }

@@ -127,6 +127,8 @@ def run_case(cs, tmp):
             ext[3 * n + 1] = 0.002
             ext[3 * n + 2] = 0.002
         cfg["ext_force"] = ",".join(repr(float(x)) for x in ext)
+    if cs.get("render"):
+        cfg["render"] = os.path.join(tmp, cs["name"])
     cpath = os.path.join(tmp, cs["name"] + ".cfg")
     with open(cpath, "w") as f:
         for k, v in cfg.items():
@@ -149,6 +151,10 @@ def run_case(cs, tmp):
         out["ext_force"] = ext
     for k, v in rec.items():
         out[k.replace(".", "_")] = v
+    if cs.get("render"):
+        for kind in ("tri", "rect", "yarn"):
+            with open(os.path.join(tmp, "%s_%s.obj" % (cs["name"], kind))) as f:
+                out["obj_" + kind] = np.array(f.read())
     np.savez_compressed(os.path.join(HERE, cs["name"] + ".npz"), **out)
     return rec
 
