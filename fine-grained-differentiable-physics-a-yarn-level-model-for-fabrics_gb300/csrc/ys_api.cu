@@ -1415,9 +1415,11 @@ ys_status solve_learned(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* 
   YS_CUDA(cudaMemcpyAsync(pc.data(), b->so.pc, sizeof(ys::PcgCloth) * b->ncloth, cudaMemcpyDeviceToHost, s));
   YS_CUDA(cudaStreamSynchronize(s));
   L.solves += 1;
+  // fall back on an expired tensor-core wait, a breakdown (bit 3), or the
+  // default iteration cap (a cap the caller set is honoured as Jacobi-PCG's)
   bool redo = err != 0;
   for (int c = 0; c < b->ncloth; ++c)
-    if (!(pc[c].status & 1) && (pc[c].status & 4)) redo = true;
+    if (!(pc[c].status & 1) && ((pc[c].status & 8) || ((pc[c].status & 4) && override_max < 0))) redo = true;
   if (redo) {
     // Jacobi-PCG for the whole batch (a cloth that converged keeps an equally
     // valid solution, but one solve keeps the batch's bookkeeping uniform)
@@ -1428,11 +1430,12 @@ ys_status solve_learned(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* 
   ys_status ret = YS_OK;
   for (int c = 0; c < b->ncloth; ++c) {
     if (pc[c].status & 1) ret = YS_ERR_NONFINITE;
+    else if ((pc[c].status & 4) && ret == YS_OK) ret = YS_ERR_MAXITER;
     if (stats) {
       stats[c].ok = (pc[c].status & 3) == 0;
       stats[c].cg_iterations = pc[c].iters;
       stats[c].cg_error = pc[c].bb > 0 ? std::sqrt(pc[c].rr / pc[c].bb) : 0.0;
-      stats[c].hit_maxiter = 0;
+      stats[c].hit_maxiter = (pc[c].status & 4) ? 1 : 0;
     }
   }
   return ret;

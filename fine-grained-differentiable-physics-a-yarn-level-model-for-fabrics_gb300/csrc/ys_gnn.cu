@@ -206,8 +206,9 @@ __global__ void k_gnn_feat(View v, GnnBufs g) {
   const ClothParams& P = v.cp[v.node_cloth[n]];
   const int u = v.node_u[n], w = v.node_v[n];
   if (q < 6) {
-    const int b = q + 1;
-    const int j = g.pat[8 * n + b];
+    const int b = q + 1;  // lower offset (gpat_du, gpat_dv)(b), whether or not G uses it
+    const int ub = u + gpat_du(b), vb = w + gpat_dv(b);
+    const int j = (ub >= 0 && ub < P.W && vb >= 0 && vb < P.H) ? n + gpat_du(b) + gpat_dv(b) * P.W : -1;
     if (j >= 0) {
       load_linv(g.linv, nt, n, Li);
       pat_block(v, n, b, Bk);
@@ -416,7 +417,7 @@ enum { kEpiEnc = 0, kEpiLayer = 1, kEpiHead = 2 };
 template <int NT_, int EPI>
 struct FwdOp {
   static constexpr int NT = NT_;
-  static constexpr bool kColMajor = EPI == kEpiHead;  // o is stored [192][ntot]
+  static constexpr bool kColMajor = EPI == kEpiHead;  // o is stored [kGOut][ntot]
   const bf16* X;
   int ld, M;
   const int* nbr;
@@ -812,9 +813,9 @@ __global__ void __launch_bounds__(kBlock) k_lp_dir(View v, Blocks b, Solver so, 
       pc.iters = conv ? it : it + 1;
       if (conv || cap) pc.active = 0;
       if (cap) pc.status |= 4;
-      if (!isfinite(rzn) || !isfinite(beta_sh)) {
+      if (!isfinite(rzn) || !isfinite(beta_sh)) {  // breakdown: bit 3
         pc.active = 0;
-        pc.status |= 4;
+        pc.status |= 8;
       }
     }
   }

@@ -6,18 +6,19 @@
 //   M^-1 = G^T G,  G block lower triangular in node order,
 //   G_i,b = N_i,b L_src(b)^-1 (b > 0),  G_i,0 = (I + N_i,0) L_i^-1,
 //
-// over the 7-block lower pattern b = self, left, down, left-down, right-down,
-// left-2, down-2 (each node's predecessors in the node order u + v W), where
+// over the lower pattern b = self, left, down (the node's predecessors along
+// its two yarns in the node order u + v W), where
 // L_i L_i^T is the Cholesky factorisation of the symmetric part of node i's
 // 5 x 5 diagonal block. M^-1 is symmetric positive definite whenever every
 // I + N_i,0 is non-singular, so the conjugate-gradient recurrences stay valid.
 //
 // Network (BF16 operands, FP32 accumulation on the tensor cores):
 //   f_i   = 128 features of node i (its scaled couplings E_i,b = L_i^-1 A_i,src L_src^-T
-//           over the lower pattern, norms of its other couplings, flags)
+//           to the left, down, left-down, right-down, left-2 and down-2 nodes,
+//           norms of its upper couplings, flags)
 //   h1    = relu(W0 f + b0)                                   (64)
 //   h_l+1 = h_l + relu(W_l [h_i, h_left, h_right, h_down, h_up] + b_l)   l = 1..3
-//   o     = Wh h4 + bh                                        (192, 175 used)
+//   o     = Wh h4 + bh                                        (128, 75 used)
 //   N_i,0 = 0.1 o[0:25],   N_i,b = -E_i,b + 0.1 o[25 b : 25 b + 25]
 // The untrained network (head weights zero) is the first-order factorised
 // approximate inverse G = (I - E_lower) L^-1.
@@ -38,10 +39,10 @@
 
 namespace ys {
 
-constexpr int kGIn = 128, kGHid = 64, kGMsg = 320, kGOut = 192, kGLayers = 3, kGBlocks = 7, kGUsed = 25 * kGBlocks;
+constexpr int kGIn = 128, kGHid = 64, kGMsg = 320, kGOut = 128, kGLayers = 3, kGBlocks = 3, kGUsed = 25 * kGBlocks;
 constexpr float kGOutScale = 0.1f;
 // packed FP32 parameter vector: W0 [64][128], b0, then per layer W [64][320], b,
-// then Wh [192][64], bh
+// then Wh [128][64], bh
 constexpr int kPW0 = 0;
 constexpr int kPb0 = kPW0 + kGHid * kGIn;
 constexpr int kPL0 = kPb0 + kGHid;
@@ -52,7 +53,8 @@ constexpr int kPWh = kPL0 + kGLayers * kPLStride;
 constexpr int kPbh = kPWh + kGOut * kGHid;
 constexpr int kGParams = kPbh + kGOut;
 constexpr int kWgradRows = 384;  // largest K_in + 1 (bias row), rounded to the 128-row tile
-// lower pattern: offsets (du, dv) of block b
+// lower offsets (du, dv) b = 0..6: self, left, down, left-down, right-down,
+// left-2, down-2; G uses the first kGBlocks, the features all six couplings
 YS_HD constexpr int gpat_du(int b) { return b == 1 ? -1 : b == 3 ? -1 : b == 4 ? 1 : b == 5 ? -2 : 0; }
 YS_HD constexpr int gpat_dv(int b) { return b == 2 ? -1 : b == 3 ? -1 : b == 4 ? -1 : b == 6 ? -2 : 0; }
 
@@ -60,16 +62,16 @@ struct GnnNet {  // device arrays
   float* w;             // [kGParams] FP32 master parameters
   __nv_bfloat16* W0;    // [64][128]
   __nv_bfloat16* Wl;    // [3][64][320]
-  __nv_bfloat16* Wh;    // [192][64]
+  __nv_bfloat16* Wh;    // [128][64]
   __nv_bfloat16* WlT;   // [3][320][64]
-  __nv_bfloat16* WhT;   // [64][192]
+  __nv_bfloat16* WhT;   // [64][128]
 };
 
 struct GnnBufs {  // device arrays sized for ntot nodes
   int ntot;
   int nsplit;           // weight-gradient node splits
   int* nbr;             // [ntot][4] yarn neighbours (left, right, down, up) or -1
-  int* pat;             // [ntot][8] source node of lower block b (b < 7) or -1
+  int* pat;             // [ntot][8] source node of block b of G (b < kGBlocks) or -1
   int* upat;            // [ntot][8] the row i whose block b has this node as source, or -1
   float* linv;          // [15][ntot] L^-1, packed lower triangle (r (r + 1) / 2 + c)
   int* chol_ok;         // [ntot] 1 if the diagonal block factorised
@@ -78,16 +80,16 @@ struct GnnBufs {  // device arrays sized for ntot nodes
   float* h;             // [4][ntot][64] h1..h4
   __nv_bfloat16* hb;    // [4][ntot][64]
   __nv_bfloat16* act;   // [3][ntot][64] relu outputs of the message layers
-  float* o;             // [192][ntot] network outputs (component-major)
-  float* G;             // [175][ntot] blocks of G, row-major 5 x 5 (training, export)
-  __nv_bfloat16* Gh;    // [175][ntot] the same in BF16 (the solve's preconditioner)
-  float* Gn;            // [175][ntot] blocks of N (training)
+  float* o;             // [128][ntot] network outputs (component-major)
+  float* G;             // [75][ntot] blocks of G, row-major 5 x 5 (training, export)
+  __nv_bfloat16* Gh;    // [75][ntot] the same in BF16 (the solve's preconditioner)
+  float* Gn;            // [75][ntot] blocks of N (training)
   float* vec;           // [4][5][ntot] training vectors (w, u, t, s)
-  __nv_bfloat16* dob;   // [ntot][192]
+  __nv_bfloat16* dob;   // [ntot][128]
   float* dh;            // [ntot][64]
   __nv_bfloat16* dzb;   // [ntot][64]
   float* dm;            // [ntot][320]
-  float* wpart;         // [nsplit][kWgradRows][192]
+  float* wpart;         // [nsplit][kWgradRows][128]
   float* grad;          // [kGParams]
   double* lpart;        // [2][nlblk] loss partials, then loss and its two scales
   int nlblk;
@@ -96,7 +98,7 @@ struct GnnBufs {  // device arrays sized for ntot nodes
 
 // learned-preconditioner PCG state lives in Solver; these hold its extras
 struct LpcgExtra {
-  const __nv_bfloat16* G;  // [175][ntot]
+  const __nv_bfloat16* G;  // [75][ntot]
   const int* pat;   // [ntot][8]
   const int* upat;  // [ntot][8]
   float* y;         // [5][ntot] G r

@@ -82,13 +82,13 @@ class LearnedPreconditioner:
         return loss.value
 
     def loss_grad(self, batch: ClothBatch, probes: Optional[np.ndarray] = None, seed: int = 1) -> dict:
-        """Loss, parameter gradient, network outputs [n][192] and G blocks
-        [n][175] for the batch's last system (no update)."""
+        """Loss, parameter gradient, network outputs [n][128] and G blocks
+        [n][75] (self, left, down) for the batch's last system (no update)."""
         n = batch.total_nodes
         loss = ctypes.c_double()
         grad = np.zeros(param_count(), np.float32)
-        out = np.zeros((n, 192), np.float32)
-        gb = np.zeros((n, 175), np.float32)
+        out = np.zeros((n, 128), np.float32)
+        gb = np.zeros((n, 75), np.float32)
         pr = None
         if probes is not None:
             pr = np.ascontiguousarray(probes, np.float32)
@@ -127,16 +127,48 @@ def training_specs(rng: np.random.Generator, n_cloths: int, min_side: int = 5, m
     return specs
 
 
+def validation_residual(net: LearnedPreconditioner, batch: ClothBatch, k: int = 5, h: float = 1e-3) -> float:
+    """Mean log10 of the relative residual |r| / |b| after k learned PCG
+    iterations on the systems `batch` assembles at its current state: the
+    conjugate-gradient speed the preconditioner is for."""
+    batch.assemble(h)
+    batch.set_preconditioner("learned", net)
+    st = batch.solve(tol=1e-10, maxiter=k)
+    batch.set_preconditioner("jacobi")
+    return float(np.mean([np.log10(max(x["cg_error"], 1e-300)) for x in st]))
+
+
 def train(net: LearnedPreconditioner, systems: int = 20000, cloths_per_batch: int = 64, steps_per_batch: int = 40,
-          lr: float = 1e-3, seed: int = 0, h: float = 1e-3, log=None) -> list:
+          lr: float = 1e-3, seed: int = 0, h: float = 1e-3, val_every: int = 25, select: bool = True,
+          log=None) -> dict:
     """Trains on `systems` linear systems the simulator generates: batches of
     `cloths_per_batch` seeded cloths are stepped with Jacobi-PCG for
     `steps_per_batch` steps, and every step's systems (one per cloth) feed one
     Adam step on the Kaporin condition number of G A G^T. The rate decays by
-    cosine to 5 % of lr. Returns the loss history."""
+    cosine to 5 % of lr. Every `val_every` steps (and before the first) the
+    network is scored on held-out systems by validation_residual, and the
+    best-scoring parameters -- possibly the starting ones -- are kept (with
+    select=False the final parameters are).
+    Returns {"loss": [...], "validation": [(step, score)], "best_step": s}."""
     rng = np.random.default_rng(seed)
+    vrng = np.random.default_rng(seed + 7919)
+    vbatch = ClothBatch(training_specs(vrng, 8, 10, 40), device=net.device)
+    for _ in range(5):
+        vbatch.step(h, tol=1e-10)
     total_steps = max(1, math.ceil(systems / cloths_per_batch))
-    hist = []
+    hist, val = [], []
+    best, best_step, best_params = np.inf, 0, net.params()
+
+    def validate(k):
+        nonlocal best, best_step, best_params
+        score = validation_residual(net, vbatch, h=h)
+        val.append((k, score))
+        if score < best:
+            best, best_step, best_params = score, k, net.params()
+        if log is not None:
+            log("step %d validation %.3f (best %.3f at %d)" % (k, score, best, best_step))
+
+    validate(0)
     k = 0
     while k < total_steps:
         batch = ClothBatch(training_specs(rng, cloths_per_batch), device=net.device)
@@ -149,11 +181,16 @@ def train(net: LearnedPreconditioner, systems: int = 20000, cloths_per_batch: in
             rate = lr * (0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * k / total_steps)))
             loss = net.train_step(batch, seed=(seed << 20) + k + 1, lr=rate)
             hist.append(loss)
-            if log is not None and k % 50 == 0:
-                log("step %d/%d loss %.5f" % (k, total_steps, loss))
             k += 1
+            if k % val_every == 0:
+                validate(k)
         batch.close()
-    return hist
+    if k % val_every:
+        validate(k)
+    vbatch.close()
+    if select:
+        net.set_params(best_params)
+    return {"loss": hist, "validation": val, "best_step": best_step}
 
 
 def main(argv=None):
@@ -170,12 +207,14 @@ def main(argv=None):
     a = ap.parse_args(argv)
     net = LearnedPreconditioner(seed=a.seed)
     t0 = time.time()
-    hist = train(net, systems=a.systems, cloths_per_batch=a.cloths, steps_per_batch=a.steps_per_batch, lr=a.lr,
-                 seed=a.seed, log=print)
-    print("trained on %d systems in %.1f s; loss %.5f -> %.5f" % (len(hist) * a.cloths, time.time() - t0,
-                                                                   float(np.mean(hist[:10])), float(np.mean(hist[-10:]))))
+    res = train(net, systems=a.systems, cloths_per_batch=a.cloths, steps_per_batch=a.steps_per_batch, lr=a.lr,
+                seed=a.seed, log=print)
+    hist = res["loss"]
+    print("trained on %d systems in %.1f s; kept the parameters of step %d (validation %.3f)" % (
+        len(hist) * a.cloths, time.time() - t0, res["best_step"], min(v for _, v in res["validation"])))
     net.save(a.out)
     np.save(os.path.splitext(a.out)[0] + "_loss.npy", np.asarray(hist))
+    np.save(os.path.splitext(a.out)[0] + "_validation.npy", np.asarray(res["validation"]))
 
 
 if __name__ == "__main__":

@@ -281,8 +281,8 @@ ys_status ys_collider_get_impacts(ys_collider *c, ys_impact *impacts, int64_t ca
  * Eigen's Jacobi-PCG, src/Solvers.cpp:3-31, which stays the default and the
  * fallback). A graph network over the crossing graph reads each assembled
  * system and emits a factorised sparse approximate inverse M^-1 = G^T G, G
- * block lower triangular over the 7-block pattern self, left, down,
- * left-down, right-down, left-2, down-2 (5 x 5 blocks; G_i,0 = (I + N_i,0)
+ * block lower triangular over the blocks self, left, down of each node
+ * (5 x 5 blocks; G_i,0 = (I + N_i,0)
  * L_i^-1, G_i,b = N_i,b L_src^-1, L_i the Cholesky factor of node i's
  * diagonal block). The conjugate-gradient iteration keeps FP64 and the same
  * stopping rule |r| <= tol |b|; M^-1 is applied in FP32 with the flexible
@@ -290,7 +290,7 @@ ys_status ys_collider_get_impacts(ys_collider *c, ys_impact *impacts, int64_t ca
 typedef struct ys_gnn ys_gnn;
 enum { YS_PREC_JACOBI = 0, YS_PREC_LEARNED = 1 };
 /* number of FP32 parameters (packed: W0 [64][128], b0 [64], 3 x (W [64][320],
- * b [64]), Wh [192][64], bh [192]) */
+ * b [64]), Wh [128][64], bh [128]) */
 int32_t ys_gnn_param_count(void);
 /* a network with seeded initial weights (output head zero: the analytic
  * first-order approximate inverse G = (I - E_lower) L^-1) */
@@ -306,9 +306,9 @@ ys_status ys_gnn_set_params(ys_gnn *g, const float *in);
  * loss before the step. */
 ys_status ys_gnn_train_step(ys_gnn *g, ys_batch *b, uint64_t seed, float lr, double *loss);
 /* Loss and gradient without an update (probes [total_nodes][5] host, or NULL
- * for seeded probes); outputs [total_nodes][192] network outputs, gblocks
- * [total_nodes][175] blocks of G (self, left, down, left-down, right-down,
- * left-2, down-2; row-major 5 x 5); any output may be NULL. */
+ * for seeded probes); outputs [total_nodes][128] network outputs, gblocks
+ * [total_nodes][75] blocks of G (self, left, down; row-major 5 x 5); any
+ * output may be NULL. */
 ys_status ys_gnn_loss_grad(ys_gnn *g, ys_batch *b, const float *probes, uint64_t seed, double *loss, float *grad,
                            float *outputs, float *gblocks);
 /* kind YS_PREC_JACOBI (default) or YS_PREC_LEARNED with network g; the batch

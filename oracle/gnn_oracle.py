@@ -27,8 +27,9 @@ SLOT_LE_NBR, SLOT_EL_NBR, SLOT_EE_NBR = 131, 143, 155
 STENCIL = [(0, 0), (-1, 0), (1, 0), (0, -1), (0, 1), (-2, 0), (2, 0), (0, -2), (0, 2), (-1, -1), (1, -1), (-1, 1),
            (1, 1)]
 YARN_NBR = [(-1, 0), (1, 0), (0, -1), (0, 1)]  # left, right, down, up
-IN, HID, MSG, OUT, LAYERS, OUT_SCALE, BLOCKS = 128, 64, 320, 192, 3, 0.1, 7
-# lower pattern of G: self, left, down, left-down, right-down, left-2, down-2
+IN, HID, MSG, OUT, LAYERS, OUT_SCALE, BLOCKS = 128, 64, 320, 128, 3, 0.1, 3
+# lower offsets: self, left, down, left-down, right-down, left-2, down-2; G uses
+# the first BLOCKS, the features the six couplings
 PATTERN = [(0, 0), (-1, 0), (0, -1), (-1, -1), (1, -1), (-2, 0), (0, -2)]
 UPPER = [(1, 0), (0, 1), (1, 1), (-1, 1), (2, 0), (0, 2)]
 P_W0 = 0
@@ -76,7 +77,7 @@ class Topology:
             return np.where(ok, idx + du + dv * self.W, -1)
         self.stencil = np.stack([nb(du, dv) for du, dv in STENCIL], 1)  # [n, 13]
         self.nbr = np.stack([nb(du, dv) for du, dv in YARN_NBR], 1)     # [n, 4]
-        self.pat = np.stack([nb(du, dv) for du, dv in PATTERN], 1)      # [n, 7]
+        self.pat = np.stack([nb(du, dv) for du, dv in PATTERN], 1)      # [n, 7] (G: first BLOCKS)
         self.upper = np.stack([nb(du, dv) for du, dv in UPPER], 1)      # [n, 6]
 
 
@@ -163,12 +164,12 @@ def scaled(slots, topo, Linv, du, dv, idx):
 
 def features(slots, topo: Topology, Linv, ok):
     """f [n, 128] (before BF16 rounding) and the scaled couplings E [n, 6, 5, 5]
-    of the lower-pattern blocks 1..6."""
+    to the six lower offsets (G uses the first BLOCKS - 1 of them)."""
     n = topo.n
     f = np.zeros((n, IN))
     E = np.zeros((n, 6, 5, 5))
     sl32 = slots.astype(np.float32).astype(np.float64)
-    for b in range(1, BLOCKS):
+    for b in range(1, 7):
         E[:, b - 1] = scaled(sl32, topo, Linv, *PATTERN[b], topo.pat[:, b])
         if b <= 2:
             f[:, 25 * (b - 1):25 * b] = E[:, b - 1].reshape(n, 25)
@@ -202,7 +203,7 @@ def network(params, f, topo: Topology):
 
 
 def n_blocks(o, E, topo: Topology):
-    """N [n, 7, 5, 5] over the lower pattern (zero where the source is outside)."""
+    """N [n, BLOCKS, 5, 5] over the lower pattern (zero where the source is outside)."""
     n = topo.n
     Ns = [OUT_SCALE * o[:, 0:25].reshape(n, 5, 5)]
     Et = torch.as_tensor(E)
@@ -213,7 +214,7 @@ def n_blocks(o, E, topo: Topology):
 
 
 def g_blocks(Nb, Linv, topo: Topology):
-    """G [n, 7, 5, 5]: (I + N_0) L_i^-1 and N_b L_src^-1."""
+    """G [n, BLOCKS, 5, 5]: (I + N_0) L_i^-1 and N_b L_src^-1."""
     Lt = torch.as_tensor(Linv)
     eye = torch.eye(5, dtype=Nb.dtype)
     out = [(eye + Nb[:, 0]) @ Lt]
@@ -267,7 +268,7 @@ def spmv(slots, x, topo: Topology):
 
 
 def evaluate(slots, topo: Topology, params, probes):
-    """dict(loss, grad [N_PARAMS], o [n, 192], G [n, 175], f, E, Linv, chol_ok)."""
+    """dict(loss, grad [N_PARAMS], o [n, 128], G [n, 75], f, E, Linv, chol_ok)."""
     Linv, ok = block_factor(slots)
     f, E = features(slots, topo, Linv, ok)
     p = torch.as_tensor(np.asarray(params, np.float64), dtype=torch.float64).requires_grad_(True)
@@ -283,7 +284,7 @@ def evaluate(slots, topo: Topology, params, probes):
     loss = torch.log(tr / nd) - 2.0 * logdet / nd
     loss.backward()
     return dict(loss=float(loss.detach()), grad=p.grad.numpy().copy(), o=o.detach().numpy(),
-                G=Gb.detach().reshape(topo.n, 175).numpy(), f=f, E=E, Linv=Linv, chol_ok=ok)
+                G=Gb.detach().reshape(topo.n, 25 * BLOCKS).numpy(), f=f, E=E, Linv=Linv, chol_ok=ok)
 
 
 def init_params(seed: int) -> np.ndarray:

