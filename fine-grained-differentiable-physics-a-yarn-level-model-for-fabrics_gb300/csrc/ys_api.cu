@@ -256,6 +256,12 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
     if (d.pose < 0 || d.pose > 1 || d.weave < 0 || d.weave > 2) return fail(YS_ERR_ARG, "bad pose or weave");
     if (!(d.L > 0) || !(d.R > 0) || d.R >= d.L) return fail(YS_ERR_ARG, "need 0 < R < L");
     if (d.n_handles < 0 || (d.n_handles > 0 && !d.handles)) return fail(YS_ERR_ARG, "bad handle list");
+    for (int hnd = 0; hnd < d.n_handles; ++hnd) {
+      // the reference's set_handles looks each up with nodes.at() and throws
+      // for a node outside the cloth (src/Cloth.cpp:386-394)
+      const int u = d.handles[2 * hnd], vv = d.handles[2 * hnd + 1];
+      if (u < 0 || u >= d.width || vv < 0 || vv >= d.length) return fail(YS_ERR_ARG, "handle outside the cloth");
+    }
   }
   YS_CUDA(cudaSetDevice(device));
   ys_batch* b = new ys_batch();
