@@ -26,7 +26,8 @@ EXPORTED = [
     "ys_collider_get_pairs", "ys_collider_find_impacts", "ys_collider_get_impacts", "ys_use_graphs",
     "ys_step_graphed", "ys_autotune", "ys_gnn_param_count", "ys_gnn_create", "ys_gnn_destroy", "ys_gnn_get_params",
     "ys_gnn_set_params", "ys_gnn_train_step", "ys_gnn_loss_grad", "ys_set_preconditioner", "ys_precond_info",
-    "ys_get_system_slots", "ys_tc_gemm_bf16", "ys_precond_refresh", "ys_get_normals",
+    "ys_get_system_slots", "ys_tc_gemm_bf16", "ys_precond_refresh", "ys_get_normals", "ys_collider_respond",
+    "ys_collider_response_impacts", "ys_collider_respond_backward",
 ]
 YS_PREC_JACOBI, YS_PREC_LEARNED = 0, 1
 YS_TANGENT_EXACT, YS_TANGENT_REFERENCE = 0, 1
@@ -149,6 +150,10 @@ def load(build_if_missing: bool = True):
     L.ys_precond_info.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     L.ys_get_system_slots.argtypes = [vp, vp, vp]
     L.ys_tc_gemm_bf16.argtypes = [ctypes.c_int32, vp, vp, vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
+    L.ys_collider_respond.argtypes = [vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, vp, vp,
+                                      ctypes.POINTER(ResponseInfo)]
+    L.ys_collider_response_impacts.argtypes = [vp, vp, ctypes.c_int64]
+    L.ys_collider_respond_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     for name in EXPORTED:
         if name not in ("ys_batch_destroy", "ys_last_error", "ys_cloth_node_offset", "ys_cloth_dim",
                         "ys_tangent_count", "ys_collider_destroy", "ys_gnn_destroy", "ys_gnn_param_count"):
@@ -165,6 +170,13 @@ class Impact(ctypes.Structure):
     """ys_impact (include/yarnsim.h)."""
     _fields_ = [("type", ctypes.c_int32), ("nodes", ctypes.c_int32 * 4), ("t", ctypes.c_double),
                 ("w", ctypes.c_double * 4), ("n", ctypes.c_double * 3), ("pair", ctypes.c_int64)]
+
+
+class ResponseInfo(ctypes.Structure):
+    """ys_response_info (include/yarnsim.h)."""
+    _fields_ = [("rounds", ctypes.c_int32), ("converged", ctypes.c_int32), ("changed", ctypes.c_int32),
+                ("zones", ctypes.c_int32), ("infeasible", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("impacts", ctypes.c_int64), ("projections", ctypes.c_int64)]
 
 
 class YarnSimError(RuntimeError):

@@ -1,7 +1,9 @@
 """Continuous collision detection of a cloth mesh against itself and an
 obstacle mesh on the GPU: the reference's Collision::find_impacts
 (src/Collision.cpp:184-208) -- its 18-DOP BVH broad phase and the
-vertex-face / edge-edge narrow phase -- behind the C ABI's ys_collider_*.
+vertex-face / edge-edge narrow phase -- behind the C ABI's ys_collider_*,
+and the impact-zone response around it (Collision::collision_response,
+src/Collision.cpp:73-156) with the backward of its projections.
 """
 from __future__ import annotations
 
@@ -46,6 +48,7 @@ class Collider:
                                             int(bool(ccd)), int(device), ctypes.c_void_p(stream) if stream else None,
                                             ctypes.byref(h)), "ys_collider_create")
         self._h = h
+        self._n_received = 0
 
     def close(self):
         if getattr(self, "_h", None):
@@ -84,3 +87,51 @@ class Collider:
         a = np.ctypeslib.as_array(buf)[:n.value]
         return dict(type=a["type"].copy(), nodes=a["nodes"].copy(), t=a["t"].copy(), w=a["w"].copy(),
                     n=a["n"].copy(), pair=a["pair"].copy())
+
+    def respond(self, v=None, mass=None, h: float = 1e-3, damp: float = 0.1, max_iter: int = 100,
+                check: bool = True) -> dict:
+        """collision_response(damp) over the positions of the last
+        set_positions: rounds of GPU detection, independent impacts, impact
+        zones and their exact inelastic projections, then v + damp (x - x_before)
+        / h when a zone moved. v [n, 3] and mass [n] are optional. Returns
+        dict(x, v, rounds, converged, changed, zones, infeasible, impacts,
+        projections); raises when max_iter rounds still found impacts (where the
+        reference exits) unless check=False."""
+        x = np.zeros((self.n_nodes, 3))
+        vv = None if v is None else np.array(v, np.float64).reshape(self.n_nodes, 3).copy()
+        m = None if mass is None else np.ascontiguousarray(mass, np.float64).reshape(self.n_nodes)
+        info = N.ResponseInfo()
+        st = N.load().ys_collider_respond(self._h, ctypes.c_void_p(m.ctypes.data) if m is not None else None,
+                                          float(h), float(damp), int(max_iter), ctypes.c_void_p(x.ctypes.data),
+                                          ctypes.c_void_p(vv.ctypes.data) if vv is not None else None,
+                                          ctypes.byref(info))
+        if st != N.YS_ERR_MAXITER or check:
+            N.check(st, "ys_collider_respond")
+        self._n_received = int(info.impacts)
+        return dict(x=x, v=vv, rounds=info.rounds, converged=bool(info.converged), changed=bool(info.changed),
+                    zones=info.zones, infeasible=info.infeasible, impacts=info.impacts,
+                    projections=info.projections)
+
+    def response_impacts(self) -> dict:
+        """The impacts the zones of the last response received, in order
+        (arrays as impacts(); "round" = the round that found each)."""
+        n = self._n_received
+        buf = (N.Impact * max(n, 1))()
+        N.check(N.load().ys_collider_response_impacts(self._h, buf, n), "ys_collider_response_impacts")
+        a = np.ctypeslib.as_array(buf)[:n]
+        return dict(type=a["type"].copy(), nodes=a["nodes"].copy(), t=a["t"].copy(), w=a["w"].copy(),
+                    n=a["n"].copy(), round=a["pair"].copy())
+
+    def respond_backward(self, dl_dx=None, dl_dv=None) -> dict:
+        """Backward of the last respond(): gradients of x and v before it and
+        of every received impact's weights [I, 4] and normal [I, 3]."""
+        n3 = (self.n_nodes, 3)
+        gx = None if dl_dx is None else np.ascontiguousarray(dl_dx, np.float64).reshape(n3)
+        gv = None if dl_dv is None else np.ascontiguousarray(dl_dv, np.float64).reshape(n3)
+        ni = self._n_received
+        ox, ov = np.zeros(n3), np.zeros(n3)
+        gw, gn = np.zeros((max(ni, 1), 4)), np.zeros((max(ni, 1), 3))
+        p = lambda a: ctypes.c_void_p(a.ctypes.data) if a is not None else None
+        N.check(N.load().ys_collider_respond_backward(self._h, p(gx), p(gv), p(ox), p(ov), p(gw), p(gn)),
+                "ys_collider_respond_backward")
+        return dict(x=ox, v=ov, w=gw[:ni], n=gn[:ni])

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -15,6 +16,7 @@
 #include "../../include/yarnsim.h"
 #include "ys_bvh.h"
 #include "ys_collide.cuh"
+#include "ys_zones.h"
 
 extern "C" ys_status ys_internal_fail(ys_status s, const char* msg);
 
@@ -76,6 +78,11 @@ struct BroadArgs {
   int* out;               // write pass: [P][3]
   int64_t* count;         // count pass: pairs of each face
   int* overflow;
+  // active faces (null: all): a pair is reported only if one of its faces is
+  // active, obstacle faces never are (update_active and the traversal's
+  // active test, src/Collision.cpp:158-182, 289-310)
+  const uint8_t* face_active;
+  const uint8_t* node_active;  // cloth-tree nodes with an active leaf below
 };
 
 // the pairs whose first face is f: cloth faces g the reference reports with
@@ -86,15 +93,17 @@ __global__ void k_broad(BroadArgs a) {
   if (f >= a.nfaces) return;
   const Kdop bf = a.cloth.box[a.leaf_of_face[f]];
   const int uf = a.upper[f], rf = a.rank[f];
+  const bool fa = a.face_active == nullptr || a.face_active[f] != 0;
   int64_t c = 0, o = WRITE ? a.offset[f] : 0;
   int stack[kStack];
   for (int pass = 0; pass < 2; ++pass) {
     const DevTree& t = pass == 0 ? a.cloth : a.obs;
-    if (t.nnodes == 0) continue;
+    if (t.nnodes == 0 || (pass == 1 && !fa)) continue;
     int sp = 0;
     stack[sp++] = 0;
     while (sp > 0) {
       const int n = stack[--sp];
+      if (!fa && a.node_active[n] == 0) continue;  // pass 0 only: no active face below
       const int g = t.face[n];
       if (g >= 0) {
         if (pass == 0) {
@@ -222,6 +231,13 @@ struct ys_collider {
   int64_t nimpacts = 0;
   DVec<int> overflow;
   bool have_pairs = false, have_impacts = false;
+  // impact-zone response
+  DVec<uint8_t> face_active, node_active;
+  std::vector<uint8_t> h_node_active;
+  ys::ZoneResponse resp;
+  std::vector<double> resp_x0;  // positions before the response
+  bool have_response = false;
+  double resp_h = 0.0, resp_damp = 0.0;
 };
 
 namespace {
@@ -293,6 +309,78 @@ void edges_of(const int* fv, int f, int e[3][2], bool obstacle, const std::vecto
     e[a][1] = fv[3 * f + b];
     if (obstacle && e[a][0] > e[a][1]) std::swap(e[a][0], e[a][1]);
   }
+}
+
+ys_status broad_phase(ys_collider* c, bool masked) {
+  BroadArgs a{};
+  a.cloth = DevTree{c->c_left.p, c->c_right.p, c->c_face.p, c->c_box.p, (int)c->ct.face.size()};
+  a.obs = DevTree{c->o_left.p, c->o_right.p, c->o_face.p, c->o_box.p, (int)c->ot.face.size()};
+  a.leaf_of_face = c->c_lof.p;
+  a.rank = c->c_rank.p;
+  a.upper = c->c_upper.p;
+  a.nfaces = c->n_faces;
+  a.thickness = c->thickness;
+  a.count = c->counts.p;
+  a.overflow = c->overflow.p;
+  a.face_active = masked ? c->face_active.p : nullptr;
+  a.node_active = masked ? c->node_active.p : nullptr;
+  YC_CUDA(cudaMemsetAsync(c->overflow.p, 0, sizeof(int), c->stream));
+  const unsigned g = (unsigned)((c->n_faces + 127) / 128);
+  k_broad<false><<<g, 128, 0, c->stream>>>(a);
+  YC_CUDA(cudaGetLastError());
+  ys_status s = scan(c, c->counts.p, c->n_faces, c->offsets.p, &c->npairs);
+  if (s != YS_OK) return s;
+  int ovf = 0;
+  YC_CUDA(cudaMemcpy(&ovf, c->overflow.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (ovf) return ys_internal_fail(YS_ERR_ARG, "BVH deeper than the traversal stack");
+  YC_CUDA(c->pairs.reserve(3 * (size_t)std::max<int64_t>(c->npairs, 1)));
+  a.offset = c->offsets.p;
+  a.out = c->pairs.p;
+  k_broad<true><<<g, 128, 0, c->stream>>>(a);
+  YC_CUDA(cudaGetLastError());
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  c->have_pairs = true;
+  c->have_impacts = false;
+  return YS_OK;
+}
+
+ys_status narrow_phase(ys_collider* c) {
+  const int64_t P = c->npairs;
+  YC_CUDA(c->slots.reserve(15 * (size_t)std::max<int64_t>(P, 1)));
+  YC_CUDA(c->icount.reserve(std::max<int64_t>(P, 1)));
+  YC_CUDA(c->ioffset.reserve(std::max<int64_t>(P, 1)));
+  CMesh m{c->x.p, c->xp.p, c->ox.p, c->oxp.p};
+  if (P) {
+    k_narrow<<<(unsigned)((P + 127) / 128), 128, 0, c->stream>>>(c->pairs.p, P, c->faces.p, c->ofaces.p, m,
+                                                                  c->thickness, c->ccd, c->slots.p, c->icount.p);
+    YC_CUDA(cudaGetLastError());
+  }
+  ys_status s = scan(c, c->icount.p, P, c->ioffset.p, &c->nimpacts);
+  if (s != YS_OK) return s;
+  YC_CUDA(c->impacts.reserve(std::max<int64_t>(c->nimpacts, 1)));
+  if (P) {
+    k_compact<<<(unsigned)((P + 127) / 128), 128, 0, c->stream>>>(c->slots.p, c->icount.p, c->ioffset.p, P,
+                                                                   c->impacts.p);
+    YC_CUDA(cudaGetLastError());
+  }
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  c->have_impacts = true;
+  return YS_OK;
+}
+
+// marks the cloth-tree nodes with an active leaf below (host tree)
+bool mark_nodes(const ys::BvhTree& t, const uint8_t* fa, std::vector<uint8_t>& out, int n) {
+  const int f = t.face[n];
+  bool on;
+  if (f >= 0) {
+    on = fa[f] != 0;
+  } else {
+    const bool l = mark_nodes(t, fa, out, t.left[n]);
+    const bool r = mark_nodes(t, fa, out, t.right[n]);
+    on = l || r;
+  }
+  out[n] = on ? 1 : 0;
+  return on;
 }
 
 }  // namespace
@@ -443,33 +531,8 @@ ys_status ys_collider_set_positions(ys_collider* c, const double* x, const doubl
 ys_status ys_collider_find_pairs(ys_collider* c, int64_t* n_pairs) {
   if (!c || c->ct.face.empty()) return ys_internal_fail(YS_ERR_ARG, "ys_collider_find_pairs before set_positions");
   YC_CUDA(cudaSetDevice(c->device));
-  BroadArgs a{};
-  a.cloth = DevTree{c->c_left.p, c->c_right.p, c->c_face.p, c->c_box.p, (int)c->ct.face.size()};
-  a.obs = DevTree{c->o_left.p, c->o_right.p, c->o_face.p, c->o_box.p, (int)c->ot.face.size()};
-  a.leaf_of_face = c->c_lof.p;
-  a.rank = c->c_rank.p;
-  a.upper = c->c_upper.p;
-  a.nfaces = c->n_faces;
-  a.thickness = c->thickness;
-  a.count = c->counts.p;
-  a.overflow = c->overflow.p;
-  YC_CUDA(cudaMemsetAsync(c->overflow.p, 0, sizeof(int), c->stream));
-  const unsigned g = (unsigned)((c->n_faces + 127) / 128);
-  k_broad<false><<<g, 128, 0, c->stream>>>(a);
-  YC_CUDA(cudaGetLastError());
-  ys_status s = scan(c, c->counts.p, c->n_faces, c->offsets.p, &c->npairs);
+  ys_status s = broad_phase(c, false);
   if (s != YS_OK) return s;
-  int ovf = 0;
-  YC_CUDA(cudaMemcpy(&ovf, c->overflow.p, sizeof(int), cudaMemcpyDeviceToHost));
-  if (ovf) return ys_internal_fail(YS_ERR_ARG, "BVH deeper than the traversal stack");
-  YC_CUDA(c->pairs.reserve(3 * (size_t)std::max<int64_t>(c->npairs, 1)));
-  a.offset = c->offsets.p;
-  a.out = c->pairs.p;
-  k_broad<true><<<g, 128, 0, c->stream>>>(a);
-  YC_CUDA(cudaGetLastError());
-  YC_CUDA(cudaStreamSynchronize(c->stream));
-  c->have_pairs = true;
-  c->have_impacts = false;
   if (n_pairs) *n_pairs = c->npairs;
   return YS_OK;
 }
@@ -486,26 +549,8 @@ ys_status ys_collider_get_pairs(ys_collider* c, int32_t* pairs, int64_t cap) {
 ys_status ys_collider_find_impacts(ys_collider* c, int64_t* n_impacts) {
   if (!c || !c->have_pairs) return ys_internal_fail(YS_ERR_ARG, "ys_collider_find_impacts before find_pairs");
   YC_CUDA(cudaSetDevice(c->device));
-  const int64_t P = c->npairs;
-  YC_CUDA(c->slots.reserve(15 * (size_t)std::max<int64_t>(P, 1)));
-  YC_CUDA(c->icount.reserve(std::max<int64_t>(P, 1)));
-  YC_CUDA(c->ioffset.reserve(std::max<int64_t>(P, 1)));
-  CMesh m{c->x.p, c->xp.p, c->ox.p, c->oxp.p};
-  if (P) {
-    k_narrow<<<(unsigned)((P + 127) / 128), 128, 0, c->stream>>>(c->pairs.p, P, c->faces.p, c->ofaces.p, m,
-                                                                  c->thickness, c->ccd, c->slots.p, c->icount.p);
-    YC_CUDA(cudaGetLastError());
-  }
-  ys_status s = scan(c, c->icount.p, P, c->ioffset.p, &c->nimpacts);
+  ys_status s = narrow_phase(c);
   if (s != YS_OK) return s;
-  YC_CUDA(c->impacts.reserve(std::max<int64_t>(c->nimpacts, 1)));
-  if (P) {
-    k_compact<<<(unsigned)((P + 127) / 128), 128, 0, c->stream>>>(c->slots.p, c->icount.p, c->ioffset.p, P,
-                                                                   c->impacts.p);
-    YC_CUDA(cudaGetLastError());
-  }
-  YC_CUDA(cudaStreamSynchronize(c->stream));
-  c->have_impacts = true;
   if (n_impacts) *n_impacts = c->nimpacts;
   return YS_OK;
 }
@@ -516,6 +561,147 @@ ys_status ys_collider_get_impacts(ys_collider* c, ys_impact* impacts, int64_t ca
   YC_CUDA(cudaSetDevice(c->device));
   if (c->nimpacts)
     YC_CUDA(cudaMemcpy(impacts, c->impacts.p, sizeof(ys_impact) * c->nimpacts, cudaMemcpyDeviceToHost));
+  return YS_OK;
+}
+
+ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h, double damp, int32_t max_iter,
+                              double* x_out, double* v, ys_response_info* info) {
+  if (!c || c->ct.face.empty()) return ys_internal_fail(YS_ERR_ARG, "ys_collider_respond before set_positions");
+  if (!x_out || !(h > 0.0) || !std::isfinite(damp) || max_iter <= 0)
+    return ys_internal_fail(YS_ERR_ARG, "bad response arguments");
+  if (node_mass)
+    for (int i = 0; i < c->n_nodes; ++i)
+      if (!(node_mass[i] > 0.0) || !std::isfinite(node_mass[i]))
+        return ys_internal_fail(YS_ERR_ARG, "node masses must be positive and finite");
+  YC_CUDA(cudaSetDevice(c->device));
+  ys::ZoneResponse& R = c->resp;
+  c->have_response = false;
+  R.n_nodes = c->n_nodes;
+  R.n_faces = c->n_faces;
+  R.faces = c->fv.data();
+  R.obs_x = c->hox.data();
+  R.thickness = c->thickness;
+  R.max_iter = max_iter;
+  c->resp_x0 = c->hx;
+  std::vector<double> x(c->hx);
+  const size_t n3 = 3 * (size_t)c->n_nodes;
+  bool first = true;
+  ys_status err = YS_OK;
+  std::vector<ys_impact> got;
+  // one detection round on the GPU: the trees keep the topology built by
+  // set_positions and are refit to the current positions (AccelStruct::update)
+  auto detect = [&](const double* xc, const uint8_t* mask, std::vector<ys::ZImpact>& out) -> int {
+    auto fail = [&](ys_status s) {
+      err = s;
+      return 1;
+    };
+    if (!first) {
+      if (cudaMemcpyAsync(c->x.p, xc, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+        return fail(ys_internal_fail(YS_ERR_CUDA, "cudaMemcpyAsync failed"));
+      ys_status s = refit(c, false);
+      if (s != YS_OK) return fail(s);
+    }
+    first = false;
+    if (mask) {
+      const size_t nn = c->ct.face.size();
+      if (c->face_active.reserve(c->n_faces) != cudaSuccess || c->node_active.reserve(nn) != cudaSuccess)
+        return fail(ys_internal_fail(YS_ERR_CUDA, "cudaMalloc failed"));
+      c->h_node_active.assign(nn, 0);
+      mark_nodes(c->ct, mask, c->h_node_active, 0);
+      if (cudaMemcpyAsync(c->face_active.p, mask, c->n_faces, cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+          cudaMemcpyAsync(c->node_active.p, c->h_node_active.data(), nn, cudaMemcpyHostToDevice, c->stream) !=
+              cudaSuccess)
+        return fail(ys_internal_fail(YS_ERR_CUDA, "cudaMemcpyAsync failed"));
+    }
+    ys_status s = broad_phase(c, mask != nullptr);
+    if (s != YS_OK) return fail(s);
+    if ((s = narrow_phase(c)) != YS_OK) return fail(s);
+    got.resize((size_t)c->nimpacts);
+    if (c->nimpacts &&
+        cudaMemcpy(got.data(), c->impacts.p, sizeof(ys_impact) * c->nimpacts, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return fail(ys_internal_fail(YS_ERR_CUDA, "cudaMemcpy failed"));
+    out.resize(got.size());
+    for (size_t i = 0; i < got.size(); ++i) {
+      ys::ZImpact& z = out[i];
+      z.type = got[i].type;
+      z.t = got[i].t;
+      for (int q = 0; q < 4; ++q) {
+        z.node[q] = got[i].nodes[q];
+        z.w[q] = got[i].w[q];
+      }
+      for (int q = 0; q < 3; ++q) z.n[q] = got[i].n[q];
+    }
+    return 0;
+  };
+  if (ys::zone_respond(R, x.data(), node_mass, detect)) return err;
+  // the collider keeps the responded positions (the cloth mesh's x)
+  c->hx = x;
+  YC_CUDA(cudaMemcpyAsync(c->x.p, c->hx.data(), n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  ys_status s = refit(c, false);
+  if (s != YS_OK) return s;
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  c->have_pairs = c->have_impacts = false;
+  std::memcpy(x_out, x.data(), n3 * sizeof(double));
+  // velocity update of collision_response (src/Collision.cpp:130-137)
+  if (v && R.changed)
+    for (size_t i = 0; i < n3; ++i) v[i] = v[i] + (damp * (x[i] - c->resp_x0[i])) / h;
+  c->resp_h = h;
+  c->resp_damp = damp;
+  c->have_response = true;
+  if (info) {
+    info->rounds = R.rounds;
+    info->converged = R.converged;
+    info->changed = R.changed;
+    info->zones = R.zones;
+    info->infeasible = R.infeasible;
+    info->reserved = 0;
+    info->impacts = (int64_t)R.accepted.size();
+    info->projections = (int64_t)R.tape.size();
+  }
+  if (!R.converged) return ys_internal_fail(YS_ERR_MAXITER, "collision response did not converge");
+  return YS_OK;
+}
+
+ys_status ys_collider_response_impacts(ys_collider* c, ys_impact* impacts, int64_t cap) {
+  if (!c || !c->have_response) return ys_internal_fail(YS_ERR_ARG, "no collision response yet");
+  const ys::ZoneResponse& R = c->resp;
+  if (cap < (int64_t)R.accepted.size()) return ys_internal_fail(YS_ERR_ARG, "impact buffer too small");
+  for (size_t i = 0; i < R.accepted.size(); ++i) {
+    const ys::ZImpact& z = R.accepted[i];
+    ys_impact& o = impacts[i];
+    o.type = z.type;
+    o.t = z.t;
+    for (int q = 0; q < 4; ++q) {
+      o.nodes[q] = z.node[q];
+      o.w[q] = z.w[q];
+    }
+    for (int q = 0; q < 3; ++q) o.n[q] = z.n[q];
+    o.pair = R.accepted_round[i];
+  }
+  return YS_OK;
+}
+
+ys_status ys_collider_respond_backward(ys_collider* c, const double* dl_dx, const double* dl_dv, double* dl_dx_in,
+                                       double* dl_dv_in, double* dl_dw, double* dl_dn) {
+  if (!c || !c->have_response) return ys_internal_fail(YS_ERR_ARG, "no collision response yet");
+  if (!dl_dx_in) return ys_internal_fail(YS_ERR_ARG, "dl_dx_in is required");
+  const ys::ZoneResponse& R = c->resp;
+  const size_t n3 = 3 * (size_t)c->n_nodes, na = R.accepted.size();
+  std::vector<double> g(n3, 0.0), gw(4 * std::max<size_t>(na, 1), 0.0), gn(3 * std::max<size_t>(na, 1), 0.0);
+  if (dl_dx) std::memcpy(g.data(), dl_dx, n3 * sizeof(double));
+  const double k = c->resp_damp / c->resp_h;
+  if (dl_dv && R.changed)
+    for (size_t i = 0; i < n3; ++i) g[i] += k * dl_dv[i];
+  ys::zone_backward(R, g.data(), gw.data(), gn.data());
+  if (dl_dv && R.changed)
+    for (size_t i = 0; i < n3; ++i) g[i] -= k * dl_dv[i];
+  std::memcpy(dl_dx_in, g.data(), n3 * sizeof(double));
+  if (dl_dv_in) {
+    if (dl_dv) std::memcpy(dl_dv_in, dl_dv, n3 * sizeof(double));
+    else std::memset(dl_dv_in, 0, n3 * sizeof(double));
+  }
+  if (dl_dw && na) std::memcpy(dl_dw, gw.data(), 4 * na * sizeof(double));
+  if (dl_dn && na) std::memcpy(dl_dn, gn.data(), 3 * na * sizeof(double));
   return YS_OK;
 }
 

@@ -277,6 +277,45 @@ ys_status ys_collider_get_pairs(ys_collider *c, int32_t *pairs, int64_t cap);
 ys_status ys_collider_find_impacts(ys_collider *c, int64_t *n_impacts);
 ys_status ys_collider_get_impacts(ys_collider *c, ys_impact *impacts, int64_t cap);
 
+/* ---- Impact-zone response: Collision::collision_response
+ * (src/Collision.cpp:73-156) over the positions given to
+ * ys_collider_set_positions (x after the step, x_prev before it). Rounds of
+ * GPU detection (after the first, only face pairs with a face next to an
+ * active zone), a greedy independent subset of the impacts sorted by time,
+ * impact zones with merging, and the inelastic projection of every zone that
+ * gained impacts (NormalOpt, src/Collision.h:139-165), solved exactly on the
+ * host (the reference's augmented Lagrangian stops at its tolerances);
+ * ties in time are broken by type, nodes, weights and normal. node_mass [n]
+ * may be NULL (equal masses, as the reference's MeshMass gives). x_out [n][3]
+ * receives the positions after the response; v [n][3] (may be NULL) is
+ * updated in place as v + damp (x - x_before) / h when any zone moved.
+ * Returns YS_ERR_MAXITER when max_iter rounds (the reference's 100) still
+ * found impacts, where the reference exits; x_out and v are written. */
+typedef struct {
+  int32_t rounds;      /* rounds that found impacts (the reference's iter) */
+  int32_t converged;   /* 1: a round found no impact within max_iter */
+  int32_t changed;     /* 1: a zone was projected (velocities updated) */
+  int32_t zones;       /* impact zones at the end */
+  int32_t infeasible;  /* projections whose constraints had no solution (zone left in place) */
+  int32_t reserved;
+  int64_t impacts;     /* impacts the zones received, over all rounds */
+  int64_t projections; /* zone projections */
+} ys_response_info;
+ys_status ys_collider_respond(ys_collider *c, const double *node_mass, double h, double damp, int32_t max_iter,
+                              double *x_out, double *v, ys_response_info *info);
+/* The impacts the zones received, in order (info.impacts of them); the
+ * pair field holds the round that found each. */
+ys_status ys_collider_response_impacts(ys_collider *c, ys_impact *impacts, int64_t cap);
+/* Backward of the last response (InelasticProjection::backward,
+ * src/Collision.cpp:496-682, and the velocity update): dl_dx, dl_dv [n][3]
+ * (either may be NULL) are the gradients of the outputs; dl_dx_in and
+ * dl_dv_in [n][3] receive those of the inputs, dl_dw [impacts][4] and
+ * dl_dn [impacts][3] (may be NULL) those of each impact's weights and
+ * normal. The gradient of a projection's anchor goes to the zone's positions
+ * at that projection, as the reference's autograd sends it. */
+ys_status ys_collider_respond_backward(ys_collider *c, const double *dl_dx, const double *dl_dv, double *dl_dx_in,
+                                       double *dl_dv_in, double *dl_dw, double *dl_dn);
+
 /* ---- learned preconditioner (no counterpart in the reference: its solve is
  * Eigen's Jacobi-PCG, src/Solvers.cpp:3-31, which stays the default and the
  * fallback). A graph network over the crossing graph reads each assembled

@@ -14,6 +14,7 @@
 #include "../../include/yarnsim.h"
 #include "../../fine-grained-differentiable-physics-a-yarn-level-model-for-fabrics_gb300/csrc/ys_items.cuh"
 #include "../../fine-grained-differentiable-physics-a-yarn-level-model-for-fabrics_gb300/csrc/ys_bvh.h"
+#include "../../fine-grained-differentiable-physics-a-yarn-level-model-for-fabrics_gb300/csrc/ys_zones.h"
 
 namespace {
 
@@ -431,6 +432,8 @@ namespace {
 struct HostColl {
   const ys::BvhTree* t[2];
   std::vector<ys::Kdop> box[2];
+  std::vector<uint8_t> act[2];  // BVHNode::_actived, used when masked
+  bool masked = false;
   std::vector<ys::CFace> faces[2];
   ys::CMesh m;
   double thick;
@@ -456,6 +459,7 @@ void hc_refit(HostColl& h, int which, int n) {
   }
 }
 void hc_pair(HostColl& h, int a, int wb, int b) {  // a: cloth node, b: node of tree wb
+  if (h.masked && !h.act[0][a] && !h.act[wb][b]) return;
   if (!ys::kdop_overlap(h.box[0][a], h.box[wb][b], h.thick)) return;
   const ys::BvhTree& ta = *h.t[0];
   const ys::BvhTree& tb = *h.t[wb];
@@ -473,7 +477,7 @@ void hc_pair(HostColl& h, int a, int wb, int b) {  // a: cloth node, b: node of 
 }
 void hc_self(HostColl& h, int n) {
   const ys::BvhTree& t = *h.t[0];
-  if (t.face[n] >= 0) return;
+  if (t.face[n] >= 0 || (h.masked && !h.act[0][n])) return;
   hc_self(h, t.left[n]);
   hc_self(h, t.right[n]);
   hc_pair(h, t.left[n], 0, t.right[n]);
@@ -553,6 +557,256 @@ int emu_collide(int nn, const double* x, const double* xp, int nf, const int* fv
   std::memcpy(pairs, h.pairs.data(), sizeof(int) * h.pairs.size());
   std::memcpy(impacts, imp.data(), sizeof(double) * imp.size());
   return 0;
+}
+
+// ---------------------------------------------------------------- response
+// The product's response loop (ys_zones.h) driven by host detection: the
+// trees built once from the positions before the response, refit every
+// round, traversed as the reference does with its active flags.
+namespace {
+ys::ZoneResponse g_resp;
+std::vector<double> g_resp_x0;
+double g_resp_k = 0.0;
+
+void hc_mark(HostColl& h, const ys::BvhTree& t, const uint8_t* fa, int n, bool& on) {
+  if (t.face[n] >= 0) {
+    on = fa[t.face[n]] != 0;
+  } else {
+    bool l = false, r = false;
+    hc_mark(h, t, fa, t.left[n], l);
+    hc_mark(h, t, fa, t.right[n], r);
+    on = l || r;
+  }
+  h.act[0][n] = on ? 1 : 0;
+}
+}  // namespace
+
+// x [nn][3] in/out, v [nn][3] in/out (may be null), mass [nn] (may be null);
+// info[8]: rounds, converged, changed, zones, infeasible, impacts,
+// projections, status
+int emu_respond(int nn, double* x, const double* xp, int nf, const int* fv, const int* fe, int no, const double* ox,
+                const double* oxp, int nof, const int* ofv, double thick, int ccd, const double* mass, double hstep,
+                double damp, int max_iter, double* v, long* info) {
+  HostColl h;
+  h.thick = thick;
+  h.ccd = ccd != 0;
+  h.faces[0].resize(nf);
+  for (int f = 0; f < nf; ++f)
+    for (int k = 0; k < 3; ++k) {
+      h.faces[0][f].v[k] = fv[3 * f + k];
+      h.faces[0][f].e[k][0] = fe[6 * f + 2 * k];
+      h.faces[0][f].e[k][1] = fe[6 * f + 2 * k + 1];
+    }
+  h.faces[1].resize(nof);
+  for (int f = 0; f < nof; ++f)
+    for (int k = 0; k < 3; ++k) {
+      const int b = k != 2 ? k + 1 : 0;
+      int e0 = ofv[3 * f + k], e1 = ofv[3 * f + b];
+      if (e0 > e1) std::swap(e0, e1);
+      h.faces[1][f].v[k] = -1 - ofv[3 * f + k];
+      h.faces[1][f].e[k][0] = -1 - e0;
+      h.faces[1][f].e[k][1] = -1 - e1;
+    }
+  std::vector<int> cv(nn), ov(no);
+  for (int i = 0; i < nn; ++i) cv[i] = i;
+  for (int i = 0; i < no; ++i) ov[i] = i;
+  ys::BvhTree ct = ys::bvh_build(nf, fv, nn, cv.data(), x, xp, h.ccd);
+  ys::BvhTree ot = ys::bvh_build(nof, ofv, no, ov.data(), ox, oxp, h.ccd);
+  h.t[0] = &ct;
+  h.t[1] = &ot;
+  h.box[0].resize(ct.face.size());
+  h.box[1].resize(ot.face.size());
+  h.act[0].assign(ct.face.size(), 1);
+  h.act[1].assign(ot.face.size(), 1);
+  std::vector<int> up{0};
+  while (up.size() < 8) {
+    std::vector<int> ch;
+    for (int n : up) {
+      if (ct.face[n] >= 0) ch.push_back(n);
+      else { ch.push_back(ct.left[n]); ch.push_back(ct.right[n]); }
+    }
+    if (ch.size() == up.size()) break;
+    up = ch;
+  }
+  auto detect = [&](const double* xc, const uint8_t* mask, std::vector<ys::ZImpact>& out) -> int {
+    h.m = ys::CMesh{xc, xp, ox, oxp};
+    hc_refit(h, 0, 0);
+    if (nof) hc_refit(h, 1, 0);
+    h.masked = mask != nullptr;
+    if (mask) {
+      bool on = false;
+      hc_mark(h, ct, mask, 0, on);
+      std::fill(h.act[1].begin(), h.act[1].end(), 0);
+    }
+    h.pairs.clear();
+    for (size_t n = 0; n < up.size(); ++n) {
+      hc_self(h, up[n]);
+      for (size_t q = 0; q < n; ++q) hc_pair(h, up[n], 0, up[q]);
+      if (nof) hc_pair(h, up[n], 1, 0);
+    }
+    out.clear();
+    for (size_t p = 0; p < h.pairs.size() / 3; ++p) {
+      const ys::CFace& f0 = h.faces[0][h.pairs[3 * p]];
+      const ys::CFace& f1 = h.faces[h.pairs[3 * p + 2]][h.pairs[3 * p + 1]];
+      ys::Impact im[15];
+      const int c = ys::cc_face_pair(h.m, f0, f1, thick, h.ccd, im);
+      for (int k = 0; k < c; ++k) {
+        ys::ZImpact z;
+        z.type = im[k].type;
+        z.t = im[k].t;
+        for (int q = 0; q < 4; ++q) {
+          z.node[q] = im[k].node[q];
+          z.w[q] = im[k].w[q];
+        }
+        for (int q = 0; q < 3; ++q) z.n[q] = im[k].n[q];
+        out.push_back(z);
+      }
+    }
+    return 0;
+  };
+  g_resp = ys::ZoneResponse();
+  g_resp.n_nodes = nn;
+  g_resp.n_faces = nf;
+  g_resp.faces = fv;
+  static std::vector<double> obs;  // kept for the backward
+  obs.assign(ox, ox + 3 * (size_t)no);
+  g_resp.obs_x = obs.data();
+  g_resp.thickness = thick;
+  g_resp.max_iter = max_iter;
+  g_resp_x0.assign(x, x + 3 * (size_t)nn);
+  ys::zone_respond(g_resp, x, mass, detect);
+  g_resp.faces = nullptr;
+  if (v && g_resp.changed)
+    for (size_t i = 0; i < 3 * (size_t)nn; ++i) v[i] = v[i] + (damp * (x[i] - g_resp_x0[i])) / hstep;
+  g_resp_k = damp / hstep;
+  info[0] = g_resp.rounds;
+  info[1] = g_resp.converged;
+  info[2] = g_resp.changed;
+  info[3] = g_resp.zones;
+  info[4] = g_resp.infeasible;
+  info[5] = (long)g_resp.accepted.size();
+  info[6] = (long)g_resp.tape.size();
+  info[7] = 0;
+  return 0;
+}
+
+// accepted impacts [A][15] as emu_collide's rows (the pair column holds the
+// round); multipliers of every projection are not exported
+int emu_response_impacts(double* out, long cap) {
+  if ((long)g_resp.accepted.size() > cap) return 1;
+  for (size_t i = 0; i < g_resp.accepted.size(); ++i) {
+    const ys::ZImpact& s = g_resp.accepted[i];
+    const double r[15] = {(double)s.type, (double)s.node[0], (double)s.node[1], (double)s.node[2], (double)s.node[3],
+                          s.t, s.w[0], s.w[1], s.w[2], s.w[3], s.n[0], s.n[1], s.n[2],
+                          (double)g_resp.accepted_round[i], 0.0};
+    std::memcpy(out + 15 * i, r, sizeof(r));
+  }
+  return 0;
+}
+
+// backward of the last emu_respond; gx [nn][3] in: dL/dx out, out: dL/dx in;
+// gv [nn][3] dL/dv out (may be null); gw [A][4], gn [A][3] out
+int emu_respond_backward(double* gx, const double* gv, double* gw, double* gn) {
+  const size_t n3 = 3 * (size_t)g_resp.n_nodes, na = g_resp.accepted.size();
+  std::vector<double> w(4 * std::max<size_t>(na, 1), 0.0), nn(3 * std::max<size_t>(na, 1), 0.0);
+  if (gv && g_resp.changed)
+    for (size_t i = 0; i < n3; ++i) gx[i] += g_resp_k * gv[i];
+  ys::zone_backward(g_resp, gx, w.data(), nn.data());
+  if (gv && g_resp.changed)
+    for (size_t i = 0; i < n3; ++i) gx[i] -= g_resp_k * gv[i];
+  if (na) {
+    std::memcpy(gw, w.data(), 4 * na * sizeof(double));
+    std::memcpy(gn, nn.data(), 3 * na * sizeof(double));
+  }
+  return 0;
+}
+
+// the least-distance solver alone: min |u| s.t. G u >= h (G [k][n])
+int emu_ldp(int n, int k, const double* G, const double* h, double* u, double* lam) {
+  return ys::ldp(n, k, G, h, u, lam);
+}
+
+// one detection round as the response runs it: trees built from xb (the
+// positions before the response) and x_prev, refit to x, traversed with the
+// active flags of face_active (null: all active); impacts [I][15] as
+// emu_collide's rows (pair column 0)
+int emu_detect(int nn, const double* xb, const double* x, const double* xp, int nf, const int* fv, const int* fe, int no,
+               const double* ox, const double* oxp, int nof, const int* ofv, double thick, int ccd,
+               const unsigned char* face_active, double* impacts, long icap, long* ni) {
+  std::vector<double> xc(x, x + 3 * (size_t)nn);
+  std::vector<double> xbb(xb, xb + 3 * (size_t)nn);
+  HostColl h;
+  h.thick = thick;
+  h.ccd = ccd != 0;
+  h.faces[0].resize(nf);
+  for (int f = 0; f < nf; ++f)
+    for (int k = 0; k < 3; ++k) {
+      h.faces[0][f].v[k] = fv[3 * f + k];
+      h.faces[0][f].e[k][0] = fe[6 * f + 2 * k];
+      h.faces[0][f].e[k][1] = fe[6 * f + 2 * k + 1];
+    }
+  h.faces[1].resize(nof);
+  for (int f = 0; f < nof; ++f)
+    for (int k = 0; k < 3; ++k) {
+      const int b = k != 2 ? k + 1 : 0;
+      int e0 = ofv[3 * f + k], e1 = ofv[3 * f + b];
+      if (e0 > e1) std::swap(e0, e1);
+      h.faces[1][f].v[k] = -1 - ofv[3 * f + k];
+      h.faces[1][f].e[k][0] = -1 - e0;
+      h.faces[1][f].e[k][1] = -1 - e1;
+    }
+  std::vector<int> cv(nn), ov(no);
+  for (int i = 0; i < nn; ++i) cv[i] = i;
+  for (int i = 0; i < no; ++i) ov[i] = i;
+  ys::BvhTree ct = ys::bvh_build(nf, fv, nn, cv.data(), xbb.data(), xp, h.ccd);
+  ys::BvhTree ot = ys::bvh_build(nof, ofv, no, ov.data(), ox, oxp, h.ccd);
+  h.t[0] = &ct;
+  h.t[1] = &ot;
+  h.box[0].resize(ct.face.size());
+  h.box[1].resize(ot.face.size());
+  h.act[0].assign(ct.face.size(), 1);
+  h.act[1].assign(ot.face.size(), nof ? 1 : 0);
+  h.m = ys::CMesh{xc.data(), xp, ox, oxp};
+  hc_refit(h, 0, 0);
+  if (nof) hc_refit(h, 1, 0);
+  h.masked = face_active != nullptr;
+  if (face_active) {
+    bool on = false;
+    hc_mark(h, ct, face_active, 0, on);
+    std::fill(h.act[1].begin(), h.act[1].end(), 0);
+  }
+  std::vector<int> up{0};
+  while (up.size() < 8) {
+    std::vector<int> ch;
+    for (int n : up) {
+      if (ct.face[n] >= 0) ch.push_back(n);
+      else { ch.push_back(ct.left[n]); ch.push_back(ct.right[n]); }
+    }
+    if (ch.size() == up.size()) break;
+    up = ch;
+  }
+  for (size_t n = 0; n < up.size(); ++n) {
+    hc_self(h, up[n]);
+    for (size_t q = 0; q < n; ++q) hc_pair(h, up[n], 0, up[q]);
+    if (nof) hc_pair(h, up[n], 1, 0);
+  }
+  long cnt = 0;
+  for (size_t p = 0; p < h.pairs.size() / 3; ++p) {
+    const ys::CFace& f0 = h.faces[0][h.pairs[3 * p]];
+    const ys::CFace& f1 = h.faces[h.pairs[3 * p + 2]][h.pairs[3 * p + 1]];
+    ys::Impact im[15];
+    const int c = ys::cc_face_pair(h.m, f0, f1, thick, h.ccd, im);
+    for (int k = 0; k < c; ++k, ++cnt) {
+      if (cnt >= icap) continue;
+      const ys::Impact& s = im[k];
+      const double r[15] = {(double)s.type, (double)s.node[0], (double)s.node[1], (double)s.node[2],
+                            (double)s.node[3], s.t, s.w[0], s.w[1], s.w[2], s.w[3], s.n[0], s.n[1], s.n[2],
+                            (double)p, 0.0};
+      std::memcpy(impacts + 15 * cnt, r, sizeof(r));
+    }
+  }
+  *ni = cnt;
+  return cnt > icap ? 1 : 0;
 }
 
 }  // extern "C"

@@ -1,0 +1,266 @@
+"""Impact-zone collision response (Collision::collision_response,
+src/Collision.cpp:73-156) and the backward of its projections
+(src/Collision.cpp:478-682) against the CPU restatement
+oracle/response_oracle.py.
+
+- CPU: the product's response loop and projection solver (csrc/ys_zones.h),
+  driven by the test-only emulator's detection, give the oracle's rounds,
+  zones and received impacts, its positions to 1e-12 m and velocities to
+  1e-9 m/s; every projection meets its optimality conditions to 1e-9 of the
+  thickness; the backward matches the oracle's restatement of the
+  reference's derivative to 1e-9 relative, and that derivative matches
+  central differences of the projection.
+- GPU: ys_collider_respond and ys_collider_respond_backward give the same
+  results through the C ABI.
+Parity with the reference's own numbers is unpinned: its projections run an
+augmented Lagrangian over Alglib, which is not part of the reference tree.
+"""
+import numpy as np
+import pytest
+
+import response_cases as RC
+from oracle import response_oracle as RO
+from pkg import gpu_available, ys
+
+SCENES = {
+    "drop20": lambda: RC.drop_scene(20, depth=1e-3),
+    "drop24_deep": lambda: RC.drop_scene(24, depth=1.6e-3, levels=4, seed=3),
+    "fold10": lambda: RC.fixture_scene("collide_fold10"),
+    "sphere12": lambda: RC.fixture_scene("collide_sphere12"),
+}
+DAMP = 0.1
+
+
+def _faces(s):
+    return RC.topology(s["W"], s["H"])[0]
+
+
+def _oracle(s, damp=DAMP, mass=None):
+    return RO.respond(s["x"], _faces(s), RC.emu_detector(s), s["thickness"], s["h"], damp, obs_x=s["obs_x"],
+                      v=s["v"], mass=mass)
+
+
+def _rows(accepted):
+    return np.array([[t, *nd, tt, *w, *n] for (t, nd, tt, w, n) in accepted]).reshape(-1, 13)
+
+
+def _canon(rows):
+    """Each received impact as its constraint: type, nodes in ascending order
+    and the coefficient w_k n of each (an edge-edge impact found with its
+    edges in the other roles is the same constraint; which of the two comes
+    first in time can flip with the last bit of the positions)."""
+    out = []
+    for r in rows:
+        nodes = r[1:5].astype(int)
+        coef = r[6:10, None] * r[None, 10:13]
+        o = np.argsort(nodes)
+        out.append((int(r[0]), tuple(nodes[o]), coef[o].reshape(-1)))
+    return out
+
+
+def _check_against_oracle(res, x, v, n_rounds, n_zones, received):
+    assert res["converged"]
+    assert n_rounds == res["rounds"] and n_zones == res["zones"]
+    mine, theirs = _canon(received), _canon(_rows(res["accepted"]))
+    assert len(mine) == len(theirs)
+    for a, b in zip(mine, theirs):
+        assert a[:2] == b[:2]
+        assert np.abs(a[2] - b[2]).max() <= 1e-12
+    assert np.abs(x - res["x"]).max() <= 1e-12
+    assert np.abs(v - res["v"]).max() <= 1e-9
+
+
+def test_ldp_meets_optimality_and_matches_scipy():
+    rng = np.random.default_rng(0)
+    for k, n in ((1, 3), (4, 6), (12, 9), (30, 12), (8, 30)):
+        G = rng.normal(size=(k, n))
+        h = G @ rng.normal(size=n) - rng.random(k) * (rng.random(k) < 0.5)  # feasible, some tight
+        u, lam, st = RC.emu_ldp(G, h)
+        uo, lo, ok = RO.ldp(G, h)
+        assert ok and st == 0
+        slack = G @ u - h
+        assert slack.min() >= -1e-12 and lam.min() >= 0.0
+        assert np.abs(lam * slack).max() <= 1e-12 * max(1.0, lam.max())
+        assert np.abs(u - G.T @ lam).max() <= 1e-12 * max(1.0, np.abs(u).max())
+        assert np.abs(u - uo).max() <= 1e-10 * max(1.0, np.abs(uo).max())
+    # duplicated and opposite constraints
+    G = np.array([[1.0, 0.0], [1.0, 0.0], [2.0, 0.0], [0.0, 1.0]])
+    u, lam, st = RC.emu_ldp(G, np.array([1.0, 1.0, 2.0, -1.0]))
+    assert st == 0 and np.allclose(u, [1.0, 0.0], atol=1e-14)
+    u, lam, st = RC.emu_ldp(np.array([[1.0], [-1.0]]), np.array([1.0, 1.0]))  # x >= 1 and x <= -1
+    assert st == 1 and not np.any(u)
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_emulated_response_matches_oracle(name):
+    s = SCENES[name]()
+    res = _oracle(s)
+    got = RC.emu_respond(s, damp=DAMP)
+    info = got["info"]
+    assert info[1] == 1 and info[2] == int(res["changed"]) and info[4] == 0
+    assert info[5] == len(res["accepted"]) and info[6] == len(res["tape"])
+    _check_against_oracle(res, got["x"], got["v"], info[0], info[3], got["impacts"])
+    for rec in res["tape"]:
+        assert RO.kkt_residual(rec, s["thickness"], s["obs_x"], res["accepted"], s["x"]) <= 1e-9
+    assert res["changed"] and res["rounds"] >= 1
+
+
+def test_response_separates_the_cloth_from_the_sphere():
+    s = RC.drop_scene(20, depth=1e-3)
+    got = RC.emu_respond(s)
+    r = np.linalg.norm(s["obs_x"], axis=1).max()
+    before = np.linalg.norm(s["x"], axis=1) - r
+    after = np.linalg.norm(got["x"], axis=1) - r
+    assert before.min() < -5e-4 and after.min() > -1e-4  # the polyhedron lies inside the sphere
+    moved = np.abs(got["x"] - s["x"]).max(axis=1) > 0
+    assert np.allclose(got["v"][~moved], s["v"][~moved], rtol=0, atol=0)
+
+
+def test_response_with_masses_matches_oracle():
+    s = RC.drop_scene(16, depth=1.2e-3, seed=5)
+    mass = 1.0 + np.random.default_rng(1).random(s["W"] * s["H"])
+    res = _oracle(s, mass=mass)
+    got = RC.emu_respond(s, mass=mass)
+    _check_against_oracle(res, got["x"], got["v"], got["info"][0], got["info"][3], got["impacts"])
+
+
+@pytest.mark.parametrize("name", ["drop20", "fold10"])
+def test_emulated_backward_matches_oracle(name):
+    s = SCENES[name]()
+    res = _oracle(s)
+    got = RC.emu_respond(s)
+    rng = np.random.default_rng(7)
+    gx, gv = rng.normal(size=s["x"].shape), rng.normal(size=s["x"].shape)
+    g, gw, gn = RC.emu_respond_backward(gx, gv, got["info"][5])
+    og, ogv, ogw, ogn = RO.respond_backward(res, s["obs_x"], s["thickness"], s["h"], DAMP, gx, gv)
+    _check_backward(g, gw, gn, got["impacts"], og, ogw, ogn, res)
+
+
+def _check_backward(g, gw, gn, received, og, ogw, ogn, res):
+    scale = lambda a: max(1.0, np.abs(a).max())
+    assert np.abs(g - og).max() <= 1e-9 * scale(og)
+    # weights and normals: impacts received with the same node roles (an
+    # edge-edge impact may arrive with its edges swapped, see _canon)
+    same = np.all(received[:, 1:5] == _rows(res["accepted"])[:, 1:5], axis=1)
+    assert same.mean() >= 0.9
+    assert np.abs(gw[same] - ogw[same]).max() <= 1e-9 * scale(ogw)
+    assert np.abs(gn[same] - ogn[same]).max() <= 1e-9 * scale(ogn)
+
+
+def test_projection_derivative_matches_central_differences():
+    """The reference's derivative of one projection (as restated) against
+    central differences of the projection in its anchor, weights and normals,
+    on the zones of the first round of a drop (their active sets are stable
+    under the perturbation)."""
+    s = RC.drop_scene(14, depth=1.2e-3, seed=2)
+    res = RO.respond(s["x"], _faces(s), RC.emu_detector(s), s["thickness"], s["h"], DAMP, obs_x=s["obs_x"],
+                     v=s["v"], max_iter=1)
+    rng = np.random.default_rng(3)
+    checked = 0
+    for rec in res["tape"][:6]:
+        nodes, imps = rec["nodes"], rec["imps"]
+        gz = rng.normal(size=3 * len(nodes))
+        gin, grads = RO.projection_backward(rec, res["accepted"], s["obs_x"], s["thickness"], gz)
+
+        def loss(xold_zone, acc):
+            x = np.array(s["x"], np.float64).copy()
+            xold = x.copy()
+            xold[nodes] = xold_zone.reshape(-1, 3)
+            r = RO.project(nodes, imps, acc, x, xold, s["obs_x"], s["thickness"], None)
+            return float(np.dot(gz, r["xout"]))
+        x0 = np.array(s["x"])[nodes].reshape(-1)
+        eps = 1e-8
+        fd = np.zeros_like(x0)
+        for i in range(len(x0)):
+            e = np.zeros_like(x0)
+            e[i] = eps
+            fd[i] = (loss(x0 + e, res["accepted"]) - loss(x0 - e, res["accepted"])) / (2 * eps)
+        assert np.abs(fd - gin).max() <= 1e-6 * max(1.0, np.abs(gin).max())
+        for idx in imps:
+            for part, k in (("w", 4), ("n", 3)):
+                for q in range(k):
+                    acc_p, acc_m = list(res["accepted"]), list(res["accepted"])
+                    t, nd, tt, w, n = acc_p[idx]
+                    arr = np.array(w if part == "w" else n, np.float64)
+                    ap, am = arr.copy(), arr.copy()
+                    ap[q] += eps
+                    am[q] -= eps
+                    if part == "w":
+                        acc_p[idx], acc_m[idx] = (t, nd, tt, tuple(ap), n), (t, nd, tt, tuple(am), n)
+                    else:
+                        acc_p[idx], acc_m[idx] = (t, nd, tt, w, tuple(ap)), (t, nd, tt, w, tuple(am))
+                    fdq = (loss(x0, acc_p) - loss(x0, acc_m)) / (2 * eps)
+                    an = grads[idx][0][q] if part == "w" else grads[idx][1][q]
+                    assert abs(fdq - an) <= 1e-5 * max(1.0, abs(an)), (part, q, fdq, an)
+        checked += 1
+    assert checked >= 3
+
+
+# ---------------------------------------------------------------- GPU
+def _collider(s):
+    of = s["obs_faces"]
+    c = ys.Collider(s["W"], s["H"], obstacle_faces=of if len(of) else None, n_obstacle_nodes=len(s["obs_x"]),
+                    thickness=s["thickness"])
+    ox = s["obs_x"] if len(s["obs_x"]) else None
+    c.set_positions(s["x"], s["x_prev"], ox, ox)
+    return c
+
+
+def _received_rows(imp):
+    return np.column_stack([imp["type"], imp["nodes"], imp["t"], imp["w"], imp["n"]]).astype(np.float64)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_gpu_response_matches_oracle(name):
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    s = SCENES[name]()
+    res = _oracle(s)
+    c = _collider(s)
+    out = c.respond(v=s["v"], h=s["h"], damp=DAMP)
+    assert out["changed"] == res["changed"] and out["infeasible"] == 0
+    assert out["impacts"] == len(res["accepted"]) and out["projections"] == len(res["tape"])
+    _check_against_oracle(res, out["x"], out["v"], out["rounds"], out["zones"], _received_rows(c.response_impacts()))
+    c.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["drop20", "fold10"])
+def test_gpu_backward_matches_oracle(name):
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    s = SCENES[name]()
+    res = _oracle(s)
+    c = _collider(s)
+    c.respond(v=s["v"], h=s["h"], damp=DAMP)
+    rng = np.random.default_rng(7)
+    gx, gv = rng.normal(size=s["x"].shape), rng.normal(size=s["x"].shape)
+    got = c.respond_backward(gx, gv)
+    og, ogv, ogw, ogn = RO.respond_backward(res, s["obs_x"], s["thickness"], s["h"], DAMP, gx, gv)
+    assert np.array_equal(got["v"], ogv)
+    _check_backward(got["x"], got["w"], got["n"], _received_rows(c.response_impacts()), og, ogw, ogn, res)
+    c.close()
+
+
+@pytest.mark.gpu
+def test_gpu_response_errors():
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    s = SCENES["drop20"]()
+    c = ys.Collider(s["W"], s["H"], obstacle_faces=s["obs_faces"], n_obstacle_nodes=len(s["obs_x"]))
+    with pytest.raises(ys.YarnSimError):
+        c.respond(v=s["v"])  # before set_positions
+    with pytest.raises(ys.YarnSimError):
+        c.respond_backward(np.zeros((s["W"] * s["H"], 3)))  # before a response
+    c.set_positions(s["x"], s["x_prev"], s["obs_x"], s["obs_x"])
+    with pytest.raises(ys.YarnSimError):
+        c.respond(v=s["v"], h=0.0)
+    with pytest.raises(ys.YarnSimError):
+        c.respond(v=s["v"], mass=np.zeros(s["W"] * s["H"]))
+    out = c.respond(v=s["v"], max_iter=1, check=False)  # one round cannot confirm convergence
+    assert not out["converged"] and out["rounds"] == 1
+    with pytest.raises(ys.YarnSimError):
+        c.set_positions(s["x"], s["x_prev"], s["obs_x"], s["obs_x"])
+        c.respond(v=s["v"], max_iter=1)
+    c.close()
