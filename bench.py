@@ -263,6 +263,50 @@ def precond_compare(ys, dev, repeats=6):
     return out
 
 
+def collision_compare(ys, dev, repeats=5):
+    """Collision detection and impact-zone response on the GPU collider,
+    timed end to end through the Python API with host arrays (tree build on
+    the host, uploads, kernels, downloads, the host zone solver): a W x W
+    cloth (1 mm spacing) moving 3 mm in one step onto a sphere (radius 30 mm,
+    20 480 faces) so its middle passes the top by 1 mm."""
+    import time
+    out = {}
+    for W in (64, 128):
+        ox, of = ys.collide.icosphere(0.03, 5)
+        u, v = np.meshgrid(np.arange(W), np.arange(W), indexing="xy")
+        xp = np.zeros((W * W, 3))
+        xp[:, 0] = (u.reshape(-1) - (W - 1) / 2) * 1e-3
+        xp[:, 1] = (v.reshape(-1) - (W - 1) / 2) * 1e-3
+        xp[:, 2] = 0.03 + 2e-3
+        x = xp.copy()
+        x[:, 2] -= 3e-3
+        x += np.random.default_rng(0).normal(0.0, 1e-5, x.shape)
+        vel = (x - xp) / H
+        c = ys.Collider(W, W, obstacle_faces=of, n_obstacle_nodes=len(ox), thickness=5e-4, device=dev)
+        det, resp, back = [], [], []
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            c.set_positions(x, xp, ox, ox)
+            P = c.pairs()
+            I = c.impacts()
+            det.append((time.perf_counter() - t0) * 1e3)
+            t0 = time.perf_counter()
+            c.set_positions(x, xp, ox, ox)
+            r = c.respond(v=vel, h=H, damp=0.1)
+            resp.append((time.perf_counter() - t0) * 1e3)
+            t0 = time.perf_counter()
+            c.respond_backward(np.ones_like(x), np.ones_like(x))
+            back.append((time.perf_counter() - t0) * 1e3)
+        c.close()
+        out["drop_%dx%d" % (W, W)] = {
+            "cloth_faces": 2 * (W - 1) ** 2, "obstacle_faces": int(len(of)), "pairs": int(len(P)),
+            "impacts_round0": int(len(I["t"])), "rounds": r["rounds"], "zones": r["zones"],
+            "received_impacts": int(r["impacts"]), "converged": r["converged"],
+            "detect_ms": float(np.median(det)), "respond_ms": float(np.median(resp)),
+            "respond_backward_ms": float(np.median(back))}
+    return out
+
+
 # ---------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -274,6 +318,7 @@ def main():
     ap.add_argument("--cloths", type=int, default=N_CLOTHS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precond", action="store_true", help="skip the learned-vs-Jacobi solve comparison")
+    ap.add_argument("--no-collision", action="store_true", help="skip the collision detection / response timing")
     ap.add_argument("--profile", action="store_true", help="print the per-kernel table to stderr")
     ap.add_argument("--schedule", default="auto", choices=["auto", "graph", "launch"],
                     help="auto: ys_autotune picks graph or launch-by-launch steps and the PCG check interval; "
@@ -415,6 +460,9 @@ def main():
     precond = None
     if rank == 0 and not args.no_precond:
         precond = precond_compare(ys, dev)
+    collision = None
+    if rank == 0 and not args.no_collision:
+        collision = collision_compare(ys, dev)
     hbm_peak, peak_kind = peaks()
     fp64_peak = measure_fp64_peak(torch)
 
@@ -452,6 +500,8 @@ def main():
             "clocks": clk.summary()}
     if precond is not None:
         line["precond"] = precond
+    if collision is not None:
+        line["collision"] = collision
 
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1

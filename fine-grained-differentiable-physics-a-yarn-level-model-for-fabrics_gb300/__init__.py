@@ -10,7 +10,7 @@ from .buildlib import build, LIB_PATH
 from .cloth import (PI, ClothBatch, ClothSpec, ClothState, Cloth, EigenSolver, Environment, InitPose,
                     PhysicsCloth, SimStep, Wind, WovenPattern, Yarn)
 from ._native import YarnSimError, load as load_library, library_path
-from .collide import Collider, cloth_mesh_topology
+from .collide import Collider, Collision, cloth_mesh_topology
 from .learn import (PARAM_NAMES, YarnSimNetHeter, constraint_para, invert_constraint_para, position_loss, rollout,
                     rollout_with_jacobian, two_yarn_spec)
 from .precond import LearnedPreconditioner, train as train_preconditioner, training_specs
@@ -20,7 +20,7 @@ __all__ = [
     "build", "LIB_PATH", "PI", "ClothBatch", "ClothSpec", "ClothState", "Cloth", "EigenSolver", "Environment",
     "InitPose", "PhysicsCloth", "SimStep", "Wind", "WovenPattern", "Yarn", "YarnSimError", "load_library",
     "library_path", "PARAM_NAMES", "YarnSimNetHeter", "constraint_para", "invert_constraint_para", "position_loss",
-    "rollout", "rollout_with_jacobian", "two_yarn_spec", "Collider", "cloth_mesh_topology",
+    "rollout", "rollout_with_jacobian", "two_yarn_spec", "Collider", "Collision", "cloth_mesh_topology",
     "LearnedPreconditioner", "train_preconditioner", "training_specs", "RenderCloth", "RenderType", "obj_text",
     "render_batch_cloth",
 ]

@@ -459,12 +459,33 @@ class PhysicsCloth:
         return self.batch.export_system(0)
 
 
-def SimStep(cloth: Cloth, phy: PhysicsCloth, h, ext_force=None, tol=0.0, maxiter=-1) -> bool:
+def SimStep(cloth: Cloth, phy: PhysicsCloth, h, ext_force=None, tol=0.0, maxiter=-1, collision=None) -> bool:
     """src/TrainHelper.cpp:15-54 (and 56-97 with ext_force): False if the
-    system or the new velocity is non-finite (the cloth is left unchanged)."""
+    system or the new velocity is non-finite (the cloth is left unchanged).
+    With a collide.Collision -- SimStep(cloth, phy, collision, h) as the
+    reference calls it, or collision=... -- the step is followed by
+    collision_response(0.1) and, when that moved anything, cloth.update()
+    (src/TrainHelper.cpp:99-158): positions and velocities written back, the
+    fixed positions of non-handle nodes following them."""
+    from .collide import Collision
+    if isinstance(h, Collision):
+        collision, h, ext_force = h, ext_force, None
     h = float(h)
+    before = phy.batch.get_state() if collision is not None else None
     stats = phy.batch.step(h, ext_force, tol=tol, maxiter=maxiter)
-    return bool(stats[0]["ok"])
+    if not stats[0]["ok"] or collision is None:
+        return bool(stats[0]["ok"])
+    st = phy.batch.get_state()
+    if collision.collision_response(0.1, st["LPos"], before["LPos"], st["LVel"]):
+        r = collision.last
+        fixed = np.zeros(len(st["LPos"]), bool)
+        for (u, v) in cloth.spec.handles:
+            fixed[u + v * cloth.width] = True
+        fix = st["LPosFix"].copy()
+        fix[~fixed] = r["x"][~fixed]
+        phy.batch.set_state(LPos=r["x"], LPosFix=fix, LVel=r["v"], EPos=st["EPos"], EPosBar=st["EPosBar"],
+                            EVel=st["EVel"])
+    return True
 
 
 class EigenSolver:

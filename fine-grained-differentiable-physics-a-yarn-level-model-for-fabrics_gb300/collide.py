@@ -26,6 +26,34 @@ def cloth_mesh_topology(width: int, length: int):
     return faces, edges
 
 
+def icosphere(radius: float, levels: int, center=(0.0, 0.0, 0.0)):
+    """An obstacle mesh: vertices [V, 3] and faces [F, 3] (int32) of an
+    icosahedron subdivided `levels` times onto a sphere (F = 20 * 4^levels)."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    v = [np.array(p, float) / np.linalg.norm(p) for p in
+         [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+          (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+         (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+         (8, 6, 7), (9, 8, 1)]
+    for _ in range(levels):
+        mid = {}
+
+        def m(a, b):
+            k = (min(a, b), max(a, b))
+            if k not in mid:
+                p = v[a] + v[b]
+                v.append(p / np.linalg.norm(p))
+                mid[k] = len(v) - 1
+            return mid[k]
+        nf = []
+        for (a, b, c) in f:
+            ab, bc, ca = m(a, b), m(b, c), m(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        f = nf
+    return np.asarray(center, float) + radius * np.array(v), np.array(f, np.int32)
+
+
 class Collider:
     """Broad and narrow phase for one cloth of width x length nodes
     (node u + v * width) and an optional obstacle (vertices [No, 3], faces
@@ -135,3 +163,32 @@ class Collider:
         N.check(N.load().ys_collider_respond_backward(self._h, p(gx), p(gv), p(ox), p(ov), p(gw), p(gn)),
                 "ys_collider_respond_backward")
         return dict(x=ox, v=ov, w=gw[:ni], n=gn[:ni])
+
+
+class Collision:
+    """src/Collision.h:64-131 for one Cloth (a W x L cloth mesh) against one
+    obstacle mesh (vertices [No, 3], faces [Fo, 3]; the reference's table and
+    ground meshes merged into one report the same pairs, src/Collision.cpp:
+    286-287). Obstacles are static: their positions before and after a step
+    are the same. collision_response(damp, x, x_prev, v) runs the response on
+    the GPU collider and returns whether anything moved; the result is in
+    .last (respond()'s dict)."""
+    max_iter = 100
+
+    def __init__(self, cloth, obstacle_x=None, obstacle_faces=None, thickness: float = 5e-4, h: float = 1e-3,
+                 ccd: bool = True, device: int = 0):
+        self.thickness, self.h, self.ccd = float(thickness), float(h), bool(ccd)
+        self.obs_x = np.zeros((0, 3)) if obstacle_x is None else np.ascontiguousarray(obstacle_x, np.float64)
+        of = None if obstacle_faces is None else np.ascontiguousarray(obstacle_faces, np.int32)
+        self.collider = Collider(cloth.width, cloth.length, obstacle_faces=of, n_obstacle_nodes=len(self.obs_x),
+                                 thickness=self.thickness, ccd=self.ccd, device=device)
+        self.last = None
+
+    def collision_response(self, damp_fac: float, x, x_prev, v) -> bool:
+        ox = self.obs_x if len(self.obs_x) else None
+        self.collider.set_positions(x, x_prev, ox, ox)
+        self.last = self.collider.respond(v=v, h=self.h, damp=damp_fac, max_iter=self.max_iter)
+        return self.last["changed"]
+
+    def close(self):
+        self.collider.close()

@@ -7,49 +7,28 @@ import numpy as np
 
 import goldens
 from emu_py import lib
+from pkg import ys
 
 _dp, _ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
 
 
 def topology(W, H):
-    """Cloth faces and edges in the reference's order (src/Cloth.cpp:271-294)."""
+    """The cloth mesh's faces and edges in the reference's order
+    (src/Cloth.cpp:288-293: every cell split along tl-br, unlike the yarn
+    faces)."""
     F, E = [], []
     for i in range(W - 1):
         for j in range(H - 1):
             tl = i + j * W
             tr, bl, br = tl + 1, tl + W, tl + W + 1
-            tris = ((tl, tr, br), (tl, br, bl)) if (i + j) % 2 == 0 else ((tl, tr, bl), (tr, br, bl))
-            for tri in tris:
+            for tri in ((tl, tr, br), (tl, br, bl)):
                 F.append(tri)
                 E.append([sorted((tri[a], tri[(a + 1) % 3])) for a in range(3)])
     return np.array(F, np.int32), np.array(E, np.int32)
 
 
 def icosphere(radius, levels):
-    """Vertices and faces of a subdivided icosahedron at the origin."""
-    t = (1.0 + 5 ** 0.5) / 2.0
-    v = [np.array(p, float) / np.linalg.norm(p) for p in
-         [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
-          (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]]
-    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
-         (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
-         (8, 6, 7), (9, 8, 1)]
-    for _ in range(levels):
-        mid = {}
-
-        def m(a, b):
-            k = (min(a, b), max(a, b))
-            if k not in mid:
-                p = v[a] + v[b]
-                v.append(p / np.linalg.norm(p))
-                mid[k] = len(v) - 1
-            return mid[k]
-        nf = []
-        for (a, b, c) in f:
-            ab, bc, ca = m(a, b), m(b, c), m(c, a)
-            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
-        f = nf
-    return radius * np.array(v), np.array(f, np.int32)
+    return ys.collide.icosphere(radius, levels)
 
 
 def drop_scene(W, depth=1e-3, spacing=1e-3, radius=0.02, levels=3, h=1e-3, seed=0):

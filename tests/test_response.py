@@ -264,3 +264,52 @@ def test_gpu_response_errors():
         c.set_positions(s["x"], s["x_prev"], s["obs_x"], s["obs_x"])
         c.respond(v=s["v"], max_iter=1)
     c.close()
+
+
+@pytest.mark.gpu
+def test_simstep_with_collision_matches_step_then_oracle_response():
+    """SimStep(cloth, phy, collision, h) (src/TrainHelper.cpp:99-158): the
+    step, collision_response(0.1) and cloth.update() give the plain step's
+    state followed by the oracle's response."""
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    yarn = ys.Yarn(R=1e-4, rho=1e-3, Y=1e3, B=1e-5)
+
+    def make():
+        cloth = ys.Cloth(10, 10, 0.05, 1e-3, 1e-4, [yarn], 1.0, 1000.0, 1000.0, 0.3, 1e-4, 1e4,
+                         ys.WovenPattern.Plain, ys.InitPose.Flat)
+        cloth.set_handles([(0, 0), (9, 0)])
+        phy = ys.PhysicsCloth(ys.Environment(cloth, (0.0, 0.0, 9.8), ys.Wind()))
+        st = phy.batch.get_state()
+        st["LVel"][:, 2] = 3.0  # into the sphere below
+        phy.batch.set_state(**st)
+        return cloth, phy, st
+    cloth, phy, st0 = make()
+    r = 0.02
+    ox, of = RC.icosphere(r, 3)
+    ox = ox + st0["LPos"].mean(axis=0) + np.array([0.0, 0.0, 2e-3 + r])
+    col = ys.Collision(cloth, ox, of, thickness=5e-4, h=1e-3)
+    assert ys.SimStep(cloth, phy, col, 1e-3)
+    got = phy.batch.get_state()
+    assert col.last["changed"] and col.last["converged"]
+    cloth2, phy2, _ = make()
+    assert ys.SimStep(cloth2, phy2, 1e-3)
+    plain = phy2.batch.get_state()
+    s = dict(W=10, H=10, x=plain["LPos"], x_prev=st0["LPos"], obs_x=ox, obs_faces=of, thickness=5e-4, h=1e-3,
+             v=plain["LVel"])
+    res = _oracle(s)
+    assert res["changed"]
+    assert np.abs(got["LPos"] - res["x"]).max() <= 1e-12
+    assert np.abs(got["LVel"] - res["v"]).max() <= 1e-9
+    fixed = np.zeros(100, bool)
+    fixed[[0, 9]] = True
+    assert np.array_equal(got["LPosFix"][~fixed], got["LPos"][~fixed])
+    assert np.array_equal(got["LPosFix"][fixed], plain["LPosFix"][fixed])
+    assert np.array_equal(got["EPos"], plain["EPos"])
+    col.close()
+
+
+def test_scene_topology_is_the_collider_mesh():
+    F, E = RC.topology(6, 5)
+    faces, edges = ys.cloth_mesh_topology(6, 5)
+    assert np.array_equal(F, faces) and np.array_equal(E, edges)
