@@ -27,7 +27,7 @@ EXPORTED = [
     "ys_step_graphed", "ys_autotune", "ys_gnn_param_count", "ys_gnn_create", "ys_gnn_destroy", "ys_gnn_get_params",
     "ys_gnn_set_params", "ys_gnn_train_step", "ys_gnn_loss_grad", "ys_set_preconditioner", "ys_precond_info",
     "ys_get_system_slots", "ys_tc_gemm_bf16", "ys_precond_refresh", "ys_get_normals", "ys_collider_respond",
-    "ys_collider_response_impacts", "ys_collider_respond_backward",
+    "ys_collider_response_impacts", "ys_collider_respond_backward", "ys_step_tangent_ext",
 ]
 YS_PREC_JACOBI, YS_PREC_LEARNED = 0, 1
 YS_TANGENT_EXACT, YS_TANGENT_REFERENCE = 0, 1
@@ -118,6 +118,7 @@ def load(build_if_missing: bool = True):
     L.ys_tangent_set_state.argtypes = [vp, vp, vp, vp, vp, vp, ctypes.c_int32]
     L.ys_tangent_get_state.argtypes = [vp, vp, vp, vp, vp, vp, ctypes.c_int32]
     L.ys_step_tangent.argtypes = [vp, ctypes.c_double, vp, ctypes.c_int32, vp, ctypes.c_int32, vp]
+    L.ys_step_tangent_ext.argtypes = [vp, ctypes.c_double, vp, vp, ctypes.c_int32, vp, ctypes.c_int32, vp]
     L.ys_cloth_mesh_topology.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp]
     L.ys_use_graphs.argtypes = [vp, ctypes.c_int32]
     L.ys_step_graphed.argtypes = [vp, ctypes.c_double, vp, ctypes.c_int32, vp, vp]

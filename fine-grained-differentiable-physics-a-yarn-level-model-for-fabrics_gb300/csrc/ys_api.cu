@@ -99,6 +99,7 @@ struct ys_batch {
     double *dA = nullptr, *dB = nullptr, *As = nullptr, *Bs = nullptr, *qsave = nullptr, *rt = nullptr, *dq = nullptr;
     double *dedge = nullptr, *dbend = nullptr, *dface = nullptr, *dshear = nullptr;
     double* io = nullptr;  // [kTangents][ntot][3] staging of host tangents
+    double* dext = nullptr;  // [kTangents][ntot][5] external-force tangents
   } tan;
   int nlines = 0;
   std::vector<double> line_R;  // yarn radius of each line's cloth
@@ -1009,9 +1010,24 @@ ys_status ys_tangent_get_state(ys_batch* b, double* dlpos, double* dlvel, double
 
 ys_status ys_step_tangent(ys_batch* b, double h, const double* ext_force, int32_t flags, const ys_solve_opts* opts,
                           int32_t kact, ys_cloth_stats* stats) {
+  return ys_step_tangent_ext(b, h, ext_force, nullptr, flags, opts, kact, stats);
+}
+
+ys_status ys_step_tangent_ext(ys_batch* b, double h, const double* ext_force, const double* dext_force, int32_t flags,
+                              const ys_solve_opts* opts, int32_t kact, ys_cloth_stats* stats) {
   if (!b) return fail(YS_ERR_ARG, "null handle");
   if (!b->tan.on) return fail(YS_ERR_ARG, "ys_step_tangent before ys_tangent_enable");
   if (kact < 0 || kact > KT) return fail(YS_ERR_ARG, "kact must be in [0, ys_tangent_count()]");
+  const double* d_dext = nullptr;
+  if (dext_force && kact > 0) {
+    if (!b->tan.dext) {
+      const ys_status sa = b->alloc(&b->tan.dext, (size_t)KT * 5 * b->ntot);
+      if (sa != YS_OK) return sa;
+    }
+    YS_CUDA(cudaMemcpyAsync(b->tan.dext, dext_force, sizeof(double) * 5 * b->ntot * kact,
+                            (flags & YS_ON_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, b->stream));
+    d_dext = b->tan.dext;
+  }
   ys_status s = ys_assemble(b, h, ext_force, flags);
   if (s != YS_OK) return s;
   std::vector<ys_cloth_stats> local;
@@ -1034,6 +1050,10 @@ ys_status ys_step_tangent(ys_batch* b, double h, const double* ext_force, int32_
   YS_CUDA(cudaGetLastError());
   b->run(YS_PROF_MISC, 1, [&] { ys::launch_tangent_rhs(dv, t.qsave, t.rt, kact, cs); });
   YS_CUDA(cudaGetLastError());
+  if (d_dext) {
+    b->run(YS_PROF_MISC, 1, [&] { ys::launch_tangent_ext(dv, d_dext, t.rt, h, kact, cs); });
+    YS_CUDA(cudaGetLastError());
+  }
   // tangent solves with the step's A and Jacobi diagonal: A dq_k = db_k - dA_k q
   // (exact), or A^T dq_k = db_k with M, D held constant -- the transpose of
   // the reference's backward b_bar = A^-1 q_bar (src/Solvers.cpp:33-58)

@@ -80,6 +80,8 @@ struct TangentState {
 void launch_assembly_dual(const View& v, const Records& R, const int* geom_nodes, int geom_n, cudaStream_t s);
 // rt[k][c][ntot] = db_k - dA_k q (or db_k when v.trunc) for k < kact
 void launch_tangent_rhs(const View& v, const double* q, double* rt, int kact, cudaStream_t s);
+// rt_k += h dext_k for the external force's tangents dext [kact][ntot][5]
+void launch_tangent_ext(const View& v, const double* dext, double* rt, double h, int kact, cudaStream_t s);
 // solution check, then Cloth::update of the state (solution so.x) and its
 // tangents (dq, [5][kTangents][ntot])
 void launch_update_dual(const View& v, const Blocks& b, const Solver& so, const double* dq, const TangentState& ts,

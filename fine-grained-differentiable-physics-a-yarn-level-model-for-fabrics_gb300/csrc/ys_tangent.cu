@@ -40,6 +40,18 @@ __global__ void k_tangent_rhs(View v, const double* __restrict__ q, double* __re
   }
 }
 
+// the external force's tangents in the right-hand sides: the gather adds
+// h ext to b (x, y, z of every node, u, v of interior nodes), so direction k
+// gains h dext_k; dext [kact][ntot][5]
+__global__ void k_tangent_ext(View v, const double* __restrict__ dext, double* __restrict__ rt, double h, int kact) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.ntot) return;
+  const int64_t nt = v.ntot;
+  const int nc = (v.flags[n] & YS_INTERIOR) ? 5 : 3;
+  for (int k = 0; k < kact; ++k)
+    for (int c = 0; c < nc; ++c) rt[((int64_t)k * 5 + c) * nt + n] += h * dext[((int64_t)k * nt + n) * 5 + c];
+}
+
 // Cloth::update of state and tangents for every cloth whose step succeeded
 __global__ void __launch_bounds__(kBlock) k_update_dual(View v, Blocks b, Solver so, const double* __restrict__ dq,
                                                         TangentState ts) {
@@ -62,6 +74,9 @@ void launch_assembly_dual(const View& v, const Records& R, const int* geom_nodes
 }
 void launch_tangent_rhs(const View& v, const double* q, double* rt, int kact, cudaStream_t s) {
   k_tangent_rhs<<<nblocks_t(v.ntot), kBlock, 0, s>>>(v, q, rt, kact);
+}
+void launch_tangent_ext(const View& v, const double* dext, double* rt, double h, int kact, cudaStream_t s) {
+  k_tangent_ext<<<nblocks_t(v.ntot), kBlock, 0, s>>>(v, dext, rt, h, kact);
 }
 void launch_update_dual(const View& v, const Blocks& b, const Solver& so, const double* dq, const TangentState& ts,
                         cudaStream_t s) {

@@ -207,6 +207,11 @@ ys_status ys_tangent_get_state(ys_batch *b, double *dlpos, double *dlvel, double
 /* ys_step, also advancing the first kact tangent directions (0..ys_tangent_count()). */
 ys_status ys_step_tangent(ys_batch *b, double h, const double *ext_force, int32_t flags, const ys_solve_opts *opts,
                           int32_t kact, ys_cloth_stats *stats);
+/* The same with tangents of the external force: dext_force [kact][total_nodes][5]
+ * (ext_force's layout; NULL = 0), so a control force's parameters can be
+ * tangent directions (ForceNet's lift and drag, src/TrainEmbed.h:96-163). */
+ys_status ys_step_tangent_ext(ys_batch *b, double h, const double *ext_force, const double *dext_force, int32_t flags,
+                              const ys_solve_opts *opts, int32_t kact, ys_cloth_stats *stats);
 
 /* Kernel accounting (no counterpart in the reference). Kernel classes: */
 enum {

@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "PhysicsCloth.h"
+#include "ForceNet.h"
 #include "Render.h"
 #include "CollisionUtil.h"
 
@@ -612,6 +613,113 @@ int run_collide(std::map<std::string, std::string>& kv) {
   return 0;
 }
 
+// ---------------------------------------------------------------------------
+// mode=embed: the reference's control learning step (src/TrainEmbed.h:84-176):
+// a ForceNet (src/ForceNet.h, float32, initialised by torch::manual_seed(seed))
+// reads the cloth state [LPos, EPos, LVel, EVel] flattened and predicts a
+// lift and a drag strength applied at the z / y DOF (first * width + second)
+// of each listed pair; the loop of train_embed with its `if (s = 5)` (an
+// assignment: after the first step the loop jumps to s = 6 and later steps
+// run without force), SimStep with the external force
+// (src/TrainHelper.cpp:56-97, restated like run_grad's step), the loss
+// |mean(goal) - mean(LPos)|^2 and loss.backward(). Writes the loss, the
+// predicted forces, every ForceNet parameter and its gradient, and the
+// final positions. One homogeneous cloth (no handles), upright, plain.
+int run_embed(std::map<std::string, std::string>& kv) {
+  const int W = static_cast<int>(get_d(kv, "width", 5));
+  const int Lh = static_cast<int>(get_d(kv, "length", 5));
+  const double height = get_d(kv, "height", 5.0);
+  const double L = get_d(kv, "L", 1e-3);
+  const double R = get_d(kv, "R", 1e-4);
+  const int sample = static_cast<int>(get_d(kv, "sample", 10));
+  ref_cg_set_options(get_d(kv, "cg_tol", DBL_EPSILON), static_cast<long>(get_d(kv, "cg_maxiter", -1)));
+  torch::manual_seed(static_cast<uint64_t>(get_d(kv, "seed", 0)));
+  std::vector<double> G = parse_list(get_s(kv, "G", "0,0,9.8"));
+  std::vector<double> wv = parse_list(get_s(kv, "wind_vel", "0,0,0"));
+  std::vector<double> hl = parse_list(get_s(kv, "force_at", "0,0,4,0,0,4,4,4"));
+  auto T1 = [&](const std::string& k, double d) { return torch::tensor({get_d(kv, k, d)}, opts); };
+  const int N = W * Lh;
+  const int force_size = 3 * N + 2 * (W - 2) * (Lh - 2);
+  Tensor lift_at = torch::zeros({force_size, 1}, opts), drag_at = torch::zeros({force_size, 1}, opts);
+  for (size_t i = 0; i + 1 < hl.size(); i += 2) {
+    const int first = static_cast<int>(hl[i]), second = static_cast<int>(hl[i + 1]);
+    lift_at.index_put_({(first * W + second) * 3 + 2, 0}, 1.0);
+    drag_at.index_put_({(first * W + second) * 3 + 1, 0}, 1.0);
+  }
+  const Tensor zero_force = torch::zeros({force_size, 1}, opts);
+  std::vector<double> goal(3 * N);
+  {
+    std::ifstream f(kv["goal"], std::ios::binary);
+    f.read(reinterpret_cast<char*>(goal.data()), goal.size() * sizeof(double));
+  }
+  const Tensor goal_t = torch::from_blob(goal.data(), {N, 3, 1}, opts).clone();
+  ForceNet net{10 * N, 2};
+  std::vector<Yarn> yarns{Yarn{R, T1("rho", 1e-3), T1("Y", 1e3), T1("B", 1e-5)}};
+  Cloth cloth(W, Lh, height, L, R, yarns, T1("kc", 1.0), T1("kf", 1000.0), T1("df", 1000.0), T1("mu", 0.3),
+              T1("S", 1e-4), T1("handle_stiffness", 1e4), WovenPattern::Plain, InitPose::Upright);
+  Wind wind{torch::tensor({wv[0], wv[1], wv[2]}, opts).view({3, 1}), T1("wind_density", 0.0), T1("wind_drag", 0.0)};
+  Environment env{&cloth, torch::tensor({G[0], G[1], G[2]}, opts).view({3, 1}), wind};
+  PhysicsCloth phy{&env};
+  phy.InitMV();
+  const Tensor h = torch::tensor({get_d(kv, "h", 1e-3)}, opts);
+  auto step = [&](const Tensor& ext) {
+    phy.FillMV();
+    const Tensor M = phy.get_SpaM();
+    const Tensor Kx = phy.get_SpaFPos();
+    const Tensor Dv = phy.get_SpaFVel();
+    const Tensor A = M - Kx * torch::pow(h, 2) - Dv * h;
+    const Tensor b = h * (phy.get_SpaF() + ext - torch::mm(Dv.transpose(0, 1), phy.get_SpaVel())) +
+                     torch::mm(M, phy.get_SpaVel());
+    Tensor new_vel = EigenSolver::apply(A, b);
+    if (!torch::isfinite(new_vel).all().item<bool>()) return false;
+    cloth.update(new_vel, phy.F_E_is_Slides[0], h);
+    phy.ResetMV();
+    return true;
+  };
+  ClothState bkup = cloth.get_ClothState();
+  bool ok = true;
+  std::vector<double> forces;
+  for (int s = 0; s < sample - 1; ++s) {
+    if (s <= 5) {
+      ClothState cs = cloth.get_ClothState();
+      Tensor in = torch::cat({cs.LPos.flatten(), cs.EPos.flatten(), cs.LVel.flatten(), cs.EVel.flatten()})
+                      .unsqueeze(0).to(torch::kFloat32);
+      Tensor pred = net->forward(in);
+      Tensor ext = lift_at * pred.index({0, 0}) + drag_at * pred.index({0, 1});
+      forces.push_back(pred.index({0, 0}).item<double>());
+      forces.push_back(pred.index({0, 1}).item<double>());
+      ok = step(ext);
+      s = 5;  // the reference's `if (s = force_stop_frame)`
+      bkup = cloth.get_ClothState();
+      if (!ok) break;
+    } else {
+      ok = step(zero_force);
+      if (!ok) break;
+    }
+  }
+  ClothState fin = ok ? cloth.get_ClothState() : bkup;
+  Tensor dc = (torch::mean(goal_t, 0) - torch::mean(fin.LPos, 0)).squeeze();
+  Tensor loss = torch::matmul(dc, dc);
+  loss.backward();
+  Writer w(get_s(kv, "out", "ref_out.bin"));
+  double lv = loss.item<double>();
+  w.put("loss", {1}, &lv);
+  w.put("forces", {static_cast<int>(forces.size())}, forces.data());
+  for (auto& p : net->named_parameters()) {
+    Tensor v = p.value().detach().to(torch::kFloat64).contiguous();
+    std::vector<long> shape(v.sizes().begin(), v.sizes().end());
+    std::vector<double> vals(v.data_ptr<double>(), v.data_ptr<double>() + v.numel());
+    w.put("param." + p.key(), shape, vals.data());
+    Tensor g = p.value().grad().defined() ? p.value().grad().to(torch::kFloat64).contiguous() : torch::zeros_like(v);
+    std::vector<double> gv(g.data_ptr<double>(), g.data_ptr<double>() + g.numel());
+    w.put("grad." + p.key(), shape, gv.data());
+  }
+  w.put_tensor("final.LPos", fin.LPos.detach().reshape({N, 3}));
+  double st = ok ? 0.0 : 1.0;
+  w.put("status", {1}, &st);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) {
     std::fprintf(stderr, "usage: %s config\n", argv[0]);
@@ -622,6 +730,7 @@ int main(int argc, char** argv) {
   if (get_s(kv, "mode", "") == "grad") return run_grad(kv);
   if (get_s(kv, "mode", "") == "vjp") return run_vjp(kv);
   if (get_s(kv, "mode", "") == "collide") return run_collide(kv);
+  if (get_s(kv, "mode", "") == "embed") return run_embed(kv);
 
   const int W = static_cast<int>(get_d(kv, "width", 5));
   const int Lh = static_cast<int>(get_d(kv, "length", 5));
