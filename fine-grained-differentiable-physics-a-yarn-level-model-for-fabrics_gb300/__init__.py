@@ -16,6 +16,7 @@ from .learn import (PARAM_NAMES, YarnSimNetHeter, constraint_para, invert_constr
 from .precond import LearnedPreconditioner, train as train_preconditioner, training_specs
 from .render import RenderCloth, RenderType, obj_text, render_batch_cloth
 from . import h5
+from . import control
 
 __all__ = [
     "build", "LIB_PATH", "PI", "ClothBatch", "ClothSpec", "ClothState", "Cloth", "EigenSolver", "Environment",

@@ -348,13 +348,25 @@ class ClothBatch:
                 "ys_tangent_get_state")
         return out
 
-    def step_tangent(self, h, ext_force=None, tol=0.0, maxiter=-1, check_every=0, kact=None):
-        """step() that also advances the first kact tangent directions."""
+    def step_tangent(self, h, ext_force=None, tol=0.0, maxiter=-1, check_every=0, kact=None, dext_force=None):
+        """step() that also advances the first kact tangent directions;
+        dext_force [K, total_nodes, 5] (numpy) are the external force's
+        tangents (ys_step_tangent_ext)."""
         kact = self.n_tangents if kact is None else int(kact)
         p, f = _ptr(ext_force)
         st = (N.ClothStats * self.n_cloths)()
-        r = N.load().ys_step_tangent(self._h, h, ctypes.c_void_p(p) if p else None, f,
-                                     ctypes.byref(self._opts(tol, maxiter, check_every)), kact, st)
+        if dext_force is not None:
+            if f:
+                raise ValueError("dext_force with a device ext_force: pass both on the host")
+            d = np.ascontiguousarray(dext_force, np.float64)
+            if d.shape != (self.n_tangents, self.total_nodes, 5):
+                raise ValueError("dext_force must be [%d, %d, 5]" % (self.n_tangents, self.total_nodes))
+            r = N.load().ys_step_tangent_ext(self._h, h, ctypes.c_void_p(p) if p else None,
+                                             ctypes.c_void_p(d.ctypes.data), 0,
+                                             ctypes.byref(self._opts(tol, maxiter, check_every)), kact, st)
+        else:
+            r = N.load().ys_step_tangent(self._h, h, ctypes.c_void_p(p) if p else None, f,
+                                         ctypes.byref(self._opts(tol, maxiter, check_every)), kact, st)
         if r not in (N.YS_OK, N.YS_ERR_NONFINITE, N.YS_ERR_MAXITER):
             N.check(r, "ys_step_tangent")
         return self._stats(st)
