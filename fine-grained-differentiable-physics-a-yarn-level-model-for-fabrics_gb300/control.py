@@ -51,11 +51,12 @@ def ForceNet(n_in: int, n_out: int = 2):
     return _ForceNet()
 
 
-def state_input(st: Dict[str, np.ndarray], nodes: slice):
-    """[1, 10 N] float32: LPos, EPos, LVel, EVel of the cloth's nodes, flattened."""
+def state_input(st: Dict[str, np.ndarray], nodes: slice, dtype=None):
+    """[1, 10 N] (float32 as the reference casts it, unless dtype is given):
+    LPos, EPos, LVel, EVel of the cloth's nodes, flattened."""
     torch = _torch()
     x = np.concatenate([st[k][nodes].reshape(-1) for k in ("LPos", "EPos", "LVel", "EVel")])
-    return torch.from_numpy(x).to(torch.float32).unsqueeze(0)
+    return torch.from_numpy(x).to(torch.float32 if dtype is None else dtype).unsqueeze(0)
 
 
 def _tangent_input(tg: Dict[str, np.ndarray], k: int, nodes: slice) -> np.ndarray:
@@ -69,12 +70,15 @@ def force_nodes(width: int, force_at: Sequence) -> List[int]:
 
 def embed_step(net, spec: ClothSpec, goal_lpos: np.ndarray, sample: int, h: float = 1e-3,
                force_at: Sequence = ((0, 0), (4, 0), (0, 4), (4, 4)), loop: str = "reference",
-               tangent_mode: int = 1, tol: float = 0.0, maxiter: int = -1, device: int = 0) -> Dict:
+               tangent_mode: int = 1, tol: float = 0.0, maxiter: int = -1, device: int = 0,
+               input_dtype=None) -> Dict:
     """One training evaluation of train_embed from the spec's initial state:
     returns dict(loss, forces [F, 2], grads {parameter name: array}, final
     LPos, dloss_dforces [F, 2]) and leaves the gradients in the network's
     .grad (accumulated, as loss.backward() does). tangent_mode 1 carries the
-    reference's EigenSolver backward (its autograd), 0 the exact derivative."""
+    reference's EigenSolver backward (its autograd), 0 the exact derivative.
+    input_dtype: the network input's dtype (float32, the reference's cast,
+    by default)."""
     torch = _torch()
     if loop not in ("reference", "intended"):
         raise ValueError("loop must be 'reference' or 'intended'")
@@ -102,7 +106,7 @@ def embed_step(net, spec: ClothSpec, goal_lpos: np.ndarray, sample: int, h: floa
     for forced in schedule:
         st = batch.get_state()
         if forced:
-            x_in = state_input(st, sl)
+            x_in = state_input(st, sl, input_dtype)
             pred = net(x_in)
             inputs.append(x_in)
             preds.append(pred)

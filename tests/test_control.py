@@ -101,7 +101,8 @@ def test_force_gradient_matches_central_differences(loop):
         net = Const(f)
         with torch.no_grad():
             net.w.copy_(torch.from_numpy(w0))
-        return ys.control.embed_step(net, spec, g["goal"], 9, loop=loop, tangent_mode=ys._native.YS_TANGENT_EXACT), net
+        return ys.control.embed_step(net, spec, g["goal"], 9, loop=loop, tangent_mode=ys._native.YS_TANGENT_EXACT,
+                                     input_dtype=torch.float64), net
     out, net = run(f0)
     an = net.f.grad.numpy()[0]
     eps = 1e-6
