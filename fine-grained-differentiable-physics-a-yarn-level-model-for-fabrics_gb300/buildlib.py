@@ -20,6 +20,11 @@ HEADERS = ["ys_common.cuh", "ys_dual.cuh", "ys_physics.cuh", "ys_items.cuh", "ys
            "ys_gnn.cuh", "ys_tc.cuh", "ys_zones.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC"]
+# the collision tests keep IEEE products and sums separate, as the reference's
+# CPU arithmetic does: a contracted cross product of two equal vectors is its
+# rounding error instead of zero, and the CCD cubic of a static face against a
+# moving vertex (exactly linear) then grows spurious roots
+PER_FILE = {"ys_collide.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -33,7 +38,8 @@ def _stale() -> bool:
     if not os.path.exists(LIB_PATH):
         return True
     t = os.path.getmtime(LIB_PATH)
-    deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS] + [os.path.join(ROOT, "include", "yarnsim.h")]
+    deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS] + [os.path.join(ROOT, "include", "yarnsim.h"),
+                                                                 os.path.abspath(__file__)]
     return any(os.path.getmtime(d) > t for d in deps)
 
 
@@ -46,7 +52,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(LIB_DIR, src.replace(".cu", ".o"))
-        cmd = [cc] + ARCH + FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [cc] + ARCH + FLAGS + PER_FILE.get(src, []) + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s" % (src, r.stderr[-4000:]))
