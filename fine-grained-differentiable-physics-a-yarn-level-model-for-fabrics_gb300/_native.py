@@ -154,7 +154,7 @@ def load(build_if_missing: bool = True):
     L.ys_collider_respond.argtypes = [vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, vp, vp,
                                       ctypes.POINTER(ResponseInfo)]
     L.ys_collider_response_impacts.argtypes = [vp, vp, ctypes.c_int64]
-    L.ys_collider_respond_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.ys_collider_respond_backward.argtypes = [vp, vp, vp, ctypes.c_int32, vp, vp, vp, vp, vp]
     for name in EXPORTED:
         if name not in ("ys_batch_destroy", "ys_last_error", "ys_cloth_node_offset", "ys_cloth_dim",
                         "ys_tangent_count", "ys_collider_destroy", "ys_gnn_destroy", "ys_gnn_param_count"):

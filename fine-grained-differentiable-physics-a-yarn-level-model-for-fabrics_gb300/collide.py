@@ -150,20 +150,24 @@ class Collider:
         return dict(type=a["type"].copy(), nodes=a["nodes"].copy(), t=a["t"].copy(), w=a["w"].copy(),
                     n=a["n"].copy(), round=a["pair"].copy())
 
-    def respond_backward(self, dl_dx=None, dl_dv=None) -> dict:
+    def respond_backward(self, dl_dx=None, dl_dv=None, impacts: bool = False, exact_root: bool = False) -> dict:
         """Backward of the last respond(): gradients of x and v before it and
-        of every received impact's weights [I, 4] and normal [I, 3]."""
+        of every received impact's weights [I, 4] and normal [I, 3]. With
+        impacts=True those are carried on into the positions the impacts were
+        computed from (x and x_prev, the reference's full autograd; the cubic
+        root's derivative as the reference's CubicSolver backward unless
+        exact_root)."""
         n3 = (self.n_nodes, 3)
         gx = None if dl_dx is None else np.ascontiguousarray(dl_dx, np.float64).reshape(n3)
         gv = None if dl_dv is None else np.ascontiguousarray(dl_dv, np.float64).reshape(n3)
         ni = self._n_received
-        ox, ov = np.zeros(n3), np.zeros(n3)
+        ox, ov, op = np.zeros(n3), np.zeros(n3), np.zeros(n3)
         gw, gn = np.zeros((max(ni, 1), 4)), np.zeros((max(ni, 1), 3))
+        flags = (1 if impacts else 0) | (2 if exact_root else 0)
         p = lambda a: ctypes.c_void_p(a.ctypes.data) if a is not None else None
-        N.check(N.load().ys_collider_respond_backward(self._h, p(gx), p(gv), p(ox), p(ov), p(gw), p(gn)),
+        N.check(N.load().ys_collider_respond_backward(self._h, p(gx), p(gv), flags, p(ox), p(ov), p(op), p(gw), p(gn)),
                 "ys_collider_respond_backward")
-        return dict(x=ox, v=ov, w=gw[:ni], n=gn[:ni])
-
+        return dict(x=ox, v=ov, x_prev=op, w=gw[:ni], n=gn[:ni])
 
 class Collision:
     """src/Collision.h:64-131 for one Cloth (a W x L cloth mesh) against one

@@ -580,6 +580,8 @@ ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h,
   R.n_faces = c->n_faces;
   R.faces = c->fv.data();
   R.obs_x = c->hox.data();
+  R.xprev = c->hxp.data();
+  R.obs_xprev = c->hoxp.data();
   R.thickness = c->thickness;
   R.max_iter = max_iter;
   c->resp_x0 = c->hx;
@@ -681,18 +683,21 @@ ys_status ys_collider_response_impacts(ys_collider* c, ys_impact* impacts, int64
   return YS_OK;
 }
 
-ys_status ys_collider_respond_backward(ys_collider* c, const double* dl_dx, const double* dl_dv, double* dl_dx_in,
-                                       double* dl_dv_in, double* dl_dw, double* dl_dn) {
+ys_status ys_collider_respond_backward(ys_collider* c, const double* dl_dx, const double* dl_dv, int32_t flags,
+                                       double* dl_dx_in, double* dl_dv_in, double* dl_dx_prev, double* dl_dw,
+                                       double* dl_dn) {
   if (!c || !c->have_response) return ys_internal_fail(YS_ERR_ARG, "no collision response yet");
   if (!dl_dx_in) return ys_internal_fail(YS_ERR_ARG, "dl_dx_in is required");
+  if (flags & ~3) return ys_internal_fail(YS_ERR_ARG, "unknown response gradient flags");
   const ys::ZoneResponse& R = c->resp;
   const size_t n3 = 3 * (size_t)c->n_nodes, na = R.accepted.size();
-  std::vector<double> g(n3, 0.0), gw(4 * std::max<size_t>(na, 1), 0.0), gn(3 * std::max<size_t>(na, 1), 0.0);
+  std::vector<double> g(n3, 0.0), gp(n3, 0.0), gw(4 * std::max<size_t>(na, 1), 0.0),
+      gn(3 * std::max<size_t>(na, 1), 0.0);
   if (dl_dx) std::memcpy(g.data(), dl_dx, n3 * sizeof(double));
   const double k = c->resp_damp / c->resp_h;
   if (dl_dv && R.changed)
     for (size_t i = 0; i < n3; ++i) g[i] += k * dl_dv[i];
-  ys::zone_backward(R, g.data(), gw.data(), gn.data());
+  ys::zone_backward(R, g.data(), gw.data(), gn.data(), flags, gp.data());
   if (dl_dv && R.changed)
     for (size_t i = 0; i < n3; ++i) g[i] -= k * dl_dv[i];
   std::memcpy(dl_dx_in, g.data(), n3 * sizeof(double));
@@ -700,6 +705,7 @@ ys_status ys_collider_respond_backward(ys_collider* c, const double* dl_dx, cons
     if (dl_dv) std::memcpy(dl_dv_in, dl_dv, n3 * sizeof(double));
     else std::memset(dl_dv_in, 0, n3 * sizeof(double));
   }
+  if (dl_dx_prev) std::memcpy(dl_dx_prev, gp.data(), n3 * sizeof(double));
   if (dl_dw && na) std::memcpy(dl_dw, gw.data(), 4 * na * sizeof(double));
   if (dl_dn && na) std::memcpy(dl_dn, gn.data(), 3 * na * sizeof(double));
   return YS_OK;

@@ -329,6 +329,7 @@ inline int ldp(int n, int k, const double* G, const double* h, double* u, double
 }
 
 struct ZoneRecord {  // one zone projection
+  int round = 0;
   std::vector<int> nodes;    // the zone's cloth nodes, zone order
   std::vector<int> imps;     // its constraints: indices of accepted impacts
   std::vector<double> a;     // objective weight inv_m m of each node
@@ -342,11 +343,15 @@ struct ZoneResponse {
   int n_nodes = 0, n_faces = 0;
   const int* faces = nullptr;     // cloth faces [F][3]
   const double* obs_x = nullptr;  // obstacle node positions [No][3]
+  const double* xprev = nullptr;  // cloth and obstacle positions at the start of the step
+  const double* obs_xprev = nullptr;
   double thickness = 0.0;
   int max_iter = 100;
   // results
   std::vector<ZImpact> accepted;  // every impact a zone received, in order
   std::vector<int> accepted_round;
+  std::vector<double> accepted_x;  // [accepted][4][3] its nodes' positions when it was found
+  std::vector<double> accepted_xp;  // [accepted][4][3] and at the start of the step
   std::vector<ZoneRecord> tape;   // every projection, in order
   int rounds = 0, converged = 0, changed = 0, zones = 0, infeasible = 0;
 };
@@ -359,9 +364,10 @@ inline double node_x(const double* x, const double* obs_x, int nd, int c) {
 
 // projects one zone in place (x: all cloth positions), records it
 inline void project(ZoneResponse& R, const std::vector<int>& nodes, const std::vector<int>& imps, const double* mass,
-                    const double* xold, double* x, std::vector<int>& local) {
+                    const double* xold, double* x, std::vector<int>& local, int round) {
   const int m = (int)nodes.size(), nv = 3 * m, k = (int)imps.size();
   ZoneRecord rec;
+  rec.round = round;
   rec.nodes = nodes;
   rec.imps = imps;
   double inv_m = 0.0;
@@ -419,6 +425,8 @@ int zone_respond(ZoneResponse& R, double* x, const double* mass, Detect&& detect
   const int n = R.n_nodes;
   R.accepted.clear();
   R.accepted_round.clear();
+  R.accepted_x.clear();
+  R.accepted_xp.clear();
   R.tape.clear();
   R.rounds = R.converged = R.changed = R.zones = R.infeasible = 0;
   std::vector<double> xold(x, x + 3 * (size_t)n);
@@ -489,6 +497,11 @@ int zone_respond(ZoneResponse& R, double* x, const double* mass, Detect&& detect
       const int id = (int)R.accepted.size();
       R.accepted.push_back(im);
       R.accepted_round.push_back(iter);
+      for (int q = 0; q < 4; ++q)
+        for (int c = 0; c < 3; ++c) {
+          R.accepted_x.push_back(zone_detail::node_x(x, R.obs_x, im.node[q], c));
+          R.accepted_xp.push_back(R.xprev ? zone_detail::node_x(R.xprev, R.obs_xprev, im.node[q], c) : 0.0);
+        }
       const int z0 = find_or_create(im.node[0] >= 0 ? im.node[0] : im.node[3]);
       for (int q = 0; q < 4; ++q) {
         if (im.node[q] < 0) continue;
@@ -507,7 +520,7 @@ int zone_respond(ZoneResponse& R, double* x, const double* mass, Detect&& detect
     for (int z : order)
       if (zs[z].active) {
         R.changed = 1;
-        zone_detail::project(R, zs[z].nodes, zs[z].imps, mass, xold.data(), x, local);
+        zone_detail::project(R, zs[z].nodes, zs[z].imps, mass, xold.data(), x, local, iter);
       }
   }
   R.rounds = iter;
@@ -516,16 +529,201 @@ int zone_respond(ZoneResponse& R, double* x, const double* mass, Detect&& detect
   return 0;
 }
 
+namespace zone_detail {
+
+// forward-mode number with the 24 directions of one impact's inputs: the
+// four nodes' positions at the end (3 k + c) and start (12 + 3 k + c) of the
+// step
+struct D24 {
+  double v;
+  double d[24];
+};
+inline D24 dc(double v) {
+  D24 r;
+  r.v = v;
+  for (double& x : r.d) x = 0.0;
+  return r;
+}
+inline D24 operator+(const D24& a, const D24& b) {
+  D24 r;
+  r.v = a.v + b.v;
+  for (int i = 0; i < 24; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+inline D24 operator-(const D24& a, const D24& b) {
+  D24 r;
+  r.v = a.v - b.v;
+  for (int i = 0; i < 24; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+inline D24 operator-(const D24& a) {
+  D24 r;
+  r.v = -a.v;
+  for (int i = 0; i < 24; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+inline D24 operator*(const D24& a, const D24& b) {
+  D24 r;
+  r.v = a.v * b.v;
+  for (int i = 0; i < 24; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  return r;
+}
+inline D24 operator/(const D24& a, const D24& b) {
+  D24 r;
+  r.v = a.v / b.v;
+  for (int i = 0; i < 24; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) / b.v;
+  return r;
+}
+inline D24 dsqrt(const D24& a) {
+  D24 r;
+  r.v = std::sqrt(a.v);
+  for (int i = 0; i < 24; ++i) r.d[i] = a.d[i] / (2.0 * r.v);
+  return r;
+}
+inline void dcross(const D24* a, const D24* b, D24* o) {
+  o[0] = a[1] * b[2] - a[2] * b[1];
+  o[1] = a[2] * b[0] - a[0] * b[2];
+  o[2] = a[0] * b[1] - a[1] * b[0];
+}
+inline D24 ddot(const D24* a, const D24* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+inline D24 dtriple(const D24* a, const D24* b, const D24* c) {
+  D24 t[3];
+  dcross(b, c, t);
+  return ddot(a, t);
+}
+
+}  // namespace zone_detail
+
+// d(w, n) / d(positions) of one impact of type `type` found at time t with
+// node positions x [4][3] (end of step) and xp [4][3] (start): J [7][24], rows
+// w0..w3, n0..n2, columns x of node k (3 k + c) then xp (12 + 3 k + c). The
+// computation is collision_test's (src/Collision.cpp:376-436: the cubic's
+// root t, the positions at t, sub_signed_vf / ee_distance, the orientation
+// of n), differentiated forward. cubic_sign -1 takes the root's exact
+// derivative dt = -(t^3 da3 + t^2 da2 + t da1 + da0) / p'(t); +1 takes the
+// reference's CubicSolver backward (src/Solvers.cpp:172-178), which drops
+// that minus sign. Returns false where the reference would have found no
+// impact (degenerate normal).
+inline bool impact_jacobian(int type, const double* x, const double* xp, double troot, int cubic_sign,
+                            double J[7][24]) {
+  using namespace zone_detail;
+  D24 X[4][3], XP[4][3];
+  for (int k = 0; k < 4; ++k)
+    for (int c = 0; c < 3; ++c) {
+      X[k][c] = dc(x[3 * k + c]);
+      X[k][c].d[3 * k + c] = 1.0;
+      XP[k][c] = dc(xp[3 * k + c]);
+      XP[k][c].d[12 + 3 * k + c] = 1.0;
+    }
+  D24 x1[3], x2[3], x3[3], v0[3], v1[3], v2[3], v3[3];
+  for (int i = 0; i < 3; ++i) {
+    v0[i] = X[0][i] - XP[0][i];
+    x1[i] = XP[1][i] - XP[0][i];
+    x2[i] = XP[2][i] - XP[0][i];
+    x3[i] = XP[3][i] - XP[0][i];
+    v1[i] = X[1][i] - XP[1][i] - v0[i];
+    v2[i] = X[2][i] - XP[2][i] - v0[i];
+    v3[i] = X[3][i] - XP[3][i] - v0[i];
+  }
+  const D24 a0 = dtriple(x1, x2, x3);
+  const D24 a1 = dtriple(v1, x2, x3) + dtriple(x1, v2, x3) + dtriple(x1, x2, v3);
+  const D24 a2 = dtriple(x1, v2, v3) + dtriple(v1, x2, v3) + dtriple(v1, v2, x3);
+  const D24 a3 = dtriple(v1, v2, v3);
+  const double t = troot;
+  const double dp = (3.0 * a3.v * t + 2.0 * a2.v) * t + a1.v;
+  D24 T = dc(t);
+  for (int i = 0; i < 24; ++i)
+    T.d[i] = cubic_sign * (((a3.d[i] * t + a2.d[i]) * t + a1.d[i]) * t + a0.d[i]) / dp;
+  D24 b1[3], b2[3], b3[3];
+  for (int i = 0; i < 3; ++i) {
+    b1[i] = x1[i] + T * v1[i];
+    b2[i] = x2[i] + T * v2[i];
+    b3[i] = x3[i] + T * v3[i];
+  }
+  D24 n[3], w[4];
+  if (type == 0) {  // sub_signed_vf_distance(b1, b2, b3)
+    D24 a[3], b[3], tt[3];
+    for (int i = 0; i < 3; ++i) {
+      a[i] = b2[i] - b1[i];
+      b[i] = b3[i] - b1[i];
+    }
+    dcross(a, b, n);
+    const D24 l = dsqrt(ddot(n, n));
+    if (!(l.v > 0.0)) return false;
+    for (int i = 0; i < 3; ++i) n[i] = n[i] / l;
+    dcross(b3, n, tt);
+    const D24 c0 = ddot(b2, tt);
+    dcross(b1, n, tt);
+    const D24 c1 = ddot(b3, tt);
+    dcross(b2, n, tt);
+    const D24 c2 = ddot(b1, tt);
+    const D24 sum = dc(1.0) / (c0 + c1 + c2);
+    w[0] = dc(1.0);
+    w[1] = -(c0 * sum);
+    w[2] = -(c1 * sum);
+    w[3] = -(c2 * sum);
+  } else {  // sub_signed_ee_distance(b1, b2, b3, b2 - b1, b3 - b1, b3 - b2)
+    D24 x1mx0[3], y0mx0[3], y1mx0[3], y0mx1[3], y1mx1[3], y1my0[3], tt[3];
+    for (int i = 0; i < 3; ++i) {
+      x1mx0[i] = b1[i];
+      y0mx0[i] = b2[i];
+      y1mx0[i] = b3[i];
+      y0mx1[i] = b2[i] - b1[i];
+      y1mx1[i] = b3[i] - b1[i];
+      y1my0[i] = b3[i] - b2[i];
+    }
+    dcross(x1mx0, y1my0, n);
+    const D24 l = dsqrt(ddot(n, n));
+    if (!(l.v > 0.0)) return false;
+    for (int i = 0; i < 3; ++i) n[i] = n[i] / l;
+    dcross(y0mx1, n, tt);
+    const D24 e0 = ddot(y1mx1, tt);
+    dcross(y1mx0, n, tt);
+    const D24 e1 = ddot(y0mx0, tt);
+    dcross(y1mx0, n, tt);
+    const D24 f0 = ddot(y1mx1, tt);
+    dcross(y0mx1, n, tt);
+    const D24 f1 = ddot(y0mx0, tt);
+    const D24 suma = dc(1.0) / (e0 + e1), sumb = dc(1.0) / (f0 + f1);
+    w[0] = e0 * suma;
+    w[1] = e1 * suma;
+    w[2] = -(f0 * sumb);
+    w[3] = -(f1 * sumb);
+  }
+  double rv[3];
+  for (int i = 0; i < 3; ++i) rv[i] = w[1].v * v1[i].v + w[2].v * v2[i].v + w[3].v * v3[i].v;
+  const double flip = (n[0].v * rv[0] + n[1].v * rv[1] + n[2].v * rv[2]) > 0.0 ? -1.0 : 1.0;
+  for (int i = 0; i < 24; ++i) {
+    for (int q = 0; q < 4; ++q) J[q][i] = w[q].d[i];
+    for (int c = 0; c < 3; ++c) J[4 + c][i] = flip * n[c].d[i];
+  }
+  return true;
+}
+
 // Backward of the projections: g [n][3] in: dL/dx after the response, out:
 // dL/dx before it (through the projections only); gw [accepted][4] and
 // gn [accepted][3] receive dL/dw and dL/dn of every accepted impact
 // (accumulated; zero them first).
-inline void zone_backward(const ZoneResponse& R, double* g, double* gw, double* gn) {
+//
+// flags & 1 also carries the impacts' weight and normal gradients into the
+// positions they were computed from, as the reference's autograd does through
+// collision_test: rounds are undone last to first, and an impact's gradient
+// is complete once the projections of its own and later rounds are undone;
+// gxp [n][3] (accumulated) receives the part for the step's start positions.
+// flags & 2 takes the cubic root's exact derivative instead of the
+// reference's CubicSolver backward (impact_jacobian).
+inline void zone_backward(const ZoneResponse& R, double* g, double* gw, double* gn, int flags = 0,
+                          double* gxp = nullptr) {
   using namespace zone_detail;
   std::vector<double> A, V, beta, lam, sm1, gz, t1, qtx, dz, dlam, r1l, lamp;
   std::vector<int> legal;
+  int last_round = 0;
+  for (const ZoneRecord& rec : R.tape) last_round = std::max(last_round, rec.round);
+  for (int r : R.accepted_round) last_round = std::max(last_round, r);
+  for (int round = last_round; round >= 0; --round) {
   for (int ri = (int)R.tape.size() - 1; ri >= 0; --ri) {
     const ZoneRecord& rec = R.tape[ri];
+    if (rec.round != round) continue;
     const int m = (int)rec.nodes.size(), nv = 3 * m, k = (int)rec.imps.size();
     auto local = [&](int nd) {
       for (int i = 0; i < m; ++i)
@@ -617,6 +815,32 @@ inline void zone_backward(const ZoneResponse& R, double* g, double* gw, double* 
     }
     for (int i = 0; i < m; ++i)
       for (int c = 0; c < 3; ++c) g[3 * (size_t)rec.nodes[i] + c] = dz[3 * i + c] / (sm1[3 * i + c] * sm1[3 * i + c]);
+  }
+  if (!(flags & 1)) continue;
+  // the impacts found this round, into the positions they were found at
+  for (size_t id = 0; id < R.accepted.size(); ++id) {
+    if (R.accepted_round[id] != round) continue;
+    const ZImpact& im = R.accepted[id];
+    double J[7][24];
+    if (!impact_jacobian(im.type, &R.accepted_x[12 * id], &R.accepted_xp[12 * id], im.t, (flags & 2) ? -1 : 1, J))
+      continue;
+    double gr[7];
+    for (int q = 0; q < 4; ++q) gr[q] = gw[4 * id + q];
+    for (int c = 0; c < 3; ++c) gr[4 + c] = gn[3 * id + c];
+    for (int q = 0; q < 4; ++q) {
+      const int nd = im.node[q];
+      if (nd < 0) continue;  // obstacles are given
+      for (int c = 0; c < 3; ++c) {
+        double sx = 0.0, sp = 0.0;
+        for (int row = 0; row < 7; ++row) {
+          sx += J[row][3 * q + c] * gr[row];
+          sp += J[row][12 + 3 * q + c] * gr[row];
+        }
+        g[3 * (size_t)nd + c] += sx;
+        if (gxp) gxp[3 * (size_t)nd + c] += sp;
+      }
+    }
+  }
   }
 }
 

@@ -317,9 +317,19 @@ ys_status ys_collider_response_impacts(ys_collider *c, ys_impact *impacts, int64
  * dl_dv_in [n][3] receive those of the inputs, dl_dw [impacts][4] and
  * dl_dn [impacts][3] (may be NULL) those of each impact's weights and
  * normal. The gradient of a projection's anchor goes to the zone's positions
- * at that projection, as the reference's autograd sends it. */
-ys_status ys_collider_respond_backward(ys_collider *c, const double *dl_dx, const double *dl_dv, double *dl_dx_in,
-                                       double *dl_dv_in, double *dl_dw, double *dl_dn);
+ * at that projection, as the reference's autograd sends it. With
+ * YS_RESPONSE_GRAD_IMPACTS the weight and normal gradients are carried on
+ * into the positions each impact was computed from (collision_test's cubic
+ * root, positions at the root, signed distances), and dl_dx_prev [n][3]
+ * (may be NULL) receives the part for the step's start positions; the root's
+ * derivative is the reference's CubicSolver backward unless
+ * YS_RESPONSE_GRAD_EXACT_ROOT is also set (that backward lacks the minus sign
+ * of the implicit derivative, src/Solvers.cpp:172-178). */
+#define YS_RESPONSE_GRAD_IMPACTS 1
+#define YS_RESPONSE_GRAD_EXACT_ROOT 2
+ys_status ys_collider_respond_backward(ys_collider *c, const double *dl_dx, const double *dl_dv, int32_t flags,
+                                       double *dl_dx_in, double *dl_dv_in, double *dl_dx_prev, double *dl_dw,
+                                       double *dl_dn);
 
 /* ---- learned preconditioner (no counterpart in the reference: its solve is
  * Eigen's Jacobi-PCG, src/Solvers.cpp:3-31, which stays the default and the

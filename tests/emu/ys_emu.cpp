@@ -671,6 +671,11 @@ int emu_respond(int nn, double* x, const double* xp, int nf, const int* fv, cons
   static std::vector<double> obs;  // kept for the backward
   obs.assign(ox, ox + 3 * (size_t)no);
   g_resp.obs_x = obs.data();
+  static std::vector<double> xprev, obsprev;
+  xprev.assign(xp, xp + 3 * (size_t)nn);
+  obsprev.assign(oxp, oxp + 3 * (size_t)no);
+  g_resp.xprev = xprev.data();
+  g_resp.obs_xprev = obsprev.data();
   g_resp.thickness = thick;
   g_resp.max_iter = max_iter;
   g_resp_x0.assign(x, x + 3 * (size_t)nn);
@@ -706,18 +711,19 @@ int emu_response_impacts(double* out, long cap) {
 
 // backward of the last emu_respond; gx [nn][3] in: dL/dx out, out: dL/dx in;
 // gv [nn][3] dL/dv out (may be null); gw [A][4], gn [A][3] out
-int emu_respond_backward(double* gx, const double* gv, double* gw, double* gn) {
+int emu_respond_backward(double* gx, const double* gv, double* gw, double* gn, int flags, double* gxp) {
   const size_t n3 = 3 * (size_t)g_resp.n_nodes, na = g_resp.accepted.size();
-  std::vector<double> w(4 * std::max<size_t>(na, 1), 0.0), nn(3 * std::max<size_t>(na, 1), 0.0);
+  std::vector<double> w(4 * std::max<size_t>(na, 1), 0.0), nn(3 * std::max<size_t>(na, 1), 0.0), p(n3, 0.0);
   if (gv && g_resp.changed)
     for (size_t i = 0; i < n3; ++i) gx[i] += g_resp_k * gv[i];
-  ys::zone_backward(g_resp, gx, w.data(), nn.data());
+  ys::zone_backward(g_resp, gx, w.data(), nn.data(), flags, p.data());
   if (gv && g_resp.changed)
     for (size_t i = 0; i < n3; ++i) gx[i] -= g_resp_k * gv[i];
   if (na) {
     std::memcpy(gw, w.data(), 4 * na * sizeof(double));
     std::memcpy(gn, nn.data(), 3 * na * sizeof(double));
   }
+  if (gxp) std::memcpy(gxp, p.data(), n3 * sizeof(double));
   return 0;
 }
 
@@ -807,6 +813,14 @@ int emu_detect(int nn, const double* xb, const double* x, const double* xp, int 
   }
   *ni = cnt;
   return cnt > icap ? 1 : 0;
+}
+
+// impact_jacobian for tests: J [7][24]
+int emu_impact_jacobian(int type, const double* x, const double* xp, double t, int sign, double* J) {
+  double Jl[7][24];
+  if (!ys::impact_jacobian(type, x, xp, t, sign, Jl)) return 1;
+  std::memcpy(J, Jl, sizeof(Jl));
+  return 0;
 }
 
 }  // extern "C"

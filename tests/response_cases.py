@@ -74,7 +74,7 @@ def _lib():
         L.emu_respond.argtypes = [c_i, _dp, _dp, c_i, _ip, _ip, c_i, _dp, _dp, c_i, _ip, c_d, c_i, _dp, c_d, c_d, c_i,
                                   _dp, ctypes.POINTER(c_l)]
         L.emu_response_impacts.argtypes = [_dp, c_l]
-        L.emu_respond_backward.argtypes = [_dp, _dp, _dp, _dp]
+        L.emu_respond_backward.argtypes = [_dp, _dp, _dp, _dp, ctypes.c_int, _dp]
         L.emu_ldp.argtypes = [c_i, c_i, _dp, _dp, _dp, _dp]
         for f in ("emu_detect", "emu_respond", "emu_response_impacts", "emu_respond_backward", "emu_ldp"):
             getattr(L, f).restype = c_i
@@ -130,15 +130,17 @@ def emu_respond(s, damp=0.1, max_iter=100, mass=None):
     return dict(x=x, v=v, info=list(info), impacts=imp[:15 * na].reshape(-1, 15))
 
 
-def emu_respond_backward(gx, gv, n_impacts):
-    """Backward of the last emu_respond: (dL/dx before, dL/dw [I, 4], dL/dn [I, 3])."""
+def emu_respond_backward(gx, gv, n_impacts, flags=0):
+    """Backward of the last emu_respond: (dL/dx before, dL/dw [I, 4],
+    dL/dn [I, 3], dL/dx_prev)."""
     L = _lib()
     g = np.ascontiguousarray(gx, np.float64).copy()
     gvv = None if gv is None else np.ascontiguousarray(gv, np.float64)
     gw, gn = np.zeros((max(n_impacts, 1), 4)), np.zeros((max(n_impacts, 1), 3))
+    gp = np.zeros_like(g)
     L.emu_respond_backward(g.ctypes.data_as(_dp), gvv.ctypes.data_as(_dp) if gvv is not None else None,
-                           gw.ctypes.data_as(_dp), gn.ctypes.data_as(_dp))
-    return g, gw[:n_impacts], gn[:n_impacts]
+                           gw.ctypes.data_as(_dp), gn.ctypes.data_as(_dp), int(flags), gp.ctypes.data_as(_dp))
+    return g, gw[:n_impacts], gn[:n_impacts], gp
 
 
 def emu_ldp(G, h):

@@ -133,7 +133,7 @@ def test_emulated_backward_matches_oracle(name):
     got = RC.emu_respond(s)
     rng = np.random.default_rng(7)
     gx, gv = rng.normal(size=s["x"].shape), rng.normal(size=s["x"].shape)
-    g, gw, gn = RC.emu_respond_backward(gx, gv, got["info"][5])
+    g, gw, gn, _ = RC.emu_respond_backward(gx, gv, got["info"][5])
     og, ogv, ogw, ogn = RO.respond_backward(res, s["obs_x"], s["thickness"], s["h"], DAMP, gx, gv)
     _check_backward(g, gw, gn, got["impacts"], og, ogw, ogn, res)
 
@@ -319,3 +319,62 @@ def test_scene_topology_is_the_collider_mesh():
     F, E = RC.topology(6, 5)
     faces, edges = ys.cloth_mesh_topology(6, 5)
     assert np.array_equal(F, faces) and np.array_equal(E, edges)
+
+
+@pytest.mark.parametrize("name", ["drop20", "drop24_deep"])
+def test_full_backward_matches_central_differences(name):
+    """The first round of the response (max_iter = 1: one detection, one
+    projection per zone) as a map of the step's end and start positions: the
+    backward with the impact chain and the root's exact derivative against
+    central differences of L = g . x_out + gv . v_out, both on the product's
+    code (emulator). One round keeps each zone's anchor and its positions the
+    same, where the reference's attribution of anchor gradients is exact."""
+    s = SCENES[name]()
+    base = RC.emu_respond(s, max_iter=1)
+    rng = np.random.default_rng(11)
+    gx, gv = rng.normal(size=s["x"].shape), rng.normal(size=s["x"].shape)
+    g, gw, gn, gp = RC.emu_respond_backward(gx, gv, base["info"][5], flags=3)
+
+    def loss(x, xp):
+        out = RC.emu_respond(dict(s, x=x, x_prev=xp), max_iter=1)
+        assert out["info"][5] == base["info"][5]  # the same impacts
+        return float(np.sum(gx * out["x"]) + np.sum(gv * out["v"]))
+    moved = np.where(np.abs(base["x"] - s["x"]).max(axis=1) > 0)[0]
+    eps = 1e-9
+    checked = 0
+    for nd in moved[:5]:
+        for c in range(3):
+            for which in ("x", "x_prev"):
+                xp_, xm_ = np.array(s["x"], float), np.array(s["x"], float)
+                pp_, pm_ = np.array(s["x_prev"], float), np.array(s["x_prev"], float)
+                (xp_ if which == "x" else pp_)[nd, c] += eps
+                (xm_ if which == "x" else pm_)[nd, c] -= eps
+                fd = (loss(xp_, pp_) - loss(xm_, pm_)) / (2 * eps)
+                an = (g if which == "x" else gp)[nd, c]
+                assert abs(fd - an) <= 1e-5 * max(1.0, abs(an)), (which, nd, c, fd, an)
+                checked += 1
+    assert checked >= 15
+    # the reference's root derivative differs only where the roots move
+    g1, _, _, gp1 = RC.emu_respond_backward(gx, gv, base["info"][5], flags=1)
+    assert np.abs(g1 - g).max() > 0.0 or np.abs(gp1 - gp).max() > 0.0
+
+
+@pytest.mark.gpu
+def test_gpu_full_backward_matches_emulated():
+    """ys_collider_respond_backward with the impact chain (both root
+    derivatives) equals the product's host code on the emulator's detection."""
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    s = SCENES["drop20"]()
+    emu = RC.emu_respond(s)
+    c = _collider(s)
+    out = c.respond(v=s["v"], h=s["h"], damp=DAMP)
+    assert out["impacts"] == emu["info"][5]
+    rng = np.random.default_rng(5)
+    gx, gv = rng.normal(size=s["x"].shape), rng.normal(size=s["x"].shape)
+    for flags in (1, 3):
+        got = c.respond_backward(gx, gv, impacts=True, exact_root=bool(flags & 2))
+        g, gw, gn, gp = RC.emu_respond_backward(gx, gv, emu["info"][5], flags=flags)
+        assert np.abs(got["x"] - g).max() <= 1e-8 * max(1.0, np.abs(g).max())
+        assert np.abs(got["x_prev"] - gp).max() <= 1e-8 * max(1.0, np.abs(gp).max())
+    c.close()
