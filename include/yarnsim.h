@@ -25,10 +25,19 @@
  *                     (src/Solvers.h:35-52, src/Solvers.cpp:3-31)
  *   ys_step           SimStep (src/TrainHelper.cpp:15-54) and
  *                     SimStep(..., ext_force) (src/TrainHelper.cpp:56-97)
+ *   ys_step_tangent(_ext)  the gradient LibTorch's autograd takes through
+ *                     SimStep and EigenSolver's backward (src/Solvers.cpp:
+ *                     33-58), forward mode, parameters or external force
+ *   ys_collider_*     Collision::find_impacts (src/Collision.cpp:184-208),
+ *                     Collision::collision_response (src/Collision.cpp:
+ *                     73-156) and InelasticProjection's backward
+ *                     (src/Collision.cpp:496-682)
  *
  * Error convention: every call returns a ys_status; a cloth whose system or
  * solution is non-finite is reported per cloth (SimStep returning false,
- * src/TrainHelper.cpp:22-48) and left unchanged. Nothing ever exits.
+ * src/TrainHelper.cpp:22-48) and left unchanged. Nothing ever exits (a
+ * response that does not converge returns YS_ERR_MAXITER where the
+ * reference exits the process).
  * Threading: one handle per host thread; calls are ordered on the handle's
  * stream.
  */
