@@ -233,7 +233,10 @@ class _Writer:
         addr = self.alloc(raw) if raw else UNDEF
         nd = arr.ndim
         space = struct.pack("<BBB5x", 1, nd, 1) + struct.pack("<%dQ" % nd, *arr.shape) * 2
-        fill = struct.pack("<BBBBI", 2, 2, 2, 1, dt.itemsize) + bytes(dt.itemsize)
+        # as the reference's saver leaves them: numeric datasets with an explicit
+        # zero fill value (its DSetCreatPropList), records with the default
+        fill = struct.pack("<BBBBI", 2, 2, 2, 1, 0) if dt.names else \
+            struct.pack("<BBBBI", 2, 2, 2, 1, dt.itemsize) + bytes(dt.itemsize)
         layout = struct.pack("<BBQQ", 3, 1, addr, len(raw))
         msgs = [_msg(0x01, space), _msg(0x03, _dtype_message(dt)), _msg(0x05, fill), _msg(0x08, layout)]
         return self.alloc(_object_header(msgs))

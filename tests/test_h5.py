@@ -128,3 +128,32 @@ def test_gpu_first_step_matches_the_reference_data_file():
         scale = max(np.abs(g[k][1]).max(), 1e-300)
         assert np.abs(st[k] - g[k][1]).max() <= 1e-12 * scale, k
     b.close()
+
+
+@pytest.mark.skipif(not os.path.exists(REF_FILE), reason="the reference's data file is not here")
+def test_writer_messages_match_the_reference_files(tmp_path):
+    """The writer's object-header messages for the reference's datasets equal
+    the ones libhdf5 wrote (dataspace, datatype and fill value byte for byte,
+    layout class and size), and its groups use the same B-tree and symbol-node
+    parameters; the reference's files also carry an old-style fill value and a
+    modification time, which readers do not need."""
+    import struct
+    p = str(tmp_path / "copy.h5")
+    ys.h5.write(p, ys.h5.read(REF_FILE))
+    ref = ys.h5._Reader(open(REF_FILE, "rb").read())
+    ours = ys.h5._Reader(open(p, "rb").read())
+    assert ref.d[:24] == ours.d[:24]  # signature, versions, sizes, group K values
+
+    def header(r, path):
+        addr = r.root[1]
+        for part in [x for x in path.split("/") if x]:
+            body = next(b for t, b in r.messages(addr) if t == 0x11)
+            bt, hp = struct.unpack_from("<QQ", body)
+            addr = r.group(bt, hp)[part]
+        return {t: b for t, b in r.messages(addr)}
+    for path in ("/Steps/Position/Node 3 1/LPOS", "/Steps/Velocity/Node 0 4/EVEL", "/Properties/Size",
+                 "/Properties/Physical properties"):
+        a, b = header(ref, path), header(ours, path)
+        for t in (0x01, 0x03, 0x05):
+            assert a[t] == b[t], (path, hex(t))
+        assert a[0x08][:2] == b[0x08][:2] and a[0x08][10:18] == b[0x08][10:18]
