@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <future>
 #include <string>
 #include <vector>
 
@@ -238,6 +239,7 @@ struct ys_collider {
   std::vector<double> resp_x0;  // positions before the response
   bool have_response = false;
   double resp_h = 0.0, resp_damp = 0.0;
+  bool obs_tree_valid = false;  // the obstacle tree and device copies match hox / hoxp
 };
 
 namespace {
@@ -487,34 +489,52 @@ ys_status ys_collider_set_positions(ys_collider* c, const double* x, const doubl
   const size_t n3 = 3 * (size_t)c->n_nodes, o3 = 3 * (size_t)c->n_obs_nodes;
   c->hx.resize(n3);
   c->hxp.resize(n3);
-  c->hox.resize(o3);
-  c->hoxp.resize(o3);
   const cudaMemcpyKind kind = (flags & YS_ON_DEVICE) ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
   YC_CUDA(cudaMemcpy(c->hx.data(), x, n3 * sizeof(double), kind));
   YC_CUDA(cudaMemcpy(c->hxp.data(), x_prev, n3 * sizeof(double), kind));
+  // an obstacle whose positions are bit-identical to the last call's keeps its
+  // tree: the build is a function of the positions alone, so the rebuild the
+  // reference does every call would give the same tree and boxes
+  bool same_obstacle = false;
   if (o3) {
-    YC_CUDA(cudaMemcpy(c->hox.data(), obs_x, o3 * sizeof(double), kind));
-    YC_CUDA(cudaMemcpy(c->hoxp.data(), obs_x_prev, o3 * sizeof(double), kind));
+    std::vector<double> ox(o3), oxp(o3);
+    YC_CUDA(cudaMemcpy(ox.data(), obs_x, o3 * sizeof(double), kind));
+    YC_CUDA(cudaMemcpy(oxp.data(), obs_x_prev, o3 * sizeof(double), kind));
+    same_obstacle = c->obs_tree_valid && c->hox.size() == o3 &&
+                    std::memcmp(ox.data(), c->hox.data(), o3 * sizeof(double)) == 0 &&
+                    std::memcmp(oxp.data(), c->hoxp.data(), o3 * sizeof(double)) == 0;
+    c->hox.swap(ox);
+    c->hoxp.swap(oxp);
+  } else {
+    c->hox.clear();
+    c->hoxp.clear();
   }
   YC_CUDA(cudaMemcpyAsync(c->x.p, c->hx.data(), n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   YC_CUDA(cudaMemcpyAsync(c->xp.p, c->hxp.data(), n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  if (o3) {
+  if (o3 && !same_obstacle) {
     YC_CUDA(cudaMemcpyAsync(c->ox.p, c->hox.data(), o3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     YC_CUDA(cudaMemcpyAsync(c->oxp.p, c->hoxp.data(), o3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   }
   // the trees of a fresh AccelStruct (src/CollisionUtil.cpp:3-9): rebuilt
-  // from these positions, as Collision::collision_response does every call
+  // from these positions, as Collision::collision_response does every call;
+  // the obstacle's on a second host thread
+  std::future<ys::BvhTree> obs_tree;
+  if (!same_obstacle)
+    obs_tree = std::async(std::launch::async, [c] {
+      std::vector<int> overts(c->n_obs_nodes);
+      for (int i = 0; i < c->n_obs_nodes; ++i) overts[i] = i;
+      return ys::bvh_build(c->n_obs_faces, c->ofv.data(), c->n_obs_nodes, overts.data(), c->hox.data(),
+                           c->hoxp.data(), c->ccd != 0);
+    });
   std::vector<int> verts(c->n_nodes);
   for (int i = 0; i < c->n_nodes; ++i) verts[i] = i;
   c->ct = ys::bvh_build(c->n_faces, c->fv.data(), c->n_nodes, verts.data(), c->hx.data(), c->hxp.data(), c->ccd != 0);
-  std::vector<int> overts(c->n_obs_nodes);
-  for (int i = 0; i < c->n_obs_nodes; ++i) overts[i] = i;
-  c->ot = ys::bvh_build(c->n_obs_faces, c->ofv.data(), c->n_obs_nodes, overts.data(), c->hox.data(), c->hoxp.data(),
-                        c->ccd != 0);
+  if (!same_obstacle) c->ot = obs_tree.get();
   ys_status s;
   if ((s = upload_tree(c, c->ct, c->c_left, c->c_right, c->c_face, c->c_levels, c->c_box, c->c_level_off)) != YS_OK)
     return s;
-  if ((s = upload_tree(c, c->ot, c->o_left, c->o_right, c->o_face, c->o_levels, c->o_box, c->o_level_off)) != YS_OK)
+  if (!same_obstacle &&
+      (s = upload_tree(c, c->ot, c->o_left, c->o_right, c->o_face, c->o_levels, c->o_box, c->o_level_off)) != YS_OK)
     return s;
   YC_CUDA(cudaMemcpyAsync(c->c_lof.p, c->ct.leaf_of_face.data(), sizeof(int) * c->n_faces, cudaMemcpyHostToDevice,
                           c->stream));
@@ -522,8 +542,9 @@ ys_status ys_collider_set_positions(ys_collider* c, const double* x, const doubl
   YC_CUDA(cudaMemcpyAsync(c->c_upper.p, c->ct.upper.data(), sizeof(int) * c->n_faces, cudaMemcpyHostToDevice,
                           c->stream));
   if ((s = refit(c, false)) != YS_OK) return s;
-  if ((s = refit(c, true)) != YS_OK) return s;
+  if (!same_obstacle && (s = refit(c, true)) != YS_OK) return s;
   YC_CUDA(cudaStreamSynchronize(c->stream));
+  c->obs_tree_valid = true;
   c->have_pairs = c->have_impacts = false;
   return YS_OK;
 }
