@@ -111,3 +111,34 @@ def test_gpu_collision_matches_reference(name):
         assert np.array_equal(mine[:, :8], theirs[:, :8])
         assert np.abs(mine[:, 8:] - theirs[:, 8:]).max() <= 1e-12
     c.close()
+
+
+@pytest.mark.gpu
+def test_gpu_obstacle_tree_reuse_matches_fresh_colliders():
+    """A collider keeps an obstacle's tree while its positions are unchanged
+    and rebuilds it when they move: pairs and impacts equal those of a fresh
+    collider either way."""
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    import response_cases as RC
+    s = RC.drop_scene(16, depth=1e-3)
+    ox, of = s["obs_x"], s["obs_faces"]
+
+    def fresh(x, xp, o):
+        c = ys.Collider(16, 16, obstacle_faces=of, n_obstacle_nodes=len(o))
+        c.set_positions(x, xp, o, o)
+        out = (c.pairs(), c.impacts())
+        c.close()
+        return out
+    c = ys.Collider(16, 16, obstacle_faces=of, n_obstacle_nodes=len(ox))
+    c.set_positions(s["x"], s["x_prev"], ox, ox)
+    c.pairs()
+    x2 = s["x"] + 2e-4 * np.random.default_rng(0).normal(size=s["x"].shape)
+    moved = ox + np.array([1e-4, 0.0, 3e-4])
+    for x, o in ((x2, ox), (x2, moved), (s["x"], moved)):
+        c.set_positions(x, s["x_prev"], o, o)
+        P, I = c.pairs(), c.impacts()
+        P0, I0 = fresh(x, s["x_prev"], o)
+        assert np.array_equal(P, P0)
+        assert np.array_equal(I["nodes"], I0["nodes"]) and np.array_equal(I["t"], I0["t"])
+    c.close()
