@@ -12,6 +12,7 @@
 #pragma once
 
 #include <cstdint>
+#include <future>
 #include <vector>
 
 #include "ys_collide.cuh"
@@ -42,39 +43,53 @@ struct Aap {  // the split plane (class aap, src/BVH.cpp:25-50)
   bool inside(const double* mid) const { return mid[xyz] > p; }
 };
 
+// the split plane of a box given by its x, y, z extents (lo, hi): the same
+// arithmetic as Aap(const Kdop&), which reads only those six bounds
+inline Aap aap_of(const double* lo, const double* hi) {
+  Kdop t;
+  for (int i = 0; i < 3; ++i) {
+    t.d[i] = lo[i];
+    t.d[i + 9] = hi[i];
+  }
+  return Aap(t);
+}
+
+// The reference's recursive construction (BVHNode(parent, lst, lst_num, ...),
+// src/BVH.cpp:178-223) with the nodes numbered as its depth-first creation
+// numbers them: a subtree of num faces takes 2 num - 1 consecutive indices
+// (itself, then its left subtree, then its right one), so disjoint subtrees
+// can be built on separate host threads and give the same tree.
 struct Builder {
-  const std::vector<Kdop>& boxes;
+  const std::vector<double>& ext;      // [F][6] x, y, z minima then maxima of each face's box
   const std::vector<double>& centers;  // [F][3]
   BvhTree& t;
-  int add_node(int dep) {
-    t.left.push_back(-1);
-    t.right.push_back(-1);
-    t.face.push_back(-1);
-    t.depth.push_back(dep);
-    if (dep > t.max_depth) t.max_depth = dep;
-    return (int)t.face.size() - 1;
+  void leaf(int f, int dep, int idx) {
+    t.face[idx] = f;
+    t.depth[idx] = dep;
+    t.leaf_of_face[f] = idx;
   }
-  int leaf(int f, int dep) {
-    const int n = add_node(dep);
-    t.face[n] = f;
-    t.leaf_of_face[f] = n;
-    return n;
-  }
-  // BVHNode(parent, lst, lst_num, ...) (src/BVH.cpp:178-223)
-  int node(int* lst, int num, int dep) {
-    if (num == 1) return leaf(lst[0], dep);
-    const int n = add_node(dep);
-    if (num == 2) {
-      const int l = leaf(lst[0], dep + 1);
-      const int r = leaf(lst[1], dep + 1);
-      t.left[n] = l;
-      t.right[n] = r;
-      return n;
+  void node(int* lst, int num, int dep, int idx, int threads) {
+    if (num == 1) {
+      leaf(lst[0], dep, idx);
+      return;
     }
-    Kdop box;
-    kdop_empty(box);
-    for (int q = 0; q < num; ++q) kdop_add(box, boxes[lst[q]]);
-    const Aap pln(box);
+    t.depth[idx] = dep;
+    if (num == 2) {
+      t.left[idx] = idx + 1;
+      t.right[idx] = idx + 2;
+      leaf(lst[0], dep + 1, idx + 1);
+      leaf(lst[1], dep + 1, idx + 2);
+      return;
+    }
+    double lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int q = 0; q < num; ++q) {
+      const double* e = &ext[6 * (size_t)lst[q]];
+      for (int i = 0; i < 3; ++i) {
+        lo[i] = kmin(e[i], lo[i]);
+        hi[i] = kmax(e[3 + i], hi[i]);
+      }
+    }
+    const Aap pln = aap_of(lo, hi);
     unsigned left_idx = 0, right_idx = (unsigned)num - 1;
     for (int q = 0; q < num; ++q) {
       const int i = lst[left_idx];
@@ -88,11 +103,16 @@ struct Builder {
     }
     const int hal = num / 2;
     const int split = (left_idx == 0 || (int)left_idx == num) ? hal : (int)left_idx;
-    const int l = node(lst, split, dep + 1);
-    const int r = node(lst + split, num - split, dep + 1);
-    t.left[n] = l;
-    t.right[n] = r;
-    return n;
+    t.left[idx] = idx + 1;
+    t.right[idx] = idx + 2 * split;
+    if (threads > 1 && num > 8192) {
+      auto lf = std::async(std::launch::async, [=] { node(lst, split, dep + 1, idx + 1, threads / 2); });
+      node(lst + split, num - split, dep + 1, idx + 2 * split, threads - threads / 2);
+      lf.get();
+    } else {
+      node(lst, split, dep + 1, idx + 1, 1);
+      node(lst + split, num - split, dep + 1, idx + 2 * split, 1);
+    }
   }
 };
 
@@ -114,7 +134,7 @@ inline BvhTree bvh_build(int nfaces, const int* fv, int nverts, const int* verts
     kdop_add_point(total, x + 3 * (size_t)verts[i]);
     if (ccd) kdop_add_point(total, xp + 3 * (size_t)verts[i]);
   }
-  std::vector<Kdop> boxes(nfaces);
+  std::vector<double> ext(6 * (size_t)nfaces);
   std::vector<double> centers(3 * (size_t)nfaces);
   const bvh_detail::Aap pln(total);
   std::vector<int> buf(nfaces);
@@ -134,24 +154,44 @@ inline BvhTree bvh_build(int nfaces, const int* fv, int nverts, const int* verts
     for (int i = 0; i < 3; ++i) centers[3 * (size_t)f + i] = ccd ? (mid[i] + midp[i]) * 0.5 : mid[i];
     if (pln.inside(&centers[3 * (size_t)f])) buf[left_idx++] = f;
     else buf[--right_idx] = f;
-    kdop_empty(boxes[f]);
-    for (int k = 0; k < 3; ++k) kdop_add_point(boxes[f], p[k]);
-    if (ccd)
-      for (int k = 0; k < 3; ++k) kdop_add_point(boxes[f], pp[k]);
+    // the face box's x, y, z bounds (kDOP18 of its points, and of their
+    // previous positions under CCD)
+    double* e = &ext[6 * (size_t)f];
+    for (int i = 0; i < 3; ++i) {
+      e[i] = e[3 + i] = p[0][i];
+      for (int k = 1; k < 3; ++k) {
+        e[i] = kmin(p[k][i], e[i]);
+        e[3 + i] = kmax(p[k][i], e[3 + i]);
+      }
+      if (ccd)
+        for (int k = 0; k < 3; ++k) {
+          e[i] = kmin(pp[k][i], e[i]);
+          e[3 + i] = kmax(pp[k][i], e[3 + i]);
+        }
+    }
   }
-  bvh_detail::Builder b{boxes, centers, t};
-  const int root = b.add_node(0);
+  const size_t nn = 2 * (size_t)nfaces - 1;
+  t.left.assign(nn, -1);
+  t.right.assign(nn, -1);
+  t.face.assign(nn, -1);
+  t.depth.assign(nn, 0);
+  bvh_detail::Builder b{ext, centers, t};
+  const int root = 0;
   if (nfaces == 1) {
     t.face[root] = buf[0];
     t.leaf_of_face[buf[0]] = root;
   } else {
     int split = (int)left_idx;
     if (left_idx == 0 || (int)left_idx == nfaces) split = nfaces / 2;
-    const int l = b.node(buf.data(), split, 1);
-    const int r = b.node(buf.data() + split, nfaces - split, 1);
-    t.left[root] = l;
-    t.right[root] = r;
+    t.left[root] = 1;
+    t.right[root] = 2 * split;
+    const int threads = nfaces > 16384 ? 8 : 1;
+    auto lf = std::async(threads > 1 ? std::launch::async : std::launch::deferred,
+                         [&] { b.node(buf.data(), split, 1, 1, threads / 2); });
+    b.node(buf.data() + split, nfaces - split, 1, 2 * split, threads - threads / 2);
+    lf.get();
   }
+  for (int d : t.depth) t.max_depth = d > t.max_depth ? d : t.max_depth;
   // leaf ranks (left to right) and upper nodes
   std::vector<int> stack{root};
   int r = 0;
