@@ -48,3 +48,32 @@ def test_call_order_and_step_size_errors():
         b.step(-1e-3)
     assert all(s["ok"] for s in b.step(1e-3))  # still usable
     b.close()
+
+
+@pytest.mark.gpu
+def test_tangent_and_control_argument_errors():
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    b = ys.ClothBatch([spec()])
+    with pytest.raises(ys.YarnSimError):
+        b.step_tangent(1e-3, dext_force=np.zeros((b.n_tangents, b.total_nodes, 5)))  # before tangent_enable
+    b.tangent_enable(0)
+    with pytest.raises(ValueError):
+        b.step_tangent(1e-3, dext_force=np.zeros((1, b.total_nodes, 5)))  # wrong shape
+    with pytest.raises(ys.YarnSimError):
+        b.step_tangent(1e-3, kact=b.n_tangents + 1)
+    st = b.step_tangent(1e-3, np.zeros((b.total_nodes, 5)), dext_force=np.zeros((b.n_tangents, b.total_nodes, 5)))
+    assert st[0]["ok"]
+    b.close()
+    with pytest.raises(ValueError):
+        ys.control.embed_step(ys.control.ForceNet(250), spec(), np.zeros((25, 3)), 5, loop="other")
+
+
+def test_response_backward_flags_are_checked_on_the_host():
+    # the flag check precedes any device work, so it runs on CPU too when a
+    # collider exists; without a device the collider cannot be made
+    if gpu_available():
+        c = ys.Collider(4, 4)
+        with pytest.raises(ys.YarnSimError):
+            c.respond_backward(np.zeros((16, 3)))  # no response yet
+        c.close()
