@@ -69,11 +69,14 @@ def test_tangent_and_control_argument_errors():
         ys.control.embed_step(ys.control.ForceNet(250), spec(), np.zeros((25, 3)), 5, loop="other")
 
 
-def test_response_backward_flags_are_checked_on_the_host():
-    # the flag check precedes any device work, so it runs on CPU too when a
-    # collider exists; without a device the collider cannot be made
-    if gpu_available():
-        c = ys.Collider(4, 4)
-        with pytest.raises(ys.YarnSimError):
-            c.respond_backward(np.zeros((16, 3)))  # no response yet
-        c.close()
+@pytest.mark.gpu
+def test_response_calls_before_a_response_are_argument_errors():
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    c = ys.Collider(4, 4)
+    with pytest.raises(ys.YarnSimError) as e:
+        c.respond_backward(np.zeros((16, 3)))  # no response yet
+    assert e.value.status == 1
+    with pytest.raises(ys.YarnSimError):
+        c.response_impacts()
+    c.close()
