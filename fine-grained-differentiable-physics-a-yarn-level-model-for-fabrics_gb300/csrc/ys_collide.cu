@@ -29,6 +29,7 @@ using ys::Impact;
 using ys::Kdop;
 
 constexpr int kStack = 64;  // traversal stack; deeper trees report an error
+constexpr int kBroadBlock = 32;
 
 #define YC_CUDA(call)                                                                   \
   do {                                                                                  \
@@ -327,8 +328,10 @@ ys_status broad_phase(ys_collider* c, bool masked) {
   a.face_active = masked ? c->face_active.p : nullptr;
   a.node_active = masked ? c->node_active.p : nullptr;
   YC_CUDA(cudaMemsetAsync(c->overflow.p, 0, sizeof(int), c->stream));
-  const unsigned g = (unsigned)((c->n_faces + 127) / 128);
-  k_broad<false><<<g, 128, 0, c->stream>>>(a);
+  // one warp per block: a cloth has only as many threads as faces (8K at
+  // 64 x 64), and 128-thread blocks left most of the 152 SMs idle
+  const unsigned g = (unsigned)((c->n_faces + kBroadBlock - 1) / kBroadBlock);
+  k_broad<false><<<g, kBroadBlock, 0, c->stream>>>(a);
   YC_CUDA(cudaGetLastError());
   ys_status s = scan(c, c->counts.p, c->n_faces, c->offsets.p, &c->npairs);
   if (s != YS_OK) return s;
@@ -338,7 +341,7 @@ ys_status broad_phase(ys_collider* c, bool masked) {
   YC_CUDA(c->pairs.reserve(3 * (size_t)std::max<int64_t>(c->npairs, 1)));
   a.offset = c->offsets.p;
   a.out = c->pairs.p;
-  k_broad<true><<<g, 128, 0, c->stream>>>(a);
+  k_broad<true><<<g, kBroadBlock, 0, c->stream>>>(a);
   YC_CUDA(cudaGetLastError());
   YC_CUDA(cudaStreamSynchronize(c->stream));
   c->have_pairs = true;
