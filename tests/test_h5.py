@@ -157,3 +157,21 @@ def test_writer_messages_match_the_reference_files(tmp_path):
         for t in (0x01, 0x03, 0x05):
             assert a[t] == b[t], (path, hex(t))
         assert a[0x08][:2] == b[0x08][:2] and a[0x08][10:18] == b[0x08][10:18]
+
+
+def test_non_square_round_trip(tmp_path):
+    """Node groups are named by (u, v) and loaded at u + v W for W != L."""
+    W, L = 6, 4
+    rng = np.random.default_rng(2)
+    st = {k: rng.normal(size=(2, W * L, 3 if k[0] == "L" else 2)) for k in KEYS}
+    phy = {n: 0.5 for n in ys.h5.physical_dtype(True).names}
+    phy["woven_pattern"] = 1
+    p = str(tmp_path / "ns.h5")
+    ys.h5.save_trajectory(p, W, L, phy, st)
+    f = ys.h5.read(p)
+    assert np.array_equal(f["/Steps/Position/Node 5 1/LPOS"], st["LPos"][:, 5 + 1 * W])
+    assert np.array_equal(f["/Steps/Velocity/Node 2 3/EVEL"], st["EVel"][:, 2 + 3 * W])
+    back = ys.h5.data_loader(p, 1, 2)
+    for k in KEYS:
+        assert np.array_equal(back[k][0], st[k][1])
+    assert ys.h5.cloth_property_loader_heter(p)[0] == {"width": W, "length": L}
