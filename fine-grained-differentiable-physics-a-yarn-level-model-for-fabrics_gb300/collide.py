@@ -122,9 +122,10 @@ class Collider:
         set_positions: rounds of GPU detection, independent impacts, impact
         zones and their exact inelastic projections, then v + damp (x - x_before)
         / h when a zone moved. v [n, 3] and mass [n] are optional. Returns
-        dict(x, v, rounds, converged, changed, zones, infeasible, impacts,
-        projections); raises when max_iter rounds still found impacts (where the
-        reference exits) unless check=False."""
+        dict(x, v, rounds, converged, changed, zones, infeasible, zone_overflow,
+        impacts, projections); raises when max_iter rounds still found impacts
+        (where the reference exits) or a zone outgrew 256 impacts, unless
+        check=False."""
         x = np.zeros((self.n_nodes, 3))
         vv = None if v is None else np.array(v, np.float64).reshape(self.n_nodes, 3).copy()
         m = None if mass is None else np.ascontiguousarray(mass, np.float64).reshape(self.n_nodes)
@@ -137,8 +138,8 @@ class Collider:
             N.check(st, "ys_collider_respond")
         self._n_received = int(info.impacts)
         return dict(x=x, v=vv, rounds=info.rounds, converged=bool(info.converged), changed=bool(info.changed),
-                    zones=info.zones, infeasible=info.infeasible, impacts=info.impacts,
-                    projections=info.projections)
+                    zones=info.zones, infeasible=info.infeasible, zone_overflow=bool(info.zone_overflow),
+                    impacts=info.impacts, projections=info.projections)
 
     def response_impacts(self) -> dict:
         """The impacts the zones of the last response received, in order

@@ -680,10 +680,13 @@ ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h,
     info->changed = R.changed;
     info->zones = R.zones;
     info->infeasible = R.infeasible;
-    info->reserved = 0;
+    info->zone_overflow = R.zone_overflow;
     info->impacts = (int64_t)R.accepted.size();
     info->projections = (int64_t)R.tape.size();
   }
+  if (R.zone_overflow)
+    return ys_internal_fail(YS_ERR_MAXITER, "collision response stopped: an impact zone gathered more than 256 impacts "
+                                            "(layers tangled beyond what the response resolves)");
   if (!R.converged) return ys_internal_fail(YS_ERR_MAXITER, "collision response did not converge");
   return YS_OK;
 }

@@ -347,6 +347,10 @@ struct ZoneResponse {
   const double* obs_xprev = nullptr;
   double thickness = 0.0;
   int max_iter = 100;
+  // a zone that gathers more impacts than this stops the response (its exact
+  // projection costs grow with the square of the impacts; such zones arise
+  // only from layers tangled beyond what a step's detection can separate)
+  int max_zone_impacts = 256;
   // results
   std::vector<ZImpact> accepted;  // every impact a zone received, in order
   std::vector<int> accepted_round;
@@ -354,6 +358,7 @@ struct ZoneResponse {
   std::vector<double> accepted_xp;  // [accepted][4][3] and at the start of the step
   std::vector<ZoneRecord> tape;   // every projection, in order
   int rounds = 0, converged = 0, changed = 0, zones = 0, infeasible = 0;
+  int zone_overflow = 0;  // stopped at a zone larger than max_zone_impacts
 };
 
 namespace zone_detail {
@@ -428,7 +433,7 @@ int zone_respond(ZoneResponse& R, double* x, const double* mass, Detect&& detect
   R.accepted_x.clear();
   R.accepted_xp.clear();
   R.tape.clear();
-  R.rounds = R.converged = R.changed = R.zones = R.infeasible = 0;
+  R.rounds = R.converged = R.changed = R.zones = R.infeasible = R.zone_overflow = 0;
   std::vector<double> xold(x, x + 3 * (size_t)n);
   // faces around each node (the verts' adj_faces of the cloth mesh)
   std::vector<int> fo(n + 1, 0), fl(3 * (size_t)R.n_faces);
@@ -518,13 +523,16 @@ int zone_respond(ZoneResponse& R, double* x, const double* mass, Detect&& detect
       zs[z0].active = true;
     }
     for (int z : order)
+      if (zs[z].active && (int)zs[z].imps.size() > R.max_zone_impacts) R.zone_overflow = 1;
+    if (R.zone_overflow) break;
+    for (int z : order)
       if (zs[z].active) {
         R.changed = 1;
         zone_detail::project(R, zs[z].nodes, zs[z].imps, mass, xold.data(), x, local, iter);
       }
   }
   R.rounds = iter;
-  R.converged = iter < R.max_iter;
+  R.converged = iter < R.max_iter && !R.zone_overflow;
   R.zones = (int)order.size();
   return 0;
 }

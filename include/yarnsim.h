@@ -304,14 +304,17 @@ ys_status ys_collider_get_impacts(ys_collider *c, ys_impact *impacts, int64_t ca
  * receives the positions after the response; v [n][3] (may be NULL) is
  * updated in place as v + damp (x - x_before) / h when any zone moved.
  * Returns YS_ERR_MAXITER when max_iter rounds (the reference's 100) still
- * found impacts, where the reference exits; x_out and v are written. */
+ * found impacts, where the reference exits, or when a zone gathers more than
+ * 256 impacts (layers tangled beyond what the response resolves: the exact
+ * projection's cost grows with the square of a zone's impacts); x_out and v
+ * are written as they stand. */
 typedef struct {
   int32_t rounds;      /* rounds that found impacts (the reference's iter) */
   int32_t converged;   /* 1: a round found no impact within max_iter */
   int32_t changed;     /* 1: a zone was projected (velocities updated) */
   int32_t zones;       /* impact zones at the end */
   int32_t infeasible;  /* projections whose constraints had no solution (zone left in place) */
-  int32_t reserved;
+  int32_t zone_overflow; /* 1: stopped at a zone of more than 256 impacts */
   int64_t impacts;     /* impacts the zones received, over all rounds */
   int64_t projections; /* zone projections */
 } ys_response_info;

@@ -583,7 +583,7 @@ void hc_mark(HostColl& h, const ys::BvhTree& t, const uint8_t* fa, int n, bool& 
 
 // x [nn][3] in/out, v [nn][3] in/out (may be null), mass [nn] (may be null);
 // info[8]: rounds, converged, changed, zones, infeasible, impacts,
-// projections, status
+// projections, zone overflow
 int emu_respond(int nn, double* x, const double* xp, int nf, const int* fv, const int* fe, int no, const double* ox,
                 const double* oxp, int nof, const int* ofv, double thick, int ccd, const double* mass, double hstep,
                 double damp, int max_iter, double* v, long* info) {
@@ -691,7 +691,7 @@ int emu_respond(int nn, double* x, const double* xp, int nf, const int* fv, cons
   info[4] = g_resp.infeasible;
   info[5] = (long)g_resp.accepted.size();
   info[6] = (long)g_resp.tape.size();
-  info[7] = 0;
+  info[7] = g_resp.zone_overflow;
   return 0;
 }
 

@@ -378,3 +378,31 @@ def test_gpu_full_backward_matches_emulated():
         assert np.abs(got["x"] - g).max() <= 1e-8 * max(1.0, np.abs(g).max())
         assert np.abs(got["x_prev"] - gp).max() <= 1e-8 * max(1.0, np.abs(gp).max())
     c.close()
+
+
+def test_tangled_layers_stop_at_the_zone_cap():
+    """The 50 x 50 sphere detection fixture is tangled beyond what a step's
+    detection separates: its zones keep merging, and the response stops when
+    one outgrows 256 impacts instead of spending minutes in ever larger exact
+    projections (the reference would run its 100 rounds and exit)."""
+    import time
+    s = RC.fixture_scene("collide_sphere50")
+    t0 = time.time()
+    got = RC.emu_respond(s)
+    assert got["info"][7] == 1 and got["info"][1] == 0
+    assert time.time() - t0 < 60.0
+
+
+@pytest.mark.gpu
+def test_gpu_tangled_layers_stop_at_the_zone_cap():
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    s = RC.fixture_scene("collide_sphere50")
+    c = _collider(s)
+    out = c.respond(v=s["v"], h=s["h"], damp=DAMP, check=False)
+    assert out["zone_overflow"] and not out["converged"]
+    c.set_positions(s["x"], s["x_prev"], s["obs_x"], s["obs_x"])
+    with pytest.raises(ys.YarnSimError) as e:
+        c.respond(v=s["v"], h=s["h"], damp=DAMP)
+    assert e.value.status == 4
+    c.close()
