@@ -632,6 +632,8 @@ int run_embed(std::map<std::string, std::string>& kv) {
   const double L = get_d(kv, "L", 1e-3);
   const double R = get_d(kv, "R", 1e-4);
   const int sample = static_cast<int>(get_d(kv, "sample", 10));
+  // loop=intended forces steps 0..5 as the comment in train_embed describes
+  const bool intended = get_s(kv, "loop", "reference") == "intended";
   ref_cg_set_options(get_d(kv, "cg_tol", DBL_EPSILON), static_cast<long>(get_d(kv, "cg_maxiter", -1)));
   torch::manual_seed(static_cast<uint64_t>(get_d(kv, "seed", 0)));
   std::vector<double> G = parse_list(get_s(kv, "G", "0,0,9.8"));
@@ -689,8 +691,12 @@ int run_embed(std::map<std::string, std::string>& kv) {
       forces.push_back(pred.index({0, 0}).item<double>());
       forces.push_back(pred.index({0, 1}).item<double>());
       ok = step(ext);
-      s = 5;  // the reference's `if (s = force_stop_frame)`
-      bkup = cloth.get_ClothState();
+      if (intended) {
+        if (s == 5) bkup = cloth.get_ClothState();
+      } else {
+        s = 5;  // the reference's `if (s = force_stop_frame)`
+        bkup = cloth.get_ClothState();
+      }
       if (!ok) break;
     } else {
       ok = step(zero_force);

@@ -54,17 +54,20 @@ def test_network_matches_the_reference_forward():
 
 
 @pytest.mark.gpu
-def test_embed_step_matches_the_reference_gradient():
+@pytest.mark.parametrize("loop", ["reference", "intended"])
+def test_embed_step_matches_the_reference_gradient(loop):
     """Loss, predicted forces and the gradient of every ForceNet parameter of
     one train_embed evaluation, with the tangents in the reference's
-    EigenSolver-backward mode, against the reference's own autograd."""
+    EigenSolver-backward mode, against the reference's own autograd: its loop
+    as written (one forced step) and forcing steps 0..5, where each force
+    also depends on the earlier ones through the network's input."""
     if not gpu_available():
         pytest.skip("no CUDA device")
-    g = _golden()
+    g = dict(np.load(GOLDEN if loop == "reference" else GOLDEN.replace(".npz", "_intended.npz")))
     net = _net(g)
     out = ys.control.embed_step(net, _spec(g), g["goal"], int(g["cfg_sample"]), h=float(g["cfg_h"]),
-                                loop="reference", tangent_mode=ys._native.YS_TANGENT_REFERENCE)
-    assert np.allclose(out["forces"][0], g["forces"], rtol=1e-6, atol=0)
+                                loop=loop, tangent_mode=ys._native.YS_TANGENT_REFERENCE)
+    assert np.allclose(out["forces"].reshape(-1), g["forces"], rtol=1e-6, atol=0)
     assert abs(out["loss"] - g["loss"][0]) <= 1e-9 * g["loss"][0]
     assert np.abs(out["final_lpos"] - g["final__LPos"]).max() <= 1e-12
     for name, grad in out["grads"].items():
