@@ -70,7 +70,9 @@ def test_embed_step_matches_the_reference_gradient(loop):
     assert np.allclose(out["forces"].reshape(-1), g["forces"], rtol=1e-6, atol=0)
     # the loss is a small difference of mass centres (5e-5 after eleven steps)
     assert abs(out["loss"] - g["loss"][0]) <= 1e-7 * g["loss"][0]
-    assert np.abs(out["final_lpos"] - g["final__LPos"]).max() <= 1e-12
+    # later forces come from float32 casts of the state, whose last bits can
+    # differ between two FP64 simulators; 1e-12 m for the one-force loop
+    assert np.abs(out["final_lpos"] - g["final__LPos"]).max() <= (1e-12 if loop == "reference" else 1e-9)
     for name, grad in out["grads"].items():
         ref = g["grad__" + name.replace(".", "__")]
         scale = max(np.abs(ref).max(), 1e-30)
