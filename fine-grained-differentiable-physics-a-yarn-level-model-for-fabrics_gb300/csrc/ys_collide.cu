@@ -43,7 +43,22 @@ struct DevTree {
   const int* face;
   Kdop* box;
   int nnodes;
+  float* fbox;  // [nnodes][18] the boxes widened to float (lower bounds down, upper up)
 };
+
+// inner-node prune in FP32 on the widened boxes: wider again by a relative
+// 1e-6 of the magnitudes, far above float rounding, it keeps every subtree
+// holding a pair the exact FP64 leaf test accepts
+__device__ __forceinline__ bool kdop_overlap_f(const float* a, const float* b, float d1, float d2) {
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const float dd = i < 3 ? d1 : d2;
+    const float slack = 1e-6f * (fabsf(a[i]) + fabsf(a[i + 9]) + fabsf(b[i]) + fabsf(b[i + 9])) + 1e-30f;
+    if (a[i] > b[i + 9] + dd + slack) return false;
+    if (a[i + 9] < b[i] - dd - slack) return false;
+  }
+  return true;
+}
 
 // boxes of the tree nodes at one depth: leaves from their face's nodes,
 // inner nodes as the union of their children (BVHNode::refit, src/BVH.cpp:150-160)
@@ -67,6 +82,10 @@ __global__ void k_refit(DevTree t, const int* __restrict__ level_nodes, int coun
     ys::kdop_add(b, t.box[t.right[n]]);
   }
   t.box[n] = b;
+  for (int k = 0; k < 9; ++k) {
+    t.fbox[18 * (int64_t)n + k] = __double2float_rd(b.d[k]);
+    t.fbox[18 * (int64_t)n + 9 + k] = __double2float_ru(b.d[k + 9]);
+  }
 }
 
 struct BroadArgs {
@@ -85,6 +104,7 @@ struct BroadArgs {
   // active test, src/Collision.cpp:158-182, 289-310)
   const uint8_t* face_active;
   const uint8_t* node_active;  // cloth-tree nodes with an active leaf below
+  float thick1, thick2;        // the thickness and sqrt(2) times it, widened, for the FP32 prune
 };
 
 // the pairs whose first face is f: cloth faces g the reference reports with
@@ -94,6 +114,11 @@ __global__ void k_broad(BroadArgs a) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= a.nfaces) return;
   const Kdop bf = a.cloth.box[a.leaf_of_face[f]];
+  float bfl[18];
+  for (int k = 0; k < 9; ++k) {
+    bfl[k] = __double2float_rd(bf.d[k]);
+    bfl[k + 9] = __double2float_ru(bf.d[k + 9]);
+  }
   const int uf = a.upper[f], rf = a.rank[f];
   const bool fa = a.face_active == nullptr || a.face_active[f] != 0;
   int64_t c = 0, o = WRITE ? a.offset[f] : 0;
@@ -119,7 +144,7 @@ __global__ void k_broad(BroadArgs a) {
         }
         ++c;
       } else {
-        if (!ys::kdop_overlap_loose(bf, t.box[n], a.thickness)) continue;
+        if (!kdop_overlap_f(bfl, t.fbox + 18 * (int64_t)n, a.thick1, a.thick2)) continue;
         if (sp + 2 > kStack) {
           atomicOr(a.overflow, 1);
           continue;
@@ -222,6 +247,7 @@ struct ys_collider {
   ys::BvhTree ct, ot;
   DVec<int> c_left, c_right, c_face, c_lof, c_rank, c_upper, c_levels, o_left, o_right, o_face, o_levels;
   DVec<Kdop> c_box, o_box;
+  DVec<float> c_fbox, o_fbox;
   std::vector<int> c_level_off, o_level_off;  // level l nodes at [off[l], off[l+1])
   // outputs
   DVec<int64_t> counts, offsets, sums, total;
@@ -273,8 +299,10 @@ ys_status upload_tree(ys_collider* c, const ys::BvhTree& t, DVec<int>& l, DVec<i
 ys_status refit(ys_collider* c, bool obstacle) {
   const ys::BvhTree& t = obstacle ? c->ot : c->ct;
   if (t.face.empty()) return YS_OK;
+  DVec<float>& fb = obstacle ? c->o_fbox : c->c_fbox;
+  YC_CUDA(fb.reserve(18 * t.face.size()));
   DevTree dt{obstacle ? c->o_left.p : c->c_left.p, obstacle ? c->o_right.p : c->c_right.p,
-             obstacle ? c->o_face.p : c->c_face.p, obstacle ? c->o_box.p : c->c_box.p, (int)t.face.size()};
+             obstacle ? c->o_face.p : c->c_face.p, obstacle ? c->o_box.p : c->c_box.p, (int)t.face.size(), fb.p};
   const std::vector<int>& off = obstacle ? c->o_level_off : c->c_level_off;
   const int* lv = obstacle ? c->o_levels.p : c->c_levels.p;
   CMesh m{c->x.p, c->xp.p, c->ox.p, c->oxp.p};
@@ -316,8 +344,10 @@ void edges_of(const int* fv, int f, int e[3][2], bool obstacle, const std::vecto
 
 ys_status broad_phase(ys_collider* c, bool masked) {
   BroadArgs a{};
-  a.cloth = DevTree{c->c_left.p, c->c_right.p, c->c_face.p, c->c_box.p, (int)c->ct.face.size()};
-  a.obs = DevTree{c->o_left.p, c->o_right.p, c->o_face.p, c->o_box.p, (int)c->ot.face.size()};
+  a.cloth = DevTree{c->c_left.p, c->c_right.p, c->c_face.p, c->c_box.p, (int)c->ct.face.size(), c->c_fbox.p};
+  a.obs = DevTree{c->o_left.p, c->o_right.p, c->o_face.p, c->o_box.p, (int)c->ot.face.size(), c->o_fbox.p};
+  a.thick1 = (float)(c->thickness * (1.0 + 1e-6));
+  a.thick2 = (float)(std::sqrt(2.0) * c->thickness * (1.0 + 1e-6));
   a.leaf_of_face = c->c_lof.p;
   a.rank = c->c_rank.p;
   a.upper = c->c_upper.p;
