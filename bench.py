@@ -159,12 +159,14 @@ def measure_fp64_peak(torch):
 
 # ---------------------------------------------------------------- CPU arm
 def _cpu_worker(args):
-    specs, idx, steps, seed = args
+    specs, idx, warm, steps, seed = args
     from oracle.oracle import ClothSpec, OracleCloth
     _, wind = workload(seed)
     cloths = [OracleCloth(ClothSpec(**specs[i])) for i in idx]
-    t0 = time.perf_counter()
-    for s in range(steps):
+    t0 = 0.0
+    for s in range(warm + steps):
+        if s == warm:
+            t0 = time.perf_counter()
         wv = wind_at(wind, s)
         for c, i in zip(cloths, idx):
             c.set_wind(wv[i])
@@ -172,7 +174,7 @@ def _cpu_worker(args):
     return time.perf_counter() - t0
 
 
-def cpu_sample(specs, seed, target_nodes, steps, cores):
+def cpu_sample(specs, seed, target_nodes, steps, cores, warm=0):
     """Times the oracle on a bounded sample of the workload's cloths; returns
     (batch steps/s extrapolated to the full batch, description)."""
     import multiprocessing as mp
@@ -196,12 +198,12 @@ def cpu_sample(specs, seed, target_nodes, steps, cores):
     shards = [s for s in shards if s]
     ctx = mp.get_context("spawn")
     with ctx.Pool(len(shards)) as pool:
-        times = pool.map(_cpu_worker, [(specs, s, steps, seed) for s in shards])
+        times = pool.map(_cpu_worker, [(specs, s, warm, steps, seed) for s in shards])
     wall = max(times)  # each worker times its own stepping loop (process start-up excluded)
     per_step = wall / steps
     value = (nodes / total) / per_step
-    desc = "%d of %d cloths (%d of %d nodes), %d step(s), %d processes; slowest worker's loop time" % (
-        len(idx), len(specs), nodes, total, steps, len(shards))
+    desc = "%d of %d cloths (%d of %d nodes), %d step(s) after %d untimed, %d processes; slowest worker's loop time" % (
+        len(idx), len(specs), nodes, total, steps, warm, len(shards))
     return value, desc, wall
 
 
@@ -342,8 +344,9 @@ def main():
         if rank != 0:
             return 0
         cores = os.cpu_count() or 1
-        steps = 1
-        value, desc, wall = cpu_sample(specs, seed, target_nodes=total_nodes, steps=1, cores=cores)
+        steps = max(1, args.steps)
+        value, desc, wall = cpu_sample(specs, seed, target_nodes=total_nodes, steps=steps, cores=cores,
+                                       warm=max(0, args.warmup))
         line = {"impl": "reference", "metric": metric, "value": value, "unit": "steps/s", "n_gpus": 0,
                 "steps": steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
