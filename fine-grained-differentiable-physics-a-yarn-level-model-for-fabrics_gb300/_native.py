@@ -28,6 +28,7 @@ EXPORTED = [
     "ys_gnn_set_params", "ys_gnn_train_step", "ys_gnn_loss_grad", "ys_set_preconditioner", "ys_precond_info",
     "ys_get_system_slots", "ys_tc_gemm_bf16", "ys_precond_refresh", "ys_get_normals", "ys_collider_respond",
     "ys_collider_response_impacts", "ys_collider_respond_backward", "ys_step_tangent_ext",
+    "ys_collider_set_max_zone_impacts",
 ]
 YS_PREC_JACOBI, YS_PREC_LEARNED = 0, 1
 YS_TANGENT_EXACT, YS_TANGENT_REFERENCE = 0, 1
@@ -154,6 +155,7 @@ def load(build_if_missing: bool = True):
     L.ys_collider_respond.argtypes = [vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32, vp, vp,
                                       ctypes.POINTER(ResponseInfo)]
     L.ys_collider_response_impacts.argtypes = [vp, vp, ctypes.c_int64]
+    L.ys_collider_set_max_zone_impacts.argtypes = [vp, ctypes.c_int32]
     L.ys_collider_respond_backward.argtypes = [vp, vp, vp, ctypes.c_int32, vp, vp, vp, vp, vp]
     for name in EXPORTED:
         if name not in ("ys_batch_destroy", "ys_last_error", "ys_cloth_node_offset", "ys_cloth_dim",

@@ -116,6 +116,11 @@ class Collider:
         return dict(type=a["type"].copy(), nodes=a["nodes"].copy(), t=a["t"].copy(), w=a["w"].copy(),
                     n=a["n"].copy(), pair=a["pair"].copy())
 
+    def set_max_zone_impacts(self, n: int):
+        """The response stops (zone_overflow) when a zone gathers more than n
+        impacts (default 256)."""
+        N.check(N.load().ys_collider_set_max_zone_impacts(self._h, int(n)), "ys_collider_set_max_zone_impacts")
+
     def respond(self, v=None, mass=None, h: float = 1e-3, damp: float = 0.1, max_iter: int = 100,
                 check: bool = True) -> dict:
         """collision_response(damp) over the positions of the last
@@ -124,8 +129,8 @@ class Collider:
         / h when a zone moved. v [n, 3] and mass [n] are optional. Returns
         dict(x, v, rounds, converged, changed, zones, infeasible, zone_overflow,
         impacts, projections); raises when max_iter rounds still found impacts
-        (where the reference exits) or a zone outgrew 256 impacts, unless
-        check=False."""
+        (where the reference exits) or a zone outgrew the zone limit
+        (set_max_zone_impacts), unless check=False."""
         x = np.zeros((self.n_nodes, 3))
         vv = None if v is None else np.array(v, np.float64).reshape(self.n_nodes, 3).copy()
         m = None if mass is None else np.ascontiguousarray(mass, np.float64).reshape(self.n_nodes)

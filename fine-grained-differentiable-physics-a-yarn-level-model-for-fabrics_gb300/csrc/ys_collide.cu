@@ -267,6 +267,7 @@ struct ys_collider {
   bool have_response = false;
   double resp_h = 0.0, resp_damp = 0.0;
   bool obs_tree_valid = false;  // the obstacle tree and device copies match hox / hoxp
+  int max_zone_impacts = 256;
 };
 
 namespace {
@@ -638,6 +639,7 @@ ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h,
   R.obs_xprev = c->hoxp.data();
   R.thickness = c->thickness;
   R.max_iter = max_iter;
+  R.max_zone_impacts = c->max_zone_impacts;
   c->resp_x0 = c->hx;
   std::vector<double> x(c->hx);
   const size_t n3 = 3 * (size_t)c->n_nodes;
@@ -715,7 +717,7 @@ ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h,
     info->projections = (int64_t)R.tape.size();
   }
   if (R.zone_overflow)
-    return ys_internal_fail(YS_ERR_MAXITER, "collision response stopped: an impact zone gathered more than 256 impacts "
+    return ys_internal_fail(YS_ERR_MAXITER, "collision response stopped: an impact zone outgrew the zone limit "
                                             "(layers tangled beyond what the response resolves)");
   if (!R.converged) return ys_internal_fail(YS_ERR_MAXITER, "collision response did not converge");
   return YS_OK;
@@ -765,6 +767,12 @@ ys_status ys_collider_respond_backward(ys_collider* c, const double* dl_dx, cons
   if (dl_dx_prev) std::memcpy(dl_dx_prev, gp.data(), n3 * sizeof(double));
   if (dl_dw && na) std::memcpy(dl_dw, gw.data(), 4 * na * sizeof(double));
   if (dl_dn && na) std::memcpy(dl_dn, gn.data(), 3 * na * sizeof(double));
+  return YS_OK;
+}
+
+ys_status ys_collider_set_max_zone_impacts(ys_collider* c, int32_t n) {
+  if (!c || n < 1) return ys_internal_fail(YS_ERR_ARG, "the zone limit must be at least 1");
+  c->max_zone_impacts = n;
   return YS_OK;
 }
 

@@ -305,7 +305,8 @@ ys_status ys_collider_get_impacts(ys_collider *c, ys_impact *impacts, int64_t ca
  * updated in place as v + damp (x - x_before) / h when any zone moved.
  * Returns YS_ERR_MAXITER when max_iter rounds (the reference's 100) still
  * found impacts, where the reference exits, or when a zone gathers more than
- * 256 impacts (layers tangled beyond what the response resolves: the exact
+ * the zone limit (256 impacts unless ys_collider_set_max_zone_impacts says
+ * otherwise) (layers tangled beyond what the response resolves: the exact
  * projection's cost grows with the square of a zone's impacts); x_out and v
  * are written as they stand. */
 typedef struct {
@@ -314,12 +315,14 @@ typedef struct {
   int32_t changed;     /* 1: a zone was projected (velocities updated) */
   int32_t zones;       /* impact zones at the end */
   int32_t infeasible;  /* projections whose constraints had no solution (zone left in place) */
-  int32_t zone_overflow; /* 1: stopped at a zone of more than 256 impacts */
+  int32_t zone_overflow; /* 1: stopped at a zone larger than the zone limit */
   int64_t impacts;     /* impacts the zones received, over all rounds */
   int64_t projections; /* zone projections */
 } ys_response_info;
 ys_status ys_collider_respond(ys_collider *c, const double *node_mass, double h, double damp, int32_t max_iter,
                               double *x_out, double *v, ys_response_info *info);
+/* The zone limit of ys_collider_respond (default 256 impacts per zone). */
+ys_status ys_collider_set_max_zone_impacts(ys_collider *c, int32_t n);
 /* The impacts the zones received, in order (info.impacts of them); the
  * pair field holds the round that found each. */
 ys_status ys_collider_response_impacts(ys_collider *c, ys_impact *impacts, int64_t cap);

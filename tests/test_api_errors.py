@@ -78,5 +78,8 @@ def test_response_calls_before_a_response_are_argument_errors():
         c.respond_backward(np.zeros((16, 3)))  # no response yet
     assert e.value.status == 1
     with pytest.raises(ys.YarnSimError):
+        c.set_max_zone_impacts(0)
+    c.set_max_zone_impacts(1000)
+    with pytest.raises(ys.YarnSimError):
         c.response_impacts()
     c.close()
