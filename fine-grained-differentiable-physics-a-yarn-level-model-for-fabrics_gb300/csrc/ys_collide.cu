@@ -29,7 +29,8 @@ using ys::Impact;
 using ys::Kdop;
 
 constexpr int kStack = 64;  // traversal stack; deeper trees report an error
-constexpr int kBroadBlock = 32;
+constexpr int kBroadBlock = 64;
+constexpr int kSliceDepth = 4;  // broad-phase slices: up to 16 subtrees per tree
 
 #define YC_CUDA(call)                                                                   \
   do {                                                                                  \
@@ -105,29 +106,39 @@ struct BroadArgs {
   const uint8_t* face_active;
   const uint8_t* node_active;  // cloth-tree nodes with an active leaf below
   float thick1, thick2;        // the thickness and sqrt(2) times it, widened, for the FP32 prune
+  const int* cslice;           // slice roots of the cloth tree, depth-first order
+  const int* oslice;           // and of the obstacle tree
+  int ncs, nos;
 };
 
-// the pairs whose first face is f: cloth faces g the reference reports with
-// f first, then obstacle faces
+// one thread per (cloth face f, slice): the slices are the subtrees rooted at
+// depth kSliceDepth of the cloth tree, then of the obstacle tree, in
+// depth-first order, so a face's pairs come out in the order of one
+// depth-first traversal of both trees: cloth faces g the reference reports
+// with f first, then obstacle faces
 template <bool WRITE>
 __global__ void k_broad(BroadArgs a) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= a.nfaces) return;
-  const Kdop bf = a.cloth.box[a.leaf_of_face[f]];
-  float bfl[18];
-  for (int k = 0; k < 9; ++k) {
-    bfl[k] = __double2float_rd(bf.d[k]);
-    bfl[k + 9] = __double2float_ru(bf.d[k + 9]);
-  }
-  const int uf = a.upper[f], rf = a.rank[f];
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int S = a.ncs + a.nos;
+  if (idx >= (int64_t)a.nfaces * S) return;
+  const int f = (int)(idx / S), sl = (int)(idx % S);
+  const int pass = sl < a.ncs ? 0 : 1;
   const bool fa = a.face_active == nullptr || a.face_active[f] != 0;
-  int64_t c = 0, o = WRITE ? a.offset[f] : 0;
-  int stack[kStack];
-  for (int pass = 0; pass < 2; ++pass) {
+  int64_t c = 0;
+  if (pass == 0 || fa) {
     const DevTree& t = pass == 0 ? a.cloth : a.obs;
-    if (t.nnodes == 0 || (pass == 1 && !fa)) continue;
+    const int root = pass == 0 ? a.cslice[sl] : a.oslice[sl - a.ncs];
+    const Kdop bf = a.cloth.box[a.leaf_of_face[f]];
+    float bfl[18];
+    for (int k = 0; k < 9; ++k) {
+      bfl[k] = __double2float_rd(bf.d[k]);
+      bfl[k + 9] = __double2float_ru(bf.d[k + 9]);
+    }
+    const int uf = a.upper[f], rf = a.rank[f];
+    const int64_t o = WRITE ? a.offset[idx] : 0;
+    int stack[kStack];
     int sp = 0;
-    stack[sp++] = 0;
+    stack[sp++] = root;
     while (sp > 0) {
       const int n = stack[--sp];
       if (!fa && a.node_active[n] == 0) continue;  // pass 0 only: no active face below
@@ -154,7 +165,7 @@ __global__ void k_broad(BroadArgs a) {
       }
     }
   }
-  if (!WRITE) a.count[f] = c;
+  if (!WRITE) a.count[idx] = c;
 }
 
 __global__ void k_narrow(const int* __restrict__ pairs, int64_t npairs, const CFace* __restrict__ faces,
@@ -268,6 +279,8 @@ struct ys_collider {
   double resp_h = 0.0, resp_damp = 0.0;
   bool obs_tree_valid = false;  // the obstacle tree and device copies match hox / hoxp
   int max_zone_impacts = 256;
+  std::vector<int> h_cslice, h_oslice;  // broad-phase slice roots
+  DVec<int> cslice, oslice;
 };
 
 namespace {
@@ -343,7 +356,40 @@ void edges_of(const int* fv, int f, int e[3][2], bool obstacle, const std::vecto
   }
 }
 
+// roots of the subtrees at depth `depth` (and leaves above it), in
+// depth-first order: the broad phase's slices
+std::vector<int> tree_slices(const ys::BvhTree& t, int depth) {
+  std::vector<int> out;
+  if (t.face.empty()) return out;
+  std::vector<int> st{0};
+  while (!st.empty()) {
+    const int n = st.back();
+    st.pop_back();
+    if (t.face[n] >= 0 || t.depth[n] >= depth) {
+      out.push_back(n);
+    } else {
+      st.push_back(t.right[n]);
+      st.push_back(t.left[n]);
+    }
+  }
+  return out;
+}
+
+ys_status upload_slices(ys_collider* c, bool obstacle) {
+  const std::vector<int>& h = obstacle ? c->h_oslice : c->h_cslice;
+  DVec<int>& d = obstacle ? c->oslice : c->cslice;
+  YC_CUDA(d.reserve(std::max<size_t>(h.size(), 1)));
+  if (!h.empty()) YC_CUDA(cudaMemcpyAsync(d.p, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice, c->stream));
+  return YS_OK;
+}
+
 ys_status broad_phase(ys_collider* c, bool masked) {
+  const int ncs = (int)c->h_cslice.size(), nos = (int)c->h_oslice.size();
+  const int64_t work = (int64_t)c->n_faces * (ncs + nos);
+  // the per-(face, slice) counts and offsets: sized before any pointer to
+  // them is taken (a reserve may move them)
+  YC_CUDA(c->counts.reserve(std::max<int64_t>(work, 1)));
+  YC_CUDA(c->offsets.reserve(std::max<int64_t>(work, 1)));
   BroadArgs a{};
   a.cloth = DevTree{c->c_left.p, c->c_right.p, c->c_face.p, c->c_box.p, (int)c->ct.face.size(), c->c_fbox.p};
   a.obs = DevTree{c->o_left.p, c->o_right.p, c->o_face.p, c->o_box.p, (int)c->ot.face.size(), c->o_fbox.p};
@@ -358,21 +404,26 @@ ys_status broad_phase(ys_collider* c, bool masked) {
   a.overflow = c->overflow.p;
   a.face_active = masked ? c->face_active.p : nullptr;
   a.node_active = masked ? c->node_active.p : nullptr;
+  a.cslice = c->cslice.p;
+  a.oslice = c->oslice.p;
+  a.ncs = ncs;
+  a.nos = nos;
   YC_CUDA(cudaMemsetAsync(c->overflow.p, 0, sizeof(int), c->stream));
-  // one warp per block: a cloth has only as many threads as faces (8K at
-  // 64 x 64), and 128-thread blocks left most of the 152 SMs idle
-  const unsigned g = (unsigned)((c->n_faces + kBroadBlock - 1) / kBroadBlock);
-  k_broad<false><<<g, kBroadBlock, 0, c->stream>>>(a);
+  const unsigned g = (unsigned)((work + kBroadBlock - 1) / kBroadBlock);
+  if (work) k_broad<false><<<g, kBroadBlock, 0, c->stream>>>(a);
   YC_CUDA(cudaGetLastError());
-  ys_status s = scan(c, c->counts.p, c->n_faces, c->offsets.p, &c->npairs);
+  ys_status s = scan(c, c->counts.p, work, c->offsets.p, &c->npairs);
   if (s != YS_OK) return s;
   int ovf = 0;
   YC_CUDA(cudaMemcpy(&ovf, c->overflow.p, sizeof(int), cudaMemcpyDeviceToHost));
   if (ovf) return ys_internal_fail(YS_ERR_ARG, "BVH deeper than the traversal stack");
+  // a face pairs at most once with every other face
+  if (c->npairs < 0 || c->npairs > (int64_t)c->n_faces * ((int64_t)c->n_faces + c->n_obs_faces))
+    return ys_internal_fail(YS_ERR_CUDA, "broad phase produced an impossible pair count");
   YC_CUDA(c->pairs.reserve(3 * (size_t)std::max<int64_t>(c->npairs, 1)));
   a.offset = c->offsets.p;
   a.out = c->pairs.p;
-  k_broad<true><<<g, kBroadBlock, 0, c->stream>>>(a);
+  if (work) k_broad<true><<<g, kBroadBlock, 0, c->stream>>>(a);
   YC_CUDA(cudaGetLastError());
   YC_CUDA(cudaStreamSynchronize(c->stream));
   c->have_pairs = true;
@@ -570,6 +621,12 @@ ys_status ys_collider_set_positions(ys_collider* c, const double* x, const doubl
   if (!same_obstacle &&
       (s = upload_tree(c, c->ot, c->o_left, c->o_right, c->o_face, c->o_levels, c->o_box, c->o_level_off)) != YS_OK)
     return s;
+  c->h_cslice = tree_slices(c->ct, kSliceDepth);
+  if ((s = upload_slices(c, false)) != YS_OK) return s;
+  if (!same_obstacle) {
+    c->h_oslice = tree_slices(c->ot, kSliceDepth);
+    if ((s = upload_slices(c, true)) != YS_OK) return s;
+  }
   YC_CUDA(cudaMemcpyAsync(c->c_lof.p, c->ct.leaf_of_face.data(), sizeof(int) * c->n_faces, cudaMemcpyHostToDevice,
                           c->stream));
   YC_CUDA(cudaMemcpyAsync(c->c_rank.p, c->ct.rank.data(), sizeof(int) * c->n_faces, cudaMemcpyHostToDevice, c->stream));
