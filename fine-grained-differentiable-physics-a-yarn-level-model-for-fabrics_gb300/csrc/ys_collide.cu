@@ -128,12 +128,10 @@ __global__ void k_broad(BroadArgs a) {
   if (pass == 0 || fa) {
     const DevTree& t = pass == 0 ? a.cloth : a.obs;
     const int root = pass == 0 ? a.cslice[sl] : a.oslice[sl - a.ncs];
-    const Kdop bf = a.cloth.box[a.leaf_of_face[f]];
-    float bfl[18];
-    for (int k = 0; k < 9; ++k) {
-      bfl[k] = __double2float_rd(bf.d[k]);
-      bfl[k + 9] = __double2float_ru(bf.d[k + 9]);
-    }
+    const int leaf = a.leaf_of_face[f];
+    const Kdop bf = a.cloth.box[leaf];
+    float bfl[18];  // the face's widened box, as refit left it for its leaf
+    for (int k = 0; k < 18; ++k) bfl[k] = a.cloth.fbox[18 * (int64_t)leaf + k];
     const int uf = a.upper[f], rf = a.rank[f];
     const int64_t o = WRITE ? a.offset[idx] : 0;
     int stack[kStack];
