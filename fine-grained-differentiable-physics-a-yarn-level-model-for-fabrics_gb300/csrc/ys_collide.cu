@@ -145,6 +145,8 @@ __global__ void k_broad(BroadArgs a) {
         if (pass == 0) {
           if (g == f || !ys::bvh_first(uf, rf, a.upper[g], a.rank[g])) continue;
         }
+        // the FP32 test first: it rejects only boxes the exact test rejects
+        if (!kdop_overlap_f(bfl, t.fbox + 18 * (int64_t)n, a.thick1, a.thick2)) continue;
         if (!ys::kdop_overlap(bf, t.box[n], a.thickness)) continue;
         if (WRITE) {
           a.out[3 * (o + c)] = f;
