@@ -406,3 +406,38 @@ def test_gpu_tangled_layers_stop_at_the_zone_cap():
         c.respond(v=s["v"], h=s["h"], damp=DAMP)
     assert e.value.status == 4
     c.close()
+
+
+def test_zone_projection_matches_a_general_qp_solver():
+    """The zone projection (least-distance programme through NNLS) against
+    scipy's SLSQP on the primal problem min 1/2 sum a |x - x_old|^2 subject
+    to w n . x >= thickness, for random zones with shared nodes."""
+    from scipy.optimize import minimize
+    rng = np.random.default_rng(4)
+    for trial in range(12):
+        m, k = int(rng.integers(2, 7)), int(rng.integers(1, 6))
+        xold = rng.normal(size=(m, 3)) * 1e-3
+        a = 0.5 + rng.random(m)
+        G = np.zeros((k, 3 * m))
+        h = np.zeros(k)
+        for j in range(k):
+            nodes = rng.choice(m, size=min(m, 3), replace=False)
+            n = rng.normal(size=3)
+            n /= np.linalg.norm(n)
+            w = rng.normal(size=len(nodes))
+            for q, nd in enumerate(nodes):
+                G[j, 3 * nd:3 * nd + 3] += w[q] * n
+            h[j] = 5e-4 - G[j] @ xold.reshape(-1) + 1e-3 * rng.random()  # violated at x_old
+        # our solver in y = sqrt(a) x: min |u| s.t. (G / sqrt(a)) u >= h
+        isa = np.repeat(1.0 / np.sqrt(a), 3)
+        u, lam, st = RC.emu_ldp(G * isa[None, :], h)
+        if st == 1:
+            continue
+        x_ours = xold.reshape(-1) + u * isa
+        res = minimize(lambda x: 0.5 * np.sum(np.repeat(a, 3) * (x - xold.reshape(-1)) ** 2), xold.reshape(-1),
+                       jac=lambda x: np.repeat(a, 3) * (x - xold.reshape(-1)),
+                       constraints=[dict(type="ineq", fun=lambda x: G @ x - (h + G @ xold.reshape(-1)),
+                                         jac=lambda x: G)],
+                       method="SLSQP", options=dict(ftol=1e-16, maxiter=500))
+        assert res.success, res.message
+        assert np.abs(res.x - x_ours).max() <= 1e-8 * max(1.0, np.abs(x_ours).max()) + 1e-10
