@@ -194,34 +194,77 @@ __global__ void k_compact(const Impact* __restrict__ slots, const int64_t* __res
   }
 }
 
-// exclusive scan of counts[n] into offset[n] (+ total), in fixed order
-constexpr int kScanChunk = 1024;
-__global__ void k_scan_chunks(const int64_t* __restrict__ c, int64_t n, int64_t* __restrict__ off,
-                              int64_t* __restrict__ sums) {
-  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t lo = b * kScanChunk;
-  if (lo >= n) return;
-  const int64_t hi = lo + kScanChunk < n ? lo + kScanChunk : n;
-  int64_t s = 0;
-  for (int64_t i = lo; i < hi; ++i) {
-    off[i] = s;
-    s += c[i];
+// exclusive scan of counts[n] into offset[n] (+ total): tiles of kScanTile
+// entries scanned by one block each (8 per thread, then a warp-shuffle scan
+// of the thread sums), the tile sums scanned by one block, then added back;
+// integer sums, so any grouping gives the same offsets
+constexpr int kScanThreads = 256, kScanPer = 8, kScanTile = kScanThreads * kScanPer;
+__device__ __forceinline__ int64_t block_exclusive_scan(int64_t v, int64_t* warp_sums, int64_t* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int64_t incl = v;
+  for (int d = 1; d < 32; d <<= 1) {
+    const int64_t o = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += o;
   }
-  sums[b] = s;
+  if (lane == 31) warp_sums[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    int64_t w = lane < nw ? warp_sums[lane] : 0;
+    int64_t wi = w;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int64_t o = __shfl_up_sync(0xffffffffu, wi, d);
+      if (lane >= d) wi += o;
+    }
+    if (lane < nw) warp_sums[lane] = wi - w;  // exclusive prefix of the warps
+    if (lane == nw - 1) *total = wi;
+  }
+  __syncthreads();
+  return warp_sums[wid] + incl - v;
 }
-__global__ void k_scan_sums(int64_t* sums, int64_t nb, int64_t* total) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  int64_t s = 0;
-  for (int64_t i = 0; i < nb; ++i) {
-    const int64_t v = sums[i];
-    sums[i] = s;
-    s += v;
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int64_t* __restrict__ c, int64_t n,
+                                                             int64_t* __restrict__ off, int64_t* __restrict__ sums) {
+  __shared__ int64_t warp_sums[32];
+  __shared__ int64_t total;
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPer;
+  int64_t v[kScanPer], s = 0;
+  for (int k = 0; k < kScanPer; ++k) {
+    v[k] = base + k < n ? c[base + k] : 0;
+    s += v[k];
   }
-  *total = s;
+  int64_t run = block_exclusive_scan(s, warp_sums, &total);
+  for (int k = 0; k < kScanPer; ++k) {
+    if (base + k < n) off[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+// one block: exclusive scan of the nb tile sums in place (nb up to
+// kScanTile per pass, looped), the grand total in *total
+__global__ void __launch_bounds__(kScanThreads) k_scan_sums(int64_t* sums, int64_t nb, int64_t* total) {
+  __shared__ int64_t warp_sums[32];
+  __shared__ int64_t part;
+  int64_t carry = 0;
+  for (int64_t b0 = 0; b0 < nb; b0 += kScanTile) {
+    const int64_t base = b0 + (int64_t)threadIdx.x * kScanPer;
+    int64_t v[kScanPer], s = 0;
+    for (int k = 0; k < kScanPer; ++k) {
+      v[k] = base + k < nb ? sums[base + k] : 0;
+      s += v[k];
+    }
+    int64_t run = carry + block_exclusive_scan(s, warp_sums, &part);
+    for (int k = 0; k < kScanPer; ++k) {
+      if (base + k < nb) sums[base + k] = run;
+      run += v[k];
+    }
+    carry += part;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
 }
 __global__ void k_scan_add(int64_t* off, int64_t n, const int64_t* __restrict__ sums) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) off[i] += sums[i / kScanChunk];
+  if (i < n) off[i] += sums[i / kScanTile];
 }
 
 template <class T>
@@ -330,12 +373,12 @@ ys_status refit(ys_collider* c, bool obstacle) {
 }
 
 ys_status scan(ys_collider* c, const int64_t* counts, int64_t n, int64_t* off, int64_t* total_host) {
-  const int64_t nb = (n + kScanChunk - 1) / kScanChunk;
+  const int64_t nb = (n + kScanTile - 1) / kScanTile;
   YC_CUDA(c->sums.reserve(std::max<int64_t>(nb, 1)));
   YC_CUDA(c->total.reserve(1));
   if (n > 0) {
-    k_scan_chunks<<<(unsigned)((nb + 127) / 128), 128, 0, c->stream>>>(counts, n, off, c->sums.p);
-    k_scan_sums<<<1, 1, 0, c->stream>>>(c->sums.p, nb, c->total.p);
+    k_scan_tiles<<<(unsigned)nb, kScanThreads, 0, c->stream>>>(counts, n, off, c->sums.p);
+    k_scan_sums<<<1, kScanThreads, 0, c->stream>>>(c->sums.p, nb, c->total.p);
     k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(off, n, c->sums.p);
     YC_CUDA(cudaGetLastError());
     YC_CUDA(cudaMemcpyAsync(total_host, c->total.p, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
