@@ -1,11 +1,12 @@
 // ys_physics.cuh -- per-element yarn forces and Jacobians of one implicit step.
 //
 // Each routine handles one element (edge, bend segment, crossing, shear
-// segment, face) and adds its contribution straight into the step's system
+// segment, face) and returns its contribution to the step's system
 //     A = M - h^2 dF/dx - h dF/dv,   b = h (F - (dF/dv)^T v) + M v
-// (src/TrainHelper.cpp:19-20) in the structured stencil layout of
-// ys_common.cuh. Elements of one launch are graph-coloured so that no two
-// threads touch the same node rows, which keeps the accumulation
+// (src/TrainHelper.cpp:19-20). The record producers (ys_elem_kernels.cuh)
+// write each element's contribution to its own record, and the per-node
+// gathers (ys_items.cuh) sum a node's records in a fixed order into the
+// structured stencil layout of ys_common.cuh, so the accumulation is
 // deterministic without atomics.
 //
 // The arithmetic restates the reference's hand-derived expressions term by

@@ -2,7 +2,8 @@
 # Builds the reference's own physics sources, unmodified, into a serial
 # (no OpenMP) test-oracle executable: oracle/_ref/ref_harness.
 #
-# Reads the sources where they lie (REF_SRC, default /root/reference/src) and
+# Reads the sources where they lie (REF_SRC; unset, oracle/ref/refpath.py
+# locates the checkout) and
 # writes nothing but oracle/_ref/. Needs only g++ and the LibTorch headers and
 # libraries that ship inside the installed torch wheel.
 #
@@ -10,8 +11,10 @@
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/../_ref"
-REF_SRC="${REF_SRC:-/root/reference/src}"
-if [ ! -d "$REF_SRC" ]; then
+if [ -z "${REF_SRC:-}" ]; then
+  REF_SRC="$(cd "$HERE/../.." && python3 -c 'from oracle.ref.refpath import ref_src; print(ref_src() or "")')"
+fi
+if [ -z "$REF_SRC" ] || [ ! -d "$REF_SRC" ]; then
   echo "reference sources not found at $REF_SRC" >&2
   exit 3
 fi

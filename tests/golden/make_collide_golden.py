@@ -11,7 +11,7 @@ other during the step, and a cloth moving into a sphere (an icosphere built
 here). Each fixture holds the inputs, the pair list in emission order and
 the impacts.
 
-Needs the reference sources (default /root/reference/src); run from the repo
+Needs the reference sources (REF_SRC, or where oracle/ref/refpath.py finds them); run from the repo
 root:  python tests/golden/make_collide_golden.py
 """
 from __future__ import annotations

@@ -12,7 +12,7 @@ the predicted forces, the loss, every parameter's gradient and the final
 positions. The goal is the last step of the trajectory file the reference
 ships (tests/golden/h5_wind_yarn12_plain5.npz).
 
-Needs the reference sources (default /root/reference/src); run from the repo
+Needs the reference sources (REF_SRC, or where oracle/ref/refpath.py finds them); run from the repo
 root:  python tests/golden/make_embed_golden.py
 """
 from __future__ import annotations

@@ -7,7 +7,7 @@ restated in oracle/ref/shim/eigen_cg.cpp). This script writes a config per
 case, runs the harness, and stores its per-step states and the dense system
 pieces at selected steps.
 
-Needs the reference sources (default /root/reference/src); run from the repo
+Needs the reference sources (REF_SRC, or where oracle/ref/refpath.py finds them); run from the repo
 root:  python tests/golden/make_golden.py
 """
 from __future__ import annotations

@@ -12,7 +12,7 @@ holds the configuration, the initial state, the ground-truth targets, the
 learned-parameter trajectory, the loss and
 d loss / d (rho0, Y0, B0, rho1, Y1, B1, S, mu).
 
-Needs the reference sources (default /root/reference/src); run from the repo
+Needs the reference sources (REF_SRC, or where oracle/ref/refpath.py finds them); run from the repo
 root:  python tests/golden/make_grad_golden.py
 """
 from __future__ import annotations

@@ -16,6 +16,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, ".."))
+sys.path.insert(0, os.path.join(HERE, "..", ".."))
 from pkg import ys  # noqa: E402
 
 STEPS = 40
@@ -23,7 +24,10 @@ REL = os.path.join("TrainingData", "Table_2", "Wind_Yarn_1_2_Plain_Size5.h5")
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    from oracle.ref.refpath import ref_root
+    root = sys.argv[1] if len(sys.argv) > 1 else ref_root()
+    if root is None:
+        sys.exit("the reference checkout is not here (set REF_ROOT)")
     path = os.path.join(root, REL)
     raw = open(path, "rb").read()
     size, phy = ys.h5.cloth_property_loader_heter(path)

@@ -13,9 +13,10 @@ import pytest
 
 import goldens
 from pkg import gpu_available, ys
+from oracle.ref.refpath import ref_file
 
 GOLDEN = os.path.join(goldens.GOLDEN_DIR, "h5_wind_yarn12_plain5.npz")
-REF_FILE = os.path.join("/root/reference", "TrainingData", "Table_2", "Wind_Yarn_1_2_Plain_Size5.h5")
+REF_FILE = ref_file("TrainingData", "Table_2", "Wind_Yarn_1_2_Plain_Size5.h5")
 KEYS = ("LPos", "LPosFix", "LVel", "EPos", "EPosBar", "EVel")
 
 
@@ -27,7 +28,7 @@ def _physical(g):
     return {str(k): float(v) for k, v in zip(g["physical_names"], g["physical"])}
 
 
-@pytest.mark.skipif(not os.path.exists(REF_FILE), reason="the reference's data file is not here")
+@pytest.mark.skipif(REF_FILE is None, reason="the reference's data file is not here")
 def test_reader_reads_the_reference_file():
     g = _golden()
     assert hashlib.sha256(open(REF_FILE, "rb").read()).hexdigest() == str(g["sha256"])
@@ -40,7 +41,7 @@ def test_reader_reads_the_reference_file():
         assert np.array_equal(head[k], g[k]) and np.array_equal(last[k][0], g["last_" + k])
 
 
-@pytest.mark.skipif(not os.path.exists(REF_FILE), reason="the reference's data file is not here")
+@pytest.mark.skipif(REF_FILE is None, reason="the reference's data file is not here")
 def test_rewritten_reference_file_reads_back_identically(tmp_path):
     a = ys.h5.read(REF_FILE)
     p = str(tmp_path / "copy.h5")
@@ -130,7 +131,7 @@ def test_gpu_first_step_matches_the_reference_data_file():
     b.close()
 
 
-@pytest.mark.skipif(not os.path.exists(REF_FILE), reason="the reference's data file is not here")
+@pytest.mark.skipif(REF_FILE is None, reason="the reference's data file is not here")
 def test_writer_messages_match_the_reference_files(tmp_path):
     """The writer's object-header messages for the reference's datasets equal
     the ones libhdf5 wrote (dataspace, datatype and fill value byte for byte,
