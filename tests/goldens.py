@@ -10,7 +10,7 @@ GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 def names():
     """Trajectory / system fixtures (tests/golden/make_golden.py)."""
     return sorted(n for n in (os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
-                  if not n.startswith(("grad_", "collide_", "h5_", "embed_")))
+                  if not n.startswith(("grad_", "collide_", "h5_", "embed_", "config")))
 
 
 def grad_names():
@@ -46,3 +46,19 @@ def state(g, step):
 def rel(a, b):
     a = np.asarray(a); b = np.asarray(b)
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def config_names():
+    """Benchmark-scale reference fixtures (tests/golden/make_config_golden.py)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN_DIR, "config*.npz")))
+
+
+def rel_comp(a, b, floor=1e-3):
+    """Largest per-component relative error |a - b| / max(|b|, floor * max|b|):
+    every component is held to the tolerance against its own size, except
+    components smaller than `floor` times the field's largest, which are held
+    against that floor (a component that is zero up to round-off has no
+    meaningful relative error of its own)."""
+    a = np.asarray(a); b = np.asarray(b)
+    scale = np.maximum(np.abs(b), floor * max(np.abs(b).max(), 1e-300))
+    return float((np.abs(a - b) / scale).max())
