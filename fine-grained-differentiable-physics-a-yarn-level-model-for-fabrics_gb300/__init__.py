@@ -8,11 +8,12 @@ raises.
 """
 from .buildlib import build, LIB_PATH
 from .cloth import (PI, ClothBatch, ClothSpec, ClothState, Cloth, EigenSolver, Environment, InitPose,
-                    PhysicsCloth, SimStep, Wind, WovenPattern, Yarn)
+                    PhysicsCloth, SimStep, Wind, WovenPattern, Yarn, Adjoint, STATE_KEYS)
 from ._native import YarnSimError, load as load_library, library_path
 from .collide import Collider, Collision, cloth_mesh_topology
 from .learn import (PARAM_NAMES, YarnSimNetHeter, constraint_para, invert_constraint_para, position_loss, rollout,
-                    rollout_with_jacobian, two_yarn_spec)
+                    rollout_with_jacobian, two_yarn_spec, CheckpointedRollout, rollout_adjoint,
+                    two_yarn_param_grad)
 from .precond import LearnedPreconditioner, train as train_preconditioner, training_specs
 from .render import RenderCloth, RenderType, obj_text, render_batch_cloth
 from . import h5
@@ -24,5 +25,5 @@ __all__ = [
     "library_path", "PARAM_NAMES", "YarnSimNetHeter", "constraint_para", "invert_constraint_para", "position_loss",
     "rollout", "rollout_with_jacobian", "two_yarn_spec", "Collider", "Collision", "cloth_mesh_topology",
     "LearnedPreconditioner", "train_preconditioner", "training_specs", "RenderCloth", "RenderType", "obj_text",
-    "render_batch_cloth",
+    "render_batch_cloth", "Adjoint", "STATE_KEYS", "CheckpointedRollout", "rollout_adjoint", "two_yarn_param_grad",
 ]

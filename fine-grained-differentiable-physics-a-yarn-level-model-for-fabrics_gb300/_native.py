@@ -28,7 +28,7 @@ EXPORTED = [
     "ys_gnn_set_params", "ys_gnn_train_step", "ys_gnn_loss_grad", "ys_set_preconditioner", "ys_precond_info",
     "ys_get_system_slots", "ys_tc_gemm_bf16", "ys_precond_refresh", "ys_get_normals", "ys_collider_respond",
     "ys_collider_response_impacts", "ys_collider_respond_backward", "ys_step_tangent_ext",
-    "ys_collider_set_max_zone_impacts",
+    "ys_collider_set_max_zone_impacts", "ys_adjoint_create", "ys_adjoint_destroy", "ys_adjoint_step",
 ]
 YS_PREC_JACOBI, YS_PREC_LEARNED = 0, 1
 YS_TANGENT_EXACT, YS_TANGENT_REFERENCE = 0, 1
@@ -157,9 +157,15 @@ def load(build_if_missing: bool = True):
     L.ys_collider_response_impacts.argtypes = [vp, vp, ctypes.c_int64]
     L.ys_collider_set_max_zone_impacts.argtypes = [vp, ctypes.c_int32]
     L.ys_collider_respond_backward.argtypes = [vp, vp, vp, ctypes.c_int32, vp, vp, vp, vp, vp]
+    L.ys_adjoint_create.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(vp)]
+    L.ys_adjoint_destroy.argtypes = [vp]
+    L.ys_adjoint_destroy.restype = None
+    L.ys_adjoint_step.argtypes = [vp, ctypes.c_double, vp, ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                  ctypes.POINTER(vp), vp, ctypes.c_int32, vp, vp]
     for name in EXPORTED:
         if name not in ("ys_batch_destroy", "ys_last_error", "ys_cloth_node_offset", "ys_cloth_dim",
-                        "ys_tangent_count", "ys_collider_destroy", "ys_gnn_destroy", "ys_gnn_param_count"):
+                        "ys_tangent_count", "ys_collider_destroy", "ys_gnn_destroy", "ys_gnn_param_count",
+                        "ys_adjoint_destroy"):
             getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L

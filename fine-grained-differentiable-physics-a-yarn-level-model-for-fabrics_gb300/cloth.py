@@ -406,6 +406,71 @@ class ClothBatch:
                     launches={n: nl[i] for i, n in enumerate(N.PROF_KINDS)}, total_launches=tot.value)
 
 
+STATE_KEYS = ("LPos", "LVel", "EPos", "EVel", "EPosBar")
+
+
+class Adjoint:
+    """Reverse-mode step of a batch (ys_adjoint_*): turns dL/d(state after a
+    step) into dL/d(state before it), dL/d(material) and dL/d(external force),
+    at a cost independent of how many inputs the gradient is taken for.
+    mode: "exact" (the derivative of the discrete step) or "reference" (the
+    gradient the reference's loss.backward() takes). copies: workspace size
+    (128 copies = one pass per step; fewer copies, more passes)."""
+
+    def __init__(self, batch: ClothBatch, mode="exact", copies: int = 128):
+        self.batch = batch
+        m = {"exact": N.YS_TANGENT_EXACT, "reference": N.YS_TANGENT_REFERENCE}[mode] if isinstance(mode, str) else mode
+        h = ctypes.c_void_p()
+        N.check(N.load().ys_adjoint_create(batch._h, int(m), int(copies), ctypes.byref(h)), "ys_adjoint_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.load().ys_adjoint_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step_back(self, h, g_next=None, ext_force=None, tol=0.0, maxiter=-1, want_ext=False):
+        """One step backwards from the batch's current state (the state at the
+        start of the step; it is left unchanged). g_next: dict of dL/d(state
+        after the step) for STATE_KEYS ([total_nodes, 3|2] numpy; missing = 0).
+        Returns (g_state, g_params, g_ext): g_state the same keys before the
+        step; g_params dict rho, Y, B [total lines] (ys_tangent_seed's line
+        order) and S, mu [n_cloths]; g_ext [total_nodes, 5] or None."""
+        b = self.batch
+        T = b.total_nodes
+        comps = dict(LPos=3, LVel=3, EPos=2, EVel=2, EPosBar=2)
+        keep = []
+        gin = (ctypes.c_void_p * 5)()
+        gout = (ctypes.c_void_p * 5)()
+        out = {}
+        for i, k in enumerate(STATE_KEYS):
+            a = None if g_next is None else g_next.get(k)
+            if a is not None:
+                a = np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(T, comps[k]))
+                keep.append(a)
+                gin[i] = a.ctypes.data
+            out[k] = np.zeros((T, comps[k]))
+            gout[i] = out[k].ctypes.data
+        nl = sum(sp.width + sp.length for sp in b.specs)
+        gp = dict(rho=np.zeros(nl), Y=np.zeros(nl), B=np.zeros(nl), S=np.zeros(b.n_cloths), mu=np.zeros(b.n_cloths))
+        gpp = (ctypes.c_void_p * 5)(*[gp[k].ctypes.data for k in ("rho", "Y", "B", "S", "mu")])
+        gext = np.zeros((T, 5)) if want_ext else None
+        p, f = _ptr(ext_force)
+        if f:
+            raise TypeError("ext_force must be a host array here")
+        st = (N.ClothStats * b.n_cloths)()
+        N.check(N.load().ys_adjoint_step(self._h, float(h), ctypes.c_void_p(p) if p else None, gin, gout, gpp,
+                                         ctypes.c_void_p(gext.ctypes.data) if want_ext else None, 0,
+                                         ctypes.byref(ClothBatch._opts(tol, maxiter, 0)), st), "ys_adjoint_step")
+        return out, gp, gext
+
+
 # ---------------------------------------------------------------------------
 # the reference's single-cloth interface
 # ---------------------------------------------------------------------------

@@ -103,6 +103,15 @@ struct ys_batch {
   } tan;
   int nlines = 0;
   std::vector<double> line_R;  // yarn radius of each line's cloth
+  // construction parameters of every cloth, kept so that an adjoint can
+  // build copies of the batch (ys_adjoint_create); pointers of `d` are
+  // re-aimed at the vectors where a desc is rebuilt
+  struct DescStore {
+    ys_cloth_desc d;
+    std::vector<double> wr, wY, wB, fr, fY, fB;
+    std::vector<int32_t> handles;
+  };
+  std::vector<DescStore> descs;
   // whole-step CUDA graph (ys_use_graphs): assembly, a conditional while node
   // over the PCG iterations, update; rebuilt when its parameters change
   struct Graph {
@@ -269,6 +278,16 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
   b->device = device;
   b->stream = static_cast<cudaStream_t>(cuda_stream);
   b->ncloth = n_cloths;
+  for (int c = 0; c < n_cloths; ++c) {
+    const ys_cloth_desc& d = descs[c];
+    ys_batch::DescStore ds;
+    ds.d = d;
+    ds.wr.assign(d.warp_rho, d.warp_rho + d.length); ds.wY.assign(d.warp_Y, d.warp_Y + d.length);
+    ds.wB.assign(d.warp_B, d.warp_B + d.length); ds.fr.assign(d.weft_rho, d.weft_rho + d.width);
+    ds.fY.assign(d.weft_Y, d.weft_Y + d.width); ds.fB.assign(d.weft_B, d.weft_B + d.width);
+    if (d.n_handles > 0) ds.handles.assign(d.handles, d.handles + 2 * d.n_handles);
+    b->descs.push_back(std::move(ds));
+  }
   // ------------------------------------------------------------ topology
   std::vector<int> node_cloth, node_u, node_v;
   std::vector<uint8_t> flags;
@@ -806,14 +825,18 @@ __global__ void k_spmv_scratch_to_aos(ys::View v, const double* __restrict__ xs,
   for (int k = 0; k < 5; ++k) y[(int64_t)n * 5 + k] = r[k];
 }
 
-// One-time set-up per device, run with that device current: the address of
-// this device's copy of the scratch array. The first call on a device may
-// make the runtime load this module there; make that first call before any
-// stream capture begins.
-ys_status noalloc_scratch(int device, double** out) {
+// The address of this device's copy of the scratch array, looked up with
+// that device current. The first lookup on a device may make the runtime load
+// this module there; make that first call before any stream capture begins.
+// Outside stream capture the address is looked up again on every call (the
+// lookup allocates nothing), so a context that was reset and reloaded the
+// module elsewhere is followed; inside a capture the last address is reused.
+ys_status noalloc_scratch(int device, cudaStream_t stream, double** out) {
   if (device < 0 || device >= kNoAllocMaxDevices) return fail(YS_ERR_ARG, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[device]) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess) cs = cudaStreamCaptureStatusNone;
+  if (!g_noalloc_ptr[device] || cs == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess)
@@ -821,6 +844,24 @@ ys_status noalloc_scratch(int device, double** out) {
     g_noalloc_ptr[device] = static_cast<double*>(p);
   }
   *out = g_noalloc_ptr[device];
+  return YS_OK;
+}
+
+// x and y must be memory of the batch's device (or managed memory): a host
+// array handed to the kernels would fault the device instead of returning an
+// error. cudaPointerGetAttributes allocates nothing.
+ys_status noalloc_check_device_ptr(const void* p, int device, const char* name) {
+  cudaPointerAttributes a{};
+  const cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(YS_ERR_ARG, std::string("ys_apply_system_noalloc: ") + name + " is not a device pointer");
+  }
+  if (a.type == cudaMemoryTypeManaged) return YS_OK;
+  if (a.type != cudaMemoryTypeDevice)
+    return fail(YS_ERR_ARG, std::string("ys_apply_system_noalloc: ") + name + " is not device memory");
+  if (a.device != device)
+    return fail(YS_ERR_ARG, std::string("ys_apply_system_noalloc: ") + name + " is memory of another device");
   return YS_OK;
 }
 
@@ -833,11 +874,17 @@ extern "C" ys_status ys_apply_system_noalloc(ys_batch* b, const double* x, doubl
     return fail(YS_ERR_ARG, "ys_apply_system_noalloc: batch has " + std::to_string(b->ntot) +
                                 " nodes, more than its scratch limit of " + std::to_string(kNoAllocMaxNodes));
   YS_CUDA(cudaSetDevice(b->device));
+  ys_status s = noalloc_check_device_ptr(x, b->device, "x");
+  if (s != YS_OK) return s;
+  s = noalloc_check_device_ptr(y, b->device, "y");
+  if (s != YS_OK) return s;
   double* xs = nullptr;
-  const ys_status s = noalloc_scratch(b->device, &xs);
+  s = noalloc_scratch(b->device, b->stream, &xs);
   if (s != YS_OK) return s;
   const int64_t n = b->ntot;
   const unsigned grid = (unsigned)((n + 255) / 256);
+  // Not timed by the handle's per-phase profile, whose records need CUDA
+  // events: the two launches are counted, their time is in no phase.
   k_to_soa<<<grid, 256, 0, b->stream>>>(x, xs, n, 5);
   k_spmv_scratch_to_aos<<<grid, 256, 0, b->stream>>>(b->v, xs, y);
   b->launches += 2;
@@ -1081,6 +1128,226 @@ ys_status ys_step_tangent_ext(ys_batch* b, double h, const double* ext_force, co
   }
   b->assembled = false;
   return ret;
+}
+
+}  // extern "C"
+
+
+// ------------------------------------------------------------ reverse mode
+struct ys_adjoint {
+  ys_batch* prim = nullptr;  // the caller's batch (not owned)
+  ys_batch* cp = nullptr;    // `copies` copies of prim's cloths, copy-major (owned)
+  int mode = YS_TANGENT_EXACT;
+  int copies = 0, passes = 0;
+  std::vector<void*> allocs;
+  double *q = nullptr, *qbar = nullptr, *lambda = nullptr, *slide_bar = nullptr, *T = nullptr;
+  double* gin[5] = {nullptr};
+  double* gout[5] = {nullptr};
+  double* gline[3] = {nullptr};
+  double* gcloth[2] = {nullptr};
+  double* gext = nullptr;      // [nt][5]
+  double* line_a = nullptr;    // pi R^2 per primal line
+  int* line_kind = nullptr;    // orientation * 3 + position mod 3
+  int* line_cloth = nullptr;
+  template <class T_>
+  ys_status alloc(T_** p, size_t count) {
+    void* m = nullptr;
+    const cudaError_t e = cudaMalloc(&m, std::max<size_t>(count, 1) * sizeof(T_));
+    if (e != cudaSuccess) return fail(YS_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    allocs.push_back(m);
+    *p = static_cast<T_*>(m);
+    return YS_OK;
+  }
+  ~ys_adjoint() {
+    if (prim) cudaSetDevice(prim->device);
+    for (void* m : allocs) cudaFree(m);
+    if (cp) ys_batch_destroy(cp);
+  }
+};
+
+namespace {
+
+constexpr int kStateComps[5] = {3, 3, 2, 2, 2};
+
+__global__ void k_adj_copy_wind(const ys::ClothParams* __restrict__ src, ys::ClothParams* dst, int ncl, int copies) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncl * copies) return;
+  const ys::ClothParams& a = src[t % ncl];
+  ys::ClothParams& d = dst[t];
+  for (int k = 0; k < 3; ++k) d.wind[k] = a.wind[k];
+}
+
+}  // namespace
+
+extern "C" {
+
+ys_status ys_adjoint_create(ys_batch* b, int32_t mode, int32_t copies, ys_adjoint** out) {
+  if (!b || !out) return fail(YS_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (mode != YS_TANGENT_EXACT && mode != YS_TANGENT_REFERENCE)
+    return fail(YS_ERR_ARG, "adjoint mode must be YS_TANGENT_EXACT or YS_TANGENT_REFERENCE");
+  const int ndir = ys::adjoint_direction_count();
+  const int maxc = (ndir + KT - 1) / KT;
+  if (copies < 1 || copies > maxc) return fail(YS_ERR_ARG, "copies must be in [1, 128]");
+  YS_CUDA(cudaSetDevice(b->device));
+  ys_adjoint* a = new ys_adjoint();
+  a->prim = b;
+  a->mode = mode;
+  a->copies = copies;
+  a->passes = (maxc + copies - 1) / copies;
+  // the copies' batch: the same cloths, `copies` times, on b's stream
+  std::vector<ys_cloth_desc> d;
+  d.reserve((size_t)copies * b->ncloth);
+  for (int c = 0; c < copies; ++c)
+    for (const ys_batch::DescStore& ds : b->descs) {
+      ys_cloth_desc e = ds.d;
+      e.warp_rho = ds.wr.data(); e.warp_Y = ds.wY.data(); e.warp_B = ds.wB.data();
+      e.weft_rho = ds.fr.data(); e.weft_Y = ds.fY.data(); e.weft_B = ds.fB.data();
+      e.handles = ds.handles.empty() ? nullptr : ds.handles.data();
+      d.push_back(e);
+    }
+  ys_status st = ys_batch_create((int32_t)d.size(), d.data(), b->device, b->stream, &a->cp);
+  if (st == YS_OK) st = ys_tangent_enable(a->cp, mode);
+  const int64_t nt = b->ntot, ntc = a->cp ? a->cp->ntot : 0;
+  auto A = [&](auto** p, size_t cnt) { if (st == YS_OK) st = a->alloc(p, cnt); };
+  A(&a->q, 5 * nt); A(&a->qbar, 5 * nt); A(&a->lambda, 5 * nt); A(&a->slide_bar, 2 * nt);
+  A(&a->T, (size_t)KT * ntc);
+  for (int i = 0; i < 5; ++i) { A(&a->gin[i], kStateComps[i] * nt); A(&a->gout[i], kStateComps[i] * nt); }
+  for (int i = 0; i < 3; ++i) A(&a->gline[i], b->nlines);
+  for (int i = 0; i < 2; ++i) A(&a->gcloth[i], b->ncloth);
+  A(&a->gext, 5 * nt);
+  A(&a->line_a, b->nlines); A(&a->line_kind, b->nlines); A(&a->line_cloth, b->nlines);
+  if (st != YS_OK) { delete a; return st; }
+  std::vector<double> la;
+  std::vector<int> lk, lc;
+  for (int c = 0; c < b->ncloth; ++c) {
+    const ys::ClothParams& P = b->cp[c];
+    for (int v = 0; v < P.H; ++v) { lk.push_back(0 * 3 + v % 3); lc.push_back(c); la.push_back(ys::kPi * P.R * P.R); }
+    for (int u = 0; u < P.W; ++u) { lk.push_back(1 * 3 + u % 3); lc.push_back(c); la.push_back(ys::kPi * P.R * P.R); }
+  }
+  if (cudaMemcpy(a->line_a, la.data(), sizeof(double) * la.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(a->line_kind, lk.data(), sizeof(int) * lk.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(a->line_cloth, lc.data(), sizeof(int) * lc.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+    delete a;
+    return fail(YS_ERR_CUDA, "cudaMemcpy of the adjoint's line tables failed");
+  }
+  *out = a;
+  return YS_OK;
+}
+
+void ys_adjoint_destroy(ys_adjoint* a) { delete a; }
+
+ys_status ys_adjoint_step(ys_adjoint* a, double h, const double* ext_force, const double* const* gin,
+                          double* const* gout, double* const* gparams, double* gext, int32_t flags,
+                          const ys_solve_opts* opts, ys_cloth_stats* stats) {
+  if (!a || !(h > 0)) return fail(YS_ERR_ARG, "bad argument");
+  ys_batch* b = a->prim;
+  ys_batch* c = a->cp;
+  YS_CUDA(cudaSetDevice(b->device));
+  cudaStream_t s = b->stream;
+  const int64_t nt = b->ntot, ntc = c->ntot;
+  // 1. the forward step's system and solution at the current state
+  ys_status st = ys_assemble(b, h, ext_force, flags);
+  if (st != YS_OK) return st;
+  st = solve_impl(b, b->v, opts, stats);
+  if (st == YS_ERR_ARG || st == YS_ERR_CUDA) return st;
+  if (st == YS_ERR_NONFINITE) return fail(YS_ERR_NONFINITE, "ys_adjoint_step: the forward step is not finite");
+  YS_CUDA(cudaMemcpyAsync(a->q, b->so.x, sizeof(double) * 5 * nt, cudaMemcpyDeviceToDevice, s));
+  // 2. the update's transpose
+  for (int i = 0; i < 5; ++i) {
+    if (gin && gin[i]) {
+      st = upload_soa(b, gin[i], a->gin[i], kStateComps[i], flags);
+      if (st != YS_OK) return st;
+    } else {
+      YS_CUDA(cudaMemsetAsync(a->gin[i], 0, sizeof(double) * kStateComps[i] * nt, s));
+    }
+  }
+  ys::AdjIO io{};
+  for (int i = 0; i < 5; ++i) { io.gin[i] = a->gin[i]; io.gout[i] = a->gout[i]; }
+  b->v.h = h;
+  b->run(YS_PROF_MISC, 1, [&] { ys::launch_adj_update(b->v, io, a->q, a->qbar, a->slide_bar, s); });
+  YS_CUDA(cudaGetLastError());
+  // 3. lambda = A^-T q_bar (exact) or A^-1 q_bar (the reference's backward)
+  {
+    ys::View vl = b->v;
+    vl.B = a->qbar;
+    b->so.trans = a->mode == YS_TANGENT_EXACT ? 1 : 0;
+    st = solve_impl(b, vl, opts, nullptr);
+    b->so.trans = 0;
+    if (st == YS_ERR_ARG || st == YS_ERR_CUDA) return st;
+    if (st == YS_ERR_NONFINITE) return fail(YS_ERR_NONFINITE, "ys_adjoint_step: the adjoint solve is not finite");
+    YS_CUDA(cudaMemcpyAsync(a->lambda, b->so.x, sizeof(double) * 5 * nt, cudaMemcpyDeviceToDevice, s));
+    YS_CUDA(cudaMemcpyAsync(b->so.x, a->q, sizeof(double) * 5 * nt, cudaMemcpyDeviceToDevice, s));
+  }
+  // 4. the copies take the state, wind, step size and external force
+  {
+    ys::View& vc = c->v;
+    const ys::View& vb = b->v;
+    const int cps = a->copies;
+    b->run(YS_PROF_MISC, 7, [&] {
+      ys::launch_adj_broadcast(vb.X, vc.X, (int)nt, 3, cps, s);
+      ys::launch_adj_broadcast(vb.V, vc.V, (int)nt, 3, cps, s);
+      ys::launch_adj_broadcast(vb.XF, vc.XF, (int)nt, 3, cps, s);
+      ys::launch_adj_broadcast(vb.UV, vc.UV, (int)nt, 2, cps, s);
+      ys::launch_adj_broadcast(vb.UVD, vc.UVD, (int)nt, 2, cps, s);
+      ys::launch_adj_broadcast(vb.UVB, vc.UVB, (int)nt, 2, cps, s);
+      k_adj_copy_wind<<<(b->ncloth * cps + 127) / 128, 128, 0, s>>>(vb.cp, const_cast<ys::ClothParams*>(vc.cp),
+                                                                     b->ncloth, cps);
+    });
+    vc.h = h;
+    vc.ext = nullptr;
+    if (ext_force) {
+      b->run(YS_PROF_MISC, 1, [&] { ys::launch_adj_broadcast(b->ext, c->ext, (int)nt, 5, cps, s); });
+      vc.ext = c->ext;
+    }
+    YS_CUDA(cudaGetLastError());
+  }
+  // 5. the residual's vector-Jacobian product, pass by pass
+  for (int i = 0; i < 3; ++i) YS_CUDA(cudaMemsetAsync(a->gline[i], 0, sizeof(double) * b->nlines, s));
+  for (int i = 0; i < 2; ++i) YS_CUDA(cudaMemsetAsync(a->gcloth[i], 0, sizeof(double) * b->ncloth, s));
+  ys::AdjParamOut gp{{a->gline[0], a->gline[1], a->gline[2]}, {a->gcloth[0], a->gcloth[1]}};
+  ys_batch::Tan& t = c->tan;
+  ys::AdjSeeds sd{t.dX, t.dV, t.dUV, t.dUVD, t.dUVB, t.drho, t.dks, t.dkb, t.dS, t.dmu};
+  ys::View dv = dual_view(c);
+  ys::Records dr = c->rec;
+  dr.dedge = t.dedge; dr.dbend = t.dbend; dr.dface = t.dface; dr.dshear = t.dshear;
+  for (int p = 0; p < a->passes; ++p) {
+    const int base = p * a->copies;
+    b->run(YS_PROF_MISC, 2, [&] {
+      ys::launch_adj_seed(c->v, (int)nt, b->nlines, b->ncloth, base, a->line_a, a->line_kind, sd, s);
+    });
+    b->run(YS_PROF_MISC, 7, [&] { ys::launch_assembly_dual(dv, dr, c->anchors, c->geom_n, s); });
+    b->run(YS_PROF_MISC, 2, [&] {
+      ys::launch_adj_broadcast(a->q, t.qsave, (int)nt, 5, a->copies, s);
+      ys::launch_tangent_rhs(dv, t.qsave, t.rt, KT, s);
+    });
+    b->run(YS_PROF_MISC, 3, [&] {
+      ys::launch_adj_contract(dv, (int)nt, a->lambda, a->slide_bar, t.rt, a->T, s);
+      ys::launch_adj_gather(b->v, base, a->copies, a->T, ntc, a->line_cloth, a->line_kind, io, gp, s);
+    });
+    YS_CUDA(cudaGetLastError());
+  }
+  // 6. outputs
+  for (int i = 0; i < 5; ++i)
+    if (gout && gout[i]) {
+      st = download_aos(b, a->gout[i], gout[i], kStateComps[i], flags);
+      if (st != YS_OK) return st;
+    }
+  const cudaMemcpyKind dk = (flags & YS_ON_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (gparams) {
+    for (int i = 0; i < 3; ++i)
+      if (gparams[i]) YS_CUDA(cudaMemcpyAsync(gparams[i], a->gline[i], sizeof(double) * b->nlines, dk, s));
+    for (int i = 0; i < 2; ++i)
+      if (gparams[3 + i]) YS_CUDA(cudaMemcpyAsync(gparams[3 + i], a->gcloth[i], sizeof(double) * b->ncloth, dk, s));
+  }
+  if (gext) {
+    b->run(YS_PROF_MISC, 1, [&] { ys::launch_adj_ext(b->v, a->lambda, a->gext, s); });
+    YS_CUDA(cudaMemcpyAsync(gext, a->gext, sizeof(double) * 5 * nt, dk, s));
+  }
+  YS_CUDA(cudaStreamSynchronize(s));
+  YS_CUDA(cudaGetLastError());
+  b->assembled = false;
+  return YS_OK;
 }
 
 }  // extern "C"

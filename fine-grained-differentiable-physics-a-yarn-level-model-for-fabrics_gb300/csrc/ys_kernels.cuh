@@ -87,4 +87,34 @@ void launch_tangent_ext(const View& v, const double* dext, double* rt, double h,
 void launch_update_dual(const View& v, const Blocks& b, const Solver& so, const double* dq, const TangentState& ts,
                         cudaStream_t s);
 
+// ---- reverse-mode step (ys_adjoint.cu)
+// state adjoints, component-major: [0] LPos [3][nt], [1] LVel [3][nt],
+// [2] EPos [2][nt], [3] EVel [2][nt], [4] EPosBar [2][nt]
+struct AdjIO {
+  const double* gin[5];  // dL/d(state after the step)
+  double* gout[5];       // dL/d(state before the step)
+};
+// the forward-mode seeds of the copies' batch (its tangent arrays)
+struct AdjSeeds {
+  double *dX, *dV, *dUV, *dUVD, *dUVB;
+  double *drho, *dks, *dkb, *dS, *dmu;
+};
+// material adjoints, accumulated: line[p][l] for p = rho, Y, B of primal
+// line l; cloth[p][c] for p = S, mu
+struct AdjParamOut {
+  double* line[3];
+  double* cloth[2];
+};
+int adjoint_direction_count();
+void launch_adj_update(const View& v, const AdjIO& io, const double* q, double* qbar, double* slide_bar,
+                       cudaStream_t s);
+void launch_adj_broadcast(const double* src, double* dst, int nt, int ncomp, int copies, cudaStream_t s);
+void launch_adj_seed(const View& vc, int nt, int nl, int ncl, int base, const double* line_a, const int* line_kind,
+                     const AdjSeeds& sd, cudaStream_t s);
+void launch_adj_contract(const View& vc, int nt, const double* lambda, const double* slide_bar, const double* rt,
+                         double* T, cudaStream_t s);
+void launch_adj_gather(const View& v, int base, int copies, const double* T, int64_t ntc, const int* line_cloth,
+                       const int* line_kind, const AdjIO& io, const AdjParamOut& gp, cudaStream_t s);
+void launch_adj_ext(const View& v, const double* lambda, double* gext, cudaStream_t s);
+
 }  // namespace ys

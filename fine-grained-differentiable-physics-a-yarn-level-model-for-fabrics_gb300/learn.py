@@ -30,7 +30,7 @@ from typing import Dict, Optional, Sequence, Tuple
 import numpy as np
 
 from . import _native as N
-from .cloth import ClothBatch, ClothSpec, InitPose, WovenPattern
+from .cloth import STATE_KEYS, Adjoint, ClothBatch, ClothSpec, InitPose, WovenPattern
 
 PARAM_NAMES = ("rho0", "Y0", "B0", "rho1", "Y1", "B1", "S", "mu")
 MODES = {"exact": N.YS_TANGENT_EXACT, "reference": N.YS_TANGENT_REFERENCE}
@@ -159,6 +159,162 @@ def rollout(theta, template: Dict, state0: Dict, steps: int, h: float = 1e-3, mo
     if _ROLLOUT is None:
         _ROLLOUT = _rollout_function()
     return _ROLLOUT.apply(theta, template, state0, steps, h, mode, tol)
+
+
+class CheckpointedRollout:
+    """A rollout of a batch whose gradient is taken in reverse mode
+    (ys_adjoint_step) with checkpoints: the forward pass keeps the state every
+    `checkpoint_every` steps (plus the trajectory it returns); the backward
+    pass steps each segment again from its checkpoint, last segment first,
+    and runs the adjoint steps of the segment backwards. Memory: one state
+    per checkpoint and the states of one segment, whatever the rollout's
+    length. The reference's loss.backward() keeps the graph of every step
+    instead (src/TrainHeter.h:160-231).
+
+    ext_forces: None, or a list of [total_nodes, 5] arrays (None entries: no
+    force) for steps 0..steps-1 -- per-node control forces."""
+
+    FULL = ("LPos", "LPosFix", "LVel", "EPos", "EPosBar", "EVel")
+
+    def __init__(self, batch: ClothBatch, state0: Dict, steps: int, h: float = 1e-3, ext_forces=None,
+                 mode: str = "exact", checkpoint_every: int = 20, tol: float = 0.0, copies: int = 128):
+        self.batch, self.steps, self.h, self.mode, self.tol = batch, int(steps), float(h), mode, tol
+        self.k = max(1, int(checkpoint_every))
+        self.ext = ext_forces
+        self.state0 = {k: np.array(state0[k], dtype=np.float64) for k in self.FULL if k in state0}
+        self.copies = copies
+        self.checkpoints = {}
+        self.ok = True
+
+    def _ext(self, s):
+        if self.ext is None:
+            return None
+        e = self.ext[s]
+        return None if e is None else np.ascontiguousarray(np.asarray(e, dtype=np.float64))
+
+    def forward(self) -> Dict[str, np.ndarray]:
+        """Runs the rollout; returns the state after every step, dict of
+        [steps, total_nodes, 3|2] arrays for STATE_KEYS."""
+        b = self.batch
+        b.set_state(**self.state0)
+        traj = {k: [] for k in STATE_KEYS}
+        for s in range(self.steps):
+            if s % self.k == 0:
+                self.checkpoints[s] = b.get_state()
+            st = b.step(self.h, self._ext(s), tol=self.tol)
+            self.ok = self.ok and all(x["ok"] for x in st)
+            cur = b.get_state()
+            for k in STATE_KEYS:
+                traj[k].append(cur[k])
+        return {k: np.array(v) for k, v in traj.items()}
+
+    def backward(self, g_traj: Dict[str, np.ndarray], want_ext: bool = False):
+        """g_traj: dL/d(state after step s) as [steps, total_nodes, 3|2]
+        arrays (missing keys: 0). Returns dict(state0=..., rho, Y, B [lines],
+        S, mu [cloths] summed over the steps, ext=[steps, total_nodes, 5] or
+        None)."""
+        b = self.batch
+        adj = Adjoint(b, self.mode, self.copies)
+        try:
+            T = b.total_nodes
+            comps = dict(LPos=3, LVel=3, EPos=2, EVel=2, EPosBar=2)
+            nl = sum(sp.width + sp.length for sp in b.specs)
+            acc = dict(rho=np.zeros(nl), Y=np.zeros(nl), B=np.zeros(nl), S=np.zeros(b.n_cloths),
+                       mu=np.zeros(b.n_cloths))
+            gext = np.zeros((self.steps, T, 5)) if want_ext else None
+
+            def injected(s):  # dL/d(state after step s), s = 1..steps
+                return {k: np.asarray(g_traj[k][s - 1], dtype=np.float64) for k in STATE_KEYS if k in g_traj}
+
+            g = {k: np.zeros((T, comps[k])) for k in STATE_KEYS}
+            for k, v in injected(self.steps).items():
+                g[k] = g[k] + v
+            for a in reversed(sorted(self.checkpoints)):
+                e = min(a + self.k, self.steps)
+                # states at the start of steps a .. e-1, stepped again from the checkpoint
+                b.set_state(**self.checkpoints[a])
+                seg = []
+                for s in range(a, e):
+                    seg.append(b.get_state())
+                    if s + 1 < e:
+                        b.step(self.h, self._ext(s), tol=self.tol)
+                for s in range(e - 1, a - 1, -1):
+                    b.set_state(**seg[s - a])
+                    gs, gp, ge = adj.step_back(self.h, g, self._ext(s), tol=self.tol, want_ext=want_ext)
+                    for k in acc:
+                        acc[k] += gp[k]
+                    if want_ext:
+                        gext[s] = ge
+                    g = gs
+                    if s >= 1:
+                        for k, v in injected(s).items():
+                            g[k] = g[k] + v
+            out = dict(acc)
+            out["state0"] = g
+            out["ext"] = gext
+            return out
+        finally:
+            adj.close()
+
+
+def two_yarn_param_grad(spec: ClothSpec, g: Dict[str, np.ndarray]) -> np.ndarray:
+    """Per-line material gradients of a two-yarn cloth (one cloth) gathered
+    into PARAM_NAMES order: yarn type t's rho, Y, B sum the lines of parity t
+    (warp line j, weft line i take type j % 2, i % 2)."""
+    parity = np.array([j % 2 for j in range(spec.length)] + [i % 2 for i in range(spec.width)])
+    out = []
+    for t in (0, 1):
+        for k in ("rho", "Y", "B"):
+            out.append(float(g[k][parity == t].sum()))
+    out.append(float(g["S"].sum()))
+    out.append(float(g["mu"].sum()))
+    return np.array(out)
+
+
+def _adjoint_rollout_function():
+    import torch
+
+    class AdjointRollout(torch.autograd.Function):
+        """traj_x, traj_e = AdjointRollout.apply(theta, template, state0, steps, h, mode, tol, k):
+        the rollout's positions as a differentiable function of theta
+        (PARAM_NAMES order), with the gradient taken in reverse mode
+        (CheckpointedRollout, a checkpoint every k steps)."""
+
+        @staticmethod
+        def forward(ctx, theta, template, state0, steps, h, mode, tol, k):
+            th = theta.detach().cpu().numpy().astype(np.float64)
+            spec = two_yarn_spec(template, th)
+            batch = ClothBatch([spec])
+            ro = CheckpointedRollout(batch, state0, steps, h, mode=mode, checkpoint_every=k, tol=tol)
+            traj = ro.forward()
+            ctx.ro, ctx.spec = ro, spec
+            dev = theta.device
+            return torch.as_tensor(traj["LPos"], device=dev), torch.as_tensor(traj["EPos"], device=dev)
+
+        @staticmethod
+        def backward(ctx, gx, ge):
+            ro = ctx.ro
+            try:
+                g = ro.backward({"LPos": gx.detach().cpu().numpy(), "EPos": ge.detach().cpu().numpy()})
+            finally:
+                ro.batch.close()
+            gt = torch.as_tensor(two_yarn_param_grad(ctx.spec, g), dtype=gx.dtype, device=gx.device)
+            return gt, None, None, None, None, None, None, None
+
+    return AdjointRollout
+
+
+_ADJ_ROLLOUT = None
+
+
+def rollout_adjoint(theta, template: Dict, state0: Dict, steps: int, h: float = 1e-3, mode: str = "exact",
+                    tol: float = 0.0, checkpoint_every: int = 20):
+    """Differentiable rollout whose backward is the reverse-mode adjoint with
+    checkpoints (see AdjointRollout); same outputs as rollout()."""
+    global _ADJ_ROLLOUT
+    if _ADJ_ROLLOUT is None:
+        _ADJ_ROLLOUT = _adjoint_rollout_function()
+    return _ADJ_ROLLOUT.apply(theta, template, state0, steps, h, mode, tol, checkpoint_every)
 
 
 def _module_base():

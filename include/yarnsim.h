@@ -176,8 +176,12 @@ ys_status ys_apply_system(ys_batch *b, const double *x, double *y, int32_t flags
  * buffer of the batch: its working memory is one static per-device scratch
  * array holding at most 65,536 nodes (YS_ERR_ARG above that). Nothing in the
  * scratch needs to start at zero. Calls that overlap in time on one device
- * share that scratch and race. The first call on a device does a one-time
- * set-up (symbol lookup); make it before any stream capture begins. */
+ * share that scratch and race. The first call on a device looks up the
+ * scratch's address (the runtime may load the library's device code then);
+ * make it before any stream capture begins. x or y that is not memory of the
+ * batch's device (or managed memory) gives YS_ERR_ARG and launches nothing.
+ * With profiling on (ys_profile) its two launches are counted but timed in
+ * no phase: timing would need CUDA events. */
 ys_status ys_apply_system_noalloc(ys_batch *b, const double *x, double *y);
 /* Waits for the handle's stream. */
 ys_status ys_synchronize(ys_batch *b);
@@ -221,6 +225,40 @@ ys_status ys_step_tangent(ys_batch *b, double h, const double *ext_force, int32_
  * tangent directions (ForceNet's lift and drag, src/TrainEmbed.h:96-163). */
 ys_status ys_step_tangent_ext(ys_batch *b, double h, const double *ext_force, const double *dext_force, int32_t flags,
                               const ys_solve_opts *opts, int32_t kact, ys_cloth_stats *stats);
+
+/* ---- Reverse mode: the adjoint of one step.
+ * Replaces the backward pass of the reference's loss.backward() through a
+ * rollout (src/TrainHeter.h:194-231, src/TrainControl.h:192-231), i.e.
+ * EigenSolver's backward (src/Solvers.cpp:33-58) plus autograd through
+ * FillMV's force terms, for any number of inputs at a cost independent of
+ * their number: per-node control forces at every step, the state, the
+ * materials. One call turns dL/d(state after a step) into dL/d(state
+ * before it), dL/d(materials) and dL/d(external force of that step):
+ *   q_bar from the update's transpose; lambda = A^-T q_bar (YS_TANGENT_EXACT:
+ *   the derivative of the discrete step) or A^-1 q_bar
+ *   (YS_TANGENT_REFERENCE: what the reference's autograd computes, A, M and
+ *   dF/dv held constant); then -lambda^T d(A q - b) / d(state, materials)
+ *   by forward-mode directional derivatives of the residual on copies of the
+ *   cloths (512 directions per step, 4 per copy), compressed by a colouring
+ *   of the nodes (row blocks depend on nodes within grid distance 4).
+ * The adjoint owns a workspace batch of `copies` copies of b's cloths
+ * (about 25 KB per copied node); 512 / (4 copies) passes per step. */
+typedef struct ys_adjoint ys_adjoint;
+/* copies: 1..128 (128: one pass per step). b must outlive the adjoint. */
+ys_status ys_adjoint_create(ys_batch *b, int32_t mode, int32_t copies, ys_adjoint **out);
+void ys_adjoint_destroy(ys_adjoint *a);
+/* One step backwards from the state b holds now (the state at the start of
+ * the step, as ys_set_state left it; b's state is not changed). h, ext_force
+ * and opts as ys_step. gin[5] = dL/d(LPos, LVel, EPos, EVel, EPosBar after the
+ * step) in ys_set_state's node layout ([total_nodes][3|2]; NULL = 0);
+ * gout[5] receives dL/d(the same, before the step) (NULL = not returned).
+ * gparams[5] (NULL entries skipped) receive dL/d rho, dL/d Y, dL/d B per yarn
+ * line ([total lines], ys_tangent_seed's order) and dL/d S, dL/d mu per cloth;
+ * gext [total_nodes][5] receives dL/d ext_force (0 where the step ignores
+ * it). flags: YS_ON_DEVICE for device arrays. stats: the forward solve. */
+ys_status ys_adjoint_step(ys_adjoint *a, double h, const double *ext_force, const double *const *gin,
+                          double *const *gout, double *const *gparams, double *gext, int32_t flags,
+                          const ys_solve_opts *opts, ys_cloth_stats *stats);
 
 /* Kernel accounting (no counterpart in the reference). Kernel classes: */
 enum {

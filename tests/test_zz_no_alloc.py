@@ -102,3 +102,25 @@ def test_rejects_batches_beyond_scratch_limit():
     assert st == N.YS_ERR_ARG
     assert "scratch limit" in N.last_error()
     b.close()
+
+
+def test_rejects_host_arrays():
+    """A host array in place of x or y is refused before anything launches."""
+    import torch
+    specs = [spec_from_golden(goldens.load("satin7x5_flat_pert"))]
+    b = ys.ClothBatch(specs)
+    b.assemble(1e-3)
+    L = N.load()
+    n = b.total_nodes
+    x_dev = torch.zeros((n, 5), dtype=torch.float64, device="cuda")
+    y_dev = torch.zeros_like(x_dev)
+    x_host = np.zeros((n, 5))
+    y_host = np.zeros((n, 5))
+    hp = lambda a: ctypes.c_void_p(a.ctypes.data)  # noqa: E731
+    before = b.profile_read(reset=False)["total_launches"]
+    assert L.ys_apply_system_noalloc(b._h, hp(x_host), _ptr(y_dev)) == N.YS_ERR_ARG
+    assert "x is not" in N.last_error()
+    assert L.ys_apply_system_noalloc(b._h, _ptr(x_dev), hp(y_host)) == N.YS_ERR_ARG
+    assert "y is not" in N.last_error()
+    assert b.profile_read(reset=False)["total_launches"] == before
+    b.close()
