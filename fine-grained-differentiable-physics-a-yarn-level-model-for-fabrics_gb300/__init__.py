@@ -18,6 +18,8 @@ from .precond import LearnedPreconditioner, train as train_preconditioner, train
 from .render import RenderCloth, RenderType, obj_text, render_batch_cloth
 from . import h5
 from . import control
+from . import drivers
+from .drivers import DropOnSphere, sim_collision, sim_control, sim_heter, sim_homo
 
 __all__ = [
     "build", "LIB_PATH", "PI", "ClothBatch", "ClothSpec", "ClothState", "Cloth", "EigenSolver", "Environment",
@@ -25,5 +27,6 @@ __all__ = [
     "library_path", "PARAM_NAMES", "YarnSimNetHeter", "constraint_para", "invert_constraint_para", "position_loss",
     "rollout", "rollout_with_jacobian", "two_yarn_spec", "Collider", "Collision", "cloth_mesh_topology",
     "LearnedPreconditioner", "train_preconditioner", "training_specs", "RenderCloth", "RenderType", "obj_text",
-    "render_batch_cloth", "Adjoint", "STATE_KEYS", "CheckpointedRollout", "rollout_adjoint", "two_yarn_param_grad",
+    "render_batch_cloth", "drivers", "DropOnSphere", "sim_collision", "sim_control", "sim_heter", "sim_homo",
+    "Adjoint", "STATE_KEYS", "CheckpointedRollout", "rollout_adjoint", "two_yarn_param_grad",
 ]

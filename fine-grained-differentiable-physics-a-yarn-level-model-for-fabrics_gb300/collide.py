@@ -128,7 +128,7 @@ class Collider:
         zones and their exact inelastic projections, then v + damp (x - x_before)
         / h when a zone moved. v [n, 3] and mass [n] are optional. Returns
         dict(x, v, rounds, converged, changed, zones, infeasible, zone_overflow,
-        impacts, projections); raises when max_iter rounds still found impacts
+        impacts, projections, reverted); raises when max_iter rounds still found impacts
         (where the reference exits) or a zone outgrew the zone limit
         (set_max_zone_impacts), unless check=False."""
         x = np.zeros((self.n_nodes, 3))
@@ -144,7 +144,7 @@ class Collider:
         self._n_received = int(info.impacts)
         return dict(x=x, v=vv, rounds=info.rounds, converged=bool(info.converged), changed=bool(info.changed),
                     zones=info.zones, infeasible=info.infeasible, zone_overflow=bool(info.zone_overflow),
-                    impacts=info.impacts, projections=info.projections)
+                    impacts=info.impacts, projections=info.projections, reverted=info.reverted)
 
     def response_impacts(self) -> dict:
         """The impacts the zones of the last response received, in order

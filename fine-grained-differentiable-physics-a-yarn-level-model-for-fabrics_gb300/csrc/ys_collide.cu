@@ -321,7 +321,7 @@ struct ys_collider {
   bool have_response = false;
   double resp_h = 0.0, resp_damp = 0.0;
   bool obs_tree_valid = false;  // the obstacle tree and device copies match hox / hoxp
-  int max_zone_impacts = 256;
+  int max_zone_impacts = 65536;
   std::vector<int> h_cslice, h_oslice;  // broad-phase slice roots
   DVec<int> cslice, oslice;
 };
@@ -815,6 +815,7 @@ ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h,
     info->zone_overflow = R.zone_overflow;
     info->impacts = (int64_t)R.accepted.size();
     info->projections = (int64_t)R.tape.size();
+    info->reverted = R.reverted;
   }
   if (R.zone_overflow)
     return ys_internal_fail(YS_ERR_MAXITER, "collision response stopped: an impact zone outgrew the zone limit "

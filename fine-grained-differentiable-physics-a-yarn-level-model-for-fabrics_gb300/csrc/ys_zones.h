@@ -20,7 +20,9 @@
 // which stops at its tolerances; here the projection is solved exactly as a
 // least-distance programme (Lawson and Hanson, "Solving Least Squares
 // Problems", 1974, ch. 23) through their non-negative least squares
-// (ch. 23, algorithm NNLS), both restated below. Ties in time, which the
+// (ch. 23, algorithm NNLS), both restated below, for zones of up to
+// exact_zone_impacts impacts, and by Hildreth's dual coordinate ascent on the
+// same programme to 1e-13 relative for larger zones. Ties in time, which the
 // reference leaves to its threads' emission order and std::sort, are broken
 // by type, nodes, weights and normal so the result does not depend on the
 // order of detection.
@@ -328,6 +330,67 @@ inline int ldp(int n, int k, const double* G, const double* h, double* u, double
   return st ? 2 : 0;
 }
 
+// The same least-distance programme for a large zone, with G sparse: row j
+// has up to 4 blocks (column block cols[4 j + q] of 3 entries
+// coef[12 j + 3 q + c]; cols < 0: unused). Hildreth's method (C. Hildreth,
+// "A quadratic programming procedure", Naval Research Logistics Quarterly,
+// 1957): coordinate ascent on the dual max_{lam >= 0} h^T lam - |G^T lam|^2 / 2
+// with u = G^T lam kept current, rows swept in order, until a sweep changes no
+// multiplier by more than tol relative and no constraint is violated by more
+// than tol (h scaled to unit maximum). Each sweep costs O(rows); the exact
+// NNLS costs O(n k^2). Returns 0, or 2 if max_sweeps passed without
+// convergence (u and lam from the last sweep).
+inline int ldp_sparse(int n, int k, const int* cols, const double* coef, const double* h, double* u, double* lam,
+                      double tol = 1e-13, int max_sweeps = 200000) {
+  double s = 0.0;
+  for (int j = 0; j < k; ++j) s = std::max(s, h[j]);
+  for (int i = 0; i < n; ++i) u[i] = 0.0;
+  for (int j = 0; j < k; ++j) lam[j] = 0.0;
+  if (!(s > 0.0)) return 0;
+  std::vector<double> g2(k, 0.0), hs(k);
+  for (int j = 0; j < k; ++j) {
+    hs[j] = h[j] / s;
+    for (int q = 0; q < 4; ++q)
+      if (cols[4 * j + q] >= 0)
+        for (int c = 0; c < 3; ++c) g2[j] += coef[12 * j + 3 * q + c] * coef[12 * j + 3 * q + c];
+  }
+  auto row_dot = [&](int j) {
+    double d = 0.0;
+    for (int q = 0; q < 4; ++q) {
+      const int b = cols[4 * j + q];
+      if (b < 0) continue;
+      for (int c = 0; c < 3; ++c) d += coef[12 * j + 3 * q + c] * u[3 * b + c];
+    }
+    return d;
+  };
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    double change = 0.0, lmax = 0.0;
+    for (int j = 0; j < k; ++j) {
+      if (!(g2[j] > 0.0)) continue;
+      const double nl = std::max(0.0, lam[j] + (hs[j] - row_dot(j)) / g2[j]);
+      const double dl = nl - lam[j];
+      if (dl != 0.0) {
+        for (int q = 0; q < 4; ++q) {
+          const int b = cols[4 * j + q];
+          if (b < 0) continue;
+          for (int c = 0; c < 3; ++c) u[3 * b + c] += dl * coef[12 * j + 3 * q + c];
+        }
+        lam[j] = nl;
+      }
+      change = std::max(change, std::fabs(dl) * std::sqrt(g2[j]));
+      lmax = std::max(lmax, nl * std::sqrt(g2[j]));
+    }
+    double viol = 0.0;
+    for (int j = 0; j < k; ++j)
+      if (g2[j] > 0.0) viol = std::max(viol, hs[j] - row_dot(j));
+    if (change <= tol * std::max(lmax, 1.0) && viol <= tol) break;
+  }
+  for (int i = 0; i < n; ++i) u[i] *= s;
+  for (int j = 0; j < k; ++j) lam[j] *= s;
+  return sweep < max_sweeps ? 0 : 2;
+}
+
 struct ZoneRecord {  // one zone projection
   int round = 0;
   std::vector<int> nodes;    // the zone's cloth nodes, zone order
@@ -335,7 +398,7 @@ struct ZoneRecord {  // one zone projection
   std::vector<double> a;     // objective weight inv_m m of each node
   std::vector<double> xout;  // [3 nodes] projected positions
   std::vector<double> lam;   // multiplier of each constraint
-  int status = 0;            // ldp() status
+  int status = 0;            // ldp() status; 3: reverted to the start of the step (see revert_factor)
 };
 
 struct ZoneResponse {
@@ -347,17 +410,31 @@ struct ZoneResponse {
   const double* obs_xprev = nullptr;
   double thickness = 0.0;
   int max_iter = 100;
-  // a zone that gathers more impacts than this stops the response (its exact
-  // projection costs grow with the square of the impacts; such zones arise
-  // only from layers tangled beyond what a step's detection can separate)
-  int max_zone_impacts = 256;
+  // zones of up to this many impacts are projected exactly (LDP through
+  // NNLS, cost O(n k^2)); larger ones -- a contact patch of a cloth lying on
+  // an obstacle chains its impacts into one zone through shared nodes -- by
+  // Hildreth's iterations on sparse rows (ldp_sparse)
+  int exact_zone_impacts = 64;
+  // a zone that gathers more impacts than this stops the response (a bound
+  // on the time and memory of one projection; layers tangled beyond what a
+  // step's detection separates keep merging zones)
+  int max_zone_impacts = 65536;
+  // A zone holds the constraints of every round it received impacts in,
+  // each linearised where it was found; on a crumpling cloth two of them can
+  // constrain one edge pair with nearly opposite normals, and the exact
+  // projection then lies far away (nodes moved by centimetres; the
+  // reference's inexact augmented Lagrangian stops long before). When the
+  // projection would move a node by more than revert_factor times (its own
+  // displacement in the step + thickness), the zone's nodes go back to their
+  // positions at the start of the step instead (needs xprev; <= 0: off).
+  double revert_factor = 4.0;
   // results
   std::vector<ZImpact> accepted;  // every impact a zone received, in order
   std::vector<int> accepted_round;
   std::vector<double> accepted_x;  // [accepted][4][3] its nodes' positions when it was found
   std::vector<double> accepted_xp;  // [accepted][4][3] and at the start of the step
   std::vector<ZoneRecord> tape;   // every projection, in order
-  int rounds = 0, converged = 0, changed = 0, zones = 0, infeasible = 0;
+  int rounds = 0, converged = 0, changed = 0, zones = 0, infeasible = 0, reverted = 0;
   int zone_overflow = 0;  // stopped at a zone larger than max_zone_impacts
 };
 
@@ -385,7 +462,10 @@ inline void project(ZoneResponse& R, const std::vector<int>& nodes, const std::v
     isa[i] = 1.0 / std::sqrt(rec.a[i]);
     local[nodes[i]] = i;
   }
-  std::vector<double> G((size_t)k * nv, 0.0), h(k), u(nv);
+  const bool dense = k <= R.exact_zone_impacts;
+  std::vector<double> G(dense ? (size_t)k * nv : 0, 0.0), h(k), u(nv);
+  std::vector<int> cols(dense ? 0 : 4 * (size_t)k, -1);
+  std::vector<double> coef(dense ? 0 : 12 * (size_t)k, 0.0);
   rec.lam.assign(k, 0.0);
   for (int j = 0; j < k; ++j) {
     const ZImpact& im = R.accepted[imps[j]];
@@ -394,8 +474,11 @@ inline void project(ZoneResponse& R, const std::vector<int>& nodes, const std::v
       const int nd = im.node[q];
       if (nd >= 0) {
         const int li = local[nd];
+        if (!dense) cols[4 * (size_t)j + q] = li;
         for (int c = 0; c < 3; ++c) {
-          G[(size_t)j * nv + 3 * li + c] += im.w[q] * im.n[c] * isa[li];
+          const double g = im.w[q] * im.n[c] * isa[li];
+          if (dense) G[(size_t)j * nv + 3 * li + c] += g;
+          else coef[12 * (size_t)j + 3 * q + c] = g;
           hj -= im.w[q] * im.n[c] * xold[3 * (size_t)nd + c];
         }
       } else {
@@ -404,13 +487,31 @@ inline void project(ZoneResponse& R, const std::vector<int>& nodes, const std::v
     }
     h[j] = hj;
   }
-  rec.status = ldp(nv, k, G.data(), h.data(), u.data(), rec.lam.data());
+  rec.status = dense ? ldp(nv, k, G.data(), h.data(), u.data(), rec.lam.data())
+                     : ldp_sparse(nv, k, cols.data(), coef.data(), h.data(), u.data(), rec.lam.data());
   if (rec.status == 1) R.infeasible++;
+  if (rec.status != 1 && R.xprev && R.revert_factor > 0.0) {
+    bool far = false;
+    for (int i = 0; i < m && !far; ++i) {
+      double mv = 0.0, st = 0.0;
+      for (int c = 0; c < 3; ++c) {
+        const size_t g = 3 * (size_t)nodes[i] + c;
+        const double d = u[3 * i + c] * isa[i];
+        mv += d * d;
+        st += (xold[g] - R.xprev[g]) * (xold[g] - R.xprev[g]);
+      }
+      far = std::sqrt(mv) > R.revert_factor * (std::sqrt(st) + R.thickness);
+    }
+    if (far) {
+      rec.status = 3;
+      R.reverted++;
+    }
+  }
   rec.xout.resize(nv);
   for (int i = 0; i < m; ++i)
     for (int c = 0; c < 3; ++c) {
       const size_t g = 3 * (size_t)nodes[i] + c;
-      const double xn = rec.status == 1 ? x[g] : xold[g] + u[3 * i + c] * isa[i];
+      const double xn = rec.status == 1 ? x[g] : rec.status == 3 ? R.xprev[g] : xold[g] + u[3 * i + c] * isa[i];
       x[g] = xn;
       rec.xout[3 * i + c] = xn;
     }
@@ -433,7 +534,7 @@ int zone_respond(ZoneResponse& R, double* x, const double* mass, Detect&& detect
   R.accepted_x.clear();
   R.accepted_xp.clear();
   R.tape.clear();
-  R.rounds = R.converged = R.changed = R.zones = R.infeasible = R.zone_overflow = 0;
+  R.rounds = R.converged = R.changed = R.zones = R.infeasible = R.zone_overflow = R.reverted = 0;
   std::vector<double> xold(x, x + 3 * (size_t)n);
   // faces around each node (the verts' adj_faces of the cloth mesh)
   std::vector<int> fo(n + 1, 0), fl(3 * (size_t)R.n_faces);
@@ -732,6 +833,14 @@ inline void zone_backward(const ZoneResponse& R, double* g, double* gw, double* 
   for (int ri = (int)R.tape.size() - 1; ri >= 0; --ri) {
     const ZoneRecord& rec = R.tape[ri];
     if (rec.round != round) continue;
+    if (rec.status == 3) {  // reverted: the zone's positions are the step's start positions
+      for (int nd : rec.nodes)
+        for (int c = 0; c < 3; ++c) {
+          if (gxp) gxp[3 * (size_t)nd + c] += g[3 * (size_t)nd + c];
+          g[3 * (size_t)nd + c] = 0.0;
+        }
+      continue;
+    }
     const int m = (int)rec.nodes.size(), nv = 3 * m, k = (int)rec.imps.size();
     auto local = [&](int nd) {
       for (int i = 0; i < m; ++i)

@@ -1,0 +1,271 @@
+"""The reference's simulation drivers (src/Simulate.h) on the package API.
+
+Each driver builds the cloth the way the reference does (Cloth, Environment,
+PhysicsCloth, set_handles) and runs its loop of SimStep (src/TrainHelper.cpp
+:15-149) on the GPU path. Instead of the fixed output paths of the reference
+(./data/*.h5, ./objs/Cloth%04d.obj) the caller passes h5_path and obj_dir
+(None: not written); every driver returns the per-step states as arrays
+[steps + 1, nodes, 3|2] (the initial state first), the layout data_loader
+reads back. `height` defaults to the reference's 5 m.
+
+- sim_homo       SimHomo       src/Simulate.h:10-106
+- sim_collision  SimCollision  src/Simulate.h:108-216 (obstacle meshes as
+                 arguments: the reference's ./obs/wall.obj and ground.obj are
+                 not in its repository)
+- sim_control    SimControl    src/Simulate.h:218-330
+- sim_heter      SimHeter      src/Simulate.h:332-452
+- DropOnSphere   the collision benchmark scene: a flat cloth dropped onto an
+                 icosphere with self-collision (the reference's collision
+                 step, SimStep with a Collision)
+"""
+from __future__ import annotations
+
+import os
+import time
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import h5 as _h5
+from .cloth import Cloth, Environment, InitPose, PhysicsCloth, SimStep, Wind, WovenPattern, Yarn
+from .collide import Collision, icosphere
+from .render import RenderCloth, RenderType
+
+FULL = ("LPos", "LPosFix", "LVel", "EPos", "EPosBar", "EVel")
+
+# the reference drivers' material (src/Simulate.h:16-32, 132-148)
+HOMO = dict(L=0.001, R=0.0005, rho=0.002, Y=500000.0, B=0.00014, kc=1.0, mu=0.5, df=1000.0, kf=1000.0, S=1000.0,
+            handle_stiffness=1e4, G=(0.0, 0.0, 9.8))
+# the benchmark configurations' material (the reference's Yarn(R, rho, Y, B)
+# arguments with R = 0.1 mm, S and mu per cloth)
+BENCH = dict(HOMO, R=0.0001, rho=0.001, Y=1000.0, B=1e-5, S=1e-4, mu=0.3)
+
+
+def _record(states: Dict[str, List[np.ndarray]], cloth: Cloth):
+    st = cloth.get_ClothState().as_dict()
+    for k in FULL:
+        states[k].append(np.array(st[k]))
+
+
+def _finish(states, cloth: Cloth, h5_path: Optional[str], physical: Dict):
+    out = {k: np.array(v) for k, v in states.items()}
+    if h5_path:
+        _h5.save_trajectory(h5_path, cloth.width, cloth.length, physical, out)
+    return out
+
+
+def _physical_homo(env: Environment, p: Dict, pattern: int) -> Dict:
+    """The H5Physical record SaveClothHomoYarn writes (src/Saver.cpp:184-300)."""
+    w = env.wind
+    return dict(Gravity=float(env.G[2]), rho=p["rho"], R=p["R"], L=p["L"], Y=p["Y"], B=p["B"], kc=p["kc"],
+                kf=p["kf"], df=p["df"], mu=p["mu"], S=p["S"], handle_stiff=p["handle_stiffness"],
+                wind_velocity_x=float(w.WindVelocity[0]), wind_velocity_y=float(w.WindVelocity[1]),
+                wind_velocity_z=float(w.WindVelocity[2]), wind_density=float(w.WindDensity),
+                wind_drag=float(w.WindDrag), woven_pattern=int(pattern))
+
+
+def _obj(cloth, obj_dir, i):
+    if obj_dir:
+        os.makedirs(obj_dir, exist_ok=True)
+        RenderCloth(cloth, os.path.join(obj_dir, "Cloth%04d.obj" % i), RenderType.MeshTriangle)
+
+
+def _run(cloth, phy, steps, h, obj_dir, ext=None, force_steps=None, collision=None):
+    states = {k: [] for k in FULL}
+    _record(states, cloth)
+    for i in range(steps):
+        if collision is not None:
+            ok = SimStep(cloth, phy, collision, h)
+        else:
+            f = ext if (ext is not None and (force_steps is None or i < force_steps)) else None
+            ok = SimStep(cloth, phy, h, f)
+        if not ok:
+            break
+        _record(states, cloth)
+        _obj(cloth, obj_dir, i)
+    return states
+
+
+def sim_homo(width: int = 10, length: int = 10, steps: int = 100, h: float = 0.001, handles=None,
+             wind=Wind((0.0, 5.0, 0.0), 2.0, 0.5), params: Optional[Dict] = None, h5_path: Optional[str] = None,
+             obj_dir: Optional[str] = None, height: float = 5.0, device: int = 0) -> Dict[str, np.ndarray]:
+    """SimHomo: a homogeneous plain cloth hanging from its two top corners in
+    wind (10 x 10, 100 steps, the reference's material)."""
+    p = dict(HOMO, **(params or {}))
+    yarn = Yarn(p["R"], p["rho"], p["Y"], p["B"])
+    cloth = Cloth(width, length, height, p["L"], p["R"], [yarn], p["kc"], p["kf"], p["df"], p["mu"], p["S"],
+                  p["handle_stiffness"], WovenPattern.Plain, InitPose.Upright)
+    env = Environment(cloth, p["G"], wind)
+    cloth.set_handles(handles if handles is not None else [(0, 0), (width - 1, 0)])
+    phy = PhysicsCloth(env, device=device)
+    states = _run(cloth, phy, steps, h, obj_dir)
+    return _finish(states, cloth, h5_path, _physical_homo(env, p, WovenPattern.Plain))
+
+
+def sim_heter(width: int = 10, length: int = 10, steps: int = 100, h: float = 0.001, handles=None,
+              yarns: Sequence[Tuple[float, float, float]] = ((0.002, 500000.0, 0.00014), (0.0025, 170000.0, 0.00011)),
+              S: float = 1000.0, wind=Wind((0.0, 5.0, 0.0), 2.0, 0.5), pattern: int = WovenPattern.Plain,
+              h5_path: Optional[str] = None, obj_dir: Optional[str] = None, height: float = 5.0,
+              device: int = 0) -> Dict[str, np.ndarray]:
+    """SimHeter: a two-yarn blend (cotton / polyester by default) hanging in
+    wind; yarn lines alternate by parity (src/Cloth.cpp:195-268)."""
+    p = dict(HOMO)
+    ys_ = [Yarn(p["R"], *y) for y in yarns]
+    cloth = Cloth(width, length, height, p["L"], p["R"], ys_, p["kc"], p["kf"], p["df"], p["mu"], S,
+                  p["handle_stiffness"], pattern, InitPose.Upright)
+    env = Environment(cloth, p["G"], wind)
+    cloth.set_handles(handles if handles is not None else [(0, 0), (width - 1, 0)])
+    phy = PhysicsCloth(env, device=device)
+    states = _run(cloth, phy, steps, h, obj_dir)
+    w = env.wind
+    physical = dict(Gravity=float(env.G[2]), Yarn1_rho=yarns[0][0], Yarn2_rho=yarns[1][0], R=p["R"], L=p["L"],
+                    Yarn1_Y=yarns[0][1], Yarn2_Y=yarns[1][1], Yarn1_B=yarns[0][2], Yarn2_B=yarns[1][2], kc=p["kc"],
+                    kf=p["kf"], df=p["df"], mu=p["mu"], S=S, handle_stiff=p["handle_stiffness"],
+                    wind_velocity_x=float(w.WindVelocity[0]), wind_velocity_y=float(w.WindVelocity[1]),
+                    wind_velocity_z=float(w.WindVelocity[2]), wind_density=float(w.WindDensity),
+                    wind_drag=float(w.WindDrag), woven_pattern=int(pattern))
+    return _finish(states, cloth, h5_path, physical)
+
+
+def control_force(width: int, length: int, up: float = 0.002, forward: float = 0.002) -> np.ndarray:
+    """SimControl's external force: lift (z) and drag (y) at the four corners
+    (the reference's DOF indices 1, 2, 13, 14, 61, 62, 73, 74 of a 5 x 5
+    cloth), in node layout [nodes, 5]."""
+    f = np.zeros((width * length, 5))
+    for n in (0, width - 1, width * (length - 1), width * length - 1):
+        f[n, 1] = forward
+        f[n, 2] = up
+    return f
+
+
+def sim_control(width: int = 5, length: int = 5, steps: int = 100, h: float = 0.001, force_steps: int = 6,
+                ext_force: Optional[np.ndarray] = None, h5_path: Optional[str] = None, obj_dir: Optional[str] = None,
+                height: float = 5.0, device: int = 0) -> Dict[str, np.ndarray]:
+    """SimControl: a free flat cloth (Y = 5e4, B = 1e-5) lifted and dragged at
+    its corners for the first `force_steps` steps (the reference zeroes the
+    force once i > 5)."""
+    p = dict(HOMO, Y=50000.0, B=0.00001)
+    yarn = Yarn(p["R"], p["rho"], p["Y"], p["B"])
+    cloth = Cloth(width, length, height, p["L"], p["R"], [yarn], p["kc"], p["kf"], p["df"], p["mu"], p["S"],
+                  p["handle_stiffness"], WovenPattern.Plain, InitPose.Flat)
+    env = Environment(cloth, p["G"], Wind((0.0, 0.0, 0.0), 2.0, 0.5))
+    cloth.set_handles([])
+    phy = PhysicsCloth(env, device=device)
+    f = control_force(width, length) if ext_force is None else np.ascontiguousarray(ext_force, np.float64)
+    states = _run(cloth, phy, steps, h, obj_dir, ext=f, force_steps=force_steps)
+    return _finish(states, cloth, h5_path, _physical_homo(env, p, WovenPattern.Plain))
+
+
+def sim_collision(obstacle_x: np.ndarray, obstacle_faces: np.ndarray, width: int = 5, length: int = 5,
+                  steps: int = 20, h: float = 0.001, height: float = 0.025, thickness: float = 0.0005,
+                  handles=None, wind=Wind((0.0, 5.0, 0.0), 2.0, 0.5), h5_path: Optional[str] = None,
+                  obj_dir: Optional[str] = None, device: int = 0) -> Dict[str, np.ndarray]:
+    """SimCollision: an upright cloth hanging in wind against obstacle
+    meshes, each step followed by the impact-zone response
+    (collision_response(0.1)). The reference loads its table and ground from
+    ./obs/wall.obj and ./obs/ground.obj; here the merged obstacle mesh is
+    passed in (vertices [V, 3], faces [F, 3])."""
+    p = dict(HOMO)
+    yarn = Yarn(p["R"], p["rho"], p["Y"], p["B"])
+    cloth = Cloth(width, length, height, p["L"], p["R"], [yarn], p["kc"], p["kf"], p["df"], p["mu"], p["S"],
+                  p["handle_stiffness"], WovenPattern.Plain, InitPose.Upright)
+    env = Environment(cloth, p["G"], wind)
+    cloth.set_handles(handles if handles is not None else [(0, 0), (width - 1, 0)])
+    phy = PhysicsCloth(env, device=device)
+    col = Collision(cloth, obstacle_x, obstacle_faces, thickness=thickness, h=h, device=device)
+    try:
+        states = _run(cloth, phy, steps, h, obj_dir, collision=col)
+    finally:
+        col.close()
+    return _finish(states, cloth, h5_path, _physical_homo(env, p, WovenPattern.Plain))
+
+
+class DropOnSphere:
+    """The collision benchmark scene: a width x width plain cloth lying flat
+    `drop` metres above the top of a fixed icosphere (radius, `levels`
+    subdivisions: 20 * 4^levels faces; 3 gives 1,280), centred over it, free
+    (no handles), falling under gravity with self-collision and cloth-sphere
+    collision every step (SimStep with a Collision, src/TrainHelper.cpp:
+    99-149: step, then collision_response(damp)), step size h. Material: the
+    benchmark configurations' (BENCH: R = 0.1 mm), collision thickness = the
+    yarn radius unless given.
+
+    damp is the velocity update after a projection, v += damp (x - x_before)
+    / h. The reference's SimStep passes 0.1: a node projected out of the
+    obstacle keeps 90 % of its approach speed, the next step drives it back
+    in, and a free-falling cloth landing on a sphere folds onto itself within
+    about 20 steps of contact (the fold's zones then move nodes by
+    millimetres per projection and speeds grow without bound). With 1.0 the
+    projection is inelastic (the velocity follows the projected position)
+    and the cloth drapes; that is the default here.
+
+    run(steps) advances the scene and times each step's parts; `frames`
+    records (x_prev, x) -- the detection's input -- at chosen steps."""
+
+    def __init__(self, width: int = 50, radius: float = 0.03, levels: int = 3, drop: float = 0.05,
+                 h: float = 5e-4, thickness: Optional[float] = None, params: Optional[Dict] = None, device: int = 0,
+                 ext_force=None, damp: float = 1.0):
+        p = dict(BENCH, **(params or {}))
+        self.p, self.h, self.width, self.damp = p, float(h), int(width), float(damp)
+        self.thickness = p["R"] if thickness is None else float(thickness)
+        half = 0.5 * (width - 1) * p["L"]
+        self.center = np.array([half, half, 0.0])
+        self.radius = float(radius)
+        self.sphere_x, self.sphere_f = icosphere(radius, levels, self.center)
+        yarn = Yarn(p["R"], p["rho"], p["Y"], p["B"])
+        self.cloth = Cloth(width, width, radius + drop, p["L"], p["R"], [yarn], p["kc"], p["kf"], p["df"], p["mu"],
+                           p["S"], p["handle_stiffness"], WovenPattern.Plain, InitPose.Flat)
+        self.env = Environment(self.cloth, p["G"], Wind())
+        self.cloth.set_handles([])
+        self.phy = PhysicsCloth(self.env, device=device)
+        self.col = Collision(self.cloth, self.sphere_x, self.sphere_f, thickness=self.thickness, h=self.h,
+                             device=device)
+        self.ext = ext_force
+        self.steps_done = 0
+        self.frames = {}
+        self.log = []
+
+    def close(self):
+        self.col.close()
+
+    def step(self, record_frame: bool = False) -> Dict:
+        """One SimStep with collision; returns its timings and response
+        counters."""
+        b = self.phy.batch
+        t0 = time.perf_counter()
+        before = b.get_state()
+        stats = b.step(self.h, self.ext)
+        ok = bool(stats[0]["ok"])
+        st = b.get_state()
+        t1 = time.perf_counter()
+        info = dict(step=self.steps_done, ok=ok, cg_iterations=stats[0]["cg_iterations"])
+        if ok:
+            if record_frame:
+                self.frames[self.steps_done] = (before["LPos"].copy(), st["LPos"].copy())
+            changed = self.col.collision_response(self.damp, st["LPos"], before["LPos"], st["LVel"])
+            r = self.col.last
+            t2 = time.perf_counter()
+            if changed:
+                # no handles: every node's fixed position follows it
+                b.set_state(LPos=r["x"], LPosFix=r["x"].copy(), LVel=r["v"], EPos=st["EPos"],
+                            EPosBar=st["EPosBar"], EVel=st["EVel"])
+            t3 = time.perf_counter()
+            info.update(changed=bool(changed), rounds=r["rounds"], zones=r["zones"], impacts=int(r["impacts"]),
+                        converged=bool(r["converged"]), zone_overflow=bool(r["zone_overflow"]),
+                        step_ms=1e3 * (t1 - t0), collision_ms=1e3 * (t2 - t1), writeback_ms=1e3 * (t3 - t2))
+        self.steps_done += 1
+        self.log.append(info)
+        return info
+
+    def run(self, steps: int, frames: Sequence[int] = ()) -> List[Dict]:
+        fr = set(int(s) for s in frames)
+        out = []
+        for _ in range(steps):
+            info = self.step(record_frame=self.steps_done in fr)
+            out.append(info)
+            if not info["ok"]:
+                break
+        return out
+
+    def state(self) -> Dict[str, np.ndarray]:
+        return self.phy.batch.get_state()

@@ -343,10 +343,12 @@ ys_status ys_collider_get_impacts(ys_collider *c, ys_impact *impacts, int64_t ca
  * updated in place as v + damp (x - x_before) / h when any zone moved.
  * Returns YS_ERR_MAXITER when max_iter rounds (the reference's 100) still
  * found impacts, where the reference exits, or when a zone gathers more than
- * the zone limit (256 impacts unless ys_collider_set_max_zone_impacts says
- * otherwise) (layers tangled beyond what the response resolves: the exact
- * projection's cost grows with the square of a zone's impacts); x_out and v
- * are written as they stand. */
+ * the zone limit (65,536 impacts unless ys_collider_set_max_zone_impacts says
+ * otherwise; layers tangled beyond what the response resolves keep merging
+ * zones); x_out and v are written as they stand. Zones of up to 64 impacts are
+ * projected exactly (least-distance programme through NNLS); larger ones -- a
+ * cloth's contact patch on an obstacle chains its impacts into one zone --
+ * by Hildreth's iterations on the same programme to 1e-13 relative. */
 typedef struct {
   int32_t rounds;      /* rounds that found impacts (the reference's iter) */
   int32_t converged;   /* 1: a round found no impact within max_iter */
@@ -356,10 +358,13 @@ typedef struct {
   int32_t zone_overflow; /* 1: stopped at a zone larger than the zone limit */
   int64_t impacts;     /* impacts the zones received, over all rounds */
   int64_t projections; /* zone projections */
+  int32_t reverted;    /* projections that would have moved a node by more than 4 x (its displacement in
+                          the step + thickness) -- nearly contradictory constraints of a crumpling cloth --
+                          and sent the zone back to its positions at the start of the step instead */
 } ys_response_info;
 ys_status ys_collider_respond(ys_collider *c, const double *node_mass, double h, double damp, int32_t max_iter,
                               double *x_out, double *v, ys_response_info *info);
-/* The zone limit of ys_collider_respond (default 256 impacts per zone). */
+/* The zone limit of ys_collider_respond (default 65,536 impacts per zone). */
 ys_status ys_collider_set_max_zone_impacts(ys_collider *c, int32_t n);
 /* The impacts the zones received, in order (info.impacts of them); the
  * pair field holds the round that found each. */

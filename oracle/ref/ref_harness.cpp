@@ -836,6 +836,9 @@ int main(int argc, char** argv) {
 
   std::vector<double> ext;
   if (kv.count("ext_force")) ext = parse_list(kv["ext_force"]);
+  // ext_steps=K: the force acts in steps 0..K-1 only (SimControl zeroes it
+  // once i > 5, src/Simulate.h:290-291); default every step
+  const int ext_steps = static_cast<int>(get_d(kv, "ext_steps", 1e9));
 
   auto dump_state = [&](const std::string& tag) {
     std::vector<double> lp(N * 3), lv(N * 3), lf(N * 3), ep(N * 2), ev(N * 2), eb(N * 2), nrm(N * 3, 0.0);
@@ -873,7 +876,7 @@ int main(int argc, char** argv) {
     const Tensor Dv = phy.get_SpaFVel();
     Tensor F = phy.get_SpaF();
     const Tensor V = phy.get_SpaVel();
-    if (!ext.empty()) F = F + torch::tensor(ext, opts).view({-1, 1});
+    if (!ext.empty() && s < ext_steps) F = F + torch::tensor(ext, opts).view({-1, 1});
     const Tensor A = M - Kx * torch::pow(h, 2) - Dv * h;
     const Tensor b = h * (F - torch::mm(Dv.transpose(0, 1), V)) + torch::mm(M, V);
     if (DetectNaN(A, false) || DetectNaN(b, false) || DetectInf(A, false) || DetectInf(b, false)) {

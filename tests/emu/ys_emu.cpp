@@ -582,8 +582,16 @@ void hc_mark(HostColl& h, const ys::BvhTree& t, const uint8_t* fa, int n, bool& 
 }  // namespace
 
 // x [nn][3] in/out, v [nn][3] in/out (may be null), mass [nn] (may be null);
-// info[8]: rounds, converged, changed, zones, infeasible, impacts,
-// projections, zone overflow
+// info[9]: rounds, converged, changed, zones, infeasible, impacts,
+// projections, zone overflow, reverted projections
+static int g_max_zone_impacts = -1;  // < 0: the response's default
+
+// zone limit of the next emu_respond calls (< 0: the default)
+int emu_set_max_zone_impacts(int n) {
+  g_max_zone_impacts = n;
+  return 0;
+}
+
 int emu_respond(int nn, double* x, const double* xp, int nf, const int* fv, const int* fe, int no, const double* ox,
                 const double* oxp, int nof, const int* ofv, double thick, int ccd, const double* mass, double hstep,
                 double damp, int max_iter, double* v, long* info) {
@@ -678,6 +686,7 @@ int emu_respond(int nn, double* x, const double* xp, int nf, const int* fv, cons
   g_resp.obs_xprev = obsprev.data();
   g_resp.thickness = thick;
   g_resp.max_iter = max_iter;
+  if (g_max_zone_impacts >= 0) g_resp.max_zone_impacts = g_max_zone_impacts;
   g_resp_x0.assign(x, x + 3 * (size_t)nn);
   ys::zone_respond(g_resp, x, mass, detect);
   g_resp.faces = nullptr;
@@ -692,6 +701,7 @@ int emu_respond(int nn, double* x, const double* xp, int nf, const int* fv, cons
   info[5] = (long)g_resp.accepted.size();
   info[6] = (long)g_resp.tape.size();
   info[7] = g_resp.zone_overflow;
+  info[8] = g_resp.reverted;
   return 0;
 }
 
@@ -730,6 +740,12 @@ int emu_respond_backward(double* gx, const double* gv, double* gw, double* gn, i
 // the least-distance solver alone: min |u| s.t. G u >= h (G [k][n])
 int emu_ldp(int n, int k, const double* G, const double* h, double* u, double* lam) {
   return ys::ldp(n, k, G, h, u, lam);
+}
+
+// the large-zone solver on the same programme, G given by sparse rows
+// (cols [k][4], coef [k][4][3])
+int emu_ldp_sparse(int n, int k, const int* cols, const double* coef, const double* h, double* u, double* lam) {
+  return ys::ldp_sparse(n, k, cols, coef, h, u, lam);
 }
 
 // one detection round as the response runs it: trees built from xb (the

@@ -113,9 +113,8 @@ def run_case(cs, tmp):
     cfg = dict(mode="collide", width=W, length=H, L=cs["L"], R=1e-4, thickness=cs["thickness"], ccd=1,
                cloth_state=sp, out=os.path.join(tmp, cs["name"] + ".bin"))
     out = dict(width=W, length=H, L=cs["L"], thickness=cs["thickness"], x=x, x_prev=xp)
-    if "sphere" in cs:
-        c, r, lv = cs["sphere"]
-        vo, fo = icosphere(c, r, lv)
+    if "sphere" in cs or "mesh" in cs:
+        vo, fo = cs["mesh"] if "mesh" in cs else icosphere(*cs["sphere"])
         op = os.path.join(tmp, cs["name"] + ".obs")
         np.concatenate([[len(vo)], vo.ravel(), vo.ravel(), [len(fo)], fo.ravel().astype(float)]).astype("<f8").tofile(op)
         cfg["obstacle"] = op
@@ -132,15 +131,32 @@ def run_case(cs, tmp):
     return out
 
 
-def main():
+def frame_cases(path):
+    """Cases from frames recorded on the GPU by record_drop_frames.py (the
+    collision benchmark scene): one fixture per frame, collide_drop50_s<step>."""
+    f = np.load(path)
+    out = []
+    for s in f["frames"]:
+        s = int(s)
+        x, xp = f["x_%d" % s].copy(), f["x_prev_%d" % s].copy()
+        out.append(dict(name="collide_drop50_s%d" % s, W=int(f["width"]), H=int(f["length"]), L=1e-3,
+                        thickness=float(f["thickness"]), state=(lambda x=x, xp=xp: (x, xp)),
+                        mesh=(f["obs_x"].copy(), f["obs_faces"].astype(np.int64))))
+    return out
+
+
+def main(argv=()):
+    """No arguments: the synthetic cases; "frames <npz>": fixtures from
+    frames of the collision benchmark scene."""
     if not os.path.exists(HARNESS):
         subprocess.run([os.path.join(ROOT, "oracle", "ref", "build_ref.sh")], check=True)
+    cases = frame_cases(argv[1]) if len(argv) > 1 and argv[0] == "frames" else CASES
     with tempfile.TemporaryDirectory() as tmp:
-        for cs in CASES:
+        for cs in cases:
             o = run_case(cs, tmp)
             print(cs["name"], "pairs", len(o["pairs"]), "impacts", len(o["impacts"]),
                   "VF", int((o["impacts"][:, 0] == 0).sum()) if len(o["impacts"]) else 0)
 
 
 if __name__ == "__main__":
-    sys.exit(main())
+    sys.exit(main(sys.argv[1:]))

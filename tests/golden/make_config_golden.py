@@ -12,6 +12,9 @@ physics sources in a serial build; see make_golden.py).
   src/Cloth.cpp:195-268), type 0 within +-20 % of the values above, type 1 =
   type 0 times factors drawn uniformly in [1.5, 3] per parameter, upright,
   two top corners pinned, h = 1e-3, 500 steps; every 10th state is kept.
+- driver_simheter10, driver_simcontrol5: the set-ups of the reference's
+  SimHeter and SimControl drivers (src/Simulate.h:218-452), 30 steps each,
+  every step kept (they pin the package's drivers, drivers.py).
 
 The harness writes every step; the fixtures keep LPos, LVel, EPos, EVel and
 EPosBar at the kept steps (the dense systems of a 17 x 17 cloth, 14 MB each,
@@ -65,24 +68,60 @@ def config1(rng, weave):
                 handles=[(0, 0), (W - 1, 0)], steps=500, keep_every=10)
 
 
+def driver_heter():
+    """SimHeter's set-up (src/Simulate.h:332-452): cotton / polyester blend,
+    R = 0.5 mm, S = 1000, mu = 0.5, upright in wind (0, 5, 0), 10 x 10, two
+    top corners pinned; 30 steps."""
+    W = H = 10
+    y0, y1 = np.array([0.002, 500000.0, 0.00014]), np.array([0.0025, 170000.0, 0.00011])
+    return dict(W=W, H=H, weave="plain", pose=0, warp=np.array([(y0, y1)[v % 2] for v in range(H)]),
+                weft=np.array([(y0, y1)[u % 2] for u in range(W)]), S=1000.0, mu=0.5, yarns=(y0, y1),
+                handles=[(0, 0), (W - 1, 0)], steps=30, keep_every=1, R=0.0005,
+                wind=((0.0, 5.0, 0.0), 2.0, 0.5))
+
+
+def driver_control():
+    """SimControl's set-up (src/Simulate.h:218-330): a free flat 5 x 5 cloth,
+    Y = 5e4, B = 1e-5, R = 0.5 mm, S = 1000, mu = 0.5, lifted and dragged at
+    its corners (0.002 N) for steps 0..5; 30 steps."""
+    W = H = 5
+    y0 = np.array([0.002, 50000.0, 0.00001])
+    ext = np.zeros(3 * W * H + 2 * (W - 2) * (H - 2))
+    for n in (0, W - 1, W * (H - 1), W * H - 1):
+        ext[3 * n + 1] = 0.002
+        ext[3 * n + 2] = 0.002
+    return dict(W=W, H=H, weave="plain", pose=1, warp=np.tile(y0, (H, 1)), weft=np.tile(y0, (W, 1)), S=1000.0,
+                mu=0.5, yarns=(y0,), handles=[], steps=30, keep_every=1, R=0.0005,
+                wind=((0.0, 0.0, 0.0), 2.0, 0.5), ext=ext, ext_steps=6)
+
+
 def cases():
     out = {"config0_plain5_flat": config0(np.random.default_rng(100))}
     for i, weave in enumerate(("plain", "twill", "satin")):
         out["config1_%s17" % weave] = config1(np.random.default_rng(101 + i), weave)
+    out["driver_simheter10"] = driver_heter()
+    out["driver_simcontrol5"] = driver_control()
     return out
 
 
 def run_case(name, cs, tmp):
     W, H = cs["W"], cs["H"]
-    L, R, height = 1e-3, LIT["R"], 0.05
+    L, R, height = 1e-3, cs.get("R", LIT["R"]), 0.05
     cfg = dict(width=W, length=H, pose="flat" if cs["pose"] == 1 else "upright", weave=cs["weave"], L=L, R=R,
                height=height, mu=repr(float(cs["mu"])), S=repr(float(cs["S"])), kc=1.0, kf=1000.0, df=1000.0,
                handle_stiffness=1e4, G="0,0,9.8", h=1e-3, handles=",".join("%d,%d" % hp for hp in cs["handles"]),
                steps=cs["steps"], dump_steps="", out=os.path.join(tmp, name + ".bin"))
+    wind = cs.get("wind")
+    if wind:
+        cfg["wind_vel"] = "%r,%r,%r" % wind[0]
+        cfg["wind_density"], cfg["wind_drag"] = wind[1], wind[2]
+    if cs.get("ext") is not None:
+        cfg["ext_force"] = ",".join(repr(float(x)) for x in cs["ext"])
+        cfg["ext_steps"] = cs["ext_steps"]
     if cs["yarns"] is not None:
-        # the reference's own two-yarn blend (Cloth constructor with two Yarns)
-        cfg["yarn0"] = ",".join(repr(float(x)) for x in cs["yarns"][0])
-        cfg["yarn1"] = ",".join(repr(float(x)) for x in cs["yarns"][1])
+        # the reference's own constructor with one yarn or a two-yarn blend
+        for i, y in enumerate(cs["yarns"]):
+            cfg["yarn%d" % i] = ",".join(repr(float(x)) for x in y)
     else:
         cfg["yarn0"] = ",".join(repr(float(x)) for x in cs["warp"][0])
         cfg["warp_lines"] = ";".join(",".join(repr(float(x)) for x in r) for r in cs["warp"])
@@ -98,8 +137,13 @@ def run_case(name, cs, tmp):
                height=height, mu=cs["mu"], S=cs["S"], kc=1.0, kf=1000.0, df=1000.0, handle_stiffness=1e4,
                G=np.array([0, 0, 9.8]), h=1e-3, warp=cs["warp"], weft=cs["weft"],
                handles=np.array(cs["handles"], dtype=np.int32).reshape(-1, 2), steps=cs["steps"],
-               kept=np.array(kept), wind_vel=np.zeros(3), wind_density=0.0, wind_drag=0.0,
-               status=rec["status"])
+               kept=np.array(kept), status=rec["status"])
+    if wind:
+        out.update(wind_vel=np.array(wind[0]), wind_density=wind[1], wind_drag=wind[2])
+    else:
+        out.update(wind_vel=np.zeros(3), wind_density=0.0, wind_drag=0.0)
+    if cs.get("ext") is not None:
+        out.update(ext_force=cs["ext"], ext_steps=cs["ext_steps"])
     for s in kept:
         for k in KEYS:
             out["s%d_%s" % (s, k)] = rec["s%d.%s" % (s, k)]

@@ -33,6 +33,23 @@ from make_golden import HARNESS, ROOT, perturbed_state, read_records  # noqa: E4
 INIT = [0.00225, 335000.0, 0.000125, 0.00245, 145000.0, 0.0001, 600.0, 0.7]
 TRUTH = [0.002, 500000.0, 0.00014, 0.0025, 170000.0, 0.00011, 1000.0, 0.5]
 
+def _config1_case(weave, seed):
+    """The 17 x 17 blend of the benchmark's heterogeneous configuration: the
+    learned parameters start from the fixture's own two yarn types, S and mu
+    (make_config_golden.py), the ground truth is a second seeded set within
+    +-30 % of it; a 20-step window from the fixture's state at step 200."""
+    g = np.load(os.path.join(HERE, "config1_%s17.npz" % weave))
+    warp = g["warp"]
+    start = [*warp[0], *warp[1], float(g["S"]), float(g["mu"])]
+    rng = np.random.default_rng(seed)
+    truth = [x * (1.0 + 0.3 * (2.0 * rng.random() - 1.0)) for x in start]
+    return dict(name="grad_config1_%s17" % weave, W=17, H=17, weave=weave, pose=0, R=float(g["R"]), steps=20,
+                start=("config1_%s17" % weave, 200), wind=((0.0, 0.0, 0.0), 0.0, 0.0), handles=[(0, 0), (16, 0)],
+                params=start, truth=truth)
+
+
+CONFIG1 = ("plain", "twill", "satin")
+
 CASES = [
     dict(name="grad_plain6_upright", W=6, H=6, weave="plain", pose=0, R=5e-4, steps=4,
          start=("plain6_stiff_upright_wind", 10), wind=((0.0, 5.0, 0.0), 2.0, 0.5), handles=[(0, 0), (5, 0)]),
@@ -57,7 +74,8 @@ def run_case(cs, tmp):
                R=cs["R"], height=height, kc=1.0, kf=1000.0, df=1000.0, handle_stiffness=1e4, G="0,0,9.8", h=1e-3,
                handles=",".join("%d,%d" % hp for hp in cs["handles"]), steps=cs["steps"],
                wind_vel="%r,%r,%r" % wind[0], wind_density=wind[1], wind_drag=wind[2], init_state=ipath,
-               params=",".join(repr(float(x)) for x in INIT), gt_params=",".join(repr(float(x)) for x in TRUTH),
+               params=",".join(repr(float(x)) for x in cs.get("params", INIT)),
+               gt_params=",".join(repr(float(x)) for x in cs.get("truth", TRUTH)),
                out=os.path.join(tmp, cs["name"] + ".bin"))
     cpath = os.path.join(tmp, cs["name"] + ".cfg")
     with open(cpath, "w") as f:
@@ -68,8 +86,8 @@ def run_case(cs, tmp):
     out = dict(width=W, length=H, weave=["plain", "twill", "satin"].index(cs["weave"]), pose=cs["pose"], L=L,
                R=cs["R"], height=height, kc=1.0, kf=1000.0, df=1000.0, handle_stiffness=1e4, G=np.array([0, 0, 9.8]),
                h=1e-3, handles=np.array(cs["handles"], dtype=np.int32).reshape(-1, 2), steps=cs["steps"],
-               wind_vel=np.array(wind[0]), wind_density=wind[1], wind_drag=wind[2], params=np.array(INIT),
-               gt_params=np.array(TRUTH))
+               wind_vel=np.array(wind[0]), wind_density=wind[1], wind_drag=wind[2],
+               params=np.array(cs.get("params", INIT)), gt_params=np.array(cs.get("truth", TRUTH)))
     for k, v in init.items():
         out["init_" + k] = np.asarray(v)
     for k, v in rec.items():
@@ -78,14 +96,17 @@ def run_case(cs, tmp):
     return rec
 
 
-def main():
+def main(argv):
+    """No arguments: the small cases; "config1": the three 17 x 17 windows
+    (minutes each, run in parallel)."""
     if not os.path.exists(HARNESS):
         subprocess.run([os.path.join(ROOT, "oracle", "ref", "build_ref.sh")], check=True)
-    with tempfile.TemporaryDirectory() as tmp:
-        for cs in CASES:
-            rec = run_case(cs, tmp)
+    cases = [_config1_case(w, 201 + i) for i, w in enumerate(CONFIG1)] if "config1" in argv else CASES
+    from concurrent.futures import ThreadPoolExecutor
+    with tempfile.TemporaryDirectory() as tmp, ThreadPoolExecutor(len(cases)) as ex:
+        for cs, rec in zip(cases, ex.map(lambda c: run_case(c, tmp), cases)):
             print(cs["name"], "loss", rec["loss"][0], "grad", rec["grad"])
 
 
 if __name__ == "__main__":
-    sys.exit(main())
+    sys.exit(main(sys.argv[1:]))

@@ -10,7 +10,7 @@ GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 def names():
     """Trajectory / system fixtures (tests/golden/make_golden.py)."""
     return sorted(n for n in (os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
-                  if not n.startswith(("grad_", "collide_", "h5_", "embed_", "config")))
+                  if not n.startswith(("grad_", "collide_", "h5_", "embed_", "config", "driver_")))
 
 
 def grad_names():

@@ -76,7 +76,11 @@ def _lib():
         L.emu_response_impacts.argtypes = [_dp, c_l]
         L.emu_respond_backward.argtypes = [_dp, _dp, _dp, _dp, ctypes.c_int, _dp]
         L.emu_ldp.argtypes = [c_i, c_i, _dp, _dp, _dp, _dp]
-        for f in ("emu_detect", "emu_respond", "emu_response_impacts", "emu_respond_backward", "emu_ldp"):
+        L.emu_set_max_zone_impacts.argtypes = [c_i]
+        L.emu_ldp_sparse.argtypes = [c_i, c_i, _ip, _dp, _dp, _dp, _dp]
+        L.emu_ldp_sparse.restype = c_i
+        for f in ("emu_detect", "emu_respond", "emu_response_impacts", "emu_respond_backward", "emu_ldp",
+                  "emu_set_max_zone_impacts"):
             getattr(L, f).restype = c_i
         L._resp_types = True
     return L
@@ -117,7 +121,7 @@ def emu_respond(s, damp=0.1, max_iter=100, mass=None):
     n = s["W"] * s["H"]
     x = x0.copy()
     v = np.ascontiguousarray(s["v"], np.float64).copy()
-    info = (ctypes.c_long * 8)()
+    info = (ctypes.c_long * 9)()
     m = None if mass is None else np.ascontiguousarray(mass, np.float64)
     L.emu_respond(n, x.ctypes.data_as(_dp), xp.ctypes.data_as(_dp), len(F), F.ctypes.data_as(_ip),
                   E.ctypes.data_as(_ip), len(ox), ox.ctypes.data_as(_dp), ox.ctypes.data_as(_dp), len(of),
@@ -150,4 +154,18 @@ def emu_ldp(G, h):
     k, n = G.shape
     u, lam = np.zeros(n), np.zeros(k)
     st = L.emu_ldp(n, k, G.ctypes.data_as(_dp), h.ctypes.data_as(_dp), u.ctypes.data_as(_dp), lam.ctypes.data_as(_dp))
+    return u, lam, st
+
+
+def emu_ldp_sparse(cols, coef, h, n):
+    """The large-zone solver: cols [k, 4] (column blocks, -1 unused),
+    coef [k, 4, 3]; returns (u, lam, status)."""
+    L = _lib()
+    cols = np.ascontiguousarray(cols, np.int32)
+    coef = np.ascontiguousarray(coef, np.float64)
+    h = np.ascontiguousarray(h, np.float64)
+    k = len(h)
+    u, lam = np.zeros(n), np.zeros(k)
+    st = L.emu_ldp_sparse(n, k, cols.ctypes.data_as(_ip), coef.ctypes.data_as(_dp), h.ctypes.data_as(_dp),
+                          u.ctypes.data_as(_dp), lam.ctypes.data_as(_dp))
     return u, lam, st

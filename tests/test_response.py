@@ -380,25 +380,49 @@ def test_gpu_full_backward_matches_emulated():
     c.close()
 
 
-def test_tangled_layers_stop_at_the_zone_cap():
+def test_tangled_layers_resolve_by_reverting_zones():
     """The 50 x 50 sphere detection fixture is tangled beyond what a step's
-    detection separates: its zones keep merging, and the response stops when
-    one outgrows 256 impacts instead of spending minutes in ever larger exact
-    projections (the reference would run its 100 rounds and exit)."""
+    detection separates: some zones gather constraints with nearly opposite
+    normals whose exact projection lies far away. Those zones go back to
+    their positions at the start of the step (reverted), and the response
+    converges in a few rounds."""
     import time
     s = RC.fixture_scene("collide_sphere50")
     t0 = time.time()
     got = RC.emu_respond(s)
-    assert got["info"][7] == 1 and got["info"][1] == 0
+    assert got["info"][1] == 1 and got["info"][7] == 0  # converged, no overflow
+    assert got["info"][8] > 0  # reverted zones
+    rev = [i for i in range(len(got["x"])) if np.array_equal(got["x"][i], s["x_prev"][i])
+           and not np.array_equal(s["x"][i], s["x_prev"][i])]
+    assert rev, "no node back at its start position"
     assert time.time() - t0 < 60.0
 
 
+def test_zone_cap_stops_the_response():
+    """A zone that gathers more impacts than the zone limit (set to 8 here)
+    stops the response (no convergence, zone_overflow) instead of projecting
+    it (the reference would run its 100 rounds and exit)."""
+    s = RC.fixture_scene("collide_sphere50")
+    L = RC._lib()
+    L.emu_set_max_zone_impacts(8)
+    try:
+        got = RC.emu_respond(s)
+    finally:
+        L.emu_set_max_zone_impacts(-1)
+    assert got["info"][7] == 1 and got["info"][1] == 0
+
+
 @pytest.mark.gpu
-def test_gpu_tangled_layers_stop_at_the_zone_cap():
+def test_gpu_tangled_layers_and_zone_cap():
     if not gpu_available():
         pytest.skip("no CUDA device")
     s = RC.fixture_scene("collide_sphere50")
     c = _collider(s)
+    out = c.respond(v=s["v"], h=s["h"], damp=DAMP)
+    emu = RC.emu_respond(s, damp=DAMP)
+    assert out["converged"] and not out["zone_overflow"] and out["reverted"] == emu["info"][8]
+    c.set_positions(s["x"], s["x_prev"], s["obs_x"], s["obs_x"])
+    c.set_max_zone_impacts(8)
     out = c.respond(v=s["v"], h=s["h"], damp=DAMP, check=False)
     assert out["zone_overflow"] and not out["converged"]
     c.set_positions(s["x"], s["x_prev"], s["obs_x"], s["obs_x"])
@@ -441,3 +465,36 @@ def test_zone_projection_matches_a_general_qp_solver():
                        method="SLSQP", options=dict(ftol=1e-16, maxiter=500))
         assert res.success, res.message
         assert np.abs(res.x - x_ours).max() <= 1e-8 * max(1.0, np.abs(x_ours).max()) + 1e-10
+
+
+def test_large_zone_solver_matches_the_exact_one():
+    """Hildreth's iterations (ldp_sparse, the solver of zones above 64
+    impacts) against the exact least-distance solver on random zones of
+    contact-like rows (4 node blocks each, shared nodes, some constraints
+    inactive): u and the multipliers to 1e-9 relative."""
+    rng = np.random.default_rng(8)
+    for trial in range(6):
+        m, k = int(rng.integers(20, 60)), int(rng.integers(30, 90))
+        n = 3 * m
+        cols = np.full((k, 4), -1, np.int32)
+        coef = np.zeros((k, 4, 3))
+        G = np.zeros((k, n))
+        for j in range(k):
+            nodes = rng.choice(m, size=int(rng.integers(1, 5)), replace=False)
+            nrm = rng.normal(size=3)
+            nrm /= np.linalg.norm(nrm)
+            w = rng.random(len(nodes))
+            w = w / w.sum() * (1 if rng.random() < 0.5 else -1)
+            for q, (nd, wq) in enumerate(zip(nodes, w)):
+                cols[j, q] = nd
+                coef[j, q] = wq * nrm
+                G[j, 3 * nd:3 * nd + 3] += wq * nrm
+        h = rng.normal(size=k) * 1e-4
+        u_e, lam_e, st_e = RC.emu_ldp(G, h)
+        if st_e != 0:
+            continue
+        u_s, lam_s, st_s = RC.emu_ldp_sparse(cols, coef, h, n)
+        assert st_s == 0
+        assert np.abs(u_s - u_e).max() <= 1e-9 * max(np.abs(u_e).max(), 1e-300), trial
+        assert np.abs(lam_s - lam_e).max() <= 1e-7 * max(np.abs(lam_e).max(), 1e-300), trial
+        assert (G @ u_s - h).min() >= -1e-12 * np.abs(h).max()
