@@ -9,6 +9,14 @@ CollisionUtil.cpp with its traversal and comp_face_impacts restated).
   weights and normals to 1e-12).
 - GPU: ys_collider_* finds the same pairs (as a set, with the reference's
   orientation of every pair) and the same impacts.
+
+The collide_drop50_s* fixtures are frames of the collision benchmark scene
+(a 50 x 50 cloth draping over a 1,280-face sphere, recorded on the GPU by
+tests/golden/record_drop_frames.py). Their pair lists are held to the same
+bit-exact standard; their impacts come from real drapes, where nearly
+coplanar faces make CCD cubics rounding-sensitive, so impacts found on one
+side only may be at most 0.5 % of them (each such test sits at the distance
+threshold) and common impacts agree in t, weights and normal to 1e-8.
 """
 import ctypes
 
@@ -37,6 +45,28 @@ def _topology(W, H):
                 F.append(tri)
                 E.append([sorted((tri[a], tri[(a + 1) % 3])) for a in range(3)])
     return np.array(F, np.int32), np.array(E, np.int32)
+
+
+def _scene_frame(name):
+    return name.startswith("collide_drop50_")
+
+
+def _impacts_agree(mine, theirs, exact):
+    """mine, theirs: rows (key columns..., t, w[4], n[3]) keyed by their first
+    len - 8 columns. exact: same rows, values to 1e-12; else the tolerance of
+    the scene frames."""
+    if exact:
+        assert mine.shape == theirs.shape
+        assert np.array_equal(mine[:, :-8], theirs[:, :-8])
+        assert np.abs(mine[:, -8:] - theirs[:, -8:]).max() <= 1e-12
+        return
+    A = {tuple(r[:-8]): r[-8:] for r in mine}
+    B = {tuple(r[:-8]): r[-8:] for r in theirs}
+    only = len(set(A) ^ set(B))
+    assert only <= max(8, 0.005 * len(B)), only
+    common = [k for k in A if k in B]
+    assert len(common) >= 0.99 * len(B)
+    assert max(np.abs(A[k] - B[k]).max() for k in common) <= 1e-8
 
 
 def _obstacle(g):
@@ -69,10 +99,9 @@ def test_emulated_collision_matches_reference(name):
     I = imps[:15 * ni.value].reshape(-1, 15)
     assert np.array_equal(P, g["pairs"])
     gi = g["impacts"]
-    assert I.shape == gi.shape
-    if len(gi):
-        assert np.array_equal(I[:, :5], gi[:, :5]) and np.array_equal(I[:, 13], gi[:, 13])
-        assert np.abs(I[:, 5:13] - gi[:, 5:13]).max() <= 1e-12
+    if len(gi) or len(I):
+        cols = lambda a: np.column_stack([a[:, 13], a[:, :5], a[:, 5:13]])  # noqa: E731
+        _impacts_agree(cols(I), cols(gi), exact=not _scene_frame(name))
 
 
 def test_cloth_mesh_topology_matches_reference_order():
@@ -98,8 +127,7 @@ def test_gpu_collision_matches_reference(name):
     assert np.array_equal(key(P), key(ref))  # same pairs, each with the reference's orientation
     imp = c.impacts()
     gi = g["impacts"]
-    assert len(imp["t"]) == len(gi)
-    if len(gi):
+    if len(gi) or len(imp["t"]):
         # match impacts by (pair faces, test): map the reference's pair index to its faces
         def rows(pairs, pidx, typ, nodes, rest):
             pf = pairs[pidx.astype(np.int64)]
@@ -107,9 +135,7 @@ def test_gpu_collision_matches_reference(name):
         mine = rows(P, imp["pair"], imp["type"], imp["nodes"], np.column_stack([imp["t"], imp["w"], imp["n"]]))
         theirs = rows(ref, gi[:, 13], gi[:, 0], gi[:, 1:5], gi[:, 5:13])
         order = lambda a: a[np.lexsort(tuple(a[:, k] for k in range(7, -1, -1)))]
-        mine, theirs = order(mine), order(theirs)
-        assert np.array_equal(mine[:, :8], theirs[:, :8])
-        assert np.abs(mine[:, 8:] - theirs[:, 8:]).max() <= 1e-12
+        _impacts_agree(order(mine), order(theirs), exact=not _scene_frame(name))
     c.close()
 
 
