@@ -269,3 +269,97 @@ class DropOnSphere:
 
     def state(self) -> Dict[str, np.ndarray]:
         return self.phy.batch.get_state()
+
+
+def centroid_target(seed: int, start: np.ndarray, lo: float = 0.10, hi: float = 0.30) -> np.ndarray:
+    """A seeded target point lo..hi metres from `start` (a centroid), in a
+    random direction of the upper half-space (z >= 0), so a cloth above an
+    obstacle is steered away from it."""
+    rng = np.random.default_rng(seed)
+    d = rng.normal(size=3)
+    d[2] = abs(d[2])
+    d /= np.linalg.norm(d)
+    return np.asarray(start, float) + (lo + (hi - lo) * rng.random()) * d
+
+
+class CentroidControl:
+    """The control problem of the collision benchmark: per-node external
+    forces f_s [nodes, 3] at every step s < steps (the state of a cloth's
+    SimStep with ext_force, src/TrainHelper.cpp:56-97) minimising
+        L = |centroid(LPos after the last step) - target|^2,
+    the mass-centre loss of the reference's control learning
+    (src/TrainControl.h:192-203) on a per-node force instead of a network.
+    gradient() runs the rollout forward (checkpoints every `checkpoint_every`
+    steps) and backward through ys_adjoint_step, giving dL/df for all
+    nodes x steps at once; optimise() takes Adam steps on the forces.
+
+    The scene is DropOnSphere's cloth before it reaches the sphere (it
+    falls 50 mm; contact comes at step 201 of h = 5e-4), so the controlled
+    window has no impacts; collide() checks that with the scene's detection."""
+
+    def __init__(self, scene: "DropOnSphere", steps: int = 100, target: Optional[np.ndarray] = None, seed: int = 0,
+                 checkpoint_every: int = 20, mode: str = "exact", copies: int = 128):
+        from .learn import CheckpointedRollout  # noqa: F401 (import check)
+        self.scene, self.steps, self.k, self.mode, self.copies = scene, int(steps), int(checkpoint_every), mode, copies
+        b = scene.phy.batch
+        self.state0 = b.get_state()
+        self.n = b.total_nodes
+        c0 = self.state0["LPos"].mean(axis=0)
+        self.target = centroid_target(seed, c0) if target is None else np.asarray(target, float)
+        self.forces = np.zeros((self.steps, self.n, 3))
+
+    def _ext(self, forces):
+        out = []
+        for s in range(self.steps):
+            e = np.zeros((self.n, 5))
+            e[:, :3] = forces[s]
+            out.append(e)
+        return out
+
+    def loss_and_traj(self, forces=None):
+        from .learn import CheckpointedRollout
+        f = self.forces if forces is None else forces
+        ro = CheckpointedRollout(self.scene.phy.batch, self.state0, self.steps, self.scene.h, self._ext(f),
+                                 self.mode, self.k, copies=self.copies)
+        traj = ro.forward()
+        c = traj["LPos"][-1].mean(axis=0)
+        return float(((c - self.target) ** 2).sum()), traj, ro
+
+    def gradient(self, forces=None):
+        """(L, dL/df [steps, nodes, 3], trajectory)."""
+        L, traj, ro = self.loss_and_traj(forces)
+        c = traj["LPos"][-1].mean(axis=0)
+        g = {k: np.zeros_like(v) for k, v in traj.items()}
+        g["LPos"][-1] = np.broadcast_to(2.0 * (c - self.target) / self.n, g["LPos"][-1].shape)
+        out = ro.backward(g, want_ext=True)
+        self.scene.phy.batch.set_state(**self.state0)
+        return L, out["ext"][:, :, :3], traj
+
+    def optimise(self, iterations: int = 20, lr: float = 2e-5) -> List[float]:
+        """Adam on the forces (lr in newtons); returns the loss before each
+        iteration and after the last."""
+        m = np.zeros_like(self.forces)
+        v = np.zeros_like(self.forces)
+        hist = []
+        for it in range(1, iterations + 1):
+            L, g, _ = self.gradient()
+            hist.append(L)
+            m = 0.9 * m + 0.1 * g
+            v = 0.999 * v + 0.001 * g * g
+            mh, vh = m / (1 - 0.9 ** it), v / (1 - 0.999 ** it)
+            self.forces -= lr * mh / (np.sqrt(vh) + 1e-30)
+        hist.append(self.loss_and_traj()[0])
+        self.scene.phy.batch.set_state(**self.state0)
+        return hist
+
+    def collide(self, traj) -> int:
+        """Impacts the scene's detection finds along the trajectory."""
+        col = self.scene.col.collider
+        n = 0
+        prev = self.state0["LPos"]
+        ox = self.scene.sphere_x
+        for x in traj["LPos"]:
+            col.set_positions(x, prev, ox, ox)
+            n += len(col.impacts()["t"]) if len(col.pairs()) else 0
+            prev = x
+        return n
