@@ -352,14 +352,23 @@ class CentroidControl:
         self.scene.phy.batch.set_state(**self.state0)
         return hist
 
-    def collide(self, traj) -> int:
-        """Impacts the scene's detection finds along the trajectory."""
+    def collide(self, traj) -> Dict[str, int]:
+        """Impacts the scene's detection finds along the trajectory: with the
+        sphere, and of the cloth with itself. The controlled rollout has no
+        collision response: the cloth starts 5 cm above the sphere, and the
+        forces that move its centroid 10-30 cm in 50 ms (about 100 m/s^2, more
+        than the benchmark yarns' stretch stiffness carries) can fold its
+        lighter edges onto it."""
         col = self.scene.col.collider
-        n = 0
+        out = dict(sphere=0, self=0)
         prev = self.state0["LPos"]
         ox = self.scene.sphere_x
         for x in traj["LPos"]:
             col.set_positions(x, prev, ox, ox)
-            n += len(col.impacts()["t"]) if len(col.pairs()) else 0
+            if len(col.pairs()):
+                nodes = col.impacts()["nodes"]
+                obs = (nodes < 0).any(axis=1)
+                out["sphere"] += int(obs.sum())
+                out["self"] += int((~obs).sum())
             prev = x
-        return n
+        return out

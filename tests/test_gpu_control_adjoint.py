@@ -9,7 +9,9 @@ src/TrainControl.h:192-203 on a per-node force at every step).
   GPU rollout along random force directions: 1e-6 relative;
 - the benchmark scene itself (50 x 50 cloth, 100 steps of h = 5e-4,
   7,500 force components per step): Adam on the forces lowers the loss, and
-  the controlled window has no impacts with the sphere.
+  the controlled window has no impacts with the sphere (the rollout has no
+  collision response; the large forces can fold the cloth's lighter edges
+  onto itself, which CentroidControl.collide reports).
 """
 import numpy as np
 import pytest
@@ -55,6 +57,6 @@ def test_drop50_control_lowers_the_loss():
         assert hist[-1] < 0.5 * hist[0], hist
         assert all(b < a for a, b in zip(hist, hist[1:])), hist
         _, traj, _ = ctl.loss_and_traj()
-        assert ctl.collide(traj) == 0
+        assert ctl.collide(traj)["sphere"] == 0
     finally:
         sc.close()
