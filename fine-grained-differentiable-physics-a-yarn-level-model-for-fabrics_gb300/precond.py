@@ -45,7 +45,10 @@ class LearnedPreconditioner:
 
     @classmethod
     def pretrained(cls, device: int = 0, path: str = PARAMS_FILE) -> "LearnedPreconditioner":
-        """The parameters shipped with the package (trained by train())."""
+        """The parameters shipped with the package: the network's starting
+        weights (head at zero, i.e. the analytic first-order inverse), which
+        train()'s selection by held-out convergence kept because no trained
+        set converged faster."""
         return cls(device=device, params=np.load(path))
 
     def close(self):
