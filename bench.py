@@ -157,6 +157,40 @@ def measure_fp64_peak(torch):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
+# FP64 flops per node of one assembly launch, counted by ncu on a 64 x 40 x 40
+# batch (102,400 nodes): 2 x DFMA + DADD + DMUL thread instructions of the
+# launch (sm__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum)
+# divided by the batch's nodes; the bends' and shear's counts depend on the
+# state only through branch outcomes, so they carry over to other batches of
+# the same cloths per node to within a few per cent
+ASSEMBLY_FP64_FLOPS_PER_NODE = None
+# DRAM bytes (read + write) of the persistent solve per pass over the rows,
+# from the same capture
+PERSIST_DRAM_BYTES_PER_ROW_PASS = None
+
+
+def schedule_name(c):
+    """'graph|launch/phases-every-E' or 'graph|launch/persistent-TxC'."""
+    g = "graph" if c["graphs"] else "launch"
+    if c["pcg"] == "persistent":
+        return "%s/persistent-%dx%d" % (g, c["pcg_threads"], c["pcg_cluster"])
+    return "%s/phases-every-%d" % (g, c["check_every"])
+
+
+def assembly_roof(prof, n, steps, fp64_peak):
+    """The assembly kernels against the FP64 ceiling: flops per node (counted
+    by ncu) x nodes / their event time per step."""
+    kinds = ("geom", "edges", "bends", "faces", "gather", "shear", "finalize")
+    ms = sum(prof["ms"].get(k, 0.0) for k in kinds) / steps
+    out = {"kernels": list(kinds), "ms_per_step": ms, "bound": "fp64", "unit": "TFLOP/s",
+           "peak": fp64_peak, "peak_source": "cuBLAS DGEMM measured in this run"}
+    if ASSEMBLY_FP64_FLOPS_PER_NODE and ms > 0:
+        fl = sum(ASSEMBLY_FP64_FLOPS_PER_NODE.values()) * n
+        out.update(flops_per_node=ASSEMBLY_FP64_FLOPS_PER_NODE, achieved=fl / (ms * 1e-3) / 1e12)
+        out["frac"] = out["achieved"] / fp64_peak
+    return out
+
+
 # ---------------------------------------------------------------- CPU arm
 def _cpu_worker(args):
     specs, idx, warm, steps, seed = args
@@ -309,6 +343,28 @@ def collision_compare(ys, dev, repeats=5):
     return out
 
 
+def schedule_compare(ys, dev):
+    """One hanging cloth of side 5, 17 and 50 (the configurations' sizes;
+    the batched workload's material): the tuner's best phase-PCG and best
+    persistent-PCG step times (ms), each over 5 steps from the same state."""
+    specs, _ = workload(7, 1)
+    out = {}
+    for W in (5, 17, 50):
+        sp = dict(specs[0], width=W, length=W, warp=specs[0]["warp"][:1].repeat(W, 0),
+                  weft=specs[0]["weft"][:1].repeat(W, 0), handles=[(0, 0), (W - 1, 0)])
+        b = ys.ClothBatch([ys.ClothSpec(**sp)], device=dev)
+        sc = b.autotune(H, tol=TOL, steps=5)
+        b.close()
+        best = {}
+        for c in sc["candidates"]:
+            k = c["pcg"]
+            if k not in best or c["ms_per_step"] < best[k]["ms_per_step"]:
+                best[k] = c
+        out["%dx%d" % (W, W)] = {k: {"ms_per_step": v["ms_per_step"], "schedule": schedule_name(v)}
+                                 for k, v in best.items()}
+    return out
+
+
 def drop_scene(ys, dev, steps=1000):
     """The collision benchmark scene end to end (DropOnSphere): a 50 x 50
     plain cloth (1 mm spacing, the batched workload's material, R = 0.1 mm,
@@ -337,6 +393,7 @@ def drop_scene(ys, dev, steps=1000):
         "max_zones": max(e["zones"] for e in ok) if ok else None,
         "received_impacts": int(sum(e["impacts"] for e in ok)),
         "ms_per_step": 1e3 * wall / max(len(log), 1),
+        "step_schedule": schedule_name(sc.schedule) if sc.schedule else None,
         "median_ms": {"step": med("step_ms"), "collision": med("collision_ms"), "writeback": med("writeback_ms")},
         "contact_median_ms": {"collision": float(np.median([e["collision_ms"] for e in ok if e["impacts"] > 0]))
                               if contact else None},
@@ -358,9 +415,11 @@ def main():
     ap.add_argument("--drop-steps", type=int, default=1000,
                     help="steps of the 50x50 drop-onto-sphere scene (0: skip it)")
     ap.add_argument("--profile", action="store_true", help="print the per-kernel table to stderr")
-    ap.add_argument("--schedule", default="auto", choices=["auto", "graph", "launch"],
-                    help="auto: ys_autotune picks graph or launch-by-launch steps and the PCG check interval; "
-                         "graph: one CUDA graph launch per step (conditional PCG loop); launch: kernel by kernel")
+    ap.add_argument("--schedule", default="auto", choices=["auto", "graph", "launch", "persistent"],
+                    help="auto: ys_autotune picks graph or launch-by-launch steps and the PCG schedule; "
+                         "graph: one CUDA graph launch per step (conditional PCG loop); launch: kernel by kernel; "
+                         "persistent: kernel by kernel with the persistent PCG (512-thread CTAs, the smallest "
+                         "cluster that holds the largest cloth)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -408,10 +467,23 @@ def main():
         batch.set_winds(wind_at(wind, 0))
         sched = batch.autotune(H, tol=TOL, steps=3)
         config["schedule"] = {"chosen_by": "ys_autotune", "graph": sched["graphs"],
-                              "check_every": sched["check_every"]}
+                              "check_every": sched["check_every"], "pcg": sched["pcg"]}
+        if sched["pcg"] == "persistent":
+            config["schedule"].update(pcg_threads=sched["pcg_threads"], pcg_cluster=sched["pcg_cluster"])
+        config["schedule"]["timed_ms_per_step"] = {schedule_name(c): round(c["ms_per_step"], 4)
+                                                   for c in sched["candidates"]}
+    elif args.schedule == "persistent":
+        big = max(s["width"] * s["length"] for s in specs)
+        cl = 1
+        while 512 * cl < big:
+            cl *= 2
+        batch.set_pcg_schedule(True, 512, cl)
+        config["schedule"] = {"chosen_by": "flag", "graph": False, "pcg": "persistent", "pcg_threads": 512,
+                              "pcg_cluster": cl}
     else:
         batch.use_graphs(args.schedule == "graph")
-        config["schedule"] = {"chosen_by": "flag", "graph": args.schedule == "graph", "check_every": 16}
+        config["schedule"] = {"chosen_by": "flag", "graph": args.schedule == "graph", "check_every": 16,
+                              "pcg": "phases"}
 
     def barrier():
         if dist is not None:
@@ -479,7 +551,8 @@ def main():
     sizes = np.array([s["width"] * s["length"] for s in specs])
     node_iters = 0  # rows the SpMV launches processed: a cloth runs iters + 1 of them
     batch.profile(True)
-    for _ in range(max(3, args.steps // 4)):
+    prof_steps = max(3, args.steps // 4)
+    for _ in range(prof_steps):
         st = do_step()
         node_iters += int(sum(n * (x["cg_iterations"] + (0 if x["hit_maxiter"] else 1)) for n, x in zip(sizes, st)))
     batch.profile(False)
@@ -495,6 +568,10 @@ def main():
         # x, p, r, q, dinv read; x, r written
         "axpy": dict(bytes=n * (5 * 5 * 8 + 2 * 5 * 8), flops=n * 5 * 8),
         "dir": dict(bytes=n * (3 * 5 * 8 + 5 * 8), flops=n * 5 * 3),
+        # the persistent solve per iteration: the 159 coefficients stream from
+        # HBM, the vectors stay on chip (b, Dinv read and x written once per
+        # solve, counted per pass over the rows below); the phase kernels' flops
+        "pcg_persist": dict(bytes=n * 159 * 8, flops=n * (2 * 159 + 10 + 5 * 8 + 5 * 3)),
     }
     precond = None
     if rank == 0 and not args.no_precond:
@@ -502,6 +579,9 @@ def main():
     collision = None
     if rank == 0 and not args.no_collision:
         collision = collision_compare(ys, dev)
+    sched_cmp = None
+    if rank == 0 and args.schedule == "auto":
+        sched_cmp = schedule_compare(ys, dev)
     drop = None
     if rank == 0 and args.drop_steps > 0:
         drop = drop_scene(ys, dev, args.drop_steps)
@@ -519,9 +599,26 @@ def main():
         return dict(gbs=a["bytes"] * frac_rows / secs / 1e9, tflops=a["flops"] * frac_rows / secs / 1e12,
                     us=secs / frac_rows * 1e6, launches=prof["launches"][kname], row_passes=frac_rows)
 
-    spmv = roof("spmv")
     roofline = None
-    if spmv:
+    persist = roof("pcg_persist")
+    spmv = roof("spmv")
+    if persist:
+        # DRAM bytes per row pass: ncu's dram__bytes_read + write of one persistent solve
+        # launch over every node of a 64-cloth batch, divided by its row passes
+        tr = PERSIST_DRAM_BYTES_PER_ROW_PASS
+        roofline = {"kernel": "k_pcg_cluster (persistent per-cloth Jacobi-PCG, %d x %d threads per cloth)" %
+                              (config["schedule"].get("pcg_cluster", 0), config["schedule"].get("pcg_threads", 0)),
+                    "bound": "hbm", "achieved": persist["gbs"], "peak": hbm_peak, "unit": "GB/s",
+                    "frac": persist["gbs"] / hbm_peak, "peak_source": peak_kind,
+                    "traffic": tr * n if tr else None,
+                    "traffic_source": "ncu capture at 102,400 nodes (64 x 40 x 40), per row pass, scaled per node"
+                                      if tr else None,
+                    "fp64": {"achieved_tflops": persist["tflops"], "dgemm_tflops": fp64_peak,
+                             "frac": persist["tflops"] / fp64_peak},
+                    "us_per_full_batch_pass": persist["us"], "full_batch_passes": persist["row_passes"],
+                    "launches": persist["launches"],
+                    "dominant_kernel_by_time": dominant, "time_share": share}
+    elif spmv:
         roofline = {"kernel": "k_pcg_spmv (stencil SpMV, 159 FP64 coefficients per node)", "bound": "hbm",
                     "achieved": spmv["gbs"], "peak": hbm_peak, "unit": "GB/s", "frac": spmv["gbs"] / hbm_peak,
                     "peak_source": peak_kind,
@@ -533,6 +630,10 @@ def main():
                     "us_per_full_batch_pass": spmv["us"], "full_batch_passes": spmv["row_passes"],
                     "launches": spmv["launches"],
                     "dominant_kernel_by_time": dominant, "time_share": share}
+    if roofline is not None:
+        roofline["pcg_ms_per_step"] = sum(prof["ms"].get(k, 0.0) for k in
+                                          ("pcg_setup", "spmv", "axpy", "dir", "pcg_persist")) / prof_steps
+        roofline["assembly"] = assembly_roof(prof, n, prof_steps, fp64_peak)
 
     line = {"metric": metric, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -546,6 +647,8 @@ def main():
         line["collision"] = collision
     if drop is not None:
         line["collision_drop50"] = drop
+    if sched_cmp is not None:
+        line["single_cloth_pcg_schedules"] = sched_cmp
 
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1

@@ -15,7 +15,8 @@ ROOT = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
 LIB_DIR = os.path.join(PKG_DIR, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libyarnsim.so")
-SOURCES = ["ys_tangent.cu", "ys_kernels.cu", "ys_api.cu", "ys_collide.cu", "ys_gnn.cu", "ys_adjoint.cu"]
+SOURCES = ["ys_tangent.cu", "ys_kernels.cu", "ys_api.cu", "ys_collide.cu", "ys_gnn.cu", "ys_adjoint.cu",
+           "ys_pcg_cluster.cu"]
 HEADERS = ["ys_common.cuh", "ys_dual.cuh", "ys_physics.cuh", "ys_items.cuh", "ys_elem_kernels.cuh", "ys_kernels.cuh", "ys_collide.cuh", "ys_bvh.h",
            "ys_gnn.cuh", "ys_tc.cuh", "ys_zones.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -261,6 +261,14 @@ class ClothBatch:
         """Run step() as one CUDA graph launch per step (see ys_use_graphs)."""
         N.check(N.load().ys_use_graphs(self._h, int(bool(enable))), "ys_use_graphs")
 
+    def set_pcg_schedule(self, persistent: bool, threads: int = 0, cluster: int = 0):
+        """Phase PCG (three launches per iteration, the default) or the
+        persistent per-cloth PCG (one launch per solve, `cluster` CTAs of
+        `threads` threads per cloth; threads * cluster >= the largest cloth's
+        nodes). Both give the same bits (see ys_set_pcg_schedule)."""
+        N.check(N.load().ys_set_pcg_schedule(self._h, 1 if persistent else 0, int(threads), int(cluster)),
+                "ys_set_pcg_schedule")
+
     def normals(self) -> np.ndarray:
         """Node normals [total_nodes, 3] of the current positions (zero on boundary nodes)."""
         out = np.zeros((self.total_nodes, 3))
@@ -306,7 +314,18 @@ class ClothBatch:
         sc = N.Schedule()
         N.check(N.load().ys_autotune(self._h, h, ctypes.byref(self._opts(tol, maxiter, 0)), int(steps),
                                      ctypes.byref(sc)), "ys_autotune")
-        return dict(graphs=bool(sc.graphs), check_every=sc.check_every, ms_per_step=sc.ms_per_step)
+        L = N.load()
+        n = L.ys_autotune_results(self._h, None, 0)
+        arr = (N.Schedule * max(n, 1))()
+        L.ys_autotune_results(self._h, ctypes.cast(arr, ctypes.c_void_p), n)
+
+        def d(x):
+            return dict(graphs=bool(x.graphs), check_every=x.check_every, ms_per_step=x.ms_per_step,
+                        pcg="persistent" if x.pcg == 1 else "phases", pcg_threads=x.pcg_threads,
+                        pcg_cluster=x.pcg_cluster)
+        out = d(sc)
+        out["candidates"] = [d(arr[i]) for i in range(n)]
+        return out
 
     # ---- forward-mode sensitivities
     @property

@@ -127,6 +127,16 @@ struct ys_batch {
     int h_it = 0;
   } graph;
   int check_every = 16;  // PCG iterations between convergence checks when the call gives none
+  // PCG schedule (ys_set_pcg_schedule): phases, or the persistent per-cloth
+  // kernel with `threads` x `csize` nodes per cloth; `order` lists the cloths
+  // largest first, so the biggest clusters start first
+  struct PcgPlan {
+    int kind = YS_PCG_PHASES;
+    int threads = 0, csize = 0;
+    int* order = nullptr;  // device [ncloth]
+    int max_nodes = 0;
+  } plan;
+  std::vector<ys_schedule> tuned;  // every schedule the last ys_autotune timed
   bool has_system = false;  // v.A / v.B hold an assembled system (kept after the update)
   // learned preconditioner (ys_set_preconditioner); buffers allocated on first use
   struct Learn {
@@ -605,8 +615,17 @@ ys_status solve_impl(ys_batch* b, const ys::View& v, const ys_solve_opts* opts, 
     k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
   });
   YS_CUDA(cudaGetLastError());
-  b->run(YS_PROF_PCG_SETUP, 2, [&] { ys::launch_pcg_setup(v, b->blk, b->so, s); });
-  int it = 0;
+  if (b->plan.kind == YS_PCG_PERSISTENT) {
+    cudaError_t e = cudaSuccess;
+    b->run(YS_PROF_PCG_PERSIST, 1, [&] {
+      e = ys::launch_pcg_cluster(v, b->so, b->plan.order, b->ncloth, b->plan.threads, b->plan.csize, cap, s);
+    });
+    if (e != cudaSuccess) return fail(YS_ERR_CUDA, std::string("persistent PCG: ") + cudaGetErrorString(e));
+  }
+  else {
+    b->run(YS_PROF_PCG_SETUP, 2, [&] { ys::launch_pcg_setup(v, b->blk, b->so, s); });
+  }
+  int it = b->plan.kind == YS_PCG_PHASES ? 0 : cap;
   while (it < cap) {
     const int n = std::min(every, cap - it);
     for (int q = 0; q < n; ++q, ++it) {
@@ -1382,6 +1401,22 @@ ys_status graph_build(ys_batch* b, int m, int cap, int override_max) {
   ys::launch_shear_records(v, R, cs);
   ys::launch_finalize(v, R, b->blk, b->so, cs);
   k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, cs>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
+  if (b->plan.kind == YS_PCG_PERSISTENT) {
+    // the whole solve is one kernel: no loop node, one graph
+    const cudaError_t e =
+        ys::launch_pcg_cluster(v, so, b->plan.order, b->ncloth, b->plan.threads, b->plan.csize, cap, cs);
+    ys::launch_update(v, b->blk, b->so, cs);
+    cudaGraph_t one = nullptr;
+    YS_CUDA(cudaStreamEndCapture(cs, &one));
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(one);
+      return fail(YS_ERR_CUDA, std::string("persistent PCG: ") + cudaGetErrorString(e));
+    }
+    G.main = one;
+    YS_CUDA(cudaGraphInstantiate(&G.exec, G.main, 0));
+    G.built = true;
+    return YS_OK;
+  }
   ys::launch_pcg_setup(v, b->blk, so, cs);
   ys::launch_graph_loop_begin(so, cs);
   YS_CUDA(cudaStreamEndCapture(cs, &pre));
@@ -1431,6 +1466,53 @@ ys_status ys_use_graphs(ys_batch* b, int32_t enable) {
   return YS_OK;
 }
 
+int32_t ys_autotune_results(const ys_batch* b, ys_schedule* out, int32_t cap) {
+  if (!b) return -1;
+  const int32_t n = (int32_t)b->tuned.size();
+  for (int32_t i = 0; out && i < n && i < cap; ++i) out[i] = b->tuned[i];
+  return n;
+}
+
+ys_status ys_set_pcg_schedule(ys_batch* b, int32_t pcg, int32_t threads, int32_t cluster) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  YS_CUDA(cudaSetDevice(b->device));
+  ys_batch::PcgPlan& P = b->plan;
+  if (pcg == YS_PCG_PHASES) {
+    P.kind = YS_PCG_PHASES;
+    b->graph.built = false;
+    return YS_OK;
+  }
+  if (pcg != YS_PCG_PERSISTENT) return fail(YS_ERR_ARG, "ys_set_pcg_schedule: unknown schedule");
+  if (!ys::pcg_cluster_shape_ok(threads, cluster))
+    return fail(YS_ERR_ARG, "ys_set_pcg_schedule: threads must be 128, 256, 512 or 1024 and cluster 1, 2, 4, 8 "
+                            "or 16, at most 16384 nodes");
+  if (!P.order) {
+    // cloths largest first
+    std::vector<int> ord(b->ncloth);
+    for (int c = 0; c < b->ncloth; ++c) ord[c] = c;
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int x, int y) { return b->cp[x].W * b->cp[x].H > b->cp[y].W * b->cp[y].H; });
+    const ys_status s = b->alloc(&P.order, b->ncloth);
+    if (s != YS_OK) return s;
+    YS_CUDA(cudaMemcpy(P.order, ord.data(), sizeof(int) * b->ncloth, cudaMemcpyHostToDevice));
+    P.max_nodes = b->cp[ord[0]].W * b->cp[ord[0]].H;
+  }
+  if (P.max_nodes > threads * cluster)
+    return fail(YS_ERR_ARG, "ys_set_pcg_schedule: the largest cloth has " + std::to_string(P.max_nodes) +
+                                " nodes, more than threads x cluster");
+  int fit = 0;
+  const cudaError_t e = ys::pcg_cluster_occupancy(threads, cluster, &fit);
+  if (e != cudaSuccess || fit < 1) {
+    cudaGetLastError();
+    return fail(YS_ERR_ARG, "ys_set_pcg_schedule: this GPU cannot run a cluster of that shape");
+  }
+  P.kind = YS_PCG_PERSISTENT;
+  P.threads = threads;
+  P.csize = cluster;
+  b->graph.built = false;
+  return YS_OK;
+}
+
 ys_status ys_step_graphed(ys_batch* b, double h, const double* ext_force, int32_t flags, const ys_solve_opts* opts,
                           ys_cloth_stats* stats) {
   if (!b || !(h > 0)) return fail(YS_ERR_ARG, "bad argument");
@@ -1463,11 +1545,14 @@ ys_status ys_step_graphed(ys_batch* b, double h, const double* ext_force, int32_
   YS_CUDA(cudaGraphLaunch(G.exec, b->stream));
   std::vector<ys::PcgCloth> pc(b->ncloth);
   YS_CUDA(cudaMemcpyAsync(pc.data(), b->so.pc, sizeof(ys::PcgCloth) * b->ncloth, cudaMemcpyDeviceToHost, b->stream));
-  YS_CUDA(cudaMemcpyAsync(&G.h_it, G.it_base, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  if (b->plan.kind == YS_PCG_PHASES)
+    YS_CUDA(cudaMemcpyAsync(&G.h_it, G.it_base, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
   YS_CUDA(cudaStreamSynchronize(b->stream));
   // kernels the graph ran: 11 (+ geometry) before the loop, 3 per iteration
-  // + 1 per trip through the body, 2 after
-  b->launches += 13 + (b->geom_n ? 1 : 0) + 3LL * G.h_it + G.h_it / m;
+  // + 1 per trip through the body, 2 after; with the persistent PCG, 9 (+
+  // geometry) before the solve, the solve, 2 after
+  if (b->plan.kind == YS_PCG_PERSISTENT) b->launches += 12 + (b->geom_n ? 1 : 0);
+  else b->launches += 13 + (b->geom_n ? 1 : 0) + 3LL * G.h_it + G.h_it / m;
   ys_status ret = YS_OK;
   for (int c = 0; c < b->ncloth; ++c) {
     if (pc[c].status & 3) ret = YS_ERR_NONFINITE;
@@ -1483,11 +1568,12 @@ ys_status ys_step_graphed(ys_batch* b, double h, const double* ext_force, int32_
   return ret;
 }
 
-// The schedule tuner: every candidate (whole-step graph or launch by launch,
-// PCG iterations between convergence checks) runs the same steps from the same
-// state and gives bit-identical results -- the choices only move launches and
-// host synchronisations -- so the tuner times each on a snapshot of the state,
-// restores it, and keeps the fastest.
+// The schedule tuner: every candidate (whole-step graph or launch by launch;
+// phase PCG with its iterations between convergence checks, or the persistent
+// per-cloth PCG in one cluster shape) runs the same steps from the same state
+// and gives bit-identical results -- the choices only move launches, host
+// synchronisations and which threads do the same arithmetic -- so the tuner
+// times each on a snapshot of the state, restores it, and keeps the fastest.
 ys_status ys_autotune(ys_batch* b, double h, const ys_solve_opts* opts, int32_t steps, ys_schedule* best) {
   if (!b || !(h > 0) || steps < 1) return fail(YS_ERR_ARG, "bad argument");
   YS_CUDA(cudaSetDevice(b->device));
@@ -1508,42 +1594,70 @@ ys_status ys_autotune(ys_batch* b, double h, const ys_solve_opts* opts, int32_t 
     return cudaSuccess;
   };
   const bool was_graph = b->graph.enabled, was_prof = b->profiling;
+  const ys_batch::PcgPlan was_plan = b->plan;
   b->profiling = false;
+  // the candidates
+  std::vector<ys_schedule> cand;
+  int max_nodes = 0;
+  for (int c = 0; c < b->ncloth; ++c) max_nodes = std::max(max_nodes, b->cp[c].W * b->cp[c].H);
+  for (int g = 0; g < 2; ++g) {
+    for (int every : {2, 4, 8, 16, 32}) {
+      ys_schedule k{};
+      k.graphs = g;
+      k.check_every = every;
+      k.pcg = YS_PCG_PHASES;
+      cand.push_back(k);
+    }
+    for (int t : {128, 256, 512, 1024})
+      for (int cl : {1, 2, 4, 8, 16}) {
+        const int cap_nodes = t * cl;
+        if (!ys::pcg_cluster_shape_ok(t, cl) || cap_nodes < max_nodes || cap_nodes >= 4 * std::max(max_nodes, 128))
+          continue;
+        ys_schedule k{};
+        k.graphs = g;
+        k.check_every = b->check_every;
+        k.pcg = YS_PCG_PERSISTENT;
+        k.pcg_threads = t;
+        k.pcg_cluster = cl;
+        cand.push_back(k);
+      }
+  }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   ys_status st = YS_OK;
   ys_schedule top{};
   top.ms_per_step = -1.0;
-  const int every_c[5] = {2, 4, 8, 16, 32};
   std::vector<ys_cloth_stats> stats(b->ncloth);
   cudaError_t ce = copy_state(true);
   if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
   if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
-  for (int g = 0; g < 2 && ce == cudaSuccess && st == YS_OK; ++g) {
-    for (int c = 0; c < 5 && ce == cudaSuccess && st == YS_OK; ++c) {
-      b->graph.enabled = g == 1;
-      ys_solve_opts o = opts ? *opts : ys_solve_opts{0.0, -1, 0};
-      o.check_every = every_c[c];
-      // one untimed step builds the graph (and warms the caches)
-      if ((ce = copy_state(false)) != cudaSuccess) break;
-      ys_status s = ys_step(b, h, nullptr, 0, &o, stats.data());
-      if (s == YS_ERR_ARG || s == YS_ERR_CUDA) { st = s; break; }
-      if ((ce = copy_state(false)) != cudaSuccess) break;
-      if ((ce = cudaEventRecord(e0, b->stream)) != cudaSuccess) break;
-      for (int k = 0; k < steps && st == YS_OK; ++k) {
-        s = ys_step(b, h, nullptr, 0, &o, stats.data());
-        if (s == YS_ERR_ARG || s == YS_ERR_CUDA) st = s;
-      }
-      if (st != YS_OK) break;
-      if ((ce = cudaEventRecord(e1, b->stream)) != cudaSuccess) break;
-      if ((ce = cudaEventSynchronize(e1)) != cudaSuccess) break;
-      float ms = 0.f;
-      if ((ce = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) break;
-      const double per = ms / steps;
-      if (top.ms_per_step < 0 || per < top.ms_per_step) {
-        top.graphs = g;
-        top.check_every = every_c[c];
-        top.ms_per_step = per;
-      }
+  b->tuned.clear();
+  for (size_t ci = 0; ci < cand.size() && ce == cudaSuccess && st == YS_OK; ++ci) {
+    const ys_schedule& k = cand[ci];
+    if (ys_set_pcg_schedule(b, k.pcg, k.pcg_threads, k.pcg_cluster) != YS_OK) continue;  // shape cannot run here
+    b->graph.enabled = k.graphs == 1;
+    ys_solve_opts o = opts ? *opts : ys_solve_opts{0.0, -1, 0};
+    o.check_every = k.check_every;
+    // one untimed step builds the graph (and warms the caches)
+    if ((ce = copy_state(false)) != cudaSuccess) break;
+    ys_status s = ys_step(b, h, nullptr, 0, &o, stats.data());
+    if (s == YS_ERR_ARG || s == YS_ERR_CUDA) { st = s; break; }
+    if ((ce = copy_state(false)) != cudaSuccess) break;
+    if ((ce = cudaEventRecord(e0, b->stream)) != cudaSuccess) break;
+    for (int j = 0; j < steps && st == YS_OK; ++j) {
+      s = ys_step(b, h, nullptr, 0, &o, stats.data());
+      if (s == YS_ERR_ARG || s == YS_ERR_CUDA) st = s;
+    }
+    if (st != YS_OK) break;
+    if ((ce = cudaEventRecord(e1, b->stream)) != cudaSuccess) break;
+    if ((ce = cudaEventSynchronize(e1)) != cudaSuccess) break;
+    float ms = 0.f;
+    if ((ce = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) break;
+    const double per = ms / steps;
+    b->tuned.push_back(k);
+    b->tuned.back().ms_per_step = per;
+    if (top.ms_per_step < 0 || per < top.ms_per_step) {
+      top = k;
+      top.ms_per_step = per;
     }
   }
   if (ce == cudaSuccess) ce = copy_state(false);
@@ -1553,16 +1667,20 @@ ys_status ys_autotune(ys_batch* b, double h, const ys_solve_opts* opts, int32_t 
   cudaFree(snap);
   b->profiling = was_prof;
   b->assembled = false;
-  if (ce != cudaSuccess) {
+  if (ce != cudaSuccess || st != YS_OK || top.ms_per_step < 0) {
     b->graph.enabled = was_graph;
-    return fail(YS_ERR_CUDA, std::string("ys_autotune: ") + cudaGetErrorString(ce));
-  }
-  if (st != YS_OK) {
-    b->graph.enabled = was_graph;
-    return st;
+    b->plan.kind = was_plan.kind;
+    b->plan.threads = was_plan.threads;
+    b->plan.csize = was_plan.csize;
+    b->graph.built = false;
+    if (ce != cudaSuccess) return fail(YS_ERR_CUDA, std::string("ys_autotune: ") + cudaGetErrorString(ce));
+    if (st != YS_OK) return st;
+    return fail(YS_ERR_CUDA, "ys_autotune: no schedule ran");
   }
   b->graph.enabled = top.graphs != 0;
   b->check_every = top.check_every;
+  const ys_status sp = ys_set_pcg_schedule(b, top.pcg, top.pcg_threads, top.pcg_cluster);
+  if (sp != YS_OK) return sp;
   if (best) *best = top;
   return YS_OK;
 }

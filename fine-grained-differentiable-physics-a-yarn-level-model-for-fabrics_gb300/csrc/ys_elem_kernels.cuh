@@ -19,8 +19,8 @@ __global__ void __launch_bounds__(kBlock) k_edge_rec(View v, Records R) {
   const ClothParams& P = v.cp[v.node_cloth[n0]];
   if (k == 0 ? v.node_u[n0] >= P.W - 1 : v.node_v[n0] >= P.H - 1) return;
   EdgeOut<T> o;
-  edge_element(v, n0, n0 + (k == 0 ? 1 : P.W), k, o);
-  edge_store(v, R.edge, R.dedge, n0, k, o);
+  edge_element(v, n0, n0 + (k == 0 ? 1 : P.W), k, o, R.edge, R.dedge);
+  edge_store_groups(v, R.edge, R.dedge, n0, k, o, false, true);
 }
 
 // one thread per (yarn direction, middle node) of a bend segment

@@ -484,13 +484,25 @@ YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double*
   return ok;
 }
 
+// The SpMV rows read their input vector through an accessor: at(j) points at
+// component 0 of node j and component c sits c * stride() further on. The
+// global form below reads a [5][ntot] array; the persistent PCG reads its
+// direction from shared memory through another accessor. Both run the same
+// arithmetic, so they give the same bits.
+struct GlobalVec {
+  const double* YS_RESTRICT x;
+  int64_t nt;
+  YS_HD const double* at(int j) const { return x + j; }
+  YS_HD int64_t stride() const { return nt; }
+};
+
 // y = A x for row block n (5 rows). Couplings to grid positions outside the
 // cloth have zero coefficients; their column index is clamped to n so the
 // load stays in bounds and adds 0 * x(n).
-YS_HD void spmv_row_s(const View& v, const double* YS_RESTRICT Ab, int64_t ss, const double* YS_RESTRICT x, int n,
-                      double y[5]) {
-  const int nt = v.ntot;
+template <class XV>
+YS_HD void spmv_row_sv(const View& v, const double* YS_RESTRICT Ab, int64_t ss, const XV& xv, int n, double y[5]) {
   auto slot = [&](const View&, int s_, int n_) { return Ab[(int64_t)s_ * ss + n_]; };
+  const int64_t xs = xv.stride();
   const ClothParams& P = v.cp[v.node_cloth[n]];
   const int u = v.node_u[n], w = v.node_v[n];
   double yl0 = 0.0, yl1 = 0.0, yl2 = 0.0;
@@ -498,33 +510,36 @@ YS_HD void spmv_row_s(const View& v, const double* YS_RESTRICT Ab, int64_t ss, c
     const int uu = u + stencil_du(s), vv = w + stencil_dv(s);
     const bool ok = uu >= 0 && uu < P.W && vv >= 0 && vv < P.H;
     const int j = ok ? n + stencil_du(s) + stencil_dv(s) * P.W : n;
-    const double xj0 = x[j], xj1 = x[nt + j], xj2 = x[2 * nt + j];
+    const double* xp = xv.at(j);
+    const double xj0 = xp[0], xj1 = xp[xs], xj2 = xp[2 * xs];
     const int b = YS_SLOT_LL + 9 * s;
     yl0 += slot(v, b + 0, n) * xj0 + slot(v, b + 1, n) * xj1 + slot(v, b + 2, n) * xj2;
     yl1 += slot(v, b + 3, n) * xj0 + slot(v, b + 4, n) * xj1 + slot(v, b + 5, n) * xj2;
     yl2 += slot(v, b + 6, n) * xj0 + slot(v, b + 7, n) * xj1 + slot(v, b + 8, n) * xj2;
   }
-  const double xu = x[3 * nt + n], xv = x[4 * nt + n];
-  yl0 += slot(v, YS_SLOT_LE_SELF + 0, n) * xu + slot(v, YS_SLOT_LE_SELF + 1, n) * xv;
-  yl1 += slot(v, YS_SLOT_LE_SELF + 2, n) * xu + slot(v, YS_SLOT_LE_SELF + 3, n) * xv;
-  yl2 += slot(v, YS_SLOT_LE_SELF + 4, n) * xu + slot(v, YS_SLOT_LE_SELF + 5, n) * xv;
-  const double xl0 = x[n], xl1 = x[nt + n], xl2 = x[2 * nt + n];
+  const double* xn = xv.at(n);
+  const double xu = xn[3 * xs], xv_ = xn[4 * xs];
+  yl0 += slot(v, YS_SLOT_LE_SELF + 0, n) * xu + slot(v, YS_SLOT_LE_SELF + 1, n) * xv_;
+  yl1 += slot(v, YS_SLOT_LE_SELF + 2, n) * xu + slot(v, YS_SLOT_LE_SELF + 3, n) * xv_;
+  yl2 += slot(v, YS_SLOT_LE_SELF + 4, n) * xu + slot(v, YS_SLOT_LE_SELF + 5, n) * xv_;
+  const double xl0 = xn[0], xl1 = xn[xs], xl2 = xn[2 * xs];
   double ye[2];
   for (int k = 0; k < 2; ++k)
     ye[k] = slot(v, YS_SLOT_EL_SELF + 3 * k + 0, n) * xl0 + slot(v, YS_SLOT_EL_SELF + 3 * k + 1, n) * xl1 +
-            slot(v, YS_SLOT_EL_SELF + 3 * k + 2, n) * xl2 + slot(v, YS_SLOT_EE_SELF + k, n) * x[(3 + k) * nt + n];
+            slot(v, YS_SLOT_EL_SELF + 3 * k + 2, n) * xl2 + slot(v, YS_SLOT_EE_SELF + k, n) * xn[(3 + k) * xs];
   for (int m = 0; m < 4; ++m) {
     const int du = m == 0 ? -1 : m == 1 ? 1 : 0, dv = m == 2 ? -1 : m == 3 ? 1 : 0;
     const int k = m < 2 ? 0 : 1;
     const int uu = u + du, vv = w + dv;
     const bool ok = uu >= 0 && uu < P.W && vv >= 0 && vv < P.H;
     const int j = ok ? n + du + dv * P.W : n;
-    const double xe = x[(3 + k) * nt + j];
+    const double* xp = xv.at(j);
+    const double xe = xp[(3 + k) * xs];
     yl0 += slot(v, YS_SLOT_LE_NBR + 3 * m + 0, n) * xe;
     yl1 += slot(v, YS_SLOT_LE_NBR + 3 * m + 1, n) * xe;
     yl2 += slot(v, YS_SLOT_LE_NBR + 3 * m + 2, n) * xe;
-    ye[k] += slot(v, YS_SLOT_EL_NBR + 3 * m + 0, n) * x[j] + slot(v, YS_SLOT_EL_NBR + 3 * m + 1, n) * x[nt + j] +
-             slot(v, YS_SLOT_EL_NBR + 3 * m + 2, n) * x[2 * nt + j] + slot(v, YS_SLOT_EE_NBR + m, n) * xe;
+    ye[k] += slot(v, YS_SLOT_EL_NBR + 3 * m + 0, n) * xp[0] + slot(v, YS_SLOT_EL_NBR + 3 * m + 1, n) * xp[xs] +
+             slot(v, YS_SLOT_EL_NBR + 3 * m + 2, n) * xp[2 * xs] + slot(v, YS_SLOT_EE_NBR + m, n) * xe;
   }
   y[0] = yl0;
   y[1] = yl1;
@@ -533,14 +548,20 @@ YS_HD void spmv_row_s(const View& v, const double* YS_RESTRICT Ab, int64_t ss, c
   y[4] = ye[1];
 }
 
+YS_HD void spmv_row_s(const View& v, const double* YS_RESTRICT Ab, int64_t ss, const double* YS_RESTRICT x, int n,
+                      double y[5]) {
+  spmv_row_sv(v, Ab, ss, GlobalVec{x, v.ntot}, n, y);
+}
+
 YS_HD void spmv_row(const View& v, const double* YS_RESTRICT x, int n, double y[5]) {
   spmv_row_s(v, v.A, v.ntot, x, n, y);
 }
 
 // y = A^T x for row block n: every coefficient that row block i stores for
 // column block n (i = n - offset of its slot) is read from row i, transposed.
-YS_HD void spmv_row_t(const View& v, const double* YS_RESTRICT x, int n, double y[5]) {
-  const int nt = v.ntot;
+template <class XV>
+YS_HD void spmv_row_tv(const View& v, const XV& xv, int n, double y[5]) {
+  const int64_t xs = xv.stride();
   const ClothParams& P = v.cp[v.node_cloth[n]];
   const int u = v.node_u[n], w = v.node_v[n];
   double yl[3] = {0.0, 0.0, 0.0}, ye[2] = {0.0, 0.0};
@@ -549,15 +570,17 @@ YS_HD void spmv_row_t(const View& v, const double* YS_RESTRICT x, int n, double 
     const int uu = u - du, vv = w - dv;  // the row that refers to n through slot s
     if (uu < 0 || uu >= P.W || vv < 0 || vv >= P.H) continue;
     const int i = n - du - dv * P.W;
-    const double x0 = x[i], x1 = x[nt + i], x2 = x[2 * nt + i];
+    const double* xp = xv.at(i);
+    const double x0 = xp[0], x1 = xp[xs], x2 = xp[2 * xs];
     const int b = YS_SLOT_LL + 9 * s;
     for (int c = 0; c < 3; ++c)
       yl[c] += slot(v, b + c, i) * x0 + slot(v, b + 3 + c, i) * x1 + slot(v, b + 6 + c, i) * x2;
   }
   {  // the node's own Eulerian couplings
-    const double x0 = x[n], x1 = x[nt + n], x2 = x[2 * nt + n];
+    const double* xp = xv.at(n);
+    const double x0 = xp[0], x1 = xp[xs], x2 = xp[2 * xs];
     for (int k = 0; k < 2; ++k) {
-      const double xe = x[(3 + k) * nt + n];
+      const double xe = xp[(3 + k) * xs];
       ye[k] += slot(v, YS_SLOT_LE_SELF + 0 + k, n) * x0 + slot(v, YS_SLOT_LE_SELF + 2 + k, n) * x1 +
                slot(v, YS_SLOT_LE_SELF + 4 + k, n) * x2 + slot(v, YS_SLOT_EE_SELF + k, n) * xe;
       for (int c = 0; c < 3; ++c) yl[c] += slot(v, YS_SLOT_EL_SELF + 3 * k + c, n) * xe;
@@ -569,9 +592,10 @@ YS_HD void spmv_row_t(const View& v, const double* YS_RESTRICT x, int n, double 
     const int uu = u - du, vv = w - dv;
     if (uu < 0 || uu >= P.W || vv < 0 || vv >= P.H) continue;
     const int i = n - du - dv * P.W;
-    const double xe = x[(3 + k) * nt + i];
-    ye[k] += slot(v, YS_SLOT_LE_NBR + 3 * m + 0, i) * x[i] + slot(v, YS_SLOT_LE_NBR + 3 * m + 1, i) * x[nt + i] +
-             slot(v, YS_SLOT_LE_NBR + 3 * m + 2, i) * x[2 * nt + i] + slot(v, YS_SLOT_EE_NBR + m, i) * xe;
+    const double* xp = xv.at(i);
+    const double xe = xp[(3 + k) * xs];
+    ye[k] += slot(v, YS_SLOT_LE_NBR + 3 * m + 0, i) * xp[0] + slot(v, YS_SLOT_LE_NBR + 3 * m + 1, i) * xp[xs] +
+             slot(v, YS_SLOT_LE_NBR + 3 * m + 2, i) * xp[2 * xs] + slot(v, YS_SLOT_EE_NBR + m, i) * xe;
     for (int c = 0; c < 3; ++c) yl[c] += slot(v, YS_SLOT_EL_NBR + 3 * m + c, i) * xe;
   }
   y[0] = yl[0];
@@ -579,6 +603,10 @@ YS_HD void spmv_row_t(const View& v, const double* YS_RESTRICT x, int n, double 
   y[2] = yl[2];
   y[3] = ye[0];
   y[4] = ye[1];
+}
+
+YS_HD void spmv_row_t(const View& v, const double* YS_RESTRICT x, int n, double y[5]) {
+  spmv_row_tv(v, GlobalVec{x, v.ntot}, n, y);
 }
 
 // Right-hand side of the tangent solve of row block n for tangent k:

@@ -68,6 +68,16 @@ void launch_graph_loop_tail(const Solver& so, int ncloth, int m, int cap, cudaGr
 void launch_update(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
 void launch_spmv(const View& v, const double* x, double* y, cudaStream_t s);
 
+// ---- persistent per-cloth PCG (ys_pcg_cluster.cu): one cluster of csize
+// CTAs of `threads` threads per listed cloth runs that cloth's whole solve
+// (set-up included) with at most `cap` iterations; a cloth needs
+// width * length <= threads * csize. Same results as the phase kernels above.
+bool pcg_cluster_shape_ok(int threads, int csize);
+// clusters of this shape that fit on the GPU at once (0: the shape cannot run)
+cudaError_t pcg_cluster_occupancy(int threads, int csize, int* clusters);
+cudaError_t launch_pcg_cluster(const View& v, const Solver& so, const int* cloths, int ncl, int threads, int csize,
+                               int cap, cudaStream_t s);
+
 // state tangents updated by the tangent step (layout [c][kTangents][ntot])
 struct TangentState {
   double* dX;

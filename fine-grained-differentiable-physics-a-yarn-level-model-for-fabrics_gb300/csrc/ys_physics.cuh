@@ -231,10 +231,19 @@ YS_HD void acc_jac(EdgeOut<T>& o, int X, double s, const EdgeJac<T>& C) {
   }
 }
 
-// All terms of one edge (src/PhysicsCloth.cpp:64-80): Mass, Gravity, Stretch,
-// Inertia, MDotVDot, ParaColli; forces and both Jacobians.
 template <class T>
-YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o) {
+YS_HD void edge_store_groups(const View& v, double* buf, double* dbuf, int n0, int k, const EdgeOut<T>& o,
+                             bool early, bool late);
+
+// All terms of one edge (src/PhysicsCloth.cpp:64-80): Mass, Gravity, Stretch,
+// Inertia, MDotVDot, ParaColli; forces and both Jacobians. With ebuf given,
+// the fields that are final once ParaColli is done (the stretch projector's
+// factors and direction, the crimp accumulators) are stored to the record
+// there, so they hold no registers through the kinetic-energy terms; the
+// caller then stores the rest with edge_store_groups(..., false, true).
+template <class T>
+YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o, double* ebuf = nullptr,
+                        double* edbuf = nullptr) {
   const int nt = v.ntot;
   const ClothParams& P = v.cp[v.node_cloth[n0]];
   const uint8_t f0 = v.flags[n0], f1 = v.flags[n1];
@@ -371,6 +380,7 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o) {
     if (o.in[1]) acc_EE(o, kK, 1, 1, ee);
     if (o.in[0] && o.in[1]) { acc_EE(o, kK, 0, 1, ee); acc_EE(o, kK, 1, 0, ee); }
   }
+  if (ebuf) edge_store_groups(v, ebuf, edbuf, n0, k, o, true, false);
 
   // ---- kinetic-energy terms: shared sums
   T m0a[3], m1a[3];
@@ -532,21 +542,31 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o) {
 
 // record layout of an edge in the per-element buffer (field-major over the
 // 2 * ntot edge slots: slot = k * ntot + n0; tangents in dbuf)
+// `early`: llP, d, cl, cle (final after the stretch and contact terms);
+// `late`: every other field
 template <class T>
-YS_HD void edge_store(const View& v, double* buf, double* dbuf, int n0, int k, const EdgeOut<T>& o) {
+YS_HD void edge_store_groups(const View& v, double* buf, double* dbuf, int n0, int k, const EdgeOut<T>& o,
+                             bool early, bool late) {
   const int nt = v.ntot;
   int f = 0;
-  auto put = [&](const T& x) { stT(buf, dbuf, 2 * (f++) + k, nt, n0, x); };
-  for (int p = 0; p < 4; ++p) put(o.llI[p]);
-  for (int p = 0; p < 4; ++p) put(o.llP[p]);
-  for (int i = 0; i < 3; ++i) put(o.d[i]);
-  for (int p = 0; p < 4; ++p) for (int r = 0; r < 3; ++r) put(o.le[p][r]);
-  for (int p = 0; p < 4; ++p) for (int r = 0; r < 3; ++r) put(o.el[p][r]);
-  for (int p = 0; p < 4; ++p) put(o.ee[p]);
-  for (int i = 0; i < 8; ++i) put(o.b[i]);
-  for (int t = 0; t < 2; ++t) { put(o.fe[t]); put(o.kee[t]); put(o.dee[t]); }
-  for (int t = 0; t < 2; ++t) for (int i = 0; i < 3; ++i) put(o.cl[t][i]);
-  for (int t = 0; t < 2; ++t) for (int i = 0; i < 3; ++i) put(o.cle[t][i]);
+  auto put = [&](const T& x, bool g) {
+    if (g) stT(buf, dbuf, 2 * f + k, nt, n0, x);
+    ++f;
+  };
+  for (int p = 0; p < 4; ++p) put(o.llI[p], late);
+  for (int p = 0; p < 4; ++p) put(o.llP[p], early);
+  for (int i = 0; i < 3; ++i) put(o.d[i], early);
+  for (int p = 0; p < 4; ++p) for (int r = 0; r < 3; ++r) put(o.le[p][r], late);
+  for (int p = 0; p < 4; ++p) for (int r = 0; r < 3; ++r) put(o.el[p][r], late);
+  for (int p = 0; p < 4; ++p) put(o.ee[p], late);
+  for (int i = 0; i < 8; ++i) put(o.b[i], late);
+  for (int t = 0; t < 2; ++t) { put(o.fe[t], late); put(o.kee[t], late); put(o.dee[t], late); }
+  for (int t = 0; t < 2; ++t) for (int i = 0; i < 3; ++i) put(o.cl[t][i], early);
+  for (int t = 0; t < 2; ++t) for (int i = 0; i < 3; ++i) put(o.cle[t][i], early);
+}
+template <class T>
+YS_HD void edge_store(const View& v, double* buf, double* dbuf, int n0, int k, const EdgeOut<T>& o) {
+  edge_store_groups(v, buf, dbuf, n0, k, o, true, true);
 }
 // field offsets of the layout above
 constexpr int kE_llI = 0, kE_llP = 4, kE_d = 8, kE_le = 11, kE_el = 23, kE_ee = 35, kE_b = 39, kE_fkd = 47,

@@ -200,11 +200,16 @@ class DropOnSphere:
     and the cloth drapes; that is the default here.
 
     run(steps) advances the scene and times each step's parts; `frames`
-    records (x_prev, x) -- the detection's input -- at chosen steps."""
+    records (x_prev, x) -- the detection's input -- at chosen steps.
+
+    tune=True times the step schedules once from the initial state
+    (ClothBatch.autotune, state restored; every schedule gives the same
+    bits) and keeps the fastest: for one cloth this is usually the
+    persistent PCG, one launch per solve."""
 
     def __init__(self, width: int = 50, radius: float = 0.03, levels: int = 3, drop: float = 0.05,
                  h: float = 5e-4, thickness: Optional[float] = None, params: Optional[Dict] = None, device: int = 0,
-                 ext_force=None, damp: float = 1.0):
+                 ext_force=None, damp: float = 1.0, tune: bool = True):
         p = dict(BENCH, **(params or {}))
         self.p, self.h, self.width, self.damp = p, float(h), int(width), float(damp)
         self.thickness = p["R"] if thickness is None else float(thickness)
@@ -221,6 +226,7 @@ class DropOnSphere:
         self.col = Collision(self.cloth, self.sphere_x, self.sphere_f, thickness=self.thickness, h=self.h,
                              device=device)
         self.ext = ext_force
+        self.schedule = self.phy.batch.autotune(self.h, steps=3) if tune else None
         self.steps_done = 0
         self.frames = {}
         self.log = []

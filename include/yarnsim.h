@@ -158,14 +158,36 @@ ys_status ys_step_graphed(ys_batch *b, double h, const double *ext_force, int32_
 /* Step schedule (no counterpart in the reference). */
 typedef struct ys_schedule {
   int32_t graphs;      /* 1: one CUDA graph per step (ys_use_graphs) */
-  int32_t check_every; /* PCG iterations between convergence checks */
+  int32_t check_every; /* PCG iterations between convergence checks (phase PCG) */
   double ms_per_step;  /* measured time of the chosen schedule */
+  int32_t pcg;         /* YS_PCG_PHASES or YS_PCG_PERSISTENT */
+  int32_t pcg_threads; /* persistent PCG: threads per CTA (128, 256, 512, 1024) */
+  int32_t pcg_cluster; /* persistent PCG: CTAs per cloth (1, 2, 4, 8, 16) */
+  int32_t pad_;
 } ys_schedule;
-/* Times every schedule (graph or launch by launch x check_every in
- * {2, 4, 8, 16, 32}) over `steps` steps of size h without an external force,
+/* PCG schedules. Both run Eigen's Jacobi-PCG with the same arithmetic and the
+ * same summation order, so they give bit-identical solutions:
+ *  - phases: three launches per iteration over every 128-node block of the
+ *    batch (SpMV, axpy, direction), convergence checked every check_every
+ *    iterations (the default);
+ *  - persistent: one launch for the whole solve, a cluster of pcg_cluster CTAs
+ *    of pcg_threads threads per cloth, each thread owning one node; needs
+ *    width * length <= pcg_threads * pcg_cluster for every cloth. */
+enum { YS_PCG_PHASES = 0, YS_PCG_PERSISTENT = 1 };
+/* Selects the PCG schedule for every later solve of the batch (steps, tangent
+ * and adjoint solves). YS_ERR_ARG if a cloth does not fit the persistent shape
+ * or the GPU cannot hold one cluster of it. */
+ys_status ys_set_pcg_schedule(ys_batch *b, int32_t pcg, int32_t threads, int32_t cluster);
+/* Times every schedule over `steps` steps of size h without an external force,
  * each from the batch's current state, which is restored afterwards, and makes
- * the fastest the batch's default. All schedules give bit-identical states. */
+ * the fastest the batch's default: graph or launch by launch x (phase PCG with
+ * check_every in {2, 4, 8, 16, 32}, or persistent PCG in every cluster shape
+ * that holds the largest cloth with at most 4x its nodes). All schedules give
+ * bit-identical states. */
 ys_status ys_autotune(ys_batch *b, double h, const ys_solve_opts *opts, int32_t steps, ys_schedule *best);
+/* The schedules the last ys_autotune timed, with their times: copies up to
+ * cap of them to out and returns how many there were (-1: null handle). */
+int32_t ys_autotune_results(const ys_batch *b, ys_schedule *out, int32_t cap);
 /* y = A x with the assembled matrices (node layout [total_nodes][5]). */
 ys_status ys_apply_system(ys_batch *b, const double *x, double *y, int32_t flags);
 /* y = A x like ys_apply_system, for callers that must not allocate at call
@@ -277,7 +299,8 @@ enum {
   YS_PROF_MISC = 12,     /* bookkeeping */
   YS_PROF_GNN = 13,      /* learned preconditioner: features, network, G blocks */
   YS_PROF_PREC = 14,     /* learned preconditioner: z = G^T G r */
-  YS_PROF_KINDS = 15
+  YS_PROF_PCG_PERSIST = 15, /* persistent per-cloth PCG (the whole solve in one launch) */
+  YS_PROF_KINDS = 16
 };
 /* enable = 1 brackets every launch with CUDA events on the handle's stream
  * (adds a little host overhead); the totals accumulate until read. */

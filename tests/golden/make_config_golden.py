@@ -11,7 +11,8 @@ physics sources in a serial build; see make_golden.py).
   rule (warp line v and weft line u take yarn v % 2 and u % 2,
   src/Cloth.cpp:195-268), type 0 within +-20 % of the values above, type 1 =
   type 0 times factors drawn uniformly in [1.5, 3] per parameter, upright,
-  two top corners pinned, h = 1e-3, 500 steps; every 10th state is kept.
+  two top corners pinned, h = 1e-3, 500 steps; every 10th state is kept,
+  and the state one step after every 20th.
 - driver_simheter10, driver_simcontrol5: the set-ups of the reference's
   SimHeter and SimControl drivers (src/Simulate.h:218-452), 30 steps each,
   every step kept (they pin the package's drivers, drivers.py).
@@ -65,7 +66,7 @@ def config1(rng, weave):
     warp = np.array([(y0, y1)[v % 2] for v in range(H)])
     weft = np.array([(y0, y1)[u % 2] for u in range(W)])
     return dict(W=W, H=H, weave=weave, pose=0, warp=warp, weft=weft, S=S, mu=mu, yarns=(y0, y1),
-                handles=[(0, 0), (W - 1, 0)], steps=500, keep_every=10)
+                handles=[(0, 0), (W - 1, 0)], steps=500, keep_every=10, pairs_every=20)
 
 
 def driver_heter():
@@ -132,7 +133,11 @@ def run_case(name, cs, tmp):
             f.write("%s=%s\n" % (k, v))
     subprocess.run([HARNESS, cpath], check=True, capture_output=True)
     rec = read_records(cfg["out"])
-    kept = [s for s in range(cs["steps"] + 1) if s % cs["keep_every"] == 0]
+    # every keep_every-th state, and the state after each pairs_every-th one
+    # (one step from the reference's own state: the per-step parity check)
+    pe = cs.get("pairs_every", 0)
+    kept = sorted(set(s for s in range(cs["steps"] + 1) if s % cs["keep_every"] == 0) |
+                  set(s + 1 for s in range(cs["steps"]) if pe and s % pe == 0))
     out = dict(width=W, length=H, weave=["plain", "twill", "satin"].index(cs["weave"]), pose=cs["pose"], L=L, R=R,
                height=height, mu=cs["mu"], S=cs["S"], kc=1.0, kf=1000.0, df=1000.0, handle_stiffness=1e4,
                G=np.array([0, 0, 9.8]), h=1e-3, warp=cs["warp"], weft=cs["weft"],
