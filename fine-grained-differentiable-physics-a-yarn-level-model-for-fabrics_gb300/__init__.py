@@ -11,7 +11,7 @@ from .cloth import (PI, ClothBatch, ClothSpec, ClothState, Cloth, EigenSolver, E
                     PhysicsCloth, SimStep, Wind, WovenPattern, Yarn, Adjoint, STATE_KEYS)
 from ._native import YarnSimError, load as load_library, library_path
 from .collide import Collider, Collision, cloth_mesh_topology
-from .learn import (PARAM_NAMES, YarnSimNetHeter, constraint_para, invert_constraint_para, position_loss, rollout,
+from .learn import (PARAM_NAMES, YarnSimNetHeter, YarnSimNetHomo, YarnSimNetColli, YarnSimNetControl, constraint_para, invert_constraint_para, position_loss, rollout,
                     rollout_with_jacobian, two_yarn_spec, CheckpointedRollout, rollout_adjoint,
                     two_yarn_param_grad)
 from .precond import LearnedPreconditioner, train as train_preconditioner, training_specs
@@ -28,5 +28,6 @@ __all__ = [
     "rollout", "rollout_with_jacobian", "two_yarn_spec", "Collider", "Collision", "cloth_mesh_topology",
     "LearnedPreconditioner", "train_preconditioner", "training_specs", "RenderCloth", "RenderType", "obj_text",
     "render_batch_cloth", "drivers", "DropOnSphere", "sim_collision", "sim_control", "sim_heter", "sim_homo",
-    "Adjoint", "STATE_KEYS", "CheckpointedRollout", "rollout_adjoint", "two_yarn_param_grad",
+    "Adjoint", "STATE_KEYS", "CheckpointedRollout", "rollout_adjoint", "two_yarn_param_grad", "YarnSimNetHomo",
+    "YarnSimNetColli", "YarnSimNetControl",
 ]

@@ -484,25 +484,27 @@ YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double*
   return ok;
 }
 
-// The SpMV rows read their input vector through an accessor: at(j) points at
-// component 0 of node j and component c sits c * stride() further on. The
-// global form below reads a [5][ntot] array; the persistent PCG reads its
-// direction from shared memory through another accessor. Both run the same
-// arithmetic, so they give the same bits.
+// The SpMV rows read their input vector through an accessor: at(j) is a
+// handle of node j and get(p, c) its component c. The global form below
+// reads a [5][ntot] array; the persistent PCG reads its direction from the
+// shared memory of the CTAs of a cluster through another accessor. Both run
+// the same arithmetic, so they give the same bits.
 struct GlobalVec {
   const double* YS_RESTRICT x;
   int64_t nt;
-  YS_HD const double* at(int j) const { return x + j; }
-  YS_HD int64_t stride() const { return nt; }
+  typedef const double* Ptr;
+  YS_HD Ptr at(int j) const { return x + j; }
+  YS_HD double get(Ptr p, int c) const { return p[c * nt]; }
 };
 
 // y = A x for row block n (5 rows). Couplings to grid positions outside the
 // cloth have zero coefficients; their column index is clamped to n so the
-// load stays in bounds and adds 0 * x(n).
+// load stays in bounds and adds 0 * x(n). Every coefficient enters one fused
+// multiply-add into its row's running sum, in slot order: 159 FMAs a row
+// block, the FP64 pipe's floor for this product.
 template <class XV>
 YS_HD void spmv_row_sv(const View& v, const double* YS_RESTRICT Ab, int64_t ss, const XV& xv, int n, double y[5]) {
   auto slot = [&](const View&, int s_, int n_) { return Ab[(int64_t)s_ * ss + n_]; };
-  const int64_t xs = xv.stride();
   const ClothParams& P = v.cp[v.node_cloth[n]];
   const int u = v.node_u[n], w = v.node_v[n];
   double yl0 = 0.0, yl1 = 0.0, yl2 = 0.0;
@@ -510,36 +512,41 @@ YS_HD void spmv_row_sv(const View& v, const double* YS_RESTRICT Ab, int64_t ss, 
     const int uu = u + stencil_du(s), vv = w + stencil_dv(s);
     const bool ok = uu >= 0 && uu < P.W && vv >= 0 && vv < P.H;
     const int j = ok ? n + stencil_du(s) + stencil_dv(s) * P.W : n;
-    const double* xp = xv.at(j);
-    const double xj0 = xp[0], xj1 = xp[xs], xj2 = xp[2 * xs];
+    const typename XV::Ptr xp = xv.at(j);
+    const double xj0 = xv.get(xp, 0), xj1 = xv.get(xp, 1), xj2 = xv.get(xp, 2);
     const int b = YS_SLOT_LL + 9 * s;
-    yl0 += slot(v, b + 0, n) * xj0 + slot(v, b + 1, n) * xj1 + slot(v, b + 2, n) * xj2;
-    yl1 += slot(v, b + 3, n) * xj0 + slot(v, b + 4, n) * xj1 + slot(v, b + 5, n) * xj2;
-    yl2 += slot(v, b + 6, n) * xj0 + slot(v, b + 7, n) * xj1 + slot(v, b + 8, n) * xj2;
+    yl0 = fma(slot(v, b + 0, n), xj0, yl0); yl0 = fma(slot(v, b + 1, n), xj1, yl0); yl0 = fma(slot(v, b + 2, n), xj2, yl0);
+    yl1 = fma(slot(v, b + 3, n), xj0, yl1); yl1 = fma(slot(v, b + 4, n), xj1, yl1); yl1 = fma(slot(v, b + 5, n), xj2, yl1);
+    yl2 = fma(slot(v, b + 6, n), xj0, yl2); yl2 = fma(slot(v, b + 7, n), xj1, yl2); yl2 = fma(slot(v, b + 8, n), xj2, yl2);
   }
-  const double* xn = xv.at(n);
-  const double xu = xn[3 * xs], xv_ = xn[4 * xs];
-  yl0 += slot(v, YS_SLOT_LE_SELF + 0, n) * xu + slot(v, YS_SLOT_LE_SELF + 1, n) * xv_;
-  yl1 += slot(v, YS_SLOT_LE_SELF + 2, n) * xu + slot(v, YS_SLOT_LE_SELF + 3, n) * xv_;
-  yl2 += slot(v, YS_SLOT_LE_SELF + 4, n) * xu + slot(v, YS_SLOT_LE_SELF + 5, n) * xv_;
-  const double xl0 = xn[0], xl1 = xn[xs], xl2 = xn[2 * xs];
+  const typename XV::Ptr xn = xv.at(n);
+  const double xu = xv.get(xn, 3), xv_ = xv.get(xn, 4);
+  yl0 = fma(slot(v, YS_SLOT_LE_SELF + 0, n), xu, yl0); yl0 = fma(slot(v, YS_SLOT_LE_SELF + 1, n), xv_, yl0);
+  yl1 = fma(slot(v, YS_SLOT_LE_SELF + 2, n), xu, yl1); yl1 = fma(slot(v, YS_SLOT_LE_SELF + 3, n), xv_, yl1);
+  yl2 = fma(slot(v, YS_SLOT_LE_SELF + 4, n), xu, yl2); yl2 = fma(slot(v, YS_SLOT_LE_SELF + 5, n), xv_, yl2);
+  const double xl0 = xv.get(xn, 0), xl1 = xv.get(xn, 1), xl2 = xv.get(xn, 2);
   double ye[2];
-  for (int k = 0; k < 2; ++k)
-    ye[k] = slot(v, YS_SLOT_EL_SELF + 3 * k + 0, n) * xl0 + slot(v, YS_SLOT_EL_SELF + 3 * k + 1, n) * xl1 +
-            slot(v, YS_SLOT_EL_SELF + 3 * k + 2, n) * xl2 + slot(v, YS_SLOT_EE_SELF + k, n) * xn[(3 + k) * xs];
+  for (int k = 0; k < 2; ++k) {
+    double e = slot(v, YS_SLOT_EL_SELF + 3 * k + 0, n) * xl0;
+    e = fma(slot(v, YS_SLOT_EL_SELF + 3 * k + 1, n), xl1, e);
+    e = fma(slot(v, YS_SLOT_EL_SELF + 3 * k + 2, n), xl2, e);
+    ye[k] = fma(slot(v, YS_SLOT_EE_SELF + k, n), k ? xv_ : xu, e);
+  }
   for (int m = 0; m < 4; ++m) {
     const int du = m == 0 ? -1 : m == 1 ? 1 : 0, dv = m == 2 ? -1 : m == 3 ? 1 : 0;
     const int k = m < 2 ? 0 : 1;
     const int uu = u + du, vv = w + dv;
     const bool ok = uu >= 0 && uu < P.W && vv >= 0 && vv < P.H;
     const int j = ok ? n + du + dv * P.W : n;
-    const double* xp = xv.at(j);
-    const double xe = xp[(3 + k) * xs];
-    yl0 += slot(v, YS_SLOT_LE_NBR + 3 * m + 0, n) * xe;
-    yl1 += slot(v, YS_SLOT_LE_NBR + 3 * m + 1, n) * xe;
-    yl2 += slot(v, YS_SLOT_LE_NBR + 3 * m + 2, n) * xe;
-    ye[k] += slot(v, YS_SLOT_EL_NBR + 3 * m + 0, n) * xp[0] + slot(v, YS_SLOT_EL_NBR + 3 * m + 1, n) * xp[xs] +
-             slot(v, YS_SLOT_EL_NBR + 3 * m + 2, n) * xp[2 * xs] + slot(v, YS_SLOT_EE_NBR + m, n) * xe;
+    const typename XV::Ptr xp = xv.at(j);
+    const double xe = xv.get(xp, 3 + k);
+    yl0 = fma(slot(v, YS_SLOT_LE_NBR + 3 * m + 0, n), xe, yl0);
+    yl1 = fma(slot(v, YS_SLOT_LE_NBR + 3 * m + 1, n), xe, yl1);
+    yl2 = fma(slot(v, YS_SLOT_LE_NBR + 3 * m + 2, n), xe, yl2);
+    ye[k] = fma(slot(v, YS_SLOT_EL_NBR + 3 * m + 0, n), xv.get(xp, 0), ye[k]);
+    ye[k] = fma(slot(v, YS_SLOT_EL_NBR + 3 * m + 1, n), xv.get(xp, 1), ye[k]);
+    ye[k] = fma(slot(v, YS_SLOT_EL_NBR + 3 * m + 2, n), xv.get(xp, 2), ye[k]);
+    ye[k] = fma(slot(v, YS_SLOT_EE_NBR + m, n), xe, ye[k]);
   }
   y[0] = yl0;
   y[1] = yl1;
@@ -561,7 +568,6 @@ YS_HD void spmv_row(const View& v, const double* YS_RESTRICT x, int n, double y[
 // column block n (i = n - offset of its slot) is read from row i, transposed.
 template <class XV>
 YS_HD void spmv_row_tv(const View& v, const XV& xv, int n, double y[5]) {
-  const int64_t xs = xv.stride();
   const ClothParams& P = v.cp[v.node_cloth[n]];
   const int u = v.node_u[n], w = v.node_v[n];
   double yl[3] = {0.0, 0.0, 0.0}, ye[2] = {0.0, 0.0};
@@ -570,20 +576,25 @@ YS_HD void spmv_row_tv(const View& v, const XV& xv, int n, double y[5]) {
     const int uu = u - du, vv = w - dv;  // the row that refers to n through slot s
     if (uu < 0 || uu >= P.W || vv < 0 || vv >= P.H) continue;
     const int i = n - du - dv * P.W;
-    const double* xp = xv.at(i);
-    const double x0 = xp[0], x1 = xp[xs], x2 = xp[2 * xs];
+    const typename XV::Ptr xp = xv.at(i);
+    const double x0 = xv.get(xp, 0), x1 = xv.get(xp, 1), x2 = xv.get(xp, 2);
     const int b = YS_SLOT_LL + 9 * s;
-    for (int c = 0; c < 3; ++c)
-      yl[c] += slot(v, b + c, i) * x0 + slot(v, b + 3 + c, i) * x1 + slot(v, b + 6 + c, i) * x2;
+    for (int c = 0; c < 3; ++c) {
+      yl[c] = fma(slot(v, b + c, i), x0, yl[c]);
+      yl[c] = fma(slot(v, b + 3 + c, i), x1, yl[c]);
+      yl[c] = fma(slot(v, b + 6 + c, i), x2, yl[c]);
+    }
   }
   {  // the node's own Eulerian couplings
-    const double* xp = xv.at(n);
-    const double x0 = xp[0], x1 = xp[xs], x2 = xp[2 * xs];
+    const typename XV::Ptr xp = xv.at(n);
+    const double x0 = xv.get(xp, 0), x1 = xv.get(xp, 1), x2 = xv.get(xp, 2);
     for (int k = 0; k < 2; ++k) {
-      const double xe = xp[(3 + k) * xs];
-      ye[k] += slot(v, YS_SLOT_LE_SELF + 0 + k, n) * x0 + slot(v, YS_SLOT_LE_SELF + 2 + k, n) * x1 +
-               slot(v, YS_SLOT_LE_SELF + 4 + k, n) * x2 + slot(v, YS_SLOT_EE_SELF + k, n) * xe;
-      for (int c = 0; c < 3; ++c) yl[c] += slot(v, YS_SLOT_EL_SELF + 3 * k + c, n) * xe;
+      const double xe = xv.get(xp, 3 + k);
+      ye[k] = fma(slot(v, YS_SLOT_LE_SELF + 0 + k, n), x0, ye[k]);
+      ye[k] = fma(slot(v, YS_SLOT_LE_SELF + 2 + k, n), x1, ye[k]);
+      ye[k] = fma(slot(v, YS_SLOT_LE_SELF + 4 + k, n), x2, ye[k]);
+      ye[k] = fma(slot(v, YS_SLOT_EE_SELF + k, n), xe, ye[k]);
+      for (int c = 0; c < 3; ++c) yl[c] = fma(slot(v, YS_SLOT_EL_SELF + 3 * k + c, n), xe, yl[c]);
     }
   }
   for (int m = 0; m < 4; ++m) {  // yarn neighbour i = n - offset(m) refers to n through m
@@ -592,11 +603,13 @@ YS_HD void spmv_row_tv(const View& v, const XV& xv, int n, double y[5]) {
     const int uu = u - du, vv = w - dv;
     if (uu < 0 || uu >= P.W || vv < 0 || vv >= P.H) continue;
     const int i = n - du - dv * P.W;
-    const double* xp = xv.at(i);
-    const double xe = xp[(3 + k) * xs];
-    ye[k] += slot(v, YS_SLOT_LE_NBR + 3 * m + 0, i) * xp[0] + slot(v, YS_SLOT_LE_NBR + 3 * m + 1, i) * xp[xs] +
-             slot(v, YS_SLOT_LE_NBR + 3 * m + 2, i) * xp[2 * xs] + slot(v, YS_SLOT_EE_NBR + m, i) * xe;
-    for (int c = 0; c < 3; ++c) yl[c] += slot(v, YS_SLOT_EL_NBR + 3 * m + c, i) * xe;
+    const typename XV::Ptr xp = xv.at(i);
+    const double xe = xv.get(xp, 3 + k);
+    ye[k] = fma(slot(v, YS_SLOT_LE_NBR + 3 * m + 0, i), xv.get(xp, 0), ye[k]);
+    ye[k] = fma(slot(v, YS_SLOT_LE_NBR + 3 * m + 1, i), xv.get(xp, 1), ye[k]);
+    ye[k] = fma(slot(v, YS_SLOT_LE_NBR + 3 * m + 2, i), xv.get(xp, 2), ye[k]);
+    ye[k] = fma(slot(v, YS_SLOT_EE_NBR + m, i), xe, ye[k]);
+    for (int c = 0; c < 3; ++c) yl[c] = fma(slot(v, YS_SLOT_EL_NBR + 3 * m + c, i), xe, yl[c]);
   }
   y[0] = yl[0];
   y[1] = yl[1];

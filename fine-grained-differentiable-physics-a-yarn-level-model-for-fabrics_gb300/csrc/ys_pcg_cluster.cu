@@ -19,6 +19,8 @@
 #include <cooperative_groups.h>
 
 #include <cfloat>
+#include <cstdint>
+#include <type_traits>
 
 #include "ys_items.cuh"
 #include "ys_kernels.cuh"
@@ -31,19 +33,37 @@ namespace {
 
 constexpr int kMaxClusterBlocks = 128;  // 128-node blocks per cloth (16 CTAs x 1024 threads)
 
-// the cluster's direction vector: node li of the cloth at rank li / T, slot li % T
+// The cluster's direction vector: node li of the cloth at rank li / T, slot
+// li % T of that CTA's [5][T] slice. Handles are 32-bit shared::cluster
+// addresses (mapa), read with ld.shared::cluster; without a cluster, plain
+// shared-memory pointers.
 template <int T, bool CLUSTER>
 struct ClusterVec {
-  double* base;  // this CTA's [5][T] slice
-  int off;       // the cloth's first node
-  __device__ __forceinline__ const double* at(int j) const {
+  double* base;    // this CTA's [5][T] slice
+  uint32_t base32; // its shared::cta address
+  int off;         // the cloth's first node
+  typedef typename std::conditional<CLUSTER, uint32_t, const double*>::type Ptr;
+  __device__ __forceinline__ Ptr at(int j) const {
     const int lj = j - off;
-    if (!CLUSTER) return base + lj;
-    const int rk = lj / T;
-    double* b = cg::this_cluster().map_shared_rank(base, rk);
-    return b + (lj - rk * T);
+    if constexpr (!CLUSTER) {
+      return base + lj;
+    } else {
+      const int rk = lj / T;
+      const uint32_t a = base32 + 8u * (uint32_t)(lj - rk * T);
+      uint32_t r;
+      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rk));
+      return r;
+    }
   }
-  __device__ __forceinline__ int64_t stride() const { return T; }
+  __device__ __forceinline__ double get(Ptr p, int c) const {
+    if constexpr (!CLUSTER) {
+      return p[c * T];
+    } else {
+      double x;
+      asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(x) : "r"(p + 8u * (uint32_t)(c * T)));
+      return x;
+    }
+  }
 };
 
 // Sums NQ per-thread values over the cloth in the batched solver's order and
@@ -121,7 +141,7 @@ __global__ void __launch_bounds__(T, 1) k_pcg_cluster(View v, Solver so, const i
   const bool own = li < N;
   const int n = off + (own ? li : 0);
   const int nt = v.ntot;
-  const ClusterVec<T, CLUSTER> pv{psm, off};
+  const ClusterVec<T, CLUSTER> pv{psm, (uint32_t)__cvta_generic_to_shared(psm), off};
   const int maxiter = pc.maxiter;
   const bool ok_sys = pc.status == 0;  // read before any CTA of the cluster can write it
   int red = 0;  // reductions so far: selects the warp-partial buffer

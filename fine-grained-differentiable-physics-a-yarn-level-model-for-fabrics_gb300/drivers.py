@@ -17,6 +17,8 @@ reads back. `height` defaults to the reference's 5 m.
 - DropOnSphere   the collision benchmark scene: a flat cloth dropped onto an
                  icosphere with self-collision (the reference's collision
                  step, SimStep with a Collision)
+- train_heter_full  train_heter_full  src/TrainHeter.h:11-306 (parameter
+                 learning from a SimHeter trajectory file)
 """
 from __future__ import annotations
 
@@ -378,3 +380,102 @@ class CentroidControl:
                 out["self"] += int((~obs).sum())
             prev = x
         return out
+
+
+# ------------------------------------------------------------ training driver
+# train_heter_full's starting values and ranges (src/TrainHeter.h:50-100;
+# ranges are (upper, lower) pairs as the reference passes them)
+HETER_INIT = dict(rho_1=0.00225, rho_2=0.00245, Y_1=335000.0, Y_2=145000.0, B_1=0.000125, B_2=0.0001, S=600.0,
+                  mu=0.7)
+HETER_RANGES = dict(rho_1=(0.003, 0.001), rho_2=(0.003, 0.001), Y_1=(800000.0, 0.0), Y_2=(300000.0, 0.0),
+                    B_1=(0.00018, 0.00005), B_2=(0.00018, 0.00005), S=(1200.0, 0.0), mu=(1.0, 0.0))
+# per-parameter SGD learning rates (src/TrainHeter.h:131-150)
+HETER_LR = dict(rho_1=0.1, rho_2=1e-4, Y_1=12e16, Y_2=7e16, B_1=0.219, B_2=0.145, S=19e10, mu=14e9)
+
+
+def train_heter_full(data_path: str, epoch: int = 1, iters: int = 1, batch: int = 1, sample: int = 10,
+                     steps: Optional[int] = None, all_steps: bool = True, random: bool = False,
+                     save_path: Optional[str] = None, init: Optional[Dict[str, float]] = None,
+                     ranges: Optional[Dict[str, Tuple[float, float]]] = None, lr: Optional[Dict[str, float]] = None,
+                     handles=None, h: float = 1e-3, mode: str = "reference", seed: int = 0,
+                     wordy: bool = False) -> Dict:
+    """train_heter_full (src/TrainHeter.h:11-306): learns the eight
+    parameters of a two-yarn cloth (rho, Y, B of each yarn type, S, mu,
+    through constraint_para) from a trajectory file SimHeter wrote
+    (data_path, the reference's HDF5 layout). Per iteration: `batch` samples
+    of `sample` consecutive states (sequential, or drawn at random), each
+    rolled out for sample - 1 steps from its first state on the GPU with the
+    forward-mode Jacobian; loss = sum over steps of mean |x - x^|^2 + mean
+    |e - e^|^2, divided by (successful steps - 1); SGD with the reference's
+    per-parameter learning rates, skipped when a gradient is not finite.
+    samples = steps // sample; iterations = (iters if random else samples //
+    batch) when all_steps, else iters. handles default to the two top
+    corners (the reference hard-codes (0, 0), (16, 0) for its 17 x 17
+    cloth). Returns dict(loss=[...], params={name: [...]}, grad={name:
+    [...]}) per training step (constrained parameters after the step; the
+    raw parameters' gradients) and, with save_path, writes loss and
+    parameters as SaveTrainProc does (datasets Loss, rho1, rho2, Y1, Y2, B1,
+    B2, S, mu; src/Saver.cpp:93-150)."""
+    import torch
+    from .learn import YarnSimNetHeter, constraint_para, invert_constraint_para, rollout_with_jacobian
+
+    size, phy = _h5.cloth_property_loader_heter(data_path)
+    W, L = int(size["width"]), int(size["length"])
+    if steps is None:
+        steps = int(len(_h5.read(data_path)["/Steps/Position/Node 0 0/LPOS"]))
+    samples = steps // sample
+    iteration = (iters if random else samples // batch) if all_steps else iters
+    ranges = dict(HETER_RANGES, **(ranges or {}))
+    init = dict(HETER_INIT, **(init or {}))
+    lr = dict(HETER_LR, **(lr or {}))
+    raw = {k: invert_constraint_para(v, *ranges[k]) for k, v in init.items()}
+    handles = handles if handles is not None else [(0, 0), (W - 1, 0)]
+    net = YarnSimNetHeter(W, L, float(phy["R"]), float(phy["L"]), raw, ranges, handles, h=h, kf=float(phy["kf"]),
+                          df=float(phy["df"]), kc=float(phy["kc"]), handle_stiffness=float(phy["handle_stiff"]),
+                          gravity=float(phy["Gravity"]),
+                          wind_vel=(phy["wind_velocity_x"], phy["wind_velocity_y"], phy["wind_velocity_z"]),
+                          wind_density=float(phy["wind_density"]), wind_drag=float(phy["wind_drag"]),
+                          woven_pattern=int(phy["woven_pattern"]), mode=mode)
+    names = ("rho_1", "rho_2", "Y_1", "Y_2", "B_1", "B_2", "S", "mu")
+    opt = torch.optim.SGD([{"params": [getattr(net, n)], "lr": lr[n]} for n in names], lr=1e5)
+    rng = np.random.default_rng(seed)
+    hist = {"loss": [], "params": {n: [] for n in names}, "grad": {n: [] for n in names}}
+    for epc in range(epoch):
+        for it in range(iteration):
+            opt.zero_grad()
+            theta = net.theta()
+            th = theta.detach().cpu().numpy()
+            gtheta = np.zeros(8)
+            loss, success = 0.0, 0
+            for bch in range(batch):
+                choice = int(rng.integers(0, samples)) if random else it * batch + bch
+                data = _h5.data_loader(data_path, choice * sample, choice * sample + sample)
+                state0 = {k: data[k][0] for k in FULL}
+                tx, te, Jx, Je, stats = rollout_with_jacobian(net.template, th, state0, sample - 1, h, mode)
+                n_ok = next((s for s, st in enumerate(stats) if not st[0]["ok"]), sample - 1)
+                for s in range(n_ok):
+                    dx = tx[s] - data["LPos"][s + 1]
+                    de = te[s] - data["EPos"][s + 1]
+                    loss += float((dx * dx).sum(-1).mean() + (de * de).sum(-1).mean())
+                    gtheta += np.einsum("nc,ncp->p", 2.0 * dx / len(dx), Jx[s])
+                    gtheta += np.einsum("nc,ncp->p", 2.0 * de / len(de), Je[s])
+                success += n_ok
+            div = max(success - 1, 1)
+            loss /= div
+            theta.backward(torch.as_tensor(gtheta / div, dtype=theta.dtype))
+            for n in names:
+                hist["grad"][n].append(float(getattr(net, n).grad[0]))
+            if all(torch.isfinite(getattr(net, n).grad).all() for n in names):
+                opt.step()
+            hist["loss"].append(loss)
+            for n in names:
+                hist["params"][n].append(float(constraint_para(getattr(net, n), *ranges[n])))
+            if wordy:
+                print("epoch %d batch %d loss %.6e" % (epc, it, loss))
+    if save_path:
+        T = len(hist["loss"])
+        ds = {"/Loss": np.array(hist["loss"]).reshape(T, 1)}
+        for n in names:
+            ds["/" + n.replace("_", "")] = np.array(hist["params"][n]).reshape(T, 1)
+        _h5.write(save_path, ds)
+    return hist

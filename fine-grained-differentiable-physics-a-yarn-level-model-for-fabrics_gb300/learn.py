@@ -172,19 +172,51 @@ class CheckpointedRollout:
     instead (src/TrainHeter.h:160-231).
 
     ext_forces: None, or a list of [total_nodes, 5] arrays (None entries: no
-    force) for steps 0..steps-1 -- per-node control forces."""
+    force) for steps 0..steps-1 -- per-node control forces.
+
+    collision: a collide.Collision of the batch's (single) cloth: every step
+    is then SimStep with collision (src/TrainHelper.cpp:99-149): the step,
+    collision_response(damp) and, when it moved anything, the write-back of
+    positions and velocities (fixed positions follow the nodes that are not
+    in `fixed`, a [total_nodes] bool mask of the handles). The backward pass
+    runs the response's backward (impacts' weights and normals carried into
+    the positions, as the reference's autograd does; exact_root: the CCD
+    root's exact derivative instead of the reference's CubicSolver backward)
+    before each step's adjoint."""
 
     FULL = ("LPos", "LPosFix", "LVel", "EPos", "EPosBar", "EVel")
 
     def __init__(self, batch: ClothBatch, state0: Dict, steps: int, h: float = 1e-3, ext_forces=None,
-                 mode: str = "exact", checkpoint_every: int = 20, tol: float = 0.0, copies: int = 128):
+                 mode: str = "exact", checkpoint_every: int = 20, tol: float = 0.0, copies: int = 128,
+                 collision=None, damp: float = 0.1, fixed=None, exact_root: bool = False):
         self.batch, self.steps, self.h, self.mode, self.tol = batch, int(steps), float(h), mode, tol
         self.k = max(1, int(checkpoint_every))
         self.ext = ext_forces
         self.state0 = {k: np.array(state0[k], dtype=np.float64) for k in self.FULL if k in state0}
         self.copies = copies
+        self.collision, self.damp, self.exact_root = collision, float(damp), bool(exact_root)
+        self.fixed = np.zeros(batch.total_nodes, bool) if fixed is None else np.asarray(fixed, bool)
         self.checkpoints = {}
         self.ok = True
+
+    def _advance(self, s):
+        """Step s from the batch's state (with the collision response when
+        given); returns whether the response moved anything."""
+        b = self.batch
+        before = b.get_state() if self.collision is not None else None
+        st = b.step(self.h, self._ext(s), tol=self.tol)
+        self.ok = self.ok and all(x["ok"] for x in st)
+        if self.collision is None or not st[0]["ok"]:
+            return False
+        cur = b.get_state()
+        if not self.collision.collision_response(self.damp, cur["LPos"], before["LPos"], cur["LVel"]):
+            return False
+        r = self.collision.last
+        fix = cur["LPosFix"].copy()
+        fix[~self.fixed] = r["x"][~self.fixed]
+        b.set_state(LPos=r["x"], LPosFix=fix, LVel=r["v"], EPos=cur["EPos"], EPosBar=cur["EPosBar"],
+                    EVel=cur["EVel"])
+        return True
 
     def _ext(self, s):
         if self.ext is None:
@@ -201,8 +233,7 @@ class CheckpointedRollout:
         for s in range(self.steps):
             if s % self.k == 0:
                 self.checkpoints[s] = b.get_state()
-            st = b.step(self.h, self._ext(s), tol=self.tol)
-            self.ok = self.ok and all(x["ok"] for x in st)
+            self._advance(s)
             cur = b.get_state()
             for k in STATE_KEYS:
                 traj[k].append(cur[k])
@@ -237,10 +268,21 @@ class CheckpointedRollout:
                 for s in range(a, e):
                     seg.append(b.get_state())
                     if s + 1 < e:
-                        b.step(self.h, self._ext(s), tol=self.tol)
+                        self._advance(s)
                 for s in range(e - 1, a - 1, -1):
+                    g_prev = None
+                    if self.collision is not None:
+                        # the step and its response again, then the response's backward
+                        b.set_state(**seg[s - a])
+                        if self._advance(s):
+                            rb = self.collision.collider.respond_backward(dl_dx=g["LPos"], dl_dv=g["LVel"],
+                                                                         impacts=True, exact_root=self.exact_root)
+                            g = dict(g, LPos=rb["x"], LVel=rb["v"])
+                            g_prev = rb["x_prev"]
                     b.set_state(**seg[s - a])
                     gs, gp, ge = adj.step_back(self.h, g, self._ext(s), tol=self.tol, want_ext=want_ext)
+                    if g_prev is not None:
+                        gs["LPos"] = gs["LPos"] + g_prev
                     for k in acc:
                         acc[k] += gp[k]
                     if want_ext:
@@ -365,6 +407,299 @@ class YarnSimNetHeter(_module_base()):
         try:
             b.set_state(**state)
             ok = b.step(self.h, tol=tol)[0]["ok"]
+            return b.get_state(), ok
+        finally:
+            b.close()
+
+
+def _homo_theta(net, names=("rho", "Y", "B")):
+    """The 8-vector of two_yarn_spec for a one-yarn cloth: both yarn types
+    carry the same constrained rho, Y, B (the lines of a homogeneous cloth);
+    S and mu are the module's parameter or constant."""
+    import torch
+    p = {}
+    for n in ("rho", "Y", "B", "S", "mu"):
+        if n in net.ranges and isinstance(getattr(net, n, None), torch.nn.Parameter):
+            p[n] = constraint_para(getattr(net, n), *net.ranges[n])
+        else:
+            p[n] = torch.tensor([float(net.const[n])], dtype=torch.float64)
+    return torch.cat([p["rho"], p["Y"], p["B"], p["rho"], p["Y"], p["B"], p["S"], p["mu"]])
+
+
+class YarnSimNetHomo(_module_base()):
+    """The reference's YarnSimNetHomo (src/YarnSimNetHomo.h:4-111): raw
+    parameters rho, Y, B, S of one yarn type mapped into their ranges by
+    constraint_para ((upper, lower) pairs, as the reference passes them),
+    mu, kf, df, kc fixed, an upright cloth at height 0 with handles, and its
+    step. rollout(state0, steps) is differentiable w.r.t. the four raw
+    parameters (forward-mode tangents; rollout_adjoint: the reverse adjoint
+    with checkpoints); forward(state) is one step without a graph (the
+    reference's forward(ClothState, bool&))."""
+
+    def __init__(self, width: int, length: int, R: float, L: float, raw: Dict[str, float],
+                 ranges: Dict[str, Tuple[float, float]], handles: Sequence[Tuple[int, int]], h: float = 1e-3,
+                 mu: float = 0.5, kf: float = 1000.0, df: float = 1000.0, kc: float = 1.0,
+                 handle_stiffness: float = 1e4, gravity: float = 9.8, wind_vel=(0.0, 0.0, 0.0),
+                 wind_density: float = 0.0, wind_drag: float = 0.0, woven_pattern: int = WovenPattern.Plain,
+                 height: float = 0.0, mode: str = "reference"):
+        import torch
+        super().__init__()
+        for n in ("rho", "Y", "B", "S"):
+            self.register_parameter(n, torch.nn.Parameter(torch.tensor([float(raw[n])], dtype=torch.float64)))
+        self.ranges = {n: ranges[n] for n in ("rho", "Y", "B", "S")}
+        self.const = dict(mu=float(mu))
+        self.h, self.mode = float(h), mode
+        self.template = dict(width=width, length=length, height=height, L=L, R=R, pose=InitPose.Upright,
+                             weave=int(woven_pattern), kc=kc, kf=kf, df=df, handle_stiffness=handle_stiffness,
+                             G=(0.0, 0.0, gravity), wind_vel=tuple(wind_vel), wind_density=wind_density,
+                             wind_drag=wind_drag, handles=list(handles))
+
+    def theta(self):
+        """The constrained parameters in PARAM_NAMES order (both yarn types equal)."""
+        return _homo_theta(self)
+
+    def spec(self) -> ClothSpec:
+        return two_yarn_spec(self.template, self.theta().detach().cpu().numpy())
+
+    def rollout(self, state0: Dict, steps: int, tol: float = 0.0):
+        return rollout(self.theta(), self.template, state0, steps, self.h, self.mode, tol)
+
+    def rollout_adjoint(self, state0: Dict, steps: int, checkpoint_every: int = 20, tol: float = 0.0):
+        return rollout_adjoint(self.theta(), self.template, state0, steps, self.h, self.mode, tol, checkpoint_every)
+
+    def forward(self, state: Dict, tol: float = 0.0) -> Tuple[Dict, bool]:
+        b = ClothBatch([self.spec()])
+        try:
+            b.set_state(**state)
+            ok = b.step(self.h, tol=tol)[0]["ok"]
+            return b.get_state(), ok
+        finally:
+            b.close()
+
+
+def _colli_rollout_function():
+    import torch
+
+    class CollisionRollout(torch.autograd.Function):
+        """traj_x, traj_e = CollisionRollout.apply(theta, net, state0, steps, k):
+        a rollout with the collision response at every step, differentiable
+        w.r.t. theta (PARAM_NAMES order) through the reverse adjoint and the
+        response's backward (CheckpointedRollout with a collision)."""
+
+        @staticmethod
+        def forward(ctx, theta, net, state0, steps, k):
+            from .collide import Collision
+            spec = two_yarn_spec(net.template, theta.detach().cpu().numpy().astype(np.float64))
+            batch = ClothBatch([spec])
+            W = spec.width
+            fixed = np.zeros(spec.num_nodes, bool)
+            for (u, v) in spec.handles:
+                fixed[u + v * W] = True
+            col = Collision(_Shape(spec), net.obstacle_x, net.obstacle_faces, thickness=net.thickness, h=net.h)
+            ro = CheckpointedRollout(batch, state0, steps, net.h, mode=net.mode, checkpoint_every=k,
+                                     collision=col, damp=0.1, fixed=fixed, exact_root=net.mode == "exact")
+            traj = ro.forward()
+            ctx.ro, ctx.spec, ctx.col = ro, spec, col
+            dev = theta.device
+            return torch.as_tensor(traj["LPos"], device=dev), torch.as_tensor(traj["EPos"], device=dev)
+
+        @staticmethod
+        def backward(ctx, gx, ge):
+            ro = ctx.ro
+            try:
+                g = ro.backward({"LPos": gx.detach().cpu().numpy(), "EPos": ge.detach().cpu().numpy()})
+            finally:
+                ro.batch.close()
+                ctx.col.close()
+            gt = torch.as_tensor(two_yarn_param_grad(ctx.spec, g), dtype=gx.dtype, device=gx.device)
+            return gt, None, None, None, None
+
+    return CollisionRollout
+
+
+class _Shape:
+    """width / length holder for collide.Collision."""
+
+    def __init__(self, spec):
+        self.width, self.length = spec.width, spec.length
+
+
+_COLLI_ROLLOUT = None
+
+
+class YarnSimNetColli(_module_base()):
+    """The reference's YarnSimNetColli (src/YarnSimNetColli.h:4-116): raw
+    rho, Y, B of one yarn type (constraint_para into their ranges), S, mu,
+    kf, df, kc fixed, an upright plain cloth at `height` with handles, and
+    SimStep with collision against the table and ground meshes (merged into
+    one obstacle, as the reference's collision reports their pairs; thickness
+    0.5 mm) -- src/TrainHelper.cpp:99-149. forward(state) is one step;
+    rollout(state0, steps) is differentiable w.r.t. the three raw
+    parameters through the reverse adjoint and the collision response's
+    backward."""
+
+    def __init__(self, width: int, length: int, height: float, R: float, L: float, raw: Dict[str, float],
+                 ranges: Dict[str, Tuple[float, float]], handles: Sequence[Tuple[int, int]], obstacle_x,
+                 obstacle_faces, h: float = 1e-3, S: float = 1000.0, mu: float = 0.5, kf: float = 1000.0,
+                 df: float = 1000.0, kc: float = 1.0, handle_stiffness: float = 1e4, gravity: float = 9.8,
+                 wind_vel=(0.0, 0.0, 0.0), wind_density: float = 0.0, wind_drag: float = 0.0,
+                 thickness: float = 0.0005, mode: str = "reference"):
+        import torch
+        super().__init__()
+        for n in ("rho", "Y", "B"):
+            self.register_parameter(n, torch.nn.Parameter(torch.tensor([float(raw[n])], dtype=torch.float64)))
+        self.ranges = {n: ranges[n] for n in ("rho", "Y", "B")}
+        self.const = dict(S=float(S), mu=float(mu))
+        self.h, self.mode, self.thickness = float(h), mode, float(thickness)
+        self.obstacle_x = np.ascontiguousarray(obstacle_x, np.float64)
+        self.obstacle_faces = np.ascontiguousarray(obstacle_faces, np.int32)
+        self.template = dict(width=width, length=length, height=height, L=L, R=R, pose=InitPose.Upright,
+                             weave=int(WovenPattern.Plain), kc=kc, kf=kf, df=df, handle_stiffness=handle_stiffness,
+                             G=(0.0, 0.0, gravity), wind_vel=tuple(wind_vel), wind_density=wind_density,
+                             wind_drag=wind_drag, handles=list(handles))
+
+    def theta(self):
+        return _homo_theta(self)
+
+    def spec(self) -> ClothSpec:
+        return two_yarn_spec(self.template, self.theta().detach().cpu().numpy())
+
+    def rollout(self, state0: Dict, steps: int, checkpoint_every: int = 20):
+        global _COLLI_ROLLOUT
+        if _COLLI_ROLLOUT is None:
+            _COLLI_ROLLOUT = _colli_rollout_function()
+        return _COLLI_ROLLOUT.apply(self.theta(), self, state0, steps, checkpoint_every)
+
+    def forward(self, state: Dict, tol: float = 0.0) -> Tuple[Dict, bool]:
+        from .collide import Collision
+        spec = self.spec()
+        b = ClothBatch([spec])
+        col = Collision(_Shape(spec), self.obstacle_x, self.obstacle_faces, thickness=self.thickness, h=self.h)
+        try:
+            fixed = np.zeros(spec.num_nodes, bool)
+            for (u, v) in spec.handles:
+                fixed[u + v * spec.width] = True
+            ro = CheckpointedRollout(b, state, 1, self.h, collision=col, damp=0.1, fixed=fixed, tol=tol)
+            b.set_state(**ro.state0)
+            ro._advance(0)
+            return b.get_state(), ro.ok
+        finally:
+            col.close()
+            b.close()
+
+
+def _control_rollout_function():
+    import torch
+
+    class ControlRollout(torch.autograd.Function):
+        """traj_x, traj_e = ControlRollout.apply(forces, net, state0, schedule, k):
+        forces [6, 2] (lift, drag) of the six force settings; schedule[s] the
+        setting of step s (6: no force). Differentiable w.r.t. the forces
+        through the reverse adjoint's dL/d(ext force)."""
+
+        @staticmethod
+        def forward(ctx, forces, net, state0, schedule, k):
+            f = forces.detach().cpu().numpy().astype(np.float64)
+            exts = [net.ext_force(int(i), f) for i in schedule]
+            batch = ClothBatch([net.spec()])
+            ro = CheckpointedRollout(batch, state0, len(schedule), net.h, ext_forces=exts, mode=net.mode,
+                                     checkpoint_every=k)
+            traj = ro.forward()
+            ctx.ro, ctx.schedule, ctx.net = ro, list(schedule), net
+            dev = forces.device
+            return torch.as_tensor(traj["LPos"], device=dev), torch.as_tensor(traj["EPos"], device=dev)
+
+        @staticmethod
+        def backward(ctx, gx, ge):
+            ro = ctx.ro
+            try:
+                g = ro.backward({"LPos": gx.detach().cpu().numpy(), "EPos": ge.detach().cpu().numpy()},
+                                want_ext=True)
+            finally:
+                ro.batch.close()
+            gf = np.zeros((6, 2))
+            nodes = ctx.net.force_nodes()
+            for s, i in enumerate(ctx.schedule):
+                if 0 <= i < 6:
+                    gf[i, 0] += g["ext"][s][nodes, 2].sum()
+                    gf[i, 1] += g["ext"][s][nodes, 1].sum()
+            return torch.as_tensor(gf, dtype=gx.dtype, device=gx.device), None, None, None, None
+
+    return ControlRollout
+
+
+_CONTROL_ROLLOUT = None
+FORCE_NAMES = ("one", "two", "three", "four", "five", "six")
+
+
+class YarnSimNetControl(_module_base()):
+    """The reference's YarnSimNetControl (src/YarnSimNet.h:132-245): six
+    settings of a lift (z) and a drag (y) force applied at the `handles`
+    nodes, twelve parameters lift_force_one .. drag_force_six; a free
+    (unpinned) upright plain cloth at height 5 with fixed material; forward
+    (state, idx) is one step under setting idx (6: no force). The force's
+    node for handle (a, b) is a * width + b, as the reference indexes it.
+    rollout(state0, schedule) is differentiable w.r.t. the twelve forces
+    (reverse adjoint, dL/d(ext force) contracted with the force positions)."""
+
+    def __init__(self, width: int, length: int, R: float, L: float, material: Dict[str, float],
+                 forces: Sequence[Tuple[float, float]], handles: Sequence[Tuple[int, int]], h: float = 1e-3,
+                 mode: str = "exact"):
+        import torch
+        super().__init__()
+        for i, (lift, drag) in enumerate(forces):
+            self.register_parameter("lift_force_" + FORCE_NAMES[i],
+                                    torch.nn.Parameter(torch.tensor([float(lift)], dtype=torch.float64)))
+            self.register_parameter("drag_force_" + FORCE_NAMES[i],
+                                    torch.nn.Parameter(torch.tensor([float(drag)], dtype=torch.float64)))
+        m = dict(material)
+        self.h, self.mode, self.handles = float(h), mode, list(handles)
+        yarn = np.array([[m["rho"], m["Y"], m["B"]]])
+        self._spec = ClothSpec(width=width, length=length, warp=yarn.repeat(length, 0), weft=yarn.repeat(width, 0),
+                               height=5.0, L=L, R=R, pose=InitPose.Upright, weave=int(WovenPattern.Plain),
+                               kc=m.get("kc", 1.0), kf=m.get("kf", 1000.0), df=m.get("df", 1000.0),
+                               mu=m.get("mu", 0.5), S=m.get("S", 1000.0),
+                               handle_stiffness=m.get("handle_stiffness", 1e4),
+                               G=(0.0, 0.0, m.get("gravity", 9.8)), wind_vel=tuple(m.get("wind_vel", (0, 0, 0))),
+                               wind_density=m.get("wind_density", 0.0), wind_drag=m.get("wind_drag", 0.0),
+                               handles=[])
+
+    def spec(self) -> ClothSpec:
+        return self._spec
+
+    def forces(self):
+        """[6, 2] tensor of (lift, drag) per setting."""
+        import torch
+        return torch.stack([torch.cat([getattr(self, "lift_force_" + n), getattr(self, "drag_force_" + n)])
+                            for n in FORCE_NAMES])
+
+    def force_nodes(self) -> np.ndarray:
+        return np.array([a * self._spec.width + b for (a, b) in self.handles], dtype=np.int64)
+
+    def ext_force(self, idx: int, forces=None) -> Optional[np.ndarray]:
+        """[N, 5] external force of setting idx (None for 6, the zero force)."""
+        if idx == 6:
+            return None
+        if not 0 <= idx < 6:
+            raise ValueError("invalid force index %d" % idx)
+        f = self.forces().detach().cpu().numpy() if forces is None else np.asarray(forces)
+        e = np.zeros((self._spec.num_nodes, 5))
+        for nd in self.force_nodes():
+            e[nd, 2] += f[idx, 0]
+            e[nd, 1] += f[idx, 1]
+        return e
+
+    def rollout(self, state0: Dict, schedule: Sequence[int], checkpoint_every: int = 20):
+        global _CONTROL_ROLLOUT
+        if _CONTROL_ROLLOUT is None:
+            _CONTROL_ROLLOUT = _control_rollout_function()
+        return _CONTROL_ROLLOUT.apply(self.forces(), self, state0, list(schedule), checkpoint_every)
+
+    def forward(self, state: Dict, idx: int, tol: float = 0.0) -> Tuple[Dict, bool]:
+        b = ClothBatch([self._spec])
+        try:
+            b.set_state(**state)
+            ok = b.step(self.h, self.ext_force(idx), tol=tol)[0]["ok"]
             return b.get_state(), ok
         finally:
             b.close()
