@@ -157,15 +157,17 @@ def measure_fp64_peak(torch):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
-# FP64 flops per node of one assembly launch, counted by ncu on a 64 x 40 x 40
-# batch (102,400 nodes): 2 x DFMA + DADD + DMUL thread instructions of the
+# FP64 flops per node of one assembly launch, counted by ncu on the first
+# 128 cloths of this workload (seed 0, 122,504 nodes; bench.py --cloths 128
+# --schedule launch): 2 x DFMA + DADD + DMUL thread instructions of the
 # launch (sm__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum)
-# divided by the batch's nodes; the bends' and shear's counts depend on the
-# state only through branch outcomes, so they carry over to other batches of
-# the same cloths per node to within a few per cent
-ASSEMBLY_FP64_FLOPS_PER_NODE = None
-# DRAM bytes (read + write) of the persistent solve per pass over the rows,
-# from the same capture
+# divided by the batch's nodes. The counts depend on the state only through
+# branch outcomes and on the sizes through the share of boundary nodes, so
+# they carry over to the 256-cloth batch to within a few per cent.
+ASSEMBLY_FP64_FLOPS_PER_NODE = {"geom": 624.5, "edges": 3379.5, "bends": 2142.3, "faces": 379.4,
+                                "gather": 1467.0, "shear": 3489.6, "finalize": 801.5}
+# DRAM bytes (read + write) of the persistent solve per pass over the rows
+# (not captured: the tuner does not pick the persistent PCG for this batch)
 PERSIST_DRAM_BYTES_PER_ROW_PASS = None
 
 

@@ -114,11 +114,13 @@ class GpuCloth {
   // when the system or the new velocity is not finite, as the reference's.
   // ext_force in the reference's DOF layout ([x of all nodes; u, v of
   // interior nodes], [dim] or [dim,1]) or undefined.
-  bool step(double h, const torch::Tensor& ext_force = torch::Tensor()) {
+  // tol > 0: PCG relative residual (default: Eigen's, the machine epsilon).
+  bool step(double h, const torch::Tensor& ext_force = torch::Tensor(), double tol = 0.0) {
     std::vector<double> e5;
     if (ext_force.defined()) e5 = to_node5(ext_force);
     ys_cloth_stats st{};
-    const ys_status r = ys_step(b_, h, e5.empty() ? nullptr : e5.data(), 0, nullptr, &st);
+    const ys_solve_opts o{tol, -1, 0};
+    const ys_status r = ys_step(b_, h, e5.empty() ? nullptr : e5.data(), 0, &o, &st);
     if (r == YS_ERR_NONFINITE) return false;
     if (r != YS_OK && r != YS_ERR_MAXITER) check(r, "ys_step");
     return st.ok != 0;
@@ -153,7 +155,7 @@ class GpuCloth {
 struct AdjointRollout : public torch::autograd::Function<AdjointRollout> {
   static torch::autograd::variable_list forward(torch::autograd::AutogradContext* ctx, torch::Tensor theta,
                                                 ClothDescription tmpl, State state0, int64_t steps, double h,
-                                                int64_t mode, int64_t k) {
+                                                int64_t mode, int64_t k, double tol = 0.0) {
     torch::Tensor th = theta.detach().to(torch::kCPU, torch::kFloat64).contiguous();
     const double* t = th.data_ptr<double>();
     const double y0[3] = {t[0], t[1], t[2]}, y1[3] = {t[3], t[4], t[5]};
@@ -168,7 +170,7 @@ struct AdjointRollout : public torch::autograd::Function<AdjointRollout> {
     std::map<int64_t, State> checkpoints;
     for (int64_t s = 0; s < steps; ++s) {
       if (s % k == 0) checkpoints[s] = cloth->get_state();
-      cloth->step(h);
+      cloth->step(h, torch::Tensor(), tol);
       State cur = cloth->get_state();
       xs.push_back(cur.LPos.view({-1, 3}));
       es.push_back(cur.EPos.view({-1, 2}));
@@ -177,6 +179,7 @@ struct AdjointRollout : public torch::autograd::Function<AdjointRollout> {
     ctx->saved_data["h"] = h;
     ctx->saved_data["mode"] = mode;
     ctx->saved_data["k"] = k;
+    ctx->saved_data["tol"] = tol;
     ctx->saved_data["cloth"] = reinterpret_cast<int64_t>(cloth);
     std::vector<torch::Tensor> flat;
     for (auto& kv : checkpoints) {
@@ -195,7 +198,8 @@ struct AdjointRollout : public torch::autograd::Function<AdjointRollout> {
                                                  torch::autograd::variable_list grads) {
     auto* cloth = reinterpret_cast<GpuCloth*>(ctx->saved_data["cloth"].toInt());
     const int64_t steps = ctx->saved_data["steps"].toInt(), k = ctx->saved_data["k"].toInt();
-    const double h = ctx->saved_data["h"].toDouble();
+    const double h = ctx->saved_data["h"].toDouble(), tol = ctx->saved_data["tol"].toDouble();
+    const ys_solve_opts opts{tol, -1, 0};
     const int mode = (int)ctx->saved_data["mode"].toInt();
     std::vector<torch::Tensor> flat = ctx->saved_data["checkpoints"].toTensorVector();
     const ClothDescription& d = cloth->description();
@@ -220,7 +224,7 @@ struct AdjointRollout : public torch::autograd::Function<AdjointRollout> {
       std::vector<State> seg;
       for (int64_t s = a; s < e; ++s) {
         seg.push_back(cloth->get_state());
-        if (s + 1 < e) cloth->step(h);
+        if (s + 1 < e) cloth->step(h, torch::Tensor(), tol);
       }
       for (int64_t s = e - 1; s >= a; --s) {
         cloth->set_state(seg[s - a]);
@@ -237,8 +241,8 @@ struct AdjointRollout : public torch::autograd::Function<AdjointRollout> {
         }
         double* gpar[5] = {pl[0].data_ptr<double>(), pl[1].data_ptr<double>(), pl[2].data_ptr<double>(),
                            pc[0].data_ptr<double>(), pc[1].data_ptr<double>()};
-        const ys_status st = ys_adjoint_step(adj, h, nullptr, gin, gout, gpar, nullptr, 0, nullptr, nullptr);
-        if (st != YS_OK) {
+        const ys_status st = ys_adjoint_step(adj, h, nullptr, gin, gout, gpar, nullptr, 0, &opts, nullptr);
+        if (st != YS_OK && st != YS_ERR_MAXITER) {
           ys_adjoint_destroy(adj);
           check(st, "ys_adjoint_step");
         }
@@ -265,7 +269,7 @@ struct AdjointRollout : public torch::autograd::Function<AdjointRollout> {
     acc[6] = gp_cloth[0][0].item<double>();
     acc[7] = gp_cloth[1][0].item<double>();
     return {gt.to(grads[0].device()), torch::Tensor(), torch::Tensor(), torch::Tensor(), torch::Tensor(),
-            torch::Tensor(), torch::Tensor()};
+            torch::Tensor(), torch::Tensor(), torch::Tensor()};
   }
 };
 

@@ -10,7 +10,8 @@
 // handles, warp / weft (files: [lines][3] rho, Y, B), init (file: LPos,
 // LPosFix, LVel [N][3], EPos, EPosBar, EVel [N][2]), steps, h, out;
 // grad: theta (8 values), targets (file: [steps][N][3] then [steps][N][2]),
-// adjoint (0 exact, 1 reference), k.
+// adjoint (0 exact, 1 reference), k, tol (PCG relative residual; default
+// Eigen's).
 #include <cstdio>
 #include <fstream>
 #include <map>
@@ -92,8 +93,9 @@ int main(int argc, char** argv) {
     torch::Tensor theta = torch::tensor(th, torch::kFloat64).requires_grad_(true);
     auto tg = file(kv.at("targets"), (size_t)steps * N * 5);
     torch::Tensor gx = tensor(tg, 0, {steps, N, 3}), ge = tensor(tg, (size_t)steps * N * 3, {steps, N, 2});
+    const double tol = kv.count("tol") ? d("tol") : 0.0;
     auto xe = yarnsim::AdjointRollout::apply(theta, desc, s0, (int64_t)steps, h, (int64_t)d("adjoint"),
-                                             (int64_t)d("k"));
+                                             (int64_t)d("k"), tol);
     torch::Tensor loss = yarnsim::position_loss(xe[0], xe[1], gx, ge);
     loss.backward();
     double l = loss.item<double>();

@@ -4,7 +4,8 @@
   fixture's state gives the fixture's next state (1e-8), with the material
   set through constraint_para of the inverted values; the rollout's gradient
   w.r.t. the four raw parameters in forward mode equals the reverse
-  adjoint's (1e-8) and central differences (exact mode, 1e-6);
+  adjoint's (1e-8) and central differences (exact mode, 1e-6, or ten times
+  the difference quotient's own error estimated from two step sizes);
 - YarnSimNetControl (src/YarnSimNet.h:132-245): forward(state, idx) is the
   step with the setting's lift and drag forces at nodes a * width + b; the
   gradient w.r.t. the twelve forces over a schedule of settings against
@@ -82,16 +83,20 @@ def test_homo_gradient_forward_reverse_and_differences():
     for i, n in enumerate(("rho", "Y", "B", "S")):
         p = getattr(net, n)
         x0 = float(p.data[0])
-        eps = 1e-6 * max(1.0, abs(x0))
-        vals = []
-        for sgn in (1, -1):
-            p.data[0] = x0 + sgn * eps
-            with torch.no_grad():
-                tx, te = net.rollout(state0, steps)
-                vals.append(float(_loss(tx, te)))
+        fds = []
+        for eps in (1e-6, 2e-6):
+            vals = []
+            for sgn in (1, -1):
+                p.data[0] = x0 + sgn * eps
+                with torch.no_grad():
+                    tx, te = net.rollout(state0, steps)
+                    vals.append(float(_loss(tx, te)))
+            fds.append((vals[0] - vals[1]) / (2 * eps))
         p.data[0] = x0
-        fd = (vals[0] - vals[1]) / (2 * eps)
-        assert abs(fd - gf[i]) <= 1e-6 * abs(fd) + 1e-12 * np.abs(gf).max(), (n, fd, gf[i])
+        fd = fds[0]
+        noise = abs(fds[0] - fds[1]) / max(abs(fd), 1e-300)  # the quotient's own error, estimated
+        err = abs(fd - gf[i]) / max(abs(fd), 1e-300)
+        assert err <= max(1e-6, 10 * noise), (n, fd, gf[i], err, noise)
 
 
 def _control_net(mode="exact"):

@@ -134,7 +134,7 @@ def test_cpp_autograd_matches_reference_gradient(driver, tmp_path, name):
     tg.astype("<f8").tofile(str(tmp_path / "targets"))
     cfg, _ = _write_case(str(tmp_path), g, init, steps,
                          dict(mode="grad", theta=",".join(repr(float(x)) for x in g["params"]),
-                              targets=str(tmp_path / "targets"), adjoint=1, k=5, mu=0.0, S=0.0))
+                              targets=str(tmp_path / "targets"), adjoint=1, k=5, mu=0.0, S=0.0, tol=1e-14))
     _run(driver, cfg)
     out = np.fromfile(str(tmp_path / "out"), "<f8")
     loss, grad = out[0], out[1:9]

@@ -195,6 +195,8 @@ def test_reference_gradient_matches_libtorch(name):
     reference's own loss.backward() computes, 1e-7 relative per parameter."""
     import torch
     g, tmpl, state0, steps, gt_x, gt_e = _grad_setup(name)
+    if not np.all(np.isfinite(g["grad"])):
+        pytest.skip("the reference's LibTorch gradient is not finite for this window")
     theta = torch.tensor(g["params"], dtype=torch.float64, requires_grad=True)
     tx, te = ys.rollout(theta, tmpl, state0, steps, 1e-3, "reference", tol=1e-14)
     loss = ys.position_loss(tx, te, gt_x, gt_e)
