@@ -256,13 +256,14 @@ struct AdjointRollout : public torch::autograd::Function<AdjointRollout> {
       }
     }
     ys_adjoint_destroy(adj);
+    const int64_t length = d.d.length;  // d belongs to the cloth freed next
     delete cloth;
     ctx->saved_data["cloth"] = (int64_t)0;
     // per-line gradients into the two yarn types (warp line v, weft line u: parity)
     torch::Tensor gt = torch::zeros({8}, o);
     auto acc = gt.accessor<double, 1>();
     for (int64_t l = 0; l < nl; ++l) {
-      const int64_t pos = l < d.d.length ? l : l - d.d.length;
+      const int64_t pos = l < length ? l : l - length;
       const int type = (int)(pos % 2);
       for (int p = 0; p < 3; ++p) acc[3 * type + p] += gp_line[p][l].item<double>();
     }
