@@ -69,6 +69,9 @@ YS_HD void gather_elements(const View& v, const Records& R, int n) {
     for (int i = 0; i < 2; ++i) EE[i] = FE[i] = KEE[i] = DEE[i] = 0.0;
     for (int i = 0; i < 5; ++i) B[i] = 0.0;
     for (int i = 0; i < 3; ++i) CL[i] = 0.0;
+    // unrolled: the accumulators are indexed by k, and a rolled loop would
+    // put them in local memory
+#pragma unroll
     for (int k = 0; k < 2; ++k) {
       // edges along k: this node as n0 (anchor n) and as n1 (anchor n - step)
       const int step = k == 0 ? 1 : W;

@@ -576,6 +576,7 @@ constexpr int kE_llI = 0, kE_llP = 4, kE_d = 8, kE_le = 11, kE_el = 23, kE_ee = 
 template <class T>
 struct BendGeom {
   T du, l1, l2, d1[3], d2[3], P1[3][3], P2[3][3], theta;
+  T c;  // cos(theta), the clamped argument of the acos
 };
 // src/ClothUnit.h:197-210; the theta clamp uses EPS = DBL_MIN
 // (src/Constants.h:25) and so never changes a finite value.
@@ -593,6 +594,7 @@ YS_HD void bend_geom(const T* x2, const T* x0, const T* x1, T du, BendGeom<T>& g
   const double lo = -1.0 + 2.2250738585072014e-308, hi = 1.0 - 2.2250738585072014e-308;
   if (c < lo) c = lo;
   if (c > hi) c = hi;
+  g.c = c;
   g.theta = acos(c);
 }
 
@@ -611,10 +613,12 @@ YS_HD void bend_terms(const BendGeom<T>& g, const T& kb, BendTerms<T>& t) {
     t.Fx1[i] = t.Fx2[i] = t.L1E1[i] = t.L2E1[i] = 0.0;
     for (int j = 0; j < 3; ++j) t.L11[i][j] = t.L12[i][j] = t.L21[i][j] = t.L22[i][j] = 0.0;
   }
-  const T th = g.theta, s = sin(th);
+  // sin and cos of theta = acos(c) from c itself: sin = sqrt((1 - c)(1 + c))
+  // (zero exactly where sin(acos(c)) is: c = +-1), cos = c
+  const T th = g.theta, s = sqrt((1.0 - g.c) * (1.0 + g.c));
   t.active = (s != 0.0);
   if (!t.active) return;
-  const T co = cos(th), du = g.du;
+  const T co = g.c, du = g.du;
   T a[3], b[3];
   matvec3(g.P1, g.d2, a);
   matvec3(g.P2, g.d1, b);
@@ -1022,8 +1026,11 @@ YS_HD void shear_element(const View& v, double* buf, double* dbuf, int n0, int s
   for (int i = 0; i < 3; ++i) { d1[i] = a1v[i] * il1; d3[i] = a3v[i] * il3; }
   proj3(d1, P1);
   proj3(d3, P3);
-  const T phi = acos(dot3(d1, d3));
-  const T s = sin(phi), co = cos(phi);
+  // the crossing angle, and its sine and cosine from its cosine c:
+  // sin = sqrt((1 - c)(1 + c)), cos = c (phi in [0, pi])
+  const T cph = dot3(d1, d3);
+  const T phi = acos(cph);
+  const T s = sqrt((1.0 - cph) * (1.0 + cph)), co = cph;
   T a3[3], a1[3];  // a3 = P1 d3, a1 = P3 d1
   matvec3(P1, d3, a3);
   matvec3(P3, d1, a1);
@@ -1072,8 +1079,9 @@ YS_HD void shear_element(const View& v, double* buf, double* dbuf, int n0, int s
     const T rl1s = il1 * is, rl3s = il3 * is;
     T px1[3], px3[3];
     for (int i = 0; i < 3; ++i) { px1[i] = -a3[i] * rl1s; px3[i] = -a1[i] * rl3s; }
-    const T gamma = (Lc * sqrt(2.0) - 2 * Lc * sin(0.5 * phi)) / R;
-    const T sh = sin(0.5 * phi), ch = cos(0.5 * phi);
+    // half-angle sine and cosine: sqrt((1 -+ c) / 2), both >= 0 for phi in [0, pi]
+    const T sh = sqrt(0.5 * (1.0 - cph)), ch = sqrt(0.5 * (1.0 + cph));
+    const T gamma = (Lc * sqrt(2.0) - 2 * Lc * sh) / R;
     const T kap = -LR * ch;                       // gamma_x = kap * phi_x
     const T Aq = phi - pl, Bq = phi - pb;
     const T phs = phi * Aq * Bq;
