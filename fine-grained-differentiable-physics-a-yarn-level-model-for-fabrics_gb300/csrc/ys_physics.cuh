@@ -204,31 +204,26 @@ YS_HD void acc_F(EdgeOut<T>& o, int dof, const T& f) {
   if ((dof & 3) == 3) o.fe[dof >> 2] += f;
 }
 
-// One edge Jacobian written with the pattern shared by Inertia_D_Pos,
-// Inertia_D_Vel, MDotVDot_D_Pos and MDotVDot_D_Vel
-// (src/PhysicsCloth.cpp:1544-1600, 1848-1900, 2226-2308, 2505-2577):
-// C(i, j) = d(force DOF i)/d(DOF j) in edge-local order; here given as the
-// isotropic node-node factors iso[p], the (x, e) columns lec[p][r] =
-// C(4a+r, 4b+3), the (e, x) rows elr[p][c] = C(4a+3, 4b+c) and eev[p] =
-// C(4a+3, 4b+3), added with sign s under the reference's interior tests.
+// One node-pair block p = 2a + b of an edge Jacobian written with the
+// pattern shared by Inertia_D_Pos, Inertia_D_Vel, MDotVDot_D_Pos and
+// MDotVDot_D_Vel (src/PhysicsCloth.cpp:1544-1600, 1848-1900, 2226-2308,
+// 2505-2577): C(i, j) = d(force DOF i)/d(DOF j) in edge-local order, given as
+// the isotropic node-node factor iso, the (x, e) column lec[r] = C(4a+r,
+// 4b+3), the (e, x) row elr[c] = C(4a+3, 4b+c) and eev = C(4a+3, 4b+3), added
+// with sign s under the reference's interior tests. Each section adds a
+// block as soon as it is formed, so no section holds all four blocks.
 template <class T>
-struct EdgeJac {
-  T iso[4], lec[4][3], elr[4][3], eev[4];
-};
-template <class T>
-YS_HD void acc_jac(EdgeOut<T>& o, int X, double s, const EdgeJac<T>& C) {
-  for (int p = 0; p < 4; ++p) acc_LLi(o, X, p >> 1, p & 1, s * C.iso[p]);
+YS_HD void acc_jac_p(EdgeOut<T>& o, int X, double s, int p, const T& iso, const T* lec, const T* elr, const T& eev) {
+  const int a = p >> 1, b = p & 1;
+  acc_LLi(o, X, a, b, s * iso);
+  const bool ok = (a == b) ? o.in[a] : (o.in[0] && o.in[1]);
+  if (!ok) return;
   T t[3];
-  for (int p = 0; p < 4; ++p) {
-    const int a = p >> 1, b = p & 1;
-    const bool ok = (a == b) ? o.in[a] : (o.in[0] && o.in[1]);
-    if (!ok) continue;
-    for (int r = 0; r < 3; ++r) t[r] = s * C.lec[p][r];
-    acc_LE(o, X, a, b, t);
-    for (int c = 0; c < 3; ++c) t[c] = s * C.elr[p][c];
-    acc_EL(o, X, a, b, t);
-    acc_EE(o, X, a, b, s * C.eev[p]);
-  }
+  for (int r = 0; r < 3; ++r) t[r] = s * lec[r];
+  acc_LE(o, X, a, b, t);
+  for (int c = 0; c < 3; ++c) t[c] = s * elr[c];
+  acc_EL(o, X, a, b, t);
+  acc_EE(o, X, a, b, s * eev);
 }
 
 template <class T>
@@ -394,7 +389,6 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o, dou
   const T sc = 1.0 / 6.0 * rho * du;
   const T wSae = dot3(w, Sae), wSea = dot3(w, Sea);
   const T pj = -(-idu);  // (-w_x0)_j for the active component j
-  EdgeJac<T> C;
 
   // ---- Inertia_F (src/PhysicsCloth.cpp:1071-1186)
   {
@@ -428,11 +422,10 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o, dou
     const T Tuu = 0.5 * ((-1.0 / 6.0) * rho * Quv0 - (1.0 / 6.0) * rho * Quv0 + (1.0 / 6.0) * rho * du * Quvuv);
     for (int p = 0; p < 4; ++p) {
       const double sgn = ((p >> 1) == (p & 1)) ? 1.0 : -1.0;
-      C.iso[p] = sgn * T00;
-      for (int r = 0; r < 3; ++r) { C.lec[p][r] = sgn * Tx0uv0[r]; C.elr[p][r] = sgn * Tuv0x0[r]; }
-      C.eev[p] = sgn * Tuu;
+      T lec[3], elr[3];
+      for (int r = 0; r < 3; ++r) { lec[r] = sgn * Tx0uv0[r]; elr[r] = sgn * Tuv0x0[r]; }
+      acc_jac_p(o, kK, 1.0, p, sgn * T00, lec, elr, sgn * Tuu);
     }
-    acc_jac(o, kK, 1.0, C);
   }
   // ---- Inertia_D_Vel (src/PhysicsCloth.cpp:1602-1901): row x_j of C = M_xj qdot
   {
@@ -450,13 +443,11 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o, dou
                          (1.0 / 6.0) * rho * du * ((-idu) * wm + (2.0 * idu) * wTw * me_[b]);
       for (int a = 0; a < 2; ++a) {
         const double sgn = a == 0 ? 1.0 : -1.0;  // rows of x1 / uv1 are the negated rows of x0 / uv0
-        const int p = 2 * a + b;
-        C.iso[p] = sgn * iso;
-        for (int r = 0; r < 3; ++r) { C.lec[p][r] = sgn * lec[r]; C.elr[p][r] = sgn * elr[r]; }
-        C.eev[p] = sgn * eev;
+        T lp[3], ep[3];
+        for (int r = 0; r < 3; ++r) { lp[r] = sgn * lec[r]; ep[r] = sgn * elr[r]; }
+        acc_jac_p(o, kD, 1.0, 2 * a + b, sgn * iso, lp, ep, sgn * eev);
       }
     }
-    acc_jac(o, kD, 1.0, C);
   }
   // ---- MDotVDot (src/PhysicsCloth.cpp:1903-2577)
   {
@@ -496,19 +487,19 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o, dou
       for (int b = 0; b < 2; ++b) {
         const T* ma = b == 0 ? m0a : m1a;
         const T me = b == 0 ? m0e : m1e;
-        const int p = 2 * b + t;
-        C.iso[p] = r6 * dud * (P1 * me) + r6 * du * (P2 * me);
+        const T iso = r6 * dud * (P1 * me) + r6 * du * (P2 * me);
+        T elr[3], lec[3];
         for (int j = 0; j < 3; ++j) {
           const T S1 = (sw * 2.0 * idu2 * dx[j]);
           const T S2 = 2 * (wxj * wd[j]) + 2 * (w[j] * wdxj);
-          C.elr[p][j] = r6 * dud * (P1 * ma[j] + S1 * me) + r6 * du * (P2 * ma[j] + S2 * me);
-          C.lec[p][j] = r6 * dud * (wuv[j] * me) - r6 * r[4 * b + j] + r6 * du * (-wduv[j] * me);
+          elr[j] = r6 * dud * (P1 * ma[j] + S1 * me) + r6 * du * (P2 * ma[j] + S2 * me);
+          lec[j] = r6 * dud * (wuv[j] * me) - r6 * r[4 * b + j] + r6 * du * (-wduv[j] * me);
         }
-        C.eev[p] = r6 * dud * (dot3(wuv, ma) + wTwuv * me) - r6 * r[4 * b + 3] +
-                   r6 * du * (-dot3(wduv, ma) + wTwduv * me);
+        const T eev = r6 * dud * (dot3(wuv, ma) + wTwuv * me) - r6 * r[4 * b + 3] +
+                      r6 * du * (-dot3(wduv, ma) + wTwduv * me);
+        acc_jac_p(o, kK, 1.0, 2 * b + t, iso, lec, elr, eev);
       }
     }
-    acc_jac(o, kK, 1.0, C);
     // MDotVDot_D_Vel, subtracted (src/PhysicsCloth.cpp:2342-2577)
     for (int t = 0; t < 2; ++t) {
       const double sw = t == 0 ? -1.0 : 1.0;
@@ -522,20 +513,20 @@ YS_HD void edge_element(const View& v, int n0, int n1, int k, EdgeOut<T>& o, dou
         const T* ma = b == 0 ? m0a : m1a;
         const T me = b == 0 ? m0e : m1e;
         const double f = (b == t) ? 2.0 : 1.0;  // [[2B, B], [B, 2B]] block factor of M_dot
-        const int p = 2 * b + t;
-        C.iso[p] = (1.0 / 6.0) * rho * du * (P1 * me) + (r6 * dud * (f * 1.0) + r6 * du * (f * 0.0));
+        const T iso = (1.0 / 6.0) * rho * du * (P1 * me) + (r6 * dud * (f * 1.0) + r6 * du * (f * 0.0));
+        T elr[3], lec[3];
         for (int j = 0; j < 3; ++j) {
           const T S1 = 2 * (w[j] * wdj);
-          C.elr[p][j] = (1.0 / 6.0) * rho * du * (P1 * ma[j] + S1 * me) +
-                        (r6 * dud * (f * -w[j]) + r6 * du * (f * -wd[j]));
-          C.lec[p][j] = cm * BMm[b][j] + (1.0 / 6.0) * rho * du * (-wdv[j] * me) +
-                        (r6 * dud * (f * -w[j]) + r6 * du * (f * -wd[j]));
+          elr[j] = (1.0 / 6.0) * rho * du * (P1 * ma[j] + S1 * me) +
+                   (r6 * dud * (f * -w[j]) + r6 * du * (f * -wd[j]));
+          lec[j] = cm * BMm[b][j] + (1.0 / 6.0) * rho * du * (-wdv[j] * me) +
+                   (r6 * dud * (f * -w[j]) + r6 * du * (f * -wd[j]));
         }
-        C.eev[p] = cm * BMm[b][3] + (1.0 / 6.0) * rho * du * (-dot3(wdv, ma) + wtwd * me) +
-                   (r6 * dud * (f * wTw) + r6 * du * (f * wTwd));
+        const T eev = cm * BMm[b][3] + (1.0 / 6.0) * rho * du * (-dot3(wdv, ma) + wtwd * me) +
+                      (r6 * dud * (f * wTw) + r6 * du * (f * wTwd));
+        acc_jac_p(o, kD, -1.0, 2 * b + t, iso, lec, elr, eev);
       }
     }
-    acc_jac(o, kD, -1.0, C);
   }
   (void)t3;
 }
