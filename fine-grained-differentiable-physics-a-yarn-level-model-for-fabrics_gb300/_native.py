@@ -190,7 +190,8 @@ class ResponseInfo(ctypes.Structure):
     """ys_response_info (include/yarnsim.h)."""
     _fields_ = [("rounds", ctypes.c_int32), ("converged", ctypes.c_int32), ("changed", ctypes.c_int32),
                 ("zones", ctypes.c_int32), ("infeasible", ctypes.c_int32), ("zone_overflow", ctypes.c_int32),
-                ("impacts", ctypes.c_int64), ("projections", ctypes.c_int64), ("reverted", ctypes.c_int32)]
+                ("impacts", ctypes.c_int64), ("projections", ctypes.c_int64), ("reverted", ctypes.c_int32),
+                ("pad_", ctypes.c_int32), ("detect_ms", ctypes.c_double), ("zones_ms", ctypes.c_double)]
 
 
 class YarnSimError(RuntimeError):

@@ -144,7 +144,8 @@ class Collider:
         self._n_received = int(info.impacts)
         return dict(x=x, v=vv, rounds=info.rounds, converged=bool(info.converged), changed=bool(info.changed),
                     zones=info.zones, infeasible=info.infeasible, zone_overflow=bool(info.zone_overflow),
-                    impacts=info.impacts, projections=info.projections, reverted=info.reverted)
+                    impacts=info.impacts, projections=info.projections, reverted=info.reverted,
+                    detect_ms=info.detect_ms, zones_ms=info.zones_ms)
 
     def response_impacts(self) -> dict:
         """The impacts the zones of the last response received, in order

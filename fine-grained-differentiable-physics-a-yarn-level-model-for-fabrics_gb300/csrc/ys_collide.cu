@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <future>
@@ -748,7 +749,14 @@ ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h,
   std::vector<ys_impact> got;
   // one detection round on the GPU: the trees keep the topology built by
   // set_positions and are refit to the current positions (AccelStruct::update)
+  double detect_ms = 0.0;
   auto detect = [&](const double* xc, const uint8_t* mask, std::vector<ys::ZImpact>& out) -> int {
+    const auto t0 = std::chrono::steady_clock::now();
+    struct Tick {
+      std::chrono::steady_clock::time_point t0;
+      double* acc;
+      ~Tick() { *acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); }
+    } tick{t0, &detect_ms};
     auto fail = [&](ys_status s) {
       err = s;
       return 1;
@@ -791,7 +799,9 @@ ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h,
     }
     return 0;
   };
+  const auto t_resp = std::chrono::steady_clock::now();
   if (ys::zone_respond(R, x.data(), node_mass, detect)) return err;
+  const double resp_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_resp).count();
   // the collider keeps the responded positions (the cloth mesh's x)
   c->hx = x;
   YC_CUDA(cudaMemcpyAsync(c->x.p, c->hx.data(), n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -816,6 +826,8 @@ ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h,
     info->impacts = (int64_t)R.accepted.size();
     info->projections = (int64_t)R.tape.size();
     info->reverted = R.reverted;
+    info->detect_ms = detect_ms;
+    info->zones_ms = resp_ms - detect_ms;
   }
   if (R.zone_overflow)
     return ys_internal_fail(YS_ERR_MAXITER, "collision response stopped: an impact zone outgrew the zone limit "

@@ -384,6 +384,9 @@ typedef struct {
   int32_t reverted;    /* projections that would have moved a node by more than 4 x (its displacement in
                           the step + thickness) -- nearly contradictory constraints of a crumpling cloth --
                           and sent the zone back to its positions at the start of the step instead */
+  int32_t pad_;
+  double detect_ms;    /* host wall time in the detection rounds (uploads, GPU detection, downloads) */
+  double zones_ms;     /* host wall time in zone building and projections */
 } ys_response_info;
 ys_status ys_collider_respond(ys_collider *c, const double *node_mass, double h, double damp, int32_t max_iter,
                               double *x_out, double *v, ys_response_info *info);
