@@ -62,31 +62,54 @@ __device__ __forceinline__ bool kdop_overlap_f(const float* a, const float* b, f
   return true;
 }
 
-// boxes of the tree nodes at one depth: leaves from their face's nodes,
-// inner nodes as the union of their children (BVHNode::refit, src/BVH.cpp:150-160)
-__global__ void k_refit(DevTree t, const int* __restrict__ level_nodes, int count, const CFace* __restrict__ faces,
-                        CMesh m, int ccd) {
+// Boxes of every tree node (BVHNode::refit, src/BVH.cpp:150-160) in one
+// launch, bottom-up: thread i computes leaf i's box from its face's nodes,
+// then climbs while it is the second of its parent's two children to arrive
+// (an atomic count per inner node; the first arrival stops), forming the
+// parent's box as the union of its children's. Unions of min / max bounds do
+// not depend on the order, so the boxes are those of a refit level by level,
+// bit for bit. No thread waits for another: every climb ends at the root or
+// at a first arrival.
+__device__ __forceinline__ void kdop_load_l2(Kdop& b, const Kdop* src) {
+  const double* p = reinterpret_cast<const double*>(src);
+#pragma unroll
+  for (int k = 0; k < 18; ++k) b.d[k] = __ldcg(p + k);
+}
+__device__ __forceinline__ void refit_store(const DevTree& t, int n, const Kdop& b) {
+  t.box[n] = b;
+  for (int k = 0; k < 9; ++k) {
+    t.fbox[18 * (int64_t)n + k] = __double2float_rd(b.d[k]);
+    t.fbox[18 * (int64_t)n + 9 + k] = __double2float_ru(b.d[k + 9]);
+  }
+}
+__global__ void k_refit_up(DevTree t, const int* __restrict__ leaves, int nleaves, const int* __restrict__ parent,
+                           int* arrive, const CFace* __restrict__ faces, CMesh m, int ccd) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
-  const int n = level_nodes[i];
-  const int f = t.face[n];
-  Kdop b;
-  if (f >= 0) {
-    const CFace& fc = faces[f];
+  if (i >= nleaves) return;
+  int n = leaves[i];
+  {
+    const CFace& fc = faces[t.face[n]];
+    Kdop b;
     ys::kdop_node(b, ys::cc_pos(m, fc.v[0], false), ys::cc_pos(m, fc.v[0], true), ccd != 0);
     for (int k = 1; k < 3; ++k) {
       Kdop nb;
       ys::kdop_node(nb, ys::cc_pos(m, fc.v[k], false), ys::cc_pos(m, fc.v[k], true), ccd != 0);
       ys::kdop_add(b, nb);
     }
-  } else {
-    b = t.box[t.left[n]];
-    ys::kdop_add(b, t.box[t.right[n]]);
+    refit_store(t, n, b);
   }
-  t.box[n] = b;
-  for (int k = 0; k < 9; ++k) {
-    t.fbox[18 * (int64_t)n + k] = __double2float_rd(b.d[k]);
-    t.fbox[18 * (int64_t)n + 9 + k] = __double2float_ru(b.d[k + 9]);
+  for (;;) {
+    const int p = parent[n];
+    if (p < 0) return;
+    __threadfence();  // this node's box is visible before the count says so
+    if (atomicAdd(arrive + p, 1) == 0) return;  // the sibling's thread goes on
+    __threadfence();
+    Kdop b, rb;
+    kdop_load_l2(b, t.box + t.left[p]);
+    kdop_load_l2(rb, t.box + t.right[p]);
+    ys::kdop_add(b, rb);
+    refit_store(t, p, b);
+    n = p;
   }
 }
 
@@ -300,10 +323,12 @@ struct ys_collider {
   std::vector<double> hx, hxp, hox, hoxp;  // host copies for the tree builds
   // trees
   ys::BvhTree ct, ot;
-  DVec<int> c_left, c_right, c_face, c_lof, c_rank, c_upper, c_levels, o_left, o_right, o_face, o_levels;
+  DVec<int> c_left, c_right, c_face, c_lof, c_rank, c_upper, o_left, o_right, o_face;
+  // bottom-up refit: parent of each node (-1 at the root), the leaves, and
+  // the arrival counters of the inner nodes
+  DVec<int> c_parent, c_leaves, c_arrive, o_parent, o_leaves, o_arrive;
   DVec<Kdop> c_box, o_box;
   DVec<float> c_fbox, o_fbox;
-  std::vector<int> c_level_off, o_level_off;  // level l nodes at [off[l], off[l+1])
   // outputs
   DVec<int64_t> counts, offsets, sums, total;
   DVec<int> pairs;
@@ -313,6 +338,7 @@ struct ys_collider {
   DVec<ys_impact> impacts;
   int64_t nimpacts = 0;
   DVec<int> overflow;
+  int64_t* pin = nullptr;  // pinned host words: [0] a scan's total, [1] the broad phase's overflow flag
   bool have_pairs = false, have_impacts = false;
   // impact-zone response
   DVec<uint8_t> face_active, node_active;
@@ -325,30 +351,38 @@ struct ys_collider {
   int max_zone_impacts = 65536;
   std::vector<int> h_cslice, h_oslice;  // broad-phase slice roots
   DVec<int> cslice, oslice;
+  ~ys_collider() {
+    if (pin) cudaFreeHost(pin);
+  }
 };
 
 namespace {
 
 ys_status upload_tree(ys_collider* c, const ys::BvhTree& t, DVec<int>& l, DVec<int>& r, DVec<int>& f,
-                      DVec<int>& levels, DVec<Kdop>& box, std::vector<int>& level_off) {
+                      DVec<Kdop>& box, DVec<int>& parent, DVec<int>& leaves, DVec<int>& arrive) {
   const size_t nn = t.face.size();
   YC_CUDA(l.reserve(nn));
   YC_CUDA(r.reserve(nn));
   YC_CUDA(f.reserve(nn));
   YC_CUDA(box.reserve(nn));
-  YC_CUDA(levels.reserve(nn));
-  std::vector<int> lv;
-  level_off.assign(t.max_depth + 2, 0);
-  for (size_t n = 0; n < nn; ++n) level_off[t.depth[n] + 1]++;
-  for (int d = 0; d <= t.max_depth; ++d) level_off[d + 1] += level_off[d];
-  lv.resize(nn);
-  std::vector<int> fill(level_off.begin(), level_off.end() - 1);
-  for (size_t n = 0; n < nn; ++n) lv[fill[t.depth[n]]++] = (int)n;
+  YC_CUDA(parent.reserve(std::max<size_t>(nn, 1)));
+  YC_CUDA(leaves.reserve(std::max<size_t>(nn, 1)));
+  YC_CUDA(arrive.reserve(std::max<size_t>(nn, 1)));
+  std::vector<int> par(nn, -1), lf;
+  for (size_t n = 0; n < nn; ++n) {
+    if (t.face[n] >= 0) {
+      lf.push_back((int)n);
+    } else {
+      par[t.left[n]] = (int)n;
+      par[t.right[n]] = (int)n;
+    }
+  }
   if (nn) {
     YC_CUDA(cudaMemcpyAsync(l.p, t.left.data(), nn * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     YC_CUDA(cudaMemcpyAsync(r.p, t.right.data(), nn * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     YC_CUDA(cudaMemcpyAsync(f.p, t.face.data(), nn * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    YC_CUDA(cudaMemcpyAsync(levels.p, lv.data(), nn * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    YC_CUDA(cudaMemcpyAsync(parent.p, par.data(), nn * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    YC_CUDA(cudaMemcpyAsync(leaves.p, lf.data(), lf.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     YC_CUDA(cudaStreamSynchronize(c->stream));
   }
   return YS_OK;
@@ -361,32 +395,40 @@ ys_status refit(ys_collider* c, bool obstacle) {
   YC_CUDA(fb.reserve(18 * t.face.size()));
   DevTree dt{obstacle ? c->o_left.p : c->c_left.p, obstacle ? c->o_right.p : c->c_right.p,
              obstacle ? c->o_face.p : c->c_face.p, obstacle ? c->o_box.p : c->c_box.p, (int)t.face.size(), fb.p};
-  const std::vector<int>& off = obstacle ? c->o_level_off : c->c_level_off;
-  const int* lv = obstacle ? c->o_levels.p : c->c_levels.p;
   CMesh m{c->x.p, c->xp.p, c->ox.p, c->oxp.p};
-  for (int d = t.max_depth; d >= 0; --d) {
-    const int cnt = off[d + 1] - off[d];
-    if (cnt) k_refit<<<(cnt + 127) / 128, 128, 0, c->stream>>>(dt, lv + off[d], cnt, obstacle ? c->ofaces.p : c->faces.p,
-                                                               m, c->ccd);
-  }
+  // one launch: every leaf's thread computes its box and carries the unions
+  // up as far as it is the second child to arrive
+  const int nleaves = obstacle ? c->n_obs_faces : c->n_faces;
+  int* arrive = obstacle ? c->o_arrive.p : c->c_arrive.p;
+  YC_CUDA(cudaMemsetAsync(arrive, 0, sizeof(int) * t.face.size(), c->stream));
+  k_refit_up<<<(nleaves + 127) / 128, 128, 0, c->stream>>>(dt, obstacle ? c->o_leaves.p : c->c_leaves.p, nleaves,
+                                                          obstacle ? c->o_parent.p : c->c_parent.p, arrive,
+                                                          obstacle ? c->ofaces.p : c->faces.p, m, c->ccd);
   YC_CUDA(cudaGetLastError());
   return YS_OK;
 }
 
-ys_status scan(ys_collider* c, const int64_t* counts, int64_t n, int64_t* off, int64_t* total_host) {
+// Exclusive scan of counts into off; *total_host receives the sum. With
+// flag, the device word is read back in the same wait (into *flag_host).
+// One host wait per scan.
+ys_status scan(ys_collider* c, const int64_t* counts, int64_t n, int64_t* off, int64_t* total_host,
+               const int* flag = nullptr, int* flag_host = nullptr) {
   const int64_t nb = (n + kScanTile - 1) / kScanTile;
   YC_CUDA(c->sums.reserve(std::max<int64_t>(nb, 1)));
   YC_CUDA(c->total.reserve(1));
+  c->pin[0] = 0;
+  c->pin[1] = 0;
   if (n > 0) {
     k_scan_tiles<<<(unsigned)nb, kScanThreads, 0, c->stream>>>(counts, n, off, c->sums.p);
     k_scan_sums<<<1, kScanThreads, 0, c->stream>>>(c->sums.p, nb, c->total.p);
     k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(off, n, c->sums.p);
     YC_CUDA(cudaGetLastError());
-    YC_CUDA(cudaMemcpyAsync(total_host, c->total.p, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
-  } else {
-    *total_host = 0;
+    YC_CUDA(cudaMemcpyAsync(c->pin, c->total.p, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
   }
+  if (flag) YC_CUDA(cudaMemcpyAsync(c->pin + 1, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   YC_CUDA(cudaStreamSynchronize(c->stream));
+  *total_host = c->pin[0];
+  if (flag_host) *flag_host = (int)(reinterpret_cast<const int*>(c->pin + 1)[0]);
   return YS_OK;
 }
 
@@ -456,10 +498,9 @@ ys_status broad_phase(ys_collider* c, bool masked) {
   const unsigned g = (unsigned)((work + kBroadBlock - 1) / kBroadBlock);
   if (work) k_broad<false><<<g, kBroadBlock, 0, c->stream>>>(a);
   YC_CUDA(cudaGetLastError());
-  ys_status s = scan(c, c->counts.p, work, c->offsets.p, &c->npairs);
-  if (s != YS_OK) return s;
   int ovf = 0;
-  YC_CUDA(cudaMemcpy(&ovf, c->overflow.p, sizeof(int), cudaMemcpyDeviceToHost));
+  ys_status s = scan(c, c->counts.p, work, c->offsets.p, &c->npairs, c->overflow.p, &ovf);
+  if (s != YS_OK) return s;
   if (ovf) return ys_internal_fail(YS_ERR_ARG, "BVH deeper than the traversal stack");
   // a face pairs at most once with every other face
   if (c->npairs < 0 || c->npairs > (int64_t)c->n_faces * ((int64_t)c->n_faces + c->n_obs_faces))
@@ -469,7 +510,8 @@ ys_status broad_phase(ys_collider* c, bool masked) {
   a.out = c->pairs.p;
   if (work) k_broad<true><<<g, kBroadBlock, 0, c->stream>>>(a);
   YC_CUDA(cudaGetLastError());
-  YC_CUDA(cudaStreamSynchronize(c->stream));
+  // no wait: the pairs are read on the stream (narrow phase) or by a
+  // synchronous copy (ys_collider_get_pairs)
   c->have_pairs = true;
   c->have_impacts = false;
   return YS_OK;
@@ -494,7 +536,7 @@ ys_status narrow_phase(ys_collider* c) {
                                                                    c->impacts.p);
     YC_CUDA(cudaGetLastError());
   }
-  YC_CUDA(cudaStreamSynchronize(c->stream));
+  // no wait: the impacts are read by a synchronous copy on this stream
   c->have_impacts = true;
   return YS_OK;
 }
@@ -593,7 +635,8 @@ ys_status ys_collider_create(int32_t n_nodes, int32_t n_faces, const int32_t* fa
       c->ox.reserve(3 * (size_t)n_obs_nodes) != cudaSuccess || c->oxp.reserve(3 * (size_t)n_obs_nodes) != cudaSuccess ||
       c->overflow.reserve(1) != cudaSuccess || c->counts.reserve(n_faces) != cudaSuccess ||
       c->offsets.reserve(n_faces) != cudaSuccess || c->c_lof.reserve(n_faces) != cudaSuccess ||
-      c->c_rank.reserve(n_faces) != cudaSuccess || c->c_upper.reserve(n_faces) != cudaSuccess)
+      c->c_rank.reserve(n_faces) != cudaSuccess || c->c_upper.reserve(n_faces) != cudaSuccess ||
+      cudaMallocHost(reinterpret_cast<void**>(&c->pin), 4 * sizeof(int64_t)) != cudaSuccess)
     return cleanup(ys_internal_fail(YS_ERR_CUDA, "cudaMalloc failed"));
   if (cudaMemcpy(c->faces.p, hf.data(), sizeof(CFace) * n_faces, cudaMemcpyHostToDevice) != cudaSuccess ||
       (n_obs_faces && cudaMemcpy(c->ofaces.p, ho.data(), sizeof(CFace) * n_obs_faces, cudaMemcpyHostToDevice) !=
@@ -660,10 +703,12 @@ ys_status ys_collider_set_positions(ys_collider* c, const double* x, const doubl
   c->ct = ys::bvh_build(c->n_faces, c->fv.data(), c->n_nodes, verts.data(), c->hx.data(), c->hxp.data(), c->ccd != 0);
   if (!same_obstacle) c->ot = obs_tree.get();
   ys_status s;
-  if ((s = upload_tree(c, c->ct, c->c_left, c->c_right, c->c_face, c->c_levels, c->c_box, c->c_level_off)) != YS_OK)
+  if ((s = upload_tree(c, c->ct, c->c_left, c->c_right, c->c_face, c->c_box, c->c_parent, c->c_leaves,
+                       c->c_arrive)) != YS_OK)
     return s;
   if (!same_obstacle &&
-      (s = upload_tree(c, c->ot, c->o_left, c->o_right, c->o_face, c->o_levels, c->o_box, c->o_level_off)) != YS_OK)
+      (s = upload_tree(c, c->ot, c->o_left, c->o_right, c->o_face, c->o_box, c->o_parent, c->o_leaves,
+                       c->o_arrive)) != YS_OK)
     return s;
   c->h_cslice = tree_slices(c->ct, kSliceDepth);
   if ((s = upload_slices(c, false)) != YS_OK) return s;
@@ -698,7 +743,8 @@ ys_status ys_collider_get_pairs(ys_collider* c, int32_t* pairs, int64_t cap) {
   if (cap < c->npairs) return ys_internal_fail(YS_ERR_ARG, "pair buffer too small");
   YC_CUDA(cudaSetDevice(c->device));
   if (c->npairs)
-    YC_CUDA(cudaMemcpy(pairs, c->pairs.p, sizeof(int) * 3 * c->npairs, cudaMemcpyDeviceToHost));
+    YC_CUDA(cudaMemcpyAsync(pairs, c->pairs.p, sizeof(int) * 3 * c->npairs, cudaMemcpyDeviceToHost, c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
   return YS_OK;
 }
 
@@ -716,7 +762,9 @@ ys_status ys_collider_get_impacts(ys_collider* c, ys_impact* impacts, int64_t ca
   if (cap < c->nimpacts) return ys_internal_fail(YS_ERR_ARG, "impact buffer too small");
   YC_CUDA(cudaSetDevice(c->device));
   if (c->nimpacts)
-    YC_CUDA(cudaMemcpy(impacts, c->impacts.p, sizeof(ys_impact) * c->nimpacts, cudaMemcpyDeviceToHost));
+    YC_CUDA(cudaMemcpyAsync(impacts, c->impacts.p, sizeof(ys_impact) * c->nimpacts, cudaMemcpyDeviceToHost,
+                            c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
   return YS_OK;
 }
 
@@ -784,7 +832,9 @@ ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h,
     if ((s = narrow_phase(c)) != YS_OK) return fail(s);
     got.resize((size_t)c->nimpacts);
     if (c->nimpacts &&
-        cudaMemcpy(got.data(), c->impacts.p, sizeof(ys_impact) * c->nimpacts, cudaMemcpyDeviceToHost) != cudaSuccess)
+        (cudaMemcpyAsync(got.data(), c->impacts.p, sizeof(ys_impact) * c->nimpacts, cudaMemcpyDeviceToHost,
+                         c->stream) != cudaSuccess ||
+         cudaStreamSynchronize(c->stream) != cudaSuccess))
       return fail(ys_internal_fail(YS_ERR_CUDA, "cudaMemcpy failed"));
     out.resize(got.size());
     for (size_t i = 0; i < got.size(); ++i) {
