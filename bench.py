@@ -172,11 +172,11 @@ PERSIST_DRAM_BYTES_PER_ROW_PASS = None
 
 
 def schedule_name(c):
-    """'graph|launch/phases-every-E' or 'graph|launch/persistent-TxC'."""
+    """'graph|launch/phases-every-E/producers-P' or 'graph|launch/persistent-TxC/producers-P'."""
     g = "graph" if c["graphs"] else "launch"
     if c["pcg"] == "persistent":
-        return "%s/persistent-%dx%d" % (g, c["pcg_threads"], c["pcg_cluster"])
-    return "%s/phases-every-%d" % (g, c["check_every"])
+        return "%s/persistent-%dx%d/producers-%d" % (g, c["pcg_threads"], c["pcg_cluster"], c["producer_threads"])
+    return "%s/phases-every-%d/producers-%d" % (g, c["check_every"], c["producer_threads"])
 
 
 def assembly_roof(prof, n, steps, fp64_peak):
@@ -470,6 +470,7 @@ def main():
         sched = batch.autotune(H, tol=TOL, steps=3)
         config["schedule"] = {"chosen_by": "ys_autotune", "graph": sched["graphs"],
                               "check_every": sched["check_every"], "pcg": sched["pcg"]}
+        config["schedule"]["producer_threads"] = sched["producer_threads"]
         if sched["pcg"] == "persistent":
             config["schedule"].update(pcg_threads=sched["pcg_threads"], pcg_cluster=sched["pcg_cluster"])
         config["schedule"]["timed_ms_per_step"] = {schedule_name(c): round(c["ms_per_step"], 4)

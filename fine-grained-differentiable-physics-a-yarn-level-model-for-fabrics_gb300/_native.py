@@ -24,7 +24,7 @@ EXPORTED = [
     "ys_tangent_set_state", "ys_tangent_get_state", "ys_step_tangent", "ys_cloth_mesh_topology",
     "ys_collider_create", "ys_collider_destroy", "ys_collider_set_positions", "ys_collider_find_pairs",
     "ys_collider_get_pairs", "ys_collider_find_impacts", "ys_collider_get_impacts", "ys_use_graphs",
-    "ys_step_graphed", "ys_autotune", "ys_set_pcg_schedule", "ys_autotune_results", "ys_gnn_param_count", "ys_gnn_create", "ys_gnn_destroy", "ys_gnn_get_params",
+    "ys_step_graphed", "ys_autotune", "ys_set_pcg_schedule", "ys_autotune_results", "ys_set_producer_threads", "ys_gnn_param_count", "ys_gnn_create", "ys_gnn_destroy", "ys_gnn_get_params",
     "ys_gnn_set_params", "ys_gnn_train_step", "ys_gnn_loss_grad", "ys_set_preconditioner", "ys_precond_info",
     "ys_get_system_slots", "ys_tc_gemm_bf16", "ys_precond_refresh", "ys_get_normals", "ys_collider_respond",
     "ys_collider_response_impacts", "ys_collider_respond_backward", "ys_step_tangent_ext",
@@ -60,7 +60,7 @@ class SolveOpts(ctypes.Structure):
 class Schedule(ctypes.Structure):
     _fields_ = [("graphs", ctypes.c_int32), ("check_every", ctypes.c_int32), ("ms_per_step", ctypes.c_double),
                 ("pcg", ctypes.c_int32), ("pcg_threads", ctypes.c_int32), ("pcg_cluster", ctypes.c_int32),
-                ("pad_", ctypes.c_int32)]
+                ("producer_threads", ctypes.c_int32)]
 
 
 class ClothStats(ctypes.Structure):
@@ -128,6 +128,7 @@ def load(build_if_missing: bool = True):
     L.ys_autotune.argtypes = [vp, ctypes.c_double, vp, ctypes.c_int32, vp]
     L.ys_set_pcg_schedule.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
     L.ys_autotune_results.argtypes = [vp, vp, ctypes.c_int32]
+    L.ys_set_producer_threads.argtypes = [vp, ctypes.c_int32]
     L.ys_autotune_results.restype = ctypes.c_int32
     L.ys_collider_create.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int32, ctypes.c_int32, vp,
                                      ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, ctypes.POINTER(vp)]

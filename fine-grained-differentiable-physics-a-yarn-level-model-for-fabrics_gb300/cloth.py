@@ -261,6 +261,11 @@ class ClothBatch:
         """Run step() as one CUDA graph launch per step (see ys_use_graphs)."""
         N.check(N.load().ys_use_graphs(self._h, int(bool(enable))), "ys_use_graphs")
 
+    def set_producer_threads(self, threads: int):
+        """Block size of the element-record producers and the gather (64..256;
+        results do not depend on it; see ys_set_producer_threads)."""
+        N.check(N.load().ys_set_producer_threads(self._h, int(threads)), "ys_set_producer_threads")
+
     def set_pcg_schedule(self, persistent: bool, threads: int = 0, cluster: int = 0):
         """Phase PCG (three launches per iteration, the default) or the
         persistent per-cloth PCG (one launch per solve, `cluster` CTAs of
@@ -322,7 +327,7 @@ class ClothBatch:
         def d(x):
             return dict(graphs=bool(x.graphs), check_every=x.check_every, ms_per_step=x.ms_per_step,
                         pcg="persistent" if x.pcg == 1 else "phases", pcg_threads=x.pcg_threads,
-                        pcg_cluster=x.pcg_cluster)
+                        pcg_cluster=x.pcg_cluster, producer_threads=x.producer_threads)
         out = d(sc)
         out["candidates"] = [d(arr[i]) for i in range(n)]
         return out

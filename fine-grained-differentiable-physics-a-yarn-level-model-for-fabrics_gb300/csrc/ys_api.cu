@@ -137,6 +137,7 @@ struct ys_batch {
     int max_nodes = 0;
   } plan;
   std::vector<ys_schedule> tuned;  // every schedule the last ys_autotune timed
+  int producer_threads = ys::kBlock;  // block size of the record producers and the gather
   bool has_system = false;  // v.A / v.B hold an assembled system (kept after the update)
   // learned preconditioner (ys_set_preconditioner); buffers allocated on first use
   struct Learn {
@@ -586,13 +587,14 @@ ys_status ys_assemble(ys_batch* b, double h, const double* ext_force, int32_t fl
   if (b->geom_n) b->run(YS_PROF_GEOM, 1, [&] { ys::launch_geom(v, b->anchors + b->geom_off, b->geom_n, s); });
   // element records (FillMV's element loops, src/PhysicsCloth.cpp:64-95)
   const ys::Records& R = b->rec;
-  b->run(YS_PROF_EDGES, 1, [&] { ys::launch_edge_records(v, R, s); });
-  b->run(YS_PROF_BENDS, 1, [&] { ys::launch_bend_records(v, R, s); });
-  b->run(YS_PROF_FACES, 1, [&] { ys::launch_face_records(v, R, s); });
+  const int pt = b->producer_threads;
+  b->run(YS_PROF_EDGES, 1, [&] { ys::launch_edge_records(v, R, s, pt); });
+  b->run(YS_PROF_BENDS, 1, [&] { ys::launch_bend_records(v, R, s, pt); });
+  b->run(YS_PROF_FACES, 1, [&] { ys::launch_face_records(v, R, s, pt); });
   // row blocks + ConSlideFriction (needs every edge and bend term; shear
   // needs its compression, src/PhysicsCloth.cpp:97-131)
-  b->run(YS_PROF_GATHER, 1, [&] { ys::launch_gather(v, R, s); });
-  b->run(YS_PROF_SHEAR, 1, [&] { ys::launch_shear_records(v, R, s); });
+  b->run(YS_PROF_GATHER, 1, [&] { ys::launch_gather(v, R, s, pt); });
+  b->run(YS_PROF_SHEAR, 1, [&] { ys::launch_shear_records(v, R, s, pt); });
   b->run(YS_PROF_FINALIZE, 1, [&] { ys::launch_finalize(v, R, b->blk, b->so, s); });
   YS_CUDA(cudaGetLastError());
   b->assembled = true;
@@ -1394,11 +1396,11 @@ ys_status graph_build(ys_batch* b, int m, int cap, int override_max) {
   YS_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
   k_reset_status<<<(b->ncloth + 127) / 128, 128, 0, cs>>>(b->so.pc, b->ncloth);
   if (b->geom_n) ys::launch_geom(v, b->anchors + b->geom_off, b->geom_n, cs);
-  ys::launch_edge_records(v, R, cs);
-  ys::launch_bend_records(v, R, cs);
-  ys::launch_face_records(v, R, cs);
-  ys::launch_gather(v, R, cs);
-  ys::launch_shear_records(v, R, cs);
+  ys::launch_edge_records(v, R, cs, b->producer_threads);
+  ys::launch_bend_records(v, R, cs, b->producer_threads);
+  ys::launch_face_records(v, R, cs, b->producer_threads);
+  ys::launch_gather(v, R, cs, b->producer_threads);
+  ys::launch_shear_records(v, R, cs, b->producer_threads);
   ys::launch_finalize(v, R, b->blk, b->so, cs);
   k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, cs>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
   if (b->plan.kind == YS_PCG_PERSISTENT) {
@@ -1463,6 +1465,15 @@ extern "C" {
 ys_status ys_use_graphs(ys_batch* b, int32_t enable) {
   if (!b) return fail(YS_ERR_ARG, "null handle");
   b->graph.enabled = enable != 0;
+  return YS_OK;
+}
+
+ys_status ys_set_producer_threads(ys_batch* b, int32_t threads) {
+  if (!b) return fail(YS_ERR_ARG, "null handle");
+  if (threads < 32 || threads > ys::kMaxProducerBlock || threads % 32)
+    return fail(YS_ERR_ARG, "ys_set_producer_threads: a multiple of 32 up to 256");
+  b->producer_threads = threads;
+  b->graph.built = false;
   return YS_OK;
 }
 
@@ -1595,6 +1606,7 @@ ys_status ys_autotune(ys_batch* b, double h, const ys_solve_opts* opts, int32_t 
   };
   const bool was_graph = b->graph.enabled, was_prof = b->profiling;
   const ys_batch::PcgPlan was_plan = b->plan;
+  const int was_pt = b->producer_threads;
   b->profiling = false;
   // the candidates
   std::vector<ys_schedule> cand;
@@ -1631,9 +1643,27 @@ ys_status ys_autotune(ys_batch* b, double h, const ys_solve_opts* opts, int32_t 
   if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
   if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
   b->tuned.clear();
-  for (size_t ci = 0; ci < cand.size() && ce == cudaSuccess && st == YS_OK; ++ci) {
-    const ys_schedule& k = cand[ci];
+  for (ys_schedule& k : cand) k.producer_threads = was_pt;
+  // first the graph / PCG choices at the batch's producer block size, then
+  // the producer block sizes under the best of those
+  const int pt_c[3] = {64, 128, 256};
+  bool widened = false;  // the producer sizes are appended once, after the first pass
+  for (size_t ci = 0; ce == cudaSuccess && st == YS_OK; ++ci) {
+    if (ci == cand.size() && !widened) {
+      widened = true;
+      if (top.ms_per_step >= 0)
+        for (int q = 0; q < 3; ++q)
+          if (pt_c[q] != was_pt) {
+            ys_schedule k = top;
+            k.producer_threads = pt_c[q];
+            cand.push_back(k);
+          }
+    }
+    if (ci >= cand.size()) break;
+    const ys_schedule k = cand[ci];
     if (ys_set_pcg_schedule(b, k.pcg, k.pcg_threads, k.pcg_cluster) != YS_OK) continue;  // shape cannot run here
+    b->producer_threads = k.producer_threads;
+    b->graph.built = false;
     b->graph.enabled = k.graphs == 1;
     ys_solve_opts o = opts ? *opts : ys_solve_opts{0.0, -1, 0};
     o.check_every = k.check_every;
@@ -1672,6 +1702,7 @@ ys_status ys_autotune(ys_batch* b, double h, const ys_solve_opts* opts, int32_t 
     b->plan.kind = was_plan.kind;
     b->plan.threads = was_plan.threads;
     b->plan.csize = was_plan.csize;
+    b->producer_threads = was_pt;
     b->graph.built = false;
     if (ce != cudaSuccess) return fail(YS_ERR_CUDA, std::string("ys_autotune: ") + cudaGetErrorString(ce));
     if (st != YS_OK) return st;
@@ -1679,6 +1710,8 @@ ys_status ys_autotune(ys_batch* b, double h, const ys_solve_opts* opts, int32_t 
   }
   b->graph.enabled = top.graphs != 0;
   b->check_every = top.check_every;
+  b->producer_threads = top.producer_threads;
+  b->graph.built = false;
   const ys_status sp = ys_set_pcg_schedule(b, top.pcg, top.pcg_threads, top.pcg_cluster);
   if (sp != YS_OK) return sp;
   if (best) *best = top;

@@ -9,6 +9,12 @@
 
 namespace ys {
 
+// The record producers and the gather: one thread per element (or node),
+// nothing shared between threads, so any block size gives the same bits; the
+// block size is a schedule choice (up to kMaxProducerBlock threads; up to
+// kBlock for the edges, whose 254 registers spill when compiled for 256-thread
+// blocks).
+
 // one thread per (yarn direction, node): the edge starting at that node
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_edge_rec(View v, Records R) {
@@ -25,7 +31,7 @@ __global__ void __launch_bounds__(kBlock) k_edge_rec(View v, Records R) {
 
 // one thread per (yarn direction, middle node) of a bend segment
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_bend_rec(View v, Records R) {
+__global__ void __launch_bounds__(kMaxProducerBlock) k_bend_rec(View v, Records R) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 2LL * v.ntot) return;
   const int k = t >= v.ntot ? 1 : 0;
@@ -40,7 +46,7 @@ __global__ void __launch_bounds__(kBlock) k_bend_rec(View v, Records R) {
 
 // one thread per grid cell (top-left node): its two faces
 template <class T>
-__global__ void k_face_rec(View v, Records R) {
+__global__ void __launch_bounds__(kMaxProducerBlock) k_face_rec(View v, Records R) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= v.ntot) return;
   const ClothParams& P = v.cp[v.node_cloth[n]];
@@ -50,14 +56,14 @@ __global__ void k_face_rec(View v, Records R) {
 
 // row blocks from edge / bend / face records, plus sliding friction
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_gather(View v, Records R) {
+__global__ void __launch_bounds__(kMaxProducerBlock) k_gather(View v, Records R) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n < v.ntot) gather_elements<T>(v, R, n);
 }
 
 // one thread per (segment type, crossing)
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_shear_rec(View v, Records R) {
+__global__ void __launch_bounds__(kMaxProducerBlock) k_shear_rec(View v, Records R) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 4LL * v.ntot) return;
   const int seg = (int)(t / v.ntot);

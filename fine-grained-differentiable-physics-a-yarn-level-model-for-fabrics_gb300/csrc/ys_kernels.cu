@@ -237,20 +237,22 @@ __global__ void k_spmv_plain(View v, const double* x, double* y) {
 void launch_geom(const View& v, const int* nodes, int n, cudaStream_t s) {
   if (n) k_geom<<<nblocks(n), kBlock, 0, s>>>(v, nodes, n);
 }
-void launch_edge_records(const View& v, const Records& R, cudaStream_t s) {
-  k_edge_rec<double><<<nblocks(2 * v.ntot), kBlock, 0, s>>>(v, R);
+static inline unsigned pblocks(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+void launch_edge_records(const View& v, const Records& R, cudaStream_t s, int t) {
+  t = t < kBlock ? t : kBlock;  // k_edge_rec is compiled for at most kBlock threads
+  k_edge_rec<double><<<pblocks(2LL * v.ntot, t), t, 0, s>>>(v, R);
 }
-void launch_bend_records(const View& v, const Records& R, cudaStream_t s) {
-  k_bend_rec<double><<<nblocks(2 * v.ntot), kBlock, 0, s>>>(v, R);
+void launch_bend_records(const View& v, const Records& R, cudaStream_t s, int t) {
+  k_bend_rec<double><<<pblocks(2LL * v.ntot, t), t, 0, s>>>(v, R);
 }
-void launch_face_records(const View& v, const Records& R, cudaStream_t s) {
-  k_face_rec<double><<<nblocks(v.ntot), kBlock, 0, s>>>(v, R);
+void launch_face_records(const View& v, const Records& R, cudaStream_t s, int t) {
+  k_face_rec<double><<<pblocks(v.ntot, t), t, 0, s>>>(v, R);
 }
-void launch_gather(const View& v, const Records& R, cudaStream_t s) {
-  k_gather<double><<<nblocks(v.ntot), kBlock, 0, s>>>(v, R);
+void launch_gather(const View& v, const Records& R, cudaStream_t s, int t) {
+  k_gather<double><<<pblocks(v.ntot, t), t, 0, s>>>(v, R);
 }
-void launch_shear_records(const View& v, const Records& R, cudaStream_t s) {
-  k_shear_rec<double><<<nblocks(4 * v.ntot), kBlock, 0, s>>>(v, R);
+void launch_shear_records(const View& v, const Records& R, cudaStream_t s, int t) {
+  k_shear_rec<double><<<pblocks(4LL * v.ntot, t), t, 0, s>>>(v, R);
 }
 void launch_finalize(const View& v, const Records& R, const Blocks& b, const Solver& so, cudaStream_t s) {
   k_finalize<<<b.nblk, kBlock, 0, s>>>(v, R, b, so);

@@ -45,13 +45,15 @@ struct Solver {
 };
 
 constexpr int kBlock = 128;
+constexpr int kMaxProducerBlock = 256;  // block size limit of the record producers and the gather
 
+// the producers' `threads` (per block, 32..kMaxProducerBlock) does not change results
 void launch_geom(const View& v, const int* nodes, int n, cudaStream_t s);
-void launch_edge_records(const View& v, const Records& R, cudaStream_t s);
-void launch_bend_records(const View& v, const Records& R, cudaStream_t s);
-void launch_face_records(const View& v, const Records& R, cudaStream_t s);
-void launch_gather(const View& v, const Records& R, cudaStream_t s);
-void launch_shear_records(const View& v, const Records& R, cudaStream_t s);
+void launch_edge_records(const View& v, const Records& R, cudaStream_t s, int threads = kBlock);
+void launch_bend_records(const View& v, const Records& R, cudaStream_t s, int threads = kBlock);
+void launch_face_records(const View& v, const Records& R, cudaStream_t s, int threads = kBlock);
+void launch_gather(const View& v, const Records& R, cudaStream_t s, int threads = kBlock);
+void launch_shear_records(const View& v, const Records& R, cudaStream_t s, int threads = kBlock);
 void launch_finalize(const View& v, const Records& R, const Blocks& b, const Solver& so, cudaStream_t s);
 void launch_pcg_setup(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
 void launch_pcg_spmv(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);

@@ -163,7 +163,7 @@ typedef struct ys_schedule {
   int32_t pcg;         /* YS_PCG_PHASES or YS_PCG_PERSISTENT */
   int32_t pcg_threads; /* persistent PCG: threads per CTA (128, 256, 512, 1024) */
   int32_t pcg_cluster; /* persistent PCG: CTAs per cloth (1, 2, 4, 8, 16) */
-  int32_t pad_;
+  int32_t producer_threads; /* block size of the record producers and the gather (64, 128, 256) */
 } ys_schedule;
 /* PCG schedules. Both run Eigen's Jacobi-PCG with the same arithmetic and the
  * same summation order, so they give bit-identical solutions:
@@ -178,11 +178,16 @@ enum { YS_PCG_PHASES = 0, YS_PCG_PERSISTENT = 1 };
  * and adjoint solves). YS_ERR_ARG if a cloth does not fit the persistent shape
  * or the GPU cannot hold one cluster of it. */
 ys_status ys_set_pcg_schedule(ys_batch *b, int32_t pcg, int32_t threads, int32_t cluster);
+/* Block size of the element-record producers and the gather (a multiple of
+ * 32 up to 256; default 128; the edges use at most 128). Results do not
+ * depend on it: one thread per element, nothing shared. */
+ys_status ys_set_producer_threads(ys_batch *b, int32_t threads);
 /* Times every schedule over `steps` steps of size h without an external force,
  * each from the batch's current state, which is restored afterwards, and makes
  * the fastest the batch's default: graph or launch by launch x (phase PCG with
  * check_every in {2, 4, 8, 16, 32}, or persistent PCG in every cluster shape
- * that holds the largest cloth with at most 4x its nodes). All schedules give
+ * that holds the largest cloth with at most 4x its nodes), then the producer
+ * block sizes 64, 128, 256 under the best of those. All schedules give
  * bit-identical states. */
 ys_status ys_autotune(ys_batch *b, double h, const ys_solve_opts *opts, int32_t steps, ys_schedule *best);
 /* The schedules the last ys_autotune timed, with their times: copies up to

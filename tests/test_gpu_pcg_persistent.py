@@ -146,3 +146,22 @@ def test_autotune_offers_the_persistent_schedule():
     for k in s0:
         assert np.array_equal(s0[k], s1[k]), k
     b.close()
+
+
+@pytest.mark.parametrize("threads", [64, 256])
+def test_producer_block_size_does_not_change_results(threads):
+    """The record producers and the gather at another block size
+    (ys_set_producer_threads): the same bits."""
+    def run(t):
+        b = ys.ClothBatch(_specs(MIXED, 9))
+        if t:
+            b.set_producer_threads(t)
+        out = []
+        for _ in range(3):
+            assert all(s["ok"] for s in b.step(1e-3, tol=1e-10))
+            out.append(b.get_state())
+        b.close()
+        return out
+    for a, c in zip(run(None), run(threads)):
+        for k in a:
+            assert np.array_equal(a[k], c[k]), k
