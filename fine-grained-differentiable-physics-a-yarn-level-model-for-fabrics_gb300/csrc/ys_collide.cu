@@ -133,7 +133,12 @@ struct BroadArgs {
   const int* cslice;           // slice roots of the cloth tree, depth-first order
   const int* oslice;           // and of the obstacle tree
   int ncs, nos;
+  // the count pass keeps each (face, slice)'s first kBroadKeep partner faces
+  // here ([work][kBroadKeep]); the write pass copies them instead of
+  // traversing again when that is all of them
+  int* keep;
 };
+constexpr int kBroadKeep = 4;
 
 // one thread per (cloth face f, slice): the slices are the subtrees rooted at
 // depth kSliceDepth of the cloth tree, then of the obstacle tree, in
@@ -149,6 +154,16 @@ __global__ void k_broad(BroadArgs a) {
   const int pass = sl < a.ncs ? 0 : 1;
   const bool fa = a.face_active == nullptr || a.face_active[f] != 0;
   int64_t c = 0;
+  if (WRITE && a.count[idx] <= kBroadKeep) {
+    // every partner was kept by the count pass, in traversal order
+    const int64_t o = a.offset[idx], nk = a.count[idx];
+    for (int64_t j = 0; j < nk; ++j) {
+      a.out[3 * (o + j)] = f;
+      a.out[3 * (o + j) + 1] = a.keep[idx * kBroadKeep + j];
+      a.out[3 * (o + j) + 2] = pass;
+    }
+    return;
+  }
   if (pass == 0 || fa) {
     const DevTree& t = pass == 0 ? a.cloth : a.obs;
     const int root = pass == 0 ? a.cslice[sl] : a.oslice[sl - a.ncs];
@@ -176,6 +191,8 @@ __global__ void k_broad(BroadArgs a) {
           a.out[3 * (o + c)] = f;
           a.out[3 * (o + c) + 1] = g;
           a.out[3 * (o + c) + 2] = pass;
+        } else if (c < kBroadKeep) {
+          a.keep[idx * kBroadKeep + c] = g;
         }
         ++c;
       } else {
@@ -192,23 +209,75 @@ __global__ void k_broad(BroadArgs a) {
   if (!WRITE) a.count[idx] = c;
 }
 
-__global__ void k_narrow(const int* __restrict__ pairs, int64_t npairs, const CFace* __restrict__ faces,
-                         const CFace* __restrict__ ofaces, CMesh m, double thickness, int ccd, Impact* slots,
-                         int64_t* count) {
+// Narrow phase in two kernels. k_narrow_mask: one thread per pair forms the
+// k-DOPs of its six nodes and decides which of the 15 tests run (cc_face_pair's
+// overlap and shared-node rules). k_narrow_test: one thread per (test, pair),
+// test-major, so a warp runs one kind of test on 32 pairs; test t of pair p
+// writes slot 15 p + t (type -1: no impact) and counts its impact for the
+// pair. The compaction then takes each pair's slots in test order: the
+// impacts, and their order, are cc_face_pair's.
+// k-DOP of every node's motion (kdop_node of its two positions): cloth node
+// i at [i], obstacle node j at [n_nodes + j]
+__global__ void k_node_kdop(CMesh m, int n_nodes, int n_obs, int ccd, Kdop* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_nodes + n_obs) return;
+  const int id = i < n_nodes ? i : -1 - (i - n_nodes);  // obstacle ids as -1 - id
+  Kdop b;
+  ys::kdop_node(b, ys::cc_pos(m, id, false), ys::cc_pos(m, id, true), ccd != 0);
+  out[i] = b;
+}
+struct NodeKdops {
+  const Kdop* k;
+  int n_nodes;
+  __device__ __forceinline__ Kdop operator()(int id) const { return k[id >= 0 ? id : n_nodes + (-1 - id)]; }
+};
+__global__ void k_narrow_mask(const int* __restrict__ pairs, int64_t npairs, const CFace* __restrict__ faces,
+                              const CFace* __restrict__ ofaces, NodeKdops nk, double thickness,
+                              int* __restrict__ mask, int64_t* __restrict__ count) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npairs) return;
   const CFace& f0 = faces[pairs[3 * p]];
   const CFace& f1 = pairs[3 * p + 2] ? ofaces[pairs[3 * p + 1]] : faces[pairs[3 * p + 1]];
-  count[p] = ys::cc_face_pair(m, f0, f1, thickness, ccd != 0, slots + 15 * p);
+  mask[p] = ys::cc_face_pair_mask(nk, f0, f1, thickness);
+  count[p] = 0;
+}
+__global__ void k_narrow_test(const int* __restrict__ pairs, int64_t npairs, const CFace* __restrict__ faces,
+                              const CFace* __restrict__ ofaces, CMesh m, const int* __restrict__ mask, Impact* slots,
+                              unsigned long long* count) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 15 * npairs) return;
+  const int t = (int)(idx / npairs);
+  const int64_t p = idx - (int64_t)t * npairs;
+  Impact& out = slots[15 * p + t];
+  out.type = -1;
+  if (!((mask[p] >> t) & 1)) return;
+  const CFace& f0 = faces[pairs[3 * p]];
+  const CFace& f1 = pairs[3 * p + 2] ? ofaces[pairs[3 * p + 1]] : faces[pairs[3 * p + 1]];
+  int type, ids[4];
+  ys::cc_pair_test_nodes(f0, f1, t, type, ids);
+  const double* xs[4];
+  const double* xps[4];
+  for (int k = 0; k < 4; ++k) {
+    xs[k] = ys::cc_pos(m, ids[k], false);
+    xps[k] = ys::cc_pos(m, ids[k], true);
+  }
+  Impact im;
+  if (ys::cc_test(type, xs, xps, im)) {
+    for (int k = 0; k < 4; ++k) im.node[k] = ids[k];
+    out = im;
+    atomicAdd(count + p, 1ull);
+  }
 }
 
 __global__ void k_compact(const Impact* __restrict__ slots, const int64_t* __restrict__ count,
                           const int64_t* __restrict__ offset, int64_t npairs, ys_impact* out) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npairs) return;
-  for (int k = 0; k < count[p]; ++k) {
-    const Impact& s = slots[15 * p + k];
-    ys_impact& r = out[offset[p] + k];
+  int64_t k = 0;
+  for (int t = 0; t < 15 && k < count[p]; ++t) {
+    const Impact& s = slots[15 * p + t];
+    if (s.type < 0) continue;
+    ys_impact& r = out[offset[p] + k++];
     r.type = s.type;
     for (int q = 0; q < 4; ++q) r.nodes[q] = s.node[q];
     r.t = s.t;
@@ -331,10 +400,13 @@ struct ys_collider {
   DVec<float> c_fbox, o_fbox;
   // outputs
   DVec<int64_t> counts, offsets, sums, total;
+  DVec<int> keep;  // the broad phase's kept partners ([work][kBroadKeep])
   DVec<int> pairs;
   int64_t npairs = 0;
   DVec<Impact> slots;
   DVec<int64_t> icount, ioffset;
+  DVec<int> tmask;  // narrow phase: the tests each pair runs (bit t)
+  DVec<Kdop> nkdop;  // narrow phase: every node's motion k-DOP (cloth, then obstacle)
   DVec<ys_impact> impacts;
   int64_t nimpacts = 0;
   DVec<int> overflow;
@@ -476,6 +548,7 @@ ys_status broad_phase(ys_collider* c, bool masked) {
   // them is taken (a reserve may move them)
   YC_CUDA(c->counts.reserve(std::max<int64_t>(work, 1)));
   YC_CUDA(c->offsets.reserve(std::max<int64_t>(work, 1)));
+  YC_CUDA(c->keep.reserve(std::max<int64_t>(work * kBroadKeep, 1)));
   BroadArgs a{};
   a.cloth = DevTree{c->c_left.p, c->c_right.p, c->c_face.p, c->c_box.p, (int)c->ct.face.size(), c->c_fbox.p};
   a.obs = DevTree{c->o_left.p, c->o_right.p, c->o_face.p, c->o_box.p, (int)c->ot.face.size(), c->o_fbox.p};
@@ -494,6 +567,7 @@ ys_status broad_phase(ys_collider* c, bool masked) {
   a.oslice = c->oslice.p;
   a.ncs = ncs;
   a.nos = nos;
+  a.keep = c->keep.p;
   YC_CUDA(cudaMemsetAsync(c->overflow.p, 0, sizeof(int), c->stream));
   const unsigned g = (unsigned)((work + kBroadBlock - 1) / kBroadBlock);
   if (work) k_broad<false><<<g, kBroadBlock, 0, c->stream>>>(a);
@@ -522,10 +596,18 @@ ys_status narrow_phase(ys_collider* c) {
   YC_CUDA(c->slots.reserve(15 * (size_t)std::max<int64_t>(P, 1)));
   YC_CUDA(c->icount.reserve(std::max<int64_t>(P, 1)));
   YC_CUDA(c->ioffset.reserve(std::max<int64_t>(P, 1)));
+  YC_CUDA(c->tmask.reserve(std::max<int64_t>(P, 1)));
+  YC_CUDA(c->nkdop.reserve(std::max(c->n_nodes + c->n_obs_nodes, 1)));
   CMesh m{c->x.p, c->xp.p, c->ox.p, c->oxp.p};
   if (P) {
-    k_narrow<<<(unsigned)((P + 127) / 128), 128, 0, c->stream>>>(c->pairs.p, P, c->faces.p, c->ofaces.p, m,
-                                                                  c->thickness, c->ccd, c->slots.p, c->icount.p);
+    const int nn = c->n_nodes + c->n_obs_nodes;
+    k_node_kdop<<<(nn + 127) / 128, 128, 0, c->stream>>>(m, c->n_nodes, c->n_obs_nodes, c->ccd, c->nkdop.p);
+    k_narrow_mask<<<(unsigned)((P + 127) / 128), 128, 0, c->stream>>>(c->pairs.p, P, c->faces.p, c->ofaces.p,
+                                                                       NodeKdops{c->nkdop.p, c->n_nodes},
+                                                                       c->thickness, c->tmask.p, c->icount.p);
+    k_narrow_test<<<(unsigned)((15 * P + 127) / 128), 128, 0, c->stream>>>(
+        c->pairs.p, P, c->faces.p, c->ofaces.p, m, c->tmask.p, c->slots.p,
+        reinterpret_cast<unsigned long long*>(c->icount.p));
     YC_CUDA(cudaGetLastError());
   }
   ys_status s = scan(c, c->icount.p, P, c->ioffset.p, &c->nimpacts);

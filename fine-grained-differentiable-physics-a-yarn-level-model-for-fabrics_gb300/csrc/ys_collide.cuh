@@ -312,6 +312,68 @@ YS_HD const double* cc_pos(const CMesh& m, int id, bool prev) {
 
 // comp_face_impacts for the pair (f0, f1): up to 15 impacts in out, in the
 // reference's order (3 + 3 vertex-face, 9 edge-edge); returns the count
+// The 15 tests of a face pair in cc_face_pair's order -- t 0..2: node t of f0
+// against f1; 3..5: node t - 3 of f1 against f0; 6..14: edge (t - 6) / 3 of
+// f0 against edge (t - 6) % 3 of f1 -- and the nodes each one takes.
+YS_HD void cc_pair_test_nodes(const CFace& f0, const CFace& f1, int t, int& type, int ids[4]) {
+  if (t < 3) {
+    type = 0;
+    ids[0] = f0.v[t]; ids[1] = f1.v[0]; ids[2] = f1.v[1]; ids[3] = f1.v[2];
+  } else if (t < 6) {
+    type = 0;
+    ids[0] = f1.v[t - 3]; ids[1] = f0.v[0]; ids[2] = f0.v[1]; ids[3] = f0.v[2];
+  } else {
+    type = 1;
+    const int* e0 = f0.e[(t - 6) / 3];
+    const int* e1 = f1.e[(t - 6) % 3];
+    ids[0] = e0[0]; ids[1] = e0[1]; ids[2] = e1[0]; ids[3] = e1[1];
+  }
+}
+
+// Bit t set when cc_face_pair would run test t: the k-DOP overlap and
+// shared-node rules of comp_face_impacts (src/Collision.cpp:327-419). nk(id)
+// gives node id's k-DOP (kdop_node of its two positions); the face and edge
+// boxes are their unions, formed in cc_face_pair's order (min / max: exact).
+template <class NodeBox>
+YS_HD int cc_face_pair_mask(const NodeBox& nk, const CFace& f0, const CFace& f1, double thickness) {
+  int mask = 0;
+  {
+    Kdop fb = nk(f1.v[0]);
+    kdop_add(fb, nk(f1.v[1]));
+    kdop_add(fb, nk(f1.v[2]));
+    for (int k = 0; k < 3; ++k) {
+      const int nd = f0.v[k];
+      if (nd == f1.v[0] || nd == f1.v[1] || nd == f1.v[2]) continue;
+      if (kdop_overlap(nk(nd), fb, thickness)) mask |= 1 << k;
+    }
+  }
+  {
+    Kdop fb = nk(f0.v[0]);
+    kdop_add(fb, nk(f0.v[1]));
+    kdop_add(fb, nk(f0.v[2]));
+    for (int k = 0; k < 3; ++k) {
+      const int nd = f1.v[k];
+      if (nd == f0.v[0] || nd == f0.v[1] || nd == f0.v[2]) continue;
+      if (kdop_overlap(nk(nd), fb, thickness)) mask |= 1 << (3 + k);
+    }
+  }
+  for (int a = 0; a < 3; ++a) {
+    const int an = a != 2 ? a + 1 : 0;
+    Kdop ea = nk(f0.v[a]);
+    kdop_add(ea, nk(f0.v[an]));
+    for (int b = 0; b < 3; ++b) {
+      const int* e0 = f0.e[a];
+      const int* e1 = f1.e[b];
+      if (e0[0] == e1[0] || e0[0] == e1[1] || e0[1] == e1[0] || e0[1] == e1[1]) continue;
+      const int bn = b != 2 ? b + 1 : 0;
+      Kdop eb = nk(f1.v[b]);
+      kdop_add(eb, nk(f1.v[bn]));
+      if (kdop_overlap(ea, eb, thickness)) mask |= 1 << (6 + 3 * a + b);
+    }
+  }
+  return mask;
+}
+
 YS_HD int cc_face_pair(const CMesh& m, const CFace& f0, const CFace& f1, double thickness, bool ccd, Impact* out) {
   Kdop nb[6], eb[6], fb[2];
   for (int k = 0; k < 3; ++k) {
