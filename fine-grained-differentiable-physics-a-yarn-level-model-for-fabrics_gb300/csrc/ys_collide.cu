@@ -7,6 +7,8 @@
 // in pair order, then the reference's test order).
 #include <cuda_runtime.h>
 
+#include <cuda/atomic>
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -101,9 +103,10 @@ __global__ void k_refit_up(DevTree t, const int* __restrict__ leaves, int nleave
   for (;;) {
     const int p = parent[n];
     if (p < 0) return;
-    __threadfence();  // this node's box is visible before the count says so
-    if (atomicAdd(arrive + p, 1) == 0) return;  // the sibling's thread goes on
-    __threadfence();
+    // release: this node's box is visible before the count says so; acquire:
+    // the second arrival sees its sibling's box
+    cuda::atomic_ref<int, cuda::thread_scope_device> cnt(arrive[p]);
+    if (cnt.fetch_add(1, cuda::memory_order_acq_rel) == 0) return;  // the sibling's thread goes on
     Kdop b, rb;
     kdop_load_l2(b, t.box + t.left[p]);
     kdop_load_l2(rb, t.box + t.right[p]);
@@ -138,7 +141,7 @@ struct BroadArgs {
   // traversing again when that is all of them
   int* keep;
 };
-constexpr int kBroadKeep = 4;
+constexpr int kBroadKeep = 16;
 
 // one thread per (cloth face f, slice): the slices are the subtrees rooted at
 // depth kSliceDepth of the cloth tree, then of the obstacle tree, in
