@@ -307,14 +307,22 @@ YS_HD bool gather_shear_finalize(const View& v, const Records& R, int n, double*
   auto addLL = [&](int du, int dv, const T* blk) {  // A[x(n)][x(n + (du, dv))] += -h^2 blk^T
     const int s = stencil_index(du, dv);
     if (s < 0) return;
+    // the block's nine slots are loaded together, then updated: a load per
+    // slot behind the previous slot's store would wait out one memory
+    // latency per slot
+    T a[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) a[i] = ldA<T>(v, YS_SLOT_LL + 9 * s + i, n);
+#pragma unroll
     for (int r = 0; r < 3; ++r)
+#pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const int sl = YS_SLOT_LL + 9 * s + 3 * r + c;
-        T a = ldA<T>(v, sl, n);
-        a += mh2 * blk[3 * c + r];
-        finf = finf && isfinite(val(a));
-        stA(v, sl, n, a);
+        T& x = a[3 * r + c];
+        x += mh2 * blk[3 * c + r];
+        finf = finf && isfinite(val(x));
       }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) stA(v, YS_SLOT_LL + 9 * s + i, n, a[i]);
   };
   auto addB = [&](int c, const T& x) {
     T b = ldT<T>(v.B, v.dB, c, nt, n);
