@@ -275,6 +275,7 @@ def precond_compare(ys, dev, repeats=6):
             b.set_preconditioner("jacobi")
             b.step(H, tol=TOL)
         steps = {}
+        b.use_graphs(True)  # both arms: one CUDA graph launch per step
         for kind, every in (("jacobi", 1), ("learned_refresh4", 4)):
             b.set_preconditioner("learned" if kind != "jacobi" else "jacobi", net if kind != "jacobi" else None)
             b.precond_refresh(every)
@@ -296,6 +297,7 @@ def precond_compare(ys, dev, repeats=6):
                         "solve_ms_with_inference": float(np.median([r[1] for r in res["learned"]])),
                         "fallbacks": fb},
             "step_ms": steps,
+            "step_schedule": "one CUDA graph per step, both preconditioners",
             "residual": "both |r| <= 1e-10 |b| (FP64)"}
     net.close()
     return out

@@ -114,17 +114,36 @@ struct ys_batch {
   std::vector<DescStore> descs;
   // whole-step CUDA graph (ys_use_graphs): assembly, a conditional while node
   // over the PCG iterations, update; rebuilt when its parameters change
+  // `built`: the parameters below are current; each graph is captured on its
+  // first use after they change
   struct Graph {
     bool enabled = false;
     bool built = false;
     cudaStream_t capture = nullptr;  // capture needs a stream of its own
-    cudaGraph_t main = nullptr;
+    cudaGraph_t main = nullptr;      // Jacobi-PCG step
     cudaGraphExec_t exec = nullptr;
+    cudaGraph_t lmain[2] = {nullptr, nullptr};  // learned-preconditioner step [with the network]
+    cudaGraphExec_t lexec[2] = {nullptr, nullptr};
+    const void* lnet = nullptr;  // the network the learned graphs were captured with
     double h = 0.0, tol = 0.0;
     bool has_ext = false;
     int override_max = -1, m = 0, cap = 0;
     int* it_base = nullptr;  // device
+    int* hold = nullptr;     // device: the learned solve handed the step to Jacobi-PCG
     int h_it = 0;
+    int h_hold = 0;
+    void drop() {
+      if (exec) cudaGraphExecDestroy(exec);
+      if (main) cudaGraphDestroy(main);
+      exec = nullptr;
+      main = nullptr;
+      for (int k = 0; k < 2; ++k) {
+        if (lexec[k]) cudaGraphExecDestroy(lexec[k]);
+        if (lmain[k]) cudaGraphDestroy(lmain[k]);
+        lexec[k] = nullptr;
+        lmain[k] = nullptr;
+      }
+    }
   } graph;
   int check_every = 16;  // PCG iterations between convergence checks when the call gives none
   // PCG schedule (ys_set_pcg_schedule): phases, or the persistent per-cloth
@@ -145,7 +164,7 @@ struct ys_batch {
     ys_gnn* net = nullptr;
     bool ready = false;
     ys::GnnBufs g{};
-    float* y = nullptr;
+    float* rf = nullptr;  // the residual in FP32 (the preconditioner's input)
     double* z = nullptr;
     int64_t fallbacks = 0;
     int64_t solves = 0;
@@ -203,8 +222,7 @@ struct ys_batch {
   }
   ~ys_batch() {
     drain();
-    if (graph.exec) cudaGraphExecDestroy(graph.exec);
-    if (graph.main) cudaGraphDestroy(graph.main);
+    graph.drop();
     if (graph.capture) cudaStreamDestroy(graph.capture);
     for (cudaEvent_t e : pool) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
@@ -680,8 +698,7 @@ ys_status ys_get_solution(ys_batch* b, double* x, int32_t flags) {
 
 ys_status ys_step(ys_batch* b, double h, const double* ext_force, int32_t flags, const ys_solve_opts* opts,
                   ys_cloth_stats* stats) {
-  if (b && b->graph.enabled && !b->profiling && b->learn.kind == YS_PREC_JACOBI)
-    return ys_step_graphed(b, h, ext_force, flags, opts, stats);
+  if (b && b->graph.enabled && !b->profiling) return ys_step_graphed(b, h, ext_force, flags, opts, stats);
   ys_status s = ys_assemble(b, h, ext_force, flags);
   if (s != YS_OK) return s;
   std::vector<ys_cloth_stats> local;
@@ -1377,23 +1394,19 @@ ys_status ys_adjoint_step(ys_adjoint* a, double h, const double* ext_force, cons
 // ----------------------------------------------------------- graphed step
 namespace {
 
-ys_status graph_build(ys_batch* b, int m, int cap, int override_max) {
+ys_status graph_prepare(ys_batch* b) {
   ys_batch::Graph& G = b->graph;
-  if (G.exec) { cudaGraphExecDestroy(G.exec); G.exec = nullptr; }
-  if (G.main) { cudaGraphDestroy(G.main); G.main = nullptr; }
   if (!G.capture) YS_CUDA(cudaStreamCreateWithFlags(&G.capture, cudaStreamNonBlocking));
-  if (!G.it_base) {
-    const ys_status s = b->alloc(&G.it_base, 1);
-    if (s != YS_OK) return s;
-  }
-  ys::Solver so = b->so;
-  so.it_base = G.it_base;
+  ys_status s = YS_OK;
+  if (!G.it_base && (s = b->alloc(&G.it_base, 1)) != YS_OK) return s;
+  if (!G.hold && (s = b->alloc(&G.hold, 1)) != YS_OK) return s;
+  return YS_OK;
+}
+
+// the kernels of ys_assemble and the PCG counters' reset, onto a capturing stream
+void capture_assembly(ys_batch* b, cudaStream_t cs, int override_max) {
   const ys::View& v = b->v;
   const ys::Records& R = b->rec;
-  cudaStream_t cs = G.capture;
-  // before the loop: ys_assemble's kernels, the PCG start, the loop counter
-  cudaGraph_t pre = nullptr, post = nullptr;
-  YS_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
   k_reset_status<<<(b->ncloth + 127) / 128, 128, 0, cs>>>(b->so.pc, b->ncloth);
   if (b->geom_n) ys::launch_geom(v, b->anchors + b->geom_off, b->geom_n, cs);
   ys::launch_edge_records(v, R, cs, b->producer_threads);
@@ -1403,8 +1416,63 @@ ys_status graph_build(ys_batch* b, int m, int cap, int override_max) {
   ys::launch_shear_records(v, R, cs, b->producer_threads);
   ys::launch_finalize(v, R, b->blk, b->so, cs);
   k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, cs>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
+}
+
+// main = pre -> while (condition) { body } -> post, each part captured from
+// the launches its function makes on the capture stream; body ends with the
+// kernel that sets the condition (handed to it)
+template <class Pre, class Body, class Post>
+ys_status build_loop_graph(ys_batch* b, Pre pre_fn, Body body_fn, Post post_fn, cudaGraph_t* main,
+                           cudaGraphExec_t* exec) {
+  cudaStream_t cs = b->graph.capture;
+  cudaGraph_t pre = nullptr, post = nullptr;
+  YS_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  pre_fn(cs);
+  YS_CUDA(cudaStreamEndCapture(cs, &pre));
+  YS_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  post_fn(cs);
+  YS_CUDA(cudaStreamEndCapture(cs, &post));
+  YS_CUDA(cudaGraphCreate(main, 0));
+  cudaGraphNode_t n_pre, n_loop, n_post;
+  YS_CUDA(cudaGraphAddChildGraphNode(&n_pre, *main, nullptr, 0, pre));
+  cudaGraphConditionalHandle hcond;
+  YS_CUDA(cudaGraphConditionalHandleCreate(&hcond, *main, 1, cudaGraphCondAssignDefault));
+  // cudaGraphNodeParams has no default constructor: zeroed storage instead
+  alignas(cudaGraphNodeParams) unsigned char cp_raw[sizeof(cudaGraphNodeParams)] = {};
+  cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cp_raw);
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = hcond;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  YS_CUDA(cudaGraphAddNode(&n_loop, *main, &n_pre, nullptr, 1, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  YS_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  body_fn(cs, hcond);
+  YS_CUDA(cudaStreamEndCapture(cs, &body));
+  YS_CUDA(cudaGraphAddChildGraphNode(&n_post, *main, &n_loop, 1, post));
+  cudaGraphDestroy(pre);
+  cudaGraphDestroy(post);
+  YS_CUDA(cudaGraphInstantiate(exec, *main, 0));
+  return YS_OK;
+}
+
+// the Jacobi-PCG step: assembly and PCG set-up, a conditional while node whose
+// body is m PCG iterations (m even keeps the r.z parity of each iteration
+// equal to its local index's) and the condition, then the solution check and
+// Cloth::update. With the persistent PCG the solve is one kernel: one graph.
+ys_status graph_build(ys_batch* b, int m, int cap, int override_max) {
+  ys_batch::Graph& G = b->graph;
+  if (G.exec) { cudaGraphExecDestroy(G.exec); G.exec = nullptr; }
+  if (G.main) { cudaGraphDestroy(G.main); G.main = nullptr; }
+  ys_status st = graph_prepare(b);
+  if (st != YS_OK) return st;
+  ys::Solver so = b->so;
+  so.it_base = G.it_base;
+  const ys::View& v = b->v;
+  cudaStream_t cs = G.capture;
   if (b->plan.kind == YS_PCG_PERSISTENT) {
-    // the whole solve is one kernel: no loop node, one graph
+    YS_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    capture_assembly(b, cs, override_max);
     const cudaError_t e =
         ys::launch_pcg_cluster(v, so, b->plan.order, b->ncloth, b->plan.threads, b->plan.csize, cap, cs);
     ys::launch_update(v, b->blk, b->so, cs);
@@ -1416,46 +1484,103 @@ ys_status graph_build(ys_batch* b, int m, int cap, int override_max) {
     }
     G.main = one;
     YS_CUDA(cudaGraphInstantiate(&G.exec, G.main, 0));
-    G.built = true;
     return YS_OK;
   }
-  ys::launch_pcg_setup(v, b->blk, so, cs);
-  ys::launch_graph_loop_begin(so, cs);
-  YS_CUDA(cudaStreamEndCapture(cs, &pre));
-  // after the loop: the solution check and Cloth::update
-  YS_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-  ys::launch_update(v, b->blk, b->so, cs);
-  YS_CUDA(cudaStreamEndCapture(cs, &post));
-  YS_CUDA(cudaGraphCreate(&G.main, 0));
-  cudaGraphNode_t n_pre, n_loop, n_post;
-  YS_CUDA(cudaGraphAddChildGraphNode(&n_pre, G.main, nullptr, 0, pre));
-  cudaGraphConditionalHandle hcond;
-  YS_CUDA(cudaGraphConditionalHandleCreate(&hcond, G.main, 1, cudaGraphCondAssignDefault));
-  // cudaGraphNodeParams has no default constructor: zeroed storage instead
-  alignas(cudaGraphNodeParams) unsigned char cp_raw[sizeof(cudaGraphNodeParams)] = {};
-  cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cp_raw);
-  cp.type = cudaGraphNodeTypeConditional;
-  cp.conditional.handle = hcond;
-  cp.conditional.type = cudaGraphCondTypeWhile;
-  cp.conditional.size = 1;
-  YS_CUDA(cudaGraphAddNode(&n_loop, G.main, &n_pre, nullptr, 1, &cp));
-  // the loop body: m PCG iterations (m even keeps the r.z parity of each
-  // iteration equal to its local index's), then the condition
-  cudaGraph_t body = cp.conditional.phGraph_out[0];
-  YS_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  for (int j = 0; j < m; ++j) {
-    ys::launch_pcg_spmv(v, b->blk, so, cs);
-    ys::launch_pcg_axpy(v, b->blk, so, j, cs);
-    ys::launch_pcg_dir(v, b->blk, so, j, cs);
+  return build_loop_graph(
+      b,
+      [&](cudaStream_t c) {
+        capture_assembly(b, c, override_max);
+        ys::launch_pcg_setup(v, b->blk, so, c);
+        ys::launch_graph_loop_begin(so, c);
+      },
+      [&](cudaStream_t c, cudaGraphConditionalHandle h) {
+        for (int j = 0; j < m; ++j) {
+          ys::launch_pcg_spmv(v, b->blk, so, c);
+          ys::launch_pcg_axpy(v, b->blk, so, j, c);
+          ys::launch_pcg_dir(v, b->blk, so, j, c);
+        }
+        ys::launch_graph_loop_tail(so, b->ncloth, m, cap, h, c);
+      },
+      [&](cudaStream_t c) { ys::launch_update(v, b->blk, b->so, c); }, &G.main, &G.exec);
+}
+
+ys_status graph_build_learned(ys_batch* b, int m, int cap, int override_max, int with_net);
+ys_status learn_ensure(ys_batch* b);
+
+// a step's result from the cloths' PCG records (read after the update)
+ys_status step_result(ys_batch* b, const std::vector<ys::PcgCloth>& pc, ys_cloth_stats* stats) {
+  ys_status ret = YS_OK;
+  for (int c = 0; c < b->ncloth; ++c) {
+    if (pc[c].status & 3) ret = YS_ERR_NONFINITE;
+    else if ((pc[c].status & 4) && ret == YS_OK) ret = YS_ERR_MAXITER;
+    if (stats) {
+      stats[c].ok = (pc[c].status & 3) == 0;
+      stats[c].cg_iterations = pc[c].iters;
+      stats[c].cg_error = pc[c].bb > 0 ? std::sqrt(pc[c].rr / pc[c].bb) : 0.0;
+      stats[c].hit_maxiter = (pc[c].status & 4) ? 1 : 0;
+    }
   }
-  ys::launch_graph_loop_tail(so, b->ncloth, m, cap, hcond, cs);
-  YS_CUDA(cudaStreamEndCapture(cs, &body));
-  YS_CUDA(cudaGraphAddChildGraphNode(&n_post, G.main, &n_loop, 1, post));
-  cudaGraphDestroy(pre);
-  cudaGraphDestroy(post);
-  YS_CUDA(cudaGraphInstantiate(&G.exec, G.main, 0));
-  G.built = true;
-  return YS_OK;
+  b->assembled = false;
+  return ret;
+}
+
+// the graphed step with the learned preconditioner: one graph with the
+// network evaluated after the assembly, one without (G reused), chosen as
+// the launch-by-launch solve chooses; when the graph's verdict kernel held
+// the update back, the assembled system is solved again by Jacobi-PCG and
+// updated launch by launch
+ys_status step_graphed_learned(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* stats, int m, int cap,
+                               int override_max) {
+  ys_batch::Graph& G = b->graph;
+  ys_batch::Learn& L = b->learn;
+  if (!L.net) return fail(YS_ERR_ARG, "learned preconditioner without a network");
+  ys_status st = learn_ensure(b);
+  if (st != YS_OK) return st;
+  const int with_net = (!L.have_g || ++L.since >= L.refresh_every) ? 1 : 0;
+  if (!G.lexec[with_net]) {
+    st = graph_build_learned(b, m, cap, override_max, with_net);
+    if (st != YS_OK) {
+      G.drop();
+      return st;
+    }
+  }
+  YS_CUDA(cudaGraphLaunch(G.lexec[with_net], b->stream));
+  if (with_net) {
+    L.have_g = true;
+    L.since = 0;
+  }
+  L.solves += 1;
+  std::vector<ys::PcgCloth> pc(b->ncloth);
+  YS_CUDA(cudaMemcpyAsync(pc.data(), b->so.pc, sizeof(ys::PcgCloth) * b->ncloth, cudaMemcpyDeviceToHost, b->stream));
+  YS_CUDA(cudaMemcpyAsync(&G.h_it, G.it_base, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  YS_CUDA(cudaMemcpyAsync(&G.h_hold, G.hold, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  // kernels the graph ran: 11 (+ geometry) before the network, 8 for the
+  // network, 4 before the loop, 4 per iteration + 1 per trip, 3 after
+  b->launches += 18 + (b->geom_n ? 1 : 0) + 8 * with_net + 4LL * G.h_it + G.h_it / m;
+  if (!G.h_hold) return step_result(b, pc, stats);
+  L.fallbacks += 1;
+  YS_CUDA(cudaMemsetAsync(L.g.err, 0, sizeof(int), b->stream));
+  b->launches += 1;
+  std::vector<ys_cloth_stats> local;
+  ys_cloth_stats* sts = stats;
+  if (!sts) {
+    local.resize(b->ncloth);
+    sts = local.data();
+  }
+  const ys_status sol = solve_impl(b, b->v, opts, sts);
+  if (sol == YS_ERR_ARG || sol == YS_ERR_CUDA) return sol;
+  b->run(YS_PROF_UPDATE, 2, [&] { ys::launch_update(b->v, b->blk, b->so, b->stream); });
+  YS_CUDA(cudaGetLastError());
+  YS_CUDA(cudaMemcpyAsync(pc.data(), b->so.pc, sizeof(ys::PcgCloth) * b->ncloth, cudaMemcpyDeviceToHost, b->stream));
+  YS_CUDA(cudaStreamSynchronize(b->stream));
+  ys_status ret = sol;
+  for (int c = 0; c < b->ncloth; ++c) {
+    sts[c].ok = (pc[c].status & 3) == 0;
+    if (!sts[c].ok) ret = YS_ERR_NONFINITE;
+  }
+  b->assembled = false;
+  return ret;
 }
 
 }  // namespace
@@ -1538,20 +1663,32 @@ ys_status ys_step_graphed(ys_batch* b, double h, const double* ext_force, int32_
   }
   const double tol = (opts && opts->tol > 0) ? opts->tol : DBL_EPSILON;
   const int override_max = (opts && opts->maxiter >= 0) ? opts->maxiter : -1;
-  int m = (opts && opts->check_every > 0) ? opts->check_every : b->check_every;
+  // iterations per trip through the loop body; the learned solve converges in
+  // a few, so its body is short unless the call asks otherwise
+  const bool learned = b->learn.kind == YS_PREC_LEARNED;
+  int m = (opts && opts->check_every > 0) ? opts->check_every : learned ? 4 : b->check_every;
   m += m & 1;
   const int cap = override_max >= 0 ? override_max : b->max_maxiter;
   b->so.tol = tol;
   if (!G.built || G.h != h || G.has_ext != (ext_force != nullptr) || G.tol != tol ||
-      G.override_max != override_max || G.m != m || G.cap != cap) {
-    ys_status s = graph_build(b, m, cap, override_max);
-    if (s != YS_OK) return s;
+      G.override_max != override_max || G.m != m || G.cap != cap || (learned && G.lnet != b->learn.net)) {
+    G.drop();
+    G.built = true;
     G.h = h;
     G.has_ext = ext_force != nullptr;
     G.tol = tol;
     G.override_max = override_max;
     G.m = m;
     G.cap = cap;
+    G.lnet = b->learn.net;
+  }
+  if (learned) return step_graphed_learned(b, opts, stats, m, cap, override_max);
+  if (!G.exec) {
+    const ys_status s = graph_build(b, m, cap, override_max);
+    if (s != YS_OK) {
+      G.drop();
+      return s;
+    }
   }
   YS_CUDA(cudaGraphLaunch(G.exec, b->stream));
   std::vector<ys::PcgCloth> pc(b->ncloth);
@@ -1564,19 +1701,7 @@ ys_status ys_step_graphed(ys_batch* b, double h, const double* ext_force, int32_
   // geometry) before the solve, the solve, 2 after
   if (b->plan.kind == YS_PCG_PERSISTENT) b->launches += 12 + (b->geom_n ? 1 : 0);
   else b->launches += 13 + (b->geom_n ? 1 : 0) + 3LL * G.h_it + G.h_it / m;
-  ys_status ret = YS_OK;
-  for (int c = 0; c < b->ncloth; ++c) {
-    if (pc[c].status & 3) ret = YS_ERR_NONFINITE;
-    else if ((pc[c].status & 4) && ret == YS_OK) ret = YS_ERR_MAXITER;
-    if (stats) {
-      stats[c].ok = (pc[c].status & 3) == 0;
-      stats[c].cg_iterations = pc[c].iters;
-      stats[c].cg_error = pc[c].bb > 0 ? std::sqrt(pc[c].rr / pc[c].bb) : 0.0;
-      stats[c].hit_maxiter = (pc[c].status & 4) ? 1 : 0;
-    }
-  }
-  b->assembled = false;
-  return ret;
+  return step_result(b, pc, stats);
 }
 
 // The schedule tuner: every candidate (whole-step graph or launch by launch;
@@ -1780,7 +1905,7 @@ ys_status learn_ensure(ys_batch* b) {
   A(&g.grad, ys::kGParams);
   A(&g.lpart, 2 * (size_t)g.nlblk + 3);
   A(&g.err, 1);
-  A(&L.y, 5 * (size_t)nt);
+  A(&L.rf, 5 * (size_t)nt);
   A(&L.z, 5 * (size_t)nt);
   if (st != YS_OK) return st;
   YS_CUDA(cudaMemsetAsync(g.err, 0, sizeof(int), b->stream));
@@ -1790,6 +1915,12 @@ ys_status learn_ensure(ys_batch* b) {
   YS_CUDA(cudaGetLastError());
   L.ready = true;
   return YS_OK;
+}
+
+// the learned PCG's buffers: G (BF16), the FP32 residual, z
+ys::LpcgExtra learned_extra(ys_batch* b) {
+  const ys_batch::Learn& L = b->learn;
+  return ys::LpcgExtra{L.g.Gh, L.rf, L.z};
 }
 
 // features, network, G blocks for the assembled system
@@ -1831,11 +1962,11 @@ ys_status solve_learned(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* 
   // the learned solve converges in a few iterations: poll every 4 unless told
   const int every = (opts && opts->check_every > 0) ? opts->check_every : 4;
   const int cap = override_max >= 0 ? override_max : b->max_maxiter;
-  const ys::LpcgExtra lx{L.g.Gh, L.g.pat, L.g.upat, L.y, L.z};
+  const ys::LpcgExtra lx = learned_extra(b);
   b->run(YS_PROF_MISC, 1, [&] {
     k_reset_pc<<<(b->ncloth + 127) / 128, 128, 0, s>>>(b->so.pc, b->maxiter_dev, b->ncloth, override_max);
   });
-  b->run(YS_PROF_PCG_SETUP, 4, [&] { ys::lpcg_setup(v, b->blk, b->so, lx, s); });
+  b->run(YS_PROF_PCG_SETUP, 3, [&] { ys::lpcg_setup(v, b->blk, b->so, lx, s); });
   YS_CUDA(cudaGetLastError());
   int it = 0;
   while (it < cap) {
@@ -1843,8 +1974,8 @@ ys_status solve_learned(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* 
     for (int q = 0; q < n; ++q, ++it) {
       const int par = it & 1;
       b->run(YS_PROF_SPMV, 1, [&] { ys::launch_pcg_spmv(v, b->blk, b->so, s); });
-      b->run(YS_PROF_AXPY, 1, [&] { ys::lpcg_axpy(v, b->blk, b->so, par, s); });
-      b->run(YS_PROF_PREC, 2, [&] { ys::lpcg_precondition(v, b->blk, b->so, lx, s); });
+      b->run(YS_PROF_AXPY, 1, [&] { ys::lpcg_axpy(v, b->blk, b->so, lx, par, s); });
+      b->run(YS_PROF_PREC, 1, [&] { ys::lpcg_precondition(v, b->blk, b->so, lx, s); });
       b->run(YS_PROF_DIR, 1, [&] { ys::lpcg_dir(v, b->blk, b->so, lx, par, it, s); });
     }
     b->run(YS_PROF_MISC, 1, [&] { ys::launch_count_active(v, b->so, s); });
@@ -1883,6 +2014,51 @@ ys_status solve_learned(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* 
     }
   }
   return ret;
+}
+
+// the learned-preconditioner step as a graph: assembly, [the network and G,]
+// the learned PCG's set-up, a conditional while node over m iterations (SpMV,
+// residual update, z = G^T G r, direction) and the condition,
+// then the verdict (hold the update back if the solve must be redone by
+// Jacobi-PCG) and the solution check and Cloth::update, which honour it
+ys_status graph_build_learned(ys_batch* b, int m, int cap, int override_max, int with_net) {
+  ys_batch::Graph& G = b->graph;
+  ys_batch::Learn& L = b->learn;
+  ys_status st = graph_prepare(b);
+  if (st != YS_OK) return st;
+  if (with_net) ys::gnn_forward_attrs();  // function attributes are set outside the capture
+  ys::Solver so = b->so;
+  so.it_base = G.it_base;
+  ys::Solver so_post = b->so;
+  so_post.hold = G.hold;
+  const ys::View& v = b->v;
+  const ys::LpcgExtra lx = learned_extra(b);
+  return build_loop_graph(
+      b,
+      [&](cudaStream_t c) {
+        capture_assembly(b, c, override_max);
+        if (with_net) {
+          ys::gnn_prepare(v, L.g, c);
+          ys::gnn_forward(L.net->net, L.g, c);
+          ys::gnn_make_g(L.g, false, c);
+        }
+        ys::lpcg_setup(v, b->blk, so, lx, c);
+        ys::launch_graph_loop_begin(so, c);
+      },
+      [&](cudaStream_t c, cudaGraphConditionalHandle h) {
+        for (int j = 0; j < m; ++j) {
+          ys::launch_pcg_spmv(v, b->blk, so, c);
+          ys::lpcg_axpy(v, b->blk, so, lx, j & 1, c);
+          ys::lpcg_precondition(v, b->blk, so, lx, c);
+          ys::lpcg_dir(v, b->blk, so, lx, j & 1, j, c);
+        }
+        ys::launch_graph_loop_tail(so, b->ncloth, m, cap, h, c);
+      },
+      [&](cudaStream_t c) {
+        ys::launch_learned_verdict(so, b->ncloth, L.g.err, override_max >= 0 ? 1 : 0, G.hold, c);
+        ys::launch_update(v, b->blk, so_post, c);
+      },
+      &G.lmain[with_net], &G.lexec[with_net]);
 }
 
 uint64_t splitmix(uint64_t& x) {

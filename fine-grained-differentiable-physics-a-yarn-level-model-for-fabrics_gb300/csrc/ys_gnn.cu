@@ -195,81 +195,98 @@ __device__ __forceinline__ float frob(const float M[5][5]) {
 // kept for the prior; features: E of left and down (50), x part of E of the
 // four other lower blocks (36)); q >= 6 the norm of the scaled coupling to
 // the upper neighbour right, up, right-up, left-up, right-2, up-2 (6); q = 0
-// also writes the flags (5) and the zero padding
-__global__ void k_gnn_feat(View v, GnnBufs g) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// also writes the flags (5) and the zero padding. A block covers kFeatNodes
+// nodes x 12 couplings and assembles their feature rows in shared memory, so
+// the rows leave in whole 16-byte chunks.
+constexpr int kFeatNodes = 32;
+constexpr int kFeatRow = kGIn + 8;  // padded shared row (BF16 elements), 16-byte multiple
+
+__global__ void __launch_bounds__(12 * kFeatNodes) k_gnn_feat(View v, GnnBufs g) {
+  __shared__ __align__(16) bf16 fs[kFeatNodes][kFeatRow];
   const int nt = v.ntot;
-  if (t >= 12LL * nt) return;
-  const int q = (int)(t / nt), n = (int)(t - (int64_t)q * nt);
-  float Li[5][5], Lj[5][5], Bk[5][5], T[5][5], E[5][5];
-  bf16* f = g.f + (int64_t)n * kGIn;
-  const ClothParams& P = v.cp[v.node_cloth[n]];
-  const int u = v.node_u[n], w = v.node_v[n];
-  if (q < 6) {
-    const int b = q + 1;  // lower offset (gpat_du, gpat_dv)(b), whether or not G uses it
-    const int ub = u + gpat_du(b), vb = w + gpat_dv(b);
-    const int j = (ub >= 0 && ub < P.W && vb >= 0 && vb < P.H) ? n + gpat_du(b) + gpat_dv(b) * P.W : -1;
-    if (j >= 0) {
-      load_linv(g.linv, nt, n, Li);
-      pat_block(v, n, b, Bk);
-      load_linv(g.linv, nt, j, Lj);
-      mul_ab(Li, Bk, T);
-      mul_abt(T, Lj, E);
-    } else {
+  const int q = threadIdx.x / kFeatNodes, ln = threadIdx.x - q * kFeatNodes;
+  const int n0 = blockIdx.x * kFeatNodes;
+  const int n = n0 + ln;
+  const int cnt = min(kFeatNodes, nt - n0);
+  bf16* f = fs[ln];
+  if (ln < cnt) {
+    float Li[5][5], Lj[5][5], Bk[5][5], T[5][5], E[5][5];
+    const ClothParams& P = v.cp[v.node_cloth[n]];
+    const int u = v.node_u[n], w = v.node_v[n];
+    if (q < 6) {
+      const int b = q + 1;  // lower offset (gpat_du, gpat_dv)(b), whether or not G uses it
+      const int ub = u + gpat_du(b), vb = w + gpat_dv(b);
+      const int j = (ub >= 0 && ub < P.W && vb >= 0 && vb < P.H) ? n + gpat_du(b) + gpat_dv(b) * P.W : -1;
+      if (j >= 0) {
+        load_linv(g.linv, nt, n, Li);
+        pat_block(v, n, b, Bk);
+        load_linv(g.linv, nt, j, Lj);
+        mul_ab(Li, Bk, T);
+        mul_abt(T, Lj, E);
+      } else {
+#pragma unroll
+        for (int r = 0; r < 5; ++r)
+#pragma unroll
+          for (int c = 0; c < 5; ++c) E[r][c] = 0.f;
+      }
 #pragma unroll
       for (int r = 0; r < 5; ++r)
 #pragma unroll
-        for (int c = 0; c < 5; ++c) E[r][c] = 0.f;
-    }
+        for (int c = 0; c < 5; ++c) g.E[(int64_t)(25 * q + 5 * r + c) * nt + n] = E[r][c];
+      if (b <= 2) {
 #pragma unroll
-    for (int r = 0; r < 5; ++r)
+        for (int r = 0; r < 5; ++r)
 #pragma unroll
-      for (int c = 0; c < 5; ++c) g.E[(int64_t)(25 * q + 5 * r + c) * nt + n] = E[r][c];
-    if (b <= 2) {
+          for (int c = 0; c < 5; ++c) f[25 * q + 5 * r + c] = __float2bfloat16(E[r][c]);
+      } else {
 #pragma unroll
-      for (int r = 0; r < 5; ++r)
+        for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < 5; ++c) f[25 * q + 5 * r + c] = __float2bfloat16(E[r][c]);
+          for (int c = 0; c < 3; ++c) f[50 + 9 * (b - 3) + 3 * r + c] = __float2bfloat16(E[r][c]);
+      }
+      if (q == 0) {
+        const uint8_t fl = v.flags[n];
+        f[92] = __float2bfloat16(g.chol_ok[n] ? 0.f : 1.f);
+        f[93] = __float2bfloat16((fl & YS_INTERIOR) ? 1.f : 0.f);
+        f[94] = __float2bfloat16((fl & YS_FIXED) ? 1.f : 0.f);
+        f[95] = __float2bfloat16((u == 0 || u == P.W - 1) ? 1.f : 0.f);
+        f[96] = __float2bfloat16((w == 0 || w == P.H - 1) ? 1.f : 0.f);
+        for (int k = 97; k < kGIn; ++k) f[k] = __float2bfloat16(0.f);
+      }
     } else {
+      const int k = q - 6;
+      const int du = k == 0 ? 1 : k == 1 ? 0 : k == 2 ? 1 : k == 3 ? -1 : k == 4 ? 2 : 0;
+      const int dv = k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 1 : k == 3 ? 1 : k == 4 ? 0 : 2;
+      float nrm = 0.f;
+      if (u + du >= 0 && u + du < P.W && w + dv >= 0 && w + dv < P.H) {
+        const int j = n + du + dv * P.W;
+        load_linv(g.linv, nt, n, Li);
+        load_linv(g.linv, nt, j, Lj);
+        if (k < 2) {
+          nbr_block(v, n, k == 0 ? 1 : 3, Bk);
+        } else {
+          const int s = stencil_index(du, dv);
 #pragma unroll
-      for (int r = 0; r < 3; ++r)
+          for (int r = 0; r < 5; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) f[50 + 9 * (b - 3) + 3 * r + c] = __float2bfloat16(E[r][c]);
+            for (int c = 0; c < 5; ++c)
+              Bk[r][c] = (r < 3 && c < 3) ? (float)slot(v, YS_SLOT_LL + 9 * s + 3 * r + c, n) : 0.f;
+        }
+        mul_ab(Li, Bk, T);
+        mul_abt(T, Lj, E);
+        nrm = frob(E);
+      }
+      f[86 + k] = __float2bfloat16(nrm);
     }
-    if (q == 0) {
-      const uint8_t fl = v.flags[n];
-      f[92] = __float2bfloat16(g.chol_ok[n] ? 0.f : 1.f);
-      f[93] = __float2bfloat16((fl & YS_INTERIOR) ? 1.f : 0.f);
-      f[94] = __float2bfloat16((fl & YS_FIXED) ? 1.f : 0.f);
-      f[95] = __float2bfloat16((u == 0 || u == P.W - 1) ? 1.f : 0.f);
-      f[96] = __float2bfloat16((w == 0 || w == P.H - 1) ? 1.f : 0.f);
-      for (int k = 97; k < kGIn; ++k) f[k] = __float2bfloat16(0.f);
-    }
-    return;
   }
-  const int k = q - 6;
-  const int du = k == 0 ? 1 : k == 1 ? 0 : k == 2 ? 1 : k == 3 ? -1 : k == 4 ? 2 : 0;
-  const int dv = k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 1 : k == 3 ? 1 : k == 4 ? 0 : 2;
-  float nrm = 0.f;
-  if (u + du >= 0 && u + du < P.W && w + dv >= 0 && w + dv < P.H) {
-    const int j = n + du + dv * P.W;
-    load_linv(g.linv, nt, n, Li);
-    load_linv(g.linv, nt, j, Lj);
-    if (k < 2) {
-      nbr_block(v, n, k == 0 ? 1 : 3, Bk);
-    } else {
-      const int s = stencil_index(du, dv);
-#pragma unroll
-      for (int r = 0; r < 5; ++r)
-#pragma unroll
-        for (int c = 0; c < 5; ++c)
-          Bk[r][c] = (r < 3 && c < 3) ? (float)slot(v, YS_SLOT_LL + 9 * s + 3 * r + c, n) : 0.f;
-    }
-    mul_ab(Li, Bk, T);
-    mul_abt(T, Lj, E);
-    nrm = frob(E);
+  __syncthreads();
+  // rows of kGIn BF16 = kGIn / 8 chunks of 16 bytes
+  constexpr int kChunks = kGIn / 8;
+  for (int k = threadIdx.x; k < cnt * kChunks; k += blockDim.x) {
+    const int row = k / kChunks, ch = k - row * kChunks;
+    *reinterpret_cast<uint4*>(g.f + (int64_t)(n0 + row) * kGIn + 8 * ch) =
+        *reinterpret_cast<const uint4*>(&fs[row][8 * ch]);
   }
-  f[86 + k] = __float2bfloat16(nrm);
 }
 
 // ------------------------------------------------------------ tensor-core GEMM
@@ -539,16 +556,25 @@ struct PlainOp {
   }
 };
 
+// dynamic shared memory of a GEMM kernel: at least 56 KB keeps at most 4
+// CTAs (4 x 128 TMEM columns) on an SM
+template <class Op, int KCH>
+constexpr int gemm_smem() {
+  return KCH * (16384 + Op::NT * 128) + 64 > kGemmSmem ? KCH * (16384 + Op::NT * 128) + 64 : kGemmSmem;
+}
 template <class Op, int KCH = 1>
-void launch_gemm(const Op& op, int M, int ncol_tiles, int nchunk, int nsplit, int* err, cudaStream_t s) {
-  // at least 56 KB keeps at most 4 CTAs (4 x 128 TMEM columns) on an SM
-  constexpr int smem_need = KCH * (16384 + Op::NT * 128) + 64;
-  constexpr int smem = smem_need > kGemmSmem ? smem_need : kGemmSmem;
+void gemm_attr() {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_tc_gemm<Op, KCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_tc_gemm<Op, KCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, gemm_smem<Op, KCH>());
     attr = true;
   }
+}
+
+template <class Op, int KCH = 1>
+void launch_gemm(const Op& op, int M, int ncol_tiles, int nchunk, int nsplit, int* err, cudaStream_t s) {
+  constexpr int smem = gemm_smem<Op, KCH>();
+  gemm_attr<Op, KCH>();
   const int per = (nchunk + nsplit - 1) / nsplit;
   const int splits = (nchunk + per - 1) / per;
   dim3 grid((M + tc::kTileM - 1) / tc::kTileM, ncol_tiles, splits);
@@ -612,35 +638,10 @@ __global__ void __launch_bounds__(kNB, 8) k_gnn_g(GnnBufs g, int keep_n) {
 }
 
 // ------------------------------------------------- blocked applications
-// y_n = sum_b G_n,b x_pat(n,b);   x in [5][nt]. Every load is issued before
-// the arithmetic (absent sources read node n with a zero weight), so one
-// memory round trip serves all seven blocks.
+// G coefficients as FP32, from FP32 (training) or BF16 (the solve) storage
 __device__ __forceinline__ float coef(const float* g, int64_t i) { return g[i]; }
 __device__ __forceinline__ float coef(const bf16* g, int64_t i) { return __bfloat162float(g[i]); }
 
-template <class TG, class TX>
-__device__ __forceinline__ void apply_rows(const TG* Gk, const int* pat, int nt, const TX* x, int n, float y[5]) {
-  int src[kGBlocks];
-#pragma unroll
-  for (int b = 0; b < kGBlocks; ++b) src[b] = pat[8 * n + b];
-  float xs[kGBlocks][5];
-#pragma unroll
-  for (int b = 0; b < kGBlocks; ++b) {
-    const int j = src[b] >= 0 ? src[b] : n;
-    const float m = src[b] >= 0 ? 1.f : 0.f;
-#pragma unroll
-    for (int c = 0; c < 5; ++c) xs[b][c] = m * (float)x[(int64_t)c * nt + j];
-  }
-#pragma unroll
-  for (int r = 0; r < 5; ++r) {
-    float s = 0.f;
-#pragma unroll
-    for (int b = 0; b < kGBlocks; ++b)
-#pragma unroll
-      for (int c = 0; c < 5; ++c) s += coef(Gk, (int64_t)(25 * b + 5 * r + c) * nt + n) * xs[b][c];
-    y[r] = s;
-  }
-}
 // z_n = sum over the rows i = upat(n, b) of G_i,b^T x_i
 template <class TG, class TX>
 __device__ __forceinline__ void apply_cols(const TG* Gk, const int* upat, int nt, const TX* x, int n, float z[5]) {
@@ -687,51 +688,120 @@ __device__ __forceinline__ double cl_sum(const Blocks& b, const double* part, in
   return s;
 }
 
-// x = 0, r = b; partials |b|^2 (row 0) and |r|^2 (row 1)
-__global__ void __launch_bounds__(kBlock) k_lp_setup(View v, Blocks b, Solver so) {
+// alpha = r.z / p.q; x += alpha p; r -= alpha q (setup: x = 0, r = b); the
+// FP32 copy of r the preconditioner reads; partial |r|^2 (row 1; setup also
+// |b|^2, row 0)
+__global__ void __launch_bounds__(kBlock) k_lp_axpy(View v, Blocks b, Solver so, LpcgExtra lx, int parity,
+                                                     int setup) {
   __shared__ double sh[kBlock / 32];
+  __shared__ double alpha_sh;
   const int blk = blockIdx.x;
+  const int c = b.blk_cloth[blk];
+  if (!setup && !so.pc[c].active) return;
   const int n = b.blk_node0[blk] + threadIdx.x;
   const int nt = v.ntot;
-  double rr = 0.0;
-  if (threadIdx.x < b.blk_count[blk])
+  const bool own = threadIdx.x < b.blk_count[blk];
+  // the loads that do not need alpha go out before the cloth sum
+  double r[5], q[5], p[5];
+  if (own)
+#pragma unroll
     for (int k = 0; k < 5; ++k) {
-      const double r = ld(v.B, k, nt, n);
-      st(so.x, k, nt, n) = 0.0;
-      st(so.r, k, nt, n) = r;
-      rr += r * r;
+      r[k] = setup ? ld(v.B, k, nt, n) : ld(so.r, k, nt, n);
+      q[k] = setup ? 0.0 : ld(so.q, k, nt, n);
+      p[k] = setup ? 0.0 : ld(so.p, k, nt, n);
     }
-  const double s = blk_sum(rr, sh);
+  if (threadIdx.x == 0) alpha_sh = setup ? 0.0 : so.pc[c].rz[parity] / cl_sum(b, so.part, 0, c);
+  __syncthreads();
+  const double alpha = alpha_sh;
+  double rr = 0.0;
+  if (own)
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      if (setup) st(so.x, k, nt, n) = 0.0;
+      else st(so.x, k, nt, n) += alpha * p[k];
+      const double rn = setup ? r[k] : fma(-alpha, q[k], r[k]);
+      st(so.r, k, nt, n) = rn;
+      lx.rf[(int64_t)k * nt + n] = (float)rn;
+      rr += rn * rn;
+    }
+  const double s1 = blk_sum(rr, sh);
   if (threadIdx.x == 0) {
-    so.part[0 * b.nblk + blk] = s;
-    so.part[1 * b.nblk + blk] = s;
+    so.part[1 * b.nblk + blk] = s1;
+    if (setup) so.part[0 * b.nblk + blk] = s1;
   }
 }
 
-// y = G r for the nodes of active cloths
-__global__ void __launch_bounds__(kBlock) k_lp_g(View v, Blocks b, Solver so, LpcgExtra lx, int setup) {
-  const int blk = blockIdx.x;
-  const int c = b.blk_cloth[blk];
-  if (!setup && !so.pc[c].active) return;
-  if (threadIdx.x >= b.blk_count[blk]) return;
-  const int n = b.blk_node0[blk] + threadIdx.x;
-  float y[5];
-  apply_rows(lx.G, lx.pat, v.ntot, so.r, n, y);
-  for (int k = 0; k < 5; ++k) lx.y[(int64_t)k * v.ntot + n] = y[k];
-}
+// z = G^T G r (FP32 r, BF16 G, FP32 sums). The rows of G are self, left
+// (n - 1) and down (n - W), so node n's z sums G_i,b^T y_i over the rows
+// i = n, n + 1, n + W, with y_i = G_i,0 r(i) + G_i,1 r(i - 1) + G_i,2 r(i - W).
+// A block of nodes [n0, n0 + cnt) computes y of the rows [n0, n0 + cnt] and
+// [n0 + W, n0 + W + cnt) (one range when they touch) into shared memory, then
+// z of its own nodes: no grid-wide barrier between G and G^T. Partials r.z
+// (row 2) and z.q (row 3); setup: p = z and r.z only.
+constexpr int kLpY = 2 * kBlock + 1;  // staged rows of a block
+static_assert(kGBlocks == 3, "the staged rows follow the self / left / down pattern");
 
-// z = G^T y; partials r.z (row 2) and z.q (row 3); at setup also p = z
-__global__ void __launch_bounds__(kBlock) k_lp_gt(View v, Blocks b, Solver so, LpcgExtra lx, int setup) {
+__global__ void __launch_bounds__(kBlock, 8) k_lp_prec(View v, Blocks b, Solver so, LpcgExtra lx, int setup) {
   __shared__ double sh[kBlock / 32];
+  __shared__ float ys_[5][kLpY];
   const int blk = blockIdx.x;
   const int c = b.blk_cloth[blk];
   if (!setup && !so.pc[c].active) return;
   const int nt = v.ntot;
-  const int n = b.blk_node0[blk] + threadIdx.x;
+  const ClothParams& P = v.cp[c];
+  const int W = P.W, H = P.H, cs = P.node_off, ce = P.node_off + P.W * P.H;
+  const int n0 = b.blk_node0[blk], cnt = b.blk_count[blk];
+  // rows n and n + 1 of the block's nodes, then rows n + W: entry e of row i
+  // is i - n0, or i - (n0 + W) + cnt + 1 for the second range when it is apart
+  const bool yone = W <= cnt + 1;
+  const int yb1 = yone ? W : cnt + 1;
+  const int ytotal = yone ? cnt + W : 2 * cnt + 1;
+  const int yoff1 = n0 + W - yb1;
+  for (int e = threadIdx.x; e < ytotal; e += kBlock) {
+    const int i = e + (yone || e < yb1 ? n0 : yoff1);
+    float y[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    if (i < ce) {
+      const int u = (i - cs) % W;
+      const int src[3] = {i, u > 0 ? i - 1 : -1, i >= cs + W ? i - W : -1};
+      float xs[3][5];
+#pragma unroll
+      for (int bb = 0; bb < 3; ++bb) {
+        const int j = src[bb] >= 0 ? src[bb] : i;
+        const float m = src[bb] >= 0 ? 1.f : 0.f;
+#pragma unroll
+        for (int cc = 0; cc < 5; ++cc) xs[bb][cc] = m * lx.rf[(int64_t)cc * nt + j];
+      }
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        float acc = 0.f;
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+          for (int cc = 0; cc < 5; ++cc) acc += coef(lx.G, (int64_t)(25 * bb + 5 * r + cc) * nt + i) * xs[bb][cc];
+        y[r] = acc;
+      }
+    }
+#pragma unroll
+    for (int cc = 0; cc < 5; ++cc) ys_[cc][e] = y[cc];
+  }
+  __syncthreads();
+  const int n = n0 + threadIdx.x;
   double rz = 0.0, zq = 0.0;
-  if (threadIdx.x < b.blk_count[blk]) {
-    float z[5];
-    apply_cols(lx.G, lx.upat, nt, lx.y, n, z);
+  if (threadIdx.x < cnt) {
+    const int u = (n - cs) % W, w = (n - cs) / W;
+    const int row[3] = {n, u < W - 1 ? n + 1 : -1, w < H - 1 ? n + W : -1};
+    float z[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int bb = 0; bb < 3; ++bb) {
+      const int i = row[bb];
+      if (i < 0) continue;
+      const int ei = i - (bb == 2 ? yoff1 : n0);
+#pragma unroll
+      for (int cc = 0; cc < 5; ++cc)
+#pragma unroll
+        for (int r = 0; r < 5; ++r) z[cc] += coef(lx.G, (int64_t)(25 * bb + 5 * r + cc) * nt + i) * ys_[r][ei];
+    }
+#pragma unroll
     for (int k = 0; k < 5; ++k) {
       const double zk = (double)z[k];
       lx.z[(int64_t)k * nt + n] = zk;
@@ -740,10 +810,12 @@ __global__ void __launch_bounds__(kBlock) k_lp_gt(View v, Blocks b, Solver so, L
       else zq += zk * ld(so.q, k, nt, n);
     }
   }
-  const double s1 = blk_sum(rz, sh);
-  if (threadIdx.x == 0) so.part[2 * b.nblk + blk] = s1;
-  const double s2 = blk_sum(zq, sh);
-  if (threadIdx.x == 0) so.part[3 * b.nblk + blk] = s2;
+  const double s2 = blk_sum(rz, sh);
+  if (threadIdx.x == 0) so.part[2 * b.nblk + blk] = s2;
+  if (!setup) {
+    const double s3 = blk_sum(zq, sh);
+    if (threadIdx.x == 0) so.part[3 * b.nblk + blk] = s3;
+  }
 }
 
 __global__ void k_lp_start(Blocks b, Solver so, int ncloth) {
@@ -763,34 +835,12 @@ __global__ void k_lp_start(Blocks b, Solver so, int ncloth) {
   pc.active = (pc.status == 0 && bb != 0.0 && rr >= thr) ? 1 : 0;
 }
 
-// alpha = r.z / p.q; x += alpha p; r -= alpha q; partial |r|^2 (row 1)
-__global__ void __launch_bounds__(kBlock) k_lp_axpy(View v, Blocks b, Solver so, int parity) {
-  __shared__ double sh[kBlock / 32];
-  __shared__ double alpha_sh;
-  const int blk = blockIdx.x;
-  const int c = b.blk_cloth[blk];
-  if (!so.pc[c].active) return;
-  if (threadIdx.x == 0) alpha_sh = so.pc[c].rz[parity] / cl_sum(b, so.part, 0, c);
-  __syncthreads();
-  const double alpha = alpha_sh;
-  const int n = b.blk_node0[blk] + threadIdx.x;
-  const int nt = v.ntot;
-  double rr = 0.0;
-  if (threadIdx.x < b.blk_count[blk])
-    for (int k = 0; k < 5; ++k) {
-      st(so.x, k, nt, n) += alpha * ld(so.p, k, nt, n);
-      const double r = ld(so.r, k, nt, n) - alpha * ld(so.q, k, nt, n);
-      st(so.r, k, nt, n) = r;
-      rr += r * r;
-    }
-  const double s = blk_sum(rr, sh);
-  if (threadIdx.x == 0) so.part[1 * b.nblk + blk] = s;
-}
-
 // stop test |r|^2 < thr, else the flexible (Polak-Ribiere) direction update
 // beta = z_new . (r_new - r_old) / (z_old . r_old) = -alpha z_new . q / rz,
 // which stays a conjugate-gradient method when M^-1 is applied in FP32
-__global__ void __launch_bounds__(kBlock) k_lp_dir(View v, Blocks b, Solver so, LpcgExtra lx, int parity, int it) {
+// (it: the iteration, counted from *so.it_base in a graph body)
+__global__ void __launch_bounds__(kBlock) k_lp_dir(View v, Blocks b, Solver so, LpcgExtra lx, int parity,
+                                                    int it_local) {
   __shared__ int go_sh;
   __shared__ double beta_sh;
   const int blk = blockIdx.x;
@@ -798,6 +848,7 @@ __global__ void __launch_bounds__(kBlock) k_lp_dir(View v, Blocks b, Solver so, 
   PcgCloth& pc = so.pc[c];
   if (!pc.active) return;
   if (threadIdx.x == 0) {
+    const int it = so.it_base ? *so.it_base + it_local : it_local;
     const double rr = cl_sum(b, so.part, 1, c);
     const double rzn = cl_sum(b, so.part, 2, c);
     const double zq = cl_sum(b, so.part, 3, c);
@@ -1133,7 +1184,7 @@ void gnn_neighbours(const View& v, const GnnBufs& g, cudaStream_t s) { k_gnn_nbr
 
 void gnn_prepare(const View& v, const GnnBufs& g, cudaStream_t s) {
   k_gnn_linv<<<nblk(v.ntot), kNB, 0, s>>>(v, g.linv, g.chol_ok);
-  k_gnn_feat<<<(int)((12LL * v.ntot + kNB - 1) / kNB), kNB, 0, s>>>(v, g);
+  k_gnn_feat<<<(v.ntot + kFeatNodes - 1) / kFeatNodes, 12 * kFeatNodes, 0, s>>>(v, g);
 }
 
 void gnn_forward(const GnnNet& net, const GnnBufs& g, cudaStream_t s) {
@@ -1154,6 +1205,12 @@ void gnn_forward(const GnnNet& net, const GnnBufs& g, cudaStream_t s) {
                            nullptr, nullptr, g.o};
     launch_gemm(op, M, kGOut / 64, 1, 1, g.err, s);
   }
+}
+
+void gnn_forward_attrs() {
+  gemm_attr<FwdOp<64, kEpiEnc>, kGIn / 64>();
+  gemm_attr<FwdOp<64, kEpiLayer>, 2>();
+  gemm_attr<FwdOp<64, kEpiHead>, 1>();
 }
 
 void gnn_make_g(const GnnBufs& g, bool keep_n, cudaStream_t s) {
@@ -1210,19 +1267,19 @@ void gnn_adam(const GnnNet& net, const GnnBufs& g, float* m, float* vv, float lr
 }
 
 void lpcg_setup(const View& v, const Blocks& b, const Solver& so, const LpcgExtra& lx, cudaStream_t s) {
-  k_lp_setup<<<b.nblk, kBlock, 0, s>>>(v, b, so);
-  k_lp_g<<<b.nblk, kBlock, 0, s>>>(v, b, so, lx, 1);
-  k_lp_gt<<<b.nblk, kBlock, 0, s>>>(v, b, so, lx, 1);
+  k_lp_axpy<<<b.nblk, kBlock, 0, s>>>(v, b, so, lx, 0, 1);
+  k_lp_prec<<<b.nblk, kBlock, 0, s>>>(v, b, so, lx, 1);
   k_lp_start<<<(v.ncloth + 127) / 128, 128, 0, s>>>(b, so, v.ncloth);
 }
 
-void lpcg_axpy(const View& v, const Blocks& b, const Solver& so, int parity, cudaStream_t s) {
-  k_lp_axpy<<<b.nblk, kBlock, 0, s>>>(v, b, so, parity);
+void lpcg_axpy(const View& v, const Blocks& b, const Solver& so, const LpcgExtra& lx, int parity, cudaStream_t s) {
+  k_lp_axpy<<<b.nblk, kBlock, 0, s>>>(v, b, so, lx, parity, 0);
 }
+
 void lpcg_precondition(const View& v, const Blocks& b, const Solver& so, const LpcgExtra& lx, cudaStream_t s) {
-  k_lp_g<<<b.nblk, kBlock, 0, s>>>(v, b, so, lx, 0);
-  k_lp_gt<<<b.nblk, kBlock, 0, s>>>(v, b, so, lx, 0);
+  k_lp_prec<<<b.nblk, kBlock, 0, s>>>(v, b, so, lx, 0);
 }
+
 void lpcg_dir(const View& v, const Blocks& b, const Solver& so, const LpcgExtra& lx, int parity, int it,
               cudaStream_t s) {
   k_lp_dir<<<b.nblk, kBlock, 0, s>>>(v, b, so, lx, parity, it);

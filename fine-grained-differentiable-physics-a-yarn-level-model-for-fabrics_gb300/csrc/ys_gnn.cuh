@@ -99,9 +99,7 @@ struct GnnBufs {  // device arrays sized for ntot nodes
 // learned-preconditioner PCG state lives in Solver; these hold its extras
 struct LpcgExtra {
   const __nv_bfloat16* G;  // [75][ntot]
-  const int* pat;   // [ntot][8]
-  const int* upat;  // [ntot][8]
-  float* y;         // [5][ntot] G r
+  float* rf;        // [5][ntot] the residual in FP32, as the preconditioner reads it
   double* z;        // [5][ntot] G^T G r
 };
 
@@ -109,6 +107,9 @@ struct LpcgExtra {
 void gnn_neighbours(const View& v, const GnnBufs& g, cudaStream_t s);
 void gnn_prepare(const View& v, const GnnBufs& g, cudaStream_t s);
 void gnn_forward(const GnnNet& net, const GnnBufs& g, cudaStream_t s);
+// sets the forward GEMMs' function attributes (done by gnn_forward's first
+// call; call it before capturing gnn_forward into a graph)
+void gnn_forward_attrs();
 // G (and, for training, the blocks of N) from the network outputs
 void gnn_make_g(const GnnBufs& g, bool keep_n, cudaStream_t s);
 void gnn_refresh_bf16(const GnnNet& net, cudaStream_t s);
@@ -118,9 +119,13 @@ void gnn_loss_grad(const View& v, const GnnNet& net, const GnnBufs& g, uint64_t 
                    cudaStream_t s);
 void gnn_adam(const GnnNet& net, const GnnBufs& g, float* m, float* vv, float lr, int step, cudaStream_t s);
 
+// x = 0, r = b, z = G^T G r, p = z and the per-cloth start of the iteration
 void lpcg_setup(const View& v, const Blocks& b, const Solver& so, const LpcgExtra& lx, cudaStream_t s);
-void lpcg_axpy(const View& v, const Blocks& b, const Solver& so, int parity, cudaStream_t s);
+// after the SpMV q = A p of iteration `parity`: x, r (and its FP32 copy)
+void lpcg_axpy(const View& v, const Blocks& b, const Solver& so, const LpcgExtra& lx, int parity, cudaStream_t s);
+// z = G^T G r with the partial dot products the direction update needs
 void lpcg_precondition(const View& v, const Blocks& b, const Solver& so, const LpcgExtra& lx, cudaStream_t s);
+// the stop test and p = z + beta p (it: the iteration, from *so.it_base in a graph body)
 void lpcg_dir(const View& v, const Blocks& b, const Solver& so, const LpcgExtra& lx, int parity, int it,
               cudaStream_t s);
 // C [M][N] = A [M][K] B [N][K]^T (BF16 in, FP32 out; N = 64 k or 128, K = 64 k)

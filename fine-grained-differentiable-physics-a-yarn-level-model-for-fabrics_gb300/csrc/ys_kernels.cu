@@ -206,6 +206,7 @@ __global__ void k_count_active(Solver so, int ncloth) {
 
 // flags a cloth whose solution holds a non-finite value (src/TrainHelper.cpp:41-48)
 __global__ void __launch_bounds__(kBlock) k_check_solution(View v, Blocks b, Solver so) {
+  if (so.hold && *so.hold) return;
   const int blk = blockIdx.x;
   const int c = b.blk_cloth[blk];
   const int n = b.blk_node0[blk] + threadIdx.x;
@@ -217,12 +218,23 @@ __global__ void __launch_bounds__(kBlock) k_check_solution(View v, Blocks b, Sol
 
 // Cloth::update for every cloth whose step succeeded
 __global__ void __launch_bounds__(kBlock) k_update(View v, Blocks b, Solver so) {
+  if (so.hold && *so.hold) return;
   const int blk = blockIdx.x;
   const int c = b.blk_cloth[blk];
   const int n = b.blk_node0[blk] + threadIdx.x;
   if (threadIdx.x >= b.blk_count[blk]) return;
   if (so.pc[c].status & 3) return;  // SimStep returns false and leaves the cloth as it was
   update_node(v, so.x, n);
+}
+
+__global__ void k_learned_verdict(Solver so, int ncloth, const int* err, int caller_cap, int* hold) {
+  int redo = *err != 0;
+  for (int c = threadIdx.x; c < ncloth; c += blockDim.x) {
+    const int st = so.pc[c].status;
+    if (!(st & 1) && ((st & 8) || ((st & 4) && !caller_cap))) redo = 1;
+  }
+  redo = __syncthreads_or(redo);
+  if (threadIdx.x == 0) *hold = redo;
 }
 
 __global__ void k_spmv_plain(View v, const double* x, double* y) {
@@ -304,6 +316,10 @@ void launch_check_solution(const View& v, const Blocks& b, const Solver& so, cud
 void launch_update(const View& v, const Blocks& b, const Solver& so, cudaStream_t s) {
   k_check_solution<<<b.nblk, kBlock, 0, s>>>(v, b, so);
   k_update<<<b.nblk, kBlock, 0, s>>>(v, b, so);
+}
+void launch_learned_verdict(const Solver& so, int ncloth, const int* err, int caller_cap, int* hold,
+                            cudaStream_t s) {
+  k_learned_verdict<<<1, 256, 0, s>>>(so, ncloth, err, caller_cap, hold);
 }
 void launch_spmv(const View& v, const double* x, double* y, cudaStream_t s) {
   k_spmv_plain<<<nblocks(v.ntot), kBlock, 0, s>>>(v, x, y);

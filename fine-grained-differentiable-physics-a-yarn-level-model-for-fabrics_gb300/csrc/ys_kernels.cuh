@@ -42,6 +42,8 @@ struct Solver {
   double tol;
   int trans;      // 1: solve A^T x = b (the reference-mode tangent solves)
   int* it_base;   // graph mode: iterations completed before this graph body (device), else null
+  const int* hold;  // graph mode: when *hold != 0 the solution check and the update leave every cloth
+                    // as it was (the learned solve handed the step to Jacobi-PCG), else null
 };
 
 constexpr int kBlock = 128;
@@ -68,6 +70,11 @@ void launch_graph_loop_begin(const Solver& so, cudaStream_t s);
 void launch_graph_loop_tail(const Solver& so, int ncloth, int m, int cap, cudaGraphConditionalHandle h,
                             cudaStream_t s);
 void launch_update(const View& v, const Blocks& b, const Solver& so, cudaStream_t s);
+// graph mode of the learned solve: *so.hold = 1 if the solve must be redone by
+// Jacobi-PCG (an expired tensor-core wait in *err, a breakdown, or the default
+// iteration cap when the caller set none; cloths with a non-finite system excepted)
+void launch_learned_verdict(const Solver& so, int ncloth, const int* err, int caller_cap, int* hold,
+                            cudaStream_t s);
 void launch_spmv(const View& v, const double* x, double* y, cudaStream_t s);
 
 // ---- persistent per-cloth PCG (ys_pcg_cluster.cu): one cluster of csize

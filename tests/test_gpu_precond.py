@@ -176,6 +176,53 @@ def test_broken_network_falls_back_to_jacobi():
     net.close()
 
 
+def test_graphed_learned_step_equals_launch_by_launch():
+    """The learned-preconditioner step as one CUDA graph launch per step (the
+    network evaluated every third solve, in the graph that holds it) gives the
+    states and iteration counts of the launch-by-launch learned step, bit for
+    bit, across a change of h."""
+    net = trained_net()
+    specs = ys.training_specs(np.random.default_rng(11), 6, 8, 30)
+    a, c = ys.ClothBatch(specs), ys.ClothBatch(specs)
+    for x in (a, c):
+        x.set_preconditioner("learned", net)
+        x.precond_refresh(3)
+    c.use_graphs(True)
+    for k in range(7):
+        h = 1e-3 if k != 4 else 5e-4
+        sa, sc = a.step(h, tol=1e-10), c.step(h, tol=1e-10)
+        assert all(s["ok"] for s in sc)
+        assert [s["cg_iterations"] for s in sa] == [s["cg_iterations"] for s in sc]
+    sa, sc = a.get_state(), c.get_state()
+    for k in sa:
+        assert np.array_equal(sa[k], sc[k]), k
+    assert a.precond_info() == c.precond_info() == dict(learned_solves=7, fallbacks=0)
+    a.close()
+    c.close()
+    net.close()
+
+
+def test_graphed_learned_step_with_a_broken_network_falls_back_to_jacobi():
+    """In the graph, a network of NaN weights breaks the learned solve down; the
+    graph's verdict kernel holds the update back and the step is solved again by
+    Jacobi-PCG: states equal the Jacobi step's bit for bit."""
+    net = ys.LearnedPreconditioner(params=np.full(ys.precond.param_count(), np.nan, np.float32))
+    specs = ys.training_specs(np.random.default_rng(5), 3, 6, 12)
+    ref, b = ys.ClothBatch(specs), ys.ClothBatch(specs)
+    b.set_preconditioner("learned", net)
+    b.use_graphs(True)
+    for _ in range(3):
+        assert all(s["ok"] for s in ref.step(1e-3, tol=1e-10))
+        assert all(s["ok"] for s in b.step(1e-3, tol=1e-10))
+    assert b.precond_info()["fallbacks"] == 3
+    x, y = ref.get_state(), b.get_state()
+    for k in x:
+        assert np.array_equal(x[k], y[k]), k
+    b.close()
+    ref.close()
+    net.close()
+
+
 def test_training_lowers_the_kaporin_number_on_held_out_systems():
     """Training (without model selection) lowers its objective, the Kaporin
     condition number of G A G^T, on systems it never saw (same systems, same
