@@ -25,6 +25,7 @@ EXPORTED = [
     "ys_collider_create", "ys_collider_destroy", "ys_collider_set_positions", "ys_collider_find_pairs",
     "ys_collider_get_pairs", "ys_collider_find_impacts", "ys_collider_get_impacts", "ys_use_graphs",
     "ys_step_graphed", "ys_autotune", "ys_set_pcg_schedule", "ys_autotune_results", "ys_set_producer_threads", "ys_gnn_param_count", "ys_gnn_create", "ys_gnn_destroy", "ys_gnn_get_params",
+    "ys_gnn_dims", "ys_gnn_set_objective",
     "ys_gnn_set_params", "ys_gnn_train_step", "ys_gnn_loss_grad", "ys_set_preconditioner", "ys_precond_info",
     "ys_get_system_slots", "ys_tc_gemm_bf16", "ys_precond_refresh", "ys_get_normals", "ys_collider_respond",
     "ys_collider_response_impacts", "ys_collider_respond_backward", "ys_step_tangent_ext",
@@ -146,6 +147,9 @@ def load(build_if_missing: bool = True):
     L.ys_gnn_param_count.argtypes = []
     L.ys_gnn_param_count.restype = ctypes.c_int32
     L.ys_gnn_create.argtypes = [ctypes.c_int32, ctypes.c_uint64, ctypes.POINTER(vp)]
+    L.ys_gnn_dims.argtypes = [ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+    L.ys_gnn_dims.restype = None
+    L.ys_gnn_set_objective.argtypes = [vp, ctypes.c_int32]
     L.ys_gnn_destroy.argtypes = [vp]
     L.ys_gnn_destroy.restype = None
     L.ys_gnn_get_params.argtypes = [vp, vp]
@@ -171,7 +175,7 @@ def load(build_if_missing: bool = True):
     for name in EXPORTED:
         if name not in ("ys_batch_destroy", "ys_last_error", "ys_cloth_node_offset", "ys_cloth_dim",
                         "ys_tangent_count", "ys_collider_destroy", "ys_gnn_destroy", "ys_gnn_param_count",
-                        "ys_adjoint_destroy"):
+                        "ys_adjoint_destroy", "ys_gnn_dims"):
             getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L

@@ -677,6 +677,9 @@ ys_status solve_impl(ys_batch* b, const ys::View& v, const ys_solve_opts* opts, 
 }
 
 ys_status solve_learned(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* stats);
+// the learned solve converges in about five iterations: it checks for
+// convergence every 6 unless told otherwise (even, as the graph body needs)
+constexpr int kLearnedCheckEvery = 6;
 
 }  // namespace
 
@@ -1666,7 +1669,7 @@ ys_status ys_step_graphed(ys_batch* b, double h, const double* ext_force, int32_
   // iterations per trip through the loop body; the learned solve converges in
   // a few, so its body is short unless the call asks otherwise
   const bool learned = b->learn.kind == YS_PREC_LEARNED;
-  int m = (opts && opts->check_every > 0) ? opts->check_every : learned ? 4 : b->check_every;
+  int m = (opts && opts->check_every > 0) ? opts->check_every : learned ? kLearnedCheckEvery : b->check_every;
   m += m & 1;
   const int cap = override_max >= 0 ? override_max : b->max_maxiter;
   b->so.tol = tol;
@@ -1853,6 +1856,7 @@ struct ys_gnn {
   float* m = nullptr;  // Adam moments
   float* vv = nullptr;
   int step = 0;
+  int objective = YS_GNN_FSAI;
   std::vector<void*> allocs;
   template <class T>
   cudaError_t alloc(T** p, size_t count) {
@@ -1896,6 +1900,7 @@ ys_status learn_ensure(ys_batch* b) {
   A(&g.G, (size_t)ys::kGUsed * nt);
   A(&g.Gh, (size_t)ys::kGUsed * nt);
   A(&g.Gn, (size_t)ys::kGUsed * nt);
+  A(&g.Nt, (size_t)ys::kGUsed * nt);
   A(&g.vec, 4 * 5 * (size_t)nt);
   A(&g.dob, (size_t)ys::kGOut * nt);
   A(&g.dh, (size_t)ys::kGHid * nt);
@@ -1959,8 +1964,7 @@ ys_status solve_learned(ys_batch* b, const ys_solve_opts* opts, ys_cloth_stats* 
   const ys::View& v = b->v;
   b->so.tol = (opts && opts->tol > 0) ? opts->tol : DBL_EPSILON;
   const int override_max = (opts && opts->maxiter >= 0) ? opts->maxiter : -1;
-  // the learned solve converges in a few iterations: poll every 4 unless told
-  const int every = (opts && opts->check_every > 0) ? opts->check_every : 4;
+  const int every = (opts && opts->check_every > 0) ? opts->check_every : kLearnedCheckEvery;
   const int cap = override_max >= 0 ? override_max : b->max_maxiter;
   const ys::LpcgExtra lx = learned_extra(b);
   b->run(YS_PROF_MISC, 1, [&] {
@@ -2074,6 +2078,17 @@ extern "C" {
 
 int32_t ys_gnn_param_count(void) { return ys::kGParams; }
 
+void ys_gnn_dims(int32_t* outputs, int32_t* blocks) {
+  if (outputs) *outputs = ys::kGOut;
+  if (blocks) *blocks = ys::kGBlocks;
+}
+
+ys_status ys_gnn_set_objective(ys_gnn* g, int32_t objective) {
+  if (!g || (objective != YS_GNN_KAPORIN && objective != YS_GNN_FSAI)) return fail(YS_ERR_ARG, "bad argument");
+  g->objective = objective;
+  return YS_OK;
+}
+
 ys_status ys_gnn_create(int32_t device, uint64_t seed, ys_gnn** out) {
   if (!out) return fail(YS_ERR_ARG, "null output");
   YS_CUDA(cudaSetDevice(device));
@@ -2168,7 +2183,7 @@ ys_status ys_gnn_loss_grad(ys_gnn* g, ys_batch* b, const float* probes, uint64_t
     YS_CUDA(cudaMemcpyAsync(G.vec, t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice, b->stream));
     YS_CUDA(cudaStreamSynchronize(b->stream));
   }
-  ys::gnn_loss_grad(b->v, g->net, G, seed, probes != nullptr, b->stream);
+  ys::gnn_loss_grad(b->v, g->net, G, seed, probes != nullptr, g->objective, b->stream);
   YS_CUDA(cudaGetLastError());
   int err = 0;
   if ((st = read_err(b, &err)) != YS_OK) return st;
@@ -2203,7 +2218,7 @@ ys_status ys_gnn_train_step(ys_gnn* g, ys_batch* b, uint64_t seed, float lr, dou
   if ((st = learn_infer(b, g, true)) != YS_OK) return st;
   b->learn.have_g = false;
   ys::GnnBufs& G = b->learn.g;
-  ys::gnn_loss_grad(b->v, g->net, G, seed, false, b->stream);
+  ys::gnn_loss_grad(b->v, g->net, G, seed, false, g->objective, b->stream);
   g->step += 1;
   ys::gnn_adam(g->net, G, g->m, g->vv, lr, g->step, b->stream);
   YS_CUDA(cudaGetLastError());

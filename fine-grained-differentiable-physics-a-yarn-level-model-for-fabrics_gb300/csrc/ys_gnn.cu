@@ -731,17 +731,19 @@ __global__ void __launch_bounds__(kBlock) k_lp_axpy(View v, Blocks b, Solver so,
   }
 }
 
-// z = G^T G r (FP32 r, BF16 G, FP32 sums). The rows of G are self, left
-// (n - 1) and down (n - W), so node n's z sums G_i,b^T y_i over the rows
-// i = n, n + 1, n + W, with y_i = G_i,0 r(i) + G_i,1 r(i - 1) + G_i,2 r(i - W).
-// A block of nodes [n0, n0 + cnt) computes y of the rows [n0, n0 + cnt] and
-// [n0 + W, n0 + W + cnt) (one range when they touch) into shared memory, then
-// z of its own nodes: no grid-wide barrier between G and G^T. Partials r.z
-// (row 2) and z.q (row 3); setup: p = z and r.z only.
-constexpr int kLpY = 2 * kBlock + 1;  // staged rows of a block
-static_assert(kGBlocks == 3, "the staged rows follow the self / left / down pattern");
+// z = G^T G r (FP32 r, BF16 G, FP32 sums). Block b of row i couples node
+// i + (du_b, dv_b) (the lower offsets gpat_du / gpat_dv, dv_b in {0, -1, -2}),
+// so node n's z sums G_i,b^T y_i over the rows i = n - (du_b, dv_b), with
+// y_i = sum_b G_i,b r(i + (du_b, dv_b)). A block of nodes [n0, n0 + cnt)
+// computes y of the rows it needs into shared memory -- by -dv_b the windows
+// [n0, n0 + cnt + 2), [n0 + W - 1, n0 + W + cnt + 1) and [n0 + 2W, n0 + 2W +
+// cnt), one range when they touch -- then z of its own nodes: no grid-wide
+// barrier between G and G^T. Partials r.z (row 2) and z.q (row 3); setup:
+// p = z and r.z only.
+constexpr int kLpY = 3 * kBlock + 4;  // staged rows of a block
+static_assert(kGBlocks <= 7, "the staged rows cover lower offsets with dv in {0, -1, -2}, du in [-2, 1]");
 
-__global__ void __launch_bounds__(kBlock, 8) k_lp_prec(View v, Blocks b, Solver so, LpcgExtra lx, int setup) {
+__global__ void __launch_bounds__(kBlock, 6) k_lp_prec(View v, Blocks b, Solver so, LpcgExtra lx, int setup) {
   __shared__ double sh[kBlock / 32];
   __shared__ float ys_[5][kLpY];
   const int blk = blockIdx.x;
@@ -751,23 +753,22 @@ __global__ void __launch_bounds__(kBlock, 8) k_lp_prec(View v, Blocks b, Solver 
   const ClothParams& P = v.cp[c];
   const int W = P.W, H = P.H, cs = P.node_off, ce = P.node_off + P.W * P.H;
   const int n0 = b.blk_node0[blk], cnt = b.blk_count[blk];
-  // rows n and n + 1 of the block's nodes, then rows n + W: entry e of row i
-  // is i - n0, or i - (n0 + W) + cnt + 1 for the second range when it is apart
+  // entry of row i in window w is i - yoff[w]
   const bool yone = W <= cnt + 1;
-  const int yb1 = yone ? W : cnt + 1;
-  const int ytotal = yone ? cnt + W : 2 * cnt + 1;
-  const int yoff1 = n0 + W - yb1;
+  const int ytotal = yone ? cnt + 2 * W : 3 * cnt + 4;
+  const int yoff0 = n0, yoff1 = yone ? n0 : n0 + W - 1 - (cnt + 2), yoff2 = yone ? n0 : n0 + 2 * W - (2 * cnt + 4);
   for (int e = threadIdx.x; e < ytotal; e += kBlock) {
-    const int i = e + (yone || e < yb1 ? n0 : yoff1);
+    const int i = e + (yone || e < cnt + 2 ? yoff0 : e < 2 * cnt + 4 ? yoff1 : yoff2);
     float y[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     if (i < ce) {
-      const int u = (i - cs) % W;
-      const int src[3] = {i, u > 0 ? i - 1 : -1, i >= cs + W ? i - W : -1};
-      float xs[3][5];
+      const int u = (i - cs) % W, w = (i - cs) / W;
+      float xs[kGBlocks][5];
 #pragma unroll
-      for (int bb = 0; bb < 3; ++bb) {
-        const int j = src[bb] >= 0 ? src[bb] : i;
-        const float m = src[bb] >= 0 ? 1.f : 0.f;
+      for (int bb = 0; bb < kGBlocks; ++bb) {
+        const int du = gpat_du(bb), dv = gpat_dv(bb);
+        const bool in = u + du >= 0 && u + du < W && w + dv >= 0;
+        const int j = in ? i + du + dv * W : i;
+        const float m = in ? 1.f : 0.f;
 #pragma unroll
         for (int cc = 0; cc < 5; ++cc) xs[bb][cc] = m * lx.rf[(int64_t)cc * nt + j];
       }
@@ -775,7 +776,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_lp_prec(View v, Blocks b, Solver 
       for (int r = 0; r < 5; ++r) {
         float acc = 0.f;
 #pragma unroll
-        for (int bb = 0; bb < 3; ++bb)
+        for (int bb = 0; bb < kGBlocks; ++bb)
 #pragma unroll
           for (int cc = 0; cc < 5; ++cc) acc += coef(lx.G, (int64_t)(25 * bb + 5 * r + cc) * nt + i) * xs[bb][cc];
         y[r] = acc;
@@ -789,13 +790,13 @@ __global__ void __launch_bounds__(kBlock, 8) k_lp_prec(View v, Blocks b, Solver 
   double rz = 0.0, zq = 0.0;
   if (threadIdx.x < cnt) {
     const int u = (n - cs) % W, w = (n - cs) / W;
-    const int row[3] = {n, u < W - 1 ? n + 1 : -1, w < H - 1 ? n + W : -1};
     float z[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-    for (int bb = 0; bb < 3; ++bb) {
-      const int i = row[bb];
-      if (i < 0) continue;
-      const int ei = i - (bb == 2 ? yoff1 : n0);
+    for (int bb = 0; bb < kGBlocks; ++bb) {
+      const int du = gpat_du(bb), dv = gpat_dv(bb);
+      if (u - du < 0 || u - du >= W || w - dv >= H) continue;
+      const int i = n - du - dv * W;
+      const int ei = i - (dv == 0 ? yoff0 : dv == -1 ? yoff1 : yoff2);
 #pragma unroll
       for (int cc = 0; cc < 5; ++cc)
 #pragma unroll
@@ -1119,6 +1120,170 @@ __global__ void k_tr_do(GnnBufs g) {
   for (int k = kGUsed; k < kGOut; ++k) d[k] = __float2bfloat16(0.f);
 }
 
+// ---- the FSAI objective. The factorised sparse approximate inverse of a
+// pattern (Kolotilina and Yeremin) minimises the Kaporin number of G A G^T
+// over the G with that pattern: per row block i, with P_i its present
+// sources (i first), S = sym(A)[P_i, P_i], X = S^-1 E_i (E_i the identity at
+// i's block), G*_i = chol(X_ii)^-1 X^T, so that (G* S G*^T)_ii = I. The
+// objective is the mean over nodes of |N - N*|_F^2, N* = (G*_i,0 L_i - I,
+// G*_i,b L_src), the network's own parametrisation of G*.
+constexpr int kFsaiMax = 5 * kGBlocks;
+
+// A(n, n + (du, dv)) in FP32: the diagonal block, a yarn neighbour's block
+// with its Eulerian couplings, the x part of the other stencil offsets, zero
+// outside the stencil
+__device__ void a_block(const View& v, int n, int du, int dv, float B[5][5]) {
+  if (du == 0 && dv == 0) {
+    diag_block(v, n, B);
+    return;
+  }
+  const int d = yarn_nbr(du, dv);
+  if (d >= 0) {
+    nbr_block(v, n, d, B);
+    return;
+  }
+  for (int r = 0; r < 5; ++r)
+    for (int c = 0; c < 5; ++c) B[r][c] = 0.f;
+  const int s = stencil_index(du, dv);
+  if (s < 0) return;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) B[r][c] = (float)slot(v, YS_SLOT_LL + 9 * s + 3 * r + c, n);
+}
+
+// N* of node n (one thread; the 35 x 35 local system lives in local memory);
+// a local system that does not factorise keeps N* = N (no gradient)
+__global__ void __launch_bounds__(kNB) k_fsai_target(View v, GnnBufs g) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = g.ntot;
+  if (n >= nt) return;
+  const ClothParams& P = v.cp[v.node_cloth[n]];
+  const int u = v.node_u[n], w = v.node_v[n];
+  int src[kGBlocks], pos[kGBlocks];
+  int m = 0;
+  for (int b = 0; b < kGBlocks; ++b) {
+    const int du = gpat_du(b), dv = gpat_dv(b);
+    const bool in = u + du >= 0 && u + du < P.W && w + dv >= 0 && w + dv < P.H;
+    src[b] = in ? n + du + dv * P.W : -1;
+    pos[b] = in ? m++ : -1;
+  }
+  const int dm = 5 * m;
+  float S[kFsaiMax][kFsaiMax];
+  for (int i = 0; i < dm; ++i)
+    for (int k = 0; k < dm; ++k) S[i][k] = 0.f;
+  for (int b1 = 0; b1 < kGBlocks; ++b1) {
+    if (src[b1] < 0) continue;
+    for (int b2 = 0; b2 < kGBlocks; ++b2) {
+      if (src[b2] < 0) continue;
+      float B[5][5];  // A(src1, src2)
+      a_block(v, src[b1], gpat_du(b2) - gpat_du(b1), gpat_dv(b2) - gpat_dv(b1), B);
+      for (int r = 0; r < 5; ++r)
+        for (int c = 0; c < 5; ++c) {
+          S[5 * pos[b1] + r][5 * pos[b2] + c] += 0.5f * B[r][c];
+          S[5 * pos[b2] + c][5 * pos[b1] + r] += 0.5f * B[r][c];
+        }
+    }
+  }
+  bool ok = true;
+  for (int k = 0; k < dm && ok; ++k) {  // S = C C^T, C in the lower triangle
+    float d = S[k][k];
+    for (int q = 0; q < k; ++q) d -= S[k][q] * S[k][q];
+    ok = d > 0.f && isfinite(d);
+    const float ck = sqrtf(fmaxf(d, FLT_MIN));
+    S[k][k] = ck;
+    for (int i = k + 1; i < dm; ++i) {
+      float t = S[i][k];
+      for (int q = 0; q < k; ++q) t -= S[i][q] * S[k][q];
+      S[i][k] = t / ck;
+    }
+  }
+  float X[kFsaiMax][5];
+  for (int c = 0; c < 5; ++c) {
+    for (int i = 0; i < dm; ++i) {
+      float t = i == c ? 1.f : 0.f;
+      for (int q = 0; q < i; ++q) t -= S[i][q] * X[q][c];
+      X[i][c] = t / S[i][i];
+    }
+    for (int i = dm - 1; i >= 0; --i) {
+      float t = X[i][c];
+      for (int q = i + 1; q < dm; ++q) t -= S[q][i] * X[q][c];
+      X[i][c] = t / S[i][i];
+    }
+  }
+  // chol(X_ii) (symmetrised), then G*^T rows: Z = Lx^-1 X^T
+  float Lx[5][5] = {};
+  for (int k = 0; k < 5 && ok; ++k) {
+    float d = 0.5f * (X[k][k] + X[k][k]);
+    for (int q = 0; q < k; ++q) d -= Lx[k][q] * Lx[k][q];
+    ok = d > 0.f && isfinite(d);
+    Lx[k][k] = sqrtf(fmaxf(d, FLT_MIN));
+    for (int i = k + 1; i < 5; ++i) {
+      float t = 0.5f * (X[i][k] + X[k][i]);
+      for (int q = 0; q < k; ++q) t -= Lx[i][q] * Lx[k][q];
+      Lx[i][k] = t / Lx[k][k];
+    }
+  }
+  for (int b = 0; b < kGBlocks; ++b) {
+    float Nb[5][5] = {};
+    if (src[b] >= 0) {
+      float Gs[5][5];  // G*_n,b
+      for (int c = 0; c < 5; ++c)
+        for (int r = 0; r < 5; ++r) {
+          float t = X[5 * pos[b] + c][r];
+          for (int q = 0; q < r; ++q) t -= Lx[r][q] * Gs[q][c];
+          Gs[r][c] = t / Lx[r][r];
+        }
+      // L_src = (L_src^-1)^-1, lower triangular
+      float Li[5][5], L[5][5] = {};
+      load_linv(g.linv, nt, src[b], Li);
+      for (int c = 0; c < 5; ++c) {
+        L[c][c] = 1.f / Li[c][c];
+        for (int r = c + 1; r < 5; ++r) {
+          float t = 0.f;
+          for (int q = c; q < r; ++q) t += Li[r][q] * L[q][c];
+          L[r][c] = -t / Li[r][r];
+        }
+      }
+      mul_ab(Gs, L, Nb);
+      if (b == 0)
+        for (int r = 0; r < 5; ++r) Nb[r][r] -= 1.f;
+    }
+    for (int r = 0; r < 5; ++r)
+      for (int c = 0; c < 5; ++c) {
+        const int64_t at = (int64_t)(25 * b + 5 * r + c) * nt + n;
+        g.Nt[at] = (ok && isfinite(Nb[r][c])) ? Nb[r][c] : g.Gn[at];
+      }
+  }
+}
+
+// d loss / d N = (2 / nodes) (N - N*), d o = 0.1 d N (BF16); per-block
+// partials of |N - N*|^2 into lpart row 0
+__global__ void __launch_bounds__(kNB) k_fsai_do(GnnBufs g) {
+  __shared__ double sh[kNB / 32];
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = g.ntot;
+  double l = 0.0;
+  if (n < nt) {
+    const float sc = 2.f / (float)nt;
+    bf16* d = g.dob + (int64_t)n * kGOut;
+    for (int k = 0; k < kGUsed; ++k) {
+      const int64_t at = (int64_t)k * nt + n;
+      const float e = g.Gn[at] - g.Nt[at];
+      l += (double)e * e;
+      d[k] = __float2bfloat16(kGOutScale * sc * e);
+    }
+    for (int k = kGUsed; k < kGOut; ++k) d[k] = __float2bfloat16(0.f);
+  }
+  const double s1 = blk_sum(l, sh);
+  if (threadIdx.x == 0) g.lpart[blockIdx.x] = s1;
+}
+
+__global__ void k_fsai_loss(GnnBufs g) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double l = 0.0;
+  for (int i = 0; i < g.nlblk; ++i) l += g.lpart[i];
+  g.lpart[2 * g.nlblk] = l / g.ntot;
+}
+
 // dz = dh * (a > 0) in BF16
 __global__ void k_relu_bwd(const float* dh, const bf16* act, const float* hpos, bf16* dzb, int count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1222,14 +1387,20 @@ void gnn_refresh_bf16(const GnnNet& net, cudaStream_t s) {
 }
 
 void gnn_loss_grad(const View& v, const GnnNet& net, const GnnBufs& g, uint64_t seed, bool probes_given,
-                   cudaStream_t s) {
+                   int objective, cudaStream_t s) {
   const int M = g.ntot;
   const int64_t hs = (int64_t)M * kGHid;
-  if (!probes_given) k_tr_probe<<<nblk(M), kNB, 0, s>>>(g, seed);
-  k_tr_u<<<nblk(M), kNB, 0, s>>>(g);
-  k_tr_t<<<g.nlblk, kNB, 0, s>>>(v, g);
-  k_tr_loss<<<1, 32, 0, s>>>(g);
-  k_tr_do<<<nblk(M), kNB, 0, s>>>(g);
+  if (objective == 1) {
+    k_fsai_target<<<nblk(M), kNB, 0, s>>>(v, g);
+    k_fsai_do<<<g.nlblk, kNB, 0, s>>>(g);
+    k_fsai_loss<<<1, 32, 0, s>>>(g);
+  } else {
+    if (!probes_given) k_tr_probe<<<nblk(M), kNB, 0, s>>>(g, seed);
+    k_tr_u<<<nblk(M), kNB, 0, s>>>(g);
+    k_tr_t<<<g.nlblk, kNB, 0, s>>>(v, g);
+    k_tr_loss<<<1, 32, 0, s>>>(g);
+    k_tr_do<<<nblk(M), kNB, 0, s>>>(g);
+  }
   const int nchunk = (M + 63) / 64;
   const int per = (nchunk + g.nsplit - 1) / g.nsplit;
   const int splits = (nchunk + per - 1) / per;

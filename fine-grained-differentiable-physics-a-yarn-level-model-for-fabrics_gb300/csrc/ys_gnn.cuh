@@ -18,7 +18,7 @@
 //           norms of its upper couplings, flags)
 //   h1    = relu(W0 f + b0)                                   (64)
 //   h_l+1 = h_l + relu(W_l [h_i, h_left, h_right, h_down, h_up] + b_l)   l = 1..3
-//   o     = Wh h4 + bh                                        (128, 75 used)
+//   o     = Wh h4 + bh                                        (192, 175 used)
 //   N_i,0 = 0.1 o[0:25],   N_i,b = -E_i,b + 0.1 o[25 b : 25 b + 25]
 // The untrained network (head weights zero) is the first-order factorised
 // approximate inverse G = (I - E_lower) L^-1.
@@ -39,10 +39,10 @@
 
 namespace ys {
 
-constexpr int kGIn = 128, kGHid = 64, kGMsg = 320, kGOut = 128, kGLayers = 3, kGBlocks = 3, kGUsed = 25 * kGBlocks;
+constexpr int kGIn = 128, kGHid = 64, kGMsg = 320, kGOut = 192, kGLayers = 3, kGBlocks = 7, kGUsed = 25 * kGBlocks;
 constexpr float kGOutScale = 0.1f;
 // packed FP32 parameter vector: W0 [64][128], b0, then per layer W [64][320], b,
-// then Wh [128][64], bh
+// then Wh [192][64], bh
 constexpr int kPW0 = 0;
 constexpr int kPb0 = kPW0 + kGHid * kGIn;
 constexpr int kPL0 = kPb0 + kGHid;
@@ -62,9 +62,9 @@ struct GnnNet {  // device arrays
   float* w;             // [kGParams] FP32 master parameters
   __nv_bfloat16* W0;    // [64][128]
   __nv_bfloat16* Wl;    // [3][64][320]
-  __nv_bfloat16* Wh;    // [128][64]
+  __nv_bfloat16* Wh;    // [192][64]
   __nv_bfloat16* WlT;   // [3][320][64]
-  __nv_bfloat16* WhT;   // [64][128]
+  __nv_bfloat16* WhT;   // [64][192]
 };
 
 struct GnnBufs {  // device arrays sized for ntot nodes
@@ -80,16 +80,17 @@ struct GnnBufs {  // device arrays sized for ntot nodes
   float* h;             // [4][ntot][64] h1..h4
   __nv_bfloat16* hb;    // [4][ntot][64]
   __nv_bfloat16* act;   // [3][ntot][64] relu outputs of the message layers
-  float* o;             // [128][ntot] network outputs (component-major)
-  float* G;             // [75][ntot] blocks of G, row-major 5 x 5 (training, export)
-  __nv_bfloat16* Gh;    // [75][ntot] the same in BF16 (the solve's preconditioner)
-  float* Gn;            // [75][ntot] blocks of N (training)
+  float* o;             // [192][ntot] network outputs (component-major)
+  float* G;             // [175][ntot] blocks of G, row-major 5 x 5 (training, export)
+  __nv_bfloat16* Gh;    // [175][ntot] the same in BF16 (the solve's preconditioner)
+  float* Gn;            // [175][ntot] blocks of N (training)
+  float* Nt;            // [175][ntot] the exact FSAI's blocks of N (the FSAI objective's target)
   float* vec;           // [4][5][ntot] training vectors (w, u, t, s)
-  __nv_bfloat16* dob;   // [ntot][128]
+  __nv_bfloat16* dob;   // [ntot][192]
   float* dh;            // [ntot][64]
   __nv_bfloat16* dzb;   // [ntot][64]
   float* dm;            // [ntot][320]
-  float* wpart;         // [nsplit][kWgradRows][128]
+  float* wpart;         // [nsplit][kWgradRows][192]
   float* grad;          // [kGParams]
   double* lpart;        // [2][nlblk] loss partials, then loss and its two scales
   int nlblk;
@@ -98,7 +99,7 @@ struct GnnBufs {  // device arrays sized for ntot nodes
 
 // learned-preconditioner PCG state lives in Solver; these hold its extras
 struct LpcgExtra {
-  const __nv_bfloat16* G;  // [75][ntot]
+  const __nv_bfloat16* G;  // [175][ntot]
   float* rf;        // [5][ntot] the residual in FP32, as the preconditioner reads it
   double* z;        // [5][ntot] G^T G r
 };
@@ -113,10 +114,11 @@ void gnn_forward_attrs();
 // G (and, for training, the blocks of N) from the network outputs
 void gnn_make_g(const GnnBufs& g, bool keep_n, cudaStream_t s);
 void gnn_refresh_bf16(const GnnNet& net, cudaStream_t s);
-// one training pass: probes from seed (or host-given in vec slot 0 when
-// probes_given), the loss and the parameter gradient into g.grad
+// one training pass, the loss and the parameter gradient into g.grad:
+// objective 0 (Kaporin number; probes from seed, or host-given in vec slot 0
+// when probes_given) or 1 (distance of N to the exact FSAI's blocks)
 void gnn_loss_grad(const View& v, const GnnNet& net, const GnnBufs& g, uint64_t seed, bool probes_given,
-                   cudaStream_t s);
+                   int objective, cudaStream_t s);
 void gnn_adam(const GnnNet& net, const GnnBufs& g, float* m, float* vv, float lr, int step, cudaStream_t s);
 
 // x = 0, r = b, z = G^T G r, p = z and the per-cloth start of the iteration

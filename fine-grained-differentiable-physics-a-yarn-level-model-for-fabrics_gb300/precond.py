@@ -3,9 +3,15 @@
 The reference solves every step with Eigen's Jacobi-preconditioned conjugate
 gradient (src/Solvers.cpp:3-31); that stays the default and the fallback. This
 module adds a graph network over the crossing graph that reads each assembled
-system and emits the blocks of a block lower-triangular G in M^-1 = G^T G,
-trained on the Kaporin condition number of G A G^T (see ys_gnn.cuh for the
-network and include/yarnsim.h for the C ABI). Training runs on the GPU with the
+system and emits the blocks of a block lower-triangular G in M^-1 = G^T G over
+seven blocks of each node (self, left, down, left-down, right-down, left-2,
+down-2). Untrained (output head at zero) it is the first-order approximate
+inverse G = (I - E_lower) L^-1; it is trained to predict the exact factorised
+sparse approximate inverse of the pattern -- the G that minimises the Kaporin
+condition number of G A G^T, which a kernel computes per node from the
+assembled system as the training target -- or, optionally, on the stochastic
+Kaporin number itself (see ys_gnn.cuh for the network and include/yarnsim.h
+for the C ABI). Training runs on the GPU with the
 library's own BF16 tensor-core forward and backward kernels, on systems the
 simulator generates from seeded batches of cloths like the plain method's
 workloads: sizes 5..50, plain / twill / satin weaves, per-line material within
@@ -27,8 +33,18 @@ from .cloth import ClothBatch, ClothSpec
 PARAMS_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "precond_params.npy")
 
 
+OBJECTIVES = {"kaporin": 0, "fsai": 1}
+
+
 def param_count() -> int:
     return int(N.load().ys_gnn_param_count())
+
+
+def dims():
+    """(network outputs per node, blocks of G per node)"""
+    o, b = ctypes.c_int32(), ctypes.c_int32()
+    N.load().ys_gnn_dims(ctypes.byref(o), ctypes.byref(b))
+    return o.value, b.value
 
 
 class LearnedPreconditioner:
@@ -45,10 +61,8 @@ class LearnedPreconditioner:
 
     @classmethod
     def pretrained(cls, device: int = 0, path: str = PARAMS_FILE) -> "LearnedPreconditioner":
-        """The parameters shipped with the package: the network's starting
-        weights (head at zero, i.e. the analytic first-order inverse), which
-        train()'s selection by held-out convergence kept because no trained
-        set converged faster."""
+        """The parameters shipped with the package, trained by main() (the
+        FSAI objective, selected by held-out convergence)."""
         return cls(device=device, params=np.load(path))
 
     def close(self):
@@ -76,22 +90,27 @@ class LearnedPreconditioner:
     def save(self, path: str):
         np.save(path, self.params())
 
+    def set_objective(self, name: str):
+        """"fsai" (distance to the exact FSAI's blocks; the default) or "kaporin"."""
+        N.check(N.load().ys_gnn_set_objective(self._h, OBJECTIVES[name]), "ys_gnn_set_objective")
+
     def train_step(self, batch: ClothBatch, seed: int, lr: float) -> float:
-        """One Adam step on the Kaporin condition number of the systems `batch`
-        assembled last; returns the loss before the step."""
+        """One Adam step on the objective over the systems `batch` assembled
+        last; returns the loss before the step."""
         loss = ctypes.c_double()
         N.check(N.load().ys_gnn_train_step(self._h, batch._h, int(seed), float(lr), ctypes.byref(loss)),
                 "ys_gnn_train_step")
         return loss.value
 
     def loss_grad(self, batch: ClothBatch, probes: Optional[np.ndarray] = None, seed: int = 1) -> dict:
-        """Loss, parameter gradient, network outputs [n][128] and G blocks
-        [n][75] (self, left, down) for the batch's last system (no update)."""
+        """Loss, parameter gradient, network outputs [n][outputs] and G blocks
+        [n][25 blocks] (pattern order) for the batch's last system (no update)."""
         n = batch.total_nodes
+        n_out, n_blk = dims()
         loss = ctypes.c_double()
         grad = np.zeros(param_count(), np.float32)
-        out = np.zeros((n, 128), np.float32)
-        gb = np.zeros((n, 75), np.float32)
+        out = np.zeros((n, n_out), np.float32)
+        gb = np.zeros((n, 25 * n_blk), np.float32)
         pr = None
         if probes is not None:
             pr = np.ascontiguousarray(probes, np.float32)
@@ -143,16 +162,17 @@ def validation_residual(net: LearnedPreconditioner, batch: ClothBatch, k: int = 
 
 def train(net: LearnedPreconditioner, systems: int = 20000, cloths_per_batch: int = 64, steps_per_batch: int = 40,
           lr: float = 1e-3, seed: int = 0, h: float = 1e-3, val_every: int = 25, select: bool = True,
-          log=None) -> dict:
+          objective: str = "fsai", log=None) -> dict:
     """Trains on `systems` linear systems the simulator generates: batches of
     `cloths_per_batch` seeded cloths are stepped with Jacobi-PCG for
     `steps_per_batch` steps, and every step's systems (one per cloth) feed one
-    Adam step on the Kaporin condition number of G A G^T. The rate decays by
+    Adam step on `objective` ("fsai" or "kaporin"). The rate decays by
     cosine to 5 % of lr. Every `val_every` steps (and before the first) the
     network is scored on held-out systems by validation_residual, and the
     best-scoring parameters -- possibly the starting ones -- are kept (with
     select=False the final parameters are).
     Returns {"loss": [...], "validation": [(step, score)], "best_step": s}."""
+    net.set_objective(objective)
     rng = np.random.default_rng(seed)
     vrng = np.random.default_rng(seed + 7919)
     vbatch = ClothBatch(training_specs(vrng, 8, 10, 40), device=net.device)

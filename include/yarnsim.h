@@ -424,17 +424,24 @@ ys_status ys_collider_respond_backward(ys_collider *c, const double *dl_dx, cons
  * Eigen's Jacobi-PCG, src/Solvers.cpp:3-31, which stays the default and the
  * fallback). A graph network over the crossing graph reads each assembled
  * system and emits a factorised sparse approximate inverse M^-1 = G^T G, G
- * block lower triangular over the blocks self, left, down of each node
- * (5 x 5 blocks; G_i,0 = (I + N_i,0)
+ * block lower triangular over seven blocks of each node: self, left, down,
+ * left-down, right-down, left-2, down-2 (5 x 5 blocks; G_i,0 = (I + N_i,0)
  * L_i^-1, G_i,b = N_i,b L_src^-1, L_i the Cholesky factor of node i's
  * diagonal block). The conjugate-gradient iteration keeps FP64 and the same
  * stopping rule |r| <= tol |b|; M^-1 is applied in FP32 with the flexible
  * (Polak-Ribiere) direction update. */
 typedef struct ys_gnn ys_gnn;
 enum { YS_PREC_JACOBI = 0, YS_PREC_LEARNED = 1 };
+/* training objectives: the Kaporin number of G A G^T (stochastic trace), or
+ * the distance of N to the blocks of the exact FSAI of the pattern (its
+ * minimiser), computed per node from the assembled system (the default) */
+enum { YS_GNN_KAPORIN = 0, YS_GNN_FSAI = 1 };
 /* number of FP32 parameters (packed: W0 [64][128], b0 [64], 3 x (W [64][320],
- * b [64]), Wh [128][64], bh [128]) */
+ * b [64]), Wh [outputs][64], bh [outputs]) */
 int32_t ys_gnn_param_count(void);
+/* network outputs per node and blocks of G per node */
+void ys_gnn_dims(int32_t *outputs, int32_t *blocks);
+ys_status ys_gnn_set_objective(ys_gnn *g, int32_t objective);
 /* a network with seeded initial weights (output head zero: the analytic
  * first-order approximate inverse G = (I - E_lower) L^-1) */
 ys_status ys_gnn_create(int32_t device, uint64_t seed, ys_gnn **out);
@@ -442,20 +449,22 @@ void ys_gnn_destroy(ys_gnn *g);
 ys_status ys_gnn_get_params(ys_gnn *g, float *out);
 /* also resets the optimiser state */
 ys_status ys_gnn_set_params(ys_gnn *g, const float *in);
-/* One Adam step (rate lr) on the Kaporin condition number of G A G^T,
- * loss = log(tr(G A G^T) / n) - (2 / n) log |det G| (n DOFs; the trace from
- * Rademacher probes drawn from seed, the determinant exact), over the systems
- * the batch assembled last (its ys_assemble or ys_step); *loss receives the
- * loss before the step. */
+/* One Adam step (rate lr) on the network's objective over the systems the
+ * batch assembled last (its ys_assemble or ys_step); *loss receives the loss
+ * before the step. YS_GNN_KAPORIN: loss = log(tr(G A G^T) / n) - (2 / n)
+ * log |det G| (n DOFs; the trace from Rademacher probes drawn from seed, the
+ * determinant exact). YS_GNN_FSAI: loss = mean over nodes of |N - N*|_F^2,
+ * N* the exact FSAI's blocks in the network's parametrisation. */
 ys_status ys_gnn_train_step(ys_gnn *g, ys_batch *b, uint64_t seed, float lr, double *loss);
 /* Loss and gradient without an update (probes [total_nodes][5] host, or NULL
- * for seeded probes); outputs [total_nodes][128] network outputs, gblocks
- * [total_nodes][75] blocks of G (self, left, down; row-major 5 x 5); any
- * output may be NULL. */
+ * for seeded probes; Kaporin objective only); outputs [total_nodes][outputs]
+ * network outputs, gblocks [total_nodes][25 blocks] blocks of G in pattern
+ * order (row-major 5 x 5); any output may be NULL. */
 ys_status ys_gnn_loss_grad(ys_gnn *g, ys_batch *b, const float *probes, uint64_t seed, double *loss, float *grad,
                            float *outputs, float *gblocks);
 /* kind YS_PREC_JACOBI (default) or YS_PREC_LEARNED with network g; the batch
- * borrows g, which must outlive its use. Learned steps run launch by launch. */
+ * borrows g, which must outlive its use. With ys_use_graphs a learned step is
+ * one graph launch (the network evaluated inside it when due). */
 ys_status ys_set_preconditioner(ys_batch *b, int32_t kind, ys_gnn *g);
 /* evaluate the network once per `every` learned solves (default 1) and reuse
  * G in between: a G from an earlier step is still a symmetric positive

@@ -5,9 +5,11 @@ The learned preconditioner has no counterpart in the reference (its solve is
 Eigen's Jacobi-PCG, src/Solvers.cpp:3-31), so this oracle restates the
 library's own definition independently of its kernels: the system features,
 the graph network (BF16 operands rounded where the tensor cores read them),
-the blocks of the block lower-triangular G, and the Kaporin loss
-log(w^T G A G^T w / n) - (2 / n) log |det G|, in float64 PyTorch on the CPU;
-its parameter gradient comes from torch.autograd, not from the hand-written
+the blocks of the block lower-triangular G, the Kaporin loss
+log(w^T G A G^T w / n) - (2 / n) log |det G|, and the FSAI objective (the
+mean squared distance of the blocks N to those of the pattern's exact
+factorised sparse approximate inverse), in float64 PyTorch on the CPU; the
+parameter gradients come from torch.autograd, not from the hand-written
 backward the GPU runs. Rounding to BF16 uses straight-through estimators (the value is rounded,
 the derivative is the identity), which is what the GPU's BF16 operands amount
 to.
@@ -27,7 +29,7 @@ SLOT_LE_NBR, SLOT_EL_NBR, SLOT_EE_NBR = 131, 143, 155
 STENCIL = [(0, 0), (-1, 0), (1, 0), (0, -1), (0, 1), (-2, 0), (2, 0), (0, -2), (0, 2), (-1, -1), (1, -1), (-1, 1),
            (1, 1)]
 YARN_NBR = [(-1, 0), (1, 0), (0, -1), (0, 1)]  # left, right, down, up
-IN, HID, MSG, OUT, LAYERS, OUT_SCALE, BLOCKS = 128, 64, 320, 128, 3, 0.1, 3
+IN, HID, MSG, OUT, LAYERS, OUT_SCALE, BLOCKS = 128, 64, 320, 192, 3, 0.1, 7
 # lower offsets: self, left, down, left-down, right-down, left-2, down-2; G uses
 # the first BLOCKS, the features the six couplings
 PATTERN = [(0, 0), (-1, 0), (0, -1), (-1, -1), (1, -1), (-2, 0), (0, -2)]
@@ -285,6 +287,65 @@ def evaluate(slots, topo: Topology, params, probes):
     loss.backward()
     return dict(loss=float(loss.detach()), grad=p.grad.numpy().copy(), o=o.detach().numpy(),
                 G=Gb.detach().reshape(topo.n, 25 * BLOCKS).numpy(), f=f, E=E, Linv=Linv, chol_ok=ok)
+
+
+def a_block(slots, du, dv):
+    """[n, 5, 5] A(i, i + (du, dv)): the diagonal block, a yarn neighbour's
+    block, the x part of another stencil offset, or zero outside the stencil."""
+    if (du, dv) == (0, 0):
+        return diag_blocks(slots)
+    if (du, dv) in YARN_NBR or (du, dv) in STENCIL:
+        return offset_block(slots, du, dv)
+    return np.zeros((slots.shape[1], 5, 5))
+
+
+def fsai_targets(slots, topo: Topology, Linv):
+    """N* [n, BLOCKS, 5, 5]: the exact FSAI of the pattern, G*_i = chol(X_ii)^-1
+    X^T with X = sym(A)[P_i, P_i]^-1 E_i, as N*_i,0 = G*_i,0 L_i - I and
+    N*_i,b = G*_i,b L_src (A from the FP32 slot values; zero for absent
+    sources)."""
+    sl32 = slots.astype(np.float32).astype(np.float64)
+    n = topo.n
+    blocks = {}
+    for b1 in range(BLOCKS):
+        for b2 in range(BLOCKS):
+            d = (PATTERN[b2][0] - PATTERN[b1][0], PATTERN[b2][1] - PATTERN[b1][1])
+            if d not in blocks:
+                blocks[d] = a_block(sl32, *d)
+    L = np.linalg.inv(Linv)
+    out = np.zeros((n, BLOCKS, 5, 5))
+    for i in range(n):
+        bs = [b for b in range(BLOCKS) if topo.pat[i, b] >= 0]
+        m = len(bs)
+        S = np.zeros((5 * m, 5 * m))
+        for a1, b1 in enumerate(bs):
+            for a2, b2 in enumerate(bs):
+                d = (PATTERN[b2][0] - PATTERN[b1][0], PATTERN[b2][1] - PATTERN[b1][1])
+                B = blocks[d][topo.pat[i, b1]]
+                S[5 * a1:5 * a1 + 5, 5 * a2:5 * a2 + 5] += 0.5 * B
+                S[5 * a2:5 * a2 + 5, 5 * a1:5 * a1 + 5] += 0.5 * B.T
+        E = np.zeros((5 * m, 5))
+        E[:5] = np.eye(5)
+        X = np.linalg.solve(S, E)
+        Lx = np.linalg.cholesky(0.5 * (X[:5] + X[:5].T))
+        Gt = np.linalg.solve(Lx, X.T)
+        for a, b in enumerate(bs):
+            out[i, b] = Gt[:, 5 * a:5 * a + 5] @ L[topo.pat[i, b]] - (np.eye(5) if b == 0 else 0.0)
+    return out
+
+
+def evaluate_fsai(slots, topo: Topology, params):
+    """dict(loss, grad [N_PARAMS], target [n, BLOCKS, 5, 5]) of the FSAI
+    objective: mean over nodes of sum_b |N_i,b - N*_i,b|_F^2."""
+    Linv, ok = block_factor(slots)
+    f, E = features(slots, topo, Linv, ok)
+    target = fsai_targets(slots, topo, Linv)
+    p = torch.as_tensor(np.asarray(params, np.float64), dtype=torch.float64).requires_grad_(True)
+    o = network(p, torch.as_tensor(f), topo)
+    Nb = n_blocks(o, E, topo)
+    loss = ((Nb - torch.as_tensor(target)) ** 2).sum() / topo.n
+    loss.backward()
+    return dict(loss=float(loss.detach()), grad=p.grad.numpy().copy(), target=target)
 
 
 def init_params(seed: int) -> np.ndarray:

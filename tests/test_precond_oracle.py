@@ -106,3 +106,51 @@ def test_rademacher_signs_are_balanced():
     w = go.rademacher(11, 400)
     assert set(np.unique(w)) == {-1.0, 1.0}
     assert abs(w.mean()) < 0.1
+
+
+def test_fsai_target_is_the_pattern_inverse_with_unit_diagonal_blocks():
+    """The exact FSAI target: G* (from N*) has the pattern, (G* S G*^T)_ii = I
+    on every diagonal block (S the symmetric part of A), and the network's
+    parametrisation of the target reproduces G* (N* = 0 for absent sources)."""
+    topo = go.Topology([(5, 4), (3, 3)], handles=[[(0, 0)], [(0, 0)]])
+    slots = synthetic_system(topo, 4)
+    Linv, ok = go.block_factor(slots)
+    Nt = go.fsai_targets(slots, topo, Linv)
+    n = topo.n
+    G = np.zeros((5 * n, 5 * n))
+    for i in range(n):
+        for b in range(go.BLOCKS):
+            j = topo.pat[i, b]
+            if j < 0:
+                assert np.all(Nt[i, b] == 0.0)
+                continue
+            Nb = Nt[i, b] + (np.eye(5) if b == 0 else 0.0)
+            G[5 * i:5 * i + 5, 5 * j:5 * j + 5] = Nb @ Linv[j]
+    # dense A from the slots (FP32 values, as the target reads them)
+    e = np.eye(5 * n)
+    A = np.stack([go.spmv(slots, torch_t(e[:, k].reshape(n, 5)), topo).numpy().reshape(-1) for k in range(5 * n)], 1)
+    S = 0.5 * (A + A.T)
+    M = G @ S @ G.T
+    for i in range(n):
+        assert np.allclose(M[5 * i:5 * i + 5, 5 * i:5 * i + 5], np.eye(5), atol=1e-9)
+
+
+def torch_t(x):
+    import torch
+    return torch.as_tensor(x, dtype=torch.float64)
+
+
+def test_fsai_objective_gradient_matches_finite_differences(smooth):
+    topo = go.Topology([(4, 4)], handles=[[(0, 0)]])
+    slots = synthetic_system(topo, 5)
+    p0 = go.init_params(6)
+    r = go.evaluate_fsai(slots, topo, p0)
+    rng = np.random.default_rng(2)
+    for _ in range(3):
+        d = rng.standard_normal(go.N_PARAMS)
+        d /= np.linalg.norm(d)
+        eps = 1e-4
+        lp = go.evaluate_fsai(slots, topo, p0 + eps * d)["loss"]
+        lm = go.evaluate_fsai(slots, topo, p0 - eps * d)["loss"]
+        fd = (lp - lm) / (2 * eps)
+        assert abs(fd - r["grad"] @ d) <= 1e-6 * max(1.0, abs(fd)), (fd, r["grad"] @ d)
