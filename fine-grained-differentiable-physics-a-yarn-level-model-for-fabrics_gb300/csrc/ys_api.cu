@@ -1933,7 +1933,7 @@ ys_status learn_infer(ys_batch* b, ys_gnn* net, bool training = false) {
   ys::GnnBufs& g = b->learn.g;
   b->run(YS_PROF_GNN, 2 + 5 + 1, [&] {
     ys::gnn_prepare(b->v, g, b->stream);
-    ys::gnn_forward(net->net, g, b->stream);
+    ys::gnn_forward(net->net, g, training, b->stream);
     ys::gnn_make_g(g, training, b->stream);
   });
   YS_CUDA(cudaGetLastError());
@@ -2043,7 +2043,7 @@ ys_status graph_build_learned(ys_batch* b, int m, int cap, int override_max, int
         capture_assembly(b, c, override_max);
         if (with_net) {
           ys::gnn_prepare(v, L.g, c);
-          ys::gnn_forward(L.net->net, L.g, c);
+          ys::gnn_forward(L.net->net, L.g, false, c);
           ys::gnn_make_g(L.g, false, c);
         }
         ys::lpcg_setup(v, b->blk, so, lx, c);

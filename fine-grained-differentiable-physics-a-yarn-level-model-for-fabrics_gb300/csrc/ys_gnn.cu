@@ -464,10 +464,10 @@ struct FwdOp {
       const int64_t at = (int64_t)node * kGHid + j;
       float hn = a;
       if (EPI == kEpiLayer) {
-        act_out[at] = __float2bfloat16(a);
+        if (act_out) act_out[at] = __float2bfloat16(a);
         hn = pre.y + a;
       }
-      h_out[at] = hn;
+      if (h_out) h_out[at] = hn;
       hb_out[at] = __float2bfloat16(hn);
     }
   }
@@ -1352,7 +1352,7 @@ void gnn_prepare(const View& v, const GnnBufs& g, cudaStream_t s) {
   k_gnn_feat<<<(v.ntot + kFeatNodes - 1) / kFeatNodes, 12 * kFeatNodes, 0, s>>>(v, g);
 }
 
-void gnn_forward(const GnnNet& net, const GnnBufs& g, cudaStream_t s) {
+void gnn_forward(const GnnNet& net, const GnnBufs& g, bool training, cudaStream_t s) {
   const int M = g.ntot;
   const int64_t hs = (int64_t)M * kGHid;
   {
@@ -1360,9 +1360,11 @@ void gnn_forward(const GnnNet& net, const GnnBufs& g, cudaStream_t s) {
     launch_gemm<decltype(op), kGIn / 64>(op, M, 1, kGIn / 64, 1, g.err, s);
   }
   for (int l = 0; l < kGLayers; ++l) {
+    // the last layer's FP32 output is read by nothing (the head reads its BF16
+    // copy); the ReLU outputs only by the training's backward pass
     FwdOp<64, kEpiLayer> op{g.hb + l * hs, kGHid, M, g.nbr, 1, net.Wl + (int64_t)l * kGHid * kGMsg, kGMsg,
-                            net.w + kPb(l), g.h + l * hs, g.h + (l + 1) * hs, g.hb + (l + 1) * hs,
-                            g.act + l * hs, nullptr};
+                            net.w + kPb(l), g.h + l * hs, l + 1 < kGLayers ? g.h + (l + 1) * hs : nullptr,
+                            g.hb + (l + 1) * hs, training ? g.act + l * hs : nullptr, nullptr};
     launch_gemm<decltype(op), 2>(op, M, 1, kGMsg / 64, 1, g.err, s);
   }
   {

@@ -107,7 +107,8 @@ struct LpcgExtra {
 // ---- launchers (ys_gnn.cu)
 void gnn_neighbours(const View& v, const GnnBufs& g, cudaStream_t s);
 void gnn_prepare(const View& v, const GnnBufs& g, cudaStream_t s);
-void gnn_forward(const GnnNet& net, const GnnBufs& g, cudaStream_t s);
+// (training: keep the ReLU outputs the backward pass reads)
+void gnn_forward(const GnnNet& net, const GnnBufs& g, bool training, cudaStream_t s);
 // sets the forward GEMMs' function attributes (done by gnn_forward's first
 // call; call it before capturing gnn_forward into a graph)
 void gnn_forward_attrs();
