@@ -299,23 +299,24 @@ def a_block(slots, du, dv):
     return np.zeros((slots.shape[1], 5, 5))
 
 
-def fsai_targets(slots, topo: Topology, Linv):
+def fsai_targets(slots, topo: Topology, Linv, blocks: int = None):
     """N* [n, BLOCKS, 5, 5]: the exact FSAI of the pattern, G*_i = chol(X_ii)^-1
     X^T with X = sym(A)[P_i, P_i]^-1 E_i, as N*_i,0 = G*_i,0 L_i - I and
     N*_i,b = G*_i,b L_src (A from the FP32 slot values; zero for absent
     sources)."""
+    nblk = BLOCKS if blocks is None else blocks
     sl32 = slots.astype(np.float32).astype(np.float64)
     n = topo.n
     blocks = {}
-    for b1 in range(BLOCKS):
-        for b2 in range(BLOCKS):
+    for b1 in range(nblk):
+        for b2 in range(nblk):
             d = (PATTERN[b2][0] - PATTERN[b1][0], PATTERN[b2][1] - PATTERN[b1][1])
             if d not in blocks:
                 blocks[d] = a_block(sl32, *d)
     L = np.linalg.inv(Linv)
-    out = np.zeros((n, BLOCKS, 5, 5))
+    out = np.zeros((n, nblk, 5, 5))
     for i in range(n):
-        bs = [b for b in range(BLOCKS) if topo.pat[i, b] >= 0]
+        bs = [b for b in range(nblk) if topo.pat[i, b] >= 0]
         m = len(bs)
         S = np.zeros((5 * m, 5 * m))
         for a1, b1 in enumerate(bs):
@@ -346,6 +347,83 @@ def evaluate_fsai(slots, topo: Topology, params):
     loss = ((Nb - torch.as_tensor(target)) ** 2).sum() / topo.n
     loss.backward()
     return dict(loss=float(loss.detach()), grad=p.grad.numpy().copy(), target=target)
+
+
+def slots_from_dense(A, b, W, H):
+    """Stencil slots [159, W H] of one cloth from the oracle's dense system
+    (3 N Lagrangian DOFs, then 2 per interior node in row order); the
+    Eulerian DOFs of boundary nodes become identity rows with a zero
+    right-hand side, as the library stores them. Returns (slots, A5, b5) with
+    A5 [5 N, 5 N] and b5 [5 N] in node-block order."""
+    N = W * H
+    idx = np.full(A.shape[0], -1)
+    for n in range(N):
+        idx[3 * n:3 * n + 3] = 5 * n + np.arange(3)
+    for v in range(1, H - 1):
+        for u in range(1, W - 1):
+            e = 3 * N + 2 * ((u - 1) + (v - 1) * (W - 2))
+            idx[e:e + 2] = 5 * (u + v * W) + np.arange(3, 5)
+    A5 = np.zeros((5 * N, 5 * N))
+    A5[np.ix_(idx, idx)] = A
+    used = np.zeros(5 * N, bool)
+    used[idx] = True
+    A5[~used, ~used] = 1.0
+    b5 = np.zeros(5 * N)
+    b5[idx] = b
+    S = np.zeros((159, N))
+    blk = lambda i, j: A5[5 * i:5 * i + 5, 5 * j:5 * j + 5]
+    for n in range(N):
+        u, v = n % W, n // W
+        D = blk(n, n)
+        for s_, (du, dv) in enumerate(STENCIL):
+            if 0 <= u + du < W and 0 <= v + dv < H:
+                S[SLOT_LL + 9 * s_:SLOT_LL + 9 * s_ + 9, n] = blk(n, n + du + dv * W)[:3, :3].reshape(9)
+        S[SLOT_LE_SELF:SLOT_LE_SELF + 6, n] = D[:3, 3:].reshape(6)
+        S[SLOT_EL_SELF:SLOT_EL_SELF + 6, n] = D[3:, :3].reshape(6)
+        S[SLOT_EE_SELF:SLOT_EE_SELF + 2, n] = np.diag(D[3:, 3:])
+        for d, (du, dv) in enumerate(YARN_NBR):
+            if 0 <= u + du < W and 0 <= v + dv < H:
+                B = blk(n, n + du + dv * W)
+                k = 3 if d < 2 else 4
+                S[SLOT_LE_NBR + 3 * d:SLOT_LE_NBR + 3 * d + 3, n] = B[:3, k]
+                S[SLOT_EL_NBR + 3 * d:SLOT_EL_NBR + 3 * d + 3, n] = B[k, :3]
+                S[SLOT_EE_NBR + d, n] = B[k, k]
+    return S, A5, b5
+
+
+def dense_g(Nb, Linv, topo: Topology, blocks: int):
+    """Dense G [5 n, 5 n] from blocks N [n, blocks, 5, 5] in the network's
+    parametrisation over the first `blocks` pattern offsets."""
+    n = topo.n
+    G = np.zeros((5 * n, 5 * n))
+    for i in range(n):
+        for b in range(blocks):
+            j = topo.pat[i, b]
+            if j >= 0:
+                G[5 * i:5 * i + 5, 5 * j:5 * j + 5] = (Nb[i, b] + (np.eye(5) if b == 0 else 0.0)) @ Linv[j]
+    return G
+
+
+def pcg_iterations(A, b, G, tol=1e-10, maxiter=500):
+    """Plain preconditioned CG with M^-1 = G^T G: iterations to |r| < tol |b|."""
+    x = np.zeros_like(b)
+    r = b.copy()
+    z = G.T @ (G @ r)
+    p = z.copy()
+    rz = r @ z
+    bb = np.linalg.norm(b)
+    for it in range(1, maxiter + 1):
+        q = A @ p
+        a = rz / (p @ q)
+        x += a * p
+        r -= a * q
+        if np.linalg.norm(r) < tol * bb:
+            return it
+        z = G.T @ (G @ r)
+        rzn = r @ z
+        p = z + (rzn / rz) * p
+        rz = rzn
+    return maxiter
 
 
 def init_params(seed: int) -> np.ndarray:

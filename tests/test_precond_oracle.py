@@ -154,3 +154,35 @@ def test_fsai_objective_gradient_matches_finite_differences(smooth):
         lm = go.evaluate_fsai(slots, topo, p0 - eps * d)["loss"]
         fd = (lp - lm) / (2 * eps)
         assert abs(fd - r["grad"] @ d) <= 1e-6 * max(1.0, abs(fd)), (fd, r["grad"] @ d)
+
+
+def test_seven_block_pattern_leaves_iterations_to_learn():
+    """Why G has seven blocks: on a system the oracle assembles (a 10 x 10
+    plain cloth after 4 steps), the exact FSAI -- the Kaporin minimiser a
+    network on the pattern can at best reach -- needs at most one PCG
+    iteration fewer than the untrained first-order form on the 3-block
+    pattern (9 -> 8), but at least two fewer on the 7-block pattern (9 -> 6)."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(7)
+    base = np.array([1e-3, 1e3, 1e-5])
+    lines = lambda n: base * (1 + 0.2 * (2 * rng.random((n, 3)) - 1))
+    W = 10
+    spec = O.ClothSpec(width=W, length=W, warp=lines(W), weft=lines(W), pose=0, weave=0, wind_vel=(0, 0.5, 0),
+                       wind_density=1.0, wind_drag=0.5, handles=[(0, 0), (W - 1, 0)])
+    c = O.OracleCloth(spec)
+    for _ in range(4):
+        c.step(1e-3, cg_tol=1e-10)
+    A, b = c.system(1e-3)
+    slots, A5, b5 = go.slots_from_dense(A, b, W, W)
+    topo = go.Topology([(W, W)], handles=[[(0, 0), (W - 1, 0)]])
+    Linv, ok = go.block_factor(slots)
+    _, E = go.features(slots, topo, Linv, ok)
+    its = {}
+    for nb in (3, 7):
+        first = np.zeros((topo.n, nb, 5, 5))
+        for bb in range(1, nb):
+            first[:, bb] = -E[:, bb - 1] * (topo.pat[:, bb] >= 0)[:, None, None]
+        exact = go.fsai_targets(slots, topo, Linv, blocks=nb)
+        its[nb] = [go.pcg_iterations(A5, b5, go.dense_g(N, Linv, topo, nb)) for N in (first, exact)]
+    assert its[3][1] >= its[3][0] - 1, its
+    assert its[7][1] <= its[7][0] - 2, its
