@@ -81,7 +81,7 @@ struct ys_batch {
   ys::Solver so{};
   int* anchors = nullptr;
   int* maxiter_dev = nullptr;
-  double* stage = nullptr;  // [5][ntot] staging for layout changes
+  double* stage = nullptr;  // [15][ntot] staging for layout changes (the six state arrays side by side)
   double* ext = nullptr;    // [5][ntot]
   int* h_nactive = nullptr; // pinned
   bool assembled = false;
@@ -232,31 +232,39 @@ struct ys_batch {
 
 namespace {
 
-ys_status upload_soa(ys_batch* b, const double* src, double* dst, int c, int32_t flags) {
+// host (or device, YS_ON_DEVICE) AoS [ntot][c] -> device SoA [c][ntot]; a
+// host array goes through the stage at `slot` (in units of ntot doubles), and
+// with sync the call returns once the host array has been read
+ys_status upload_soa(ys_batch* b, const double* src, double* dst, int c, int32_t flags, int64_t slot = 0,
+                     bool sync = true) {
   const int64_t n = b->ntot;
   if (!src) return YS_OK;
   const double* d_src = src;
   if (!(flags & YS_ON_DEVICE)) {
-    YS_CUDA(cudaMemcpyAsync(b->stage, src, sizeof(double) * n * c, cudaMemcpyHostToDevice, b->stream));
-    d_src = b->stage;
+    YS_CUDA(cudaMemcpyAsync(b->stage + slot * n, src, sizeof(double) * n * c, cudaMemcpyHostToDevice, b->stream));
+    d_src = b->stage + slot * n;
   }
   b->launches += 1;
   k_to_soa<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(d_src, dst, n, c);
   YS_CUDA(cudaGetLastError());
-  if (!(flags & YS_ON_DEVICE)) YS_CUDA(cudaStreamSynchronize(b->stream));  // stage is reused
+  if (sync && !(flags & YS_ON_DEVICE)) YS_CUDA(cudaStreamSynchronize(b->stream));
   return YS_OK;
 }
 
-ys_status download_aos(ys_batch* b, const double* src, double* dst, int c, int32_t flags) {
+// device SoA [c][ntot] -> AoS [ntot][c] on the host (through the stage at
+// `slot`; with sync the call returns once the host array is filled) or on the
+// device
+ys_status download_aos(ys_batch* b, const double* src, double* dst, int c, int32_t flags, int64_t slot = 0,
+                       bool sync = true) {
   const int64_t n = b->ntot;
   if (!dst) return YS_OK;
-  double* d_dst = (flags & YS_ON_DEVICE) ? dst : b->stage;
+  double* d_dst = (flags & YS_ON_DEVICE) ? dst : b->stage + slot * n;
   b->launches += 1;
   k_to_aos<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(src, d_dst, n, c);
   YS_CUDA(cudaGetLastError());
   if (!(flags & YS_ON_DEVICE)) {
-    YS_CUDA(cudaMemcpyAsync(dst, b->stage, sizeof(double) * n * c, cudaMemcpyDeviceToHost, b->stream));
-    YS_CUDA(cudaStreamSynchronize(b->stream));
+    YS_CUDA(cudaMemcpyAsync(dst, d_dst, sizeof(double) * n * c, cudaMemcpyDeviceToHost, b->stream));
+    if (sync) YS_CUDA(cudaStreamSynchronize(b->stream));
   }
   return YS_OK;
 }
@@ -420,7 +428,7 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
   A(&b->rec.nonfinite, nt);
   A(&b->so.x, 5 * nt); A(&b->so.r, 5 * nt); A(&b->so.p, 5 * nt); A(&b->so.q, 5 * nt); A(&b->so.dinv, 5 * nt);
   A(&b->so.part, 4 * blk_cloth.size()); A(&b->so.pc, n_cloths); A(&b->so.nactive, 1);
-  A(&b->stage, 5 * nt); A(&b->ext, 5 * nt);
+  A(&b->stage, 15 * nt); A(&b->ext, 5 * nt);
   if (st != YS_OK) { delete b; return st; }
   if (cudaMallocHost(&b->h_nactive, sizeof(int)) != cudaSuccess) {
     delete b;
@@ -510,13 +518,19 @@ ys_status ys_set_state(ys_batch* b, const double* lpos, const double* lposfix, c
                        const double* epos, const double* eposbar, const double* evel, int32_t flags) {
   if (!b) return fail(YS_ERR_ARG, "null handle");
   YS_CUDA(cudaSetDevice(b->device));
-  ys_status s;
-  if ((s = upload_soa(b, lpos, b->v.X, 3, flags)) != YS_OK) return s;
-  if ((s = upload_soa(b, lposfix, b->v.XF, 3, flags)) != YS_OK) return s;
-  if ((s = upload_soa(b, lvel, b->v.V, 3, flags)) != YS_OK) return s;
-  if ((s = upload_soa(b, epos, b->v.UV, 2, flags)) != YS_OK) return s;
-  if ((s = upload_soa(b, eposbar, b->v.UVB, 2, flags)) != YS_OK) return s;
-  if ((s = upload_soa(b, evel, b->v.UVD, 2, flags)) != YS_OK) return s;
+  // the six arrays through their own stage slots, one wait at the end
+  const double* src[6] = {lpos, lposfix, lvel, epos, eposbar, evel};
+  double* dst[6] = {b->v.X, b->v.XF, b->v.V, b->v.UV, b->v.UVB, b->v.UVD};
+  const int comps[6] = {3, 3, 3, 2, 2, 2};
+  int64_t slot = 0;
+  bool any = false;
+  for (int k = 0; k < 6; ++k) {
+    const ys_status s = upload_soa(b, src[k], dst[k], comps[k], flags, slot, false);
+    if (s != YS_OK) return s;
+    any = any || src[k];
+    slot += comps[k];
+  }
+  if (any && !(flags & YS_ON_DEVICE)) YS_CUDA(cudaStreamSynchronize(b->stream));
   b->assembled = false;
   return YS_OK;
 }
@@ -525,13 +539,19 @@ ys_status ys_get_state(ys_batch* b, double* lpos, double* lposfix, double* lvel,
                        double* evel, int32_t flags) {
   if (!b) return fail(YS_ERR_ARG, "null handle");
   YS_CUDA(cudaSetDevice(b->device));
-  ys_status s;
-  if ((s = download_aos(b, b->v.X, lpos, 3, flags)) != YS_OK) return s;
-  if ((s = download_aos(b, b->v.XF, lposfix, 3, flags)) != YS_OK) return s;
-  if ((s = download_aos(b, b->v.V, lvel, 3, flags)) != YS_OK) return s;
-  if ((s = download_aos(b, b->v.UV, epos, 2, flags)) != YS_OK) return s;
-  if ((s = download_aos(b, b->v.UVB, eposbar, 2, flags)) != YS_OK) return s;
-  if ((s = download_aos(b, b->v.UVD, evel, 2, flags)) != YS_OK) return s;
+  // the six arrays through their own stage slots, one wait at the end
+  double* dst[6] = {lpos, lposfix, lvel, epos, eposbar, evel};
+  const double* src[6] = {b->v.X, b->v.XF, b->v.V, b->v.UV, b->v.UVB, b->v.UVD};
+  const int comps[6] = {3, 3, 3, 2, 2, 2};
+  int64_t slot = 0;
+  bool any = false;
+  for (int k = 0; k < 6; ++k) {
+    const ys_status s = download_aos(b, src[k], dst[k], comps[k], flags, slot, false);
+    if (s != YS_OK) return s;
+    any = any || dst[k];
+    slot += comps[k];
+  }
+  if (any && !(flags & YS_ON_DEVICE)) YS_CUDA(cudaStreamSynchronize(b->stream));
   return YS_OK;
 }
 
