@@ -29,10 +29,12 @@ using ::sqrt;
 using ::tanh;
 
 // Number of tangent directions a forward-mode step carries. Four keeps the
-// dual element kernels within reach of the register file; with eight, the
-// optimised build of the dual gather kernel computed wrong values on sm_103a
-// (CUDA 13.0) while the unoptimised (-G) build and the host build agreed, so
-// more directions are carried by more passes or by copies of a cloth in one
+// dual element kernels within reach of the register file. With eight, the
+// dual gather k_gather<Dual<8>> computes wrong values on sm_103a (CUDA 13.0)
+// whenever the compiler front end optimises it (-Xcicc -O1 and above; every
+// ptxas level alike), while its -Xcicc -O0 build, the -G build and the host
+// build under address and undefined-behaviour sanitizers are right; so more
+// directions are carried by more passes or by copies of a cloth in one
 // batch, each with its own seeds.
 constexpr int kTangents = 4;
 
