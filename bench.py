@@ -580,7 +580,31 @@ def main():
     }
     precond = None
     if rank == 0 and not args.no_precond:
+        # the learned preconditioner on this workload itself, after the runs
+        # above, in the schedule they used (the state keeps advancing)
+        net = ys.LearnedPreconditioner.pretrained(device=dev)
+        on_workload = {}
+        for kind in ("jacobi", "learned_refresh4"):
+            if kind != "jacobi":
+                batch.set_preconditioner("learned", net)
+                batch.precond_refresh(4)
+            for _ in range(2):
+                do_step()
+            ts, its = [], []
+            for _ in range(8):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                st = do_step()
+                torch.cuda.synchronize()
+                ts.append((time.perf_counter() - t0) * 1e3)
+                assert all(x["ok"] and x["cg_error"] <= TOL for x in st)
+                its.append(max(x["cg_iterations"] for x in st))
+            on_workload[kind] = {"step_ms": float(np.median(ts)), "max_iterations": float(np.mean(its))}
+        on_workload["fallbacks"] = batch.precond_info()["fallbacks"]
+        batch.set_preconditioner("jacobi")
+        net.close()
         precond = precond_compare(ys, dev)
+        precond["bench_workload"] = on_workload
     collision = None
     if rank == 0 and not args.no_collision:
         collision = collision_compare(ys, dev)
