@@ -221,7 +221,7 @@ def main(argv=None):
     import argparse
     import time
     ap = argparse.ArgumentParser()
-    ap.add_argument("--systems", type=int, default=20000)
+    ap.add_argument("--systems", type=int, default=800000)
     ap.add_argument("--cloths", type=int, default=64)
     ap.add_argument("--steps-per-batch", type=int, default=40)
     ap.add_argument("--lr", type=float, default=2e-3)
