@@ -1918,7 +1918,7 @@ ys_status learn_ensure(ys_batch* b) {
   A(&g.act, 3 * (size_t)ys::kGHid * nt);
   A(&g.o, (size_t)ys::kGOut * nt);
   A(&g.G, (size_t)ys::kGUsed * nt);
-  A(&g.Gh, (size_t)ys::kGUsed * nt);
+  A(&g.Gh, (size_t)ys::kGPairs * nt);
   A(&g.Gn, (size_t)ys::kGUsed * nt);
   A(&g.Nt, (size_t)ys::kGUsed * nt);
   A(&g.vec, 4 * 5 * (size_t)nt);

@@ -602,8 +602,8 @@ __global__ void __launch_bounds__(kNB, 8) k_gnn_g(GnnBufs g, int keep_n) {
   const int b = (int)(t / nt), n = (int)(t - (int64_t)b * nt);
   const int j = g.pat[8 * n + b];
   if (j < 0) {
+    for (int q = 0; q < 13; ++q) g.Gh[(int64_t)(13 * b + q) * nt + n] = __floats2bfloat162_rn(0.f, 0.f);
     for (int k = 0; k < 25; ++k) {
-      g.Gh[(int64_t)(25 * b + k) * nt + n] = __float2bfloat16(0.f);
       if (keep_n) g.G[(int64_t)(25 * b + k) * nt + n] = 0.f;
       if (keep_n) g.Gn[(int64_t)(25 * b + k) * nt + n] = 0.f;
     }
@@ -628,19 +628,19 @@ __global__ void __launch_bounds__(kNB, 8) k_gnn_g(GnnBufs g, int keep_n) {
     for (int r = 0; r < 5; ++r) N[r][r] += 1.f;
   mul_ab(N, L, Gb);
 #pragma unroll
-  for (int r = 0; r < 5; ++r)
+  for (int q = 0; q < 13; ++q)
+    g.Gh[(int64_t)(13 * b + q) * nt + n] =
+        __floats2bfloat162_rn(Gb[(2 * q) / 5][(2 * q) % 5], 2 * q + 1 < 25 ? Gb[(2 * q + 1) / 5][(2 * q + 1) % 5] : 0.f);
+  if (keep_n)
 #pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      const int64_t at = (int64_t)(25 * b + 5 * r + c) * nt + n;
-      g.Gh[at] = __float2bfloat16(Gb[r][c]);
-      if (keep_n) g.G[at] = Gb[r][c];
-    }
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) g.G[(int64_t)(25 * b + 5 * r + c) * nt + n] = Gb[r][c];
 }
 
 // ------------------------------------------------- blocked applications
-// G coefficients as FP32, from FP32 (training) or BF16 (the solve) storage
+// a G coefficient of the FP32 copy (training)
 __device__ __forceinline__ float coef(const float* g, int64_t i) { return g[i]; }
-__device__ __forceinline__ float coef(const bf16* g, int64_t i) { return __bfloat162float(g[i]); }
 
 // z_n = sum over the rows i = upat(n, b) of G_i,b^T x_i
 template <class TG, class TX>
@@ -772,15 +772,16 @@ __global__ void __launch_bounds__(kBlock, 6) k_lp_prec(View v, Blocks b, Solver 
 #pragma unroll
         for (int cc = 0; cc < 5; ++cc) xs[bb][cc] = m * lx.rf[(int64_t)cc * nt + j];
       }
+      // coefficient k = 5 r + c of block bb comes with its pair; each y[r]
+      // sums in block, then column order
 #pragma unroll
-      for (int r = 0; r < 5; ++r) {
-        float acc = 0.f;
+      for (int bb = 0; bb < kGBlocks; ++bb)
 #pragma unroll
-        for (int bb = 0; bb < kGBlocks; ++bb)
-#pragma unroll
-          for (int cc = 0; cc < 5; ++cc) acc += coef(lx.G, (int64_t)(25 * bb + 5 * r + cc) * nt + i) * xs[bb][cc];
-        y[r] = acc;
-      }
+        for (int q = 0; q < 13; ++q) {
+          const float2 g2 = __bfloat1622float2(lx.G[(int64_t)(13 * bb + q) * nt + i]);
+          y[(2 * q) / 5] += g2.x * xs[bb][(2 * q) % 5];
+          if (2 * q + 1 < 25) y[(2 * q + 1) / 5] += g2.y * xs[bb][(2 * q + 1) % 5];
+        }
     }
 #pragma unroll
     for (int cc = 0; cc < 5; ++cc) ys_[cc][e] = y[cc];
@@ -798,9 +799,11 @@ __global__ void __launch_bounds__(kBlock, 6) k_lp_prec(View v, Blocks b, Solver 
       const int i = n - du - dv * W;
       const int ei = i - (dv == 0 ? yoff0 : dv == -1 ? yoff1 : yoff2);
 #pragma unroll
-      for (int cc = 0; cc < 5; ++cc)
-#pragma unroll
-        for (int r = 0; r < 5; ++r) z[cc] += coef(lx.G, (int64_t)(25 * bb + 5 * r + cc) * nt + i) * ys_[r][ei];
+      for (int q = 0; q < 13; ++q) {
+        const float2 g2 = __bfloat1622float2(lx.G[(int64_t)(13 * bb + q) * nt + i]);
+        z[(2 * q) % 5] += g2.x * ys_[(2 * q) / 5][ei];
+        if (2 * q + 1 < 25) z[(2 * q + 1) % 5] += g2.y * ys_[(2 * q + 1) / 5][ei];
+      }
     }
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
@@ -1305,11 +1308,6 @@ __global__ void k_msg_bwd(const float* dm, const int* nbr, float* dh, int ntot, 
   }
   dh[i] = s;
 }
-__global__ void k_copy_f(const float* a, float* b, int count) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < count) b[i] = a[i];
-}
-
 // Adam on the FP32 master parameters
 __global__ void k_adam(float* w, const float* grad, float* m, float* v, int count, float lr, float b1, float b2,
                        float eps, float c1, float c2) {

@@ -41,6 +41,9 @@ namespace ys {
 
 constexpr int kGIn = 128, kGHid = 64, kGMsg = 320, kGOut = 192, kGLayers = 3, kGBlocks = 7, kGUsed = 25 * kGBlocks;
 constexpr float kGOutScale = 0.1f;
+// the solve's BF16 copy of G holds each block's 25 coefficients in 13 pairs
+// (the last padded with zero): pair q of block b of node n at [13 b + q][n]
+constexpr int kGPairs = 13 * kGBlocks;
 // packed FP32 parameter vector: W0 [64][128], b0, then per layer W [64][320], b,
 // then Wh [192][64], bh
 constexpr int kPW0 = 0;
@@ -82,7 +85,7 @@ struct GnnBufs {  // device arrays sized for ntot nodes
   __nv_bfloat16* act;   // [3][ntot][64] relu outputs of the message layers
   float* o;             // [192][ntot] network outputs (component-major)
   float* G;             // [175][ntot] blocks of G, row-major 5 x 5 (training, export)
-  __nv_bfloat16* Gh;    // [175][ntot] the same in BF16 (the solve's preconditioner)
+  __nv_bfloat162* Gh;   // [kGPairs][ntot] the same in BF16 pairs (the solve's preconditioner)
   float* Gn;            // [175][ntot] blocks of N (training)
   float* Nt;            // [175][ntot] the exact FSAI's blocks of N (the FSAI objective's target)
   float* vec;           // [4][5][ntot] training vectors (w, u, t, s)
@@ -99,7 +102,7 @@ struct GnnBufs {  // device arrays sized for ntot nodes
 
 // learned-preconditioner PCG state lives in Solver; these hold its extras
 struct LpcgExtra {
-  const __nv_bfloat16* G;  // [175][ntot]
+  const __nv_bfloat162* G;  // [kGPairs][ntot]
   float* rf;        // [5][ntot] the residual in FP32, as the preconditioner reads it
   double* z;        // [5][ntot] G^T G r
 };
