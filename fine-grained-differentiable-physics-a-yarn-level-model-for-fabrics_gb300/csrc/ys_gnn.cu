@@ -847,16 +847,31 @@ __global__ void __launch_bounds__(kBlock) k_lp_dir(View v, Blocks b, Solver so, 
                                                     int it_local) {
   __shared__ int go_sh;
   __shared__ double beta_sh;
+  __shared__ double sums_sh[4];
   const int blk = blockIdx.x;
   const int c = b.blk_cloth[blk];
   PcgCloth& pc = so.pc[c];
   if (!pc.active) return;
+  // the four cloth sums (p.q, |r|^2, r.z, z.q), each in block order, in four
+  // lanes at once; the direction's operands load meanwhile
+  const int n = b.blk_node0[blk] + threadIdx.x;
+  const int nt = v.ntot;
+  const bool own = threadIdx.x < b.blk_count[blk];
+  double zk[5], pk[5];
+  if (own)
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      zk[k] = lx.z[(int64_t)k * nt + n];
+      pk[k] = ld(so.p, k, nt, n);
+    }
+  if (threadIdx.x < 4) sums_sh[threadIdx.x] = cl_sum(b, so.part, threadIdx.x, c);
+  __syncthreads();
   if (threadIdx.x == 0) {
     const int it = so.it_base ? *so.it_base + it_local : it_local;
-    const double rr = cl_sum(b, so.part, 1, c);
-    const double rzn = cl_sum(b, so.part, 2, c);
-    const double zq = cl_sum(b, so.part, 3, c);
-    const double alpha = pc.rz[parity] / cl_sum(b, so.part, 0, c);
+    const double rr = sums_sh[1];
+    const double rzn = sums_sh[2];
+    const double zq = sums_sh[3];
+    const double alpha = pc.rz[parity] / sums_sh[0];
     const bool lead = blk == b.cloth_blk0[c];
     const bool conv = rr < pc.thr;
     const bool cap = !conv && it + 1 >= pc.maxiter;
@@ -877,11 +892,9 @@ __global__ void __launch_bounds__(kBlock) k_lp_dir(View v, Blocks b, Solver so, 
   __syncthreads();
   if (!go_sh || !isfinite(beta_sh)) return;
   const double beta = beta_sh;
-  const int n = b.blk_node0[blk] + threadIdx.x;
-  const int nt = v.ntot;
-  if (threadIdx.x < b.blk_count[blk])
-    for (int k = 0; k < 5; ++k)
-      st(so.p, k, nt, n) = lx.z[(int64_t)k * nt + n] + beta * ld(so.p, k, nt, n);
+  if (own)
+#pragma unroll
+    for (int k = 0; k < 5; ++k) st(so.p, k, nt, n) = zk[k] + beta * pk[k];
 }
 
 // ------------------------------------------------------------- training
