@@ -419,6 +419,8 @@ def main():
     ap.add_argument("--drop-steps", type=int, default=1000,
                     help="steps of the 50x50 drop-onto-sphere scene (0: skip it)")
     ap.add_argument("--profile", action="store_true", help="print the per-kernel table to stderr")
+    ap.add_argument("--precond-only", action="store_true",
+                    help="run only the learned-vs-Jacobi comparison and print its JSON (a profiling target)")
     ap.add_argument("--schedule", default="auto", choices=["auto", "graph", "launch", "persistent"],
                     help="auto: ys_autotune picks graph or launch-by-launch steps and the PCG schedule; "
                          "graph: one CUDA graph launch per step (conditional PCG loop); launch: kernel by kernel; "
@@ -465,6 +467,9 @@ def main():
         dist.init_process_group("nccl")
     dev = local_rank
     torch.cuda.set_device(dev)
+    if args.precond_only:
+        print(json.dumps({"precond": precond_compare(ys, dev)}))
+        return 0
 
     batch = ys.ClothBatch([ys.ClothSpec(**s) for s in specs], device=dev)
     if args.schedule == "auto":
