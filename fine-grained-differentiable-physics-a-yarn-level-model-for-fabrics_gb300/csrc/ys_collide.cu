@@ -140,6 +140,9 @@ struct BroadArgs {
   // here ([work][kBroadKeep]); the write pass copies them instead of
   // traversing again when that is all of them
   int* keep;
+  // write pass: pair slots available (a pair at or past it is not written
+  // and sets bit 1 of *overflow)
+  int64_t cap;
 };
 constexpr int kBroadKeep = 16;
 
@@ -161,6 +164,10 @@ __global__ void k_broad(BroadArgs a) {
     // every partner was kept by the count pass, in traversal order
     const int64_t o = a.offset[idx], nk = a.count[idx];
     for (int64_t j = 0; j < nk; ++j) {
+      if (o + j >= a.cap) {
+        atomicOr(a.overflow, 2);
+        break;
+      }
       a.out[3 * (o + j)] = f;
       a.out[3 * (o + j) + 1] = a.keep[idx * kBroadKeep + j];
       a.out[3 * (o + j) + 2] = pass;
@@ -191,9 +198,13 @@ __global__ void k_broad(BroadArgs a) {
         if (!kdop_overlap_f(bfl, t.fbox + 18 * (int64_t)n, a.thick1, a.thick2)) continue;
         if (!ys::kdop_overlap(bf, t.box[n], a.thickness)) continue;
         if (WRITE) {
-          a.out[3 * (o + c)] = f;
-          a.out[3 * (o + c) + 1] = g;
-          a.out[3 * (o + c) + 2] = pass;
+          if (o + c < a.cap) {
+            a.out[3 * (o + c)] = f;
+            a.out[3 * (o + c) + 1] = g;
+            a.out[3 * (o + c) + 2] = pass;
+          } else {
+            atomicOr(a.overflow, 2);
+          }
         } else if (c < kBroadKeep) {
           a.keep[idx * kBroadKeep + c] = g;
         }
@@ -234,11 +245,18 @@ struct NodeKdops {
   int n_nodes;
   __device__ __forceinline__ Kdop operator()(int id) const { return k[id >= 0 ? id : n_nodes + (-1 - id)]; }
 };
+// (np_dev: the pair count on the device, the launch covering npairs >= it
+// entries, or null: npairs pairs)
 __global__ void k_narrow_mask(const int* __restrict__ pairs, int64_t npairs, const CFace* __restrict__ faces,
                               const CFace* __restrict__ ofaces, NodeKdops nk, double thickness,
-                              int* __restrict__ mask, int64_t* __restrict__ count) {
+                              int* __restrict__ mask, int64_t* __restrict__ count, const int64_t* np_dev) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npairs) return;
+  if (np_dev && p >= *np_dev) {
+    count[p] = 0;  // the scan of the impact counts covers the launch's npairs entries
+    mask[p] = 0;
+    return;
+  }
   const CFace& f0 = faces[pairs[3 * p]];
   const CFace& f1 = pairs[3 * p + 2] ? ofaces[pairs[3 * p + 1]] : faces[pairs[3 * p + 1]];
   mask[p] = ys::cc_face_pair_mask(nk, f0, f1, thickness);
@@ -251,6 +269,7 @@ __global__ void k_narrow_test(const int* __restrict__ pairs, int64_t npairs, con
   if (idx >= 15 * npairs) return;
   const int t = (int)(idx / npairs);
   const int64_t p = idx - (int64_t)t * npairs;
+  // (pairs past a device count have mask 0: k_narrow_mask)
   Impact& out = slots[15 * p + t];
   out.type = -1;
   if (!((mask[p] >> t) & 1)) return;
@@ -272,14 +291,22 @@ __global__ void k_narrow_test(const int* __restrict__ pairs, int64_t npairs, con
   }
 }
 
+// (np_dev as for k_narrow_mask; impacts at or past cap are not written and
+// set bit 2 of *overflow)
 __global__ void k_compact(const Impact* __restrict__ slots, const int64_t* __restrict__ count,
-                          const int64_t* __restrict__ offset, int64_t npairs, ys_impact* out) {
+                          const int64_t* __restrict__ offset, int64_t npairs, ys_impact* out,
+                          const int64_t* np_dev, int64_t cap, int* overflow) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npairs) return;
+  if (np_dev && p >= *np_dev) return;
   int64_t k = 0;
   for (int t = 0; t < 15 && k < count[p]; ++t) {
     const Impact& s = slots[15 * p + t];
     if (s.type < 0) continue;
+    if (offset[p] + k >= cap) {
+      atomicOr(overflow, 4);
+      return;
+    }
     ys_impact& r = out[offset[p] + k++];
     r.type = s.type;
     for (int q = 0; q < 4; ++q) r.nodes[q] = s.node[q];
@@ -414,6 +441,12 @@ struct ys_collider {
   int64_t nimpacts = 0;
   DVec<int> overflow;
   int64_t* pin = nullptr;  // pinned host words: [0] a scan's total, [1] the broad phase's overflow flag
+  // one-wait detection rounds: capacities of the pair and impact buffers
+  // (by round kind: [0] every face, [1] the active faces of later rounds,
+  // which find far fewer pairs), and the pinned copy of the impacts
+  int64_t cap_pairs[2] = {4096, 1024}, cap_imp[2] = {1024, 256};
+  ys_impact* pin_imp = nullptr;
+  int64_t pin_imp_cap = 0;
   bool have_pairs = false, have_impacts = false;
   // impact-zone response
   DVec<uint8_t> face_active, node_active;
@@ -428,6 +461,7 @@ struct ys_collider {
   DVec<int> cslice, oslice;
   ~ys_collider() {
     if (pin) cudaFreeHost(pin);
+    if (pin_imp) cudaFreeHost(pin_imp);
   }
 };
 
@@ -486,6 +520,19 @@ ys_status refit(ys_collider* c, bool obstacle) {
 // Exclusive scan of counts into off; *total_host receives the sum. With
 // flag, the device word is read back in the same wait (into *flag_host).
 // One host wait per scan.
+// the scan's kernels alone: exclusive scan of counts[n] into off, the total
+// into *total_dev (the tile sums in c->sums, reserved by the caller)
+void scan_kernels(ys_collider* c, const int64_t* counts, int64_t n, int64_t* off, int64_t* total_dev) {
+  const int64_t nb = (n + kScanTile - 1) / kScanTile;
+  if (n > 0) {
+    k_scan_tiles<<<(unsigned)nb, kScanThreads, 0, c->stream>>>(counts, n, off, c->sums.p);
+    k_scan_sums<<<1, kScanThreads, 0, c->stream>>>(c->sums.p, nb, total_dev);
+    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(off, n, c->sums.p);
+  } else {
+    cudaMemsetAsync(total_dev, 0, sizeof(int64_t), c->stream);
+  }
+}
+
 ys_status scan(ys_collider* c, const int64_t* counts, int64_t n, int64_t* off, int64_t* total_host,
                const int* flag = nullptr, int* flag_host = nullptr) {
   const int64_t nb = (n + kScanTile - 1) / kScanTile;
@@ -544,15 +591,17 @@ ys_status upload_slices(ys_collider* c, bool obstacle) {
   return YS_OK;
 }
 
-ys_status broad_phase(ys_collider* c, bool masked) {
+// the broad phase's arguments (the write pass's offsets, output and capacity
+// are filled in by the caller); reserves the per-(face, slice) buffers
+ys_status broad_args(ys_collider* c, bool masked, BroadArgs& a, int64_t& work) {
   const int ncs = (int)c->h_cslice.size(), nos = (int)c->h_oslice.size();
-  const int64_t work = (int64_t)c->n_faces * (ncs + nos);
+  work = (int64_t)c->n_faces * (ncs + nos);
   // the per-(face, slice) counts and offsets: sized before any pointer to
   // them is taken (a reserve may move them)
   YC_CUDA(c->counts.reserve(std::max<int64_t>(work, 1)));
   YC_CUDA(c->offsets.reserve(std::max<int64_t>(work, 1)));
   YC_CUDA(c->keep.reserve(std::max<int64_t>(work * kBroadKeep, 1)));
-  BroadArgs a{};
+  a = BroadArgs{};
   a.cloth = DevTree{c->c_left.p, c->c_right.p, c->c_face.p, c->c_box.p, (int)c->ct.face.size(), c->c_fbox.p};
   a.obs = DevTree{c->o_left.p, c->o_right.p, c->o_face.p, c->o_box.p, (int)c->ot.face.size(), c->o_fbox.p};
   a.thick1 = (float)(c->thickness * (1.0 + 1e-6));
@@ -571,12 +620,20 @@ ys_status broad_phase(ys_collider* c, bool masked) {
   a.ncs = ncs;
   a.nos = nos;
   a.keep = c->keep.p;
+  return YS_OK;
+}
+
+ys_status broad_phase(ys_collider* c, bool masked) {
+  BroadArgs a;
+  int64_t work = 0;
+  ys_status s = broad_args(c, masked, a, work);
+  if (s != YS_OK) return s;
   YC_CUDA(cudaMemsetAsync(c->overflow.p, 0, sizeof(int), c->stream));
   const unsigned g = (unsigned)((work + kBroadBlock - 1) / kBroadBlock);
   if (work) k_broad<false><<<g, kBroadBlock, 0, c->stream>>>(a);
   YC_CUDA(cudaGetLastError());
   int ovf = 0;
-  ys_status s = scan(c, c->counts.p, work, c->offsets.p, &c->npairs, c->overflow.p, &ovf);
+  s = scan(c, c->counts.p, work, c->offsets.p, &c->npairs, c->overflow.p, &ovf);
   if (s != YS_OK) return s;
   if (ovf) return ys_internal_fail(YS_ERR_ARG, "BVH deeper than the traversal stack");
   // a face pairs at most once with every other face
@@ -585,6 +642,7 @@ ys_status broad_phase(ys_collider* c, bool masked) {
   YC_CUDA(c->pairs.reserve(3 * (size_t)std::max<int64_t>(c->npairs, 1)));
   a.offset = c->offsets.p;
   a.out = c->pairs.p;
+  a.cap = c->npairs;
   if (work) k_broad<true><<<g, kBroadBlock, 0, c->stream>>>(a);
   YC_CUDA(cudaGetLastError());
   // no wait: the pairs are read on the stream (narrow phase) or by a
@@ -607,7 +665,7 @@ ys_status narrow_phase(ys_collider* c) {
     k_node_kdop<<<(nn + 127) / 128, 128, 0, c->stream>>>(m, c->n_nodes, c->n_obs_nodes, c->ccd, c->nkdop.p);
     k_narrow_mask<<<(unsigned)((P + 127) / 128), 128, 0, c->stream>>>(c->pairs.p, P, c->faces.p, c->ofaces.p,
                                                                        NodeKdops{c->nkdop.p, c->n_nodes},
-                                                                       c->thickness, c->tmask.p, c->icount.p);
+                                                                       c->thickness, c->tmask.p, c->icount.p, nullptr);
     k_narrow_test<<<(unsigned)((15 * P + 127) / 128), 128, 0, c->stream>>>(
         c->pairs.p, P, c->faces.p, c->ofaces.p, m, c->tmask.p, c->slots.p,
         reinterpret_cast<unsigned long long*>(c->icount.p));
@@ -618,12 +676,94 @@ ys_status narrow_phase(ys_collider* c) {
   YC_CUDA(c->impacts.reserve(std::max<int64_t>(c->nimpacts, 1)));
   if (P) {
     k_compact<<<(unsigned)((P + 127) / 128), 128, 0, c->stream>>>(c->slots.p, c->icount.p, c->ioffset.p, P,
-                                                                   c->impacts.p);
+                                                                   c->impacts.p, nullptr, c->nimpacts,
+                                                                   c->overflow.p);
     YC_CUDA(cudaGetLastError());
   }
   // no wait: the impacts are read by a synchronous copy on this stream
   c->have_impacts = true;
   return YS_OK;
+}
+
+// One detection round of the impact-zone response with a single wait: the
+// pair and impact counts stay on the device, and the narrow phase, the scans
+// and the compaction run over buffers sized by capacities the collider
+// keeps (grown from the counts a round finds). The counts, the overflow
+// flags and up to cap_imp impacts come back in one copy. A round whose pairs
+// or impacts outgrew the capacities (flag bits 1, 2) is run again with
+// capacities that hold them; its pair list, impacts and their order are the
+// two-wait path's (the same kernels over the same counts).
+ys_status detect_one_wait(ys_collider* c, bool masked, std::vector<ys_impact>& got) {
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    BroadArgs a;
+    int64_t work = 0;
+    ys_status s = broad_args(c, masked, a, work);
+    if (s != YS_OK) return s;
+    const int kind = masked ? 1 : 0;
+    const int64_t cp = c->cap_pairs[kind], ci = c->cap_imp[kind];
+    const int64_t nb = (std::max<int64_t>(work, cp) + kScanTile - 1) / kScanTile;
+    YC_CUDA(c->sums.reserve(std::max<int64_t>(nb, 1)));
+    YC_CUDA(c->total.reserve(2));
+    YC_CUDA(c->pairs.reserve(3 * (size_t)cp));
+    YC_CUDA(c->slots.reserve(15 * (size_t)cp));
+    YC_CUDA(c->icount.reserve(cp));
+    YC_CUDA(c->ioffset.reserve(cp));
+    YC_CUDA(c->tmask.reserve(cp));
+    YC_CUDA(c->nkdop.reserve(std::max(c->n_nodes + c->n_obs_nodes, 1)));
+    YC_CUDA(c->impacts.reserve(ci));
+    if (c->pin_imp_cap < ci) {
+      if (c->pin_imp) cudaFreeHost(c->pin_imp);
+      c->pin_imp = nullptr;
+      c->pin_imp_cap = 0;
+      YC_CUDA(cudaMallocHost(reinterpret_cast<void**>(&c->pin_imp), sizeof(ys_impact) * (size_t)ci));
+      c->pin_imp_cap = ci;
+    }
+    int64_t* np_dev = c->total.p;      // pairs
+    int64_t* ni_dev = c->total.p + 1;  // impacts
+    YC_CUDA(cudaMemsetAsync(c->overflow.p, 0, sizeof(int), c->stream));
+    const unsigned g = (unsigned)((work + kBroadBlock - 1) / kBroadBlock);
+    if (work) k_broad<false><<<g, kBroadBlock, 0, c->stream>>>(a);
+    scan_kernels(c, c->counts.p, work, c->offsets.p, np_dev);
+    a.offset = c->offsets.p;
+    a.out = c->pairs.p;
+    a.cap = cp;
+    if (work) k_broad<true><<<g, kBroadBlock, 0, c->stream>>>(a);
+    CMesh m{c->x.p, c->xp.p, c->ox.p, c->oxp.p};
+    const int nn = c->n_nodes + c->n_obs_nodes;
+    k_node_kdop<<<(nn + 127) / 128, 128, 0, c->stream>>>(m, c->n_nodes, c->n_obs_nodes, c->ccd, c->nkdop.p);
+    k_narrow_mask<<<(unsigned)((cp + 127) / 128), 128, 0, c->stream>>>(c->pairs.p, cp, c->faces.p, c->ofaces.p,
+                                                                        NodeKdops{c->nkdop.p, c->n_nodes},
+                                                                        c->thickness, c->tmask.p, c->icount.p,
+                                                                        np_dev);
+    k_narrow_test<<<(unsigned)((15 * cp + 127) / 128), 128, 0, c->stream>>>(
+        c->pairs.p, cp, c->faces.p, c->ofaces.p, m, c->tmask.p, c->slots.p,
+        reinterpret_cast<unsigned long long*>(c->icount.p));
+    scan_kernels(c, c->icount.p, cp, c->ioffset.p, ni_dev);
+    k_compact<<<(unsigned)((cp + 127) / 128), 128, 0, c->stream>>>(c->slots.p, c->icount.p, c->ioffset.p, cp,
+                                                                    c->impacts.p, np_dev, ci, c->overflow.p);
+    YC_CUDA(cudaGetLastError());
+    YC_CUDA(cudaMemcpyAsync(c->pin, c->total.p, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    YC_CUDA(cudaMemcpyAsync(c->pin + 2, c->overflow.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    YC_CUDA(cudaMemcpyAsync(c->pin_imp, c->impacts.p, sizeof(ys_impact) * (size_t)ci, cudaMemcpyDeviceToHost,
+                            c->stream));
+    YC_CUDA(cudaStreamSynchronize(c->stream));
+    const int64_t np = c->pin[0], ni = c->pin[1];
+    const int ovf = (int)(reinterpret_cast<const int*>(c->pin + 2)[0]);
+    if (ovf & 1) return ys_internal_fail(YS_ERR_ARG, "BVH deeper than the traversal stack");
+    if (np < 0 || np > (int64_t)c->n_faces * ((int64_t)c->n_faces + c->n_obs_faces))
+      return ys_internal_fail(YS_ERR_CUDA, "broad phase produced an impossible pair count");
+    c->npairs = np;
+    c->nimpacts = ni;
+    if (ovf & 6) {  // grow and run the round again
+      c->cap_pairs[kind] = std::max(c->cap_pairs[kind], np + np / 2 + 1024);
+      c->cap_imp[kind] = std::max(c->cap_imp[kind], ni + ni / 2 + 256);
+      continue;
+    }
+    c->have_pairs = c->have_impacts = true;
+    got.assign(c->pin_imp, c->pin_imp + ni);
+    return YS_OK;
+  }
+  return ys_internal_fail(YS_ERR_CUDA, "detection round: capacities did not settle");
 }
 
 // marks the cloth-tree nodes with an active leaf below (host tree)
@@ -912,15 +1052,8 @@ ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h,
               cudaSuccess)
         return fail(ys_internal_fail(YS_ERR_CUDA, "cudaMemcpyAsync failed"));
     }
-    ys_status s = broad_phase(c, mask != nullptr);
+    ys_status s = detect_one_wait(c, mask != nullptr, got);
     if (s != YS_OK) return fail(s);
-    if ((s = narrow_phase(c)) != YS_OK) return fail(s);
-    got.resize((size_t)c->nimpacts);
-    if (c->nimpacts &&
-        (cudaMemcpyAsync(got.data(), c->impacts.p, sizeof(ys_impact) * c->nimpacts, cudaMemcpyDeviceToHost,
-                         c->stream) != cudaSuccess ||
-         cudaStreamSynchronize(c->stream) != cudaSuccess))
-      return fail(ys_internal_fail(YS_ERR_CUDA, "cudaMemcpy failed"));
     out.resize(got.size());
     for (size_t i = 0; i < got.size(); ++i) {
       ys::ZImpact& z = out[i];
