@@ -11,8 +11,13 @@
 // reference reports.
 #pragma once
 
+#include <algorithm>
+#include <condition_variable>
 #include <cstdint>
+#include <functional>
 #include <future>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "ys_collide.cuh"
@@ -25,6 +30,77 @@ struct BvhTree {
   std::vector<int> rank;                      // per face: leaf order left to right
   std::vector<int> upper;                     // per face: index of its upper node
   int max_depth = 0;
+};
+
+// A few host threads kept for the tree builds (a collider builds its cloth's
+// tree every step; creating threads each time would cost what they save).
+// run(n, f) calls f(0) ... f(n - 1) on the pool's threads and the caller's
+// and returns when all have returned.
+class BuildPool {
+ public:
+  explicit BuildPool(int threads) {
+    for (int i = 0; i + 1 < threads; ++i) workers_.emplace_back([this] { loop(); });
+  }
+  ~BuildPool() {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (std::thread& t : workers_) t.join();
+  }
+  int size() const { return (int)workers_.size() + 1; }
+  void run(int n, const std::function<void(int)>& f) {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      job_ = &f;
+      njob_ = n;
+      next_ = 0;
+      left_ = n;
+      ++gen_;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> l(mu_);
+    done_.wait(l, [this] { return left_ == 0; });
+    job_ = nullptr;
+  }
+
+ private:
+  void work() {
+    for (;;) {
+      int i;
+      const std::function<void(int)>* f;
+      {
+        std::lock_guard<std::mutex> g(mu_);
+        if (!job_ || next_ >= njob_) return;
+        i = next_++;
+        f = job_;
+      }
+      (*f)(i);
+      std::lock_guard<std::mutex> g(mu_);
+      if (--left_ == 0) done_.notify_all();
+    }
+  }
+  void loop() {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> l(mu_);
+        cv_.wait(l, [&] { return stop_ || gen_ != seen; });
+        if (stop_) return;
+        seen = gen_;
+      }
+      work();
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex mu_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)>* job_ = nullptr;
+  int njob_ = 0, next_ = 0, left_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
 };
 
 namespace bvh_detail {
@@ -68,19 +144,10 @@ struct Builder {
     t.depth[idx] = dep;
     t.leaf_of_face[f] = idx;
   }
-  void node(int* lst, int num, int dep, int idx, int threads) {
-    if (num == 1) {
-      leaf(lst[0], dep, idx);
-      return;
-    }
+  // the node's own work for num >= 3 faces: its box, split plane and
+  // partition of lst; fills its entry and returns the left child's face count
+  int split_node(int* lst, int num, int dep, int idx) {
     t.depth[idx] = dep;
-    if (num == 2) {
-      t.left[idx] = idx + 1;
-      t.right[idx] = idx + 2;
-      leaf(lst[0], dep + 1, idx + 1);
-      leaf(lst[1], dep + 1, idx + 2);
-      return;
-    }
     double lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     for (int q = 0; q < num; ++q) {
       const double* e = &ext[6 * (size_t)lst[q]];
@@ -105,6 +172,22 @@ struct Builder {
     const int split = (left_idx == 0 || (int)left_idx == num) ? hal : (int)left_idx;
     t.left[idx] = idx + 1;
     t.right[idx] = idx + 2 * split;
+    return split;
+  }
+  void node(int* lst, int num, int dep, int idx, int threads) {
+    if (num == 1) {
+      leaf(lst[0], dep, idx);
+      return;
+    }
+    if (num == 2) {
+      t.depth[idx] = dep;
+      t.left[idx] = idx + 1;
+      t.right[idx] = idx + 2;
+      leaf(lst[0], dep + 1, idx + 1);
+      leaf(lst[1], dep + 1, idx + 2);
+      return;
+    }
+    const int split = split_node(lst, num, dep, idx);
     if (threads > 1 && num > 8192) {
       auto lf = std::async(std::launch::async, [=] { node(lst, split, dep + 1, idx + 1, threads / 2); });
       node(lst + split, num - split, dep + 1, idx + 2 * split, threads - threads / 2);
@@ -114,6 +197,21 @@ struct Builder {
       node(lst + split, num - split, dep + 1, idx + 2 * split, 1);
     }
   }
+  // the subtrees under the first levels, for a pool: splits nodes of more
+  // than `min_faces` faces until depth `top`, recording each subtree left
+  struct Task {
+    int* lst;
+    int num, dep, idx;
+  };
+  void top(int* lst, int num, int dep, int idx, int depth_left, int min_faces, std::vector<Task>& out) {
+    if (depth_left == 0 || num <= min_faces || num < 3) {
+      out.push_back({lst, num, dep, idx});
+      return;
+    }
+    const int split = split_node(lst, num, dep, idx);
+    top(lst, split, dep + 1, idx + 1, depth_left - 1, min_faces, out);
+    top(lst + split, num - split, dep + 1, idx + 2 * split, depth_left - 1, min_faces, out);
+  }
 };
 
 }  // namespace bvh_detail
@@ -122,53 +220,82 @@ struct Builder {
 // under CCD); face v[k] are node ids into x (this routine never sees
 // obstacle ids). verts: the mesh's vertex order for the root box (node ids).
 inline BvhTree bvh_build(int nfaces, const int* fv, int nverts, const int* verts, const double* x, const double* xp,
-                         bool ccd) {
+                         bool ccd, BuildPool* pool = nullptr) {
   BvhTree t;
   t.leaf_of_face.assign(nfaces, -1);
   t.rank.assign(nfaces, 0);
   t.upper.assign(nfaces, 0);
   if (nfaces == 0) return t;
+  // with a pool (and enough faces) the vertex box, the faces' geometry and
+  // the subtrees below the first levels are computed on its threads: min /
+  // max bounds do not depend on the grouping, the root's partition stays a
+  // pass in face order, and disjoint subtrees give the same tree
+  const bool par = pool && pool->size() > 1 && nfaces >= 2048;
+  const int nch = par ? pool->size() : 1;
+  auto chunk = [&](int ch, int n, int& lo, int& hi) {
+    lo = (int)((int64_t)n * ch / nch);
+    hi = (int)((int64_t)n * (ch + 1) / nch);
+  };
   Kdop total;
   kdop_empty(total);
-  for (int i = 0; i < nverts; ++i) {
-    kdop_add_point(total, x + 3 * (size_t)verts[i]);
-    if (ccd) kdop_add_point(total, xp + 3 * (size_t)verts[i]);
+  {
+    std::vector<Kdop> part(nch);
+    auto vbox = [&](int ch) {
+      int lo, hi;
+      chunk(ch, nverts, lo, hi);
+      kdop_empty(part[ch]);
+      for (int i = lo; i < hi; ++i) {
+        kdop_add_point(part[ch], x + 3 * (size_t)verts[i]);
+        if (ccd) kdop_add_point(part[ch], xp + 3 * (size_t)verts[i]);
+      }
+    };
+    if (par) pool->run(nch, vbox);
+    else vbox(0);
+    for (int ch = 0; ch < nch; ++ch) kdop_add(total, part[ch]);
   }
   std::vector<double> ext(6 * (size_t)nfaces);
   std::vector<double> centers(3 * (size_t)nfaces);
   const bvh_detail::Aap pln(total);
+  auto face_geom = [&](int ch) {
+    int lo, hi;
+    chunk(ch, nfaces, lo, hi);
+    for (int f = lo; f < hi; ++f) {
+      const double* p[3];
+      const double* pp[3];
+      for (int k = 0; k < 3; ++k) {
+        p[k] = x + 3 * (size_t)fv[3 * f + k];
+        pp[k] = xp + 3 * (size_t)fv[3 * f + k];
+      }
+      double mid[3], midp[3];
+      for (int i = 0; i < 3; ++i) {  // middle_xyz (src/BVH.cpp:3-13)
+        mid[i] = 0.5 * (kmin(kmin(p[0][i], p[1][i]), p[2][i]) + kmax(kmax(p[0][i], p[1][i]), p[2][i]));
+        midp[i] = 0.5 * (kmin(kmin(pp[0][i], pp[1][i]), pp[2][i]) + kmax(kmax(pp[0][i], pp[1][i]), pp[2][i]));
+      }
+      for (int i = 0; i < 3; ++i) centers[3 * (size_t)f + i] = ccd ? (mid[i] + midp[i]) * 0.5 : mid[i];
+      // the face box's x, y, z bounds (kDOP18 of its points, and of their
+      // previous positions under CCD)
+      double* e = &ext[6 * (size_t)f];
+      for (int i = 0; i < 3; ++i) {
+        e[i] = e[3 + i] = p[0][i];
+        for (int k = 1; k < 3; ++k) {
+          e[i] = kmin(p[k][i], e[i]);
+          e[3 + i] = kmax(p[k][i], e[3 + i]);
+        }
+        if (ccd)
+          for (int k = 0; k < 3; ++k) {
+            e[i] = kmin(pp[k][i], e[i]);
+            e[3 + i] = kmax(pp[k][i], e[3 + i]);
+          }
+      }
+    }
+  };
+  if (par) pool->run(nch, face_geom);
+  else face_geom(0);
   std::vector<int> buf(nfaces);
   unsigned left_idx = 0, right_idx = (unsigned)nfaces;
   for (int f = 0; f < nfaces; ++f) {
-    const double* p[3];
-    const double* pp[3];
-    for (int k = 0; k < 3; ++k) {
-      p[k] = x + 3 * (size_t)fv[3 * f + k];
-      pp[k] = xp + 3 * (size_t)fv[3 * f + k];
-    }
-    double mid[3], midp[3];
-    for (int i = 0; i < 3; ++i) {  // middle_xyz (src/BVH.cpp:3-13)
-      mid[i] = 0.5 * (kmin(kmin(p[0][i], p[1][i]), p[2][i]) + kmax(kmax(p[0][i], p[1][i]), p[2][i]));
-      midp[i] = 0.5 * (kmin(kmin(pp[0][i], pp[1][i]), pp[2][i]) + kmax(kmax(pp[0][i], pp[1][i]), pp[2][i]));
-    }
-    for (int i = 0; i < 3; ++i) centers[3 * (size_t)f + i] = ccd ? (mid[i] + midp[i]) * 0.5 : mid[i];
     if (pln.inside(&centers[3 * (size_t)f])) buf[left_idx++] = f;
     else buf[--right_idx] = f;
-    // the face box's x, y, z bounds (kDOP18 of its points, and of their
-    // previous positions under CCD)
-    double* e = &ext[6 * (size_t)f];
-    for (int i = 0; i < 3; ++i) {
-      e[i] = e[3 + i] = p[0][i];
-      for (int k = 1; k < 3; ++k) {
-        e[i] = kmin(p[k][i], e[i]);
-        e[3 + i] = kmax(p[k][i], e[3 + i]);
-      }
-      if (ccd)
-        for (int k = 0; k < 3; ++k) {
-          e[i] = kmin(pp[k][i], e[i]);
-          e[3 + i] = kmax(pp[k][i], e[3 + i]);
-        }
-    }
   }
   const size_t nn = 2 * (size_t)nfaces - 1;
   t.left.assign(nn, -1);
@@ -185,11 +312,21 @@ inline BvhTree bvh_build(int nfaces, const int* fv, int nverts, const int* verts
     if (left_idx == 0 || (int)left_idx == nfaces) split = nfaces / 2;
     t.left[root] = 1;
     t.right[root] = 2 * split;
-    const int threads = nfaces > 16384 ? 8 : 1;
-    auto lf = std::async(threads > 1 ? std::launch::async : std::launch::deferred,
-                         [&] { b.node(buf.data(), split, 1, 1, threads / 2); });
-    b.node(buf.data() + split, nfaces - split, 1, 2 * split, threads - threads / 2);
-    lf.get();
+    if (par) {
+      std::vector<bvh_detail::Builder::Task> tasks;
+      b.top(buf.data(), split, 1, 1, 2, 256, tasks);
+      b.top(buf.data() + split, nfaces - split, 1, 2 * split, 2, 256, tasks);
+      pool->run((int)tasks.size(), [&](int i) {
+        const bvh_detail::Builder::Task& k = tasks[i];
+        b.node(k.lst, k.num, k.dep, k.idx, 1);
+      });
+    } else {
+      const int threads = nfaces > 16384 ? 8 : 1;
+      auto lf = std::async(threads > 1 ? std::launch::async : std::launch::deferred,
+                           [&] { b.node(buf.data(), split, 1, 1, threads / 2); });
+      b.node(buf.data() + split, nfaces - split, 1, 2 * split, threads - threads / 2);
+      lf.get();
+    }
   }
   for (int d : t.depth) t.max_depth = d > t.max_depth ? d : t.max_depth;
   // leaf ranks (left to right) and upper nodes

@@ -11,6 +11,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <memory>
+#include <thread>
 #include <cmath>
 #include <cstring>
 #include <future>
@@ -459,6 +461,9 @@ struct ys_collider {
   int max_zone_impacts = 65536;
   std::vector<int> h_cslice, h_oslice;  // broad-phase slice roots
   DVec<int> cslice, oslice;
+  // host threads for the cloth tree's build (the obstacle's, when it is
+  // rebuilt, runs beside it on a thread of its own)
+  std::unique_ptr<ys::BuildPool> pool;
   ~ys_collider() {
     if (pin) cudaFreeHost(pin);
     if (pin_imp) cudaFreeHost(pin_imp);
@@ -867,6 +872,11 @@ ys_status ys_collider_create(int32_t n_nodes, int32_t n_faces, const int32_t* fa
       (n_obs_faces && cudaMemcpy(c->ofaces.p, ho.data(), sizeof(CFace) * n_obs_faces, cudaMemcpyHostToDevice) !=
                           cudaSuccess))
     return cleanup(ys_internal_fail(YS_ERR_CUDA, "cudaMemcpy failed"));
+  {
+    const unsigned hc = std::thread::hardware_concurrency();
+    const int nthreads = (int)std::min(4u, std::max(1u, hc));
+    if (nthreads > 1) c->pool.reset(new ys::BuildPool(nthreads));
+  }
   *out = c;
   return YS_OK;
 }
@@ -925,7 +935,8 @@ ys_status ys_collider_set_positions(ys_collider* c, const double* x, const doubl
     });
   std::vector<int> verts(c->n_nodes);
   for (int i = 0; i < c->n_nodes; ++i) verts[i] = i;
-  c->ct = ys::bvh_build(c->n_faces, c->fv.data(), c->n_nodes, verts.data(), c->hx.data(), c->hxp.data(), c->ccd != 0);
+  c->ct = ys::bvh_build(c->n_faces, c->fv.data(), c->n_nodes, verts.data(), c->hx.data(), c->hxp.data(), c->ccd != 0,
+                        c->pool.get());
   if (!same_obstacle) c->ot = obs_tree.get();
   ys_status s;
   if ((s = upload_tree(c, c->ct, c->c_left, c->c_right, c->c_face, c->c_box, c->c_parent, c->c_leaves,
