@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libyarnsim.so")
 SOURCES = ["ys_tangent.cu", "ys_kernels.cu", "ys_api.cu", "ys_collide.cu", "ys_gnn.cu", "ys_adjoint.cu",
            "ys_pcg_cluster.cu"]
 HEADERS = ["ys_common.cuh", "ys_dual.cuh", "ys_physics.cuh", "ys_items.cuh", "ys_elem_kernels.cuh", "ys_kernels.cuh", "ys_collide.cuh", "ys_bvh.h",
-           "ys_gnn.cuh", "ys_tc.cuh", "ys_zones.h"]
+           "ys_gnn.cuh", "ys_tc.cuh", "ys_zones.h", "ys_pool.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC"]
 # the collision tests keep IEEE products and sums separate, as the reference's

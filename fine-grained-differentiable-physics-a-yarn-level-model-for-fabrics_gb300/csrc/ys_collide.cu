@@ -1079,7 +1079,7 @@ ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h,
     return 0;
   };
   const auto t_resp = std::chrono::steady_clock::now();
-  if (ys::zone_respond(R, x.data(), node_mass, detect)) return err;
+  if (ys::zone_respond(R, x.data(), node_mass, detect, c->pool.get())) return err;
   const double resp_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_resp).count();
   // the collider keeps the responded positions (the cloth mesh's x)
   c->hx = x;

@@ -36,6 +36,8 @@
 // anchor goes to the zone's positions at the time of the projection.
 #pragma once
 
+#include "ys_pool.h"
+
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -445,10 +447,12 @@ inline double node_x(const double* x, const double* obs_x, int nd, int c) {
 }
 
 // projects one zone in place (x: all cloth positions), records it
-inline void project(ZoneResponse& R, const std::vector<int>& nodes, const std::vector<int>& imps, const double* mass,
-                    const double* xold, double* x, std::vector<int>& local, int round) {
+// one zone's projection into rec; it writes x and local at the zone's own
+// nodes only, so zones with disjoint nodes can be projected at once
+inline void project_zone(const ZoneResponse& R, const std::vector<int>& nodes, const std::vector<int>& imps,
+                         const double* mass, const double* xold, double* x, std::vector<int>& local, int round,
+                         ZoneRecord& rec) {
   const int m = (int)nodes.size(), nv = 3 * m, k = (int)imps.size();
-  ZoneRecord rec;
   rec.round = round;
   rec.nodes = nodes;
   rec.imps = imps;
@@ -489,7 +493,6 @@ inline void project(ZoneResponse& R, const std::vector<int>& nodes, const std::v
   }
   rec.status = dense ? ldp(nv, k, G.data(), h.data(), u.data(), rec.lam.data())
                      : ldp_sparse(nv, k, cols.data(), coef.data(), h.data(), u.data(), rec.lam.data());
-  if (rec.status == 1) R.infeasible++;
   if (rec.status != 1 && R.xprev && R.revert_factor > 0.0) {
     bool far = false;
     for (int i = 0; i < m && !far; ++i) {
@@ -502,10 +505,7 @@ inline void project(ZoneResponse& R, const std::vector<int>& nodes, const std::v
       }
       far = std::sqrt(mv) > R.revert_factor * (std::sqrt(st) + R.thickness);
     }
-    if (far) {
-      rec.status = 3;
-      R.reverted++;
-    }
+    if (far) rec.status = 3;
   }
   rec.xout.resize(nv);
   for (int i = 0; i < m; ++i)
@@ -516,6 +516,12 @@ inline void project(ZoneResponse& R, const std::vector<int>& nodes, const std::v
       rec.xout[3 * i + c] = xn;
     }
   for (int i = 0; i < m; ++i) local[nodes[i]] = -1;
+}
+
+// the record's outcome into R (its counters and the tape, in zone order)
+inline void record_zone(ZoneResponse& R, ZoneRecord&& rec) {
+  if (rec.status == 1) R.infeasible++;
+  if (rec.status == 3) R.reverted++;
   R.tape.push_back(std::move(rec));
 }
 
@@ -527,7 +533,7 @@ inline void project(ZoneResponse& R, const std::vector<int>& nodes, const std::v
 // face_active is given) and returns 0 on success. mass [n] may be null
 // (equal masses). Returns the detector's first non-zero status, else 0.
 template <class Detect>
-int zone_respond(ZoneResponse& R, double* x, const double* mass, Detect&& detect) {
+int zone_respond(ZoneResponse& R, double* x, const double* mass, Detect&& detect, BuildPool* pool = nullptr) {
   const int n = R.n_nodes;
   R.accepted.clear();
   R.accepted_round.clear();
@@ -557,6 +563,8 @@ int zone_respond(ZoneResponse& R, double* x, const double* mass, Detect&& detect
   std::vector<uint8_t> face_active(R.n_faces);
   std::vector<ZImpact> found, indep;
   std::vector<char> taken(n, 0);
+  std::vector<int> active;
+  std::vector<ZoneRecord> recs;
   auto find_or_create = [&](int nd) {
     if (zone_of[nd] >= 0) return zone_of[nd];
     zs.push_back(Zone());
@@ -626,11 +634,22 @@ int zone_respond(ZoneResponse& R, double* x, const double* mass, Detect&& detect
     for (int z : order)
       if (zs[z].active && (int)zs[z].imps.size() > R.max_zone_impacts) R.zone_overflow = 1;
     if (R.zone_overflow) break;
+    // the active zones' projections: their nodes are disjoint, so on a pool
+    // they run at once and are recorded in zone order afterwards
+    active.clear();
     for (int z : order)
-      if (zs[z].active) {
-        R.changed = 1;
-        zone_detail::project(R, zs[z].nodes, zs[z].imps, mass, xold.data(), x, local, iter);
-      }
+      if (zs[z].active) active.push_back(z);
+    if (!active.empty()) R.changed = 1;
+    recs.clear();
+    recs.resize(active.size());
+    auto proj = [&](int i) {
+      const Zone& zn = zs[active[i]];
+      zone_detail::project_zone(R, zn.nodes, zn.imps, mass, xold.data(), x, local, iter, recs[i]);
+    };
+    if (pool && pool->size() > 1 && active.size() > 1) pool->run((int)active.size(), proj);
+    else
+      for (size_t i = 0; i < active.size(); ++i) proj((int)i);
+    for (ZoneRecord& rec : recs) zone_detail::record_zone(R, std::move(rec));
   }
   R.rounds = iter;
   R.converged = iter < R.max_iter && !R.zone_overflow;
