@@ -772,18 +772,13 @@ ys_status detect_one_wait(ys_collider* c, bool masked, std::vector<ys_impact>& g
 }
 
 // marks the cloth-tree nodes with an active leaf below (host tree)
-bool mark_nodes(const ys::BvhTree& t, const uint8_t* fa, std::vector<uint8_t>& out, int n) {
-  const int f = t.face[n];
-  bool on;
-  if (f >= 0) {
-    on = fa[f] != 0;
-  } else {
-    const bool l = mark_nodes(t, fa, out, t.left[n]);
-    const bool r = mark_nodes(t, fa, out, t.right[n]);
-    on = l || r;
+// (preorder numbering puts both children after their parent, so one pass
+// from the last node to the root sees every child before its parent)
+void mark_nodes(const ys::BvhTree& t, const uint8_t* fa, std::vector<uint8_t>& out) {
+  for (int n = (int)t.face.size() - 1; n >= 0; --n) {
+    const int f = t.face[n];
+    out[n] = f >= 0 ? (fa[f] != 0 ? 1 : 0) : (out[t.left[n]] | out[t.right[n]]);
   }
-  out[n] = on ? 1 : 0;
-  return on;
 }
 
 }  // namespace
@@ -1057,7 +1052,7 @@ ys_status ys_collider_respond(ys_collider* c, const double* node_mass, double h,
       if (c->face_active.reserve(c->n_faces) != cudaSuccess || c->node_active.reserve(nn) != cudaSuccess)
         return fail(ys_internal_fail(YS_ERR_CUDA, "cudaMalloc failed"));
       c->h_node_active.assign(nn, 0);
-      mark_nodes(c->ct, mask, c->h_node_active, 0);
+      mark_nodes(c->ct, mask, c->h_node_active);
       if (cudaMemcpyAsync(c->face_active.p, mask, c->n_faces, cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
           cudaMemcpyAsync(c->node_active.p, c->h_node_active.data(), nn, cudaMemcpyHostToDevice, c->stream) !=
               cudaSuccess)
