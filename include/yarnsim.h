@@ -339,7 +339,10 @@ typedef struct {
 ys_status ys_cloth_mesh_topology(int32_t width, int32_t length, int32_t *faces, int32_t *face_edges);
 /* A collider for a cloth mesh (node ids 0..n_nodes-1) and an obstacle mesh
  * (n_obs_faces may be 0); thickness dilates the boxes (src/BVH.cpp:268-286);
- * ccd = 1: boxes span both positions of the step. */
+ * ccd = 1: boxes span both positions of the step. The collider keeps up to
+ * three host threads (with the calling one, four) for the cloth tree's build
+ * and the response's zone projections, until ys_collider_destroy; its calls
+ * are not to be made from two host threads at once. */
 ys_status ys_collider_create(int32_t n_nodes, int32_t n_faces, const int32_t *faces, const int32_t *face_edges,
                              int32_t n_obs_nodes, int32_t n_obs_faces, const int32_t *obs_faces, double thickness,
                              int32_t ccd, int32_t device, void *cuda_stream, ys_collider **out);
