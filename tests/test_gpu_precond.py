@@ -1,7 +1,9 @@
 """Learned preconditioner on the GPU: the tcgen05 GEMM against torch, the
-network's outputs, G blocks, Kaporin loss and hand-written gradient against
-the CPU oracle (torch float64 autograd), training, and the learned solve
-against Jacobi-PCG at the same FP64 residual."""
+network's outputs, G blocks, both training objectives (the exact-FSAI
+regression and the Kaporin number) and their hand-written gradients against
+the CPU oracle (torch float64 autograd), training and what it gains over the
+untrained network, the learned solve against Jacobi-PCG at the same FP64
+residual, and the learned step as one CUDA graph (fallback included)."""
 import os
 import sys
 
