@@ -86,6 +86,71 @@ def wind_at(wind, step):
 
 
 # ---------------------------------------------------------------- helpers
+class NvmlSampler:
+    """SM clock, its maximum and the active clock-event reasons, read through
+    NVML (read-only queries) by a thread every `period` seconds."""
+    CLOCK_SM = 1  # nvmlClockType_t NVML_CLOCK_SM
+    REASONS = ((0x8, "hw_slowdown"), (0x40, "hw_thermal_slowdown"), (0x20, "sw_thermal_slowdown"),
+               (0x4, "sw_power_cap"))
+
+    def __init__(self, index=0, period=0.002):
+        import ctypes
+        self.c = ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.lib = lib
+        self.h = ctypes.c_void_p()
+        bus = None
+        try:
+            import torch
+            p = torch.cuda.get_device_properties(index)
+            bus = "%08x:%02x:%02x.0" % (p.pci_domain_id, p.pci_bus_id, p.pci_device_id)
+        except Exception:
+            bus = None
+        rc = lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(self.h)) if bus else 1
+        if rc != 0 and lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.h)) != 0:
+            raise RuntimeError("no NVML handle for device %d" % index)
+        self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(self.h, self.CLOCK_SM, ctypes.byref(mx)) != 0:
+            raise RuntimeError("nvmlDeviceGetMaxClockInfo failed")
+        self.max_mhz = float(mx.value)
+        self.period = period
+        self.sm, self.bits = [], 0
+        self.stop = threading.Event()
+
+    def _sample(self):
+        c = self.c
+        clk, r = c.c_uint(), c.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.h, self.CLOCK_SM, c.byref(clk)) == 0:
+            self.sm.append(float(clk.value))
+        if self.reasons_fn(self.h, c.byref(r)) == 0:
+            self.bits |= r.value
+
+    def _run(self):
+        while not self.stop.is_set():
+            self._sample()
+            time.sleep(self.period)
+
+    def __enter__(self):
+        self._sample()
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=5)
+        self._sample()
+
+    def summary(self):
+        return {"sm_mhz": statistics.median(self.sm) if self.sm else None, "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(n for b, n in self.REASONS if self.bits & b), "samples": len(self.sm),
+                "source": "nvml, every %g ms" % (self.period * 1e3)}
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -96,8 +161,16 @@ class ClockSampler:
         self.index = index
         self.rows = []
         self.proc = None
+        self.nvml = None
 
     def __enter__(self):
+        # NVML polled every 2 ms when libnvidia-ml loads: a timed region of a
+        # fraction of a second still gets dozens of samples
+        try:
+            self.nvml = NvmlSampler(self.index).__enter__()
+            return self
+        except Exception:
+            self.nvml = None
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -113,6 +186,8 @@ class ClockSampler:
             self.rows.append([x.strip() for x in line.split(",")])
 
     def __exit__(self, *a):
+        if self.nvml is not None:
+            self.nvml.__exit__(*a)
         if self.proc:
             self.proc.terminate()
             try:
@@ -121,6 +196,8 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml is not None:
+            return self.nvml.summary()
         sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
         mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
