@@ -120,6 +120,10 @@ struct ys_batch {
     bool enabled = false;
     bool built = false;
     cudaStream_t capture = nullptr;  // capture needs a stream of its own
+    // two more capture streams and their fork / join events: the record
+    // producers that read none of each other's output are graph branches
+    cudaStream_t side[2] = {nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
     cudaGraph_t main = nullptr;      // Jacobi-PCG step
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t lmain[2] = {nullptr, nullptr};  // learned-preconditioner step [with the network]
@@ -224,6 +228,11 @@ struct ys_batch {
     drain();
     graph.drop();
     if (graph.capture) cudaStreamDestroy(graph.capture);
+    for (int k = 0; k < 2; ++k) {
+      if (graph.side[k]) cudaStreamDestroy(graph.side[k]);
+      if (graph.join[k]) cudaEventDestroy(graph.join[k]);
+    }
+    if (graph.fork) cudaEventDestroy(graph.fork);
     for (cudaEvent_t e : pool) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
     if (h_nactive) cudaFreeHost(h_nactive);
@@ -1420,21 +1429,36 @@ namespace {
 ys_status graph_prepare(ys_batch* b) {
   ys_batch::Graph& G = b->graph;
   if (!G.capture) YS_CUDA(cudaStreamCreateWithFlags(&G.capture, cudaStreamNonBlocking));
+  for (int k = 0; k < 2; ++k) {
+    if (!G.side[k]) YS_CUDA(cudaStreamCreateWithFlags(&G.side[k], cudaStreamNonBlocking));
+    if (!G.join[k]) YS_CUDA(cudaEventCreateWithFlags(&G.join[k], cudaEventDisableTiming));
+  }
+  if (!G.fork) YS_CUDA(cudaEventCreateWithFlags(&G.fork, cudaEventDisableTiming));
   ys_status s = YS_OK;
   if (!G.it_base && (s = b->alloc(&G.it_base, 1)) != YS_OK) return s;
   if (!G.hold && (s = b->alloc(&G.hold, 1)) != YS_OK) return s;
   return YS_OK;
 }
 
-// the kernels of ys_assemble and the PCG counters' reset, onto a capturing stream
+// the kernels of ys_assemble and the PCG counters' reset, onto a capturing
+// stream. The producers form three branches of the graph, each writing its
+// own record buffer from the state: normals then bends (bends read the
+// normals), edges, faces; the gather joins them.
 void capture_assembly(ys_batch* b, cudaStream_t cs, int override_max) {
   const ys::View& v = b->v;
   const ys::Records& R = b->rec;
+  ys_batch::Graph& G = b->graph;
   k_reset_status<<<(b->ncloth + 127) / 128, 128, 0, cs>>>(b->so.pc, b->ncloth);
+  cudaEventRecord(G.fork, cs);
+  for (int k = 0; k < 2; ++k) cudaStreamWaitEvent(G.side[k], G.fork, 0);
+  ys::launch_edge_records(v, R, G.side[0], b->producer_threads);
+  ys::launch_face_records(v, R, G.side[1], b->producer_threads);
   if (b->geom_n) ys::launch_geom(v, b->anchors + b->geom_off, b->geom_n, cs);
-  ys::launch_edge_records(v, R, cs, b->producer_threads);
   ys::launch_bend_records(v, R, cs, b->producer_threads);
-  ys::launch_face_records(v, R, cs, b->producer_threads);
+  for (int k = 0; k < 2; ++k) {
+    cudaEventRecord(G.join[k], G.side[k]);
+    cudaStreamWaitEvent(cs, G.join[k], 0);
+  }
   ys::launch_gather(v, R, cs, b->producer_threads);
   ys::launch_shear_records(v, R, cs, b->producer_threads);
   ys::launch_finalize(v, R, b->blk, b->so, cs);
