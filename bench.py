@@ -602,13 +602,13 @@ def main():
         e0.record()
         for _ in range(args.steps):
             st = do_step()
-            iters.append(max(s["cg_iterations"] for s in st))
+            iters.append(st.max_iterations)
         e1.record()
         torch.cuda.synchronize()
     barrier()
     ms = e0.elapsed_time(e1)
     launches = batch.profile_read(reset=True)["total_launches"]
-    ok = all(s["ok"] for s in st)
+    ok = st.all_ok
     if dist is not None:
         ms = max_over_ranks(ms, dist, "cuda")
     ms_per_step = ms / args.steps

@@ -9,6 +9,7 @@ loop like SimHomo (src/Simulate.h:78-101) reads the same.
 """
 from __future__ import annotations
 
+import collections.abc
 import ctypes
 import enum
 from dataclasses import dataclass, field
@@ -19,6 +20,55 @@ import numpy as np
 from . import _native as N
 
 PI = 3.1415926535897  # src/Constants.h:24
+
+
+class StepStats(collections.abc.Sequence):
+    """Per-cloth results of a solve or step (the C ABI's ys_cloth_stats
+    array): a sequence of dicts {ok, cg_iterations, cg_error, hit_maxiter},
+    each built when it is read, and whole-batch aggregates computed over the
+    array, so a step of many cloths costs no per-cloth Python work unless
+    its entries are read."""
+
+    _dtype = None
+
+    def __init__(self, arr):
+        if StepStats._dtype is None:
+            StepStats._dtype = np.ctypeslib.as_array(arr).dtype
+        self._a = np.frombuffer(arr, dtype=StepStats._dtype)
+
+    def __len__(self):
+        return len(self._a)
+
+    def _one(self, s):
+        return dict(ok=bool(s["ok"]), cg_iterations=int(s["cg_iterations"]), cg_error=float(s["cg_error"]),
+                    hit_maxiter=bool(s["hit_maxiter"]))
+
+    def __getitem__(self, i):
+        if isinstance(i, slice):
+            return [self._one(s) for s in self._a[i]]
+        return self._one(self._a[i])
+
+    def __eq__(self, other):
+        return list(self) == list(other)
+
+    def __repr__(self):
+        return repr(list(self))
+
+    @property
+    def all_ok(self) -> bool:
+        return bool(np.all(self._a["ok"] != 0))
+
+    @property
+    def max_iterations(self) -> int:
+        return int(self._a["cg_iterations"].max()) if len(self._a) else 0
+
+    @property
+    def max_error(self) -> float:
+        return float(self._a["cg_error"].max()) if len(self._a) else 0.0
+
+    @property
+    def iterations(self) -> np.ndarray:
+        return self._a["cg_iterations"].copy()
 
 
 class WovenPattern(enum.IntEnum):
@@ -227,8 +277,7 @@ class ClothBatch:
         return o
 
     def _stats(self, arr):
-        return [dict(ok=bool(s.ok), cg_iterations=s.cg_iterations, cg_error=s.cg_error,
-                     hit_maxiter=bool(s.hit_maxiter)) for s in arr]
+        return StepStats(arr)
 
     def assemble(self, h, ext_force=None):
         """FillMV + system formation; ext_force: [total_nodes, 5] (x,y,z,u,v)."""

@@ -84,6 +84,8 @@ struct ys_batch {
   double* stage = nullptr;  // [15][ntot] staging for layout changes (the six state arrays side by side)
   double* ext = nullptr;    // [5][ntot]
   int* h_nactive = nullptr; // pinned
+  double* h_wind = nullptr;  // pinned [ncloth][3]: ys_set_winds' copy of the caller's array
+  cudaEvent_t wind_ev = nullptr;  // recorded after the copy out of h_wind
   bool assembled = false;
   int max_maxiter = 0;
   // launch accounting and optional per-kernel-class event timing
@@ -236,6 +238,8 @@ struct ys_batch {
     for (cudaEvent_t e : pool) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
     if (h_nactive) cudaFreeHost(h_nactive);
+    if (h_wind) cudaFreeHost(h_wind);
+    if (wind_ev) cudaEventDestroy(wind_ev);
   }
 };
 
@@ -439,9 +443,11 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
   A(&b->so.part, 4 * blk_cloth.size()); A(&b->so.pc, n_cloths); A(&b->so.nactive, 1);
   A(&b->stage, 15 * nt); A(&b->ext, 5 * nt);
   if (st != YS_OK) { delete b; return st; }
-  if (cudaMallocHost(&b->h_nactive, sizeof(int)) != cudaSuccess) {
+  if (cudaMallocHost(&b->h_nactive, sizeof(int)) != cudaSuccess ||
+      cudaMallocHost(&b->h_wind, sizeof(double) * 3 * n_cloths) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->wind_ev, cudaEventDisableTiming) != cudaSuccess) {
     delete b;
-    return fail(YS_ERR_CUDA, "cudaMallocHost failed");
+    return fail(YS_ERR_CUDA, "cudaMallocHost / cudaEventCreate failed");
   }
   auto up = [&](void* dst, const void* src, size_t nbytes) -> ys_status {
     YS_CUDA(cudaMemcpy(dst, src, nbytes, cudaMemcpyHostToDevice));
@@ -604,14 +610,20 @@ ys_status ys_set_winds(ys_batch* b, const double* wind_vel, int32_t flags) {
   YS_CUDA(cudaSetDevice(b->device));
   const double* src = wind_vel;
   if (!(flags & YS_ON_DEVICE)) {
-    YS_CUDA(cudaMemcpyAsync(b->stage, wind_vel, sizeof(double) * 3 * b->ncloth, cudaMemcpyHostToDevice, b->stream));
+    // the caller's array is copied into pinned memory here, so the call
+    // returns once it is read without waiting for the stream; the previous
+    // call's copy out of that memory has finished first
+    const size_t nb = sizeof(double) * 3 * b->ncloth;
+    YS_CUDA(cudaEventSynchronize(b->wind_ev));
+    std::memcpy(b->h_wind, wind_vel, nb);
+    YS_CUDA(cudaMemcpyAsync(b->stage, b->h_wind, nb, cudaMemcpyHostToDevice, b->stream));
+    YS_CUDA(cudaEventRecord(b->wind_ev, b->stream));
     src = b->stage;
   }
   b->launches += 1;
   k_set_winds<<<(b->ncloth + 127) / 128, 128, 0, b->stream>>>(const_cast<ys::ClothParams*>(b->v.cp), src,
                                                                  b->ncloth);
   YS_CUDA(cudaGetLastError());
-  if (!(flags & YS_ON_DEVICE)) YS_CUDA(cudaStreamSynchronize(b->stream));
   for (int c = 0; c < b->ncloth; ++c)
     for (int k = 0; k < 3; ++k) b->cp[c].wind[k] = wind_vel == src ? b->cp[c].wind[k] : wind_vel[3 * c + k];
   return YS_OK;
