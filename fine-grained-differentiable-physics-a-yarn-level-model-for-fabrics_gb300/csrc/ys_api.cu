@@ -37,15 +37,30 @@ ys_status fail(ys_status s, const std::string& msg) {
   } while (0)
 
 // node-major [n][c] <-> component-major [c][n]
-__global__ void k_to_soa(const double* __restrict__ in, double* __restrict__ out, int64_t n, int c) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  for (int k = 0; k < c; ++k) out[k * n + i] = in[i * c + k];
+// AoS [n][c] <-> SoA [c][n] (c <= kMaxComps), kTrBlock nodes per block: the
+// AoS side is moved as one contiguous run of kTrBlock * c doubles (each warp
+// touches consecutive addresses, which matters when that side is host memory
+// read or written over the C2C link), transposed in shared memory
+constexpr int kTrBlock = 256, kMaxComps = 5;
+__global__ void __launch_bounds__(kTrBlock) k_to_soa(const double* __restrict__ in, double* __restrict__ out,
+                                                      int64_t n, int c) {
+  __shared__ double sh[kTrBlock * kMaxComps];
+  const int64_t n0 = (int64_t)blockIdx.x * kTrBlock;
+  const int cnt = (int)(n - n0 < kTrBlock ? n - n0 : kTrBlock);
+  for (int j = threadIdx.x; j < cnt * c; j += kTrBlock) sh[j] = in[n0 * c + j];
+  __syncthreads();
+  if (threadIdx.x < cnt)
+    for (int k = 0; k < c; ++k) out[k * n + n0 + threadIdx.x] = sh[threadIdx.x * c + k];
 }
-__global__ void k_to_aos(const double* __restrict__ in, double* __restrict__ out, int64_t n, int c) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  for (int k = 0; k < c; ++k) out[i * c + k] = in[k * n + i];
+__global__ void __launch_bounds__(kTrBlock) k_to_aos(const double* __restrict__ in, double* __restrict__ out,
+                                                      int64_t n, int c) {
+  __shared__ double sh[kTrBlock * kMaxComps];
+  const int64_t n0 = (int64_t)blockIdx.x * kTrBlock;
+  const int cnt = (int)(n - n0 < kTrBlock ? n - n0 : kTrBlock);
+  if (threadIdx.x < cnt)
+    for (int k = 0; k < c; ++k) sh[threadIdx.x * c + k] = in[k * n + n0 + threadIdx.x];
+  __syncthreads();
+  for (int j = threadIdx.x; j < cnt * c; j += kTrBlock) out[n0 * c + j] = sh[j];
 }
 // iteration bookkeeping only; the status bits set by the assembly are kept
 __global__ void k_reset_pc(ys::PcgCloth* pc, const int* maxiter, int ncloth, int maxiter_override) {
@@ -248,14 +263,33 @@ namespace {
 // host (or device, YS_ON_DEVICE) AoS [ntot][c] -> device SoA [c][ntot]; a
 // host array goes through the stage at `slot` (in units of ntot doubles), and
 // with sync the call returns once the host array has been read
+// the device's address of a page-locked host array (cudaMallocHost,
+// cudaHostAlloc, cudaHostRegister: what a pinned tensor's storage is), or
+// null for pageable or device memory
+double* mapped_host(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? static_cast<double*>(a.devicePointer) : nullptr;
+}
+
+// a page-locked host array is read (written) by the transposition kernel
+// itself, with no stage copy
 ys_status upload_soa(ys_batch* b, const double* src, double* dst, int c, int32_t flags, int64_t slot = 0,
                      bool sync = true) {
   const int64_t n = b->ntot;
   if (!src) return YS_OK;
+  if (c > kMaxComps) return fail(YS_ERR_ARG, "upload_soa: too many components");
   const double* d_src = src;
   if (!(flags & YS_ON_DEVICE)) {
-    YS_CUDA(cudaMemcpyAsync(b->stage + slot * n, src, sizeof(double) * n * c, cudaMemcpyHostToDevice, b->stream));
-    d_src = b->stage + slot * n;
+    if (const double* m = mapped_host(src)) {
+      d_src = m;
+    } else {
+      YS_CUDA(cudaMemcpyAsync(b->stage + slot * n, src, sizeof(double) * n * c, cudaMemcpyHostToDevice, b->stream));
+      d_src = b->stage + slot * n;
+    }
   }
   b->launches += 1;
   k_to_soa<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(d_src, dst, n, c);
@@ -271,12 +305,14 @@ ys_status download_aos(ys_batch* b, const double* src, double* dst, int c, int32
                        bool sync = true) {
   const int64_t n = b->ntot;
   if (!dst) return YS_OK;
-  double* d_dst = (flags & YS_ON_DEVICE) ? dst : b->stage + slot * n;
+  if (c > kMaxComps) return fail(YS_ERR_ARG, "download_aos: too many components");
+  double* m = (flags & YS_ON_DEVICE) ? nullptr : mapped_host(dst);
+  double* d_dst = (flags & YS_ON_DEVICE) ? dst : m ? m : b->stage + slot * n;
   b->launches += 1;
   k_to_aos<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(src, d_dst, n, c);
   YS_CUDA(cudaGetLastError());
   if (!(flags & YS_ON_DEVICE)) {
-    YS_CUDA(cudaMemcpyAsync(dst, d_dst, sizeof(double) * n * c, cudaMemcpyDeviceToHost, b->stream));
+    if (!m) YS_CUDA(cudaMemcpyAsync(dst, d_dst, sizeof(double) * n * c, cudaMemcpyDeviceToHost, b->stream));
     if (sync) YS_CUDA(cudaStreamSynchronize(b->stream));
   }
   return YS_OK;
