@@ -117,7 +117,11 @@ int64_t ys_cloth_dim(const ys_batch *b, int32_t c);
 
 /* Node-ordered state of the whole batch (node = offset(c) + u + v*W):
  * lpos, lposfix, lvel: [total_nodes][3]; epos, eposbar, evel: [total_nodes][2].
- * Any pointer may be NULL (that field is left untouched). */
+ * Any pointer may be NULL (that field is left untouched). Host arrays in
+ * page-locked memory (cudaMallocHost / cudaHostAlloc / cudaHostRegister) are
+ * read or written by the device directly; pageable ones go through a device
+ * stage. Either way both calls return once the host arrays are read or
+ * filled. */
 ys_status ys_set_state(ys_batch *b, const double *lpos, const double *lposfix, const double *lvel,
                        const double *epos, const double *eposbar, const double *evel, int32_t flags);
 ys_status ys_get_state(ys_batch *b, double *lpos, double *lposfix, double *lvel, double *epos, double *eposbar,
