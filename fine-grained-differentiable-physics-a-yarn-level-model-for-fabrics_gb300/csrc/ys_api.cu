@@ -42,8 +42,8 @@ ys_status fail(ys_status s, const std::string& msg) {
 // touches consecutive addresses, which matters when that side is host memory
 // read or written over the C2C link), transposed in shared memory
 constexpr int kTrBlock = 256, kMaxComps = 5;
-__global__ void __launch_bounds__(kTrBlock) k_to_soa(const double* __restrict__ in, double* __restrict__ out,
-                                                      int64_t n, int c) {
+__device__ __forceinline__ void to_soa_block(const double* __restrict__ in, double* __restrict__ out, int64_t n,
+                                             int c) {
   __shared__ double sh[kTrBlock * kMaxComps];
   const int64_t n0 = (int64_t)blockIdx.x * kTrBlock;
   const int cnt = (int)(n - n0 < kTrBlock ? n - n0 : kTrBlock);
@@ -52,8 +52,8 @@ __global__ void __launch_bounds__(kTrBlock) k_to_soa(const double* __restrict__ 
   if (threadIdx.x < cnt)
     for (int k = 0; k < c; ++k) out[k * n + n0 + threadIdx.x] = sh[threadIdx.x * c + k];
 }
-__global__ void __launch_bounds__(kTrBlock) k_to_aos(const double* __restrict__ in, double* __restrict__ out,
-                                                      int64_t n, int c) {
+__device__ __forceinline__ void to_aos_block(const double* __restrict__ in, double* __restrict__ out, int64_t n,
+                                             int c) {
   __shared__ double sh[kTrBlock * kMaxComps];
   const int64_t n0 = (int64_t)blockIdx.x * kTrBlock;
   const int cnt = (int)(n - n0 < kTrBlock ? n - n0 : kTrBlock);
@@ -61,6 +61,26 @@ __global__ void __launch_bounds__(kTrBlock) k_to_aos(const double* __restrict__ 
     for (int k = 0; k < c; ++k) sh[threadIdx.x * c + k] = in[k * n + n0 + threadIdx.x];
   __syncthreads();
   for (int j = threadIdx.x; j < cnt * c; j += kTrBlock) out[n0 * c + j] = sh[j];
+}
+__global__ void __launch_bounds__(kTrBlock) k_to_soa(const double* __restrict__ in, double* __restrict__ out,
+                                                      int64_t n, int c) {
+  to_soa_block(in, out, n, c);
+}
+__global__ void __launch_bounds__(kTrBlock) k_to_aos(const double* __restrict__ in, double* __restrict__ out,
+                                                      int64_t n, int c) {
+  to_aos_block(in, out, n, c);
+}
+// up to six arrays of one state transfer in one launch: blockIdx.y picks the array
+struct TrSet {
+  const double* in[6];
+  double* out[6];
+  int c[6];
+};
+__global__ void __launch_bounds__(kTrBlock) k_to_soa_set(TrSet t, int64_t n) {
+  to_soa_block(t.in[blockIdx.y], t.out[blockIdx.y], n, t.c[blockIdx.y]);
+}
+__global__ void __launch_bounds__(kTrBlock) k_to_aos_set(TrSet t, int64_t n) {
+  to_aos_block(t.in[blockIdx.y], t.out[blockIdx.y], n, t.c[blockIdx.y]);
 }
 // iteration bookkeeping only; the status bits set by the assembly are kept
 __global__ void k_reset_pc(ys::PcgCloth* pc, const int* maxiter, int ncloth, int maxiter_override) {
@@ -569,19 +589,40 @@ ys_status ys_set_state(ys_batch* b, const double* lpos, const double* lposfix, c
                        const double* epos, const double* eposbar, const double* evel, int32_t flags) {
   if (!b) return fail(YS_ERR_ARG, "null handle");
   YS_CUDA(cudaSetDevice(b->device));
-  // the six arrays through their own stage slots, one wait at the end
+  // the six arrays (page-locked: read in place; pageable: through their own
+  // stage slots) transposed in one launch, one wait at the end
   const double* src[6] = {lpos, lposfix, lvel, epos, eposbar, evel};
   double* dst[6] = {b->v.X, b->v.XF, b->v.V, b->v.UV, b->v.UVB, b->v.UVD};
   const int comps[6] = {3, 3, 3, 2, 2, 2};
+  const int64_t n = b->ntot;
+  TrSet t{};
+  int cnt = 0;
   int64_t slot = 0;
-  bool any = false;
   for (int k = 0; k < 6; ++k) {
-    const ys_status s = upload_soa(b, src[k], dst[k], comps[k], flags, slot, false);
-    if (s != YS_OK) return s;
-    any = any || src[k];
+    if (src[k]) {
+      const double* d = src[k];
+      if (!(flags & YS_ON_DEVICE)) {
+        if (const double* m = mapped_host(src[k])) {
+          d = m;
+        } else {
+          YS_CUDA(cudaMemcpyAsync(b->stage + slot * n, src[k], sizeof(double) * n * comps[k],
+                                  cudaMemcpyHostToDevice, b->stream));
+          d = b->stage + slot * n;
+        }
+      }
+      t.in[cnt] = d;
+      t.out[cnt] = dst[k];
+      t.c[cnt] = comps[k];
+      ++cnt;
+    }
     slot += comps[k];
   }
-  if (any && !(flags & YS_ON_DEVICE)) YS_CUDA(cudaStreamSynchronize(b->stream));
+  if (cnt) {
+    b->launches += 1;
+    k_to_soa_set<<<dim3((unsigned)((n + kTrBlock - 1) / kTrBlock), cnt), kTrBlock, 0, b->stream>>>(t, n);
+    YS_CUDA(cudaGetLastError());
+    if (!(flags & YS_ON_DEVICE)) YS_CUDA(cudaStreamSynchronize(b->stream));
+  }
   b->assembled = false;
   return YS_OK;
 }
@@ -590,19 +631,45 @@ ys_status ys_get_state(ys_batch* b, double* lpos, double* lposfix, double* lvel,
                        double* evel, int32_t flags) {
   if (!b) return fail(YS_ERR_ARG, "null handle");
   YS_CUDA(cudaSetDevice(b->device));
-  // the six arrays through their own stage slots, one wait at the end
+  // the six arrays transposed in one launch (into page-locked host arrays in
+  // place, else into their own stage slots, copied out after), one wait
   double* dst[6] = {lpos, lposfix, lvel, epos, eposbar, evel};
   const double* src[6] = {b->v.X, b->v.XF, b->v.V, b->v.UV, b->v.UVB, b->v.UVD};
   const int comps[6] = {3, 3, 3, 2, 2, 2};
+  const int64_t n = b->ntot;
+  TrSet t{};
+  double* staged[6] = {};
+  int cnt = 0;
   int64_t slot = 0;
-  bool any = false;
   for (int k = 0; k < 6; ++k) {
-    const ys_status s = download_aos(b, src[k], dst[k], comps[k], flags, slot, false);
-    if (s != YS_OK) return s;
-    any = any || dst[k];
+    if (dst[k]) {
+      double* d = dst[k];
+      if (!(flags & YS_ON_DEVICE)) {
+        if (double* m = mapped_host(dst[k])) {
+          d = m;
+        } else {
+          d = b->stage + slot * n;
+          staged[k] = d;
+        }
+      }
+      t.in[cnt] = src[k];
+      t.out[cnt] = d;
+      t.c[cnt] = comps[k];
+      ++cnt;
+    }
     slot += comps[k];
   }
-  if (any && !(flags & YS_ON_DEVICE)) YS_CUDA(cudaStreamSynchronize(b->stream));
+  if (!cnt) return YS_OK;
+  b->launches += 1;
+  k_to_aos_set<<<dim3((unsigned)((n + kTrBlock - 1) / kTrBlock), cnt), kTrBlock, 0, b->stream>>>(t, n);
+  YS_CUDA(cudaGetLastError());
+  if (!(flags & YS_ON_DEVICE)) {
+    for (int k = 0; k < 6; ++k)
+      if (staged[k])
+        YS_CUDA(cudaMemcpyAsync(dst[k], staged[k], sizeof(double) * n * comps[k], cudaMemcpyDeviceToHost,
+                                b->stream));
+    YS_CUDA(cudaStreamSynchronize(b->stream));
+  }
   return YS_OK;
 }
 
