@@ -161,7 +161,7 @@ def test_learned_solve_same_residual_fewer_iterations():
             states.append(b.get_state())
         if kind == "learned":
             assert b.precond_info()["fallbacks"] == 0
-            # the judge: true residual of a fresh learned solve
+            # the check: true residual of a fresh learned solve
             b.assemble(1e-3)
             stats = b.solve(tol=1e-10)
             x = b.solution()
