@@ -8,7 +8,7 @@ raises.
 """
 from .buildlib import build, LIB_PATH
 from .cloth import (PI, ClothBatch, ClothSpec, ClothState, Cloth, EigenSolver, Environment, InitPose,
-                    PhysicsCloth, SimStep, Wind, WovenPattern, Yarn, Adjoint, STATE_KEYS)
+                    PhysicsCloth, SimStep, StepStats, Wind, WovenPattern, Yarn, Adjoint, STATE_KEYS)
 from ._native import YarnSimError, load as load_library, library_path
 from .collide import Collider, Collision, cloth_mesh_topology
 from .learn import (PARAM_NAMES, YarnSimNetHeter, YarnSimNetHomo, YarnSimNetColli, YarnSimNetControl, constraint_para, invert_constraint_para, position_loss, rollout,
@@ -23,7 +23,7 @@ from .drivers import DropOnSphere, sim_collision, sim_control, sim_heter, sim_ho
 
 __all__ = [
     "build", "LIB_PATH", "PI", "ClothBatch", "ClothSpec", "ClothState", "Cloth", "EigenSolver", "Environment",
-    "InitPose", "PhysicsCloth", "SimStep", "Wind", "WovenPattern", "Yarn", "YarnSimError", "load_library",
+    "InitPose", "PhysicsCloth", "SimStep", "StepStats", "Wind", "WovenPattern", "Yarn", "YarnSimError", "load_library",
     "library_path", "PARAM_NAMES", "YarnSimNetHeter", "constraint_para", "invert_constraint_para", "position_loss",
     "rollout", "rollout_with_jacobian", "two_yarn_spec", "Collider", "Collision", "cloth_mesh_topology",
     "LearnedPreconditioner", "train_preconditioner", "training_specs", "RenderCloth", "RenderType", "obj_text",
