@@ -119,6 +119,9 @@ struct ys_batch {
   double* stage = nullptr;  // [15][ntot] staging for layout changes (the six state arrays side by side)
   double* ext = nullptr;    // [5][ntot]
   int* h_nactive = nullptr; // pinned
+  double* vecs = nullptr;    // the PCG vectors x, r, p, q, dinv in one allocation
+  size_t l2_window = 0;      // bytes of it kept in L2 by the graph's capture streams
+  float l2_hit = 0.0f;
   double* h_wind = nullptr;  // pinned [ncloth][3]: ys_set_winds' copy of the caller's array
   cudaEvent_t wind_ev = nullptr;  // recorded after the copy out of h_wind
   bool assembled = false;
@@ -495,7 +498,11 @@ ys_status ys_batch_create(int32_t n_cloths, const ys_cloth_desc* descs, int32_t 
   A(&b->rec.edge, (size_t)ys::kEdgeFields * 2 * nt); A(&b->rec.bend, (size_t)ys::kBendFields * 2 * nt);
   A(&b->rec.face, 6 * nt); A(&b->rec.shear, (size_t)ys::kShearFields * 4 * nt);
   A(&b->rec.nonfinite, nt);
-  A(&b->so.x, 5 * nt); A(&b->so.r, 5 * nt); A(&b->so.p, 5 * nt); A(&b->so.q, 5 * nt); A(&b->so.dinv, 5 * nt);
+  A(&b->vecs, 25 * nt);
+  if (b->vecs) {
+    b->so.x = b->vecs; b->so.r = b->vecs + 5 * nt; b->so.p = b->vecs + 10 * nt;
+    b->so.q = b->vecs + 15 * nt; b->so.dinv = b->vecs + 20 * nt;
+  }
   A(&b->so.part, 4 * blk_cloth.size()); A(&b->so.pc, n_cloths); A(&b->so.nactive, 1);
   A(&b->stage, 15 * nt); A(&b->ext, 5 * nt);
   if (st != YS_OK) { delete b; return st; }
@@ -1541,9 +1548,46 @@ ys_status ys_adjoint_step(ys_adjoint* a, double h, const double* ext_force, cons
 // ----------------------------------------------------------- graphed step
 namespace {
 
+// The PCG's vectors (x, r, p, q, dinv: 200 B a node) as an L2 access-policy
+// window on the capture stream, so the kernels captured from it keep them in
+// L2 while the SpMV streams the matrix (1,272 B a node) through it: a
+// persisting set-aside of up to the device's maximum for this context, the
+// window's hit ratio scaled down when the vectors outgrow it.
+void l2_window_setup(ys_batch* b, cudaStream_t s) {
+  if (!b->vecs) return;
+  if (!b->l2_window) {
+    int max_persist = 0, max_window = 0;
+    if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, b->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, b->device) != cudaSuccess ||
+        max_persist <= 0 || max_window <= 0) {
+      cudaGetLastError();
+      return;
+    }
+    const size_t bytes = sizeof(double) * 25 * (size_t)b->ntot;
+    const size_t window = std::min(bytes, (size_t)max_window);
+    const size_t persist = std::min(window, (size_t)max_persist);
+    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, persist) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    b->l2_window = window;
+    b->l2_hit = (float)((double)persist / (double)window);
+  }
+  cudaStreamAttrValue a = {};
+  a.accessPolicyWindow.base_ptr = b->vecs;
+  a.accessPolicyWindow.num_bytes = b->l2_window;
+  a.accessPolicyWindow.hitRatio = b->l2_hit;
+  a.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+  a.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+  if (cudaStreamSetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &a) != cudaSuccess) cudaGetLastError();
+}
+
 ys_status graph_prepare(ys_batch* b) {
   ys_batch::Graph& G = b->graph;
-  if (!G.capture) YS_CUDA(cudaStreamCreateWithFlags(&G.capture, cudaStreamNonBlocking));
+  if (!G.capture) {
+    YS_CUDA(cudaStreamCreateWithFlags(&G.capture, cudaStreamNonBlocking));
+    l2_window_setup(b, G.capture);
+  }
   for (int k = 0; k < 2; ++k) {
     if (!G.side[k]) YS_CUDA(cudaStreamCreateWithFlags(&G.side[k], cudaStreamNonBlocking));
     if (!G.join[k]) YS_CUDA(cudaEventCreateWithFlags(&G.join[k], cudaEventDisableTiming));
