@@ -154,7 +154,11 @@ ys_status ys_step(ys_batch *b, double h, const double *ext_force, int32_t flags,
  * when no cloth iterates or at the iteration cap), the check and the update --
  * captured on first use and again when h, the presence of an external force
  * or the solve options change. Results equal the launch-by-launch step bit
- * for bit. Ignored while ys_profile is on. */
+ * for bit. Ignored while ys_profile is on. The graph's kernels keep the PCG
+ * vectors in L2 through an access-policy window on the handle's own capture
+ * stream, for which the first graph build sets this context's persisting-L2
+ * limit (cudaLimitPersistingL2CacheSize) to the window's size, at most the
+ * device's maximum; the caller's stream is not changed. */
 ys_status ys_use_graphs(ys_batch *b, int32_t enable);
 /* ys_step through the graph regardless of ys_use_graphs. */
 ys_status ys_step_graphed(ys_batch *b, double h, const double *ext_force, int32_t flags, const ys_solve_opts *opts,
